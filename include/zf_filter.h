@@ -1,0 +1,210 @@
+/*
+ * zf_filter.h -- C ABI of the GB300 in-loop filter stage (deblock, CDEF,
+ * Wiener loop restoration) for the zenav1-svt AV1 still-image encoder.
+ *
+ * Every entry point here replaces one call site of the reference encoder's
+ * filter stage (rust/crates/svtav1-encoder/src/pipeline.rs:2813-3482). The
+ * reference functions are safe Rust over tight planes; this library takes
+ * the same planes as plain pointers and sizes so that a thin Rust crate
+ * outside the encoder's #![forbid(unsafe_code)] crates can bind it.
+ *
+ * Conventions
+ *  - Planes are tight: luma stride = width, chroma stride = width/2 (4:2:0).
+ *    8-bit planes are uint8_t, 10-bit planes are uint16_t (values < 1024).
+ *  - width/height are the 8-aligned canvas the deblock/CDEF passes run on;
+ *    true_width/true_height are the coded dims (<= aligned) that the
+ *    deblock onScreen guard and loop restoration use.
+ *  - Return codes: ZF_OK (0) or a negative ZF_ERR_* code; the reference's
+ *    EncodeError variants map onto AllocFailed, InvalidDimensions,
+ *    UnsupportedConfig and Cancelled. No C++ exception crosses the ABI.
+ *  - A zf_ctx owns one CUDA stream and its device scratch; it is not
+ *    thread-safe (one caller at a time, as &mut EncodePipeline is).
+ *  - Decision outputs use caller-owned arrays sized by zf_query_sizes().
+ */
+#ifndef ZF_FILTER_H
+#define ZF_FILTER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ZF_ABI_VERSION 1
+
+enum {
+    ZF_OK = 0,
+    ZF_ERR_ALLOC = -1,        /* EncodeError::AllocFailed */
+    ZF_ERR_INVALID_DIMS = -2, /* EncodeError::InvalidDimensions */
+    ZF_ERR_UNSUPPORTED = -3,  /* EncodeError::UnsupportedConfig */
+    ZF_ERR_CANCELLED = -4,    /* EncodeError::Cancelled */
+    ZF_ERR_CUDA = -5,         /* a CUDA runtime call or kernel failed */
+    ZF_ERR_ARG = -6,          /* NULL pointer or malformed argument */
+    ZF_ERR_GEOM = -7,         /* packed mi geometry is not a valid AV1 tiling */
+    ZF_ERR_TIMEOUT = -8       /* a bounded device-side wait gave up */
+};
+
+/* Restoration types (C enum order, svtav1-dsp/src/restoration.rs:87-90). */
+enum { ZF_RESTORE_NONE = 0, ZF_RESTORE_WIENER = 1, ZF_RESTORE_SGRPROJ = 2 };
+
+/*
+ * Packed per-4x4 (mode-info unit) deblock geometry, one uint32 per mi in
+ * raster order over (width/4) x (height/4). It carries what the reference's
+ * DeblockGeom (svtav1-encoder/src/deblock.rs:532-579) records per mi:
+ *   bits  0..2  log2(block width)  - 2   (block 4..128 px)
+ *   bits  3..5  log2(block height) - 2
+ *   bits  6..8  log2(luma TX width)  - 2 (TX 4..64 px)
+ *   bits  9..11 log2(luma TX height) - 2
+ *   bit  12     skip        (signaled skip_txfm, read by CDEF)
+ *   bit  13     skip_inter  (skip && is_inter, read by deblock)
+ * DeblockGeom's explicit block_id is not stored: AV1 blocks are aligned to
+ * their own dimensions, so two mi units share a block exactly when their
+ * aligned block origins coincide. zf_pack_geom() builds the record from the
+ * reference's arrays and rejects inputs for which that does not hold.
+ */
+#define ZF_MI_SKIP (1u << 12)
+#define ZF_MI_SKIP_INTER (1u << 13)
+
+typedef struct zf_frame {
+    int32_t bit_depth;          /* 8 or 10 */
+    int32_t width, height;      /* aligned canvas, multiples of 8 */
+    int32_t true_width, true_height;
+    int32_t chroma_420;         /* 1: U and V planes present (width/2 x height/2) */
+    int32_t preset;             /* encoder preset 0..13 */
+    int32_t qindex;             /* base_q_idx 0..255 */
+    int32_t sharpness;          /* loop_filter_sharpness 0..7 */
+    int32_t sc_class5;          /* screen-content arm of the qp CDEF picker */
+    int32_t enable_restoration; /* sequence-level enable_restoration */
+    int32_t planes_on_device;   /* 1: src/rec/mi are device pointers */
+    const void *src[3];         /* source planes */
+    void *rec[3];               /* in: pre-deblock recon; out: final filtered recon */
+    const uint32_t *mi;         /* packed geometry, (width/4)*(height/4) */
+} zf_frame;
+
+typedef struct zf_lr_unit {
+    int16_t vfilter[8];
+    int16_t hfilter[8];
+    uint8_t rtype;
+    uint8_t pad[7];
+} zf_lr_unit;
+
+typedef struct zf_lr_plane {
+    int32_t frame_rtype;
+    int32_t unit_size;
+    int32_t hunits, vunits;
+} zf_lr_plane;
+
+typedef struct zf_decisions {
+    uint8_t lf[4];              /* [luma vert, luma horz, U, V] (LfLevels) */
+    uint8_t cdef_damping;
+    uint8_t cdef_bits;
+    uint8_t cdef_y[8], cdef_uv[8]; /* packed strengths, 1 << cdef_bits used */
+    int32_t nhfb, nvfb;         /* 64x64 filter blocks per row / column */
+    uint8_t *cdef_fb_idx;       /* caller array nhfb*nvfb, may be NULL */
+    zf_lr_plane lr[3];
+    zf_lr_unit *lr_units[3];    /* caller arrays hunits*vunits, may be NULL */
+} zf_decisions;
+
+typedef struct zf_stats {
+    uint64_t cdef_filtered_px;  /* CdefStats::filtered_px (8-bit apply) */
+    uint64_t cdef_changed_px;   /* CdefStats::changed_px */
+    int32_t cdef_sb_count;      /* filter blocks with a non-skip 8x8 */
+    int32_t lr_wiener_units;    /* units applied with RESTORE_WIENER */
+    int32_t lr_frame_rtype[3];
+    int32_t pad;
+} zf_stats;
+
+typedef struct zf_sizes {
+    int32_t nhfb, nvfb;
+    int32_t lr_hunits[3], lr_vunits[3];
+    int32_t lr_unit_size;
+    int32_t pad;
+    uint64_t device_bytes;      /* device footprint of one frame in flight */
+} zf_sizes;
+
+typedef struct zf_opts {
+    int32_t device;             /* CUDA device ordinal */
+    int32_t pad;
+    uint64_t hbm_budget_bytes;  /* 0: no limit */
+    volatile int32_t *cancel_flag; /* polled between passes; non-zero => ZF_ERR_CANCELLED */
+} zf_opts;
+
+typedef struct zf_ctx zf_ctx;
+
+/* Library/ABI identification. */
+int32_t zf_abi_version(void);
+
+/* Context lifetime: one CUDA stream + device scratch per context. */
+int32_t zf_create(zf_ctx **out, const zf_opts *opts);
+void zf_destroy(zf_ctx *ctx);
+/* Text of the last error recorded on this context ("" when none). */
+const char *zf_last_error(const zf_ctx *ctx);
+/* Synchronise the context's stream. */
+int32_t zf_sync(zf_ctx *ctx);
+
+/* Output array sizes for a frame (filter blocks, restoration units). */
+int32_t zf_query_sizes(const zf_frame *f, zf_sizes *out);
+
+/*
+ * Pack the reference DeblockGeom arrays (deblock.rs:532-579: block_id, bw,
+ * bh, tw, th, skip, skip_inter per mi) into the uint32 records above.
+ * Returns ZF_ERR_GEOM when a block or transform is not aligned to its own
+ * dimensions or block_id disagrees with the aligned block origin.
+ */
+int32_t zf_pack_geom(int32_t mi_cols, int32_t mi_rows, const uint32_t *block_id,
+                     const uint8_t *bw, const uint8_t *bh, const uint8_t *tw,
+                     const uint8_t *th, const uint8_t *skip, const uint8_t *skip_inter,
+                     uint32_t *out);
+
+/*
+ * The whole filter stage for one key frame, replacing
+ * pipeline.rs:2886-3455: deblock level pick + apply, CDEF pick + apply,
+ * Wiener search + stripe-boundary save + apply. rec[] is overwritten with
+ * the final filtered recon; the decisions the frame header and tile syntax
+ * need are written to *out. stats may be NULL.
+ */
+int32_t zf_filter_stage(zf_ctx *ctx, const zf_frame *f, zf_decisions *out, zf_stats *stats);
+
+/*
+ * Batched form: n frames of any size and bit depth go through one launch
+ * per filter pass (device work lists over (frame, tile) descriptors).
+ * Per-frame results are identical to n separate zf_filter_stage calls.
+ */
+int32_t zf_submit_batch(zf_ctx *ctx, const zf_frame *frames, int32_t n,
+                        zf_decisions *outs, zf_stats *stats);
+
+/* --- Per-call-site entry points (one per reference function) ----------- */
+
+/* deblock::pick_filter_levels_full_search (presets <= 5, deblock.rs:481)
+ * or pick_filter_levels_key_frame (deblock.rs:55). Reads src and the
+ * pre-deblock rec; writes lf[4]. */
+int32_t zf_deblock_pick(zf_ctx *ctx, const zf_frame *f, uint8_t lf[4]);
+
+/* deblock::apply_deblock_frame[_hbd] (deblock.rs:938, :976): rec in place. */
+int32_t zf_deblock_apply(zf_ctx *ctx, const zf_frame *f, const uint8_t lf[4]);
+
+/* The CDEF pick of pipeline.rs:3042-3144: cdef_search_still[_hbd]
+ * (cdef.rs:1166, :1374), the all-skip outcome (cdef.rs:282) or the qp
+ * closed form (cdef.rs:151). Reads src and the post-deblock rec. */
+int32_t zf_cdef_search(zf_ctx *ctx, const zf_frame *f, zf_decisions *out);
+
+/* cdef::apply_cdef_frame[_hbd] (cdef.rs:343, :556): rec in place (the
+ * pre-CDEF snapshot is taken internally). */
+int32_t zf_cdef_apply(zf_ctx *ctx, const zf_frame *f, const zf_decisions *d, zf_stats *stats);
+
+/* restoration::search_restoration_still[_bd] (restoration.rs:644, :675):
+ * reads src and the post-CDEF rec, writes out->lr / out->lr_units. */
+int32_t zf_lr_search(zf_ctx *ctx, const zf_frame *f, zf_decisions *out);
+
+/* restoration::save_lr_boundaries + apply_restoration_frame
+ * (restoration.rs:938, :992): f->rec holds the post-CDEF planes (updated in
+ * place), pre_cdef[] the post-deblock planes the stripe boundaries come
+ * from (same layout and memory kind as rec). */
+int32_t zf_lr_apply(zf_ctx *ctx, const zf_frame *f, const void *const pre_cdef[3],
+                    const zf_decisions *d);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ZF_FILTER_H */

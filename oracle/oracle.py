@@ -1,0 +1,171 @@
+"""ctypes binding of the CPU ORACLE (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline load this
+module, as the checker; the product library never calls it.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+def _pkg():
+    import importlib.util
+    name = "zenav1_svt_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    path = os.path.join(ROOT, "zenav1-svt_gb300", "__init__.py")
+    spec = importlib.util.spec_from_file_location(name, path, submodule_search_locations=[os.path.dirname(path)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+abi = _pkg().abi
+
+BORDER_C, BORDER_PORT = 0, 1
+
+
+class ZfoGeom(C.Structure):
+    _fields_ = [("mi_cols", C.c_int32), ("mi_rows", C.c_int32), ("block_id", C.c_void_p),
+                ("bw", C.c_void_p), ("bh", C.c_void_p), ("tw", C.c_void_p), ("th", C.c_void_p),
+                ("skip", C.c_void_p), ("skip_inter", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    sys.path.insert(0, HERE)
+    import build as obuild  # oracle/build.py
+    sys.path.pop(0)
+    path = obuild.build()
+    L = C.CDLL(path)
+    P = C.POINTER
+    L.zfo_filter_stage.argtypes = [P(abi.ZfFrame), P(ZfoGeom), P(abi.ZfDecisions), P(abi.ZfStats), C.c_int32]
+    L.zfo_deblock_pick.argtypes = [P(abi.ZfFrame), P(ZfoGeom), P(C.c_uint8)]
+    L.zfo_deblock_apply.argtypes = [P(abi.ZfFrame), P(ZfoGeom), P(C.c_uint8)]
+    L.zfo_cdef_search.argtypes = [P(abi.ZfFrame), P(ZfoGeom), P(abi.ZfDecisions), C.c_void_p, C.c_void_p,
+                                  P(C.c_int32)]
+    L.zfo_cdef_apply.argtypes = [P(abi.ZfFrame), P(ZfoGeom), P(abi.ZfDecisions), P(abi.ZfStats)]
+    L.zfo_lr_search.argtypes = [P(abi.ZfFrame), P(abi.ZfDecisions), C.c_int32]
+    L.zfo_lr_apply.argtypes = [P(abi.ZfFrame), P(C.c_void_p), P(abi.ZfDecisions), C.c_int32]
+    L.zfo_lf_thresholds.argtypes = [C.c_int32, C.c_int32, P(C.c_int32)]
+    L.zfo_lpf.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.zfo_cdef_find_dir.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(C.c_int32), P(C.c_int32)]
+    L.zfo_cdef_filter_block.argtypes = [C.c_void_p] + [C.c_int32] * 3 + [C.c_void_p] + [C.c_int32] * 9
+    L.zfo_adjust_strength.argtypes = [C.c_int32, C.c_int32]
+    L.zfo_cdef_finish_rd.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P(C.c_int32),
+                                     P(C.c_int32)]
+    L.zfo_cdef_qp_params.argtypes = [C.c_int32, C.c_int32, C.c_int32, P(C.c_int32)]
+    L.zfo_deblock_key_frame_levels.argtypes = [C.c_int32, C.c_int32, P(C.c_uint8)]
+    L.zfo_dlf_hillclimb_replay.argtypes = [P(C.c_int64), C.c_int32, P(C.c_int32), P(C.c_int32)]
+    L.zfo_lambda.argtypes = [C.c_int32, C.c_int32]
+    L.zfo_lambda.restype = C.c_uint32
+    L.zfo_compute_stats.argtypes = [C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64,
+                                    C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                    C.c_void_p, C.c_int32]
+    L.zfo_wiener_solve.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, P(C.c_int32), P(C.c_int32),
+                                   P(C.c_int16), P(C.c_int16)]
+    L.zfo_wiener_solve.restype = C.c_int64
+    L.zfo_count_wiener_bits.argtypes = [C.c_int32] + [P(C.c_int16)] * 4
+    L.zfo_count_units_in_tile.argtypes = [C.c_int32, C.c_int32]
+    L.zfo_rdcost_dbl.argtypes = [C.c_int64, C.c_int64, C.c_int64]
+    L.zfo_rdcost_dbl.restype = C.c_double
+    L.zfo_wiener_convolve.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_int32,
+                                      P(C.c_int16), P(C.c_int16), C.c_int32, C.c_int32, C.c_int32]
+    L.zfo_sse_region.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.zfo_sse_region.restype = C.c_int64
+    _lib = L
+    return L
+
+
+def geom_struct(geom):
+    arrs = geom.arrays()
+    g = ZfoGeom()
+    g.mi_cols, g.mi_rows = geom.mi_cols, geom.mi_rows
+    g.block_id, g.bw, g.bh, g.tw, g.th, g.skip, g.skip_inter = [a.ctypes.data for a in arrs]
+    g._keep = arrs
+    return g
+
+
+def _frame(fr, rec):
+    mi = np.zeros(1, np.uint32)  # the oracle reads the explicit geometry
+    s = abi.make_frame_struct(fr, fr.src, rec, mi)
+    s._keep = mi
+    return s
+
+
+def filter_stage(fr, rec=None, border=BORDER_C):
+    rec = fr.copy_rec() if rec is None else rec
+    g = geom_struct(fr.geom)
+    s = _frame(fr, rec)
+    d = abi.Decisions(fr.w, fr.h, fr.true_w, fr.true_h)
+    st = abi.ZfStats()
+    rc = lib().zfo_filter_stage(C.byref(s), C.byref(g), C.byref(d.c), C.byref(st), border)
+    assert rc == 0, rc
+    return d.as_dict(), {"cdef_filtered_px": st.cdef_filtered_px, "cdef_changed_px": st.cdef_changed_px,
+                         "cdef_sb_count": st.cdef_sb_count, "lr_wiener_units": st.lr_wiener_units,
+                         "lr_frame_rtype": list(st.lr_frame_rtype)}, rec
+
+
+def deblock_pick(fr, rec):
+    g = geom_struct(fr.geom)
+    s = _frame(fr, rec)
+    lf = (C.c_uint8 * 4)()
+    assert lib().zfo_deblock_pick(C.byref(s), C.byref(g), lf) == 0
+    return list(lf)
+
+
+def deblock_apply(fr, rec, lf):
+    g = geom_struct(fr.geom)
+    s = _frame(fr, rec)
+    assert lib().zfo_deblock_apply(C.byref(s), C.byref(g), (C.c_uint8 * 4)(*lf)) == 0
+
+
+def cdef_search(fr, rec):
+    """Returns (Decisions, mse rows [nfb, 2*ncand] or None, has_row [nfb])."""
+    g = geom_struct(fr.geom)
+    s = _frame(fr, rec)
+    d = abi.Decisions(fr.w, fr.h, fr.true_w, fr.true_h)
+    nfb = d.nhfb * d.nvfb
+    mse = np.zeros((nfb, 2 * 48), np.uint64)
+    has = np.zeros(nfb, np.uint8)
+    nc = C.c_int32()
+    # the oracle writes rows with stride 2*ncand; pass a scratch and reshape.
+    flat = np.zeros(nfb * 2 * 48, np.uint64)
+    assert lib().zfo_cdef_search(C.byref(s), C.byref(g), C.byref(d.c), flat.ctypes.data, has.ctypes.data,
+                                 C.byref(nc)) == 0
+    n = nc.value
+    rows = flat[:nfb * 2 * n].reshape(nfb, 2 * n) if n else None
+    del mse
+    return d, rows, has
+
+
+def cdef_apply(fr, rec, dec):
+    g = geom_struct(fr.geom)
+    s = _frame(fr, rec)
+    st = abi.ZfStats()
+    assert lib().zfo_cdef_apply(C.byref(s), C.byref(g), C.byref(dec.c), C.byref(st)) == 0
+    return {"cdef_filtered_px": st.cdef_filtered_px, "cdef_changed_px": st.cdef_changed_px}
+
+
+def lr_search(fr, rec, border=BORDER_C):
+    s = _frame(fr, rec)
+    d = abi.Decisions(fr.w, fr.h, fr.true_w, fr.true_h)
+    assert lib().zfo_lr_search(C.byref(s), C.byref(d.c), border) == 0
+    return d
+
+
+def lr_apply(fr, rec, pre_cdef, dec, border=BORDER_C):
+    s = _frame(fr, rec)
+    pre = (C.c_void_p * 3)(*[p.ctypes.data for p in pre_cdef])
+    assert lib().zfo_lr_apply(C.byref(s), pre, C.byref(dec.c), border) == 0

@@ -1,0 +1,2429 @@
+// zf_oracle.cpp -- CPU ORACLE (test infrastructure; see zf_oracle.h).
+//
+// A C++17 restatement of the zenav1-svt reference filter stage. Paths in
+// the citations are relative to the reference project:
+//   DSP/ = rust/crates/svtav1-dsp/src/
+//   ENC/ = rust/crates/svtav1-encoder/src/
+//   ENT/ = rust/crates/svtav1-entropy/src/
+// Every function follows the cited scalar reference body operation for
+// operation (same integer widths, same truncating divisions, same f32/f64
+// evaluation order); nothing here is tuned for speed. Build with
+// -ffp-contract=off so the float pickers round exactly like the reference.
+
+#include "zf_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../include/zf_av1_tables.h"
+
+namespace {
+
+using i8 = int8_t;
+using i16 = int16_t;
+using i32 = int32_t;
+using i64 = int64_t;
+using u8 = uint8_t;
+using u16 = uint16_t;
+using u32 = uint32_t;
+using u64 = uint64_t;
+
+template <typename T> static inline T clampv(T v, T lo, T hi) { return v < lo ? lo : (v > hi ? hi : v); }
+static inline i32 iabs(i32 v) { return v < 0 ? -v : v; }
+static inline i64 iabs64(i64 v) { return v < 0 ? -v : v; }
+
+// ===========================================================================
+// Lambdas (ENC/pd0.rs:218-222, :330-346)
+// ===========================================================================
+
+// kf_full_lambda_8bit_unweighted (ENC/pd0.rs:218).
+static u32 kf_full_lambda_8bit_unweighted(int qindex) {
+    i64 dc_q = zf_dc_qlookup_8[qindex];
+    double q = (double)dc_q;
+    i64 rdmult = (i64)((3.3 + 0.0015 * q) * q * q);
+    return (u32)((rdmult * 150) >> 7);
+}
+// kf_full_lambda_bd10_unweighted (ENC/pd0.rs:330).
+static u32 kf_full_lambda_bd10_unweighted(int qindex) {
+    i64 qi = zf_dc_qlookup_10[qindex];
+    double q = (double)qi;
+    i64 rdmult = (i64)((3.3 + 0.0015 * q) * q * q);
+    rdmult = (rdmult + 8) >> 4;
+    rdmult = std::max<i64>(rdmult, 1);
+    return (u32)((rdmult * 128) >> 7);
+}
+// kf_full_lambda_bd10_pic (ENC/pd0.rs:343).
+static u32 kf_full_lambda_bd10_pic(int qindex) { return kf_full_lambda_bd10_unweighted(qindex) * 16; }
+
+// ===========================================================================
+// Deblock (DSP/loop_filter.rs, DSP/hbd.rs:1060-1440, ENC/deblock.rs)
+// ===========================================================================
+
+struct LfThresh { u8 mblim, lim, hev_thr; };
+
+// lf_thresholds (DSP/loop_filter.rs:50-65).
+static LfThresh lf_thresholds(int level, int sharpness) {
+    i32 lvl = level;
+    i32 sh = sharpness;
+    i32 bil = lvl >> ((sh > 0) + (sh > 4));
+    if (sh > 0 && bil > 9 - sh) bil = 9 - sh;
+    if (bil < 1) bil = 1;
+    LfThresh t;
+    t.mblim = (u8)(2 * (lvl + 2) + bil);
+    t.lim = (u8)bil;
+    t.hev_thr = (u8)(level >> 4);
+    return t;
+}
+
+// ---- 8-bit kernels (DSP/loop_filter.rs:67-282) ----
+static inline i8 signed_char_clamp(i32 t) { return (i8)clampv(t, -128, 127); }
+static inline i8 mbit(bool c) { return (i8)(c ? -1 : 0); }
+
+static i8 filter_mask2(u8 limit, u8 blimit, i32 p1, i32 p0, i32 q0, i32 q1) {
+    i8 mask = 0;
+    mask |= mbit(iabs(p1 - p0) > limit);
+    mask |= mbit(iabs(q1 - q0) > limit);
+    mask |= mbit(iabs(p0 - q0) * 2 + iabs(p1 - q1) / 2 > blimit);
+    return (i8)~mask;
+}
+static i8 filter_mask(u8 limit, u8 blimit, i32 p3, i32 p2, i32 p1, i32 p0, i32 q0, i32 q1, i32 q2,
+                      i32 q3) {
+    i32 l = limit;
+    i8 mask = 0;
+    mask |= mbit(iabs(p3 - p2) > l);
+    mask |= mbit(iabs(p2 - p1) > l);
+    mask |= mbit(iabs(p1 - p0) > l);
+    mask |= mbit(iabs(q1 - q0) > l);
+    mask |= mbit(iabs(q2 - q1) > l);
+    mask |= mbit(iabs(q3 - q2) > l);
+    mask |= mbit(iabs(p0 - q0) * 2 + iabs(p1 - q1) / 2 > blimit);
+    return (i8)~mask;
+}
+static i8 filter_mask3_chroma(u8 limit, u8 blimit, i32 p2, i32 p1, i32 p0, i32 q0, i32 q1, i32 q2) {
+    i32 l = limit;
+    i8 mask = 0;
+    mask |= mbit(iabs(p2 - p1) > l);
+    mask |= mbit(iabs(p1 - p0) > l);
+    mask |= mbit(iabs(q1 - q0) > l);
+    mask |= mbit(iabs(q2 - q1) > l);
+    mask |= mbit(iabs(p0 - q0) * 2 + iabs(p1 - q1) / 2 > blimit);
+    return (i8)~mask;
+}
+static i8 flat_mask3_chroma(i32 t, i32 p2, i32 p1, i32 p0, i32 q0, i32 q1, i32 q2) {
+    i8 mask = 0;
+    mask |= mbit(iabs(p1 - p0) > t);
+    mask |= mbit(iabs(q1 - q0) > t);
+    mask |= mbit(iabs(p2 - p0) > t);
+    mask |= mbit(iabs(q2 - q0) > t);
+    return (i8)~mask;
+}
+static i8 flat_mask4(i32 t, i32 p3, i32 p2, i32 p1, i32 p0, i32 q0, i32 q1, i32 q2, i32 q3) {
+    i8 mask = 0;
+    mask |= mbit(iabs(p1 - p0) > t);
+    mask |= mbit(iabs(q1 - q0) > t);
+    mask |= mbit(iabs(p2 - p0) > t);
+    mask |= mbit(iabs(q2 - q0) > t);
+    mask |= mbit(iabs(p3 - p0) > t);
+    mask |= mbit(iabs(q3 - q0) > t);
+    return (i8)~mask;
+}
+static i8 hev_mask(i32 t, i32 p1, i32 p0, i32 q0, i32 q1) {
+    i8 hev = 0;
+    hev |= mbit(iabs(p1 - p0) > t);
+    hev |= mbit(iabs(q1 - q0) > t);
+    return hev;
+}
+// filter4 (DSP/loop_filter.rs:181-203).
+static void filter4_line(i8 mask, u8 thresh, u8 *w) {
+    i8 ps1 = (i8)(u8)(w[0] ^ 0x80);
+    i8 ps0 = (i8)(u8)(w[1] ^ 0x80);
+    i8 qs0 = (i8)(u8)(w[2] ^ 0x80);
+    i8 qs1 = (i8)(u8)(w[3] ^ 0x80);
+    i8 hev = hev_mask(thresh, w[0], w[1], w[2], w[3]);
+    i8 filter = (i8)(signed_char_clamp((i32)ps1 - (i32)qs1) & hev);
+    filter = (i8)(signed_char_clamp((i32)filter + 3 * ((i32)qs0 - (i32)ps0)) & mask);
+    i8 filter1 = (i8)(signed_char_clamp((i32)filter + 4) >> 3);
+    i8 filter2 = (i8)(signed_char_clamp((i32)filter + 3) >> 3);
+    w[2] = (u8)((u8)signed_char_clamp((i32)qs0 - (i32)filter1) ^ 0x80);
+    w[1] = (u8)((u8)signed_char_clamp((i32)ps0 + (i32)filter2) ^ 0x80);
+    i8 f = (i8)((i8)((((i32)filter1) + 1) >> 1) & (i8)~hev);
+    w[3] = (u8)((u8)signed_char_clamp((i32)qs1 - (i32)f) ^ 0x80);
+    w[0] = (u8)((u8)signed_char_clamp((i32)ps1 + (i32)f) ^ 0x80);
+}
+static inline u8 rpot3(i32 x) { return (u8)((x + 4) >> 3); }
+static inline u8 rpot4(i32 x) { return (u8)((x + 8) >> 4); }
+// filter6 (DSP/loop_filter.rs:220-234).
+static void filter6_line(i8 mask, u8 thresh, i8 flat, u8 *w) {
+    if (flat != 0 && mask != 0) {
+        i32 p2 = w[0], p1 = w[1], p0 = w[2], q0 = w[3], q1 = w[4], q2 = w[5];
+        w[1] = rpot3(p2 * 3 + p1 * 2 + p0 * 2 + q0);
+        w[2] = rpot3(p2 + p1 * 2 + p0 * 2 + q0 * 2 + q1);
+        w[3] = rpot3(p1 + p0 * 2 + q0 * 2 + q1 * 2 + q2);
+        w[4] = rpot3(p0 + q0 * 2 + q1 * 2 + q2 * 3);
+    } else {
+        filter4_line(mask, thresh, w + 1);
+    }
+}
+// filter8 (DSP/loop_filter.rs:238-254).
+static void filter8_line(i8 mask, u8 thresh, i8 flat, u8 *w) {
+    if (flat != 0 && mask != 0) {
+        i32 p3 = w[0], p2 = w[1], p1 = w[2], p0 = w[3], q0 = w[4], q1 = w[5], q2 = w[6], q3 = w[7];
+        w[1] = rpot3(p3 + p3 + p3 + 2 * p2 + p1 + p0 + q0);
+        w[2] = rpot3(p3 + p3 + p2 + 2 * p1 + p0 + q0 + q1);
+        w[3] = rpot3(p3 + p2 + p1 + 2 * p0 + q0 + q1 + q2);
+        w[4] = rpot3(p2 + p1 + p0 + 2 * q0 + q1 + q2 + q3);
+        w[5] = rpot3(p1 + p0 + q0 + 2 * q1 + q2 + q3 + q3);
+        w[6] = rpot3(p0 + q0 + q1 + 2 * q2 + q3 + q3 + q3);
+    } else {
+        filter4_line(mask, thresh, w + 2);
+    }
+}
+// filter14 (DSP/loop_filter.rs:258-282).
+static void filter14_line(i8 mask, u8 thresh, i8 flat, i8 flat2, u8 *w) {
+    if (flat2 != 0 && flat != 0 && mask != 0) {
+        i32 p6 = w[0], p5 = w[1], p4 = w[2], p3 = w[3], p2 = w[4], p1 = w[5], p0 = w[6];
+        i32 q0 = w[7], q1 = w[8], q2 = w[9], q3 = w[10], q4 = w[11], q5 = w[12], q6 = w[13];
+        w[1] = rpot4(p6 * 7 + p5 * 2 + p4 * 2 + p3 + p2 + p1 + p0 + q0);
+        w[2] = rpot4(p6 * 5 + p5 * 2 + p4 * 2 + p3 * 2 + p2 + p1 + p0 + q0 + q1);
+        w[3] = rpot4(p6 * 4 + p5 + p4 * 2 + p3 * 2 + p2 * 2 + p1 + p0 + q0 + q1 + q2);
+        w[4] = rpot4(p6 * 3 + p5 + p4 + p3 * 2 + p2 * 2 + p1 * 2 + p0 + q0 + q1 + q2 + q3);
+        w[5] = rpot4(p6 * 2 + p5 + p4 + p3 + p2 * 2 + p1 * 2 + p0 * 2 + q0 + q1 + q2 + q3 + q4);
+        w[6] = rpot4(p6 + p5 + p4 + p3 + p2 + p1 * 2 + p0 * 2 + q0 * 2 + q1 + q2 + q3 + q4 + q5);
+        w[7] = rpot4(p5 + p4 + p3 + p2 + p1 + p0 * 2 + q0 * 2 + q1 * 2 + q2 + q3 + q4 + q5 + q6);
+        w[8] = rpot4(p4 + p3 + p2 + p1 + p0 + q0 * 2 + q1 * 2 + q2 * 2 + q3 + q4 + q5 + q6 * 2);
+        w[9] = rpot4(p3 + p2 + p1 + p0 + q0 + q1 * 2 + q2 * 2 + q3 * 2 + q4 + q5 + q6 * 3);
+        w[10] = rpot4(p2 + p1 + p0 + q0 + q1 + q2 * 2 + q3 * 2 + q4 * 2 + q5 + q6 * 4);
+        w[11] = rpot4(p1 + p0 + q0 + q1 + q2 + q3 * 2 + q4 * 2 + q5 * 2 + q6 * 5);
+        w[12] = rpot4(p0 + q0 + q1 + q2 + q3 + q4 * 2 + q5 * 2 + q6 * 7);
+    } else {
+        filter8_line(mask, thresh, flat, w + 3);
+    }
+}
+
+// ---- highbd kernels (DSP/hbd.rs:1066-1310) ----
+static inline i32 signed_char_clamp_high(i32 t, int bd) {
+    if (bd == 10) return clampv(t, -512, 511);
+    if (bd == 12) return clampv(t, -2048, 2047);
+    return clampv(t, -128, 127);
+}
+static i16 highbd_hev_mask(u8 thresh, i32 p1, i32 p0, i32 q0, i32 q1, int bd) {
+    i32 t16 = (i32)thresh << (bd - 8);
+    i16 hev = 0;
+    hev |= (i16)(iabs(p1 - p0) > t16 ? -1 : 0);
+    hev |= (i16)(iabs(q1 - q0) > t16 ? -1 : 0);
+    return hev;
+}
+static i8 highbd_filter_mask2(u8 limit, u8 blimit, i32 p1, i32 p0, i32 q0, i32 q1, int bd) {
+    int s = bd - 8;
+    i32 l16 = (i32)limit << s, b16 = (i32)blimit << s;
+    i8 mask = 0;
+    mask |= mbit(iabs(p1 - p0) > l16);
+    mask |= mbit(iabs(q1 - q0) > l16);
+    mask |= mbit(iabs(p0 - q0) * 2 + iabs(p1 - q1) / 2 > b16);
+    return (i8)~mask;
+}
+static i8 highbd_filter_mask(u8 limit, u8 blimit, i32 p3, i32 p2, i32 p1, i32 p0, i32 q0, i32 q1,
+                             i32 q2, i32 q3, int bd) {
+    int s = bd - 8;
+    i32 l16 = (i32)limit << s, b16 = (i32)blimit << s;
+    i8 mask = 0;
+    mask |= mbit(iabs(p3 - p2) > l16);
+    mask |= mbit(iabs(p2 - p1) > l16);
+    mask |= mbit(iabs(p1 - p0) > l16);
+    mask |= mbit(iabs(q1 - q0) > l16);
+    mask |= mbit(iabs(q2 - q1) > l16);
+    mask |= mbit(iabs(q3 - q2) > l16);
+    mask |= mbit(iabs(p0 - q0) * 2 + iabs(p1 - q1) / 2 > b16);
+    return (i8)~mask;
+}
+static i8 highbd_filter_mask3_chroma(u8 limit, u8 blimit, i32 p2, i32 p1, i32 p0, i32 q0, i32 q1,
+                                     i32 q2, int bd) {
+    int s = bd - 8;
+    i32 l16 = (i32)limit << s, b16 = (i32)blimit << s;
+    i8 mask = 0;
+    mask |= mbit(iabs(p2 - p1) > l16);
+    mask |= mbit(iabs(p1 - p0) > l16);
+    mask |= mbit(iabs(q1 - q0) > l16);
+    mask |= mbit(iabs(q2 - q1) > l16);
+    mask |= mbit(iabs(p0 - q0) * 2 + iabs(p1 - q1) / 2 > b16);
+    return (i8)~mask;
+}
+static i8 highbd_flat_mask3_chroma(u8 thresh, i32 p2, i32 p1, i32 p0, i32 q0, i32 q1, i32 q2, int bd) {
+    i32 t16 = (i32)thresh << (bd - 8);
+    i8 mask = 0;
+    mask |= mbit(iabs(p1 - p0) > t16);
+    mask |= mbit(iabs(q1 - q0) > t16);
+    mask |= mbit(iabs(p2 - p0) > t16);
+    mask |= mbit(iabs(q2 - q0) > t16);
+    return (i8)~mask;
+}
+static i8 highbd_flat_mask4(u8 thresh, i32 p3, i32 p2, i32 p1, i32 p0, i32 q0, i32 q1, i32 q2, i32 q3,
+                            int bd) {
+    i32 t16 = (i32)thresh << (bd - 8);
+    i8 mask = 0;
+    mask |= mbit(iabs(p1 - p0) > t16);
+    mask |= mbit(iabs(q1 - q0) > t16);
+    mask |= mbit(iabs(p2 - p0) > t16);
+    mask |= mbit(iabs(q2 - q0) > t16);
+    mask |= mbit(iabs(p3 - p0) > t16);
+    mask |= mbit(iabs(q3 - q0) > t16);
+    return (i8)~mask;
+}
+// highbd_filter4 (DSP/hbd.rs:1211-1232).
+static void highbd_filter4(i8 mask, u8 thresh, u16 *w, int bd) {
+    int shift = bd - 8;
+    i32 bias = 0x80 << shift;
+    i32 ps1 = (i32)w[0] - bias, ps0 = (i32)w[1] - bias, qs0 = (i32)w[2] - bias, qs1 = (i32)w[3] - bias;
+    i32 hev = (i32)highbd_hev_mask(thresh, w[0], w[1], w[2], w[3], bd);
+    i32 filter = signed_char_clamp_high(ps1 - qs1, bd) & hev;
+    filter = signed_char_clamp_high(filter + 3 * (qs0 - ps0), bd) & (i32)mask;
+    i32 filter1 = signed_char_clamp_high(filter + 4, bd) >> 3;
+    i32 filter2 = signed_char_clamp_high(filter + 3, bd) >> 3;
+    w[2] = (u16)(signed_char_clamp_high(qs0 - filter1, bd) + bias);
+    w[1] = (u16)(signed_char_clamp_high(ps0 + filter2, bd) + bias);
+    i32 outer = ((filter1 + 1) >> 1) & ~hev;
+    w[3] = (u16)(signed_char_clamp_high(qs1 - outer, bd) + bias);
+    w[0] = (u16)(signed_char_clamp_high(ps1 + outer, bd) + bias);
+}
+static inline u16 rpot3h(i32 x) { return (u16)((x + 4) >> 3); }
+static inline u16 rpot4h(i32 x) { return (u16)((x + 8) >> 4); }
+static void highbd_filter6(i8 mask, u8 thresh, i8 flat, u16 *w, int bd) {
+    if (flat != 0 && mask != 0) {
+        i32 p2 = w[0], p1 = w[1], p0 = w[2], q0 = w[3], q1 = w[4], q2 = w[5];
+        w[1] = rpot3h(p2 * 3 + p1 * 2 + p0 * 2 + q0);
+        w[2] = rpot3h(p2 + p1 * 2 + p0 * 2 + q0 * 2 + q1);
+        w[3] = rpot3h(p1 + p0 * 2 + q0 * 2 + q1 * 2 + q2);
+        w[4] = rpot3h(p0 + q0 * 2 + q1 * 2 + q2 * 3);
+    } else {
+        highbd_filter4(mask, thresh, w + 1, bd);
+    }
+}
+static void highbd_filter8(i8 mask, u8 thresh, i8 flat, u16 *w, int bd) {
+    if (flat != 0 && mask != 0) {
+        i32 p3 = w[0], p2 = w[1], p1 = w[2], p0 = w[3], q0 = w[4], q1 = w[5], q2 = w[6], q3 = w[7];
+        w[1] = rpot3h(p3 + p3 + p3 + 2 * p2 + p1 + p0 + q0);
+        w[2] = rpot3h(p3 + p3 + p2 + 2 * p1 + p0 + q0 + q1);
+        w[3] = rpot3h(p3 + p2 + p1 + 2 * p0 + q0 + q1 + q2);
+        w[4] = rpot3h(p2 + p1 + p0 + 2 * q0 + q1 + q2 + q3);
+        w[5] = rpot3h(p1 + p0 + q0 + 2 * q1 + q2 + q3 + q3);
+        w[6] = rpot3h(p0 + q0 + q1 + 2 * q2 + q3 + q3 + q3);
+    } else {
+        highbd_filter4(mask, thresh, w + 2, bd);
+    }
+}
+static void highbd_filter14(i8 mask, u8 thresh, i8 flat, i8 flat2, u16 *w, int bd) {
+    if (flat2 != 0 && flat != 0 && mask != 0) {
+        i32 p6 = w[0], p5 = w[1], p4 = w[2], p3 = w[3], p2 = w[4], p1 = w[5], p0 = w[6];
+        i32 q0 = w[7], q1 = w[8], q2 = w[9], q3 = w[10], q4 = w[11], q5 = w[12], q6 = w[13];
+        w[1] = rpot4h(p6 * 7 + p5 * 2 + p4 * 2 + p3 + p2 + p1 + p0 + q0);
+        w[2] = rpot4h(p6 * 5 + p5 * 2 + p4 * 2 + p3 * 2 + p2 + p1 + p0 + q0 + q1);
+        w[3] = rpot4h(p6 * 4 + p5 + p4 * 2 + p3 * 2 + p2 * 2 + p1 + p0 + q0 + q1 + q2);
+        w[4] = rpot4h(p6 * 3 + p5 + p4 + p3 * 2 + p2 * 2 + p1 * 2 + p0 + q0 + q1 + q2 + q3);
+        w[5] = rpot4h(p6 * 2 + p5 + p4 + p3 + p2 * 2 + p1 * 2 + p0 * 2 + q0 + q1 + q2 + q3 + q4);
+        w[6] = rpot4h(p6 + p5 + p4 + p3 + p2 + p1 * 2 + p0 * 2 + q0 * 2 + q1 + q2 + q3 + q4 + q5);
+        w[7] = rpot4h(p5 + p4 + p3 + p2 + p1 + p0 * 2 + q0 * 2 + q1 * 2 + q2 + q3 + q4 + q5 + q6);
+        w[8] = rpot4h(p4 + p3 + p2 + p1 + p0 + q0 * 2 + q1 * 2 + q2 * 2 + q3 + q4 + q5 + q6 * 2);
+        w[9] = rpot4h(p3 + p2 + p1 + p0 + q0 + q1 * 2 + q2 * 2 + q3 * 2 + q4 + q5 + q6 * 3);
+        w[10] = rpot4h(p2 + p1 + p0 + q0 + q1 + q2 * 2 + q3 * 2 + q4 * 2 + q5 + q6 * 4);
+        w[11] = rpot4h(p1 + p0 + q0 + q1 + q2 + q3 * 2 + q4 * 2 + q5 * 2 + q6 * 5);
+        w[12] = rpot4h(p0 + q0 + q1 + q2 + q3 + q4 * 2 + q5 * 2 + q6 * 7);
+    } else {
+        highbd_filter8(mask, thresh, flat, w + 3, bd);
+    }
+}
+
+// One 4-line edge segment: lpf_{horizontal,vertical}_{4,6,8,14}
+// (DSP/loop_filter.rs:305-412) and the _hbd twins (DSP/hbd.rs:1335-1440).
+// `vert` selects the vertical-edge kernel (taps contiguous, 4 rows); the
+// horizontal-edge kernel steps taps by `pitch` over 4 columns.
+static void lpf_u8(u8 *buf, i64 off, i64 pitch, bool vert, int len, LfThresh t) {
+    for (int i = 0; i < 4; ++i) {
+        i64 base = vert ? off + i * pitch : off + i;
+        i64 step = vert ? 1 : pitch;
+        u8 w[14];
+        i64 start = base - (len / 2) * step;
+        for (int k = 0; k < len; ++k) w[k] = buf[start + k * step];
+        if (len == 4) {
+            i8 mask = filter_mask2(t.lim, t.mblim, w[0], w[1], w[2], w[3]);
+            filter4_line(mask, t.hev_thr, w);
+        } else if (len == 6) {
+            i8 mask = filter_mask3_chroma(t.lim, t.mblim, w[0], w[1], w[2], w[3], w[4], w[5]);
+            i8 flat = flat_mask3_chroma(1, w[0], w[1], w[2], w[3], w[4], w[5]);
+            filter6_line(mask, t.hev_thr, flat, w);
+        } else if (len == 8) {
+            i8 mask = filter_mask(t.lim, t.mblim, w[0], w[1], w[2], w[3], w[4], w[5], w[6], w[7]);
+            i8 flat = flat_mask4(1, w[0], w[1], w[2], w[3], w[4], w[5], w[6], w[7]);
+            filter8_line(mask, t.hev_thr, flat, w);
+        } else {
+            i8 mask = filter_mask(t.lim, t.mblim, w[3], w[4], w[5], w[6], w[7], w[8], w[9], w[10]);
+            i8 flat = flat_mask4(1, w[3], w[4], w[5], w[6], w[7], w[8], w[9], w[10]);
+            i8 flat2 = flat_mask4(1, w[0], w[1], w[2], w[6], w[7], w[11], w[12], w[13]);
+            filter14_line(mask, t.hev_thr, flat, flat2, w);
+        }
+        for (int k = 0; k < len; ++k) buf[start + k * step] = w[k];
+    }
+}
+static void lpf_u16(u16 *buf, i64 off, i64 pitch, bool vert, int len, LfThresh t, int bd) {
+    for (int i = 0; i < 4; ++i) {
+        i64 base = vert ? off + i * pitch : off + i;
+        i64 step = vert ? 1 : pitch;
+        u16 w[14];
+        i64 start = base - (len / 2) * step;
+        for (int k = 0; k < len; ++k) w[k] = buf[start + k * step];
+        if (len == 4) {
+            i8 mask = highbd_filter_mask2(t.lim, t.mblim, w[0], w[1], w[2], w[3], bd);
+            highbd_filter4(mask, t.hev_thr, w, bd);
+        } else if (len == 6) {
+            i8 mask = highbd_filter_mask3_chroma(t.lim, t.mblim, w[0], w[1], w[2], w[3], w[4], w[5], bd);
+            i8 flat = highbd_flat_mask3_chroma(1, w[0], w[1], w[2], w[3], w[4], w[5], bd);
+            highbd_filter6(mask, t.hev_thr, flat, w, bd);
+        } else if (len == 8) {
+            i8 mask = highbd_filter_mask(t.lim, t.mblim, w[0], w[1], w[2], w[3], w[4], w[5], w[6], w[7], bd);
+            i8 flat = highbd_flat_mask4(1, w[0], w[1], w[2], w[3], w[4], w[5], w[6], w[7], bd);
+            highbd_filter8(mask, t.hev_thr, flat, w, bd);
+        } else {
+            i8 mask = highbd_filter_mask(t.lim, t.mblim, w[3], w[4], w[5], w[6], w[7], w[8], w[9], w[10], bd);
+            i8 flat = highbd_flat_mask4(1, w[3], w[4], w[5], w[6], w[7], w[8], w[9], w[10], bd);
+            i8 flat2 = highbd_flat_mask4(1, w[0], w[1], w[2], w[6], w[7], w[11], w[12], w[13], bd);
+            highbd_filter14(mask, t.hev_thr, flat, flat2, w, bd);
+        }
+        for (int k = 0; k < len; ++k) buf[start + k * step] = w[k];
+    }
+}
+static inline void lpf_any(u8 *b, i64 off, i64 pitch, bool vert, int len, LfThresh t, int) {
+    lpf_u8(b, off, pitch, vert, len, t);
+}
+static inline void lpf_any(u16 *b, i64 off, i64 pitch, bool vert, int len, LfThresh t, int bd) {
+    lpf_u16(b, off, pitch, vert, len, t, bd);
+}
+
+// DeblockGeom (ENC/deblock.rs:532-679) over the explicit arrays.
+struct Geom {
+    int mi_cols, mi_rows, true_w, true_h;
+    const u32 *block_id;
+    const u8 *bw, *bh, *tw, *th, *skip, *skip_inter;
+    // is_8x8_all_skip (ENC/deblock.rs:652-661).
+    bool is_8x8_all_skip(int mi_row, int mi_col) const {
+        for (int r = mi_row; r < std::min(mi_row + 2, mi_rows); ++r)
+            for (int c = mi_col; c < std::min(mi_col + 2, mi_cols); ++c)
+                if (!skip[(size_t)r * mi_cols + c]) return false;
+        return true;
+    }
+    // cdef_frame_all_skip (ENC/deblock.rs:669-678).
+    bool cdef_frame_all_skip() const {
+        for (int r = 0; r < mi_rows; r += 2)
+            for (int c = 0; c < mi_cols; c += 2)
+                if (!is_8x8_all_skip(r, c)) return false;
+        return true;
+    }
+};
+
+// lpf_params (ENC/deblock.rs:698-796). Returns the advance in plane-mi
+// units; *len = filter length or 0.
+static int lpf_params(const Geom &g, bool vert, int x, int y, int plane, int ss, int level, int *len) {
+    *len = 0;
+    int true_pw = g.true_w >> ss, true_ph = g.true_h >> ss;
+    if (x >= true_pw || y >= true_ph) return 1;
+    size_t mi_row = (size_t)(ss | ((y << ss) >> 2));
+    size_t mi_col = (size_t)(ss | ((x << ss) >> 2));
+    size_t idx = mi_row * g.mi_cols + mi_col;
+    auto tx_dims = [&](size_t i, int *tw, int *th) {
+        if (plane == 0) {
+            *tw = g.tw[i];
+            *th = g.th[i];
+        } else {
+            *tw = std::max(g.bw[i] >> 1, 4);
+            *th = std::max(g.bh[i] >> 1, 4);
+        }
+    };
+    int tw, th;
+    tx_dims(idx, &tw, &th);
+    int ts_dim = vert ? tw : th;
+    int advance = ts_dim >> 2;
+    int coord = vert ? x : y;
+    if ((coord & (ts_dim - 1)) != 0) return advance;
+    if (coord == 0) return advance;
+    size_t prev_idx = vert ? idx - ((size_t)1 << ss) : idx - ((size_t)g.mi_cols << ss);
+    int ptw, pth;
+    tx_dims(prev_idx, &ptw, &pth);
+    int pv_dim = vert ? ptw : pth;
+    bool curr_skipped = g.skip_inter[idx] != 0;
+    bool pv_skip = g.skip_inter[prev_idx] != 0;
+    bool pu_edge = g.block_id[prev_idx] != g.block_id[idx];
+    if (level != 0 && (!pv_skip || !curr_skipped || pu_edge)) {
+        int min_dim = std::min(ts_dim, pv_dim);
+        *len = (min_dim == 4) ? 4 : (plane != 0 ? 6 : (min_dim == 8 ? 8 : 14));
+    }
+    return advance;
+}
+
+// filter_plane / filter_plane_hbd (ENC/deblock.rs:811-928): all vertical
+// edges, then all horizontal edges.
+template <typename T>
+static void filter_plane(T *buf, int stride, int plane_w, int plane_h, int plane, int ss, int level_vert,
+                         int level_horz, const Geom &g, int sharpness, int bd) {
+    int mi_cols_p = plane_w / 4, mi_rows_p = plane_h / 4;
+    LfThresh tv = lf_thresholds(level_vert, sharpness);
+    for (int my = 0; my < mi_rows_p; ++my) {
+        int mx = 0;
+        while (mx < mi_cols_p) {
+            int len;
+            int adv = lpf_params(g, true, mx * 4, my * 4, plane, ss, level_vert, &len);
+            if (len) lpf_any(buf, (i64)(my * 4) * stride + mx * 4, stride, true, len, tv, bd);
+            mx += adv;
+        }
+    }
+    LfThresh th = lf_thresholds(level_horz, sharpness);
+    for (int mx = 0; mx < mi_cols_p; ++mx) {
+        int my = 0;
+        while (my < mi_rows_p) {
+            int len;
+            int adv = lpf_params(g, false, mx * 4, my * 4, plane, ss, level_horz, &len);
+            if (len) lpf_any(buf, (i64)(my * 4) * stride + mx * 4, stride, false, len, th, bd);
+            my += adv;
+        }
+    }
+}
+
+// apply_deblock_frame[_hbd] (ENC/deblock.rs:938-1006).
+template <typename T>
+static void apply_deblock_frame(T *y, T *u, T *v, int w, int h, bool chroma, const Geom &g, const u8 l[4],
+                                int sharpness, int bd) {
+    if (l[0] == 0 && l[1] == 0) return;
+    filter_plane(y, w, w, h, 0, 0, l[0], l[1], g, sharpness, bd);
+    if (chroma) {
+        int cw = w / 2, ch = h / 2;
+        if (l[2] != 0) filter_plane(u, cw, cw, ch, 1, 1, l[2], l[2], g, sharpness, bd);
+        if (l[3] != 0) filter_plane(v, cw, cw, ch, 2, 1, l[3], l[3], g, sharpness, bd);
+    }
+}
+
+// plane_sse (ENC/deblock.rs:208-220) / full_distortion_kernel16_bits
+// (DSP/hbd.rs:936-956).
+template <typename T> static i64 plane_sse(const T *a, const T *b, int w, int h) {
+    u64 sum = 0;
+    for (int r = 0; r < h; ++r)
+        for (int c = 0; c < w; ++c) {
+            i64 d = (i64)a[(size_t)r * w + c] - (i64)b[(size_t)r * w + c];
+            sum += (u64)(d * d);
+        }
+    return (i64)sum;
+}
+
+// pick_filter_levels_key_frame (ENC/deblock.rs:55-81).
+static void key_frame_levels(int qindex, int bd, u8 out[4]) {
+    i32 fg;
+    if (bd == 8) {
+        i32 q = zf_ac_qlookup_8[qindex];
+        fg = (q * 17563 - 421574 + (1 << 17)) >> 18;
+    } else {
+        i32 q = zf_ac_qlookup_10[qindex];
+        fg = ((q * 20723 + 4060632 + (1 << 19)) >> 20) - 4;
+    }
+    i32 fgc = fg / 2;
+    u8 y = (u8)clampv(fg, 0, 63), uv = (u8)clampv(fgc, 0, 63);
+    out[0] = y;
+    out[1] = y;
+    out[2] = uv;
+    out[3] = uv;
+}
+
+// search_filter_level (ENC/deblock.rs:307-411), still/key specialization,
+// over a callback that returns try_filter_plane's SSE for a level.
+template <typename F> static int search_filter_level(F &&try_level, int conv_th) {
+    const int min_l = 0, max_l = 63;
+    int filt_direction = 0;
+    int filt_mid = 0;  // last_frame_filter_level is all zero
+    int filter_step = filt_mid < 16 ? 4 : filt_mid / 4;
+    i64 ss_err[64];
+    for (auto &e : ss_err) e = -1;
+    i64 best_err = try_level(filt_mid);
+    int filt_best = filt_mid;
+    ss_err[filt_mid] = best_err;
+    int tot_convergence = 0;
+    while (filter_step > 0) {
+        int filt_high = std::min(filt_mid + filter_step, max_l);
+        int filt_low = std::max(filt_mid - filter_step, min_l);
+        i64 bias = (best_err >> (15 - (filt_mid / 8))) * (i64)filter_step;
+        bias >>= 1;
+        if (filt_direction <= 0 && filt_low != filt_mid) {
+            if (ss_err[filt_low] < 0) ss_err[filt_low] = try_level(filt_low);
+            if (ss_err[filt_low] < best_err + bias) {
+                if (ss_err[filt_low] < best_err) best_err = ss_err[filt_low];
+                filt_best = filt_low;
+            }
+        }
+        if (filt_direction >= 0 && filt_high != filt_mid) {
+            if (ss_err[filt_high] < 0) ss_err[filt_high] = try_level(filt_high);
+            if (ss_err[filt_high] < best_err - bias) {
+                best_err = ss_err[filt_high];
+                filt_best = filt_high;
+            }
+        }
+        if (filt_best == filt_mid) {
+            tot_convergence += 1;
+            if (tot_convergence == conv_th)
+                filter_step = 0;
+            else
+                filter_step /= 2;
+            filt_direction = 0;
+        } else {
+            filt_direction = filt_best < filt_mid ? -1 : 1;
+            filt_mid = filt_best;
+        }
+    }
+    return filt_best;
+}
+
+// pick_filter_levels_full_search (ENC/deblock.rs:481-524) with
+// try_filter_plane (:228-293).
+template <typename T>
+static void pick_levels_full_search(const T *const src[3], const T *const rec[3], int w, int h, bool chroma,
+                                    const Geom &g, int conv_th, int sharpness, int bd, u8 out[4]) {
+    std::vector<T> scratch;
+    auto try_plane = [&](int plane, int lvl) -> i64 {
+        int pw = plane ? w / 2 : w, ph = plane ? h / 2 : h, ss = plane ? 1 : 0;
+        scratch.assign(rec[plane], rec[plane] + (size_t)pw * ph);
+        if (lvl != 0) filter_plane(scratch.data(), pw, pw, ph, plane, ss, lvl, lvl, g, sharpness, bd);
+        return plane_sse(src[plane], scratch.data(), pw, ph);
+    };
+    int fy = search_filter_level([&](int l) { return try_plane(0, l); }, conv_th);
+    int fu = 0, fv = 0;
+    if (fy != 0 && chroma) {
+        fu = search_filter_level([&](int l) { return try_plane(1, l); }, conv_th);
+        fv = search_filter_level([&](int l) { return try_plane(2, l); }, conv_th);
+    }
+    out[0] = (u8)fy;
+    out[1] = (u8)fy;
+    out[2] = (u8)fu;
+    out[3] = (u8)fv;
+}
+
+// ===========================================================================
+// CDEF (DSP/cdef.rs, DSP/hbd.rs:1533-1900, ENC/cdef.rs)
+// ===========================================================================
+
+constexpr int CDEF_VBORDER = 3;
+constexpr int CDEF_HBORDER = 8;
+constexpr int CDEF_BSTRIDE = 144;
+constexpr int CDEF_INBUF_SIZE = CDEF_BSTRIDE * (128 + 2 * CDEF_VBORDER);
+constexpr u16 CDEF_VERY_LARGE = 0x7f7f;
+constexpr int BLOCK_4X4 = 0, BLOCK_4X8 = 1, BLOCK_8X4 = 2, BLOCK_8X8 = 3;
+
+// eb_cdef_directions_padded (DSP/cdef.rs:73-89).
+static const int CDEF_DIRS[12][2] = {
+    {CDEF_BSTRIDE, 2 * CDEF_BSTRIDE},      {CDEF_BSTRIDE, 2 * CDEF_BSTRIDE - 1},
+    {-CDEF_BSTRIDE + 1, -2 * CDEF_BSTRIDE + 2}, {1, -CDEF_BSTRIDE + 2},
+    {1, 2},                                {1, CDEF_BSTRIDE + 2},
+    {CDEF_BSTRIDE + 1, 2 * CDEF_BSTRIDE + 2}, {CDEF_BSTRIDE, 2 * CDEF_BSTRIDE + 1},
+    {CDEF_BSTRIDE, 2 * CDEF_BSTRIDE},      {CDEF_BSTRIDE, 2 * CDEF_BSTRIDE - 1},
+    {-CDEF_BSTRIDE + 1, -2 * CDEF_BSTRIDE + 2}, {1, -CDEF_BSTRIDE + 2},
+};
+static inline int cdef_direction(int dir, int k) { return CDEF_DIRS[dir + 2][k]; }
+static const int CDEF_PRI_TAPS[2][2] = {{4, 2}, {3, 3}};
+static const int CDEF_SEC_TAPS[2][2] = {{2, 1}, {2, 1}};
+
+static inline int get_msb(u32 n) { return 31 - __builtin_clz(n); }
+
+// constrain (DSP/cdef.rs:113-120).
+static inline i32 constrain(i32 diff, i32 threshold, i32 damping) {
+    if (threshold == 0) return 0;
+    i32 shift = std::max(0, damping - get_msb((u32)threshold));
+    i32 sign = diff < 0 ? -1 : 1;
+    i32 ad = iabs(diff);
+    return sign * std::min(ad, std::max(0, threshold - (ad >> shift)));
+}
+// adjust_strength (DSP/cdef.rs:125-136).
+static inline i32 adjust_strength(i32 strength, i32 var) {
+    i32 i = (var >> 6) != 0 ? std::min(get_msb((u32)(var >> 6)), 12) : 0;
+    return var != 0 ? (strength * (4 + i) + 8) >> 4 : 0;
+}
+// cdef_find_dir (DSP/cdef.rs:143-198).
+static void cdef_find_dir(const u16 *img, int stride, int coeff_shift, int *out_dir, int *out_var) {
+    i32 cost[8] = {0};
+    i32 partial[8][15];
+    std::memset(partial, 0, sizeof(partial));
+    i32 best_cost = 0;
+    int best_dir = 0;
+    static const i32 DIV_TABLE[9] = {0, 840, 420, 280, 210, 168, 140, 120, 105};
+    for (int i = 0; i < 8; ++i)
+        for (int j = 0; j < 8; ++j) {
+            i32 x = ((i32)img[i * stride + j] >> coeff_shift) - 128;
+            partial[0][i + j] += x;
+            partial[1][i + j / 2] += x;
+            partial[2][i] += x;
+            partial[3][3 + i - j / 2] += x;
+            partial[4][7 + i - j] += x;
+            partial[5][3 - i / 2 + j] += x;
+            partial[6][j] += x;
+            partial[7][i / 2 + j] += x;
+        }
+    for (int i = 0; i < 8; ++i) {
+        cost[2] += partial[2][i] * partial[2][i];
+        cost[6] += partial[6][i] * partial[6][i];
+    }
+    cost[2] *= DIV_TABLE[8];
+    cost[6] *= DIV_TABLE[8];
+    for (int i = 0; i < 7; ++i) {
+        cost[0] += (partial[0][i] * partial[0][i] + partial[0][14 - i] * partial[0][14 - i]) * DIV_TABLE[i + 1];
+        cost[4] += (partial[4][i] * partial[4][i] + partial[4][14 - i] * partial[4][14 - i]) * DIV_TABLE[i + 1];
+    }
+    cost[0] += partial[0][7] * partial[0][7] * DIV_TABLE[8];
+    cost[4] += partial[4][7] * partial[4][7] * DIV_TABLE[8];
+    for (int i = 1; i < 8; i += 2) {
+        for (int j = 0; j < 5; ++j) cost[i] += partial[i][3 + j] * partial[i][3 + j];
+        cost[i] *= DIV_TABLE[8];
+        for (int j = 0; j < 3; ++j)
+            cost[i] += (partial[i][j] * partial[i][j] + partial[i][10 - j] * partial[i][10 - j]) * DIV_TABLE[2 * j + 2];
+    }
+    for (int i = 0; i < 8; ++i)
+        if (cost[i] > best_cost) {
+            best_cost = cost[i];
+            best_dir = i;
+        }
+    i32 var = best_cost - cost[(best_dir + 4) & 7];
+    var >>= 10;
+    *out_dir = best_dir;
+    *out_var = var;
+}
+
+// svt_cdef_filter_block_c core (DSP/cdef.rs:931-1034, dst8; DSP/hbd.rs:1765-1850,
+// dst16): the same arithmetic, the store type differs.
+template <typename D>
+static void cdef_filter_block(D *dst, i64 doff, int dstride, const u16 *inb, i64 ioff, i32 pri_strength,
+                              i32 sec_strength, int dir, i32 pri_damping, i32 sec_damping, int bsize,
+                              int coeff_shift, int sub) {
+    const int *pri_taps = CDEF_PRI_TAPS[(pri_strength >> coeff_shift) & 1];
+    const int *sec_taps = CDEF_SEC_TAPS[(pri_strength >> coeff_shift) & 1];
+    int rows = (bsize == BLOCK_8X8 || bsize == BLOCK_4X8) ? 8 : 4;
+    int cols = (bsize == BLOCK_8X8 || bsize == BLOCK_8X4) ? 8 : 4;
+    auto at = [&](int i, int j, int off) -> u16 { return inb[ioff + (i64)i * CDEF_BSTRIDE + j + off]; };
+    for (int i = 0; i < rows; i += sub) {
+        for (int j = 0; j < cols; ++j) {
+            i16 sum = 0;
+            i16 x = (i16)at(i, j, 0);
+            i32 max = x, min = x;
+            for (int k = 0; k < 2; ++k) {
+                i16 p0 = (i16)at(i, j, cdef_direction(dir, k));
+                i16 p1 = (i16)at(i, j, -cdef_direction(dir, k));
+                sum = (i16)(sum + (i16)(pri_taps[k] * constrain((i32)p0 - (i32)x, pri_strength, pri_damping)));
+                sum = (i16)(sum + (i16)(pri_taps[k] * constrain((i32)p1 - (i32)x, pri_strength, pri_damping)));
+                if ((u16)p0 != CDEF_VERY_LARGE) max = std::max((i32)p0, max);
+                if ((u16)p1 != CDEF_VERY_LARGE) max = std::max((i32)p1, max);
+                min = std::min((i32)p0, min);
+                min = std::min((i32)p1, min);
+                i16 s0 = (i16)at(i, j, cdef_direction(dir + 2, k));
+                i16 s1 = (i16)at(i, j, -cdef_direction(dir + 2, k));
+                i16 s2 = (i16)at(i, j, cdef_direction(dir - 2, k));
+                i16 s3 = (i16)at(i, j, -cdef_direction(dir - 2, k));
+                if ((u16)s0 != CDEF_VERY_LARGE) max = std::max((i32)s0, max);
+                if ((u16)s1 != CDEF_VERY_LARGE) max = std::max((i32)s1, max);
+                if ((u16)s2 != CDEF_VERY_LARGE) max = std::max((i32)s2, max);
+                if ((u16)s3 != CDEF_VERY_LARGE) max = std::max((i32)s3, max);
+                min = std::min((i32)s0, min);
+                min = std::min((i32)s1, min);
+                min = std::min((i32)s2, min);
+                min = std::min((i32)s3, min);
+                sum = (i16)(sum + (i16)(sec_taps[k] * constrain((i32)s0 - (i32)x, sec_strength, sec_damping)));
+                sum = (i16)(sum + (i16)(sec_taps[k] * constrain((i32)s1 - (i32)x, sec_strength, sec_damping)));
+                sum = (i16)(sum + (i16)(sec_taps[k] * constrain((i32)s2 - (i32)x, sec_strength, sec_damping)));
+                sum = (i16)(sum + (i16)(sec_taps[k] * constrain((i32)s3 - (i32)x, sec_strength, sec_damping)));
+            }
+            i32 y = clampv((i32)x + ((8 + (i32)sum - (i32)(sum < 0)) >> 4), min, max);
+            dst[doff + (i64)i * dstride + j] = (D)y;
+        }
+    }
+}
+
+// build_src (ENC/cdef.rs:517-544).
+template <typename P>
+static void build_src(u16 *src, const P *pre, int plane_w, int plane_h, int y0, int x0, int vsize, int hsize) {
+    for (int r = 0; r < vsize + 2 * CDEF_VBORDER; ++r) {
+        int gy = y0 + r - CDEF_VBORDER;
+        u16 *row = src + r * CDEF_BSTRIDE;
+        int n = hsize + 2 * CDEF_HBORDER;
+        if (gy < 0 || gy >= plane_h) {
+            for (int c = 0; c < n; ++c) row[c] = CDEF_VERY_LARGE;
+            continue;
+        }
+        for (int c = 0; c < n; ++c) {
+            int gx = x0 + c - CDEF_HBORDER;
+            row[c] = (gx < 0 || gx >= plane_w) ? CDEF_VERY_LARGE : (u16)pre[(size_t)gy * plane_w + gx];
+        }
+    }
+}
+
+struct CdefPick {
+    int damping = 3, bits = 0;
+    std::vector<std::pair<u8, u8>> strengths{{0, 0}};
+    std::vector<u8> fb_idx;
+    int nhfb = 0;
+    bool any(bool mono) const {
+        return bits != 0 || strengths[0].first != 0 || (!mono && strengths[0].second != 0);
+    }
+    std::pair<u8, u8> fb_strengths(int fbr, int fbc) const {
+        if (bits == 0) return strengths[0];
+        return strengths[fb_idx[(size_t)fbr * nhfb + fbc]];
+    }
+};
+
+// apply_cdef_frame (ENC/cdef.rs:343-506) and apply_cdef_frame_hbd
+// (:556-708): the same walk with coeff_shift = bd - 8 threaded through.
+template <typename T>
+static void apply_cdef_frame(T *y, T *u, T *v, int width, int height, bool chroma, const Geom &g,
+                             const CdefPick &params, int bd, zf_stats *stats) {
+    if (!params.any(!chroma)) return;
+    int coeff_shift = bd - 8;
+    int damping = params.damping + coeff_shift;
+    int nvfb = (height + 63) / 64, nhfb = (width + 63) / 64;
+    std::vector<T> pre_y(y, y + (size_t)width * height), pre_u, pre_v;
+    if (chroma) {
+        pre_u.assign(u, u + (size_t)(width / 2) * (height / 2));
+        pre_v.assign(v, v + (size_t)(width / 2) * (height / 2));
+    }
+    std::vector<u16> src(CDEF_INBUF_SIZE);
+    int dir[8][8] = {}, var[8][8] = {};
+    const int base = CDEF_VBORDER * CDEF_BSTRIDE + CDEF_HBORDER;
+    for (int fbr = 0; fbr < nvfb; ++fbr) {
+        int vsize = std::min(64, height - fbr * 64);
+        for (int fbc = 0; fbc < nhfb; ++fbc) {
+            int hsize = std::min(64, width - fbc * 64);
+            std::vector<std::pair<int, int>> dlist;
+            for (int by = 0; by < vsize / 8; ++by)
+                for (int bx = 0; bx < hsize / 8; ++bx)
+                    if (!g.is_8x8_all_skip(fbr * 16 + by * 2, fbc * 16 + bx * 2)) dlist.push_back({by, bx});
+            if (dlist.empty()) continue;
+            auto fbs = params.fb_strengths(fbr, fbc);
+            int lvl_y = (fbs.first / 4) << coeff_shift;
+            int sec_y = fbs.first % 4;
+            sec_y += (sec_y == 3);
+            sec_y <<= coeff_shift;
+            int lvl_uv = 0, sec_uv = 0;
+            if (chroma) {
+                lvl_uv = (fbs.second / 4) << coeff_shift;
+                sec_uv = fbs.second % 4;
+                sec_uv += (sec_uv == 3);
+                sec_uv <<= coeff_shift;
+            }
+            bool zero_y = lvl_y == 0 && sec_y == 0;
+            bool zero_uv = lvl_uv == 0 && sec_uv == 0;
+            build_src(src.data(), pre_y.data(), width, height, fbr * 64, fbc * 64, vsize, hsize);
+            for (auto &b : dlist)
+                cdef_find_dir(src.data() + base + b.first * 8 * CDEF_BSTRIDE + b.second * 8, CDEF_BSTRIDE,
+                              coeff_shift, &dir[b.first][b.second], &var[b.first][b.second]);
+            if (!zero_y) {
+                for (auto &b : dlist) {
+                    int by = b.first, bx = b.second;
+                    int t = adjust_strength(lvl_y, var[by][bx]);
+                    if (t == 0 && sec_y == 0) continue;
+                    i64 doff = (i64)(fbr * 64 + by * 8) * width + fbc * 64 + bx * 8;
+                    T before[64];
+                    for (int r = 0; r < 8; ++r)
+                        for (int c = 0; c < 8; ++c) before[r * 8 + c] = y[doff + (i64)r * width + c];
+                    cdef_filter_block(y, doff, width, src.data(), base + by * 8 * CDEF_BSTRIDE + bx * 8, t, sec_y,
+                                      lvl_y != 0 ? dir[by][bx] : 0, damping, damping, BLOCK_8X8, coeff_shift, 1);
+                    if (stats && bd == 8) {
+                        stats->cdef_filtered_px += 64;
+                        for (int r = 0; r < 8; ++r)
+                            for (int c = 0; c < 8; ++c)
+                                if (y[doff + (i64)r * width + c] != before[r * 8 + c]) stats->cdef_changed_px += 1;
+                    }
+                }
+            }
+            if (chroma && !zero_uv) {
+                int cw = width / 2, ch = height / 2;
+                for (int p = 0; p < 2; ++p) {
+                    const T *pre_c = p == 0 ? pre_u.data() : pre_v.data();
+                    T *buf = p == 0 ? u : v;
+                    build_src(src.data(), pre_c, cw, ch, fbr * 32, fbc * 32, vsize / 2, hsize / 2);
+                    for (auto &b : dlist) {
+                        int by = b.first, bx = b.second;
+                        i64 doff = (i64)(fbr * 32 + by * 4) * cw + fbc * 32 + bx * 4;
+                        T before[16];
+                        for (int r = 0; r < 4; ++r)
+                            for (int c = 0; c < 4; ++c) before[r * 4 + c] = buf[doff + (i64)r * cw + c];
+                        cdef_filter_block(buf, doff, cw, src.data(), base + by * 4 * CDEF_BSTRIDE + bx * 4, lvl_uv,
+                                          sec_uv, lvl_uv != 0 ? dir[by][bx] : 0, damping - 1, damping - 1, BLOCK_4X4,
+                                          coeff_shift, 1);
+                        if (stats && bd == 8) {
+                            stats->cdef_filtered_px += 16;
+                            for (int r = 0; r < 4; ++r)
+                                for (int c = 0; c < 4; ++c)
+                                    if (buf[doff + (i64)r * cw + c] != before[r * 4 + c]) stats->cdef_changed_px += 1;
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+// pick_cdef_params_key_frame (ENC/cdef.rs:151-206).
+static void cdef_qp_params(int qindex, int bd, bool screen, int out[3]) {
+    i32 q_raw = bd == 8 ? zf_ac_qlookup_8[qindex] : zf_ac_qlookup_10[qindex];
+    i32 q_i = q_raw >> (bd - 8);
+    i32 y_f1, y_f2, uv_f1, uv_f2;
+    if (screen) {
+        double q = (double)q_i;
+        y_f1 = (i32)(5.88217781e-06 * q * q + 6.10391455e-03 * q + 9.95043102e-02);
+        y_f2 = (i32)(-7.79934857e-06 * q * q + 6.58957830e-03 * q + 8.81045025e-01);
+        uv_f1 = (i32)(-6.79500136e-06 * q * q + 1.02695586e-02 * q + 1.36126802e-01);
+        uv_f2 = (i32)(-9.99613695e-08 * q * q - 1.79361339e-05 * q + 1.17022324e+0);
+    } else {
+        float q = (float)q_i;
+        auto rnd = [](float v) -> i32 { return (i32)roundf(v); };
+        y_f1 = rnd(q * q * 0.0000033731974f + q * 0.008070594f + 0.0187634f);
+        y_f2 = rnd(q * q * 0.0000029167343f + q * 0.0027798624f + 0.0079405f);
+        uv_f1 = rnd(q * q * -0.0000130790995f + q * 0.012892405f - 0.00748388f);
+        uv_f2 = rnd(q * q * 0.0000032651783f + q * 0.00035520183f + 0.00228092f);
+    }
+    y_f1 = clampv(y_f1, 0, 15);
+    y_f2 = clampv(y_f2, 0, 3);
+    uv_f1 = clampv(uv_f1, 0, 15);
+    uv_f2 = clampv(uv_f2, 0, 3);
+    out[0] = 3 + (qindex >> 6);
+    out[1] = y_f1 * 4 + y_f2;
+    out[2] = uv_f1 * 4 + uv_f2;
+}
+
+// cdef_search_cfg_for_preset (ENC/cdef.rs:788-810).
+struct CdefSearchCfg { std::vector<int> fs; int first_pass_num; int subsampling; };
+static const int PF_GI[16] = {0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40, 44, 48, 52, 56, 60};
+static CdefSearchCfg cdef_search_cfg_for_preset(int preset) {
+    std::vector<int> first, extra;
+    if (preset == 0) {
+        first = {0, 1, 2, 4, 5, 6, 8, 9, 10, 12, 13, 14};
+        extra = {1, 2, 3};
+    } else if (preset <= 3) {
+        first = {0, 4, 8, 12, 15};
+        extra = {1, 2, 3};
+    } else if (preset <= 5) {
+        first = {0, 7, 15};
+        extra = {2};
+    } else {
+        first = {0, 15};
+        extra = {2};
+    }
+    CdefSearchCfg c;
+    for (int i : first) c.fs.push_back(PF_GI[i]);
+    c.first_pass_num = (int)c.fs.size();
+    for (int i : first)
+        for (int d : extra) c.fs.push_back(PF_GI[i] + d);
+    c.subsampling = preset >= 6 ? 4 : 1;
+    return c;
+}
+
+// RDCOST (ENC/cdef.rs:814-816).
+static inline u64 rdc(u64 lambda, u64 rate, u64 dist) { return ((rate * lambda + 256) >> 9) + (dist << 7); }
+
+using MseRow = std::vector<u64>;  // [0, n_cand) luma, [n_cand, 2 n_cand) joint uv
+
+// search_one_dual (ENC/cdef.rs:824-862).
+static u64 search_one_dual(int *lev0, int *lev1, int nb_strengths, const std::vector<MseRow> &mse, int n_cand) {
+    std::vector<u64> tot((size_t)n_cand * n_cand, 0);
+    for (const MseRow &row : mse) {
+        u64 best = (u64)1 << 63;
+        for (int gi = 0; gi < nb_strengths; ++gi) {
+            u64 curr = row[lev0[gi]] + row[n_cand + lev1[gi]];
+            if (curr < best) best = curr;
+        }
+        for (int j = 0; j < n_cand; ++j)
+            for (int k = 0; k < n_cand; ++k) {
+                u64 curr = row[j] + row[n_cand + k];
+                tot[(size_t)j * n_cand + k] += std::min(curr, best);
+            }
+    }
+    u64 best_tot = (u64)1 << 63;
+    int b0 = 0, b1 = 0;
+    for (int j = 0; j < n_cand; ++j)
+        for (int k = 0; k < n_cand; ++k) {
+            u64 t = tot[(size_t)j * n_cand + k];
+            if (t < best_tot) {
+                best_tot = t;
+                b0 = j;
+                b1 = k;
+            }
+        }
+    lev0[nb_strengths] = b0;
+    lev1[nb_strengths] = b1;
+    return best_tot;
+}
+// joint_strength_search_dual (ENC/cdef.rs:866-885).
+static u64 joint_strength_search_dual(int *lev0, int *lev1, int nb, const std::vector<MseRow> &mse, int n_cand) {
+    u64 best_tot = (u64)1 << 63;
+    for (int i = 0; i < nb; ++i) best_tot = search_one_dual(lev0, lev1, i, mse, n_cand);
+    for (int it = 0; it < 4 * nb; ++it) {
+        for (int j = 0; j < nb - 1; ++j) {
+            lev0[j] = lev0[j + 1];
+            lev1[j] = lev1[j + 1];
+        }
+        best_tot = search_one_dual(lev0, lev1, nb - 1, mse, n_cand);
+    }
+    return best_tot;
+}
+// finish_cdef_rd_bd (ENC/cdef.rs:911-944).
+static int finish_cdef_rd(const std::vector<MseRow> &mse, int n_cand, int qindex, int bd, std::vector<int> &blev0,
+                          std::vector<int> &blev1) {
+    size_t sb_count = mse.size();
+    u64 lambda = bd == 8 ? kf_full_lambda_8bit_unweighted(qindex) : kf_full_lambda_bd10_unweighted(qindex);
+    u64 best_cost = (u64)1 << 63;
+    int best_bits = 0;
+    blev0.assign(1, 0);
+    blev1.assign(1, 0);
+    for (int i = 0; i <= 3; ++i) {
+        int nb = 1 << i;
+        int lev0[16] = {0}, lev1[16] = {0};
+        u64 tot = joint_strength_search_dual(lev0, lev1, nb, mse, n_cand);
+        u64 total_bits = (u64)(sb_count * i + nb * 6 * 2);
+        u64 cost = rdc(lambda, total_bits << 9, tot * 16);
+        if (cost < best_cost) {
+            best_cost = cost;
+            best_bits = i;
+            blev0.assign(lev0, lev0 + nb);
+            blev1.assign(lev1, lev1 + nb);
+        }
+    }
+    return best_bits;
+}
+
+// filter_fb_packed[_hbd] (ENC/cdef.rs:952-1124): one fb at one candidate
+// into the packed tmp buffer.
+template <typename T>
+static void filter_fb_packed(T *tmp, const u16 *src_pad, const std::vector<std::pair<int, int>> &dlist, int strength,
+                             int damping, int pli, int sub, int coeff_shift, int dir[8][8], int var[8][8],
+                             bool *dirinit) {
+    int pri_strength = (strength / 4) << coeff_shift;
+    int sec = strength % 4;
+    int sec_strength = (sec + (sec == 3)) << coeff_shift;
+    damping = damping + coeff_shift - (pli != 0);
+    int bsx = pli == 0 ? 3 : 2, bsy = bsx;
+    int bsize = pli == 0 ? BLOCK_8X8 : BLOCK_4X4;
+    const int base = CDEF_VBORDER * CDEF_BSTRIDE + CDEF_HBORDER;
+    if (strength == 0) {
+        for (size_t bi = 0; bi < dlist.size(); ++bi) {
+            int by = dlist[bi].first, bx = dlist[bi].second;
+            i64 ioff = base + (i64)(by << bsy) * CDEF_BSTRIDE + (bx << bsx);
+            i64 doff = (i64)bi << (bsx + bsy);
+            for (int iy = 0; iy < (1 << bsy); iy += sub)
+                for (int ix = 0; ix < (1 << bsx); ++ix) tmp[doff + (iy << bsx) + ix] = (T)src_pad[ioff + (i64)iy * CDEF_BSTRIDE + ix];
+        }
+        return;
+    }
+    if (pli == 0 && !*dirinit) {
+        for (auto &b : dlist)
+            cdef_find_dir(src_pad + base + b.first * 8 * CDEF_BSTRIDE + b.second * 8, CDEF_BSTRIDE, coeff_shift,
+                          &dir[b.first][b.second], &var[b.first][b.second]);
+        *dirinit = true;
+    }
+    for (size_t bi = 0; bi < dlist.size(); ++bi) {
+        int by = dlist[bi].first, bx = dlist[bi].second;
+        int t = pli != 0 ? pri_strength : adjust_strength(pri_strength, var[by][bx]);
+        i64 doff = (i64)bi << (bsx + bsy);
+        i64 ioff = base + (i64)(by << bsy) * CDEF_BSTRIDE + (bx << bsx);
+        cdef_filter_block(tmp, doff, 1 << bsx, src_pad, ioff, t, sec_strength, pri_strength != 0 ? dir[by][bx] : 0,
+                          damping, damping, bsize, coeff_shift, sub);
+    }
+}
+
+// dist_packed (ENC/cdef.rs:1128-1153) / compute_cdef_dist_16bit
+// (DSP/cdef.rs:1160-1187): SSE over the subsampled rows, >> 2*coeff_shift.
+template <typename T>
+static u64 dist_packed(const T *tmp, const T *src_plane, int plane_w, int fb_y0, int fb_x0,
+                       const std::vector<std::pair<int, int>> &dlist, bool luma, int sub, int coeff_shift) {
+    int dim = luma ? 8 : 4;
+    u64 sum = 0;
+    for (size_t bi = 0; bi < dlist.size(); ++bi) {
+        int by = dlist[bi].first, bx = dlist[bi].second;
+        i64 s0 = (i64)(fb_y0 + by * dim) * plane_w + fb_x0 + bx * dim;
+        i64 p0 = (i64)bi * dim * dim;
+        for (int i = 0; i < dim; i += sub)
+            for (int j = 0; j < dim; ++j) {
+                i32 e = (i32)src_plane[s0 + (i64)i * plane_w + j] - (i32)tmp[p0 + i * dim + j];
+                sum += (u64)(e * e);
+            }
+    }
+    return sum >> (2 * coeff_shift);
+}
+
+constexpr u64 DEFAULT_MSE_UV = 1040400;
+
+// cdef_search_still[_hbd] (ENC/cdef.rs:1166-1352, :1374-1568). Returns
+// false for the AllSkip outcome.
+template <typename T>
+static bool cdef_search_still(const CdefSearchCfg &cfg, const T *const rec[3], const T *const srcp[3], int width,
+                              int height, bool chroma, const Geom &g, int qindex, int bd, CdefPick *pick,
+                              u64 *mse_out, u8 *fb_has_row) {
+    int coeff_shift = bd - 8;
+    int damping = 3 + (qindex >> 6);
+    int nvfb = (height + 63) / 64, nhfb = (width + 63) / 64;
+    int n_cand = (int)cfg.fs.size();
+    int sub_y = std::min(cfg.subsampling, 4), sub_uv = std::min(cfg.subsampling, 1);
+    std::vector<MseRow> mse;
+    std::vector<std::pair<int, int>> fb_addr;
+    std::vector<u16> src_pad(CDEF_INBUF_SIZE);
+    std::vector<T> tmp(64 * 64);
+    for (int fbr = 0; fbr < nvfb; ++fbr) {
+        int vsize = std::min(64, height - fbr * 64);
+        for (int fbc = 0; fbc < nhfb; ++fbc) {
+            int hsize = std::min(64, width - fbc * 64);
+            std::vector<std::pair<int, int>> dlist;
+            for (int by = 0; by < vsize / 8; ++by)
+                for (int bx = 0; bx < hsize / 8; ++bx)
+                    if (!g.is_8x8_all_skip(fbr * 16 + by * 2, fbc * 16 + bx * 2)) dlist.push_back({by, bx});
+            if (fb_has_row) fb_has_row[(size_t)fbr * nhfb + fbc] = 0;
+            if (dlist.empty()) continue;
+            MseRow row((size_t)2 * n_cand, 0);
+            int dir[8][8] = {}, var[8][8] = {};
+            bool dirinit = false;
+            build_src(src_pad.data(), rec[0], width, height, fbr * 64, fbc * 64, vsize, hsize);
+            for (int gi = 0; gi < n_cand; ++gi) {
+                filter_fb_packed(tmp.data(), src_pad.data(), dlist, cfg.fs[gi], damping, 0, sub_y, coeff_shift, dir,
+                                 var, &dirinit);
+                u64 d = dist_packed(tmp.data(), srcp[0], width, fbr * 64, fbc * 64, dlist, true, sub_y, coeff_shift);
+                row[gi] = d * (u64)sub_y;
+            }
+            if (chroma) {
+                int cw = width / 2, ch = height / 2;
+                for (int gi = cfg.first_pass_num; gi < n_cand; ++gi) row[n_cand + gi] = DEFAULT_MSE_UV * 64;
+                for (int p = 1; p <= 2; ++p) {
+                    build_src(src_pad.data(), rec[p], cw, ch, fbr * 32, fbc * 32, vsize / 2, hsize / 2);
+                    for (int gi = 0; gi < cfg.first_pass_num; ++gi) {
+                        filter_fb_packed(tmp.data(), src_pad.data(), dlist, cfg.fs[gi], damping, 1, sub_uv,
+                                         coeff_shift, dir, var, &dirinit);
+                        u64 d = dist_packed(tmp.data(), srcp[p], cw, fbr * 32, fbc * 32, dlist, false, sub_uv,
+                                            coeff_shift);
+                        row[n_cand + gi] += d * (u64)sub_uv;
+                    }
+                }
+            }
+            if (mse_out) std::memcpy(mse_out + ((size_t)fbr * nhfb + fbc) * 2 * n_cand, row.data(), row.size() * 8);
+            if (fb_has_row) fb_has_row[(size_t)fbr * nhfb + fbc] = 1;
+            mse.push_back(row);
+            fb_addr.push_back({fbr, fbc});
+        }
+    }
+    if (mse.empty()) return false;
+    std::vector<int> lev0, lev1;
+    int bits = finish_cdef_rd(mse, n_cand, qindex, bd, lev0, lev1);
+    int nb = 1 << bits;
+    pick->fb_idx.assign((size_t)nvfb * nhfb, 0);
+    for (size_t i = 0; i < fb_addr.size(); ++i) {
+        int best_gi = 0;
+        u64 best = UINT64_MAX;
+        for (int gi = 0; gi < nb; ++gi) {
+            u64 cur = mse[i][lev0[gi]] + mse[i][n_cand + lev1[gi]];
+            if (cur < best) {
+                best_gi = gi;
+                best = cur;
+            }
+        }
+        pick->fb_idx[(size_t)fb_addr[i].first * nhfb + fb_addr[i].second] = (u8)best_gi;
+    }
+    pick->strengths.clear();
+    for (int gi = 0; gi < nb; ++gi) pick->strengths.push_back({(u8)cfg.fs[lev0[gi]], (u8)cfg.fs[lev1[gi]]});
+    pick->damping = 3 + (qindex >> 6);
+    pick->bits = bits;
+    pick->nhfb = nhfb;
+    return true;
+}
+
+// The CDEF pick of pipeline.rs:3042-3144 for a still key frame.
+template <typename T>
+static CdefPick cdef_pick(const T *const rec[3], const T *const src[3], int w, int h, bool chroma, const Geom &g,
+                          int preset, int qindex, int bd, bool sc_class5, u64 *mse_out, u8 *fb_has_row,
+                          int *ncand_out) {
+    CdefPick p;
+    int nhfb = (w + 63) / 64;
+    if (preset <= 6) {
+        CdefSearchCfg cfg = cdef_search_cfg_for_preset(preset);
+        if (ncand_out) *ncand_out = (int)cfg.fs.size();
+        if (g.cdef_frame_all_skip()) {
+            p.damping = 3 + (qindex >> 6);
+            if (fb_has_row) std::memset(fb_has_row, 0, (size_t)nhfb * ((h + 63) / 64));
+            return p;
+        }
+        if (!cdef_search_still(cfg, rec, src, w, h, chroma, g, qindex, bd, &p, mse_out, fb_has_row)) {
+            p = CdefPick();
+            p.damping = 3 + (qindex >> 6);
+        }
+        return p;
+    }
+    if (ncand_out) *ncand_out = 0;
+    int q[3];
+    cdef_qp_params(qindex, bd, sc_class5, q);
+    p.damping = q[0];
+    p.strengths = {{(u8)q[1], (u8)q[2]}};
+    return p;
+}
+
+// ===========================================================================
+// Loop restoration (DSP/restoration.rs, ENC/restoration.rs, ENT/lr.rs)
+// ===========================================================================
+
+constexpr int WIENER_WIN = 7, WIENER_WIN_CHROMA = 5, WIENER_HALFWIN = 3;
+constexpr int WIENER_FILT_STEP = 128;
+constexpr int TAP0_MIDV = 3, TAP1_MIDV = -7, TAP2_MIDV = 15;
+constexpr int TAP0_MINV = TAP0_MIDV - 8, TAP1_MINV = TAP1_MIDV - 16, TAP2_MINV = TAP2_MIDV - 32;
+constexpr int TAP0_MAXV = TAP0_MIDV - 1 + 8, TAP1_MAXV = TAP1_MIDV - 1 + 16, TAP2_MAXV = TAP2_MIDV - 1 + 32;
+constexpr int PROC_UNIT = 64, UNIT_OFFSET = 8, RBORDER = 3, CTX_VERT = 2, EXTRA_HORZ = 4, UNITSIZE_MAX = 256;
+constexpr int FILTER_BITS = 7, ROUND0_BITS = 3, ROUND1_BITS = 2 * FILTER_BITS - ROUND0_BITS;
+
+struct WienerInfo {
+    i16 vfilter[8], hfilter[8];
+};
+// set_default_wiener (DSP/restoration.rs:100-118).
+static WienerInfo default_wiener() {
+    WienerInfo w;
+    const i16 mid[8] = {TAP0_MIDV, TAP1_MIDV, TAP2_MIDV, (i16)(-2 * (TAP2_MIDV + TAP1_MIDV + TAP0_MIDV)),
+                        TAP2_MIDV, TAP1_MIDV, TAP0_MIDV, 0};
+    std::memcpy(w.vfilter, mid, sizeof(mid));
+    std::memcpy(w.hfilter, mid, sizeof(mid));
+    return w;
+}
+
+static inline i32 round_power_of_two(i32 v, int n) { return (v + (1 << (n - 1))) >> n; }
+
+// wiener_convolve_add_src[_hbd] (DSP/restoration.rs:138-195, :1820-1871).
+// The 8-bit body is the bd = 8 instance of the highbd one.
+template <typename T>
+static void wiener_convolve_add_src(const T *src, i64 src_origin, i64 src_stride, T *dst, i64 dst_origin,
+                                    i64 dst_stride, const i16 *hf, const i16 *vf, int w, int h, int bd) {
+    int ih = h + 6;
+    std::vector<u16> temp((size_t)(ih + 1) * std::max(w, 1), 0);
+    int ts = w;
+    i32 clamp_limit = (1 << (bd + 1 + FILTER_BITS - ROUND0_BITS)) - 1;
+    for (int y = 0; y < ih; ++y) {
+        i64 row_base = src_origin + (i64)y * src_stride - 3 * src_stride;
+        for (int x = 0; x < w; ++x) {
+            auto px = [&](int k) -> i32 { return (i32)src[row_base + x + k - 3]; };
+            i32 sum = (px(3) << FILTER_BITS) + (1 << (bd + FILTER_BITS - 1));
+            for (int k = 0; k < 8; ++k) sum += px(k) * (i32)hf[k];
+            temp[(size_t)y * ts + x] = (u16)clampv(round_power_of_two(sum, ROUND0_BITS), 0, clamp_limit);
+        }
+    }
+    i32 pixel_max = (1 << bd) - 1;
+    for (int x = 0; x < w; ++x)
+        for (int y = 0; y < h; ++y) {
+            size_t b = (size_t)y * ts + x;
+            i32 center = temp[b + 3 * ts];
+            i32 sum = (center << FILTER_BITS) - (1 << (bd + ROUND1_BITS - 1));
+            for (int k = 0; k < 8; ++k) sum += (i32)temp[b + (size_t)k * ts] * (i32)vf[k];
+            dst[dst_origin + (i64)y * dst_stride + x] = (T)clampv(round_power_of_two(sum, ROUND1_BITS), 0, pixel_max);
+        }
+}
+
+// find_average[_hbd] (DSP/restoration.rs:198-215, :1707-1724).
+template <typename T>
+static i64 find_average(const T *src, i64 origin, i64 stride, int hs, int he, int vs, int ve) {
+    u64 sum = 0;
+    for (int i = vs; i < ve; ++i)
+        for (int j = hs; j < he; ++j) sum += (u64)src[origin + (i64)i * stride + j];
+    return (i64)(sum / ((u64)(ve - vs) * (u64)(he - hs)));
+}
+
+// compute_stats (DSP/restoration.rs:567-632, 8-bit: i16 deltas, i32
+// products, i64 sums) and compute_stats_hbd (:1738-1807: i32 deltas, i64
+// products, then the bit-depth divider on the upper triangle + mirror).
+template <typename T>
+static void compute_stats(int win, const T *dgd, i64 dgd_origin, i64 dgd_stride, const T *src, i64 src_origin,
+                          i64 src_stride, int hs, int he, int vs, int ve, i64 *m, i64 *h, int bd) {
+    int win2 = win * win, half = win >> 1;
+    i64 avg = find_average(dgd, dgd_origin, dgd_stride, hs, he, vs, ve);
+    std::fill(m, m + win2, 0);
+    std::fill(h, h + (size_t)win2 * win2, 0);
+    i64 y[49];
+    for (int i = vs; i < ve; ++i)
+        for (int j = hs; j < he; ++j) {
+            i64 x = (i64)src[src_origin + (i64)i * src_stride + j] - avg;
+            int idx = 0;
+            for (int k = -half; k <= half; ++k)
+                for (int l = -half; l <= half; ++l)
+                    y[idx++] = (i64)dgd[dgd_origin + (i64)(i + l) * dgd_stride + (j + k)] - avg;
+            for (int k = 0; k < win2; ++k) {
+                m[k] += y[k] * x;
+                for (int l = k; l < win2; ++l) h[(size_t)k * win2 + l] += y[k] * y[l];
+            }
+        }
+    i64 divider = bd == 12 ? 16 : (bd == 10 ? 4 : 1);
+    if (divider == 1) {
+        for (int k = 0; k < win2; ++k)
+            for (int l = k + 1; l < win2; ++l) h[(size_t)l * win2 + k] = h[(size_t)k * win2 + l];
+    } else {
+        for (int k = 0; k < win2; ++k) {
+            m[k] /= divider;
+            h[(size_t)k * win2 + k] /= divider;
+            for (int l = k + 1; l < win2; ++l) {
+                h[(size_t)k * win2 + l] /= divider;
+                h[(size_t)l * win2 + k] = h[(size_t)k * win2 + l];
+            }
+        }
+    }
+}
+
+constexpr i64 TAP_SCALE = 1 << 16;
+
+static inline int wrap_index(int i, int win) {
+    int half1 = (win >> 1) + 1;
+    return i >= half1 ? win - 1 - i : i;
+}
+// linsolve_wiener (DSP/restoration.rs:809-846).
+static bool linsolve_wiener(int n, i64 *a, int stride, i64 *b, i32 *x) {
+    for (int k = 0; k < n - 1; ++k) {
+        for (int i = n - 1; i >= k + 1; --i) {
+            if (iabs64(a[(i - 1) * stride + k]) < iabs64(a[i * stride + k])) {
+                for (int j = 0; j < n; ++j) std::swap(a[i * stride + j], a[(i - 1) * stride + j]);
+                std::swap(b[i], b[i - 1]);
+            }
+        }
+        for (int i = k; i < n - 1; ++i) {
+            if (a[k * stride + k] == 0) return false;
+            i64 c = a[(i + 1) * stride + k];
+            i64 cd = a[k * stride + k];
+            for (int j = 0; j < n; ++j) a[(i + 1) * stride + j] -= c / 256 * a[k * stride + j] / cd * 256;
+            b[i + 1] -= c * b[k] / cd;
+        }
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        if (a[i * stride + i] == 0) return false;
+        i64 c = 0;
+        for (int j = i + 1; j < n; ++j) c += a[i * stride + j] * (i64)x[j] / TAP_SCALE;
+        x[i] = (i32)(TAP_SCALE * (b[i] - c) / a[i * stride + i]);
+    }
+    return true;
+}
+// normalize_and_solve (DSP/restoration.rs:913-941).
+static void normalize_and_solve(int win, int half1, i64 *av, i64 *bv, i32 *out) {
+    i64 a_h1 = av[half1 - 1];
+    for (int i = 0; i < half1 - 1; ++i)
+        av[i] -= a_h1 * 2 + bv[i * half1 + half1 - 1] - 2 * bv[(half1 - 1) * half1 + (half1 - 1)];
+    for (int i = 0; i < half1 - 1; ++i)
+        for (int j = 0; j < half1 - 1; ++j)
+            bv[i * half1 + j] -=
+                2 * (bv[i * half1 + (half1 - 1)] + bv[(half1 - 1) * half1 + j] - 2 * bv[(half1 - 1) * half1 + (half1 - 1)]);
+    i32 s[WIENER_WIN] = {0};
+    if (linsolve_wiener(half1 - 1, bv, half1, av, s)) {
+        s[half1 - 1] = (i32)TAP_SCALE;
+        for (int i = half1; i < win; ++i) {
+            s[i] = s[win - 1 - i];
+            s[half1 - 1] -= 2 * s[i];
+        }
+        std::memcpy(out, s, sizeof(i32) * win);
+    }
+}
+// update_a_sep_sym (DSP/restoration.rs:849-878).
+static void update_a_sep_sym(int win, const i64 *m, const i64 *h, i32 *a, const i32 *b) {
+    int win2 = win * win, half1 = (win >> 1) + 1;
+    i64 av[WIENER_HALFWIN + 1] = {0}, bv[(WIENER_HALFWIN + 1) * (WIENER_HALFWIN + 1)] = {0};
+    for (int i = 0; i < win; ++i)
+        for (int j = 0; j < win; ++j) {
+            int jj = wrap_index(j, win);
+            av[jj] += m[i * win + j] * (i64)b[i] / TAP_SCALE;
+        }
+    for (int i = 0; i < win; ++i)
+        for (int j = 0; j < win; ++j)
+            for (int k = 0; k < win; ++k)
+                for (int l = 0; l < win; ++l) {
+                    int kk = wrap_index(k, win), ll = wrap_index(l, win);
+                    i64 hv = h[(size_t)j * win * win2 + i * win + (size_t)k * win2 + l];
+                    bv[ll * half1 + kk] += hv * (i64)b[i] / TAP_SCALE * (i64)b[j] / TAP_SCALE;
+                }
+    normalize_and_solve(win, half1, av, bv, a);
+}
+// update_b_sep_sym (DSP/restoration.rs:881-909).
+static void update_b_sep_sym(int win, const i64 *m, const i64 *h, const i32 *a, i32 *b) {
+    int win2 = win * win, half1 = (win >> 1) + 1;
+    i64 av[WIENER_HALFWIN + 1] = {0}, bv[(WIENER_HALFWIN + 1) * (WIENER_HALFWIN + 1)] = {0};
+    for (int i = 0; i < win; ++i) {
+        int ii = wrap_index(i, win);
+        for (int j = 0; j < win; ++j) av[ii] += m[i * win + j] * (i64)a[j] / TAP_SCALE;
+    }
+    for (int i = 0; i < win; ++i)
+        for (int j = 0; j < win; ++j) {
+            int ii = wrap_index(i, win), jj = wrap_index(j, win);
+            for (int k = 0; k < win; ++k)
+                for (int l = 0; l < win; ++l) {
+                    i64 hv = h[(size_t)i * win * win2 + j * win + (size_t)k * win2 + l];
+                    bv[jj * half1 + ii] += hv * (i64)a[k] / TAP_SCALE * (i64)a[l] / TAP_SCALE;
+                }
+        }
+    normalize_and_solve(win, half1, av, bv, b);
+}
+// wiener_decompose_sep_sym (DSP/restoration.rs:945-974).
+static void wiener_decompose_sep_sym(int win, const i64 *m, const i64 *h, i32 *a, i32 *b) {
+    static const i32 INIT[WIENER_WIN] = {TAP0_MIDV, TAP1_MIDV, TAP2_MIDV,
+                                         WIENER_FILT_STEP - 2 * (TAP0_MIDV + TAP1_MIDV + TAP2_MIDV),
+                                         TAP2_MIDV, TAP1_MIDV, TAP0_MIDV};
+    int plane_off = (WIENER_WIN - win) >> 1;
+    for (int i = 0; i < win; ++i) {
+        i32 v = (i32)(TAP_SCALE / WIENER_FILT_STEP) * INIT[i + plane_off];
+        a[i] = v;
+        b[i] = v;
+    }
+    for (int it = 1; it < 5; ++it) {
+        update_a_sep_sym(win, m, h, a, b);
+        update_b_sep_sym(win, m, h, a, b);
+    }
+}
+// finalize_sym_filter (DSP/restoration.rs:978-1005).
+static void finalize_sym_filter(int win, const i32 *f, i16 *fi) {
+    int half = win >> 1;
+    for (int i = 0; i < half; ++i) {
+        i64 dividend = (i64)f[i] * WIENER_FILT_STEP;
+        i64 divisor = TAP_SCALE;
+        fi[i] = (i16)(dividend < 0 ? (dividend - divisor / 2) / divisor : (dividend + divisor / 2) / divisor);
+    }
+    if (win == WIENER_WIN) {
+        fi[0] = (i16)clampv<i32>(fi[0], TAP0_MINV, TAP0_MAXV);
+        fi[1] = (i16)clampv<i32>(fi[1], TAP1_MINV, TAP1_MAXV);
+        fi[2] = (i16)clampv<i32>(fi[2], TAP2_MINV, TAP2_MAXV);
+    } else {
+        fi[2] = (i16)clampv<i32>(fi[1], TAP2_MINV, TAP2_MAXV);
+        fi[1] = (i16)clampv<i32>(fi[0], TAP1_MINV, TAP1_MAXV);
+        fi[0] = 0;
+    }
+    fi[WIENER_WIN - 1] = fi[0];
+    fi[WIENER_WIN - 2] = fi[1];
+    fi[WIENER_WIN - 3] = fi[2];
+    fi[3] = (i16)(-2 * (fi[0] + fi[1] + fi[2]));
+    fi[7] = 0;
+}
+// compute_score (DSP/restoration.rs:1009-1056).
+static i64 compute_score(int win, const i64 *m, const i64 *h, const i16 *vf, const i16 *hf) {
+    i16 a[WIENER_WIN] = {0}, b[WIENER_WIN] = {0};
+    int plane_off = (WIENER_WIN - win) >> 1;
+    int win2 = win * win;
+    a[WIENER_HALFWIN] = WIENER_FILT_STEP;
+    b[WIENER_HALFWIN] = WIENER_FILT_STEP;
+    for (int i = 0; i < WIENER_HALFWIN; ++i) {
+        a[i] = vf[i];
+        a[WIENER_WIN - i - 1] = vf[i];
+        b[i] = hf[i];
+        b[WIENER_WIN - i - 1] = hf[i];
+        a[WIENER_HALFWIN] = (i16)(a[WIENER_HALFWIN] - 2 * a[i]);
+        b[WIENER_HALFWIN] = (i16)(b[WIENER_HALFWIN] - 2 * b[i]);
+    }
+    i32 ab[49];
+    for (int k = 0; k < win; ++k)
+        for (int l = 0; l < win; ++l) ab[k * win + l] = (i32)a[l + plane_off] * (i32)b[k + plane_off];
+    i64 p = 0, q = 0;
+    for (int k = 0; k < win2; ++k) {
+        p += (i64)ab[k] * m[k] / WIENER_FILT_STEP / WIENER_FILT_STEP;
+        for (int l = 0; l < win2; ++l)
+            q += (i64)ab[k] * h[(size_t)k * win2 + l] * (i64)ab[l] / WIENER_FILT_STEP / WIENER_FILT_STEP /
+                 WIENER_FILT_STEP / WIENER_FILT_STEP;
+    }
+    i64 score = q - 2 * p;
+    i64 i_p = m[win2 >> 1];
+    i64 i_q = h[(size_t)(win2 >> 1) * win2 + (win2 >> 1)];
+    return score - (i_q - 2 * i_p);
+}
+
+// extend_frame (DSP/restoration.rs:1065-1092).
+template <typename T>
+static void extend_frame(T *data, i64 origin, int width, int height, i64 stride, int bh, int bv) {
+    for (int i = 0; i < height; ++i) {
+        i64 row = origin + (i64)i * stride;
+        T left = data[row], right = data[row + width - 1];
+        for (int k = 1; k <= bh; ++k) {
+            data[row - k] = left;
+            data[row + width - 1 + k] = right;
+        }
+    }
+    int full_w = width + 2 * bh;
+    i64 top_row = origin - bh;
+    for (int i = 1; i <= bv; ++i) std::memmove(data + top_row - (i64)i * stride, data + top_row, sizeof(T) * full_w);
+    i64 bottom_row = origin - bh + (i64)(height - 1) * stride;
+    for (int i = 1; i <= bv; ++i) std::memmove(data + bottom_row + (i64)i * stride, data + bottom_row, sizeof(T) * full_w);
+}
+
+struct TileLimits { int h_start, h_end, v_start, v_end; };
+struct PixelRect { int left, top, right, bottom; };
+
+template <typename T> struct StripeBoundaries {
+    std::vector<T> above, below;
+    i64 stride = 0;
+};
+
+// get_stripe_boundary_info (DSP/restoration.rs:1124-1147).
+static void get_stripe_boundary_info(const TileLimits &lim, const PixelRect &r, int ss_y, bool *ca, bool *cb) {
+    *ca = true;
+    *cb = true;
+    int full = PROC_UNIT >> ss_y, off = UNIT_OFFSET >> ss_y;
+    bool first = lim.v_start == r.top;
+    int hgt = full - (first ? off : 0);
+    bool last = lim.v_start + hgt >= r.bottom;
+    if (first) *ca = false;
+    if (last) *cb = false;
+}
+
+template <typename T> struct LineBuffers { T above[RBORDER][400]; T below[RBORDER][400]; };
+
+// setup_processing_stripe_boundary (DSP/restoration.rs:1159-1203).
+template <typename T>
+static void setup_stripe_boundary(const TileLimits &lim, const StripeBoundaries<T> &rsb, int rsb_row, int h, T *data,
+                                  i64 data_origin, i64 data_stride, LineBuffers<T> &rlbs, bool ca, bool cb) {
+    i64 bs = rsb.stride;
+    int bx0 = lim.h_start;
+    int line_size = (lim.h_end - lim.h_start) + 2 * EXTRA_HORZ;
+    int data_x0 = lim.h_start - EXTRA_HORZ;
+    if (ca) {
+        i64 tl = data_origin + data_x0 + (i64)lim.v_start * data_stride;
+        for (int i = -RBORDER; i < 0; ++i) {
+            int buf_row = rsb_row + std::max(i + CTX_VERT, 0);
+            i64 boff = bx0 + (i64)buf_row * bs;
+            i64 dst = tl + (i64)i * data_stride;
+            std::memcpy(rlbs.above[i + RBORDER], data + dst, sizeof(T) * line_size);
+            std::memcpy(data + dst, rsb.above.data() + boff, sizeof(T) * line_size);
+        }
+    }
+    if (cb) {
+        int stripe_end = lim.v_start + h;
+        i64 bl = data_origin + data_x0 + (i64)stripe_end * data_stride;
+        for (int i = 0; i < RBORDER; ++i) {
+            int buf_row = rsb_row + std::min(i, CTX_VERT - 1);
+            i64 boff = bx0 + (i64)buf_row * bs;
+            i64 dst = bl + (i64)i * data_stride;
+            std::memcpy(rlbs.below[i], data + dst, sizeof(T) * line_size);
+            std::memcpy(data + dst, rsb.below.data() + boff, sizeof(T) * line_size);
+        }
+    }
+}
+// restore_processing_stripe_boundary (DSP/restoration.rs:1207-1243).
+template <typename T>
+static void restore_stripe_boundary(const TileLimits &lim, const LineBuffers<T> &rlbs, int h, T *data,
+                                    i64 data_origin, i64 data_stride, bool ca, bool cb) {
+    int line_size = (lim.h_end - lim.h_start) + 2 * EXTRA_HORZ;
+    int data_x0 = lim.h_start - EXTRA_HORZ;
+    if (ca) {
+        i64 tl = data_origin + data_x0 + (i64)lim.v_start * data_stride;
+        for (int i = -RBORDER; i < 0; ++i)
+            std::memcpy(data + tl + (i64)i * data_stride, rlbs.above[i + RBORDER], sizeof(T) * line_size);
+    }
+    if (cb) {
+        int sb = lim.v_start + h;
+        i64 bl = data_origin + data_x0 + (i64)sb * data_stride;
+        for (int i = 0; i < RBORDER; ++i) {
+            if (sb + i >= lim.v_end + RBORDER) break;
+            std::memcpy(data + bl + (i64)i * data_stride, rlbs.below[i], sizeof(T) * line_size);
+        }
+    }
+}
+// wiener_filter_stripe[_hbd] (DSP/restoration.rs:1248-1277, :1876-1907).
+template <typename T>
+static void wiener_filter_stripe(const WienerInfo &wi, int stripe_w, int stripe_h, int pu_w, const T *src, i64 so,
+                                 i64 ss, T *dst, i64 dof, i64 ds, int bd) {
+    for (int j = 0; j < stripe_w; j += pu_w) {
+        int w = std::min(pu_w, (stripe_w - j + 15) & ~15);
+        wiener_convolve_add_src(src, so + j, ss, dst, dof + j, ds, wi.hfilter, wi.vfilter, w, stripe_h, bd);
+    }
+}
+// loop_restoration_filter_unit (DSP/restoration.rs:1288-1385; the search
+// arm at need_boundaries = false is :1921-1979 for u16).
+template <typename T>
+static void filter_unit(bool need_boundaries, const TileLimits &lim, int rtype, const WienerInfo &wi,
+                        const StripeBoundaries<T> *rsb, const PixelRect &rect, int ss, T *data, i64 data_origin,
+                        i64 stride, T *dst, i64 dst_origin, i64 dst_stride, int bd) {
+    int unit_h = lim.v_end - lim.v_start, unit_w = lim.h_end - lim.h_start;
+    i64 data_tl = data_origin + (i64)lim.v_start * stride + lim.h_start;
+    i64 dst_tl = dst_origin + (i64)lim.v_start * dst_stride + lim.h_start;
+    if (rtype == ZF_RESTORE_NONE) {
+        for (int i = 0; i < unit_h; ++i)
+            std::memcpy(dst + dst_tl + (i64)i * dst_stride, data + data_tl + (i64)i * stride, sizeof(T) * unit_w);
+        return;
+    }
+    int pu_w = PROC_UNIT >> ss;
+    LineBuffers<T> rlbs;
+    TileLimits rem = lim;
+    int i = 0;
+    while (i < unit_h) {
+        rem.v_start = lim.v_start + i;
+        bool ca, cb;
+        get_stripe_boundary_info(rem, rect, ss, &ca, &cb);
+        int full = PROC_UNIT >> ss, off = UNIT_OFFSET >> ss;
+        int tile_stripe = (rem.v_start - rect.top + off) / full;
+        int rsb_row = CTX_VERT * tile_stripe;
+        int nominal = full - (tile_stripe == 0 ? off : 0);
+        int h = std::min(nominal, rem.v_end - rem.v_start);
+        if (need_boundaries) setup_stripe_boundary(rem, *rsb, rsb_row, h, data, data_origin, stride, rlbs, ca, cb);
+        wiener_filter_stripe(wi, unit_w, h, pu_w, data, data_tl + (i64)i * stride, stride, dst,
+                             dst_tl + (i64)i * dst_stride, dst_stride, bd);
+        if (need_boundaries) restore_stripe_boundary(rem, rlbs, h, data, data_origin, stride, ca, cb);
+        i += h;
+    }
+}
+
+// count_units_in_tile (DSP/restoration.rs:1388-1390).
+static int count_units_in_tile(int unit_size, int tile_size) {
+    return std::max((tile_size + (unit_size >> 1)) / unit_size, 1);
+}
+// foreach_rest_unit_in_tile (DSP/restoration.rs:1395-1448).
+template <typename F>
+static void foreach_rest_unit_in_tile(const PixelRect &r, int hunits, int unit_size, int ss_y, F &&f) {
+    int tile_w = r.right - r.left, tile_h = r.bottom - r.top;
+    int ext = unit_size * 3 / 2;
+    int y0 = 0, i = 0;
+    while (y0 < tile_h) {
+        int rem_h = tile_h - y0;
+        int h = rem_h < ext ? rem_h : unit_size;
+        TileLimits lim{0, 0, r.top + y0, r.top + y0 + h};
+        int voff = UNIT_OFFSET >> ss_y;
+        lim.v_start = std::max(r.top, lim.v_start - voff);
+        if (lim.v_end < r.bottom) lim.v_end -= voff;
+        int x0 = 0, j = 0;
+        while (x0 < tile_w) {
+            int rem_w = tile_w - x0;
+            int w = rem_w < ext ? rem_w : unit_size;
+            lim.h_start = r.left + x0;
+            lim.h_end = r.left + x0 + w;
+            f(lim, i * hunits + j);
+            x0 += w;
+            j += 1;
+        }
+        y0 += h;
+        i += 1;
+    }
+}
+
+// extend_lines (DSP/restoration.rs:1451-1466).
+template <typename T> static void extend_lines(T *buf, i64 start, int width, int height, i64 stride, int extend) {
+    for (int i = 0; i < height; ++i) {
+        i64 row = start + (i64)i * stride;
+        T l = buf[row], rr = buf[row + width - 1];
+        for (int k = 1; k <= extend; ++k) {
+            buf[row - k] = l;
+            buf[row + width - 1 + k] = rr;
+        }
+    }
+}
+// save_deblock_boundary_lines (DSP/restoration.rs:1470-1512).
+template <typename T>
+static void save_deblock_boundary_lines(const T *src, i64 src_stride, int src_w, int src_h, int row, int stripe,
+                                        bool above, StripeBoundaries<T> &b) {
+    std::vector<T> &buf = above ? b.above : b.below;
+    i64 rows = EXTRA_HORZ + (i64)CTX_VERT * stripe * b.stride;
+    int lines = std::min(CTX_VERT, src_h - row);
+    for (int i = 0; i < lines; ++i)
+        std::memcpy(buf.data() + rows + (i64)i * b.stride, src + (i64)(row + i) * src_stride, sizeof(T) * src_w);
+    if (lines == 1) std::memmove(buf.data() + rows + b.stride, buf.data() + rows, sizeof(T) * src_w);
+    extend_lines(buf.data(), rows, src_w, CTX_VERT, b.stride, EXTRA_HORZ);
+}
+// save_cdef_boundary_lines (DSP/restoration.rs:1516-1548).
+template <typename T>
+static void save_cdef_boundary_lines(const T *src, i64 src_stride, int src_w, int row, int stripe, bool above,
+                                     StripeBoundaries<T> &b) {
+    std::vector<T> &buf = above ? b.above : b.below;
+    i64 rows = EXTRA_HORZ + (i64)CTX_VERT * stripe * b.stride;
+    for (int i = 0; i < CTX_VERT; ++i)
+        std::memcpy(buf.data() + rows + (i64)i * b.stride, src + (i64)row * src_stride, sizeof(T) * src_w);
+    extend_lines(buf.data(), rows, src_w, CTX_VERT, b.stride, EXTRA_HORZ);
+}
+// save_tile_row_boundary_lines (DSP/restoration.rs:1554-1644).
+template <typename T>
+static void save_tile_row_boundary_lines(const T *src, i64 src_stride, int src_w, int src_h, int ss_y, bool after_cdef,
+                                         StripeBoundaries<T> &b) {
+    int sh = PROC_UNIT >> ss_y, soff = UNIT_OFFSET >> ss_y;
+    for (int ts = 0;; ++ts) {
+        int y0 = std::max(ts * sh - soff, 0);
+        if (y0 >= src_h) break;
+        int y1 = std::min((ts + 1) * sh - soff, src_h);
+        bool use_above = ts > 0, use_below = y1 < src_h;
+        if (!after_cdef) {
+            if (use_above) save_deblock_boundary_lines(src, src_stride, src_w, src_h, y0 - CTX_VERT, ts, true, b);
+            if (use_below) save_deblock_boundary_lines(src, src_stride, src_w, src_h, y1, ts, false, b);
+        } else {
+            if (!use_above) save_cdef_boundary_lines(src, src_stride, src_w, y0, ts, true, b);
+            if (!use_below) save_cdef_boundary_lines(src, src_stride, src_w, y1 - 1, ts, false, b);
+        }
+    }
+}
+// alloc_stripe_boundaries (DSP/restoration.rs:1649-1661).
+template <typename T> static StripeBoundaries<T> alloc_stripe_boundaries(int fw, int fh, int ss_x) {
+    int num = (UNIT_OFFSET + fh + 63) / 64;
+    int pw = ((fw + ss_x) >> ss_x) + 2 * EXTRA_HORZ;
+    StripeBoundaries<T> b;
+    b.stride = (pw + 31) & ~31;
+    size_t sz = (size_t)num * b.stride * CTX_VERT;
+    b.above.assign(sz, 0);
+    b.below.assign(sz, 0);
+    return b;
+}
+
+// sse_region (DSP/restoration.rs:1666-1684) and sse_region_hbd
+// (:1991-2036, with the u32 truncation of every partial sum).
+static i64 sse_region(const u8 *a, i64 ao, i64 as, const u8 *b, i64 bo, i64 bs, int w, int h) {
+    i64 sse = 0;
+    for (int i = 0; i < h; ++i)
+        for (int j = 0; j < w; ++j) {
+            i64 d = (i64)a[ao + i * as + j] - (i64)b[bo + i * bs + j];
+            sse += d * d;
+        }
+    return sse;
+}
+static i64 sse_region(const u16 *a, i64 ao, i64 as, const u16 *b, i64 bo, i64 bs, int w, int h) {
+    auto var = [&](i64 a0, i64 b0, int ww, int hh) -> i64 {
+        i64 s = 0;
+        for (int i = 0; i < hh; ++i)
+            for (int j = 0; j < ww; ++j) {
+                i64 d = (i64)a[a0 + i * as + j] - (i64)b[b0 + i * bs + j];
+                s += d * d;
+            }
+        return s;
+    };
+    int dw = w % 16, dh = h % 16;
+    i64 total = 0;
+    if (dw > 0) total += (i64)(u32)var(ao + w - dw, bo + w - dw, dw, h);
+    if (dh > 0) total += (i64)(u32)var(ao + (i64)(h - dh) * as, bo + (i64)(h - dh) * bs, w - dw, dh);
+    for (int y = 0; y < h / 16; ++y)
+        for (int x = 0; x < w / 16; ++x)
+            total += (i64)(u32)var(ao + (i64)y * 16 * as + x * 16, bo + (i64)y * 16 * bs + x * 16, 16, 16);
+    return total;
+}
+
+// ---- tap bit count (ENT/lr.rs:38-309) ----
+static inline u16 recenter_nonneg(u16 r, u16 v) {
+    if (v > (r << 1)) return v;
+    if (v >= r) return (u16)((v - r) << 1);
+    return (u16)(((r - v) << 1) - 1);
+}
+static inline u16 recenter_finite_nonneg(u16 n, u16 r, u16 v) {
+    if ((r << 1) <= n) return recenter_nonneg(r, v);
+    return recenter_nonneg((u16)(n - 1 - r), (u16)(n - 1 - v));
+}
+static i32 count_primitive_quniform(u16 n, u16 v) {
+    if (n <= 1) return 0;
+    i32 l = get_msb((u32)n - 1) + 1;
+    i32 m = (1 << l) - n;
+    return (i32)v < m ? l - 1 : l;
+}
+static i32 count_primitive_subexpfin(u16 n, u16 k, u16 v) {
+    i32 count = 0, i = 0, mk = 0;
+    for (;;) {
+        i32 b = i != 0 ? k + i - 1 : k;
+        i32 a = 1 << b;
+        if ((i32)n <= mk + 3 * a) {
+            count += count_primitive_quniform((u16)(n - mk), (u16)(v - mk));
+            break;
+        }
+        bool t = (i32)v >= mk + a;
+        count += 1;
+        if (t) {
+            i += 1;
+            mk += a;
+        } else {
+            count += b;
+            break;
+        }
+    }
+    return count;
+}
+static i32 count_primitive_refsubexpfin(u16 n, u16 k, u16 r, u16 v) {
+    return count_primitive_subexpfin(n, k, recenter_finite_nonneg(n, r, v));
+}
+// count_wiener_bits (ENT/lr.rs:240-309).
+static i32 count_wiener_bits(int win, const i16 *vf, const i16 *hf, const i16 *rvf, const i16 *rhf) {
+    auto tap = [](const i16 *f, const i16 *rf, int idx, int minv, int maxv, int k) -> i32 {
+        return count_primitive_refsubexpfin((u16)(maxv - minv + 1), (u16)k, (u16)(rf[idx] - minv), (u16)(f[idx] - minv));
+    };
+    i32 bits = 0;
+    if (win == WIENER_WIN) bits += tap(vf, rvf, 0, TAP0_MINV, TAP0_MAXV, 1);
+    bits += tap(vf, rvf, 1, TAP1_MINV, TAP1_MAXV, 2);
+    bits += tap(vf, rvf, 2, TAP2_MINV, TAP2_MAXV, 3);
+    if (win == WIENER_WIN) bits += tap(hf, rhf, 0, TAP0_MINV, TAP0_MAXV, 1);
+    bits += tap(hf, rhf, 1, TAP1_MINV, TAP1_MAXV, 2);
+    bits += tap(hf, rhf, 2, TAP2_MINV, TAP2_MAXV, 3);
+    return bits;
+}
+
+// RDCOST_DBL (ENC/restoration.rs:455-457).
+static double rdcost_dbl(i64 rdmult, i64 rate, i64 dist) {
+    return ((double)rate * (double)rdmult) / (double)(1u << 9) + (double)dist * (double)(1u << 7);
+}
+// wiener_restore_cost (ENC/restoration.rs:443-451): the default-CDF flag
+// costs, pinned by the reference test at :1192-1194.
+static const i64 RESTORE_COST[2] = {768, 320};
+
+struct WnCtrls { bool enabled, use_chroma; int tap_lvl; bool use_refinement, max_one_step; };
+// wn_filter_ctrls_allintra (ENC/restoration.rs:82-108).
+static WnCtrls wn_filter_ctrls_allintra(int preset) {
+    if (preset <= 3) return {true, true, 2, true, true};
+    if (preset <= 6) return {true, true, 2, false, true};
+    return {false, false, 2, false, true};
+}
+
+// PaddedPlaneT (ENC/restoration.rs:158-223) with a selectable right border.
+template <typename T> struct Padded {
+    std::vector<T> data;
+    i64 stride, origin;
+    int w, h;
+    Padded(int w_, int h_, int br) : w(w_), h(h_) {
+        const int B = 4;
+        stride = w + B + br;
+        data.assign((size_t)stride * (h + 2 * B), 0);
+        origin = (i64)B * stride + B;
+    }
+    void fill_from(const T *src, i64 src_stride) {
+        for (int y = 0; y < h; ++y) std::memcpy(data.data() + origin + (i64)y * stride, src + (i64)y * src_stride, sizeof(T) * w);
+    }
+    void copy_to(T *dst, i64 dst_stride) const {
+        for (int y = 0; y < h; ++y) std::memcpy(dst + (i64)y * dst_stride, data.data() + origin + (i64)y * stride, sizeof(T) * w);
+    }
+};
+static inline int right_border(int mode) { return mode == ZFO_LR_BORDER_PORT ? 4 : 32; }
+
+struct PlaneRest {
+    int frame_rtype = 0, unit_size = UNITSIZE_MAX, hunits = 1, vunits = 1;
+    std::vector<u8> rtype;
+    std::vector<WienerInfo> wiener;
+};
+
+// try_restoration_unit (ENC/restoration.rs:472-507).
+template <typename T>
+static i64 try_restoration_unit(Padded<T> &dgd, Padded<T> &trial, const T *src, i64 src_stride, const TileLimits &lim,
+                                const PixelRect &rect, int ss, const WienerInfo &wi, int bd) {
+    filter_unit<T>(false, lim, ZF_RESTORE_WIENER, wi, nullptr, rect, ss, dgd.data.data(), dgd.origin, dgd.stride,
+                   trial.data.data(), trial.origin, trial.stride, bd);
+    return sse_region(src, (i64)lim.v_start * src_stride + lim.h_start, src_stride, trial.data.data(),
+                      trial.origin + (i64)lim.v_start * trial.stride + lim.h_start, trial.stride,
+                      lim.h_end - lim.h_start, lim.v_end - lim.v_start);
+}
+// finer_tile_search_wiener (ENC/restoration.rs:513-636).
+template <typename T>
+static i64 finer_tile_search_wiener(const WnCtrls &c, Padded<T> &dgd, Padded<T> &trial, const T *src, i64 src_stride,
+                                    const TileLimits &lim, const PixelRect &rect, int ss, WienerInfo &wi, int win,
+                                    int bd) {
+    int plane_off = (WIENER_WIN - win) >> 1;
+    i64 err = try_restoration_unit(dgd, trial, src, src_stride, lim, rect, ss, wi, bd);
+    if (!c.use_refinement) return err;
+    const int start_step = 4, end_step = c.max_one_step ? 4 : 1;
+    const i16 tap_min[3] = {TAP0_MINV, TAP1_MINV, TAP2_MINV}, tap_max[3] = {TAP0_MAXV, TAP1_MAXV, TAP2_MAXV};
+    const int halfwin = WIENER_WIN >> 1;
+    for (int s = start_step; s >= end_step; s >>= 1) {
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int p = plane_off; p < halfwin; ++p) {
+                bool skip = false;
+                for (;;) {
+                    i16 *f = pass == 0 ? wi.hfilter : wi.vfilter;
+                    if (f[p] - s >= tap_min[p]) {
+                        f[p] = (i16)(f[p] - s);
+                        f[WIENER_WIN - p - 1] = (i16)(f[WIENER_WIN - p - 1] - s);
+                        f[halfwin] = (i16)(f[halfwin] + 2 * s);
+                        i64 err2 = try_restoration_unit(dgd, trial, src, src_stride, lim, rect, ss, wi, bd);
+                        if (err2 > err) {
+                            f[p] = (i16)(f[p] + s);
+                            f[WIENER_WIN - p - 1] = (i16)(f[WIENER_WIN - p - 1] + s);
+                            f[halfwin] = (i16)(f[halfwin] - 2 * s);
+                        } else {
+                            err = err2;
+                            skip = true;
+                            if (s == start_step && !c.max_one_step) continue;
+                        }
+                    }
+                    break;
+                }
+                if (skip) break;
+                for (;;) {
+                    i16 *f = pass == 0 ? wi.hfilter : wi.vfilter;
+                    if (f[p] + s <= tap_max[p]) {
+                        f[p] = (i16)(f[p] + s);
+                        f[WIENER_WIN - p - 1] = (i16)(f[WIENER_WIN - p - 1] + s);
+                        f[halfwin] = (i16)(f[halfwin] - 2 * s);
+                        i64 err2 = try_restoration_unit(dgd, trial, src, src_stride, lim, rect, ss, wi, bd);
+                        if (err2 > err) {
+                            f[p] = (i16)(f[p] - s);
+                            f[WIENER_WIN - p - 1] = (i16)(f[WIENER_WIN - p - 1] - s);
+                            f[halfwin] = (i16)(f[halfwin] + 2 * s);
+                        } else {
+                            err = err2;
+                            if (s == start_step && !c.max_one_step) continue;
+                        }
+                    }
+                    break;
+                }
+            }
+        }
+    }
+    return err;
+}
+
+// search_restoration_still_bd (ENC/restoration.rs:675-924). src/recon are
+// tight true-dim (chroma ceil) planes.
+template <typename T>
+static void search_restoration(const WnCtrls &c, const T *const src[3], const T *const recon[3], int w, int h,
+                               bool has_chroma, i64 rdmult, int bd, int border_mode, PlaneRest out[3]) {
+    int wn_luma = c.tap_lvl == 1 ? WIENER_WIN : WIENER_WIN_CHROMA;
+    int unit_size = UNITSIZE_MAX;
+    int plane_end = (has_chroma && c.use_chroma) ? 2 : 0;
+    for (int plane = 0; plane < 3; ++plane) {
+        bool is_uv = plane > 0;
+        int ss = is_uv ? 1 : 0;
+        int pw = is_uv ? (w + 1) / 2 : w, ph = is_uv ? (h + 1) / 2 : h;
+        int hunits = count_units_in_tile(unit_size, pw), vunits = count_units_in_tile(unit_size, ph);
+        PlaneRest &pr = out[plane];
+        pr.unit_size = unit_size;
+        pr.hunits = hunits;
+        pr.vunits = vunits;
+        size_t nunits = (size_t)hunits * vunits;
+        pr.rtype.assign(nunits, ZF_RESTORE_NONE);
+        pr.wiener.assign(nunits, default_wiener());
+        pr.frame_rtype = ZF_RESTORE_NONE;
+        if (plane > plane_end) continue;
+        const T *s = src[plane], *r = recon[plane];
+        int win = plane == 0 ? wn_luma : WIENER_WIN_CHROMA;
+        PixelRect rect{0, 0, pw, ph};
+        Padded<T> dgd(pw, ph, right_border(border_mode));
+        dgd.fill_from(r, pw);
+        extend_frame(dgd.data.data(), dgd.origin, pw, ph, dgd.stride, 4, 3);
+        Padded<T> trial(pw, ph, right_border(border_mode));
+        std::vector<i64> sse_none(nunits, 0), sse_wn(nunits, INT64_MAX);
+        std::vector<WienerInfo> wiener(nunits, default_wiener());
+        foreach_rest_unit_in_tile(rect, hunits, unit_size, ss, [&](const TileLimits &lim, int ui) {
+            sse_none[ui] = sse_region(s, (i64)lim.v_start * pw + lim.h_start, pw, r, (i64)lim.v_start * pw + lim.h_start,
+                                      pw, lim.h_end - lim.h_start, lim.v_end - lim.v_start);
+        });
+        foreach_rest_unit_in_tile(rect, hunits, unit_size, ss, [&](const TileLimits &lim, int ui) {
+            int win2 = win * win;
+            std::vector<i64> m(49, 0), hh((size_t)win2 * win2, 0);
+            compute_stats(win, dgd.data.data(), dgd.origin, dgd.stride, s, 0, pw, lim.h_start, lim.h_end,
+                          lim.v_start, lim.v_end, m.data(), hh.data(), bd);
+            i32 vd[WIENER_WIN] = {0}, hd[WIENER_WIN] = {0};
+            wiener_decompose_sep_sym(win, m.data(), hh.data(), vd, hd);
+            WienerInfo wi;
+            std::memset(&wi, 0, sizeof(wi));
+            finalize_sym_filter(win, vd, wi.vfilter);
+            finalize_sym_filter(win, hd, wi.hfilter);
+            i64 score = compute_score(win, m.data(), hh.data(), wi.vfilter, wi.hfilter);
+            if (score > 0) {
+                sse_wn[ui] = INT64_MAX;
+                return;
+            }
+            i64 e = finer_tile_search_wiener(c, dgd, trial, s, pw, lim, rect, ss, wi, win, bd);
+            sse_wn[ui] = e;
+            wiener[ui] = wi;
+        });
+        i64 sse_frame_none = 0;
+        for (size_t u = 0; u < nunits; ++u) sse_frame_none += sse_none[u];
+        double cost_none_frame = rdcost_dbl(rdmult, 0, sse_frame_none);
+        i64 bits_frame = 0, sse_frame = 0;
+        WienerInfo ref = default_wiener();
+        std::vector<u8> picks(nunits, ZF_RESTORE_NONE);
+        for (size_t u = 0; u < nunits; ++u) {
+            if (sse_wn[u] == INT64_MAX) {
+                bits_frame += RESTORE_COST[0];
+                sse_frame += sse_none[u];
+                continue;
+            }
+            i64 cnt = count_wiener_bits(win, wiener[u].vfilter, wiener[u].hfilter, ref.vfilter, ref.hfilter);
+            i64 bits_wn = RESTORE_COST[1] + (cnt << 9);
+            i64 bits_none = RESTORE_COST[0];
+            double cost_none = rdcost_dbl(rdmult, bits_none >> 4, sse_none[u]);
+            double cost_wn = rdcost_dbl(rdmult, bits_wn >> 4, sse_wn[u]);
+            if (cost_wn < cost_none) {
+                picks[u] = ZF_RESTORE_WIENER;
+                bits_frame += bits_wn;
+                sse_frame += sse_wn[u];
+                ref = wiener[u];
+            } else {
+                bits_frame += bits_none;
+                sse_frame += sse_none[u];
+            }
+        }
+        double cost_wn_frame = rdcost_dbl(rdmult, bits_frame >> 4, sse_frame);
+        pr.frame_rtype = cost_wn_frame < cost_none_frame ? ZF_RESTORE_WIENER : ZF_RESTORE_NONE;
+        for (size_t u = 0; u < nunits; ++u) {
+            pr.rtype[u] = pr.frame_rtype == ZF_RESTORE_WIENER ? picks[u] : (u8)ZF_RESTORE_NONE;
+            pr.wiener[u] = wiener[u];
+        }
+    }
+}
+
+// save_lr_boundaries (ENC/restoration.rs:938-977).
+template <typename T>
+static void save_lr_boundaries(const T *const pre[3], const T *const post[3], int w, int h, int stride_y,
+                               int stride_uv, bool has_chroma, StripeBoundaries<T> out[3]) {
+    for (int plane = 0; plane < 3; ++plane) {
+        bool is_uv = plane > 0;
+        int ss = is_uv ? 1 : 0;
+        int pw = is_uv ? (w + 1) / 2 : w, ph = is_uv ? (h + 1) / 2 : h;
+        int stride = is_uv ? stride_uv : stride_y;
+        out[plane] = alloc_stripe_boundaries<T>(w, h, ss);
+        if (is_uv && !has_chroma) continue;
+        save_tile_row_boundary_lines(pre[plane], stride, pw, ph, ss, false, out[plane]);
+        save_tile_row_boundary_lines(post[plane], stride, pw, ph, ss, true, out[plane]);
+    }
+}
+// apply_restoration_frame (ENC/restoration.rs:992-1052); the u16 instance
+// is new (the reference applies LR at 8 bits only) and uses the same walk.
+template <typename T>
+static void apply_restoration_frame(T *const recon[3], int w, int h, int stride_y, int stride_uv, bool has_chroma,
+                                    const PlaneRest info[3], const StripeBoundaries<T> bounds[3], int bd,
+                                    int border_mode) {
+    for (int plane = 0; plane < 3; ++plane) {
+        const PlaneRest &pr = info[plane];
+        if (pr.frame_rtype == ZF_RESTORE_NONE) continue;
+        bool is_uv = plane > 0;
+        if (is_uv && !has_chroma) continue;
+        int ss = is_uv ? 1 : 0;
+        int pw = is_uv ? (w + 1) / 2 : w, ph = is_uv ? (h + 1) / 2 : h;
+        int stride = is_uv ? stride_uv : stride_y;
+        Padded<T> data(pw, ph, right_border(border_mode));
+        data.fill_from(recon[plane], stride);
+        extend_frame(data.data.data(), data.origin, pw, ph, data.stride, 3, 3);
+        Padded<T> dst(pw, ph, right_border(border_mode));
+        PixelRect rect{0, 0, pw, ph};
+        foreach_rest_unit_in_tile(rect, pr.hunits, pr.unit_size, ss, [&](const TileLimits &lim, int ui) {
+            filter_unit<T>(true, lim, pr.rtype[ui], pr.wiener[ui], &bounds[plane], rect, ss, data.data.data(),
+                           data.origin, data.stride, dst.data.data(), dst.origin, dst.stride, bd);
+        });
+        dst.copy_to(recon[plane], stride);
+    }
+}
+
+// ===========================================================================
+// ABI glue
+// ===========================================================================
+
+static Geom make_geom(const zf_frame *f, const zfo_geom *g) {
+    Geom G;
+    G.mi_cols = g->mi_cols;
+    G.mi_rows = g->mi_rows;
+    G.true_w = f->true_width;
+    G.true_h = f->true_height;
+    G.block_id = g->block_id;
+    G.bw = g->bw;
+    G.bh = g->bh;
+    G.tw = g->tw;
+    G.th = g->th;
+    G.skip = g->skip;
+    G.skip_inter = g->skip_inter;
+    return G;
+}
+
+static int validate(const zf_frame *f) {
+    if (!f) return ZF_ERR_ARG;
+    if (f->bit_depth != 8 && f->bit_depth != 10) return ZF_ERR_UNSUPPORTED;
+    if (f->width <= 0 || f->height <= 0 || (f->width & 7) || (f->height & 7)) return ZF_ERR_INVALID_DIMS;
+    if (f->true_width <= 0 || f->true_height <= 0 || f->true_width > f->width || f->true_height > f->height)
+        return ZF_ERR_INVALID_DIMS;
+    if (f->qindex < 0 || f->qindex > 255 || f->preset < 0 || f->preset > 13 || f->sharpness < 0 || f->sharpness > 7)
+        return ZF_ERR_ARG;
+    return ZF_OK;
+}
+
+static void write_cdef(const CdefPick &p, int nhfb, int nvfb, zf_decisions *out) {
+    out->cdef_damping = (u8)p.damping;
+    out->cdef_bits = (u8)p.bits;
+    std::memset(out->cdef_y, 0, 8);
+    std::memset(out->cdef_uv, 0, 8);
+    for (size_t i = 0; i < p.strengths.size() && i < 8; ++i) {
+        out->cdef_y[i] = p.strengths[i].first;
+        out->cdef_uv[i] = p.strengths[i].second;
+    }
+    out->nhfb = nhfb;
+    out->nvfb = nvfb;
+    if (out->cdef_fb_idx) {
+        for (int i = 0; i < nhfb * nvfb; ++i) out->cdef_fb_idx[i] = p.bits ? p.fb_idx[i] : 0;
+    }
+}
+static CdefPick read_cdef(const zf_decisions *d, int nhfb) {
+    CdefPick p;
+    p.damping = d->cdef_damping;
+    p.bits = d->cdef_bits;
+    p.strengths.clear();
+    for (int i = 0; i < (1 << p.bits); ++i) p.strengths.push_back({d->cdef_y[i], d->cdef_uv[i]});
+    p.nhfb = nhfb;
+    if (p.bits) p.fb_idx.assign(d->cdef_fb_idx, d->cdef_fb_idx + (size_t)d->nhfb * d->nvfb);
+    return p;
+}
+static void write_lr(const PlaneRest pr[3], zf_decisions *out) {
+    for (int p = 0; p < 3; ++p) {
+        out->lr[p].frame_rtype = pr[p].frame_rtype;
+        out->lr[p].unit_size = pr[p].unit_size;
+        out->lr[p].hunits = pr[p].hunits;
+        out->lr[p].vunits = pr[p].vunits;
+        if (out->lr_units[p]) {
+            for (size_t u = 0; u < pr[p].rtype.size(); ++u) {
+                zf_lr_unit &o = out->lr_units[p][u];
+                std::memset(&o, 0, sizeof(o));
+                o.rtype = pr[p].rtype[u];
+                std::memcpy(o.vfilter, pr[p].wiener[u].vfilter, 16);
+                std::memcpy(o.hfilter, pr[p].wiener[u].hfilter, 16);
+            }
+        }
+    }
+}
+static void read_lr(const zf_decisions *d, PlaneRest pr[3]) {
+    for (int p = 0; p < 3; ++p) {
+        pr[p].frame_rtype = d->lr[p].frame_rtype;
+        pr[p].unit_size = d->lr[p].unit_size;
+        pr[p].hunits = d->lr[p].hunits;
+        pr[p].vunits = d->lr[p].vunits;
+        size_t n = (size_t)pr[p].hunits * pr[p].vunits;
+        pr[p].rtype.assign(n, ZF_RESTORE_NONE);
+        pr[p].wiener.assign(n, default_wiener());
+        if (d->lr_units[p] && pr[p].frame_rtype != ZF_RESTORE_NONE)
+            for (size_t u = 0; u < n; ++u) {
+                pr[p].rtype[u] = d->lr_units[p][u].rtype;
+                std::memcpy(pr[p].wiener[u].vfilter, d->lr_units[p][u].vfilter, 16);
+                std::memcpy(pr[p].wiener[u].hfilter, d->lr_units[p][u].hfilter, 16);
+            }
+    }
+}
+
+static bool lr_enabled(const zf_frame *f) {
+    return f->enable_restoration && wn_filter_ctrls_allintra(f->preset).enabled && f->true_width >= 64 &&
+           f->true_height >= 64;
+}
+static i64 lr_rdmult(const zf_frame *f) {
+    return f->bit_depth == 10 ? (i64)kf_full_lambda_bd10_pic(f->qindex) : (i64)kf_full_lambda_8bit_unweighted(f->qindex);
+}
+
+template <typename T> static int deblock_pick_t(const zf_frame *f, const Geom &g, u8 lf[4]) {
+    if (f->preset <= 5) {
+        const T *src[3] = {(const T *)f->src[0], (const T *)f->src[1], (const T *)f->src[2]};
+        const T *rec[3] = {(const T *)f->rec[0], (const T *)f->rec[1], (const T *)f->rec[2]};
+        pick_levels_full_search(src, rec, f->width, f->height, f->chroma_420 != 0, g, f->preset <= 3 ? 0 : 1,
+                                f->sharpness, f->bit_depth, lf);
+    } else {
+        key_frame_levels(f->qindex, f->bit_depth, lf);
+    }
+    return ZF_OK;
+}
+
+template <typename T> static void lr_search_t(const zf_frame *f, zf_decisions *out, int border_mode) {
+    PlaneRest pr[3];
+    int w = f->true_width, h = f->true_height;
+    int cw = (w + 1) / 2, ch = (h + 1) / 2;
+    bool has_chroma = f->chroma_420 != 0;
+    if (!lr_enabled(f)) {
+        for (int p = 0; p < 3; ++p) {
+            int pw = p ? cw : w, ph = p ? ch : h;
+            pr[p].hunits = count_units_in_tile(UNITSIZE_MAX, pw);
+            pr[p].vunits = count_units_in_tile(UNITSIZE_MAX, ph);
+            pr[p].rtype.assign((size_t)pr[p].hunits * pr[p].vunits, 0);
+            pr[p].wiener.assign(pr[p].rtype.size(), default_wiener());
+        }
+        write_lr(pr, out);
+        return;
+    }
+    // Tight true / ceil-chroma extraction (pipeline.rs:3280-3305).
+    std::vector<T> s[3], r[3];
+    for (int p = 0; p < 3; ++p) {
+        if (p > 0 && !has_chroma) break;
+        int pw = p ? cw : w, ph = p ? ch : h, st = p ? f->width / 2 : f->width;
+        s[p].resize((size_t)pw * ph);
+        r[p].resize((size_t)pw * ph);
+        for (int y = 0; y < ph; ++y) {
+            std::memcpy(&s[p][(size_t)y * pw], (const T *)f->src[p] + (size_t)y * st, sizeof(T) * pw);
+            std::memcpy(&r[p][(size_t)y * pw], (const T *)f->rec[p] + (size_t)y * st, sizeof(T) * pw);
+        }
+    }
+    const T *sp[3] = {s[0].data(), s[1].data(), s[2].data()};
+    const T *rp[3] = {r[0].data(), r[1].data(), r[2].data()};
+    search_restoration(wn_filter_ctrls_allintra(f->preset), sp, rp, w, h, has_chroma, lr_rdmult(f), f->bit_depth,
+                       border_mode, pr);
+    write_lr(pr, out);
+}
+
+template <typename T> static void lr_apply_t(const zf_frame *f, const void *const pre_cdef[3], const zf_decisions *d,
+                                             int border_mode) {
+    PlaneRest pr[3];
+    read_lr(d, pr);
+    bool any = false;
+    for (int p = 0; p < 3; ++p) any |= pr[p].frame_rtype != ZF_RESTORE_NONE;
+    if (!any) return;
+    const T *pre[3] = {(const T *)pre_cdef[0], (const T *)pre_cdef[1], (const T *)pre_cdef[2]};
+    const T *post[3] = {(const T *)f->rec[0], (const T *)f->rec[1], (const T *)f->rec[2]};
+    StripeBoundaries<T> b[3];
+    save_lr_boundaries(pre, post, f->true_width, f->true_height, f->width, f->width / 2, f->chroma_420 != 0, b);
+    T *rec[3] = {(T *)f->rec[0], (T *)f->rec[1], (T *)f->rec[2]};
+    apply_restoration_frame(rec, f->true_width, f->true_height, f->width, f->width / 2, f->chroma_420 != 0, pr, b,
+                            f->bit_depth, border_mode);
+}
+
+template <typename T>
+static int filter_stage_t(const zf_frame *f, const Geom &g, zf_decisions *out, zf_stats *st, int border_mode) {
+    int w = f->width, h = f->height;
+    bool chroma = f->chroma_420 != 0;
+    T *rec[3] = {(T *)f->rec[0], (T *)f->rec[1], (T *)f->rec[2]};
+    const T *crec[3] = {rec[0], rec[1], rec[2]};
+    const T *src[3] = {(const T *)f->src[0], (const T *)f->src[1], (const T *)f->src[2]};
+    // Deblock pick + apply (pipeline.rs:2886-3010).
+    u8 lf[4];
+    deblock_pick_t<T>(f, g, lf);
+    std::memcpy(out->lf, lf, 4);
+    apply_deblock_frame(rec[0], rec[1], rec[2], w, h, chroma, g, lf, f->sharpness, f->bit_depth);
+    // CDEF pick (pipeline.rs:3042-3144) + pre-CDEF snapshot + apply.
+    CdefPick p = cdef_pick(crec, src, w, h, chroma, g, f->preset, f->qindex, f->bit_depth, f->sc_class5 != 0,
+                           nullptr, nullptr, nullptr);
+    int nhfb = (w + 63) / 64, nvfb = (h + 63) / 64;
+    write_cdef(p, nhfb, nvfb, out);
+    if (st) {
+        int cnt = 0;
+        for (int fbr = 0; fbr < nvfb; ++fbr)
+            for (int fbc = 0; fbc < nhfb; ++fbc) {
+                bool any = false;
+                for (int by = 0; by < std::min(64, h - fbr * 64) / 8 && !any; ++by)
+                    for (int bx = 0; bx < std::min(64, w - fbc * 64) / 8 && !any; ++bx)
+                        any = !g.is_8x8_all_skip(fbr * 16 + by * 2, fbc * 16 + bx * 2);
+                cnt += any;
+            }
+        st->cdef_sb_count = cnt;
+    }
+    std::vector<T> pre[3];
+    for (int pl = 0; pl < 3; ++pl) {
+        if (pl > 0 && !chroma) break;
+        size_t n = pl ? (size_t)(w / 2) * (h / 2) : (size_t)w * h;
+        pre[pl].assign(rec[pl], rec[pl] + n);
+    }
+    apply_cdef_frame(rec[0], rec[1], rec[2], w, h, chroma, g, p, f->bit_depth, st);
+    // Wiener LR (pipeline.rs:3236-3455).
+    lr_search_t<T>(f, out, border_mode);
+    const void *prev[3] = {pre[0].data(), chroma ? pre[1].data() : nullptr, chroma ? pre[2].data() : nullptr};
+    lr_apply_t<T>(f, prev, out, border_mode);
+    if (st) {
+        st->lr_wiener_units = 0;
+        for (int pl = 0; pl < 3; ++pl) {
+            st->lr_frame_rtype[pl] = out->lr[pl].frame_rtype;
+            if (out->lr_units[pl] && out->lr[pl].frame_rtype != ZF_RESTORE_NONE)
+                for (int u = 0; u < out->lr[pl].hunits * out->lr[pl].vunits; ++u)
+                    st->lr_wiener_units += out->lr_units[pl][u].rtype == ZF_RESTORE_WIENER;
+        }
+    }
+    return ZF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t zfo_filter_stage(const zf_frame *f, const zfo_geom *g, zf_decisions *out, zf_stats *stats,
+                         int32_t lr_border_mode) {
+    int e = validate(f);
+    if (e) return e;
+    if (!g || !out) return ZF_ERR_ARG;
+    Geom G = make_geom(f, g);
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    if (f->bit_depth == 8) return filter_stage_t<u8>(f, G, out, stats, lr_border_mode);
+    return filter_stage_t<u16>(f, G, out, stats, lr_border_mode);
+}
+
+int32_t zfo_deblock_pick(const zf_frame *f, const zfo_geom *g, uint8_t lf[4]) {
+    int e = validate(f);
+    if (e) return e;
+    Geom G = make_geom(f, g);
+    return f->bit_depth == 8 ? deblock_pick_t<u8>(f, G, lf) : deblock_pick_t<u16>(f, G, lf);
+}
+
+int32_t zfo_deblock_apply(const zf_frame *f, const zfo_geom *g, const uint8_t lf[4]) {
+    int e = validate(f);
+    if (e) return e;
+    Geom G = make_geom(f, g);
+    if (f->bit_depth == 8)
+        apply_deblock_frame((u8 *)f->rec[0], (u8 *)f->rec[1], (u8 *)f->rec[2], f->width, f->height,
+                            f->chroma_420 != 0, G, lf, f->sharpness, 8);
+    else
+        apply_deblock_frame((u16 *)f->rec[0], (u16 *)f->rec[1], (u16 *)f->rec[2], f->width, f->height,
+                            f->chroma_420 != 0, G, lf, f->sharpness, f->bit_depth);
+    return ZF_OK;
+}
+
+int32_t zfo_cdef_search(const zf_frame *f, const zfo_geom *g, zf_decisions *out, uint64_t *mse_out,
+                        uint8_t *fb_has_row, int32_t *ncand_out) {
+    int e = validate(f);
+    if (e) return e;
+    Geom G = make_geom(f, g);
+    int nhfb = (f->width + 63) / 64, nvfb = (f->height + 63) / 64;
+    CdefPick p;
+    int nc = 0;
+    if (f->bit_depth == 8) {
+        const u8 *rec[3] = {(const u8 *)f->rec[0], (const u8 *)f->rec[1], (const u8 *)f->rec[2]};
+        const u8 *src[3] = {(const u8 *)f->src[0], (const u8 *)f->src[1], (const u8 *)f->src[2]};
+        p = cdef_pick(rec, src, f->width, f->height, f->chroma_420 != 0, G, f->preset, f->qindex, 8,
+                      f->sc_class5 != 0, mse_out, fb_has_row, &nc);
+    } else {
+        const u16 *rec[3] = {(const u16 *)f->rec[0], (const u16 *)f->rec[1], (const u16 *)f->rec[2]};
+        const u16 *src[3] = {(const u16 *)f->src[0], (const u16 *)f->src[1], (const u16 *)f->src[2]};
+        p = cdef_pick(rec, src, f->width, f->height, f->chroma_420 != 0, G, f->preset, f->qindex, f->bit_depth,
+                      f->sc_class5 != 0, mse_out, fb_has_row, &nc);
+    }
+    if (ncand_out) *ncand_out = nc;
+    write_cdef(p, nhfb, nvfb, out);
+    return ZF_OK;
+}
+
+int32_t zfo_cdef_apply(const zf_frame *f, const zfo_geom *g, const zf_decisions *d, zf_stats *stats) {
+    int e = validate(f);
+    if (e) return e;
+    Geom G = make_geom(f, g);
+    int nhfb = (f->width + 63) / 64;
+    CdefPick p = read_cdef(d, nhfb);
+    if (f->bit_depth == 8)
+        apply_cdef_frame((u8 *)f->rec[0], (u8 *)f->rec[1], (u8 *)f->rec[2], f->width, f->height, f->chroma_420 != 0,
+                         G, p, 8, stats);
+    else
+        apply_cdef_frame((u16 *)f->rec[0], (u16 *)f->rec[1], (u16 *)f->rec[2], f->width, f->height,
+                         f->chroma_420 != 0, G, p, f->bit_depth, stats);
+    return ZF_OK;
+}
+
+int32_t zfo_lr_search(const zf_frame *f, zf_decisions *out, int32_t lr_border_mode) {
+    int e = validate(f);
+    if (e) return e;
+    if (f->bit_depth == 8)
+        lr_search_t<u8>(f, out, lr_border_mode);
+    else
+        lr_search_t<u16>(f, out, lr_border_mode);
+    return ZF_OK;
+}
+
+int32_t zfo_lr_apply(const zf_frame *f, const void *const pre_cdef[3], const zf_decisions *d,
+                     int32_t lr_border_mode) {
+    int e = validate(f);
+    if (e) return e;
+    if (f->bit_depth == 8)
+        lr_apply_t<u8>(f, pre_cdef, d, lr_border_mode);
+    else
+        lr_apply_t<u16>(f, pre_cdef, d, lr_border_mode);
+    return ZF_OK;
+}
+
+void zfo_lf_thresholds(int32_t level, int32_t sharpness, int32_t out[3]) {
+    LfThresh t = lf_thresholds(level, sharpness);
+    out[0] = t.mblim;
+    out[1] = t.lim;
+    out[2] = t.hev_thr;
+}
+
+void zfo_lpf(void *buf, int32_t bd, int32_t off, int32_t pitch, int32_t vert, int32_t len, int32_t level,
+             int32_t sharpness) {
+    LfThresh t = lf_thresholds(level, sharpness);
+    if (bd == 8)
+        lpf_u8((u8 *)buf, off, pitch, vert != 0, len, t);
+    else
+        lpf_u16((u16 *)buf, off, pitch, vert != 0, len, t, bd);
+}
+
+void zfo_cdef_find_dir(const uint16_t *img, int32_t stride, int32_t coeff_shift, int32_t *dir, int32_t *var) {
+    int d, v;
+    cdef_find_dir(img, stride, coeff_shift, &d, &v);
+    *dir = d;
+    *var = v;
+}
+
+void zfo_cdef_filter_block(void *dst, int32_t dst_is_u16, int32_t doff, int32_t dstride, const uint16_t *inb,
+                           int32_t ioff, int32_t pri, int32_t sec, int32_t dir, int32_t pri_damping,
+                           int32_t sec_damping, int32_t bsize, int32_t coeff_shift, int32_t sub) {
+    if (dst_is_u16)
+        cdef_filter_block((u16 *)dst, doff, dstride, inb, ioff, pri, sec, dir, pri_damping, sec_damping, bsize,
+                          coeff_shift, sub);
+    else
+        cdef_filter_block((u8 *)dst, doff, dstride, inb, ioff, pri, sec, dir, pri_damping, sec_damping, bsize,
+                          coeff_shift, sub);
+}
+
+int32_t zfo_adjust_strength(int32_t strength, int32_t var) { return adjust_strength(strength, var); }
+
+int32_t zfo_cdef_finish_rd(const uint64_t *mse, int32_t n_fb, int32_t n_cand, int32_t qindex, int32_t bit_depth,
+                           int32_t *lev0, int32_t *lev1) {
+    std::vector<MseRow> rows((size_t)n_fb);
+    for (int i = 0; i < n_fb; ++i) rows[i].assign(mse + (size_t)i * 2 * n_cand, mse + (size_t)(i + 1) * 2 * n_cand);
+    std::vector<int> l0, l1;
+    int bits = finish_cdef_rd(rows, n_cand, qindex, bit_depth, l0, l1);
+    for (size_t i = 0; i < l0.size(); ++i) {
+        lev0[i] = l0[i];
+        lev1[i] = l1[i];
+    }
+    return bits;
+}
+
+void zfo_cdef_qp_params(int32_t qindex, int32_t bit_depth, int32_t screen, int32_t out[3]) {
+    int o[3];
+    cdef_qp_params(qindex, bit_depth, screen != 0, o);
+    out[0] = o[0];
+    out[1] = o[1];
+    out[2] = o[2];
+}
+
+void zfo_deblock_key_frame_levels(int32_t qindex, int32_t bit_depth, uint8_t out[4]) {
+    key_frame_levels(qindex, bit_depth, out);
+}
+
+int32_t zfo_dlf_hillclimb_replay(const int64_t *errs, int32_t conv_th, int32_t *tried, int32_t *n_tries) {
+    int n = 0;
+    int lvl = search_filter_level(
+        [&](int l) -> i64 {
+            tried[n++] = l;
+            return errs[l];
+        },
+        conv_th);
+    *n_tries = n;
+    return lvl;
+}
+
+uint32_t zfo_lambda(int32_t which, int32_t qindex) {
+    switch (which) {
+        case 0: return kf_full_lambda_8bit_unweighted(qindex);
+        case 1: return kf_full_lambda_bd10_unweighted(qindex);
+        default: return kf_full_lambda_bd10_pic(qindex);
+    }
+}
+
+void zfo_compute_stats(int32_t win, const void *dgd, int64_t dgd_origin, int32_t dgd_stride, const void *src,
+                       int64_t src_origin, int32_t src_stride, int32_t h_start, int32_t h_end, int32_t v_start,
+                       int32_t v_end, int64_t *m, int64_t *h, int32_t bd) {
+    if (bd == 8)
+        compute_stats(win, (const u8 *)dgd, dgd_origin, dgd_stride, (const u8 *)src, src_origin, src_stride, h_start,
+                      h_end, v_start, v_end, m, h, 8);
+    else
+        compute_stats(win, (const u16 *)dgd, dgd_origin, dgd_stride, (const u16 *)src, src_origin, src_stride,
+                      h_start, h_end, v_start, v_end, m, h, bd);
+}
+
+int64_t zfo_wiener_solve(int32_t win, const int64_t *m, const int64_t *h, int32_t vd[7], int32_t hd[7],
+                         int16_t vf[8], int16_t hf[8]) {
+    i32 a[7] = {0}, b[7] = {0};
+    wiener_decompose_sep_sym(win, m, h, a, b);
+    for (int i = 0; i < 7; ++i) {
+        vd[i] = a[i];
+        hd[i] = b[i];
+    }
+    std::memset(vf, 0, 16);
+    std::memset(hf, 0, 16);
+    finalize_sym_filter(win, a, vf);
+    finalize_sym_filter(win, b, hf);
+    return compute_score(win, m, h, vf, hf);
+}
+
+int32_t zfo_count_wiener_bits(int32_t win, const int16_t vf[8], const int16_t hf[8], const int16_t rvf[8],
+                              const int16_t rhf[8]) {
+    return count_wiener_bits(win, vf, hf, rvf, rhf);
+}
+
+int32_t zfo_count_units_in_tile(int32_t unit_size, int32_t tile_size) {
+    return count_units_in_tile(unit_size, tile_size);
+}
+
+double zfo_rdcost_dbl(int64_t rdmult, int64_t rate, int64_t dist) { return rdcost_dbl(rdmult, rate, dist); }
+
+void zfo_wiener_convolve(const void *src, int64_t src_origin, int32_t src_stride, void *dst, int64_t dst_origin,
+                         int32_t dst_stride, const int16_t hf[8], const int16_t vf[8], int32_t w, int32_t h,
+                         int32_t bd) {
+    if (bd == 8)
+        wiener_convolve_add_src((const u8 *)src, src_origin, src_stride, (u8 *)dst, dst_origin, dst_stride, hf, vf, w,
+                                h, 8);
+    else
+        wiener_convolve_add_src((const u16 *)src, src_origin, src_stride, (u16 *)dst, dst_origin, dst_stride, hf, vf,
+                                w, h, bd);
+}
+
+int64_t zfo_sse_region(const void *a, int32_t a_stride, const void *b, int32_t b_stride, int32_t w, int32_t h,
+                       int32_t bd) {
+    if (bd == 8) return sse_region((const u8 *)a, 0, a_stride, (const u8 *)b, 0, b_stride, w, h);
+    return sse_region((const u16 *)a, 0, a_stride, (const u16 *)b, 0, b_stride, w, h);
+}
+
+}  // extern "C"

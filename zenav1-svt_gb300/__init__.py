@@ -1,0 +1,209 @@
+"""GB300 in-loop filter stage for the zenav1-svt AV1 still-image encoder.
+
+Python binding of the C ABI in include/zf_filter.h (libzf.so, built by
+build.py). The functions mirror the reference encoder's filter-stage entry
+points (rust/crates/svtav1-encoder/src/{deblock,cdef,restoration}.rs) with
+the same argument meaning and the same error behaviour (the EncodeError
+variants surface as ZfError with the reference's variant name):
+
+  pick_filter_levels        deblock::pick_filter_levels_full_search /
+                            pick_filter_levels_key_frame      (deblock.rs:481, :55)
+  apply_deblock_frame       deblock::apply_deblock_frame[_hbd] (deblock.rs:938, :976)
+  cdef_search_still         the CDEF pick of pipeline.rs:3042-3144
+  apply_cdef_frame          cdef::apply_cdef_frame[_hbd]      (cdef.rs:343, :556)
+  search_restoration_still  restoration::search_restoration_still[_bd]
+  apply_restoration_frame   restoration::save_lr_boundaries +
+                            apply_restoration_frame           (restoration.rs:938, :992)
+  filter_stage              the whole stage (pipeline.rs:2886-3455)
+  submit_batch              many frames, one launch per pass
+
+There is no CPU fallback: every call runs the CUDA kernels, and loading
+fails loudly when the library has not been built.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import Decisions, ZfDecisions, ZfFrame, ZfOpts, ZfSizes, ZfStats
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libzf.so")
+
+_lib = None
+
+
+class ZfError(RuntimeError):
+    def __init__(self, code, msg=""):
+        self.code = code
+        self.kind = abi.ERRORS.get(code, "Unknown")
+        super().__init__("%s (%d): %s" % (self.kind, code, msg))
+
+
+def lib():
+    """Load libzf.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libzf.so is not built (%s); run __graft_entry__.build() or "
+                           "python zenav1-svt_gb300/build.py" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    L.zf_abi_version.restype = C.c_int32
+    L.zf_create.argtypes = [P(C.c_void_p), P(ZfOpts)]
+    L.zf_destroy.argtypes = [C.c_void_p]
+    L.zf_destroy.restype = None
+    L.zf_last_error.argtypes = [C.c_void_p]
+    L.zf_last_error.restype = C.c_char_p
+    L.zf_sync.argtypes = [C.c_void_p]
+    L.zf_query_sizes.argtypes = [P(ZfFrame), P(ZfSizes)]
+    L.zf_pack_geom.argtypes = [C.c_int32, C.c_int32] + [C.c_void_p] * 8
+    L.zf_filter_stage.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions), P(ZfStats)]
+    L.zf_submit_batch.argtypes = [C.c_void_p, P(ZfFrame), C.c_int32, P(ZfDecisions), P(ZfStats)]
+    L.zf_deblock_pick.argtypes = [C.c_void_p, P(ZfFrame), P(C.c_uint8)]
+    L.zf_deblock_apply.argtypes = [C.c_void_p, P(ZfFrame), P(C.c_uint8)]
+    L.zf_cdef_search.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions)]
+    L.zf_cdef_apply.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions), P(ZfStats)]
+    L.zf_lr_search.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions)]
+    L.zf_lr_apply.argtypes = [C.c_void_p, P(ZfFrame), P(C.c_void_p), P(ZfDecisions)]
+    for name in ("zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
+                 "zf_submit_batch", "zf_deblock_pick", "zf_deblock_apply", "zf_cdef_search",
+                 "zf_cdef_apply", "zf_lr_search", "zf_lr_apply"):
+        getattr(L, name).restype = C.c_int32
+    _lib = L
+    return L
+
+
+def pack_geom(geom):
+    """DeblockGeom arrays -> packed uint32 mi records (zf_pack_geom)."""
+    arrs = geom.arrays()
+    out = np.zeros(geom.mi_rows * geom.mi_cols, np.uint32)
+    rc = lib().zf_pack_geom(geom.mi_cols, geom.mi_rows, *[a.ctypes.data for a in arrs], out.ctypes.data)
+    if rc != 0:
+        raise ZfError(rc, "geometry is not an aligned AV1 block/transform tiling")
+    return out
+
+
+def stats_dict(s):
+    return {"cdef_filtered_px": s.cdef_filtered_px, "cdef_changed_px": s.cdef_changed_px,
+            "cdef_sb_count": s.cdef_sb_count, "lr_wiener_units": s.lr_wiener_units,
+            "lr_frame_rtype": list(s.lr_frame_rtype)}
+
+
+class Context:
+    """One CUDA stream + device arena (zf_create); not thread-safe."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0, cancel_flag=None):
+        L = lib()
+        self._cancel = cancel_flag
+        opts = ZfOpts()
+        opts.device = device
+        opts.hbm_budget_bytes = hbm_budget_bytes
+        if cancel_flag is not None:
+            opts.cancel_flag = C.cast(cancel_flag, C.POINTER(C.c_int32))
+        h = C.c_void_p()
+        rc = L.zf_create(C.byref(h), C.byref(opts))
+        if rc != 0:
+            raise ZfError(rc, "zf_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().zf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise ZfError(rc, lib().zf_last_error(self.h).decode())
+
+    def sync(self):
+        self._check(lib().zf_sync(self.h))
+
+    # -- whole stage --------------------------------------------------------
+    def filter_stage(self, fr, mi=None, rec=None):
+        """Run the whole stage on a synth.Frame. Returns (decisions dict,
+        stats dict, filtered planes)."""
+        mi = pack_geom(fr.geom) if mi is None else mi
+        rec = fr.copy_rec() if rec is None else rec
+        s = abi.make_frame_struct(fr, fr.src, rec, mi)
+        d = Decisions(fr.w, fr.h, fr.true_w, fr.true_h)
+        st = ZfStats()
+        self._check(lib().zf_filter_stage(self.h, C.byref(s), C.byref(d.c), C.byref(st)))
+        return d.as_dict(), stats_dict(st), rec
+
+    def submit_batch(self, frames, mis=None, recs=None):
+        n = len(frames)
+        mis = [pack_geom(f.geom) for f in frames] if mis is None else mis
+        recs = [f.copy_rec() for f in frames] if recs is None else recs
+        arr = (ZfFrame * n)()
+        decs = [Decisions(f.w, f.h, f.true_w, f.true_h) for f in frames]
+        darr = (ZfDecisions * n)()
+        for i, f in enumerate(frames):
+            arr[i] = abi.make_frame_struct(f, f.src, recs[i], mis[i])
+            darr[i] = decs[i].c
+        st = (ZfStats * n)()
+        self._check(lib().zf_submit_batch(self.h, arr, n, darr, st))
+        out = []
+        for i in range(n):
+            decs[i].c = darr[i]
+            out.append((decs[i].as_dict(), stats_dict(st[i]), recs[i]))
+        return out
+
+    # -- per call site ------------------------------------------------------
+    def pick_filter_levels(self, fr, rec, mi=None):
+        mi = pack_geom(fr.geom) if mi is None else mi
+        s = abi.make_frame_struct(fr, fr.src, rec, mi)
+        lf = (C.c_uint8 * 4)()
+        self._check(lib().zf_deblock_pick(self.h, C.byref(s), lf))
+        return list(lf)
+
+    def apply_deblock_frame(self, fr, rec, lf, mi=None):
+        mi = pack_geom(fr.geom) if mi is None else mi
+        s = abi.make_frame_struct(fr, fr.src, rec, mi)
+        lv = (C.c_uint8 * 4)(*lf)
+        self._check(lib().zf_deblock_apply(self.h, C.byref(s), lv))
+
+    def cdef_search_still(self, fr, rec, mi=None):
+        mi = pack_geom(fr.geom) if mi is None else mi
+        s = abi.make_frame_struct(fr, fr.src, rec, mi)
+        d = Decisions(fr.w, fr.h, fr.true_w, fr.true_h)
+        self._check(lib().zf_cdef_search(self.h, C.byref(s), C.byref(d.c)))
+        return d
+
+    def apply_cdef_frame(self, fr, rec, dec, mi=None):
+        mi = pack_geom(fr.geom) if mi is None else mi
+        s = abi.make_frame_struct(fr, fr.src, rec, mi)
+        st = ZfStats()
+        self._check(lib().zf_cdef_apply(self.h, C.byref(s), C.byref(dec.c), C.byref(st)))
+        return stats_dict(st)
+
+    def search_restoration_still(self, fr, rec, mi=None):
+        mi = pack_geom(fr.geom) if mi is None else mi
+        s = abi.make_frame_struct(fr, fr.src, rec, mi)
+        d = Decisions(fr.w, fr.h, fr.true_w, fr.true_h)
+        self._check(lib().zf_lr_search(self.h, C.byref(s), C.byref(d.c)))
+        return d
+
+    def apply_restoration_frame(self, fr, rec, pre_cdef, dec, mi=None):
+        mi = pack_geom(fr.geom) if mi is None else mi
+        s = abi.make_frame_struct(fr, fr.src, rec, mi)
+        pre = (C.c_void_p * 3)(*[p.ctypes.data for p in pre_cdef])
+        self._check(lib().zf_lr_apply(self.h, C.byref(s), pre, C.byref(dec.c)))
+
+
+def query_sizes(fr, mi=None):
+    mi = pack_geom(fr.geom) if mi is None else mi
+    s = abi.make_frame_struct(fr, fr.src, fr.rec, mi)
+    z = ZfSizes()
+    rc = lib().zf_query_sizes(C.byref(s), C.byref(z))
+    if rc != 0:
+        raise ZfError(rc, "zf_query_sizes")
+    return z

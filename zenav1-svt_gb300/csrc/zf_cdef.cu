@@ -1,0 +1,558 @@
+// zf_cdef.cu -- CDEF strength search and apply on the GPU.
+//
+// Reference: svtav1-dsp/src/cdef.rs (find_dir :143-198, constrain :113,
+// adjust_strength :125, the scalar block filter :931-1034 and its dst16
+// twin hbd.rs:1765-1850) and svtav1-encoder/src/cdef.rs (search
+// :1166-1568, finish :812-944, apply :343-708).
+//
+// The CDEF working buffer of the reference is a per-64x64 copy of the
+// post-deblock plane with CDEF_VERY_LARGE (0x7f7f) outside the aligned
+// canvas. Here a CTA owns one 64x64 filter block and stages exactly that
+// (plus the 2-pixel reach of the taps) in shared memory, so every pixel of
+// every candidate reads the same values as the reference's build_src.
+#include "zf_dev.cuh"
+
+namespace zf {
+
+constexpr uint16_t kVeryLarge = 0x7f7f;
+constexpr int CR = 68;  // luma region edge: 64 + 2 * 2 halo
+constexpr int CRC = 36; // chroma region edge: 32 + 2 * 2
+
+// Cdef_Directions (AV1 spec 7.15.3) as (dy, dx).
+__constant__ int8_t kDir[8][2][2] = {
+    {{-1, 1}, {-2, 2}}, {{0, 1}, {-1, 2}}, {{0, 1}, {0, 2}}, {{0, 1}, {1, 2}},
+    {{1, 1}, {2, 2}},   {{1, 0}, {2, 1}},  {{1, 0}, {2, 0}}, {{1, 0}, {2, -1}},
+};
+
+__device__ __forceinline__ int msb(unsigned v) { return 31 - __clz(v); }
+
+// constrain (cdef.rs:113-120).
+__device__ __forceinline__ int constrain(int diff, int threshold, int damping) {
+    if (threshold == 0) return 0;
+    int shift = max(0, damping - msb((unsigned)threshold));
+    int ad = abs(diff);
+    int v = min(ad, max(0, threshold - (ad >> shift)));
+    return diff < 0 ? -v : v;
+}
+
+// adjust_strength (cdef.rs:125-136).
+__device__ __forceinline__ int adjust_strength(int strength, int var) {
+    int i = (var >> 6) != 0 ? min(msb((unsigned)(var >> 6)), 12) : 0;
+    return var != 0 ? (strength * (4 + i) + 8) >> 4 : 0;
+}
+
+// cdef_find_dir (cdef.rs:143-198) on an 8x8 block at `img` (stride rs).
+__device__ void find_dir(const uint16_t *img, int rs, int coeff_shift, int *odir, int *ovar) {
+    int cost[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int partial[8][15];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 15; ++b) partial[a][b] = 0;
+    const int div[9] = {0, 840, 420, 280, 210, 168, 140, 120, 105};
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            int x = ((int)img[i * rs + j] >> coeff_shift) - 128;
+            partial[0][i + j] += x;
+            partial[1][i + j / 2] += x;
+            partial[2][i] += x;
+            partial[3][3 + i - j / 2] += x;
+            partial[4][7 + i - j] += x;
+            partial[5][3 - i / 2 + j] += x;
+            partial[6][j] += x;
+            partial[7][i / 2 + j] += x;
+        }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        cost[2] += partial[2][i] * partial[2][i];
+        cost[6] += partial[6][i] * partial[6][i];
+    }
+    cost[2] *= div[8];
+    cost[6] *= div[8];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        cost[0] += (partial[0][i] * partial[0][i] + partial[0][14 - i] * partial[0][14 - i]) * div[i + 1];
+        cost[4] += (partial[4][i] * partial[4][i] + partial[4][14 - i] * partial[4][14 - i]) * div[i + 1];
+    }
+    cost[0] += partial[0][7] * partial[0][7] * div[8];
+    cost[4] += partial[4][7] * partial[4][7] * div[8];
+#pragma unroll
+    for (int i = 1; i < 8; i += 2) {
+#pragma unroll
+        for (int j = 0; j < 5; ++j) cost[i] += partial[i][3 + j] * partial[i][3 + j];
+        cost[i] *= div[8];
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            cost[i] += (partial[i][j] * partial[i][j] + partial[i][10 - j] * partial[i][10 - j]) * div[2 * j + 2];
+    }
+    int best_cost = 0, best_dir = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+        if (cost[i] > best_cost) {
+            best_cost = cost[i];
+            best_dir = i;
+        }
+    *odir = best_dir;
+    *ovar = (best_cost - cost[(best_dir + 4) & 7]) >> 10;
+}
+
+// One output pixel of svt_cdef_filter_block_c: wrapping int16 tap sum,
+// taps read as int16, the sentinel excluded from max only.
+__device__ __forceinline__ int cdef_px(const uint16_t *reg, int rs, int pos, int pri, int sec, int dir, int pdamp,
+                                       int sdamp, int coeff_shift) {
+    const int ptap0 = ((pri >> coeff_shift) & 1) ? 3 : 4, ptap1 = ((pri >> coeff_shift) & 1) ? 3 : 2;
+    const int x = (int16_t)reg[pos];
+    int16_t sum = 0;
+    int mx = x, mn = x;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int ptap = k ? ptap1 : ptap0, stap = k ? 1 : 2;
+        const int od = kDir[dir][k][0] * rs + kDir[dir][k][1];
+        const int o2 = kDir[(dir + 2) & 7][k][0] * rs + kDir[(dir + 2) & 7][k][1];
+        const int o6 = kDir[(dir + 6) & 7][k][0] * rs + kDir[(dir + 6) & 7][k][1];
+        const uint16_t r0 = reg[pos + od], r1 = reg[pos - od];
+        const int p0 = (int16_t)r0, p1 = (int16_t)r1;
+        sum = (int16_t)(sum + (int16_t)(ptap * constrain(p0 - x, pri, pdamp)));
+        sum = (int16_t)(sum + (int16_t)(ptap * constrain(p1 - x, pri, pdamp)));
+        if (r0 != kVeryLarge) mx = max(p0, mx);
+        if (r1 != kVeryLarge) mx = max(p1, mx);
+        mn = min(p0, mn);
+        mn = min(p1, mn);
+        const uint16_t t0 = reg[pos + o2], t1 = reg[pos - o2], t2 = reg[pos + o6], t3 = reg[pos - o6];
+        const int s0 = (int16_t)t0, s1 = (int16_t)t1, s2 = (int16_t)t2, s3 = (int16_t)t3;
+        if (t0 != kVeryLarge) mx = max(s0, mx);
+        if (t1 != kVeryLarge) mx = max(s1, mx);
+        if (t2 != kVeryLarge) mx = max(s2, mx);
+        if (t3 != kVeryLarge) mx = max(s3, mx);
+        mn = min(s0, mn);
+        mn = min(s1, mn);
+        mn = min(s2, mn);
+        mn = min(s3, mn);
+        sum = (int16_t)(sum + (int16_t)(stap * constrain(s0 - x, sec, sdamp)));
+        sum = (int16_t)(sum + (int16_t)(stap * constrain(s1 - x, sec, sdamp)));
+        sum = (int16_t)(sum + (int16_t)(stap * constrain(s2 - x, sec, sdamp)));
+        sum = (int16_t)(sum + (int16_t)(stap * constrain(s3 - x, sec, sdamp)));
+    }
+    const int y = x + ((8 + (int)sum - (int)(sum < 0)) >> 4);
+    return min(max(y, mn), mx);
+}
+
+// Stage a plane window [y0-2, y0+n+2) x [x0-2, x0+n+2) with the sentinel
+// outside the aligned plane (build_src, cdef.rs:517-544).
+__device__ void load_region(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n, uint16_t *reg) {
+    const int rs = n + 4;
+    for (int i = threadIdx.x; i < rs * rs; i += blockDim.x) {
+        int ry = i / rs, rx = i - ry * rs;
+        int y = y0 - 2 + ry, x = x0 - 2 + rx;
+        reg[i] = (x >= 0 && x < pw && y >= 0 && y < ph) ? (uint16_t)ldpx(plane, (int64_t)y * pw + x, bd) : kVeryLarge;
+    }
+}
+
+// Non-skip 8x8 blocks of one filter block (the dlist, cdef.rs:1203-1213):
+// bit (by*8+bx) of the returned mask; blocks past a partial fb are 0.
+__device__ uint64_t fb_dlist(const FrameDesc &f, int fbr, int fbc) {
+    const int vsize = min(64, f.h - fbr * 64), hsize = min(64, f.w - fbc * 64);
+    uint64_t m = 0;
+    for (int by = 0; by < vsize / 8; ++by)
+        for (int bx = 0; bx < hsize / 8; ++bx) {
+            const int r = fbr * 16 + by * 2, c = fbc * 16 + bx * 2;
+            bool all = true;
+            for (int rr = r; rr < min(r + 2, f.mi_rows); ++rr)
+                for (int cc = c; cc < min(c + 2, f.mi_cols); ++cc)
+                    all = all && mi_skip(f.mi[(int64_t)rr * f.mi_cols + cc]);
+            if (!all) m |= 1ull << (by * 8 + bx);
+        }
+    return m;
+}
+
+__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v, unsigned long long *scratch) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+    __syncthreads();
+    unsigned long long s = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += scratch[w];
+    return s;  // valid in thread 0
+}
+
+// Search: one CTA per filter block. Writes the fb's luma and joint-chroma
+// mse rows (cdef_search_still[_hbd]) and whether the fb has a row.
+__global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, const WorkItem *items, int nitems) {
+    __shared__ uint16_t reg[CR * CR];
+    __shared__ uint16_t src[64 * 64];
+    __shared__ int sdir[64], svar[64];
+    __shared__ unsigned long long red[8];
+    __shared__ int blist[64];
+    __shared__ int nblk;
+    const int it = find_item(items, nitems, blockIdx.x);
+    const WorkItem wi = items[it];
+    const FrameDesc &f = frames[wi.frame];
+    const CdefParams &cp = f.cdef;
+    const int fb = blockIdx.x - wi.cta_begin;
+    const int fbr = fb / f.nhfb, fbc = fb - fbr * f.nhfb;
+    const int bd = f.bd, cs = bd - 8;
+    const uint64_t dl = fb_dlist(f, fbr, fbc);
+    if (threadIdx.x == 0) {
+        f.fb_row[fb] = dl != 0;
+        int n = 0;
+        for (int b = 0; b < 64; ++b)
+            if ((dl >> b) & 1) blist[n++] = b;
+        nblk = n;
+    }
+    if (dl == 0) return;
+    const int n_cand = cp.ncand;
+    uint64_t *row = f.mse + (int64_t)fb * 2 * n_cand;
+    const int damping = cp.damping;
+    // ---- luma
+    const int x0 = fbc * 64, y0 = fbr * 64;
+    load_region(f.B[0], bd, f.w, f.h, x0, y0, 64, reg);
+    for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
+        int y = y0 + i / 64, x = x0 + (i & 63);
+        src[i] = (x < f.w && y < f.h) ? (uint16_t)ldpx(f.S[0], (int64_t)y * f.w + x, bd) : 0;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
+        const int b = blist[k], by = b >> 3, bx = b & 7;
+        find_dir(reg + (by * 8 + 2) * CR + bx * 8 + 2, CR, cs, &sdir[b], &svar[b]);
+    }
+    __syncthreads();
+    const int sub = cp.sub_y;
+    const int rows_per = 8 / sub;  // sampled rows per 8x8 block
+    const int slots = nblk * rows_per * 8;
+    for (int gi = 0; gi < n_cand; ++gi) {
+        const int strength = cp.fs[gi];
+        const int pri = (strength / 4) << cs;
+        const int s = strength % 4;
+        const int sec = (s + (s == 3)) << cs;
+        const int dmp = damping + cs;
+        unsigned long long acc = 0;
+        for (int q = threadIdx.x; q < slots; q += blockDim.x) {
+            const int k = q / (rows_per * 8), rem = q - k * rows_per * 8;
+            const int i = (rem >> 3) * sub, j = rem & 7;
+            const int b = blist[k], by = b >> 3, bx = b & 7;
+            const int py = by * 8 + i, px = bx * 8 + j;
+            const int t = adjust_strength(pri, svar[b]);
+            const int y = cdef_px(reg, CR, (py + 2) * CR + px + 2, t, sec, pri ? sdir[b] : 0, dmp, dmp, cs);
+            const int e = (int)src[py * 64 + px] - y;
+            acc += (unsigned long long)((long long)e * e);
+        }
+        unsigned long long tot = block_sum_u64(acc, red);
+        if (threadIdx.x == 0) row[gi] = (tot >> (2 * cs)) * (unsigned long long)sub;
+    }
+    // ---- chroma: U then V accumulate into the joint row
+    if (!f.chroma) {
+        if (threadIdx.x == 0)
+            for (int gi = 0; gi < n_cand; ++gi) row[n_cand + gi] = 0;
+        return;
+    }
+    __shared__ unsigned long long uvacc[kMaxCand];
+    if (threadIdx.x == 0)
+        for (int gi = 0; gi < n_cand; ++gi) uvacc[gi] = 0;
+    const int cw = f.w / 2, ch = f.h / 2, cx0 = fbc * 32, cy0 = fbr * 32;
+    for (int p = 1; p <= 2; ++p) {
+        __syncthreads();
+        load_region(f.B[p], bd, cw, ch, cx0, cy0, 32, reg);
+        for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+            int y = cy0 + i / 32, x = cx0 + (i & 31);
+            src[i] = (x < cw && y < ch) ? (uint16_t)ldpx(f.S[p], (int64_t)y * cw + x, bd) : 0;
+        }
+        __syncthreads();
+        const int cslots = nblk * 16;
+        for (int gi = 0; gi < cp.first_pass_num; ++gi) {
+            const int strength = cp.fs[gi];
+            const int pri = (strength / 4) << cs;
+            const int s = strength % 4;
+            const int sec = (s + (s == 3)) << cs;
+            const int dmp = damping + cs - 1;
+            unsigned long long acc = 0;
+            for (int q = threadIdx.x; q < cslots; q += blockDim.x) {
+                const int k = q >> 4, i = (q >> 2) & 3, j = q & 3;
+                const int b = blist[k], by = b >> 3, bx = b & 7;
+                const int py = by * 4 + i, px = bx * 4 + j;
+                const int y = cdef_px(reg, CRC, (py + 2) * CRC + px + 2, pri, sec, pri ? sdir[b] : 0, dmp, dmp, cs);
+                const int e = (int)src[py * 32 + px] - y;
+                acc += (unsigned long long)((long long)e * e);
+            }
+            unsigned long long tot = block_sum_u64(acc, red);
+            if (threadIdx.x == 0) uvacc[gi] += (tot >> (2 * cs)) * (unsigned long long)cp.sub_uv;
+        }
+    }
+    if (threadIdx.x == 0) {
+        for (int gi = 0; gi < n_cand; ++gi)
+            row[n_cand + gi] = gi < cp.first_pass_num ? uvacc[gi] : 1040400ull * 64ull;
+    }
+}
+
+// ---- finish: the joint strength search of one frame in one CTA ----------
+
+// RDCOST (cdef.rs:814-816).
+__device__ __forceinline__ unsigned long long rdc(unsigned long long lambda, unsigned long long rate,
+                                                  unsigned long long dist) {
+    return ((rate * lambda + 256) >> 9) + (dist << 7);
+}
+
+// search_one_dual (cdef.rs:824-862), all threads of the CTA.
+__device__ unsigned long long search_one_dual(const FrameDesc &f, int nfb, int n_cand, int *lev0, int *lev1,
+                                              int nbs, unsigned long long *tot, unsigned long long *rv, int *ri) {
+    const uint64_t *mse = f.mse;
+    const int npairs = n_cand * n_cand;
+    for (int p = threadIdx.x; p < npairs; p += blockDim.x) tot[p] = 0;
+    for (int fb = threadIdx.x; fb < nfb; fb += blockDim.x) {
+        if (!f.fb_row[fb]) continue;
+        const uint64_t *row = mse + (int64_t)fb * 2 * n_cand;
+        unsigned long long best = 1ull << 63;
+        for (int gi = 0; gi < nbs; ++gi) {
+            unsigned long long c = row[lev0[gi]] + row[n_cand + lev1[gi]];
+            if (c < best) best = c;
+        }
+        f.cdef_best[fb] = best;
+    }
+    __syncthreads();
+    const int tpp = max(1, (int)blockDim.x / npairs);
+    const int work = npairs * tpp;
+    for (int w = threadIdx.x; w < work; w += blockDim.x) {
+        const int p = w / tpp, part = w - p * tpp;
+        const int j = p / n_cand, k = p - j * n_cand;
+        unsigned long long s = 0;
+        for (int fb = part; fb < nfb; fb += tpp) {
+            if (!f.fb_row[fb]) continue;
+            const uint64_t *row = mse + (int64_t)fb * 2 * n_cand;
+            unsigned long long c = row[j] + row[n_cand + k];
+            unsigned long long b = f.cdef_best[fb];
+            s += c < b ? c : b;
+        }
+        atomicAdd(&tot[p], s);
+    }
+    __syncthreads();
+    // argmin with strict < in (j, k) raster order: the lowest index wins ties.
+    unsigned long long bv = ~0ull;
+    int bi = 0x7fffffff;
+    for (int p = threadIdx.x; p < npairs; p += blockDim.x) {
+        unsigned long long v = tot[p] < (1ull << 63) ? tot[p] : (1ull << 63);
+        if (v < bv || (v == bv && p < bi)) {
+            bv = v;
+            bi = p;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long ov = __shfl_down_sync(0xffffffffu, bv, o);
+        int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ov < bv || (ov == bv && oi < bi)) {
+            bv = ov;
+            bi = oi;
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        rv[threadIdx.x >> 5] = bv;
+        ri[threadIdx.x >> 5] = bi;
+    }
+    __syncthreads();
+    __shared__ unsigned long long res_v;
+    if (threadIdx.x == 0) {
+        unsigned long long v = ~0ull;
+        int idx = 0x7fffffff;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+            if (rv[w] < v || (rv[w] == v && ri[w] < idx)) {
+                v = rv[w];
+                idx = ri[w];
+            }
+        // best_tot starts at 1 << 63 with strict <: a sum never below it
+        // leaves (0, 0).
+        if (v >= (1ull << 63)) {
+            idx = 0;
+            v = 1ull << 63;
+        }
+        lev0[nbs] = idx / n_cand;
+        lev1[nbs] = idx % n_cand;
+        res_v = v;
+    }
+    __syncthreads();
+    return res_v;
+}
+
+__global__ void __launch_bounds__(1024) k_cdef_finish(FrameDesc *frames, const int *frame_ids) {
+    __shared__ unsigned long long tot[kMaxCand * kMaxCand];
+    __shared__ unsigned long long rv[32];
+    __shared__ int ri[32];
+    __shared__ int lev0[17], lev1[17], blev0[8], blev1[8];
+    __shared__ int best_bits, sbc;
+    FrameDesc &f = frames[frame_ids[blockIdx.x]];
+    CdefParams &cp = f.cdef;
+    if (cp.mode != 1) return;
+    const int nfb = f.nhfb * f.nvfb, n_cand = cp.ncand;
+    if (threadIdx.x == 0) sbc = 0;
+    __syncthreads();
+    int cnt = 0;
+    for (int fb = threadIdx.x; fb < nfb; fb += blockDim.x) cnt += f.fb_row[fb];
+    atomicAdd(&sbc, cnt);
+    __syncthreads();
+    const int sb_count = sbc;
+    if (sb_count == 0) {  // every filter block all-skip: cdef.rs:282-288
+        if (threadIdx.x == 0) {
+            cp.bits = 0;
+            cp.y_str[0] = 0;
+            cp.uv_str[0] = 0;
+        }
+        for (int fb = threadIdx.x; fb < nfb; fb += blockDim.x) f.fb_idx[fb] = 0;
+        return;
+    }
+    unsigned long long best_cost = 1ull << 63;
+    if (threadIdx.x == 0) best_bits = 0;
+    for (int i = 0; i <= 3; ++i) {
+        const int nb = 1 << i;
+        if (threadIdx.x < 17) {
+            lev0[threadIdx.x] = 0;
+            lev1[threadIdx.x] = 0;
+        }
+        __syncthreads();
+        unsigned long long t = 1ull << 63;
+        for (int s = 0; s < nb; ++s) t = search_one_dual(f, nfb, n_cand, lev0, lev1, s, tot, rv, ri);
+        for (int r = 0; r < 4 * nb; ++r) {
+            if (threadIdx.x == 0)
+                for (int j = 0; j < nb - 1; ++j) {
+                    lev0[j] = lev0[j + 1];
+                    lev1[j] = lev1[j + 1];
+                }
+            __syncthreads();
+            t = search_one_dual(f, nfb, n_cand, lev0, lev1, nb - 1, tot, rv, ri);
+        }
+        const unsigned long long total_bits = (unsigned long long)sb_count * i + nb * 12;
+        const unsigned long long cost = rdc(cp.lambda, total_bits << 9, t * 16);
+        if (cost < best_cost) {
+            best_cost = cost;
+            if (threadIdx.x == 0) {
+                best_bits = i;
+                for (int k = 0; k < nb; ++k) {
+                    blev0[k] = lev0[k];
+                    blev1[k] = lev1[k];
+                }
+            }
+        }
+        __syncthreads();
+    }
+    const int nb = 1 << best_bits;
+    for (int fb = threadIdx.x; fb < nfb; fb += blockDim.x) {
+        int best_gi = 0;
+        if (f.fb_row[fb]) {
+            const uint64_t *row = f.mse + (int64_t)fb * 2 * n_cand;
+            unsigned long long best = ~0ull;
+            for (int gi = 0; gi < nb; ++gi) {
+                unsigned long long c = row[blev0[gi]] + row[n_cand + blev1[gi]];
+                if (c < best) {
+                    best = c;
+                    best_gi = gi;
+                }
+            }
+        }
+        f.fb_idx[fb] = (uint8_t)best_gi;
+    }
+    if (threadIdx.x == 0) {
+        cp.bits = best_bits;
+        for (int gi = 0; gi < 8; ++gi) {
+            cp.y_str[gi] = gi < nb ? (uint8_t)cp.fs[blev0[gi]] : 0;
+            cp.uv_str[gi] = gi < nb ? (uint8_t)cp.fs[blev1[gi]] : 0;
+        }
+    }
+}
+
+// ---- apply: one CTA per filter block, B (post-deblock) -> A -----------
+
+__global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems) {
+    __shared__ uint16_t reg[CR * CR];
+    __shared__ int sdir[64], svar[64];
+    __shared__ unsigned long long red[8];
+    const int it = find_item(items, nitems, blockIdx.x);
+    const WorkItem wi = items[it];
+    const FrameDesc &f = frames[wi.frame];
+    const CdefParams &cp = f.cdef;
+    const int fb = blockIdx.x - wi.cta_begin;
+    const int fbr = fb / f.nhfb, fbc = fb - fbr * f.nhfb;
+    const int bd = f.bd, cs = bd - 8;
+    const int x0 = fbc * 64, y0 = fbr * 64;
+    const int vsize = min(64, f.h - y0), hsize = min(64, f.w - x0);
+    // Decoder do_cdef gate (cdef.rs:84-88).
+    const bool any = cp.bits != 0 || cp.y_str[0] != 0 || (f.chroma && cp.uv_str[0] != 0);
+    const uint64_t dl_all = fb_dlist(f, fbr, fbc);
+    if (threadIdx.x == 0) f.fb_row[fb] = dl_all != 0;
+    const uint64_t dl = any ? dl_all : 0;
+    if (dl == 0) {  // copy-through
+        for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
+            int y = y0 + i / 64, x = x0 + (i & 63);
+            if (x < f.w && y < f.h) stpx(f.A[0], (int64_t)y * f.w + x, bd, ldpx(f.B[0], (int64_t)y * f.w + x, bd));
+        }
+        if (f.chroma)
+            for (int p = 1; p <= 2; ++p)
+                for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+                    int y = y0 / 2 + i / 32, x = x0 / 2 + (i & 31);
+                    if (x < f.w / 2 && y < f.h / 2)
+                        stpx(f.A[p], (int64_t)y * (f.w / 2) + x, bd, ldpx(f.B[p], (int64_t)y * (f.w / 2) + x, bd));
+                }
+        return;
+    }
+    const int sidx = cp.bits == 0 ? 0 : f.fb_idx[fb];
+    const int ys = cp.y_str[sidx], uvs = f.chroma ? cp.uv_str[sidx] : 0;
+    const int lvl_y = (ys / 4) << cs, sec_y = ((ys % 4) + ((ys % 4) == 3)) << cs;
+    const int lvl_uv = (uvs / 4) << cs, sec_uv = ((uvs % 4) + ((uvs % 4) == 3)) << cs;
+    const int damping = cp.damping + cs;
+    load_region(f.B[0], bd, f.w, f.h, x0, y0, 64, reg);
+    __syncthreads();
+    for (int b = threadIdx.x; b < 64; b += blockDim.x)
+        if ((dl >> b) & 1) find_dir(reg + ((b >> 3) * 8 + 2) * CR + (b & 7) * 8 + 2, CR, cs, &sdir[b], &svar[b]);
+    __syncthreads();
+    unsigned long long filt = 0, changed = 0;
+    const bool zero_y = lvl_y == 0 && sec_y == 0;
+    for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
+        const int py = i / 64, px = i & 63;
+        if (py >= vsize || px >= hsize) continue;
+        const int b = (py >> 3) * 8 + (px >> 3);
+        const int x = reg[(py + 2) * CR + px + 2];
+        int y = x;
+        if (!zero_y && ((dl >> b) & 1)) {
+            const int t = adjust_strength(lvl_y, svar[b]);
+            if (!(t == 0 && sec_y == 0)) {
+                y = cdef_px(reg, CR, (py + 2) * CR + px + 2, t, sec_y, lvl_y ? sdir[b] : 0, damping, damping, cs);
+                filt += 1;
+                changed += y != x;
+            }
+        }
+        stpx(f.A[0], (int64_t)(y0 + py) * f.w + x0 + px, bd, y);
+    }
+    if (f.chroma) {
+        const bool zero_uv = lvl_uv == 0 && sec_uv == 0;
+        const int cw = f.w / 2, ch = f.h / 2, cx0 = x0 / 2, cy0 = y0 / 2;
+        for (int p = 1; p <= 2; ++p) {
+            __syncthreads();
+            load_region(f.B[p], bd, cw, ch, cx0, cy0, 32, reg);
+            __syncthreads();
+            for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+                const int py = i / 32, px = i & 31;
+                if (py >= vsize / 2 || px >= hsize / 2) continue;
+                const int b = (py >> 2) * 8 + (px >> 2);
+                const int x = reg[(py + 2) * CRC + px + 2];
+                int y = x;
+                if (!zero_uv && ((dl >> b) & 1)) {
+                    y = cdef_px(reg, CRC, (py + 2) * CRC + px + 2, lvl_uv, sec_uv, lvl_uv ? sdir[b] : 0, damping - 1,
+                                damping - 1, cs);
+                    filt += 1;
+                    changed += y != x;
+                }
+                stpx(f.A[p], (int64_t)(cy0 + py) * cw + cx0 + px, bd, y);
+            }
+        }
+    }
+    if (bd == 8 && f.cdef_stats) {
+        unsigned long long a = block_sum_u64(filt, red);
+        unsigned long long c = block_sum_u64(changed, red);
+        if (threadIdx.x == 0) {
+            atomicAdd(&f.cdef_stats[0], a);
+            atomicAdd(&f.cdef_stats[1], c);
+        }
+    }
+}
+
+}  // namespace zf

@@ -1,0 +1,349 @@
+// zf_deblock.cu -- AV1 deblocking filter on the GPU.
+//
+// Semantics follow the reference's decoder-exact frame pass
+// (svtav1-encoder/src/deblock.rs:811-1006): every vertical edge of a plane
+// is filtered, then every horizontal edge, with the edge set, filter length
+// and thresholds of lpf_params (deblock.rs:698-796) and the lpf kernels of
+// svtav1-dsp/src/loop_filter.rs:67-412 / hbd.rs:1066-1440.
+//
+// GPU formulation. Within one pass the edge windows never overlap (the
+// filter length is capped by the transform widths on both sides), so all
+// edges of a pass are independent. A CTA owns a 64x64 output tile; it loads
+// the tile plus a 12-pixel halo into shared memory, filters every vertical
+// edge that can touch the tile's columns over all halo rows, synchronises,
+// filters every horizontal edge that can touch the tile's rows, and writes
+// (apply) or scores (level search) the tile. The halo covers the farthest
+// reach of the 14-tap filter (an edge 5 px outside modifies the tile and
+// reads 7 px further), so each tile is exact in isolation and the plane is
+// read once and written once.
+//
+// An edge position (x, y) on the 4x4 grid filters exactly when the
+// sequential walk of filter_plane would visit it and lpf_params returns a
+// length: the walk visits the transform origins, which for a tiling of
+// transforms aligned to their own size are the positions with
+// coord % tx_dim == 0 (the host packer rejects any other tiling).
+#include "zf_dev.cuh"
+
+namespace zf {
+
+constexpr int DB_T = 64;             // output tile edge
+constexpr int DB_H = 12;             // halo
+constexpr int DB_R = DB_T + 2 * DB_H;  // region edge (88)
+constexpr int DB_BANDS = DB_R / 4;   // 22 four-row bands in the region
+constexpr int DB_EDGES = 19;         // edges at tile origin -4 .. +68
+
+struct Thr {
+    int mblim, lim, hev;
+};
+
+// lf_thresholds (svtav1-dsp/src/loop_filter.rs:50-65).
+__device__ __forceinline__ Thr lf_thresholds(int level, int sharp) {
+    int bil = level >> ((sharp > 0) + (sharp > 4));
+    if (sharp > 0 && bil > 9 - sharp) bil = 9 - sharp;
+    if (bil < 1) bil = 1;
+    Thr t;
+    t.mblim = 2 * (level + 2) + bil;
+    t.lim = bil;
+    t.hev = level >> 4;
+    return t;
+}
+
+__device__ __forceinline__ int clamp_sc(int t, int bd) {
+    int lo = -(128 << (bd - 8)), hi = (128 << (bd - 8)) - 1;
+    return t < lo ? lo : (t > hi ? hi : t);
+}
+
+// highbd_filter4 (hbd.rs:1211-1232); at bd 8 it is the 8-bit filter4
+// (loop_filter.rs:181-203) with the sign flip written as a bias.
+__device__ __forceinline__ void filter4(int mask, int hev, int *w, int bd) {
+    int bias = 0x80 << (bd - 8);
+    int ps1 = w[0] - bias, ps0 = w[1] - bias, qs0 = w[2] - bias, qs1 = w[3] - bias;
+    int filter = clamp_sc(ps1 - qs1, bd) & hev;
+    filter = clamp_sc(filter + 3 * (qs0 - ps0), bd) & mask;
+    int f1 = clamp_sc(filter + 4, bd) >> 3;
+    int f2 = clamp_sc(filter + 3, bd) >> 3;
+    w[2] = clamp_sc(qs0 - f1, bd) + bias;
+    w[1] = clamp_sc(ps0 + f2, bd) + bias;
+    int outer = ((f1 + 1) >> 1) & ~hev;
+    w[3] = clamp_sc(qs1 - outer, bd) + bias;
+    w[0] = clamp_sc(ps1 + outer, bd) + bias;
+}
+
+// One line of one edge. `p` points at q0 in shared memory, `st` is the tap
+// step (1 for vertical edges, the row pitch for horizontal edges).
+__device__ __forceinline__ void filter_line(uint16_t *p, int st, int len, Thr t, int bd) {
+    int w[14];
+    const int half = len >> 1;
+#pragma unroll
+    for (int k = 0; k < 14; ++k)
+        if (k < len) w[k] = p[(k - half) * st];
+    const int sh = bd - 8;
+    const int lim = t.lim << sh, blim = t.mblim << sh, thr = t.hev << sh, one = 1 << sh;
+    auto ad = [](int a, int b) { return a > b ? a - b : b - a; };
+    if (len == 4) {
+        int p1 = w[0], p0 = w[1], q0 = w[2], q1 = w[3];
+        bool m = ad(p1, p0) <= lim && ad(q1, q0) <= lim && ad(p0, q0) * 2 + ad(p1, q1) / 2 <= blim;
+        int hev = (ad(p1, p0) > thr || ad(q1, q0) > thr) ? -1 : 0;
+        filter4(m ? -1 : 0, hev, w, bd);
+    } else if (len == 6) {
+        int p2 = w[0], p1 = w[1], p0 = w[2], q0 = w[3], q1 = w[4], q2 = w[5];
+        bool m = ad(p2, p1) <= lim && ad(p1, p0) <= lim && ad(q1, q0) <= lim && ad(q2, q1) <= lim &&
+                 ad(p0, q0) * 2 + ad(p1, q1) / 2 <= blim;
+        bool flat = ad(p1, p0) <= one && ad(q1, q0) <= one && ad(p2, p0) <= one && ad(q2, q0) <= one;
+        if (flat && m) {
+            w[1] = (p2 * 3 + p1 * 2 + p0 * 2 + q0 + 4) >> 3;
+            w[2] = (p2 + p1 * 2 + p0 * 2 + q0 * 2 + q1 + 4) >> 3;
+            w[3] = (p1 + p0 * 2 + q0 * 2 + q1 * 2 + q2 + 4) >> 3;
+            w[4] = (p0 + q0 * 2 + q1 * 2 + q2 * 3 + 4) >> 3;
+        } else {
+            int hev = (ad(p1, p0) > thr || ad(q1, q0) > thr) ? -1 : 0;
+            filter4(m ? -1 : 0, hev, w + 1, bd);
+        }
+    } else {
+        int *v = len == 8 ? w : w + 3;  // the [p3..q3] window
+        int p3 = v[0], p2 = v[1], p1 = v[2], p0 = v[3], q0 = v[4], q1 = v[5], q2 = v[6], q3 = v[7];
+        bool m = ad(p3, p2) <= lim && ad(p2, p1) <= lim && ad(p1, p0) <= lim && ad(q1, q0) <= lim &&
+                 ad(q2, q1) <= lim && ad(q3, q2) <= lim && ad(p0, q0) * 2 + ad(p1, q1) / 2 <= blim;
+        bool flat = ad(p1, p0) <= one && ad(q1, q0) <= one && ad(p2, p0) <= one && ad(q2, q0) <= one &&
+                    ad(p3, p0) <= one && ad(q3, q0) <= one;
+        bool flat2 = false;
+        if (len == 14)
+            flat2 = ad(w[1], p0) <= one && ad(w[12], q0) <= one && ad(w[2], p0) <= one && ad(w[11], q0) <= one &&
+                    ad(w[0], p0) <= one && ad(w[13], q0) <= one;
+        if (len == 14 && flat2 && flat && m) {
+            int p6 = w[0], p5 = w[1], p4 = w[2], q4 = w[11], q5 = w[12], q6 = w[13];
+            w[1] = (p6 * 7 + p5 * 2 + p4 * 2 + p3 + p2 + p1 + p0 + q0 + 8) >> 4;
+            w[2] = (p6 * 5 + p5 * 2 + p4 * 2 + p3 * 2 + p2 + p1 + p0 + q0 + q1 + 8) >> 4;
+            w[3] = (p6 * 4 + p5 + p4 * 2 + p3 * 2 + p2 * 2 + p1 + p0 + q0 + q1 + q2 + 8) >> 4;
+            w[4] = (p6 * 3 + p5 + p4 + p3 * 2 + p2 * 2 + p1 * 2 + p0 + q0 + q1 + q2 + q3 + 8) >> 4;
+            w[5] = (p6 * 2 + p5 + p4 + p3 + p2 * 2 + p1 * 2 + p0 * 2 + q0 + q1 + q2 + q3 + q4 + 8) >> 4;
+            w[6] = (p6 + p5 + p4 + p3 + p2 + p1 * 2 + p0 * 2 + q0 * 2 + q1 + q2 + q3 + q4 + q5 + 8) >> 4;
+            w[7] = (p5 + p4 + p3 + p2 + p1 + p0 * 2 + q0 * 2 + q1 * 2 + q2 + q3 + q4 + q5 + q6 + 8) >> 4;
+            w[8] = (p4 + p3 + p2 + p1 + p0 + q0 * 2 + q1 * 2 + q2 * 2 + q3 + q4 + q5 + q6 * 2 + 8) >> 4;
+            w[9] = (p3 + p2 + p1 + p0 + q0 + q1 * 2 + q2 * 2 + q3 * 2 + q4 + q5 + q6 * 3 + 8) >> 4;
+            w[10] = (p2 + p1 + p0 + q0 + q1 + q2 * 2 + q3 * 2 + q4 * 2 + q5 + q6 * 4 + 8) >> 4;
+            w[11] = (p1 + p0 + q0 + q1 + q2 + q3 * 2 + q4 * 2 + q5 * 2 + q6 * 5 + 8) >> 4;
+            w[12] = (p0 + q0 + q1 + q2 + q3 + q4 * 2 + q5 * 2 + q6 * 7 + 8) >> 4;
+        } else if (flat && m) {
+            v[1] = (p3 + p3 + p3 + 2 * p2 + p1 + p0 + q0 + 4) >> 3;
+            v[2] = (p3 + p3 + p2 + 2 * p1 + p0 + q0 + q1 + 4) >> 3;
+            v[3] = (p3 + p2 + p1 + 2 * p0 + q0 + q1 + q2 + 4) >> 3;
+            v[4] = (p2 + p1 + p0 + 2 * q0 + q1 + q2 + q3 + 4) >> 3;
+            v[5] = (p1 + p0 + q0 + 2 * q1 + q2 + q3 + q3 + 4) >> 3;
+            v[6] = (p0 + q0 + q1 + 2 * q2 + q3 + q3 + q3 + 4) >> 3;
+        } else {
+            int hev = (ad(p1, p0) > thr || ad(q1, q0) > thr) ? -1 : 0;
+            filter4(m ? -1 : 0, hev, v + 2, bd);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 14; ++k)
+        if (k < len) p[(k - half) * st] = (uint16_t)w[k];
+}
+
+// Transform dims of a packed mi for a plane: luma TX grid, or the chroma TX
+// max(b/2, 4) of the covering block (deblock.rs:728-743).
+__device__ __forceinline__ void tx_dims(uint32_t r, int plane, int *tw, int *th) {
+    if (plane == 0) {
+        *tw = mi_tw(r);
+        *th = mi_th(r);
+    } else {
+        *tw = max(mi_bw(r) >> 1, 4);
+        *th = max(mi_bh(r) >> 1, 4);
+    }
+}
+
+// Filter length for the edge at plane position (x, y) (both multiples of 4),
+// 0 when nothing is filtered (lpf_params, deblock.rs:698-796).
+__device__ int edge_len(const FrameDesc &f, bool vert, int x, int y, int plane, int level) {
+    const int ss = plane ? 1 : 0;
+    if (level == 0) return 0;
+    if (x >= (f.tw >> ss) || y >= (f.th >> ss)) return 0;
+    const int mr = ss | ((y << ss) >> 2), mc = ss | ((x << ss) >> 2);
+    if (mr >= f.mi_rows || mc >= f.mi_cols) return 0;
+    const uint32_t cur = f.mi[(int64_t)mr * f.mi_cols + mc];
+    int tw, th;
+    tx_dims(cur, plane, &tw, &th);
+    const int ts = vert ? tw : th;
+    const int coord = vert ? x : y;
+    if ((coord & (ts - 1)) != 0 || coord == 0) return 0;
+    const int pr = vert ? mr : mr - (1 << ss), pc = vert ? mc - (1 << ss) : mc;
+    const uint32_t prv = f.mi[(int64_t)pr * f.mi_cols + pc];
+    int ptw, pth;
+    tx_dims(prv, plane, &ptw, &pth);
+    const int pv = vert ? ptw : pth;
+    // pu_edge: different covering blocks <=> different aligned block origins.
+    const int cbw = mi_bw(cur) >> 2, cbh = mi_bh(cur) >> 2, pbw = mi_bw(prv) >> 2, pbh = mi_bh(prv) >> 2;
+    const bool pu_edge = (mr & ~(cbh - 1)) != (pr & ~(pbh - 1)) || (mc & ~(cbw - 1)) != (pc & ~(pbw - 1));
+    if (!mi_skip_inter(prv) || !mi_skip_inter(cur) || pu_edge) {
+        const int md = min(ts, pv);
+        return md == 4 ? 4 : (plane ? 6 : (md == 8 ? 8 : 14));
+    }
+    return 0;
+}
+
+struct DbTile {
+    const FrameDesc *f;
+    int plane, pw, ph, x0, y0;
+};
+
+// Load the region of a tile into shared memory as u16.
+__device__ void db_load(const DbTile &t, const uint8_t *plane, uint16_t *reg) {
+    const int bd = t.f->bd;
+    for (int i = threadIdx.x; i < DB_R * DB_R; i += blockDim.x) {
+        int ry = i / DB_R, rx = i - ry * DB_R;
+        int y = t.y0 - DB_H + ry, x = t.x0 - DB_H + rx;
+        int v = 0;
+        if (x >= 0 && x < t.pw && y >= 0 && y < t.ph) v = ldpx(plane, (int64_t)y * t.pw + x, bd);
+        reg[i] = (uint16_t)v;
+    }
+}
+
+// Edge lengths of a tile: vl[band][edge] for vertical edges over the region
+// rows, hl[col band][edge] for horizontal edges over the tile columns.
+__device__ void db_params(const DbTile &t, int lvl_v, int lvl_h, uint8_t *vl, uint8_t *hl) {
+    const FrameDesc &f = *t.f;
+    for (int i = threadIdx.x; i < DB_BANDS * DB_EDGES; i += blockDim.x) {
+        int band = i / DB_EDGES, e = i - band * DB_EDGES;
+        int y = t.y0 - DB_H + band * 4, x = t.x0 - 4 + e * 4;
+        int len = 0;
+        if (y >= 0 && y < t.ph && x >= 0 && x < t.pw) len = edge_len(f, true, x, y, t.plane, lvl_v);
+        vl[i] = (uint8_t)len;
+    }
+    for (int i = threadIdx.x; i < (DB_T / 4) * DB_EDGES; i += blockDim.x) {
+        int cb = i / DB_EDGES, e = i - cb * DB_EDGES;
+        int x = t.x0 + cb * 4, y = t.y0 - 4 + e * 4;
+        int len = 0;
+        if (y >= 0 && y < t.ph && x >= 0 && x < t.pw) len = edge_len(f, false, x, y, t.plane, lvl_h);
+        hl[i] = (uint8_t)len;
+    }
+}
+
+// Both passes on the region in shared memory.
+__device__ void db_filter(const DbTile &t, uint16_t *reg, const uint8_t *vl, const uint8_t *hl, int lvl_v,
+                          int lvl_h) {
+    const int bd = t.f->bd, sharp = t.f->sharpness;
+    const Thr tv = lf_thresholds(lvl_v, sharp), th = lf_thresholds(lvl_h, sharp);
+    for (int i = threadIdx.x; i < DB_BANDS * DB_EDGES * 4; i += blockDim.x) {
+        int be = i >> 2, line = i & 3;
+        int len = vl[be];
+        if (!len) continue;
+        int band = be / DB_EDGES, e = be - band * DB_EDGES;
+        int ry = band * 4 + line, rx = DB_H - 4 + e * 4;
+        filter_line(reg + ry * DB_R + rx, 1, len, tv, bd);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < (DB_T / 4) * DB_EDGES * 4; i += blockDim.x) {
+        int be = i >> 2, line = i & 3;
+        int len = hl[be];
+        if (!len) continue;
+        int cb = be / DB_EDGES, e = be - cb * DB_EDGES;
+        int rx = DB_H + cb * 4 + line, ry = DB_H - 4 + e * 4;
+        filter_line(reg + ry * DB_R + rx, DB_R, len, th, bd);
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void plane_geom(const FrameDesc &f, int plane, int *pw, int *ph) {
+    *pw = plane ? f.w / 2 : f.w;
+    *ph = plane ? f.h / 2 : f.h;
+}
+
+// Apply: A -> B for one 64x64 tile. Plane gating of apply_deblock_frame
+// (deblock.rs:951-967): both luma levels zero disables every plane; a chroma
+// plane needs its own level.
+__global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, const WorkItem *items, int nitems) {
+    __shared__ uint16_t reg[DB_R * DB_R];
+    __shared__ uint8_t vl[DB_BANDS * DB_EDGES], hl[(DB_T / 4) * DB_EDGES];
+    const int it = find_item(items, nitems, blockIdx.x);
+    const WorkItem wi = items[it];
+    const FrameDesc &f = frames[wi.frame];
+    const int plane = wi.plane;
+    int pw, ph;
+    plane_geom(f, plane, &pw, &ph);
+    const int tiles_x = (pw + DB_T - 1) / DB_T;
+    const int tix = blockIdx.x - wi.cta_begin;
+    DbTile t{&f, plane, pw, ph, (tix % tiles_x) * DB_T, (tix / tiles_x) * DB_T};
+    int lv, lh;
+    if (f.lf[0] == 0 && f.lf[1] == 0) {
+        lv = lh = 0;
+    } else if (plane == 0) {
+        lv = f.lf[0];
+        lh = f.lf[1];
+    } else {
+        lv = lh = f.lf[1 + plane];
+    }
+    const int bd = f.bd;
+    if (lv == 0 && lh == 0) {  // copy-through
+        for (int i = threadIdx.x; i < DB_T * DB_T; i += blockDim.x) {
+            int y = t.y0 + i / DB_T, x = t.x0 + (i % DB_T);
+            if (x < pw && y < ph) {
+                int64_t o = (int64_t)y * pw + x;
+                stpx(f.B[plane], o, bd, ldpx(f.A[plane], o, bd));
+            }
+        }
+        return;
+    }
+    db_load(t, f.A[plane], reg);
+    db_params(t, lv, lh, vl, hl);
+    __syncthreads();
+    db_filter(t, reg, vl, hl, lv, lh);
+    for (int i = threadIdx.x; i < DB_T * DB_T; i += blockDim.x) {
+        int ty = i / DB_T, tx = i % DB_T;
+        int y = t.y0 + ty, x = t.x0 + tx;
+        if (x < pw && y < ph) stpx(f.B[plane], (int64_t)y * pw + x, bd, reg[(ty + DB_H) * DB_R + tx + DB_H]);
+    }
+}
+
+// Level search: SSE(source, plane filtered at level L in both directions)
+// over the full aligned plane (try_filter_plane, deblock.rs:228-293), for
+// up to two candidate levels per launch. items[].a = index of the (frame,
+// plane) search slot; sse[slot * 2 + k] accumulates level levels[slot*2+k].
+__global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, const WorkItem *items, int nitems,
+                                                     const int *levels, unsigned long long *sse) {
+    __shared__ uint16_t reg[DB_R * DB_R];
+    __shared__ uint16_t pristine[DB_R * DB_R];
+    __shared__ uint8_t vl[DB_BANDS * DB_EDGES], hl[(DB_T / 4) * DB_EDGES];
+    __shared__ unsigned long long part[8];
+    const int it = find_item(items, nitems, blockIdx.x);
+    const WorkItem wi = items[it];
+    const FrameDesc &f = frames[wi.frame];
+    const int plane = wi.plane, slot = wi.a;
+    int pw, ph;
+    plane_geom(f, plane, &pw, &ph);
+    const int tiles_x = (pw + DB_T - 1) / DB_T;
+    const int tix = blockIdx.x - wi.cta_begin;
+    DbTile t{&f, plane, pw, ph, (tix % tiles_x) * DB_T, (tix / tiles_x) * DB_T};
+    const int bd = f.bd;
+    db_load(t, f.A[plane], pristine);
+    __syncthreads();
+    for (int k = 0; k < 2; ++k) {
+        const int lvl = levels[slot * 2 + k];
+        if (lvl < 0) continue;
+        for (int i = threadIdx.x; i < DB_R * DB_R; i += blockDim.x) reg[i] = pristine[i];
+        if (lvl != 0) db_params(t, lvl, lvl, vl, hl);
+        __syncthreads();
+        if (lvl != 0) db_filter(t, reg, vl, hl, lvl, lvl);
+        unsigned long long acc = 0;
+        for (int i = threadIdx.x; i < DB_T * DB_T; i += blockDim.x) {
+            int ty = i / DB_T, tx = i % DB_T;
+            int y = t.y0 + ty, x = t.x0 + tx;
+            if (x < pw && y < ph) {
+                int d = ldpx(f.S[plane], (int64_t)y * pw + x, bd) - (int)reg[(ty + DB_H) * DB_R + tx + DB_H];
+                acc += (unsigned long long)((long long)d * d);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long s = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += part[w];
+            atomicAdd(&sse[slot * 2 + k], s);
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace zf

@@ -1,0 +1,131 @@
+// zf_dev.cuh -- device-side data layout shared by the filter-stage kernels.
+//
+// A launch processes a batch of frames. Every frame is described by one
+// FrameDesc in device memory; every kernel walks a flat list of work items
+// (frame, plane, tile) whose CTA ranges are prefix-summed on the host, so a
+// single launch covers any mix of sizes and bit depths. Pixels are stored
+// tight (stride = plane width) as uint8 (8-bit) or uint16 (10-bit); kernels
+// branch on the frame's bit depth at load/store time only.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace zf {
+
+constexpr int kMaxCand = 48;        // CDEF candidates at preset 0
+constexpr int kMaxUnits = 4096;     // restoration units per plane (guarded on host)
+
+// Restoration unit rectangle in plane pixels (TileLimits,
+// svtav1-dsp/src/restoration.rs:1096-1101).
+struct UnitRect {
+    int h_start, h_end, v_start, v_end;
+};
+
+// Per-unit Wiener state, written by the stats/solve/trial/finish kernels.
+struct LrUnit {
+    int64_t sum;                // sum of dgd over the unit (find_average numerator)
+    unsigned long long sse_blk; // sse_region parts: 16x16 blocks, right strip,
+    unsigned long long sse_rgt; // bottom strip (the strips are truncated to
+    unsigned long long sse_bot; // u32 at 10 bits, restoration.rs:1991-2036)
+    int64_t sse_none;
+    int64_t sse_wn;             // trial SSE, INT64_MAX when the score reverts
+    int64_t score;
+    int64_t m[49];              // M, raw sums (before the bit-depth divider)
+    int64_t h[2401];            // H upper triangle, row-major win2 x win2
+    int32_t vd[7], hd[7];
+    int16_t vf[8], hf[8];
+    int32_t rtype;
+    int32_t pad;
+};
+
+struct LrPlane {
+    int on;              // plane searched
+    int win;             // 5 or 7
+    int pw, ph;          // true plane dims (chroma ceil)
+    int stride;          // storage stride (aligned canvas)
+    int hunits, vunits;
+    int frame_rtype;
+    int refine;          // finer_tile_search_wiener refinement (presets <= 3)
+    UnitRect *rects;     // hunits*vunits
+    LrUnit *units;       // hunits*vunits
+};
+
+struct CdefParams {
+    int mode;            // 0: off (nothing signaled), 1: search, 2: fixed pick
+    int damping, bits;
+    int ncand, first_pass_num, sub_y, sub_uv;
+    int pad;
+    uint64_t lambda;
+    int fs[kMaxCand];
+    uint8_t y_str[8], uv_str[8];
+};
+
+struct FrameDesc {
+    int bd;                 // 8 or 10
+    int w, h;               // aligned canvas
+    int tw, th;             // true dims
+    int chroma;             // 4:2:0 planes present
+    int preset, qindex, sharpness;
+    int mi_cols, mi_rows;
+    int nhfb, nvfb;
+    uint8_t lf[4];          // deblock levels (written before the apply)
+    // Planes: A = input recon, later post-CDEF; B = post-deblock (pre-CDEF);
+    // C = post-LR (final). S = source.
+    uint8_t *A[3], *B[3], *C[3];
+    const uint8_t *S[3];
+    const uint32_t *mi;
+    // CDEF
+    CdefParams cdef;
+    uint64_t *mse;          // nfb x 2 x ncand
+    uint8_t *fb_row;        // nfb: fb has a non-skip 8x8
+    uint8_t *fb_idx;        // nfb
+    uint64_t *cdef_best;    // nfb scratch for the joint search
+    unsigned long long *cdef_stats;  // [filtered, changed, sb_count]
+    // LR
+    LrPlane lr[3];
+    int64_t rdmult;
+    int lr_on;
+};
+
+// One entry of a launch work list: a tile of a frame/plane, owning CTAs
+// [cta_begin, cta_begin + ctas).
+struct WorkItem {
+    int frame, plane;
+    int a, b;               // item-specific (e.g. unit index, stripe)
+    int cta_begin, ctas;
+};
+
+// Binary search for the work item owning blockIdx.x.
+__device__ __forceinline__ int find_item(const WorkItem *items, int n, int cta) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (items[mid].cta_begin <= cta) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---- pixel access --------------------------------------------------------
+__device__ __forceinline__ int ldpx(const uint8_t *p, int64_t idx, int bd) {
+    return bd == 8 ? (int)p[idx] : (int)reinterpret_cast<const uint16_t *>(p)[idx];
+}
+__device__ __forceinline__ void stpx(uint8_t *p, int64_t idx, int bd, int v) {
+    if (bd == 8) p[idx] = (uint8_t)v; else reinterpret_cast<uint16_t *>(p)[idx] = (uint16_t)v;
+}
+
+// ---- packed geometry (zf_filter.h) --------------------------------------
+__device__ __forceinline__ int mi_bw(uint32_t r) { return 4 << (r & 7); }
+__device__ __forceinline__ int mi_bh(uint32_t r) { return 4 << ((r >> 3) & 7); }
+__device__ __forceinline__ int mi_tw(uint32_t r) { return 4 << ((r >> 6) & 7); }
+__device__ __forceinline__ int mi_th(uint32_t r) { return 4 << ((r >> 9) & 7); }
+__device__ __forceinline__ bool mi_skip(uint32_t r) { return (r >> 12) & 1; }
+__device__ __forceinline__ bool mi_skip_inter(uint32_t r) { return (r >> 13) & 1; }
+
+// Error flag shared by all kernels of a context (first error wins).
+struct DevStatus {
+    int code;
+    int where;
+};
+
+}  // namespace zf

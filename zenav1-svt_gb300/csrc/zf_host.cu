@@ -1,0 +1,1019 @@
+// zf_host.cu -- host orchestration and the C ABI (include/zf_filter.h).
+//
+// One call runs a batch of frames through the selected passes. Everything a
+// pass needs is laid out in one device arena: three working plane sets per
+// frame (A: input recon, reused for the post-CDEF planes; B: post-deblock;
+// C: post-restoration), the source planes, the packed geometry and the
+// search scratch. Decisions are computed on the device (CDEF joint search,
+// Wiener solve and frame RD) so the passes after the deblock level search
+// are one fixed sequence of launches; only the deblock hill-climb of
+// presets <= 5 round-trips to the host, one step per launch.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/zf_av1_tables.h"
+#include "../../include/zf_filter.h"
+#include "zf_kernels.cuh"
+
+using zf::CdefParams;
+using zf::FrameDesc;
+using zf::LrPlane;
+using zf::LrUnit;
+using zf::UnitRect;
+using zf::WorkItem;
+
+struct zf_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint8_t *arena = nullptr;
+    size_t arena_cap = 0;
+    uint64_t budget = 0;
+    volatile int32_t *cancel = nullptr;
+};
+
+namespace {
+
+enum : unsigned {
+    STG_DB_PICK = 1u << 0,
+    STG_DB_APPLY = 1u << 1,
+    STG_CDEF_SEARCH = 1u << 2,
+    STG_CDEF_APPLY = 1u << 3,
+    STG_LR_SEARCH = 1u << 4,
+    STG_LR_APPLY = 1u << 5,
+    STG_ALL = 0x3f,
+};
+
+// Where the caller's rec[] goes in, and which plane set comes back out.
+enum PlaneSet { SET_A = 0, SET_B = 1, SET_C = 2 };
+
+struct Run {
+    unsigned stages;
+    PlaneSet rec_in;
+    PlaneSet rec_out;
+    bool pre_cdef_in;       // zf_lr_apply: pre_cdef[] -> B
+    const void *const *pre_cdef;
+    bool lf_given;          // decisions provided by the caller
+    bool cdef_given;
+    bool lr_given;
+};
+
+int fail(zf_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+#define CU(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(ctx, ZF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));    \
+    } while (0)
+
+// ---- reference decision helpers (host scalar) ----------------------------
+
+// kf_full_lambda_8bit_unweighted (svtav1-encoder/src/pd0.rs:218).
+uint32_t lambda_8bit_unweighted(int q) {
+    const double d = (double)zf_dc_qlookup_8[q];
+    const int64_t rdmult = (int64_t)((3.3 + 0.0015 * d) * d * d);
+    return (uint32_t)((rdmult * 150) >> 7);
+}
+// kf_full_lambda_bd10_unweighted (pd0.rs:330).
+uint32_t lambda_bd10_unweighted(int q) {
+    const double d = (double)zf_dc_qlookup_10[q];
+    int64_t rdmult = (int64_t)((3.3 + 0.0015 * d) * d * d);
+    rdmult = (rdmult + 8) >> 4;
+    rdmult = std::max<int64_t>(rdmult, 1);
+    return (uint32_t)((rdmult * 128) >> 7);
+}
+
+// pick_filter_levels_key_frame (deblock.rs:55-81).
+void key_frame_levels(int q, int bd, uint8_t out[4]) {
+    int fg;
+    if (bd == 8) {
+        const int qs = zf_ac_qlookup_8[q];
+        fg = (qs * 17563 - 421574 + (1 << 17)) >> 18;
+    } else {
+        const int qs = zf_ac_qlookup_10[q];
+        fg = ((qs * 20723 + 4060632 + (1 << 19)) >> 20) - 4;
+    }
+    const int fc = fg / 2;
+    const uint8_t y = (uint8_t)std::min(std::max(fg, 0), 63), uv = (uint8_t)std::min(std::max(fc, 0), 63);
+    out[0] = out[1] = y;
+    out[2] = out[3] = uv;
+}
+
+// pick_cdef_params_key_frame (cdef.rs:151-206): f32 + roundf (intra arm) or
+// f64 + truncation (screen arm). Compiled with -ffp-contract=off.
+void cdef_qp_params(int q, int bd, bool screen, int out[3]) {
+    const int q_raw = bd == 8 ? zf_ac_qlookup_8[q] : zf_ac_qlookup_10[q];
+    const int qi = q_raw >> (bd - 8);
+    int y1, y2, u1, u2;
+    if (screen) {
+        const double d = (double)qi;
+        y1 = (int)(5.88217781e-06 * d * d + 6.10391455e-03 * d + 9.95043102e-02);
+        y2 = (int)(-7.79934857e-06 * d * d + 6.58957830e-03 * d + 8.81045025e-01);
+        u1 = (int)(-6.79500136e-06 * d * d + 1.02695586e-02 * d + 1.36126802e-01);
+        u2 = (int)(-9.99613695e-08 * d * d - 1.79361339e-05 * d + 1.17022324e+0);
+    } else {
+        const float f = (float)qi;
+        y1 = (int)roundf(f * f * 0.0000033731974f + f * 0.008070594f + 0.0187634f);
+        y2 = (int)roundf(f * f * 0.0000029167343f + f * 0.0027798624f + 0.0079405f);
+        u1 = (int)roundf(f * f * -0.0000130790995f + f * 0.012892405f - 0.00748388f);
+        u2 = (int)roundf(f * f * 0.0000032651783f + f * 0.00035520183f + 0.00228092f);
+    }
+    auto cl = [](int v, int hi) { return std::min(std::max(v, 0), hi); };
+    out[0] = 3 + (q >> 6);
+    out[1] = cl(y1, 15) * 4 + cl(y2, 3);
+    out[2] = cl(u1, 15) * 4 + cl(u2, 3);
+}
+
+// cdef_search_cfg_for_preset (cdef.rs:788-810).
+void cdef_search_cfg(int preset, CdefParams &cp) {
+    static const int PF[16] = {0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40, 44, 48, 52, 56, 60};
+    std::vector<int> first, extra;
+    if (preset == 0) {
+        first = {0, 1, 2, 4, 5, 6, 8, 9, 10, 12, 13, 14};
+        extra = {1, 2, 3};
+    } else if (preset <= 3) {
+        first = {0, 4, 8, 12, 15};
+        extra = {1, 2, 3};
+    } else if (preset <= 5) {
+        first = {0, 7, 15};
+        extra = {2};
+    } else {
+        first = {0, 15};
+        extra = {2};
+    }
+    int n = 0;
+    for (int i : first) cp.fs[n++] = PF[i];
+    cp.first_pass_num = n;
+    for (int i : first)
+        for (int d : extra) cp.fs[n++] = PF[i] + d;
+    cp.ncand = n;
+    const int sub = preset >= 6 ? 4 : 1;
+    cp.sub_y = std::min(sub, 4);
+    cp.sub_uv = std::min(sub, 1);
+}
+
+int count_units_in_tile(int unit, int size) { return std::max((size + (unit >> 1)) / unit, 1); }
+
+// foreach_rest_unit_in_tile (svtav1-dsp/src/restoration.rs:1395-1448).
+void rest_units(int pw, int ph, int ss, std::vector<UnitRect> &out) {
+    const int unit = 256, ext = unit * 3 / 2;
+    out.clear();
+    for (int y0 = 0; y0 < ph;) {
+        const int rh = ph - y0, h = rh < ext ? rh : unit;
+        UnitRect r;
+        r.v_start = y0;
+        r.v_end = y0 + h;
+        const int voff = 8 >> ss;
+        r.v_start = std::max(0, r.v_start - voff);
+        if (r.v_end < ph) r.v_end -= voff;
+        for (int x0 = 0; x0 < pw;) {
+            const int rw = pw - x0, w = rw < ext ? rw : unit;
+            r.h_start = x0;
+            r.h_end = x0 + w;
+            out.push_back(r);
+            x0 += w;
+        }
+        y0 += h;
+    }
+}
+
+// The deblock level hill-climb of search_filter_level (deblock.rs:307-411)
+// replayed over the SSEs measured so far: returns the levels that the next
+// step needs (both candidates of a step are requested together), or marks
+// the search done.
+struct HillClimb {
+    int64_t err[64];
+    bool have[64];
+    int conv_th = 0;
+    bool done = false;
+    int result = 0;
+    HillClimb() {
+        for (int i = 0; i < 64; ++i) {
+            err[i] = 0;
+            have[i] = false;
+        }
+    }
+    int needs(int out[2]) {
+        if (!have[0]) {
+            out[0] = 0;
+            out[1] = 4;
+            return 2;
+        }
+        int dir = 0, mid = 0, step = 4, best = 0, conv = 0;
+        int64_t best_err = err[0];
+        while (step > 0) {
+            const int hi = std::min(mid + step, 63), lo = std::max(mid - step, 0);
+            int64_t bias = (best_err >> (15 - (mid / 8))) * (int64_t)step;
+            bias >>= 1;
+            const bool need_lo = dir <= 0 && lo != mid, need_hi = dir >= 0 && hi != mid;
+            int n = 0;
+            if (need_lo && !have[lo]) out[n++] = lo;
+            if (need_hi && !have[hi]) out[n++] = hi;
+            if (n) return n;
+            if (need_lo && err[lo] < best_err + bias) {
+                if (err[lo] < best_err) best_err = err[lo];
+                best = lo;
+            }
+            if (need_hi && err[hi] < best_err - bias) {
+                best_err = err[hi];
+                best = hi;
+            }
+            if (best == mid) {
+                conv += 1;
+                if (conv == conv_th) step = 0;
+                else step /= 2;
+                dir = 0;
+            } else {
+                dir = best < mid ? -1 : 1;
+                mid = best;
+            }
+        }
+        done = true;
+        result = best;
+        return 0;
+    }
+};
+
+// ---- per-frame plan -------------------------------------------------------
+
+struct Plan {
+    const zf_frame *in = nullptr;
+    zf_decisions *out = nullptr;
+    FrameDesc d;
+    size_t px = 1;                    // bytes per pixel
+    size_t pbytes[3] = {0, 0, 0};     // plane bytes (aligned canvas)
+    int nplanes = 1;
+    int nfb = 0;
+    size_t off_set[3][3];             // [set A/B/C][plane]
+    size_t off_src[3];
+    size_t off_mi = 0, off_mse = 0, off_fbrow = 0, off_fbidx = 0, off_best = 0, off_stats = 0;
+    size_t off_rects[3], off_units[3];
+    std::vector<UnitRect> rects[3];
+    int hunits[3], vunits[3];
+    bool db_search = false;
+};
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) & ~(a - 1); }
+
+int validate_frame(zf_ctx *ctx, const zf_frame *f) {
+    if (!f) return fail(ctx, ZF_ERR_ARG, "frame is NULL");
+    if (f->bit_depth != 8 && f->bit_depth != 10) return fail(ctx, ZF_ERR_UNSUPPORTED, "bit_depth must be 8 or 10");
+    if (f->width <= 0 || f->height <= 0 || (f->width & 7) || (f->height & 7))
+        return fail(ctx, ZF_ERR_INVALID_DIMS, "width/height must be positive multiples of 8");
+    if (f->true_width <= 0 || f->true_height <= 0 || f->true_width > f->width || f->true_height > f->height)
+        return fail(ctx, ZF_ERR_INVALID_DIMS, "true dims must be in (0, aligned dims]");
+    if (f->width > 16384 || f->height > 16384) return fail(ctx, ZF_ERR_INVALID_DIMS, "frame larger than 16384");
+    if (f->qindex < 0 || f->qindex > 255 || f->preset < 0 || f->preset > 13 || f->sharpness < 0 || f->sharpness > 7)
+        return fail(ctx, ZF_ERR_ARG, "qindex/preset/sharpness out of range");
+    if (!f->src[0] || !f->rec[0] || !f->mi) return fail(ctx, ZF_ERR_ARG, "missing plane or geometry pointer");
+    if (f->chroma_420 && (!f->src[1] || !f->src[2] || !f->rec[1] || !f->rec[2]))
+        return fail(ctx, ZF_ERR_ARG, "missing chroma plane");
+    return ZF_OK;
+}
+
+bool lr_enabled(const zf_frame *f) {
+    return f->enable_restoration && f->preset <= 6 && f->true_width >= 64 && f->true_height >= 64;
+}
+
+void plan_frame(Plan &p, const zf_frame *f, size_t &cursor) {
+    p.in = f;
+    std::memset(&p.d, 0, sizeof(p.d));
+    FrameDesc &d = p.d;
+    d.bd = f->bit_depth;
+    d.w = f->width;
+    d.h = f->height;
+    d.tw = f->true_width;
+    d.th = f->true_height;
+    d.chroma = f->chroma_420 ? 1 : 0;
+    d.preset = f->preset;
+    d.qindex = f->qindex;
+    d.sharpness = f->sharpness;
+    d.mi_cols = f->width / 4;
+    d.mi_rows = f->height / 4;
+    d.nhfb = (f->width + 63) / 64;
+    d.nvfb = (f->height + 63) / 64;
+    p.nfb = d.nhfb * d.nvfb;
+    p.px = f->bit_depth == 8 ? 1 : 2;
+    p.nplanes = f->chroma_420 ? 3 : 1;
+    p.pbytes[0] = (size_t)f->width * f->height * p.px;
+    p.pbytes[1] = p.pbytes[2] = (size_t)(f->width / 2) * (f->height / 2) * p.px;
+    auto take = [&](size_t n) {
+        cursor = align_up(cursor, 256);
+        size_t o = cursor;
+        cursor += n;
+        return o;
+    };
+    for (int s = 0; s < 3; ++s)
+        for (int pl = 0; pl < 3; ++pl) p.off_set[s][pl] = pl < p.nplanes ? take(p.pbytes[pl]) : 0;
+    for (int pl = 0; pl < 3; ++pl) p.off_src[pl] = pl < p.nplanes ? take(p.pbytes[pl]) : 0;
+    p.off_mi = take((size_t)d.mi_cols * d.mi_rows * 4);
+    p.off_mse = take((size_t)p.nfb * 2 * zf::kMaxCand * 8);
+    p.off_fbrow = take(p.nfb);
+    p.off_fbidx = take(p.nfb);
+    p.off_best = take((size_t)p.nfb * 8);
+    p.off_stats = take(4 * 8);
+    // CDEF policy (pipeline.rs:3042-3144).
+    CdefParams &cp = d.cdef;
+    if (f->preset <= 6) {
+        cp.mode = 1;
+        cdef_search_cfg(f->preset, cp);
+        cp.damping = 3 + (f->qindex >> 6);
+        cp.lambda = f->bit_depth == 8 ? lambda_8bit_unweighted(f->qindex) : lambda_bd10_unweighted(f->qindex);
+    } else {
+        int q[3];
+        cdef_qp_params(f->qindex, f->bit_depth, f->sc_class5 != 0, q);
+        cp.mode = 2;
+        cp.damping = q[0];
+        cp.bits = 0;
+        cp.y_str[0] = (uint8_t)q[1];
+        cp.uv_str[0] = (uint8_t)q[2];
+    }
+    // Loop restoration (pipeline.rs:3225-3381).
+    d.lr_on = lr_enabled(f) ? 1 : 0;
+    d.rdmult = f->bit_depth == 10 ? (int64_t)lambda_bd10_unweighted(f->qindex) * 16
+                                  : (int64_t)lambda_8bit_unweighted(f->qindex);
+    for (int pl = 0; pl < 3; ++pl) {
+        const int ss = pl ? 1 : 0;
+        const int pw = pl ? (f->true_width + 1) / 2 : f->true_width;
+        const int ph = pl ? (f->true_height + 1) / 2 : f->true_height;
+        p.hunits[pl] = count_units_in_tile(256, pw);
+        p.vunits[pl] = count_units_in_tile(256, ph);
+        LrPlane &L = d.lr[pl];
+        L.on = d.lr_on && (pl == 0 || f->chroma_420);
+        L.win = 5;  // filter_tap_lvl 2 at every enabled preset (restoration.rs:82-107)
+        L.pw = pw;
+        L.ph = ph;
+        L.stride = pl ? f->width / 2 : f->width;
+        L.hunits = p.hunits[pl];
+        L.vunits = p.vunits[pl];
+        L.refine = f->preset <= 3;
+        rest_units(pw, ph, ss, p.rects[pl]);
+        p.off_rects[pl] = take(p.rects[pl].size() * sizeof(UnitRect));
+        p.off_units[pl] = take(L.on ? p.rects[pl].size() * sizeof(LrUnit) : 0);
+    }
+    p.db_search = f->preset <= 5;
+}
+
+void bind_pointers(Plan &p, uint8_t *base) {
+    FrameDesc &d = p.d;
+    for (int pl = 0; pl < 3; ++pl) {
+        const bool on = pl < p.nplanes;
+        d.A[pl] = on ? base + p.off_set[0][pl] : nullptr;
+        d.B[pl] = on ? base + p.off_set[1][pl] : nullptr;
+        d.C[pl] = on ? base + p.off_set[2][pl] : nullptr;
+        d.S[pl] = on ? base + p.off_src[pl] : nullptr;
+        d.lr[pl].rects = (UnitRect *)(base + p.off_rects[pl]);
+        d.lr[pl].units = d.lr[pl].on ? (LrUnit *)(base + p.off_units[pl]) : nullptr;
+    }
+    d.mi = (const uint32_t *)(base + p.off_mi);
+    d.mse = (uint64_t *)(base + p.off_mse);
+    d.fb_row = base + p.off_fbrow;
+    d.fb_idx = base + p.off_fbidx;
+    d.cdef_best = (uint64_t *)(base + p.off_best);
+    d.cdef_stats = (unsigned long long *)(base + p.off_stats);
+}
+
+int ensure_arena(zf_ctx *ctx, size_t need) {
+    if (ctx->budget && need > ctx->budget)
+        return fail(ctx, ZF_ERR_ALLOC, "device footprint " + std::to_string(need) + " exceeds the HBM budget");
+    if (need <= ctx->arena_cap) return ZF_OK;
+    if (ctx->arena) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->arena);
+        ctx->arena = nullptr;
+        ctx->arena_cap = 0;
+    }
+    size_t cap = align_up(need + need / 8, 1 << 20);
+    if (cudaMalloc((void **)&ctx->arena, cap) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, ZF_ERR_ALLOC, "cudaMalloc of the device arena failed");
+    }
+    ctx->arena_cap = cap;
+    return ZF_OK;
+}
+
+int check_cancel(zf_ctx *ctx) {
+    if (ctx->cancel && *ctx->cancel) {
+        cudaStreamSynchronize(ctx->stream);
+        return fail(ctx, ZF_ERR_CANCELLED, "cancelled");
+    }
+    return ZF_OK;
+}
+
+// Copy a plane between caller memory (host or device) and the arena.
+int copy_in(zf_ctx *ctx, void *dst, const void *src, size_t n, bool on_device) {
+    CU(cudaMemcpyAsync(dst, src, n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->stream));
+    return ZF_OK;
+}
+int copy_out(zf_ctx *ctx, void *dst, const void *src, size_t n, bool on_device) {
+    CU(cudaMemcpyAsync(dst, src, n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
+    return ZF_OK;
+}
+
+// Work lists: one item per tile range; CTA ranges are prefix sums.
+struct WorkList {
+    std::vector<WorkItem> items;
+    int ctas = 0;
+    void add(int frame, int plane, int a, int b, int n) {
+        if (n <= 0) return;
+        WorkItem w;
+        w.frame = frame;
+        w.plane = plane;
+        w.a = a;
+        w.b = b;
+        w.cta_begin = ctas;
+        w.ctas = n;
+        items.push_back(w);
+        ctas += n;
+    }
+};
+
+int upload_list(zf_ctx *ctx, const WorkList &wl, uint8_t *dst) {
+    if (wl.items.empty()) return ZF_OK;
+    CU(cudaMemcpyAsync(dst, wl.items.data(), wl.items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    return ZF_OK;
+}
+
+int launch_check(zf_ctx *ctx, const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, ZF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return ZF_OK;
+}
+
+#define TRY(x)                  \
+    do {                        \
+        int r_ = (x);           \
+        if (r_ != ZF_OK) return r_; \
+    } while (0)
+
+int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf_stats *stats, const Run &run) {
+    if (!ctx) return ZF_ERR_ARG;
+    if (n <= 0 || !frames) return fail(ctx, ZF_ERR_ARG, "empty batch");
+    CU(cudaSetDevice(ctx->device));
+    TRY(check_cancel(ctx));
+    std::vector<Plan> plans((size_t)n);
+    size_t cursor = 0;
+    for (int i = 0; i < n; ++i) {
+        TRY(validate_frame(ctx, &frames[i]));
+        plan_frame(plans[i], &frames[i], cursor);
+        plans[i].out = outs ? &outs[i] : nullptr;
+    }
+    // Work lists (host-known shapes).
+    WorkList wl_db, wl_cs, wl_ca, wl_sum, wl_st5, wl_st7, wl_unit, wl_apply;
+    std::vector<int> cdef_frames;
+    for (int i = 0; i < n; ++i) {
+        Plan &p = plans[i];
+        for (int pl = 0; pl < p.nplanes; ++pl) {
+            const int pw = pl ? p.d.w / 2 : p.d.w, ph = pl ? p.d.h / 2 : p.d.h;
+            wl_db.add(i, pl, 0, 0, ((pw + 63) / 64) * ((ph + 63) / 64));
+        }
+        if (p.d.cdef.mode == 1 && !run.cdef_given) {
+            wl_cs.add(i, 0, 0, 0, p.nfb);
+            cdef_frames.push_back(i);
+        }
+        wl_ca.add(i, 0, 0, 0, p.nfb);
+        for (int pl = 0; pl < 3; ++pl) {
+            const LrPlane &L = p.d.lr[pl];
+            if (!L.on) continue;
+            for (size_t u = 0; u < p.rects[pl].size(); ++u) {
+                const UnitRect &r = p.rects[pl][u];
+                const int uh = r.v_end - r.v_start;
+                for (int c = 0; c < uh; c += zf::kSumRowsHost) wl_sum.add(i, pl, (int)u, c, 1);
+                for (int c = 0; c < uh; c += zf::kStatRowsHost) (L.win == 5 ? wl_st5 : wl_st7).add(i, pl, (int)u, c, 1);
+                wl_unit.add(i, pl, (int)u, 0, 1);
+            }
+            const int ss = pl ? 1 : 0, full = 64 >> ss, off = 8 >> ss;
+            const int nstripes = (L.ph + off + full - 1) / full;
+            const int ntiles = (L.pw + 63) / 64;
+            // unit of a (stripe, tile): rows and columns of the unit grid
+            for (int s = 0; s < nstripes; ++s) {
+                const int ys = std::max(0, s * full - off);
+                for (int t = 0; t < ntiles; ++t) {
+                    const int x = t * 64;
+                    int uidx = -1;
+                    for (size_t u = 0; u < p.rects[pl].size(); ++u) {
+                        const UnitRect &r = p.rects[pl][u];
+                        if (ys >= r.v_start && ys < r.v_end && x >= r.h_start && x < r.h_end) {
+                            uidx = (int)u;
+                            break;
+                        }
+                    }
+                    if (uidx >= 0) wl_apply.add(i, pl, uidx, (s << 16) | t, 1);
+                }
+            }
+        }
+    }
+    const size_t desc_bytes = align_up((size_t)n * sizeof(FrameDesc), 256);
+    auto lsz = [](const WorkList &w) { return align_up(w.items.size() * sizeof(WorkItem) + 16, 256); };
+    const size_t o_desc = align_up(cursor, 256);
+    size_t c2 = o_desc + desc_bytes;
+    const size_t o_db = c2;
+    c2 += lsz(wl_db);
+    const size_t o_cs = c2;
+    c2 += lsz(wl_cs);
+    const size_t o_ca = c2;
+    c2 += lsz(wl_ca);
+    const size_t o_sum = c2;
+    c2 += lsz(wl_sum);
+    const size_t o_st5 = c2;
+    c2 += lsz(wl_st5);
+    const size_t o_st7 = c2;
+    c2 += lsz(wl_st7);
+    const size_t o_unit = c2;
+    c2 += lsz(wl_unit);
+    const size_t o_apply = c2;
+    c2 += lsz(wl_apply);
+    const size_t o_cf = c2;
+    c2 += align_up(cdef_frames.size() * 4 + 16, 256);
+    // deblock search scratch: up to 3 slots per frame
+    const size_t o_dbs_items = c2;
+    c2 += align_up((size_t)n * 3 * 8 * sizeof(WorkItem) + 16, 256);
+    const size_t o_dbs_lv = c2;
+    c2 += align_up((size_t)n * 3 * 2 * 4, 256);
+    const size_t o_dbs_sse = c2;
+    c2 += align_up((size_t)n * 3 * 2 * 8, 256);
+    TRY(ensure_arena(ctx, c2));
+    uint8_t *base = ctx->arena;
+    cudaStream_t st = ctx->stream;
+    for (auto &p : plans) bind_pointers(p, base);
+    FrameDesc *d_desc = (FrameDesc *)(base + o_desc);
+
+    // ---- inputs
+    for (int i = 0; i < n; ++i) {
+        Plan &p = plans[i];
+        const zf_frame *f = p.in;
+        const bool dev = f->planes_on_device != 0;
+        const int set = run.rec_in;
+        for (int pl = 0; pl < p.nplanes; ++pl) {
+            TRY(copy_in(ctx, base + p.off_set[set][pl], f->rec[pl], p.pbytes[pl], dev));
+            TRY(copy_in(ctx, base + p.off_src[pl], f->src[pl], p.pbytes[pl], dev));
+            if (run.pre_cdef_in) TRY(copy_in(ctx, base + p.off_set[SET_B][pl], run.pre_cdef[pl], p.pbytes[pl], dev));
+        }
+        TRY(copy_in(ctx, base + p.off_mi, f->mi, (size_t)p.d.mi_cols * p.d.mi_rows * 4, dev));
+        for (int pl = 0; pl < 3; ++pl)
+            if (!p.rects[pl].empty())
+                CU(cudaMemcpyAsync(base + p.off_rects[pl], p.rects[pl].data(), p.rects[pl].size() * sizeof(UnitRect),
+                                   cudaMemcpyHostToDevice, st));
+        CU(cudaMemsetAsync(base + p.off_stats, 0, 32, st));
+        // decisions the caller provides
+        const zf_decisions *dec = p.out;
+        if (run.lf_given) std::memcpy(p.d.lf, dec->lf, 4);
+        if (run.cdef_given) {
+            CdefParams &cp = p.d.cdef;
+            cp.mode = 2;
+            cp.damping = dec->cdef_damping;
+            cp.bits = dec->cdef_bits;
+            std::memcpy(cp.y_str, dec->cdef_y, 8);
+            std::memcpy(cp.uv_str, dec->cdef_uv, 8);
+            if (cp.bits) {
+                if (!dec->cdef_fb_idx) return fail(ctx, ZF_ERR_ARG, "cdef_bits > 0 needs cdef_fb_idx");
+                CU(cudaMemcpyAsync(base + p.off_fbidx, dec->cdef_fb_idx, p.nfb, cudaMemcpyHostToDevice, st));
+            }
+        }
+        if (run.lr_given) {
+            for (int pl = 0; pl < 3; ++pl) {
+                LrPlane &L = p.d.lr[pl];
+                if (pl >= p.nplanes) {
+                    L.on = 0;
+                    continue;
+                }
+                L.on = dec->lr[pl].frame_rtype != ZF_RESTORE_NONE;
+                L.frame_rtype = dec->lr[pl].frame_rtype;
+                if (!L.on) continue;
+                if (dec->lr[pl].hunits != p.hunits[pl] || dec->lr[pl].vunits != p.vunits[pl] || !dec->lr_units[pl])
+                    return fail(ctx, ZF_ERR_ARG, "restoration unit grid does not match the frame");
+                const size_t nu = p.rects[pl].size();
+                std::vector<LrUnit> hu(nu);
+                std::memset(hu.data(), 0, nu * sizeof(LrUnit));
+                for (size_t u = 0; u < nu; ++u) {
+                    hu[u].rtype = dec->lr_units[pl][u].rtype;
+                    std::memcpy(hu[u].vf, dec->lr_units[pl][u].vfilter, 16);
+                    std::memcpy(hu[u].hf, dec->lr_units[pl][u].hfilter, 16);
+                }
+                // units storage exists only for searched planes; reuse the
+                // rects offset region sizing by re-planning is avoided by
+                // requiring the plane to be LR-enabled at plan time.
+                if (!p.d.lr[pl].units) return fail(ctx, ZF_ERR_UNSUPPORTED, "restoration disabled for this frame");
+                CU(cudaMemcpyAsync(p.d.lr[pl].units, hu.data(), nu * sizeof(LrUnit), cudaMemcpyHostToDevice, st));
+            }
+        }
+    }
+
+    // ---- deblock level pick (presets <= 5: device SSE trials + host hill-climb)
+    if (run.stages & STG_DB_PICK) {
+        struct Slot {
+            int frame, plane;
+            HillClimb hc;
+        };
+        std::vector<Slot> slots;
+        for (int i = 0; i < n; ++i) {
+            Plan &p = plans[i];
+            if (p.db_search) {
+                Slot s{i, 0, HillClimb()};
+                s.hc.conv_th = p.in->preset <= 3 ? 0 : 1;
+                slots.push_back(s);
+            } else {
+                key_frame_levels(p.in->qindex, p.in->bit_depth, p.d.lf);
+            }
+        }
+        {
+            std::vector<FrameDesc> hd((size_t)n);
+            for (int i = 0; i < n; ++i) hd[i] = plans[i].d;
+            CU(cudaMemcpyAsync(d_desc, hd.data(), (size_t)n * sizeof(FrameDesc), cudaMemcpyHostToDevice, st));
+            CU(cudaStreamSynchronize(st));
+        }
+        bool chroma_phase = false;
+        for (int guard = 0; guard < 256 && !slots.empty(); ++guard) {
+            WorkList wl;
+            std::vector<int> lv;
+            std::vector<int> owner;
+            for (size_t k = 0; k < slots.size(); ++k) {
+                Slot &s = slots[k];
+                if (s.hc.done) continue;
+                int need[2];
+                const int m = s.hc.needs(need);
+                if (m == 0) continue;
+                const int slot = (int)owner.size();
+                owner.push_back((int)k);
+                lv.push_back(need[0]);
+                lv.push_back(m > 1 ? need[1] : -1);
+                const Plan &p = plans[s.frame];
+                const int pw = s.plane ? p.d.w / 2 : p.d.w, ph = s.plane ? p.d.h / 2 : p.d.h;
+                wl.add(s.frame, s.plane, slot, 0, ((pw + 63) / 64) * ((ph + 63) / 64));
+            }
+            if (owner.empty()) {
+                bool all_done = true;
+                for (auto &s : slots) all_done = all_done && s.hc.done;
+                if (!all_done) return fail(ctx, ZF_ERR_UNSUPPORTED, "deblock search stalled");
+                if (chroma_phase) break;
+                // luma finished: record levels, start chroma where luma > 0
+                std::vector<Slot> next;
+                for (auto &s : slots) {
+                    Plan &p = plans[s.frame];
+                    p.d.lf[0] = p.d.lf[1] = (uint8_t)s.hc.result;
+                    p.d.lf[2] = p.d.lf[3] = 0;
+                    if (s.hc.result != 0 && p.nplanes == 3)
+                        for (int pl = 1; pl <= 2; ++pl) {
+                            Slot c{s.frame, pl, HillClimb()};
+                            c.hc.conv_th = s.hc.conv_th;
+                            next.push_back(c);
+                        }
+                }
+                slots.swap(next);
+                chroma_phase = true;
+                continue;
+            }
+            if ((int)owner.size() > n * 3) return fail(ctx, ZF_ERR_UNSUPPORTED, "too many search slots");
+            CU(cudaMemcpyAsync(base + o_dbs_items, wl.items.data(), wl.items.size() * sizeof(WorkItem),
+                               cudaMemcpyHostToDevice, st));
+            CU(cudaMemcpyAsync(base + o_dbs_lv, lv.data(), lv.size() * 4, cudaMemcpyHostToDevice, st));
+            CU(cudaMemsetAsync(base + o_dbs_sse, 0, lv.size() * 8, st));
+            zf::k_deblock_sse<<<wl.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_dbs_items),
+                                                       (int)wl.items.size(), (const int *)(base + o_dbs_lv),
+                                                       (unsigned long long *)(base + o_dbs_sse));
+            TRY(launch_check(ctx, "k_deblock_sse"));
+            std::vector<unsigned long long> sse(lv.size());
+            CU(cudaMemcpyAsync(sse.data(), base + o_dbs_sse, sse.size() * 8, cudaMemcpyDeviceToHost, st));
+            CU(cudaStreamSynchronize(st));
+            TRY(check_cancel(ctx));
+            for (size_t sl = 0; sl < owner.size(); ++sl) {
+                Slot &s = slots[owner[sl]];
+                for (int k = 0; k < 2; ++k) {
+                    const int l = lv[sl * 2 + k];
+                    if (l < 0) continue;
+                    s.hc.err[l] = (int64_t)sse[sl * 2 + k];
+                    s.hc.have[l] = true;
+                }
+            }
+        }
+        if (chroma_phase)
+            for (auto &s : slots) plans[s.frame].d.lf[1 + s.plane] = (uint8_t)s.hc.result;
+    }
+
+    // ---- descriptors and work lists to the device
+    {
+        std::vector<FrameDesc> hd((size_t)n);
+        for (int i = 0; i < n; ++i) hd[i] = plans[i].d;
+        CU(cudaMemcpyAsync(d_desc, hd.data(), (size_t)n * sizeof(FrameDesc), cudaMemcpyHostToDevice, st));
+    }
+    TRY(upload_list(ctx, wl_db, base + o_db));
+    TRY(upload_list(ctx, wl_cs, base + o_cs));
+    TRY(upload_list(ctx, wl_ca, base + o_ca));
+    TRY(upload_list(ctx, wl_sum, base + o_sum));
+    TRY(upload_list(ctx, wl_st5, base + o_st5));
+    TRY(upload_list(ctx, wl_st7, base + o_st7));
+    TRY(upload_list(ctx, wl_unit, base + o_unit));
+    TRY(upload_list(ctx, wl_apply, base + o_apply));
+    if (!cdef_frames.empty())
+        CU(cudaMemcpyAsync(base + o_cf, cdef_frames.data(), cdef_frames.size() * 4, cudaMemcpyHostToDevice, st));
+
+    // ---- deblock apply: A -> B
+    if (run.stages & STG_DB_APPLY) {
+        zf::k_deblock_apply<<<wl_db.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_db),
+                                                        (int)wl_db.items.size());
+        TRY(launch_check(ctx, "k_deblock_apply"));
+        TRY(check_cancel(ctx));
+    }
+    // ---- CDEF search + finish on B
+    if ((run.stages & STG_CDEF_SEARCH) && !cdef_frames.empty()) {
+        zf::k_cdef_search<<<wl_cs.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_cs),
+                                                      (int)wl_cs.items.size());
+        TRY(launch_check(ctx, "k_cdef_search"));
+        zf::k_cdef_finish<<<(int)cdef_frames.size(), 1024, 0, st>>>(d_desc, (const int *)(base + o_cf));
+        TRY(launch_check(ctx, "k_cdef_finish"));
+        TRY(check_cancel(ctx));
+    }
+    // ---- CDEF apply: B -> A
+    if (run.stages & STG_CDEF_APPLY) {
+        zf::k_cdef_apply<<<wl_ca.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_ca), (int)wl_ca.items.size());
+        TRY(launch_check(ctx, "k_cdef_apply"));
+        TRY(check_cancel(ctx));
+    }
+    // ---- Wiener search on A
+    if ((run.stages & STG_LR_SEARCH) && !run.lr_given) {
+        for (int i = 0; i < n; ++i)
+            for (int pl = 0; pl < 3; ++pl)
+                if (plans[i].d.lr[pl].on)
+                    CU(cudaMemsetAsync(plans[i].d.lr[pl].units, 0, plans[i].rects[pl].size() * sizeof(LrUnit), st));
+        if (wl_sum.ctas) {
+            zf::k_lr_sums<<<wl_sum.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_sum),
+                                                      (int)wl_sum.items.size());
+            TRY(launch_check(ctx, "k_lr_sums"));
+        }
+        if (wl_st5.ctas) {
+            CU(zf::launch_lr_stats(5, wl_st5.ctas, st, d_desc, (const WorkItem *)(base + o_st5),
+                                   (int)wl_st5.items.size()));
+        }
+        if (wl_st7.ctas) {
+            CU(zf::launch_lr_stats(7, wl_st7.ctas, st, d_desc, (const WorkItem *)(base + o_st7),
+                                   (int)wl_st7.items.size()));
+        }
+        if (wl_unit.ctas) {
+            zf::k_lr_solve<<<wl_unit.ctas, 128, 0, st>>>(d_desc, (const WorkItem *)(base + o_unit),
+                                                        (int)wl_unit.items.size());
+            TRY(launch_check(ctx, "k_lr_solve"));
+            zf::k_lr_trial<<<wl_unit.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_unit),
+                                                        (int)wl_unit.items.size());
+            TRY(launch_check(ctx, "k_lr_trial"));
+        }
+        zf::k_lr_finish<<<(n * 3 + 127) / 128, 128, 0, st>>>(d_desc, n);
+        TRY(launch_check(ctx, "k_lr_finish"));
+        TRY(check_cancel(ctx));
+    }
+    // ---- Wiener apply: A (+ B boundary lines) -> C
+    if (run.stages & STG_LR_APPLY) {
+        for (int i = 0; i < n; ++i)
+            for (int pl = 0; pl < plans[i].nplanes; ++pl)
+                CU(cudaMemcpyAsync(base + plans[i].off_set[SET_C][pl], base + plans[i].off_set[SET_A][pl],
+                                   plans[i].pbytes[pl], cudaMemcpyDeviceToDevice, st));
+        if (wl_apply.ctas) {
+            zf::k_lr_apply<<<wl_apply.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_apply),
+                                                         (int)wl_apply.items.size());
+            TRY(launch_check(ctx, "k_lr_apply"));
+        }
+    }
+
+    // ---- outputs
+    std::vector<FrameDesc> back((size_t)n);
+    CU(cudaMemcpyAsync(back.data(), d_desc, (size_t)n * sizeof(FrameDesc), cudaMemcpyDeviceToHost, st));
+    std::vector<std::vector<uint8_t>> fbidx((size_t)n), fbrow((size_t)n);
+    std::vector<std::vector<unsigned long long>> cst((size_t)n);
+    std::vector<std::vector<LrUnit>> units((size_t)n * 3);
+    for (int i = 0; i < n; ++i) {
+        Plan &p = plans[i];
+        const zf_frame *f = p.in;
+        const bool dev = f->planes_on_device != 0;
+        if (run.stages & (STG_DB_APPLY | STG_CDEF_APPLY | STG_LR_APPLY))
+            for (int pl = 0; pl < p.nplanes; ++pl)
+                TRY(copy_out(ctx, f->rec[pl], base + p.off_set[run.rec_out][pl], p.pbytes[pl], dev));
+        fbidx[i].resize(p.nfb);
+        fbrow[i].resize(p.nfb);
+        cst[i].resize(4);
+        CU(cudaMemcpyAsync(fbidx[i].data(), base + p.off_fbidx, p.nfb, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(fbrow[i].data(), base + p.off_fbrow, p.nfb, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(cst[i].data(), base + p.off_stats, 32, cudaMemcpyDeviceToHost, st));
+        if (run.stages & STG_LR_SEARCH)
+            for (int pl = 0; pl < 3; ++pl)
+                if (p.d.lr[pl].on) {
+                    units[(size_t)i * 3 + pl].resize(p.rects[pl].size());
+                    CU(cudaMemcpyAsync(units[(size_t)i * 3 + pl].data(), p.d.lr[pl].units,
+                                       p.rects[pl].size() * sizeof(LrUnit), cudaMemcpyDeviceToHost, st));
+                }
+    }
+    CU(cudaStreamSynchronize(st));
+    TRY(launch_check(ctx, "stream"));
+    for (int i = 0; i < n; ++i) {
+        Plan &p = plans[i];
+        const FrameDesc &b = back[i];
+        zf_decisions *o = p.out;
+        if (o) {
+            if (run.stages & STG_DB_PICK) std::memcpy(o->lf, p.d.lf, 4);
+            o->nhfb = b.nhfb;
+            o->nvfb = b.nvfb;
+            if ((run.stages & STG_CDEF_SEARCH) && !run.cdef_given) {
+                o->cdef_damping = (uint8_t)b.cdef.damping;
+                o->cdef_bits = (uint8_t)b.cdef.bits;
+                std::memcpy(o->cdef_y, b.cdef.y_str, 8);
+                std::memcpy(o->cdef_uv, b.cdef.uv_str, 8);
+                if (o->cdef_fb_idx)
+                    for (int k = 0; k < p.nfb; ++k) o->cdef_fb_idx[k] = b.cdef.bits ? fbidx[i][k] : 0;
+            }
+            if ((run.stages & STG_LR_SEARCH) && !run.lr_given) {
+                for (int pl = 0; pl < 3; ++pl) {
+                    o->lr[pl].frame_rtype = b.lr[pl].on ? b.lr[pl].frame_rtype : ZF_RESTORE_NONE;
+                    o->lr[pl].unit_size = 256;
+                    o->lr[pl].hunits = p.hunits[pl];
+                    o->lr[pl].vunits = p.vunits[pl];
+                    if (!o->lr_units[pl]) continue;
+                    const size_t nu = (size_t)p.hunits[pl] * p.vunits[pl];
+                    const std::vector<LrUnit> &uu = units[(size_t)i * 3 + pl];
+                    for (size_t u = 0; u < nu; ++u) {
+                        zf_lr_unit &lu = o->lr_units[pl][u];
+                        std::memset(&lu, 0, sizeof(lu));
+                        if (uu.empty()) {
+                            static const int16_t def[8] = {3, -7, 15, -22, 15, -7, 3, 0};
+                            std::memcpy(lu.vfilter, def, 16);
+                            std::memcpy(lu.hfilter, def, 16);
+                            continue;
+                        }
+                        lu.rtype = (uint8_t)uu[u].rtype;
+                        std::memcpy(lu.vfilter, uu[u].vf, 16);
+                        std::memcpy(lu.hfilter, uu[u].hf, 16);
+                    }
+                }
+            }
+        }
+        if (stats) {
+            zf_stats &s = stats[i];
+            std::memset(&s, 0, sizeof(s));
+            s.cdef_filtered_px = cst[i][0];
+            s.cdef_changed_px = cst[i][1];
+            int sbc = 0;
+            for (int k = 0; k < p.nfb; ++k) sbc += fbrow[i][k];
+            s.cdef_sb_count = sbc;
+            for (int pl = 0; pl < 3; ++pl) {
+                s.lr_frame_rtype[pl] = b.lr[pl].on ? b.lr[pl].frame_rtype : 0;
+                if (b.lr[pl].on && b.lr[pl].frame_rtype && !units[(size_t)i * 3 + pl].empty())
+                    for (auto &u : units[(size_t)i * 3 + pl]) s.lr_wiener_units += u.rtype == 1;
+            }
+        }
+    }
+    return ZF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t zf_abi_version(void) { return ZF_ABI_VERSION; }
+
+int32_t zf_create(zf_ctx **out, const zf_opts *opts) {
+    if (!out) return ZF_ERR_ARG;
+    *out = nullptr;
+    zf_ctx *c = new (std::nothrow) zf_ctx();
+    if (!c) return ZF_ERR_ALLOC;
+    c->device = opts ? opts->device : 0;
+    c->budget = opts ? opts->hbm_budget_bytes : 0;
+    c->cancel = opts ? opts->cancel_flag : nullptr;
+    if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        return ZF_ERR_CUDA;
+    }
+    *out = c;
+    return ZF_OK;
+}
+
+void zf_destroy(zf_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->arena) cudaFree(ctx->arena);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *zf_last_error(const zf_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int32_t zf_sync(zf_ctx *ctx) {
+    if (!ctx) return ZF_ERR_ARG;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return ZF_OK;
+}
+
+int32_t zf_query_sizes(const zf_frame *f, zf_sizes *out) {
+    if (!f || !out) return ZF_ERR_ARG;
+    int e = validate_frame(nullptr, f);
+    if (e) return e;
+    Plan p;
+    size_t cursor = 0;
+    plan_frame(p, f, cursor);
+    std::memset(out, 0, sizeof(*out));
+    out->nhfb = p.d.nhfb;
+    out->nvfb = p.d.nvfb;
+    for (int pl = 0; pl < 3; ++pl) {
+        out->lr_hunits[pl] = p.hunits[pl];
+        out->lr_vunits[pl] = p.vunits[pl];
+    }
+    out->lr_unit_size = 256;
+    out->device_bytes = cursor;
+    return ZF_OK;
+}
+
+int32_t zf_pack_geom(int32_t mi_cols, int32_t mi_rows, const uint32_t *block_id, const uint8_t *bw,
+                     const uint8_t *bh, const uint8_t *tw, const uint8_t *th, const uint8_t *skip,
+                     const uint8_t *skip_inter, uint32_t *out) {
+    if (mi_cols <= 0 || mi_rows <= 0 || !block_id || !bw || !bh || !tw || !th || !skip || !skip_inter || !out)
+        return ZF_ERR_ARG;
+    auto lg = [](int v, int lo, int hi) -> int {
+        if (v < lo || v > hi || (v & (v - 1))) return -1;
+        int l = 0;
+        while ((4 << l) < v) ++l;
+        return l;
+    };
+    for (int r = 0; r < mi_rows; ++r)
+        for (int c = 0; c < mi_cols; ++c) {
+            const size_t i = (size_t)r * mi_cols + c;
+            const int lbw = lg(bw[i], 4, 128), lbh = lg(bh[i], 4, 128), ltw = lg(tw[i], 4, 64), lth = lg(th[i], 4, 64);
+            if (lbw < 0 || lbh < 0 || ltw < 0 || lth < 0) return ZF_ERR_GEOM;
+            // Block alignment: block_id must be the aligned block origin.
+            const int orow = r & ~((bh[i] >> 2) - 1), ocol = c & ~((bw[i] >> 2) - 1);
+            if (block_id[i] != (uint32_t)((size_t)orow * mi_cols + ocol)) return ZF_ERR_GEOM;
+            // Transform tiling: the mi at the aligned TX origin (same row /
+            // column) carries the same transform dims.
+            const int tr = r & ~((th[i] >> 2) - 1), tc = c & ~((tw[i] >> 2) - 1);
+            const size_t ti = (size_t)tr * mi_cols + tc;
+            if (tw[ti] != tw[i] || th[ti] != th[i]) return ZF_ERR_GEOM;
+            out[i] = (uint32_t)lbw | ((uint32_t)lbh << 3) | ((uint32_t)ltw << 6) | ((uint32_t)lth << 9) |
+                     (skip[i] ? ZF_MI_SKIP : 0u) | (skip_inter[i] ? ZF_MI_SKIP_INTER : 0u);
+        }
+    return ZF_OK;
+}
+
+int32_t zf_filter_stage(zf_ctx *ctx, const zf_frame *f, zf_decisions *out, zf_stats *stats) {
+    if (!out) return fail(ctx, ZF_ERR_ARG, "decisions is NULL");
+    Run r{STG_ALL, SET_A, SET_C, false, nullptr, false, false, false};
+    return run_batch(ctx, f, 1, out, stats, r);
+}
+
+int32_t zf_submit_batch(zf_ctx *ctx, const zf_frame *frames, int32_t n, zf_decisions *outs, zf_stats *stats) {
+    if (!outs) return fail(ctx, ZF_ERR_ARG, "decisions is NULL");
+    Run r{STG_ALL, SET_A, SET_C, false, nullptr, false, false, false};
+    return run_batch(ctx, frames, n, outs, stats, r);
+}
+
+int32_t zf_deblock_pick(zf_ctx *ctx, const zf_frame *f, uint8_t lf[4]) {
+    if (!lf) return fail(ctx, ZF_ERR_ARG, "lf is NULL");
+    zf_decisions d;
+    std::memset(&d, 0, sizeof(d));
+    Run r{STG_DB_PICK, SET_A, SET_A, false, nullptr, false, false, false};
+    int e = run_batch(ctx, f, 1, &d, nullptr, r);
+    if (e == ZF_OK) std::memcpy(lf, d.lf, 4);
+    return e;
+}
+
+int32_t zf_deblock_apply(zf_ctx *ctx, const zf_frame *f, const uint8_t lf[4]) {
+    if (!lf) return fail(ctx, ZF_ERR_ARG, "lf is NULL");
+    zf_decisions d;
+    std::memset(&d, 0, sizeof(d));
+    std::memcpy(d.lf, lf, 4);
+    Run r{STG_DB_APPLY, SET_A, SET_B, false, nullptr, true, false, false};
+    return run_batch(ctx, f, 1, &d, nullptr, r);
+}
+
+int32_t zf_cdef_search(zf_ctx *ctx, const zf_frame *f, zf_decisions *out) {
+    if (!out) return fail(ctx, ZF_ERR_ARG, "decisions is NULL");
+    Run r{STG_CDEF_SEARCH, SET_B, SET_B, false, nullptr, false, false, false};
+    return run_batch(ctx, f, 1, out, nullptr, r);
+}
+
+int32_t zf_cdef_apply(zf_ctx *ctx, const zf_frame *f, const zf_decisions *d, zf_stats *stats) {
+    if (!d) return fail(ctx, ZF_ERR_ARG, "decisions is NULL");
+    zf_decisions dd = *d;
+    Run r{STG_CDEF_APPLY, SET_B, SET_A, false, nullptr, false, true, false};
+    return run_batch(ctx, f, 1, &dd, stats, r);
+}
+
+int32_t zf_lr_search(zf_ctx *ctx, const zf_frame *f, zf_decisions *out) {
+    if (!out) return fail(ctx, ZF_ERR_ARG, "decisions is NULL");
+    Run r{STG_LR_SEARCH, SET_A, SET_A, false, nullptr, false, false, false};
+    return run_batch(ctx, f, 1, out, nullptr, r);
+}
+
+int32_t zf_lr_apply(zf_ctx *ctx, const zf_frame *f, const void *const pre_cdef[3], const zf_decisions *d) {
+    if (!d || !pre_cdef) return fail(ctx, ZF_ERR_ARG, "decisions or pre_cdef is NULL");
+    zf_decisions dd = *d;
+    Run r{STG_LR_APPLY, SET_A, SET_C, true, pre_cdef, false, false, true};
+    return run_batch(ctx, f, 1, &dd, nullptr, r);
+}
+
+}  // extern "C"

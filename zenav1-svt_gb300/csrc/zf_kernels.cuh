@@ -1,0 +1,28 @@
+// zf_kernels.cuh -- kernel entry points of the filter stage (defined in
+// zf_deblock.cu, zf_cdef.cu, zf_lr.cu; launched from zf_host.cu).
+#pragma once
+
+#include "zf_dev.cuh"
+
+namespace zf {
+
+__global__ void k_deblock_apply(const FrameDesc *frames, const WorkItem *items, int nitems);
+__global__ void k_deblock_sse(const FrameDesc *frames, const WorkItem *items, int nitems, const int *levels,
+                              unsigned long long *sse);
+
+__global__ void k_cdef_search(const FrameDesc *frames, const WorkItem *items, int nitems);
+__global__ void k_cdef_finish(FrameDesc *frames, const int *frame_ids);
+__global__ void k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems);
+
+__global__ void k_lr_sums(FrameDesc *frames, const WorkItem *items, int nitems);
+cudaError_t launch_lr_stats(int win, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
+                            int nitems);
+__global__ void k_lr_solve(FrameDesc *frames, const WorkItem *items, int nitems);
+__global__ void k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems);
+__global__ void k_lr_finish(FrameDesc *frames, int nframes);
+__global__ void k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems);
+
+constexpr int kSumRowsHost = 16;   // k_lr_sums rows per CTA
+constexpr int kStatRowsHost = 16;  // k_lr_stats rows per CTA
+
+}  // namespace zf

@@ -1,0 +1,797 @@
+// zf_lr.cu -- Wiener loop restoration (search + apply) on the GPU.
+//
+// Reference: svtav1-dsp/src/restoration.rs (convolve :138-195 / :1820-1871,
+// find_average :198, compute_stats :567-632 / :1738-1807, the tap solver
+// :801-1056, stripes :1124-1385, sse_region :1666 / :1991) and
+// svtav1-encoder/src/restoration.rs (search :675-924, apply :992-1052).
+//
+// Search data path: the reference extends the post-CDEF plane by edge
+// replication (4 columns, 3 rows) before reading any window; every read
+// that reaches a kept output here clamps its coordinates to the true plane,
+// which is the same value. The search filters without stripe boundaries,
+// where the 64-row stripe split and the 16-rounded processing-unit width
+// change which call computes a pixel but not its value, so a unit is
+// filtered as one separable 2-D convolution.
+//
+// Integer regrouping: M and H are sums of exact integer products; this file
+// accumulates them in per-thread int32 partials over at most a few hundred
+// pixels (products <= 1023^2, so no overflow) and folds them into int64, the
+// same exact value the reference's per-pixel int64 accumulation reaches.
+#include <climits>
+
+#include "zf_dev.cuh"
+
+namespace zf {
+
+constexpr int64_t kTapScale = 1 << 16;
+constexpr int kStep = 128;  // WIENER_FILT_STEP
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__device__ __forceinline__ int plane_stride(const FrameDesc &f, int p) { return p ? f.w / 2 : f.w; }
+
+// ---------------------------------------------------------------------------
+// 1. Per-unit sums: find_average numerator and sse_region(src, dgd).
+// items: a = unit, b = first row of the chunk (relative to v_start).
+// ---------------------------------------------------------------------------
+constexpr int kSumRows = 16;
+
+__global__ void __launch_bounds__(256) k_lr_sums(FrameDesc *frames, const WorkItem *items, int nitems) {
+    __shared__ unsigned long long red[4][8];
+    const int it = find_item(items, nitems, blockIdx.x);
+    const WorkItem wi = items[it];
+    FrameDesc &f = frames[wi.frame];
+    const LrPlane &pl = f.lr[wi.plane];
+    const UnitRect r = pl.rects[wi.a];
+    LrUnit &u = pl.units[wi.a];
+    const int bd = f.bd, stride = plane_stride(f, wi.plane);
+    const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
+    const int dw = uw % 16, dh = uh % 16;
+    const int i0 = wi.b, i1 = min(uh, wi.b + kSumRows);
+    unsigned long long s = 0, blk = 0, rgt = 0, bot = 0;
+    const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
+    for (int q = threadIdx.x; q < (i1 - i0) * uw; q += blockDim.x) {
+        const int i = i0 + q / uw, j = q % uw;
+        const int64_t o = (int64_t)(r.v_start + i) * stride + r.h_start + j;
+        const int d = ldpx(dg, o, bd);
+        const int e = ldpx(sr, o, bd) - d;
+        const unsigned long long e2 = (unsigned long long)((long long)e * e);
+        s += (unsigned long long)d;
+        if (j >= uw - dw) rgt += e2;
+        else if (i >= uh - dh) bot += e2;
+        else blk += e2;
+    }
+    unsigned long long v[4] = {s, blk, rgt, bot};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        unsigned long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+        unsigned long long *dst = threadIdx.x == 0 ? (unsigned long long *)&u.sum
+                                : threadIdx.x == 1 ? &u.sse_blk : threadIdx.x == 2 ? &u.sse_rgt : &u.sse_bot;
+        atomicAdd(dst, t);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2. compute_stats: M[k] += y_k x, H[k][l] += y_k y_l (l >= k), y the win x
+// win window of (dgd - avg) in column-major order (idx = col * win + row).
+// A CTA takes kStatRows rows of one unit. Work is split into jobs: one job
+// per pair of window columns (ci <= cj) holding the win x win block of H,
+// plus one job for M; each job is run by `groups` threads over interleaved
+// pixels.
+// ---------------------------------------------------------------------------
+constexpr int kStatRows = 16;
+constexpr int kMaxUnitW = 384 + 8;
+
+template <int WIN>
+__global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkItem *items, int nitems) {
+    constexpr int HALF = WIN / 2;
+    constexpr int WIN2 = WIN * WIN;
+    constexpr int NJOBS = WIN * (WIN + 1) / 2 + 1;
+    __shared__ int16_t dgd[(kStatRows + 2 * HALF) * kMaxUnitW];
+    __shared__ int16_t src[kStatRows * kMaxUnitW];
+    __shared__ long long part[NJOBS * WIN2];
+    const int it = find_item(items, nitems, blockIdx.x);
+    const WorkItem wi = items[it];
+    FrameDesc &f = frames[wi.frame];
+    const LrPlane &pl = f.lr[wi.plane];
+    const UnitRect r = pl.rects[wi.a];
+    LrUnit &u = pl.units[wi.a];
+    const int bd = f.bd, stride = plane_stride(f, wi.plane);
+    const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
+    const int i0 = wi.b, i1 = min(uh, wi.b + kStatRows), nr = i1 - i0;
+    const int64_t npx = (int64_t)uw * uh;
+    const int avg = (int)((unsigned long long)u.sum / (unsigned long long)npx);
+    const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
+    const int dws = uw + 2 * HALF;  // staged dgd row width
+    for (int q = threadIdx.x; q < (nr + 2 * HALF) * dws; q += blockDim.x) {
+        const int rr = q / dws, cc = q - rr * dws;
+        const int y = clampi(r.v_start + i0 - HALF + rr, 0, pl.ph - 1);
+        const int x = clampi(r.h_start - HALF + cc, 0, pl.pw - 1);
+        dgd[q] = (int16_t)(ldpx(dg, (int64_t)y * stride + x, bd) - avg);
+    }
+    for (int q = threadIdx.x; q < nr * uw; q += blockDim.x) {
+        const int rr = q / uw, cc = q - rr * uw;
+        src[q] = (int16_t)(ldpx(sr, (int64_t)(r.v_start + i0 + rr) * stride + r.h_start + cc, bd) - avg);
+    }
+    for (int q = threadIdx.x; q < NJOBS * WIN2; q += blockDim.x) part[q] = 0;
+    __syncthreads();
+    const int groups = blockDim.x / NJOBS;
+    const int job = threadIdx.x / groups, grp = threadIdx.x - job * groups;
+    if (job < NJOBS) {
+        int ci = 0, cj = 0;
+        const bool mjob = job == NJOBS - 1;
+        if (!mjob) {
+            int k = job;
+            while (k >= WIN - ci) {
+                k -= WIN - ci;
+                ++ci;
+            }
+            cj = ci + k;
+        }
+        int acc[WIN][WIN];
+#pragma unroll
+        for (int a = 0; a < WIN; ++a)
+#pragma unroll
+            for (int b = 0; b < WIN; ++b) acc[a][b] = 0;
+        const int npix = nr * uw;
+        for (int q = grp; q < npix; q += groups) {
+            const int i = q / uw, j = q - i * uw;
+            // window row rr, column c: dgd[(i + rr) * dws + j + c]
+            if (mjob) {
+                const int x = src[i * uw + j];
+#pragma unroll
+                for (int c = 0; c < WIN; ++c)
+#pragma unroll
+                    for (int rr = 0; rr < WIN; ++rr) acc[c][rr] += dgd[(i + rr) * dws + j + c] * x;
+            } else {
+                int av[WIN], bv[WIN];
+#pragma unroll
+                for (int rr = 0; rr < WIN; ++rr) {
+                    av[rr] = dgd[(i + rr) * dws + j + ci];
+                    bv[rr] = dgd[(i + rr) * dws + j + cj];
+                }
+#pragma unroll
+                for (int a = 0; a < WIN; ++a)
+#pragma unroll
+                    for (int b = 0; b < WIN; ++b) acc[a][b] += av[a] * bv[b];
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < WIN; ++a)
+#pragma unroll
+            for (int b = 0; b < WIN; ++b)
+                atomicAdd((unsigned long long *)&part[job * WIN2 + a * WIN + b],
+                          (unsigned long long)(long long)acc[a][b]);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < NJOBS * WIN2; q += blockDim.x) {
+        const int jb = q / WIN2, a = (q / WIN) % WIN, b = q % WIN;
+        if (jb == NJOBS - 1) {
+            atomicAdd((unsigned long long *)&u.m[a * WIN + b], (unsigned long long)part[q]);
+        } else {
+            int ci = 0, k = jb;
+            while (k >= WIN - ci) {
+                k -= WIN - ci;
+                ++ci;
+            }
+            const int cj = ci + k;
+            const int kk = ci * WIN + a, ll = cj * WIN + b;
+            if (ll >= kk) atomicAdd((unsigned long long *)&u.h[kk * WIN2 + ll], (unsigned long long)part[q]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3. Solve: wiener_decompose_sep_sym + finalize_sym_filter + compute_score
+// (restoration.rs:801-1056), one CTA per unit. The update_{a,b} sums are
+// sums of independently truncated terms, so threads split the terms and the
+// bins are reduced exactly.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int wrap_index(int i, int win) {
+    const int h1 = (win >> 1) + 1;
+    return i >= h1 ? win - 1 - i : i;
+}
+
+__device__ bool linsolve(int n, int64_t *a, int stride, int64_t *b, int32_t *x) {
+    for (int k = 0; k < n - 1; ++k) {
+        for (int i = n - 1; i >= k + 1; --i) {
+            int64_t u = a[(i - 1) * stride + k], v = a[i * stride + k];
+            if ((u < 0 ? -u : u) < (v < 0 ? -v : v)) {
+                for (int j = 0; j < n; ++j) {
+                    int64_t t = a[i * stride + j];
+                    a[i * stride + j] = a[(i - 1) * stride + j];
+                    a[(i - 1) * stride + j] = t;
+                }
+                int64_t t = b[i];
+                b[i] = b[i - 1];
+                b[i - 1] = t;
+            }
+        }
+        for (int i = k; i < n - 1; ++i) {
+            if (a[k * stride + k] == 0) return false;
+            const int64_t c = a[(i + 1) * stride + k], cd = a[k * stride + k];
+            for (int j = 0; j < n; ++j) a[(i + 1) * stride + j] -= c / 256 * a[k * stride + j] / cd * 256;
+            b[i + 1] -= c * b[k] / cd;
+        }
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        if (a[i * stride + i] == 0) return false;
+        int64_t c = 0;
+        for (int j = i + 1; j < n; ++j) c += a[i * stride + j] * (int64_t)x[j] / kTapScale;
+        x[i] = (int32_t)(kTapScale * (b[i] - c) / a[i * stride + i]);
+    }
+    return true;
+}
+
+// normalize_and_solve (restoration.rs:913-941), one thread.
+__device__ void normalize_and_solve(int win, int64_t *av, int64_t *bv, int32_t *out) {
+    const int h1 = (win >> 1) + 1;
+    const int64_t ah = av[h1 - 1];
+    for (int i = 0; i < h1 - 1; ++i) av[i] -= ah * 2 + bv[i * h1 + h1 - 1] - 2 * bv[(h1 - 1) * h1 + (h1 - 1)];
+    for (int i = 0; i < h1 - 1; ++i)
+        for (int j = 0; j < h1 - 1; ++j)
+            bv[i * h1 + j] -= 2 * (bv[i * h1 + (h1 - 1)] + bv[(h1 - 1) * h1 + j] - 2 * bv[(h1 - 1) * h1 + (h1 - 1)]);
+    int32_t s[7] = {0, 0, 0, 0, 0, 0, 0};
+    if (linsolve(h1 - 1, bv, h1, av, s)) {
+        s[h1 - 1] = (int32_t)kTapScale;
+        for (int i = h1; i < win; ++i) {
+            s[i] = s[win - 1 - i];
+            s[h1 - 1] -= 2 * s[i];
+        }
+        for (int i = 0; i < win; ++i) out[i] = s[i];
+    }
+}
+
+// Block-wide int64 sum of `n` per-thread bins into out[] (thread 0 valid).
+template <int NB>
+__device__ void reduce_bins(int64_t (&bins)[NB], int n, int64_t *out) {
+    __shared__ unsigned long long sb[NB];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) sb[k] = 0;
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        unsigned long long v = (unsigned long long)bins[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&sb[k], v);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) out[k] = (int64_t)sb[k];
+    __syncthreads();
+}
+
+// One update_{a,b}_sep_sym (restoration.rs:849-909). `upd_a` selects which
+// factor is solved; `fix` is the other one.
+__device__ void update_sep_sym(bool upd_a, int win, const int64_t *M, const int64_t *H, const int32_t *fix,
+                               int32_t *outv, int64_t *sav, int64_t *sbv) {
+    const int win2 = win * win, h1 = (win >> 1) + 1;
+    int64_t bins[20];
+#pragma unroll
+    for (int k = 0; k < 20; ++k) bins[k] = 0;
+    // av terms
+    for (int t = threadIdx.x; t < win2; t += blockDim.x) {
+        const int i = t / win, j = t - i * win;
+        if (upd_a) bins[16 + wrap_index(j, win)] += M[i * win + j] * (int64_t)fix[i] / kTapScale;
+        else bins[16 + wrap_index(i, win)] += M[i * win + j] * (int64_t)fix[j] / kTapScale;
+    }
+    // bv terms
+    const int n4 = win2 * win2;
+    for (int t = threadIdx.x; t < n4; t += blockDim.x) {
+        const int i = t / (win * win2), r1 = t - i * win * win2;
+        const int j = r1 / win2, r2 = r1 - j * win2;
+        const int k = r2 / win, l = r2 - k * win;
+        if (upd_a) {
+            const int64_t hv = H[(int64_t)j * win * win2 + i * win + k * win2 + l];
+            bins[wrap_index(l, win) * 4 + wrap_index(k, win)] +=
+                hv * (int64_t)fix[i] / kTapScale * (int64_t)fix[j] / kTapScale;
+        } else {
+            const int64_t hv = H[(int64_t)i * win * win2 + j * win + k * win2 + l];
+            bins[wrap_index(j, win) * 4 + wrap_index(i, win)] +=
+                hv * (int64_t)fix[k] / kTapScale * (int64_t)fix[l] / kTapScale;
+        }
+    }
+    __shared__ int64_t red[20];
+    reduce_bins<20>(bins, 20, red);
+    if (threadIdx.x == 0) {
+        for (int a = 0; a < h1; ++a) sav[a] = red[16 + a];
+        for (int a = 0; a < h1; ++a)
+            for (int b = 0; b < h1; ++b) sbv[a * h1 + b] = red[a * 4 + b];
+        normalize_and_solve(win, sav, sbv, outv);
+    }
+    __syncthreads();
+}
+
+__device__ void finalize_sym(int win, const int32_t *f, int16_t *fi) {
+    const int half = win >> 1;
+    for (int i = 0; i < half; ++i) {
+        const int64_t d = (int64_t)f[i] * kStep, q = kTapScale;
+        fi[i] = (int16_t)(d < 0 ? (d - q / 2) / q : (d + q / 2) / q);
+    }
+    if (win == 7) {
+        fi[0] = (int16_t)clampi(fi[0], -5, 10);
+        fi[1] = (int16_t)clampi(fi[1], -23, 8);
+        fi[2] = (int16_t)clampi(fi[2], -17, 46);
+    } else {
+        fi[2] = (int16_t)clampi(fi[1], -17, 46);
+        fi[1] = (int16_t)clampi(fi[0], -23, 8);
+        fi[0] = 0;
+    }
+    fi[6] = fi[0];
+    fi[5] = fi[1];
+    fi[4] = fi[2];
+    fi[3] = (int16_t)(-2 * (fi[0] + fi[1] + fi[2]));
+    fi[7] = 0;
+}
+
+// items: a = unit. One CTA (128 threads) per unit.
+__global__ void __launch_bounds__(128) k_lr_solve(FrameDesc *frames, const WorkItem *items, int nitems) {
+    __shared__ int64_t H[2401];
+    __shared__ int64_t M[49];
+    __shared__ int32_t a[7], b[7];
+    __shared__ int64_t sav[4], sbv[16];
+    __shared__ int16_t vf[8], hf[8];
+    const WorkItem wi = items[blockIdx.x];
+    FrameDesc &f = frames[wi.frame];
+    const LrPlane &pl = f.lr[wi.plane];
+    LrUnit &u = pl.units[wi.a];
+    const int win = pl.win, win2 = win * win;
+    const int64_t div = f.bd == 10 ? 4 : 1;
+    // Bit-depth divider on M and the upper triangle, then mirror
+    // (compute_stats_hbd, restoration.rs:1799-1806).
+    for (int k = threadIdx.x; k < win2; k += blockDim.x) M[k] = u.m[k] / div;
+    for (int t = threadIdx.x; t < win2 * win2; t += blockDim.x) {
+        const int k = t / win2, l = t - k * win2;
+        if (l >= k) {
+            const int64_t v = u.h[t] / div;
+            H[t] = v;
+            H[l * win2 + k] = v;
+        }
+    }
+    if (threadIdx.x == 0) {
+        const int uw = pl.rects[wi.a].h_end - pl.rects[wi.a].h_start;
+        const int uh = pl.rects[wi.a].v_end - pl.rects[wi.a].v_start;
+        (void)uw;
+        (void)uh;
+        if (f.bd == 8) u.sse_none = (int64_t)(u.sse_blk + u.sse_rgt + u.sse_bot);
+        else u.sse_none = (int64_t)u.sse_blk + (int64_t)(uint32_t)u.sse_rgt + (int64_t)(uint32_t)u.sse_bot;
+        const int off = (7 - win) >> 1;
+        const int init[7] = {3, -7, 15, kStep - 2 * (3 - 7 + 15), 15, -7, 3};
+        for (int i = 0; i < win; ++i) {
+            a[i] = (int32_t)(kTapScale / kStep) * init[i + off];
+            b[i] = a[i];
+        }
+    }
+    __syncthreads();
+    for (int round = 1; round < 5; ++round) {
+        update_sep_sym(true, win, M, H, b, a, sav, sbv);
+        update_sep_sym(false, win, M, H, a, b, sav, sbv);
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 8; ++i) {
+            vf[i] = 0;
+            hf[i] = 0;
+        }
+        finalize_sym(win, a, vf);
+        finalize_sym(win, b, hf);
+        for (int i = 0; i < 7; ++i) {
+            u.vd[i] = i < win ? a[i] : 0;
+            u.hd[i] = i < win ? b[i] : 0;
+        }
+        for (int i = 0; i < 8; ++i) {
+            u.vf[i] = vf[i];
+            u.hf[i] = hf[i];
+        }
+    }
+    __syncthreads();
+    // compute_score (restoration.rs:1009-1056).
+    __shared__ int32_t ab[49];
+    if (threadIdx.x == 0) {
+        int16_t av[7] = {0}, bv[7] = {0};
+        const int off = (7 - win) >> 1;
+        av[3] = kStep;
+        bv[3] = kStep;
+        for (int i = 0; i < 3; ++i) {
+            av[i] = vf[i];
+            av[6 - i] = vf[i];
+            bv[i] = hf[i];
+            bv[6 - i] = hf[i];
+            av[3] = (int16_t)(av[3] - 2 * av[i]);
+            bv[3] = (int16_t)(bv[3] - 2 * bv[i]);
+        }
+        for (int k = 0; k < win; ++k)
+            for (int l = 0; l < win; ++l) ab[k * win + l] = (int32_t)av[l + off] * (int32_t)bv[k + off];
+    }
+    __syncthreads();
+    int64_t bins[2] = {0, 0};
+    for (int k = threadIdx.x; k < win2; k += blockDim.x) bins[0] += (int64_t)ab[k] * M[k] / kStep / kStep;
+    for (int t = threadIdx.x; t < win2 * win2; t += blockDim.x) {
+        const int k = t / win2, l = t - k * win2;
+        bins[1] += (int64_t)ab[k] * H[t] * (int64_t)ab[l] / kStep / kStep / kStep / kStep;
+    }
+    __shared__ int64_t pq[2];
+    reduce_bins<2>(bins, 2, pq);
+    if (threadIdx.x == 0) {
+        const int64_t score = pq[1] - 2 * pq[0];
+        const int64_t ip = M[win2 >> 1], iq = H[(win2 >> 1) * win2 + (win2 >> 1)];
+        u.score = score - (iq - 2 * ip);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4. Trial filter + SSE (try_restoration_unit, restoration.rs:472-507) and
+// the refinement hill-climb (finer_tile_search_wiener, :513-636). One CTA
+// per unit.
+// ---------------------------------------------------------------------------
+constexpr int TT_W = 64, TT_H = 32;
+
+struct Taps {
+    int16_t v[8], h[8];
+};
+
+// Horizontal then vertical pass of wiener_convolve_add_src[_hbd] for one
+// output pixel column tile; `row_src(r)` yields the data row pointer
+// (already clamped / substituted) in plane coordinates.
+__device__ __forceinline__ int wiener_h(const int *px, const int16_t *hf, int bd) {
+    int sum = (px[3] << 7) + (1 << (bd + 7 - 1));
+#pragma unroll
+    for (int k = 0; k < 8; ++k) sum += px[k] * hf[k];
+    const int lim = (1 << (bd + 1 + 7 - 3)) - 1;
+    return clampi((sum + 4) >> 3, 0, lim);
+}
+__device__ __forceinline__ int wiener_v(const int *tp, const int16_t *vf, int bd) {
+    int sum = (tp[3] << 7) - (1 << (bd + 11 - 1));
+#pragma unroll
+    for (int k = 0; k < 8; ++k) sum += tp[k] * vf[k];
+    return clampi((sum + (1 << 10)) >> 11, 0, (1 << bd) - 1);
+}
+
+// SSE of the unit filtered with `t` against the source; three parts as in
+// sse_region_hbd. Returns the combined value in thread 0 (all threads get it).
+__device__ int64_t trial_sse(const FrameDesc &f, int plane, const LrPlane &pl, const UnitRect &r, const Taps &t,
+                             uint16_t *stage, uint16_t *tmp, unsigned long long *red) {
+    const int bd = f.bd, stride = plane_stride(f, plane);
+    const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
+    const int dw = uw % 16, dh = uh % 16;
+    const uint8_t *dg = f.A[plane], *sr = f.S[plane];
+    unsigned long long blk = 0, rgt = 0, bot = 0;
+    constexpr int SW = TT_W + 7, SH = TT_H + 7;
+    for (int ty = 0; ty < uh; ty += TT_H) {
+        for (int tx = 0; tx < uw; tx += TT_W) {
+            const int y0 = r.v_start + ty, x0 = r.h_start + tx;
+            __syncthreads();
+            for (int q = threadIdx.x; q < SH * SW; q += blockDim.x) {
+                const int rr = q / SW, cc = q - rr * SW;
+                const int y = clampi(y0 - 3 + rr, 0, pl.ph - 1), x = clampi(x0 - 3 + cc, 0, pl.pw - 1);
+                stage[q] = (uint16_t)ldpx(dg, (int64_t)y * stride + x, bd);
+            }
+            __syncthreads();
+            for (int q = threadIdx.x; q < SH * TT_W; q += blockDim.x) {
+                const int rr = q / TT_W, cc = q - rr * TT_W;
+                int px[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) px[k] = stage[rr * SW + cc + k];
+                tmp[q] = (uint16_t)wiener_h(px, t.h, bd);
+            }
+            __syncthreads();
+            for (int q = threadIdx.x; q < TT_H * TT_W; q += blockDim.x) {
+                const int rr = q / TT_W, cc = q - rr * TT_W;
+                const int i = ty + rr, j = tx + cc;
+                if (i >= uh || j >= uw) continue;
+                int tp[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) tp[k] = tmp[(rr + k) * TT_W + cc];
+                const int y = wiener_v(tp, t.v, bd);
+                const int e = ldpx(sr, (int64_t)(y0 + rr) * stride + x0 + cc, bd) - y;
+                const unsigned long long e2 = (unsigned long long)((long long)e * e);
+                if (j >= uw - dw) rgt += e2;
+                else if (i >= uh - dh) bot += e2;
+                else blk += e2;
+            }
+        }
+    }
+    unsigned long long v[3] = {blk, rgt, bot};
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        if ((threadIdx.x & 31) == 0) red[k * 8 + (threadIdx.x >> 5)] = v[k];
+    }
+    __syncthreads();
+    __shared__ int64_t res;
+    if (threadIdx.x == 0) {
+        unsigned long long s[3] = {0, 0, 0};
+        for (int k = 0; k < 3; ++k)
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s[k] += red[k * 8 + w];
+        res = bd == 8 ? (int64_t)(s[0] + s[1] + s[2]) : (int64_t)s[0] + (int64_t)(uint32_t)s[1] + (int64_t)(uint32_t)s[2];
+    }
+    __syncthreads();
+    return res;
+}
+
+__global__ void __launch_bounds__(256) k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems) {
+    __shared__ uint16_t stage[(TT_H + 7) * (TT_W + 7)];
+    __shared__ uint16_t tmp[(TT_H + 7) * TT_W];
+    __shared__ unsigned long long red[24];
+    __shared__ Taps t;
+    const WorkItem wi = items[blockIdx.x];
+    FrameDesc &f = frames[wi.frame];
+    const LrPlane &pl = f.lr[wi.plane];
+    LrUnit &u = pl.units[wi.a];
+    const UnitRect r = pl.rects[wi.a];
+    if (u.score > 0) {
+        if (threadIdx.x == 0) u.sse_wn = INT64_MAX;
+        return;
+    }
+    if (threadIdx.x < 8) {
+        t.v[threadIdx.x] = u.vf[threadIdx.x];
+        t.h[threadIdx.x] = u.hf[threadIdx.x];
+    }
+    __syncthreads();
+    int64_t err = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red);
+    if (pl.refine) {
+        // use_refinement with max_one_refinement_step: one step size (4).
+        const int plane_off = (7 - pl.win) >> 1;
+        const int tap_min[3] = {-5, -23, -17}, tap_max[3] = {10, 8, 46};
+        const int s = 4;
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int p = plane_off; p < 3; ++p) {
+                bool skip = false;
+                // minus direction
+                int16_t *fp = pass == 0 ? t.h : t.v;
+                if (fp[p] - s >= tap_min[p]) {
+                    __syncthreads();
+                    if (threadIdx.x == 0) {
+                        fp[p] -= s;
+                        fp[6 - p] -= s;
+                        fp[3] += 2 * s;
+                    }
+                    __syncthreads();
+                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red);
+                    if (e2 > err) {
+                        __syncthreads();
+                        if (threadIdx.x == 0) {
+                            fp[p] += s;
+                            fp[6 - p] += s;
+                            fp[3] -= 2 * s;
+                        }
+                        __syncthreads();
+                    } else {
+                        err = e2;
+                        skip = true;
+                    }
+                }
+                if (skip) break;
+                // plus direction
+                if (fp[p] + s <= tap_max[p]) {
+                    __syncthreads();
+                    if (threadIdx.x == 0) {
+                        fp[p] += s;
+                        fp[6 - p] += s;
+                        fp[3] -= 2 * s;
+                    }
+                    __syncthreads();
+                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red);
+                    if (e2 > err) {
+                        __syncthreads();
+                        if (threadIdx.x == 0) {
+                            fp[p] -= s;
+                            fp[6 - p] -= s;
+                            fp[3] += 2 * s;
+                        }
+                        __syncthreads();
+                    } else {
+                        err = e2;
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        u.sse_wn = err;
+        for (int i = 0; i < 8; ++i) {
+            u.vf[i] = t.v[i];
+            u.hf[i] = t.h[i];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 5. Frame RD (search_restoration_still_bd finish, restoration.rs:847-897):
+// one thread per (frame, plane); reference-chained count_wiener_bits and
+// RDCOST_DBL in IEEE double without contraction.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int d_msb(unsigned v) { return 31 - __clz(v); }
+__device__ int recenter_nonneg(int r, int v) {
+    if (v > (r << 1)) return v;
+    if (v >= r) return (v - r) << 1;
+    return ((r - v) << 1) - 1;
+}
+__device__ int recenter_finite_nonneg(int n, int r, int v) {
+    if ((r << 1) <= n) return recenter_nonneg(r, v);
+    return recenter_nonneg(n - 1 - r, n - 1 - v);
+}
+__device__ int count_quniform(int n, int v) {
+    if (n <= 1) return 0;
+    const int l = d_msb((unsigned)(n - 1)) + 1;
+    const int m = (1 << l) - n;
+    return v < m ? l - 1 : l;
+}
+__device__ int count_subexpfin(int n, int k, int v) {
+    int count = 0, i = 0, mk = 0;
+    for (;;) {
+        const int b = i ? k + i - 1 : k;
+        const int a = 1 << b;
+        if (n <= mk + 3 * a) {
+            count += count_quniform(n - mk, v - mk);
+            break;
+        }
+        count += 1;
+        if (v >= mk + a) {
+            i += 1;
+            mk += a;
+        } else {
+            count += b;
+            break;
+        }
+    }
+    return count;
+}
+__device__ int count_wiener_bits(int win, const int16_t *vf, const int16_t *hf, const int16_t *rvf,
+                                 const int16_t *rhf) {
+    auto tap = [](const int16_t *f, const int16_t *rf, int idx, int minv, int maxv, int k) {
+        return count_subexpfin(maxv - minv + 1, k, recenter_finite_nonneg(maxv - minv + 1, rf[idx] - minv, f[idx] - minv));
+    };
+    int bits = 0;
+    if (win == 7) bits += tap(vf, rvf, 0, -5, 10, 1);
+    bits += tap(vf, rvf, 1, -23, 8, 2);
+    bits += tap(vf, rvf, 2, -17, 46, 3);
+    if (win == 7) bits += tap(hf, rhf, 0, -5, 10, 1);
+    bits += tap(hf, rhf, 1, -23, 8, 2);
+    bits += tap(hf, rhf, 2, -17, 46, 3);
+    return bits;
+}
+__device__ __forceinline__ double rdcost_dbl(int64_t rdmult, int64_t rate, int64_t dist) {
+    return __dadd_rn(__ddiv_rn(__dmul_rn((double)rate, (double)rdmult), 512.0), __dmul_rn((double)dist, 128.0));
+}
+
+__global__ void k_lr_finish(FrameDesc *frames, int nframes) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nframes * 3) return;
+    FrameDesc &f = frames[id / 3];
+    LrPlane &pl = f.lr[id % 3];
+    if (!pl.on) {
+        pl.frame_rtype = 0;
+        return;
+    }
+    const int n = pl.hunits * pl.vunits;
+    int64_t sse_none_frame = 0;
+    for (int k = 0; k < n; ++k) sse_none_frame += pl.units[k].sse_none;
+    const double cost_none_frame = rdcost_dbl(f.rdmult, 0, sse_none_frame);
+    int64_t bits_frame = 0, sse_frame = 0;
+    int16_t rv[8] = {3, -7, 15, -22, 15, -7, 3, 0}, rh[8] = {3, -7, 15, -22, 15, -7, 3, 0};
+    for (int k = 0; k < n; ++k) {
+        LrUnit &u = pl.units[k];
+        u.rtype = 0;
+        if (u.sse_wn == INT64_MAX) {
+            bits_frame += 768;
+            sse_frame += u.sse_none;
+            continue;
+        }
+        const int64_t cnt = count_wiener_bits(pl.win, u.vf, u.hf, rv, rh);
+        const int64_t bits_wn = 320 + (cnt << 9), bits_none = 768;
+        const double cn = rdcost_dbl(f.rdmult, bits_none >> 4, u.sse_none);
+        const double cw = rdcost_dbl(f.rdmult, bits_wn >> 4, u.sse_wn);
+        if (cw < cn) {
+            u.rtype = 1;
+            bits_frame += bits_wn;
+            sse_frame += u.sse_wn;
+            for (int i = 0; i < 8; ++i) {
+                rv[i] = u.vf[i];
+                rh[i] = u.hf[i];
+            }
+        } else {
+            bits_frame += bits_none;
+            sse_frame += u.sse_none;
+        }
+    }
+    const double cost_wn_frame = rdcost_dbl(f.rdmult, bits_frame >> 4, sse_frame);
+    pl.frame_rtype = cost_wn_frame < cost_none_frame ? 1 : 0;
+    if (pl.frame_rtype == 0)
+        for (int k = 0; k < n; ++k) pl.units[k].rtype = 0;
+}
+
+// ---------------------------------------------------------------------------
+// 6. Apply (apply_restoration_frame, restoration.rs:992-1052) with the
+// stripe boundaries of save_lr_boundaries: one CTA per (plane, stripe,
+// 64-px column tile), C = filtered, already holding a copy of A. Rows
+// above / below a stripe come from the post-deblock (pre-CDEF) plane B at
+// interior stripe edges (the only lines the single-tile apply reads) and
+// from the edge-replicated post-CDEF plane at the frame top / bottom.
+// items: a = unit index, b = stripe << 16 | column tile.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems) {
+    constexpr int SW = TT_W + 7;
+    constexpr int MAXH = 64 + 7;
+    __shared__ uint16_t stage[MAXH * SW];
+    __shared__ uint16_t tmp[MAXH * TT_W];
+    const WorkItem wi = items[blockIdx.x];
+    const FrameDesc &f = frames[wi.frame];
+    const LrPlane &pl = f.lr[wi.plane];
+    if (!pl.on || pl.frame_rtype == 0) return;
+    const LrUnit &u = pl.units[wi.a];
+    if (u.rtype != 1) return;
+    const int ss = wi.plane ? 1 : 0;
+    const int full = 64 >> ss, off = 8 >> ss;
+    const int s = wi.b >> 16, ct = wi.b & 0xffff;
+    const int ys = max(0, s * full - off), ye = min(pl.ph, (s + 1) * full - off);
+    const int x0 = ct * TT_W, ncol = min(TT_W, pl.pw - x0);
+    const int nrow = ye - ys;
+    const bool copy_above = s > 0, copy_below = ye < pl.ph;
+    const int bd = f.bd, stride = plane_stride(f, wi.plane);
+    const uint8_t *post = f.A[wi.plane], *pre = f.B[wi.plane];
+    const int rows = nrow + 7;
+    for (int q = threadIdx.x; q < rows * SW; q += blockDim.x) {
+        const int rr = q / SW, cc = q - rr * SW;
+        const int y = ys - 3 + rr;
+        const int x = clampi(x0 - 3 + cc, 0, pl.pw - 1);
+        const uint8_t *src = post;
+        int yy;
+        if (y < ys) {
+            if (copy_above) {
+                src = pre;
+                yy = y == ys - 1 ? ys - 1 : ys - 2;
+            } else {
+                yy = clampi(y, 0, pl.ph - 1);
+            }
+        } else if (y >= ye) {
+            if (copy_below) {
+                src = pre;
+                yy = y == ye ? ye : min(ye + 1, pl.ph - 1);
+            } else {
+                yy = clampi(y, 0, pl.ph - 1);
+            }
+        } else {
+            yy = y;
+        }
+        stage[q] = (uint16_t)ldpx(src, (int64_t)yy * stride + x, bd);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < rows * TT_W; q += blockDim.x) {
+        const int rr = q / TT_W, cc = q - rr * TT_W;
+        int px[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) px[k] = stage[rr * SW + cc + k];
+        tmp[q] = (uint16_t)wiener_h(px, u.hf, bd);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nrow * TT_W; q += blockDim.x) {
+        const int rr = q / TT_W, cc = q - rr * TT_W;
+        if (cc >= ncol) continue;
+        int tp[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) tp[k] = tmp[(rr + k) * TT_W + cc];
+        stpx(f.C[wi.plane], (int64_t)(ys + rr) * stride + x0 + cc, bd, wiener_v(tp, u.vf, bd));
+    }
+}
+
+}  // namespace zf
+
+namespace zf {
+// Host-side launcher: the templated kernel is instantiated and launched in
+// this translation unit (whole-program compilation cannot launch a template
+// instantiation owned by another unit).
+cudaError_t launch_lr_stats(int win, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
+                            int nitems) {
+    if (win == 5) k_lr_stats<5><<<ctas, 256, 0, st>>>(frames, items, nitems);
+    else k_lr_stats<7><<<ctas, 256, 0, st>>>(frames, items, nitems);
+    return cudaGetLastError();
+}
+}  // namespace zf
