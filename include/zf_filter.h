@@ -142,6 +142,9 @@ void zf_destroy(zf_ctx *ctx);
 const char *zf_last_error(const zf_ctx *ctx);
 /* Synchronise the context's stream. */
 int32_t zf_sync(zf_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or timing events against the library's launches. */
+void *zf_stream(const zf_ctx *ctx);
 
 /* Output array sizes for a frame (filter blocks, restoration units). */
 int32_t zf_query_sizes(const zf_frame *f, zf_sizes *out);
@@ -203,6 +206,23 @@ int32_t zf_lr_search(zf_ctx *ctx, const zf_frame *f, zf_decisions *out);
  * from (same layout and memory kind as rec). */
 int32_t zf_lr_apply(zf_ctx *ctx, const zf_frame *f, const void *const pre_cdef[3],
                     const zf_decisions *d);
+
+/* --- Observability ------------------------------------------------------- */
+
+typedef struct zf_kernel_time {
+    char name[32];
+    uint64_t launches;
+    double total_ms;            /* CUDA-event time on the context's stream */
+} zf_kernel_time;
+
+/* Kernel launches issued by this context since zf_create. */
+uint64_t zf_launch_count(const zf_ctx *ctx);
+/* enable != 0: bracket every kernel launch with CUDA events (adds a little
+ * host overhead); the per-kernel totals accumulate until zf_profile_reset. */
+int32_t zf_profile_enable(zf_ctx *ctx, int32_t enable);
+void zf_profile_reset(zf_ctx *ctx);
+/* Copies up to max entries; returns the number of distinct kernels. */
+int32_t zf_profile_read(const zf_ctx *ctx, zf_kernel_time *out, int32_t max);
 
 #ifdef __cplusplus
 }

@@ -68,6 +68,15 @@ def lib():
     L.zf_cdef_apply.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions), P(ZfStats)]
     L.zf_lr_search.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions)]
     L.zf_lr_apply.argtypes = [C.c_void_p, P(ZfFrame), P(C.c_void_p), P(ZfDecisions)]
+    L.zf_stream.argtypes = [C.c_void_p]
+    L.zf_stream.restype = C.c_void_p
+    L.zf_launch_count.argtypes = [C.c_void_p]
+    L.zf_launch_count.restype = C.c_uint64
+    L.zf_profile_enable.argtypes = [C.c_void_p, C.c_int32]
+    L.zf_profile_reset.argtypes = [C.c_void_p]
+    L.zf_profile_reset.restype = None
+    L.zf_profile_read.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
+    L.zf_profile_read.restype = C.c_int32
     for name in ("zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
                  "zf_submit_batch", "zf_deblock_pick", "zf_deblock_apply", "zf_cdef_search",
                  "zf_cdef_apply", "zf_lr_search", "zf_lr_apply"):
@@ -126,6 +135,31 @@ class Context:
 
     def sync(self):
         self._check(lib().zf_sync(self.h))
+
+    def stream_handle(self):
+        return lib().zf_stream(self.h)
+
+    def launch_count(self):
+        return lib().zf_launch_count(self.h)
+
+    def profile(self, enable=True):
+        self._check(lib().zf_profile_enable(self.h, 1 if enable else 0))
+
+    def profile_reset(self):
+        lib().zf_profile_reset(self.h)
+
+    def profile_read(self):
+        """{kernel name: (launches, total_ms)} measured with CUDA events."""
+        buf = (abi.ZfKernelTime * 64)()
+        n = lib().zf_profile_read(self.h, buf, 64)
+        return {buf[i].name.decode(): (buf[i].launches, buf[i].total_ms) for i in range(min(n, 64))}
+
+    def filter_stage_raw(self, s, dec, st):
+        """zf_filter_stage on a prepared zf_frame / Decisions / ZfStats."""
+        self._check(lib().zf_filter_stage(self.h, C.byref(s), C.byref(dec.c), C.byref(st)))
+
+    def submit_batch_raw(self, frames_arr, n, decs_arr, stats_arr):
+        self._check(lib().zf_submit_batch(self.h, frames_arr, n, decs_arr, stats_arr))
 
     # -- whole stage --------------------------------------------------------
     def filter_stage(self, fr, mi=None, rec=None):

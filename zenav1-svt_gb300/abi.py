@@ -58,6 +58,10 @@ class ZfOpts(C.Structure):
                 ("cancel_flag", C.POINTER(C.c_int32))]
 
 
+class ZfKernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double)]
+
+
 def ptr(a):
     return C.c_void_p(a.ctypes.data) if a is not None else None
 

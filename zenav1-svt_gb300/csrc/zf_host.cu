@@ -34,7 +34,59 @@ struct zf_ctx {
     size_t arena_cap = 0;
     uint64_t budget = 0;
     volatile int32_t *cancel = nullptr;
+    // launch accounting / optional event profiling
+    uint64_t launches = 0;
+    bool profiling = false;
+    struct Pending {
+        const char *name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::vector<zf_kernel_time> totals;
 };
+
+namespace {
+// Bracket one launch: count it and, when profiling, record events on the
+// context stream around it.
+struct LaunchScope {
+    zf_ctx *ctx;
+    const char *name;
+    cudaEvent_t a = nullptr, b = nullptr;
+    LaunchScope(zf_ctx *c, const char *n) : ctx(c), name(n) {
+        ctx->launches++;
+        if (ctx->profiling && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess)
+            cudaEventRecord(a, ctx->stream);
+    }
+    ~LaunchScope() {
+        if (a && b) {
+            cudaEventRecord(b, ctx->stream);
+            ctx->pending.push_back({name, a, b});
+        }
+    }
+};
+// Fold completed event pairs into the per-kernel totals (after a sync).
+void collect_profile(zf_ctx *ctx) {
+    for (auto &p : ctx->pending) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+        zf_kernel_time *t = nullptr;
+        for (auto &k : ctx->totals)
+            if (std::strncmp(k.name, p.name, sizeof(k.name)) == 0) t = &k;
+        if (!t) {
+            zf_kernel_time k;
+            std::memset(&k, 0, sizeof(k));
+            std::strncpy(k.name, p.name, sizeof(k.name) - 1);
+            ctx->totals.push_back(k);
+            t = &ctx->totals.back();
+        }
+        t->launches += 1;
+        t->total_ms += ms;
+    }
+    ctx->pending.clear();
+}
+}  // namespace
 
 namespace {
 
@@ -677,9 +729,10 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                                cudaMemcpyHostToDevice, st));
             CU(cudaMemcpyAsync(base + o_dbs_lv, lv.data(), lv.size() * 4, cudaMemcpyHostToDevice, st));
             CU(cudaMemsetAsync(base + o_dbs_sse, 0, lv.size() * 8, st));
+            { LaunchScope ls_(ctx, "k_deblock_sse");
             zf::k_deblock_sse<<<wl.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_dbs_items),
                                                        (int)wl.items.size(), (const int *)(base + o_dbs_lv),
-                                                       (unsigned long long *)(base + o_dbs_sse));
+                                                       (unsigned long long *)(base + o_dbs_sse)); }
             TRY(launch_check(ctx, "k_deblock_sse"));
             std::vector<unsigned long long> sse(lv.size());
             CU(cudaMemcpyAsync(sse.data(), base + o_dbs_sse, sse.size() * 8, cudaMemcpyDeviceToHost, st));
@@ -718,23 +771,27 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
 
     // ---- deblock apply: A -> B
     if (run.stages & STG_DB_APPLY) {
+        { LaunchScope ls_(ctx, "k_deblock_apply");
         zf::k_deblock_apply<<<wl_db.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_db),
-                                                        (int)wl_db.items.size());
+                                                        (int)wl_db.items.size()); }
         TRY(launch_check(ctx, "k_deblock_apply"));
         TRY(check_cancel(ctx));
     }
     // ---- CDEF search + finish on B
     if ((run.stages & STG_CDEF_SEARCH) && !cdef_frames.empty()) {
+        { LaunchScope ls_(ctx, "k_cdef_search");
         zf::k_cdef_search<<<wl_cs.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_cs),
-                                                      (int)wl_cs.items.size());
+                                                      (int)wl_cs.items.size()); }
         TRY(launch_check(ctx, "k_cdef_search"));
-        zf::k_cdef_finish<<<(int)cdef_frames.size(), 1024, 0, st>>>(d_desc, (const int *)(base + o_cf));
+        { LaunchScope ls_(ctx, "k_cdef_finish");
+        zf::k_cdef_finish<<<(int)cdef_frames.size(), 1024, 0, st>>>(d_desc, (const int *)(base + o_cf)); }
         TRY(launch_check(ctx, "k_cdef_finish"));
         TRY(check_cancel(ctx));
     }
     // ---- CDEF apply: B -> A
     if (run.stages & STG_CDEF_APPLY) {
-        zf::k_cdef_apply<<<wl_ca.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_ca), (int)wl_ca.items.size());
+        { LaunchScope ls_(ctx, "k_cdef_apply");
+        zf::k_cdef_apply<<<wl_ca.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_ca), (int)wl_ca.items.size()); }
         TRY(launch_check(ctx, "k_cdef_apply"));
         TRY(check_cancel(ctx));
     }
@@ -745,27 +802,33 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 if (plans[i].d.lr[pl].on)
                     CU(cudaMemsetAsync(plans[i].d.lr[pl].units, 0, plans[i].rects[pl].size() * sizeof(LrUnit), st));
         if (wl_sum.ctas) {
+            { LaunchScope ls_(ctx, "k_lr_sums");
             zf::k_lr_sums<<<wl_sum.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_sum),
-                                                      (int)wl_sum.items.size());
+                                                      (int)wl_sum.items.size()); }
             TRY(launch_check(ctx, "k_lr_sums"));
         }
         if (wl_st5.ctas) {
+            LaunchScope ls5_(ctx, "k_lr_stats5");
             CU(zf::launch_lr_stats(5, wl_st5.ctas, st, d_desc, (const WorkItem *)(base + o_st5),
                                    (int)wl_st5.items.size()));
         }
         if (wl_st7.ctas) {
+            LaunchScope ls7_(ctx, "k_lr_stats7");
             CU(zf::launch_lr_stats(7, wl_st7.ctas, st, d_desc, (const WorkItem *)(base + o_st7),
                                    (int)wl_st7.items.size()));
         }
         if (wl_unit.ctas) {
+            { LaunchScope ls_(ctx, "k_lr_solve");
             zf::k_lr_solve<<<wl_unit.ctas, 128, 0, st>>>(d_desc, (const WorkItem *)(base + o_unit),
-                                                        (int)wl_unit.items.size());
+                                                        (int)wl_unit.items.size()); }
             TRY(launch_check(ctx, "k_lr_solve"));
+            { LaunchScope ls_(ctx, "k_lr_trial");
             zf::k_lr_trial<<<wl_unit.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_unit),
-                                                        (int)wl_unit.items.size());
+                                                        (int)wl_unit.items.size()); }
             TRY(launch_check(ctx, "k_lr_trial"));
         }
-        zf::k_lr_finish<<<(n * 3 + 127) / 128, 128, 0, st>>>(d_desc, n);
+        { LaunchScope ls_(ctx, "k_lr_finish");
+        zf::k_lr_finish<<<(n * 3 + 127) / 128, 128, 0, st>>>(d_desc, n); }
         TRY(launch_check(ctx, "k_lr_finish"));
         TRY(check_cancel(ctx));
     }
@@ -776,8 +839,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 CU(cudaMemcpyAsync(base + plans[i].off_set[SET_C][pl], base + plans[i].off_set[SET_A][pl],
                                    plans[i].pbytes[pl], cudaMemcpyDeviceToDevice, st));
         if (wl_apply.ctas) {
+            { LaunchScope ls_(ctx, "k_lr_apply");
             zf::k_lr_apply<<<wl_apply.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_apply),
-                                                         (int)wl_apply.items.size());
+                                                         (int)wl_apply.items.size()); }
             TRY(launch_check(ctx, "k_lr_apply"));
         }
     }
@@ -811,6 +875,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     }
     CU(cudaStreamSynchronize(st));
     TRY(launch_check(ctx, "stream"));
+    collect_profile(ctx);
     for (int i = 0; i < n; ++i) {
         Plan &p = plans[i];
         const FrameDesc &b = back[i];
@@ -957,6 +1022,30 @@ int32_t zf_pack_geom(int32_t mi_cols, int32_t mi_rows, const uint32_t *block_id,
                      (skip[i] ? ZF_MI_SKIP : 0u) | (skip_inter[i] ? ZF_MI_SKIP_INTER : 0u);
         }
     return ZF_OK;
+}
+
+uint64_t zf_launch_count(const zf_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+void *zf_stream(const zf_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int32_t zf_profile_enable(zf_ctx *ctx, int32_t enable) {
+    if (!ctx) return ZF_ERR_ARG;
+    ctx->profiling = enable != 0;
+    return ZF_OK;
+}
+
+void zf_profile_reset(zf_ctx *ctx) {
+    if (!ctx) return;
+    cudaStreamSynchronize(ctx->stream);
+    collect_profile(ctx);
+    ctx->totals.clear();
+}
+
+int32_t zf_profile_read(const zf_ctx *ctx, zf_kernel_time *out, int32_t max) {
+    if (!ctx) return ZF_ERR_ARG;
+    const int n = (int)ctx->totals.size();
+    for (int i = 0; i < n && i < max && out; ++i) out[i] = ctx->totals[i];
+    return n;
 }
 
 int32_t zf_filter_stage(zf_ctx *ctx, const zf_frame *f, zf_decisions *out, zf_stats *stats) {
