@@ -343,7 +343,7 @@ def run_ours(args):
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": {"value": round(e2e, 3), "unit": "MPix/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e_ms, 3)},
-                "gpu_launches": int(launches // max(args.steps, 1)),
+                "gpu_launches": int(launches),
                 "roofline": roofline, "kernels": kernels, "clocks": clk}
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_sample()
@@ -354,6 +354,36 @@ def run_ours(args):
     return 0
 
 
+def run_profile(args):
+    """Profiler driver (for ncu): device-resident plain path only, no e2e,
+    no CPU baseline, no clock sampling. --pw/--ph pick the frame size."""
+    import torch
+    ge.build()
+    pkg = ge._pkg()
+    from zenav1_svt_gb300 import abi, synth
+    frames = [synth.make_frame(synth.frame_seed(2, 100 + i), args.pw, args.ph, 8, qp, preset, "power")
+              for i, (preset, qp) in enumerate(WORKLOAD[:args.nframes])]
+    ctx = pkg.Context(0)
+    dev = torch.device("cuda", 0)
+    keep, structs = [], []
+    for f in frames:
+        s = [torch.from_numpy(p.copy()).to(dev) for p in f.src]
+        r = [torch.from_numpy(p.copy()).to(dev) for p in f.rec]
+        m = torch.from_numpy(pkg.pack_geom(f.geom).view(np.int32)).to(dev)
+        keep += [s, r, m]
+        structs.append((abi.make_frame_struct(f, [x.data_ptr() for x in s], [x.data_ptr() for x in r], m.data_ptr(),
+                                              on_device=True), abi.Decisions(f.w, f.h, f.true_w, f.true_h),
+                        abi.ZfStats()))
+    torch.cuda.synchronize()
+    for _ in range(args.warmup + args.steps):
+        for s, d, st in structs:
+            ctx.filter_stage_raw(s, d, st)
+    ctx.sync()
+    print("profile run done: %d frames %dx%d, %d passes" % (len(frames), args.pw, args.ph, args.warmup + args.steps))
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,7 +391,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--profile-run", action="store_true", help="plain device path only, for ncu")
+    ap.add_argument("--pw", type=int, default=W4K)
+    ap.add_argument("--ph", type=int, default=H4K)
+    ap.add_argument("--nframes", type=int, default=4)
     args = ap.parse_args()
+    if args.profile_run:
+        return run_profile(args)
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)

@@ -10,6 +10,8 @@
 // canvas. Here a CTA owns one 64x64 filter block and stages exactly that
 // (plus the 2-pixel reach of the taps) in shared memory, so every pixel of
 // every candidate reads the same values as the reference's build_src.
+#include <cooperative_groups.h>
+
 #include "zf_dev.cuh"
 
 namespace zf {
@@ -295,137 +297,180 @@ __device__ __forceinline__ unsigned long long rdc(unsigned long long lambda, uns
     return ((rate * lambda + 256) >> 9) + (dist << 7);
 }
 
-// search_one_dual (cdef.rs:824-862), all threads of the CTA.
-__device__ unsigned long long search_one_dual(const FrameDesc &f, int nfb, int n_cand, int *lev0, int *lev1,
-                                              int nbs, unsigned long long *tot, unsigned long long *rv, int *ri) {
-    const uint64_t *mse = f.mse;
-    const int npairs = n_cand * n_cand;
-    for (int p = threadIdx.x; p < npairs; p += blockDim.x) tot[p] = 0;
-    for (int fb = threadIdx.x; fb < nfb; fb += blockDim.x) {
-        if (!f.fb_row[fb]) continue;
-        const uint64_t *row = mse + (int64_t)fb * 2 * n_cand;
-        unsigned long long best = 1ull << 63;
-        for (int gi = 0; gi < nbs; ++gi) {
-            unsigned long long c = row[lev0[gi]] + row[n_cand + lev1[gi]];
-            if (c < best) best = c;
-        }
-        f.cdef_best[fb] = best;
-    }
-    __syncthreads();
-    const int tpp = max(1, (int)blockDim.x / npairs);
-    const int work = npairs * tpp;
-    for (int w = threadIdx.x; w < work; w += blockDim.x) {
-        const int p = w / tpp, part = w - p * tpp;
-        const int j = p / n_cand, k = p - j * n_cand;
-        unsigned long long s = 0;
-        for (int fb = part; fb < nfb; fb += tpp) {
-            if (!f.fb_row[fb]) continue;
-            const uint64_t *row = mse + (int64_t)fb * 2 * n_cand;
-            unsigned long long c = row[j] + row[n_cand + k];
-            unsigned long long b = f.cdef_best[fb];
-            s += c < b ? c : b;
-        }
-        atomicAdd(&tot[p], s);
-    }
-    __syncthreads();
-    // argmin with strict < in (j, k) raster order: the lowest index wins ties.
-    unsigned long long bv = ~0ull;
-    int bi = 0x7fffffff;
-    for (int p = threadIdx.x; p < npairs; p += blockDim.x) {
-        unsigned long long v = tot[p] < (1ull << 63) ? tot[p] : (1ull << 63);
-        if (v < bv || (v == bv && p < bi)) {
-            bv = v;
-            bi = p;
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        unsigned long long ov = __shfl_down_sync(0xffffffffu, bv, o);
-        int oi = __shfl_down_sync(0xffffffffu, bi, o);
-        if (ov < bv || (ov == bv && oi < bi)) {
-            bv = ov;
-            bi = oi;
-        }
-    }
-    if ((threadIdx.x & 31) == 0) {
-        rv[threadIdx.x >> 5] = bv;
-        ri[threadIdx.x >> 5] = bi;
-    }
-    __syncthreads();
-    __shared__ unsigned long long res_v;
-    if (threadIdx.x == 0) {
-        unsigned long long v = ~0ull;
-        int idx = 0x7fffffff;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
-            if (rv[w] < v || (rv[w] == v && ri[w] < idx)) {
-                v = rv[w];
-                idx = ri[w];
-            }
-        // best_tot starts at 1 << 63 with strict <: a sum never below it
-        // leaves (0, 0).
-        if (v >= (1ull << 63)) {
-            idx = 0;
-            v = 1ull << 63;
-        }
-        lev0[nbs] = idx / n_cand;
-        lev1[nbs] = idx % n_cand;
-        res_v = v;
-    }
-    __syncthreads();
-    return res_v;
-}
+// finish_cdef_rd + the per-fb index (cdef.rs:897-944, :1326-1344) for one
+// frame on a cluster of kFinCluster CTAs. The filter blocks are split into
+// kFinCluster contiguous ranges; each CTA compacts the rows of its range
+// (column-major u32: every per-filter-block mse is below 2^29 -- at most
+// 4096 px x 1023^2 >> 4 per plane, times sub <= 4 -- so the u32 copy is
+// lossless and a luma + chroma row sum fits u32) into its shared memory.
+// Each search_one_dual step (cdef.rs:824-862) sums its range into a local
+// partial, the cluster barrier publishes the partials, every CTA adds all
+// of them over distributed shared memory and takes the same argmin, so the
+// 75 sequential steps of the joint search stay in lockstep without a trip
+// to global memory.
+constexpr int kFinCluster = 8;
+constexpr int kFinThreads = 512;
 
-__global__ void __launch_bounds__(1024) k_cdef_finish(FrameDesc *frames, const int *frame_ids) {
-    __shared__ unsigned long long tot[kMaxCand * kMaxCand];
+__global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThreads)
+    k_cdef_finish(FrameDesc *frames, const int *frame_ids, int smem_bytes) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    extern __shared__ uint32_t dyn[];
+    __shared__ unsigned long long tot[kMaxCand * kMaxCand];   // this CTA's partial
+    __shared__ unsigned long long tsum[kMaxCand * kMaxCand];  // cluster-wide sum
     __shared__ unsigned long long rv[32];
     __shared__ int ri[32];
+    __shared__ int scan[kFinThreads];
     __shared__ int lev0[17], lev1[17], blev0[8], blev1[8];
-    __shared__ int best_bits, sbc;
-    FrameDesc &f = frames[frame_ids[blockIdx.x]];
+    __shared__ int best_bits, local_sb;
+    __shared__ unsigned long long res_v;
+    const int rank = (int)cl.block_rank();
+    FrameDesc &f = frames[frame_ids[blockIdx.x / kFinCluster]];
     CdefParams &cp = f.cdef;
-    if (cp.mode != 1) return;
-    const int nfb = f.nhfb * f.nvfb, n_cand = cp.ncand;
-    if (threadIdx.x == 0) sbc = 0;
-    __syncthreads();
+    if (cp.mode != 1) return;  // uniform over the cluster
+    const int nfb = f.nhfb * f.nvfb, n_cand = cp.ncand, n2 = 2 * n_cand, npairs = n_cand * n_cand;
+    const int T = blockDim.x, t = threadIdx.x;
+    const int fb0 = (int)((int64_t)nfb * rank / kFinCluster), fb1 = (int)((int64_t)nfb * (rank + 1) / kFinCluster);
+    // compaction of this range's filter blocks with rows, in fb order
+    const int span = fb1 - fb0, chunk = (span + T - 1) / T;
+    const int c0 = fb0 + min(span, t * chunk), c1 = fb0 + min(span, t * chunk + chunk);
     int cnt = 0;
-    for (int fb = threadIdx.x; fb < nfb; fb += blockDim.x) cnt += f.fb_row[fb];
-    atomicAdd(&sbc, cnt);
+    for (int fb = c0; fb < c1; ++fb) cnt += f.fb_row[fb];
+    scan[t] = cnt;
     __syncthreads();
-    const int sb_count = sbc;
-    if (sb_count == 0) {  // every filter block all-skip: cdef.rs:282-288
-        if (threadIdx.x == 0) {
+    for (int o = 1; o < T; o <<= 1) {
+        const int v = t >= o ? scan[t - o] : 0;
+        __syncthreads();
+        scan[t] += v;
+        __syncthreads();
+    }
+    const int sbr = scan[T - 1];
+    int pos = fb0 + scan[t] - cnt;
+    for (int fb = c0; fb < c1; ++fb)
+        if (f.fb_row[fb]) f.cdef_ids[pos++] = fb;
+    for (int fb = fb0 + t; fb < fb1; fb += T) f.fb_idx[fb] = 0;
+    if (t == 0) local_sb = sbr;
+    cl.sync();
+    int sb = 0;
+    for (int r = 0; r < kFinCluster; ++r) sb += *cl.map_shared_rank(&local_sb, r);
+    if (sb == 0) {  // every filter block all-skip: cdef.rs:282-288
+        if (rank == 0 && t == 0) {
             cp.bits = 0;
             cp.y_str[0] = 0;
             cp.uv_str[0] = 0;
         }
-        for (int fb = threadIdx.x; fb < nfb; fb += blockDim.x) f.fb_idx[fb] = 0;
+        cl.sync();
         return;
     }
-    unsigned long long best_cost = 1ull << 63;
-    if (threadIdx.x == 0) best_bits = 0;
-    for (int i = 0; i <= 3; ++i) {
-        const int nb = 1 << i;
-        if (threadIdx.x < 17) {
-            lev0[threadIdx.x] = 0;
-            lev1[threadIdx.x] = 0;
+    const bool in_smem = (size_t)sbr * (n2 + 1) * 4 <= (size_t)smem_bytes;
+    uint32_t *R = in_smem ? dyn : f.cdef_rows32 + (size_t)fb0 * n2;
+    uint32_t *best = in_smem ? dyn + (size_t)sbr * n2 : reinterpret_cast<uint32_t *>(f.cdef_best) + fb0;
+    for (int q = t; q < sbr * n2; q += T) {
+        const int k = q / sbr, s = q - k * sbr;  // column-major: R[k * sbr + s]
+        R[q] = (uint32_t)f.mse[(int64_t)f.cdef_ids[fb0 + s] * n2 + k];
+    }
+    __syncthreads();
+
+    // One search_one_dual step over the whole frame.
+    auto step = [&](int nbs) -> unsigned long long {
+        for (int p = t; p < npairs; p += T) tot[p] = 0;
+        for (int s = t; s < sbr; s += T) {
+            uint32_t b = 0xffffffffu;  // +infinity for an empty strength set
+            for (int gi = 0; gi < nbs; ++gi) {
+                const uint32_t c = R[lev0[gi] * sbr + s] + R[(n_cand + lev1[gi]) * sbr + s];
+                b = c < b ? c : b;
+            }
+            best[s] = b;
         }
         __syncthreads();
-        unsigned long long t = 1ull << 63;
-        for (int s = 0; s < nb; ++s) t = search_one_dual(f, nfb, n_cand, lev0, lev1, s, tot, rv, ri);
+        const int tpp = max(1, T / npairs);
+        for (int w = t; w < npairs * tpp; w += T) {
+            const int p = w / tpp, part = w - p * tpp;
+            const int j = p / n_cand, k = p - j * n_cand;
+            const uint32_t *rj = R + (size_t)j * sbr, *rk = R + (size_t)(n_cand + k) * sbr;
+            unsigned long long acc = 0;
+            for (int s = part; s < sbr; s += tpp) {
+                const uint32_t c = rj[s] + rk[s], b = best[s];
+                acc += c < b ? c : b;
+            }
+            atomicAdd(&tot[p], acc);
+        }
+        cl.sync();  // partials complete everywhere
+        for (int p = t; p < npairs; p += T) {
+            unsigned long long v = 0;
+            for (int r = 0; r < kFinCluster; ++r) v += cl.map_shared_rank(tot, r)[p];
+            tsum[p] = v;
+        }
+        cl.sync();  // every CTA has read every partial before the next step
+        // argmin with strict < in (j, k) raster order: lowest index wins ties
+        unsigned long long bv = ~0ull;
+        int bi = 0x7fffffff;
+        for (int p = t; p < npairs; p += T) {
+            const unsigned long long v = tsum[p];
+            if (v < bv || (v == bv && p < bi)) {
+                bv = v;
+                bi = p;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ov = __shfl_down_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+            if (ov < bv || (ov == bv && oi < bi)) {
+                bv = ov;
+                bi = oi;
+            }
+        }
+        if ((t & 31) == 0) {
+            rv[t >> 5] = bv;
+            ri[t >> 5] = bi;
+        }
+        __syncthreads();
+        if (t == 0) {
+            unsigned long long v = ~0ull;
+            int idx = 0x7fffffff;
+            for (int w = 0; w < T / 32; ++w)
+                if (rv[w] < v || (rv[w] == v && ri[w] < idx)) {
+                    v = rv[w];
+                    idx = ri[w];
+                }
+            if (v >= (1ull << 63)) {  // best_tot starts at 1 << 63 with strict <
+                idx = 0;
+                v = 1ull << 63;
+            }
+            lev0[nbs] = idx / n_cand;
+            lev1[nbs] = idx % n_cand;
+            res_v = v;
+        }
+        __syncthreads();
+        return res_v;
+    };
+
+    unsigned long long best_cost = 1ull << 63;
+    if (t == 0) best_bits = 0;
+    for (int i = 0; i <= 3; ++i) {
+        const int nb = 1 << i;
+        if (t < 17) {
+            lev0[t] = 0;
+            lev1[t] = 0;
+        }
+        __syncthreads();
+        unsigned long long tt = 1ull << 63;
+        for (int s = 0; s < nb; ++s) tt = step(s);
         for (int r = 0; r < 4 * nb; ++r) {
-            if (threadIdx.x == 0)
+            if (t == 0)
                 for (int j = 0; j < nb - 1; ++j) {
                     lev0[j] = lev0[j + 1];
                     lev1[j] = lev1[j + 1];
                 }
             __syncthreads();
-            t = search_one_dual(f, nfb, n_cand, lev0, lev1, nb - 1, tot, rv, ri);
+            tt = step(nb - 1);
         }
-        const unsigned long long total_bits = (unsigned long long)sb_count * i + nb * 12;
-        const unsigned long long cost = rdc(cp.lambda, total_bits << 9, t * 16);
+        const unsigned long long total_bits = (unsigned long long)sb * i + nb * 12;
+        const unsigned long long cost = rdc(cp.lambda, total_bits << 9, tt * 16);
         if (cost < best_cost) {
             best_cost = cost;
-            if (threadIdx.x == 0) {
+            if (t == 0) {
                 best_bits = i;
                 for (int k = 0; k < nb; ++k) {
                     blev0[k] = lev0[k];
@@ -436,22 +481,19 @@ __global__ void __launch_bounds__(1024) k_cdef_finish(FrameDesc *frames, const i
         __syncthreads();
     }
     const int nb = 1 << best_bits;
-    for (int fb = threadIdx.x; fb < nfb; fb += blockDim.x) {
+    for (int s = t; s < sbr; s += T) {
         int best_gi = 0;
-        if (f.fb_row[fb]) {
-            const uint64_t *row = f.mse + (int64_t)fb * 2 * n_cand;
-            unsigned long long best = ~0ull;
-            for (int gi = 0; gi < nb; ++gi) {
-                unsigned long long c = row[blev0[gi]] + row[n_cand + blev1[gi]];
-                if (c < best) {
-                    best = c;
-                    best_gi = gi;
-                }
+        unsigned long long bst = ~0ull;
+        for (int gi = 0; gi < nb; ++gi) {
+            const unsigned long long c = (unsigned long long)R[blev0[gi] * sbr + s] + R[(n_cand + blev1[gi]) * sbr + s];
+            if (c < bst) {
+                bst = c;
+                best_gi = gi;
             }
         }
-        f.fb_idx[fb] = (uint8_t)best_gi;
+        f.fb_idx[f.cdef_ids[fb0 + s]] = (uint8_t)best_gi;
     }
-    if (threadIdx.x == 0) {
+    if (rank == 0 && t == 0) {
         cp.bits = best_bits;
         for (int gi = 0; gi < 8; ++gi) {
             cp.y_str[gi] = gi < nb ? (uint8_t)cp.fs[blev0[gi]] : 0;

@@ -81,6 +81,8 @@ struct FrameDesc {
     uint8_t *fb_row;        // nfb: fb has a non-skip 8x8
     uint8_t *fb_idx;        // nfb
     uint64_t *cdef_best;    // nfb scratch for the joint search
+    int *cdef_ids;          // nfb: compacted filter-block ids with rows
+    uint32_t *cdef_rows32;  // nfb x 2 x ncand: compacted rows (global fallback)
     unsigned long long *cdef_stats;  // [filtered, changed, sb_count]
     // LR
     LrPlane lr[3];

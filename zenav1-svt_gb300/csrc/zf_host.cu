@@ -307,6 +307,7 @@ struct Plan {
     size_t off_set[3][3];             // [set A/B/C][plane]
     size_t off_src[3];
     size_t off_mi = 0, off_mse = 0, off_fbrow = 0, off_fbidx = 0, off_best = 0, off_stats = 0;
+    size_t off_ids = 0, off_rows32 = 0;
     size_t off_rects[3], off_units[3];
     std::vector<UnitRect> rects[3];
     int hunits[3], vunits[3];
@@ -314,6 +315,9 @@ struct Plan {
 };
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) & ~(a - 1); }
+
+// Dynamic shared memory opted in for k_cdef_finish's compacted rows.
+constexpr size_t kFinishSmemCap = 160 * 1024;
 
 int validate_frame(zf_ctx *ctx, const zf_frame *f) {
     if (!f) return fail(ctx, ZF_ERR_ARG, "frame is NULL");
@@ -371,6 +375,8 @@ void plan_frame(Plan &p, const zf_frame *f, size_t &cursor) {
     p.off_fbrow = take(p.nfb);
     p.off_fbidx = take(p.nfb);
     p.off_best = take((size_t)p.nfb * 8);
+    p.off_ids = take((size_t)p.nfb * 4);
+    p.off_rows32 = take((size_t)p.nfb * 2 * zf::kMaxCand * 4);
     p.off_stats = take(4 * 8);
     // CDEF policy (pipeline.rs:3042-3144).
     CdefParams &cp = d.cdef;
@@ -430,6 +436,8 @@ void bind_pointers(Plan &p, uint8_t *base) {
     d.fb_row = base + p.off_fbrow;
     d.fb_idx = base + p.off_fbidx;
     d.cdef_best = (uint64_t *)(base + p.off_best);
+    d.cdef_ids = (int *)(base + p.off_ids);
+    d.cdef_rows32 = (uint32_t *)(base + p.off_rows32);
     d.cdef_stats = (unsigned long long *)(base + p.off_stats);
 }
 
@@ -784,7 +792,16 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                                                       (int)wl_cs.items.size()); }
         TRY(launch_check(ctx, "k_cdef_search"));
         { LaunchScope ls_(ctx, "k_cdef_finish");
-        zf::k_cdef_finish<<<(int)cdef_frames.size(), 1024, 0, st>>>(d_desc, (const int *)(base + o_cf)); }
+        // dynamic shared memory for the compacted rows: the largest frame
+        // of the batch, capped (frames that do not fit use global scratch)
+        size_t want = 0;
+        for (int fi : cdef_frames)
+            want = std::max(want, ((size_t)plans[fi].nfb + zf::kFinClusterHost - 1) / zf::kFinClusterHost *
+                                      (2 * plans[fi].d.cdef.ncand + 1) * 4);
+        const int smem = (int)std::min<size_t>(want, kFinishSmemCap);
+        CU(cudaFuncSetAttribute(zf::k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinishSmemCap));
+        zf::k_cdef_finish<<<(int)cdef_frames.size() * zf::kFinClusterHost, zf::kFinThreadsHost, smem, st>>>(
+            d_desc, (const int *)(base + o_cf), smem); }
         TRY(launch_check(ctx, "k_cdef_finish"));
         TRY(check_cancel(ctx));
     }
@@ -828,7 +845,13 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             TRY(launch_check(ctx, "k_lr_trial"));
         }
         { LaunchScope ls_(ctx, "k_lr_finish");
-        zf::k_lr_finish<<<(n * 3 + 127) / 128, 128, 0, st>>>(d_desc, n); }
+        int max_units = 1;
+        for (auto &p : plans)
+            for (int pl = 0; pl < 3; ++pl) max_units = std::max(max_units, p.hunits[pl] * p.vunits[pl]);
+        const int smem = max_units * 32;
+        if (smem > 48 * 1024)
+            CU(cudaFuncSetAttribute(zf::k_lr_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        zf::k_lr_finish<<<n * 3, 32, smem, st>>>(d_desc, n); }
         TRY(launch_check(ctx, "k_lr_finish"));
         TRY(check_cancel(ctx));
     }

@@ -11,7 +11,7 @@ __global__ void k_deblock_sse(const FrameDesc *frames, const WorkItem *items, in
                               unsigned long long *sse);
 
 __global__ void k_cdef_search(const FrameDesc *frames, const WorkItem *items, int nitems);
-__global__ void k_cdef_finish(FrameDesc *frames, const int *frame_ids);
+__global__ void k_cdef_finish(FrameDesc *frames, const int *frame_ids, int smem_bytes);
 __global__ void k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems);
 
 __global__ void k_lr_sums(FrameDesc *frames, const WorkItem *items, int nitems);
@@ -22,6 +22,8 @@ __global__ void k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems)
 __global__ void k_lr_finish(FrameDesc *frames, int nframes);
 __global__ void k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems);
 
+constexpr int kFinClusterHost = 8;  // k_cdef_finish: CTAs per frame (cluster size)
+constexpr int kFinThreadsHost = 512;
 constexpr int kSumRowsHost = 16;   // k_lr_sums rows per CTA
 constexpr int kStatRowsHost = 16;  // k_lr_stats rows per CTA
 

@@ -662,50 +662,95 @@ __device__ __forceinline__ double rdcost_dbl(int64_t rdmult, int64_t rate, int64
     return __dadd_rn(__ddiv_rn(__dmul_rn((double)rate, (double)rdmult), 512.0), __dmul_rn((double)dist, 128.0));
 }
 
-__global__ void k_lr_finish(FrameDesc *frames, int nframes) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+// Per-unit RD inputs staged in shared memory (count_wiener_bits reads taps
+// 0..2 of each filter only).
+struct RdUnit {
+    int64_t sse_none, sse_wn;
+    int16_t v[3], h[3];
+    int16_t pick, pad;
+};
+
+__device__ int count_bits3(int win, const int16_t *v, const int16_t *h, const int16_t *rv, const int16_t *rh) {
+    auto tap = [](int f, int rf, int minv, int maxv, int k) {
+        return count_subexpfin(maxv - minv + 1, k, recenter_finite_nonneg(maxv - minv + 1, rf - minv, f - minv));
+    };
+    int bits = 0;
+    if (win == 7) bits += tap(v[0], rv[0], -5, 10, 1);
+    bits += tap(v[1], rv[1], -23, 8, 2);
+    bits += tap(v[2], rv[2], -17, 46, 3);
+    if (win == 7) bits += tap(h[0], rh[0], -5, 10, 1);
+    bits += tap(h[1], rh[1], -23, 8, 2);
+    bits += tap(h[2], rh[2], -17, 46, 3);
+    return bits;
+}
+
+// One warp per (frame, plane): lanes stage the unit data, lane 0 walks the
+// units in order with the reference-filter chain, lanes write the picks.
+__global__ void __launch_bounds__(32) k_lr_finish(FrameDesc *frames, int nframes) {
+    extern __shared__ unsigned char lr_dyn[];
+    RdUnit *U = reinterpret_cast<RdUnit *>(lr_dyn);
+    __shared__ int frame_rtype;
+    const int id = blockIdx.x;
     if (id >= nframes * 3) return;
     FrameDesc &f = frames[id / 3];
     LrPlane &pl = f.lr[id % 3];
+    const int lane = threadIdx.x;
     if (!pl.on) {
-        pl.frame_rtype = 0;
+        if (lane == 0) pl.frame_rtype = 0;
         return;
     }
     const int n = pl.hunits * pl.vunits;
-    int64_t sse_none_frame = 0;
-    for (int k = 0; k < n; ++k) sse_none_frame += pl.units[k].sse_none;
-    const double cost_none_frame = rdcost_dbl(f.rdmult, 0, sse_none_frame);
-    int64_t bits_frame = 0, sse_frame = 0;
-    int16_t rv[8] = {3, -7, 15, -22, 15, -7, 3, 0}, rh[8] = {3, -7, 15, -22, 15, -7, 3, 0};
-    for (int k = 0; k < n; ++k) {
-        LrUnit &u = pl.units[k];
-        u.rtype = 0;
-        if (u.sse_wn == INT64_MAX) {
-            bits_frame += 768;
-            sse_frame += u.sse_none;
-            continue;
+    int64_t part = 0;
+    for (int k = lane; k < n; k += 32) {
+        const LrUnit &u = pl.units[k];
+        RdUnit r;
+        r.sse_none = u.sse_none;
+        r.sse_wn = u.sse_wn;
+        for (int i = 0; i < 3; ++i) {
+            r.v[i] = u.vf[i];
+            r.h[i] = u.hf[i];
         }
-        const int64_t cnt = count_wiener_bits(pl.win, u.vf, u.hf, rv, rh);
-        const int64_t bits_wn = 320 + (cnt << 9), bits_none = 768;
-        const double cn = rdcost_dbl(f.rdmult, bits_none >> 4, u.sse_none);
-        const double cw = rdcost_dbl(f.rdmult, bits_wn >> 4, u.sse_wn);
-        if (cw < cn) {
-            u.rtype = 1;
-            bits_frame += bits_wn;
-            sse_frame += u.sse_wn;
-            for (int i = 0; i < 8; ++i) {
-                rv[i] = u.vf[i];
-                rh[i] = u.hf[i];
-            }
-        } else {
-            bits_frame += bits_none;
-            sse_frame += u.sse_none;
-        }
+        r.pick = 0;
+        U[k] = r;
+        part += u.sse_none;
     }
-    const double cost_wn_frame = rdcost_dbl(f.rdmult, bits_frame >> 4, sse_frame);
-    pl.frame_rtype = cost_wn_frame < cost_none_frame ? 1 : 0;
-    if (pl.frame_rtype == 0)
-        for (int k = 0; k < n; ++k) pl.units[k].rtype = 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+    __syncwarp();
+    if (lane == 0) {
+        const double cost_none_frame = rdcost_dbl(f.rdmult, 0, part);
+        int64_t bits_frame = 0, sse_frame = 0;
+        int16_t rv[3] = {3, -7, 15}, rh[3] = {3, -7, 15};
+        for (int k = 0; k < n; ++k) {
+            RdUnit &u = U[k];
+            if (u.sse_wn == INT64_MAX) {
+                bits_frame += 768;
+                sse_frame += u.sse_none;
+                continue;
+            }
+            const int64_t cnt = count_bits3(pl.win, u.v, u.h, rv, rh);
+            const int64_t bits_wn = 320 + (cnt << 9), bits_none = 768;
+            const double cn = rdcost_dbl(f.rdmult, bits_none >> 4, u.sse_none);
+            const double cw = rdcost_dbl(f.rdmult, bits_wn >> 4, u.sse_wn);
+            if (cw < cn) {
+                u.pick = 1;
+                bits_frame += bits_wn;
+                sse_frame += u.sse_wn;
+                for (int i = 0; i < 3; ++i) {
+                    rv[i] = u.v[i];
+                    rh[i] = u.h[i];
+                }
+            } else {
+                bits_frame += bits_none;
+                sse_frame += u.sse_none;
+            }
+        }
+        const double cost_wn_frame = rdcost_dbl(f.rdmult, bits_frame >> 4, sse_frame);
+        frame_rtype = cost_wn_frame < cost_none_frame ? 1 : 0;
+        pl.frame_rtype = frame_rtype;
+    }
+    __syncwarp();
+    for (int k = lane; k < n; k += 32) pl.units[k].rtype = frame_rtype ? U[k].pick : 0;
 }
 
 // ---------------------------------------------------------------------------
