@@ -207,6 +207,29 @@ int32_t zf_lr_search(zf_ctx *ctx, const zf_frame *f, zf_decisions *out);
 int32_t zf_lr_apply(zf_ctx *ctx, const zf_frame *f, const void *const pre_cdef[3],
                     const zf_decisions *d);
 
+/*
+ * Allocation-free CDEF strength search. No counterpart in the reference: it
+ * computes the same decisions as zf_cdef_search, for callers that cannot
+ * allocate device memory once running (an encoder loop that reserves all
+ * memory at start-up, code running while a stream capture is open, a
+ * process on a fully reserved GPU slice). It needs no zf_ctx and calls no
+ * allocator: its scratch is a static device array of about 1 MiB that every
+ * GPU loading the library keeps until exit.
+ *  - f must have planes_on_device = 1: rec = post-deblock planes, src, mi
+ *    are device pointers; out (and out->cdef_fb_idx) are host memory.
+ *  - stream is a cudaStream_t (NULL: the legacy default stream); the call
+ *    returns after synchronising it.
+ *  - Limits: at most 2048 64x64 filter blocks (3840x2160 has 2040) ->
+ *    ZF_ERR_INVALID_DIMS beyond; at most 20 candidate strengths (presets
+ *    1..6; preset 0) -> ZF_ERR_UNSUPPORTED. Presets >= 7 return the qp
+ *    closed form without device work.
+ *  - The first call on a device looks up the array's device address with
+ *    that device current; make that first call before any stream capture.
+ *  - All calls share the one array: calls that overlap on the GPU (other
+ *    streams, other host threads) race and must be serialised by the caller.
+ */
+int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_decisions *out);
+
 /* --- Observability ------------------------------------------------------- */
 
 typedef struct zf_kernel_time {

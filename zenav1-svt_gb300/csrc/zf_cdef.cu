@@ -598,3 +598,134 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
 }
 
 }  // namespace zf
+
+// ===========================================================================
+// Allocation-free CDEF strength search (zf_cdef_search_noalloc).
+//
+// Some callers cannot allocate device memory once they are running: an
+// encoder loop that reserves every byte at start-up and must not touch the
+// allocator per frame, code that runs while another component holds a
+// stream capture open (cudaMalloc is not allowed then), or a process on a
+// GPU slice whose memory is already fully reserved. For them this entry
+// point runs the same two kernels as zf_cdef_search, with all scratch in the
+// file-scope array below instead of a context arena. The array is modest
+// (about 1 MiB) and every GPU that loads the library holds it until the
+// process exits. Limits: at most kNoAllocMaxFb 64x64 filter blocks (a
+// 3840x2160 frame has 2040) and at most kNoAllocMaxCand candidate strengths
+// (presets 1..6; preset 0's 48 candidates are rejected).
+// ===========================================================================
+
+#include <mutex>
+
+#include "../../include/zf_filter.h"
+
+namespace zf {
+int describe_cdef_frame(const zf_frame *f, FrameDesc *d);  // zf_host.cu
+
+constexpr int kNoAllocMaxFb = 2048;
+constexpr int kNoAllocMaxCand = 20;
+
+struct NoAllocScratch {
+    FrameDesc desc;
+    WorkItem item;
+    int frame_id;
+    int pad;
+    uint64_t mse[kNoAllocMaxFb * 2 * kNoAllocMaxCand];
+    uint64_t best[kNoAllocMaxFb];
+    uint32_t rows32[kNoAllocMaxFb * 2 * kNoAllocMaxCand];
+    int ids[kNoAllocMaxFb];
+    uint8_t fb_row[kNoAllocMaxFb];
+    uint8_t fb_idx[kNoAllocMaxFb];
+};
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// Device address of g_noalloc_scratch per device, looked up on the first
+// call made with that device current.
+constexpr int kMaxDevices = 64;
+static NoAllocScratch *g_noalloc_addr[kMaxDevices];
+static std::mutex g_noalloc_mu;
+}  // namespace zf
+
+extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_decisions *out) {
+    using namespace zf;
+    if (!f || !out) return ZF_ERR_ARG;
+    if (!f->planes_on_device) return ZF_ERR_ARG;
+    FrameDesc d;
+    int e = describe_cdef_frame(f, &d);
+    if (e != ZF_OK) return e;
+    const int nfb = d.nhfb * d.nvfb;
+    out->nhfb = d.nhfb;
+    out->nvfb = d.nvfb;
+    if (d.cdef.mode != 1) {  // qp closed form: no device work (cdef.rs:151)
+        out->cdef_damping = (uint8_t)d.cdef.damping;
+        out->cdef_bits = 0;
+        std::memset(out->cdef_y, 0, 8);
+        std::memset(out->cdef_uv, 0, 8);
+        out->cdef_y[0] = d.cdef.y_str[0];
+        out->cdef_uv[0] = d.cdef.uv_str[0];
+        if (out->cdef_fb_idx) std::memset(out->cdef_fb_idx, 0, nfb);
+        return ZF_OK;
+    }
+    if (nfb > kNoAllocMaxFb) return ZF_ERR_INVALID_DIMS;   // frame larger than the static scratch
+    if (d.cdef.ncand > kNoAllocMaxCand) return ZF_ERR_UNSUPPORTED;  // preset 0
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return ZF_ERR_CUDA;
+    NoAllocScratch *sc;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void *p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+                cudaGetLastError();
+                return ZF_ERR_CUDA;
+            }
+            g_noalloc_addr[dev] = static_cast<NoAllocScratch *>(p);
+        }
+        sc = g_noalloc_addr[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    for (int p = 0; p < 3; ++p) {
+        const bool on = p == 0 || f->chroma_420;
+        d.B[p] = on ? (uint8_t *)f->rec[p] : nullptr;
+        d.S[p] = on ? (const uint8_t *)f->src[p] : nullptr;
+    }
+    d.mi = f->mi;
+    d.mse = sc->mse;
+    d.fb_row = sc->fb_row;
+    d.fb_idx = sc->fb_idx;
+    d.cdef_best = sc->best;
+    d.cdef_ids = sc->ids;
+    d.cdef_rows32 = sc->rows32;
+    d.cdef_stats = nullptr;
+    WorkItem item;
+    item.frame = 0;
+    item.plane = 0;
+    item.a = item.b = 0;
+    item.cta_begin = 0;
+    item.ctas = nfb;
+    const int frame_id = 0;
+    // Every field the kernels read is rewritten here; the kernels write every
+    // mse row, fb_row and fb_idx entry they later read, so nothing left from
+    // a previous call is consumed.
+    if (cudaMemcpyAsync(&sc->desc, &d, sizeof(d), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(&sc->item, &item, sizeof(item), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(&sc->frame_id, &frame_id, sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return ZF_ERR_CUDA;
+    k_cdef_search<<<nfb, 256, 0, st>>>(&sc->desc, &sc->item, 1);
+    const int per_cta = (nfb + kFinCluster - 1) / kFinCluster * (2 * d.cdef.ncand + 1) * 4;  // < 48 KiB
+    k_cdef_finish<<<kFinCluster, kFinThreads, per_cta, st>>>(&sc->desc, &sc->frame_id, per_cta);
+    if (cudaGetLastError() != cudaSuccess) return ZF_ERR_CUDA;
+    FrameDesc back;
+    if (cudaMemcpyAsync(&back, &sc->desc, sizeof(back), cudaMemcpyDeviceToHost, st) != cudaSuccess) return ZF_ERR_CUDA;
+    if (out->cdef_fb_idx &&
+        cudaMemcpyAsync(out->cdef_fb_idx, sc->fb_idx, nfb, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return ZF_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return ZF_ERR_CUDA;
+    out->cdef_damping = (uint8_t)back.cdef.damping;
+    out->cdef_bits = (uint8_t)back.cdef.bits;
+    std::memcpy(out->cdef_y, back.cdef.y_str, 8);
+    std::memcpy(out->cdef_uv, back.cdef.uv_str, 8);
+    if (out->cdef_fb_idx && back.cdef.bits == 0) std::memset(out->cdef_fb_idx, 0, nfb);
+    return ZF_OK;
+}

@@ -212,6 +212,25 @@ void cdef_search_cfg(int preset, CdefParams &cp) {
     cp.sub_uv = std::min(sub, 1);
 }
 
+// CDEF policy of pipeline.rs:3042-3144 for a still key frame: the RDO
+// search at presets <= 6, the qp closed form above.
+void cdef_policy(const zf_frame *f, CdefParams &cp) {
+    if (f->preset <= 6) {
+        cp.mode = 1;
+        cdef_search_cfg(f->preset, cp);
+        cp.damping = 3 + (f->qindex >> 6);
+        cp.lambda = f->bit_depth == 8 ? lambda_8bit_unweighted(f->qindex) : lambda_bd10_unweighted(f->qindex);
+    } else {
+        int q[3];
+        cdef_qp_params(f->qindex, f->bit_depth, f->sc_class5 != 0, q);
+        cp.mode = 2;
+        cp.damping = q[0];
+        cp.bits = 0;
+        cp.y_str[0] = (uint8_t)q[1];
+        cp.uv_str[0] = (uint8_t)q[2];
+    }
+}
+
 int count_units_in_tile(int unit, int size) { return std::max((size + (unit >> 1)) / unit, 1); }
 
 // foreach_rest_unit_in_tile (svtav1-dsp/src/restoration.rs:1395-1448).
@@ -378,22 +397,7 @@ void plan_frame(Plan &p, const zf_frame *f, size_t &cursor) {
     p.off_ids = take((size_t)p.nfb * 4);
     p.off_rows32 = take((size_t)p.nfb * 2 * zf::kMaxCand * 4);
     p.off_stats = take(4 * 8);
-    // CDEF policy (pipeline.rs:3042-3144).
-    CdefParams &cp = d.cdef;
-    if (f->preset <= 6) {
-        cp.mode = 1;
-        cdef_search_cfg(f->preset, cp);
-        cp.damping = 3 + (f->qindex >> 6);
-        cp.lambda = f->bit_depth == 8 ? lambda_8bit_unweighted(f->qindex) : lambda_bd10_unweighted(f->qindex);
-    } else {
-        int q[3];
-        cdef_qp_params(f->qindex, f->bit_depth, f->sc_class5 != 0, q);
-        cp.mode = 2;
-        cp.damping = q[0];
-        cp.bits = 0;
-        cp.y_str[0] = (uint8_t)q[1];
-        cp.uv_str[0] = (uint8_t)q[2];
-    }
+    cdef_policy(f, d.cdef);
     // Loop restoration (pipeline.rs:3225-3381).
     d.lr_on = lr_enabled(f) ? 1 : 0;
     d.rdmult = f->bit_depth == 10 ? (int64_t)lambda_bd10_unweighted(f->qindex) * 16
@@ -959,6 +963,31 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
 }
 
 }  // namespace
+
+namespace zf {
+// Dims and CDEF policy of a frame descriptor (no pointers), for entry points
+// outside this file that build their own descriptor.
+int describe_cdef_frame(const zf_frame *f, FrameDesc *d) {
+    const int e = validate_frame(nullptr, f);
+    if (e != ZF_OK) return e;
+    std::memset(d, 0, sizeof(*d));
+    d->bd = f->bit_depth;
+    d->w = f->width;
+    d->h = f->height;
+    d->tw = f->true_width;
+    d->th = f->true_height;
+    d->chroma = f->chroma_420 ? 1 : 0;
+    d->preset = f->preset;
+    d->qindex = f->qindex;
+    d->sharpness = f->sharpness;
+    d->mi_cols = f->width / 4;
+    d->mi_rows = f->height / 4;
+    d->nhfb = (f->width + 63) / 64;
+    d->nvfb = (f->height + 63) / 64;
+    cdef_policy(f, d->cdef);
+    return ZF_OK;
+}
+}  // namespace zf
 
 extern "C" {
 

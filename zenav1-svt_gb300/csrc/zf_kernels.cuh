@@ -2,6 +2,7 @@
 // zf_deblock.cu, zf_cdef.cu, zf_lr.cu; launched from zf_host.cu).
 #pragma once
 
+#include "../../include/zf_filter.h"
 #include "zf_dev.cuh"
 
 namespace zf {
@@ -21,6 +22,9 @@ __global__ void k_lr_solve(FrameDesc *frames, const WorkItem *items, int nitems)
 __global__ void k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems);
 __global__ void k_lr_finish(FrameDesc *frames, int nframes);
 __global__ void k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems);
+
+// Fills dims and the CDEF policy of *d from a frame (host; zf_host.cu).
+int describe_cdef_frame(const zf_frame *f, FrameDesc *d);
 
 constexpr int kFinClusterHost = 8;  // k_cdef_finish: CTAs per frame (cluster size)
 constexpr int kFinThreadsHost = 512;
