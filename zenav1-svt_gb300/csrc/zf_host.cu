@@ -552,7 +552,8 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 const UnitRect &r = p.rects[pl][u];
                 const int uh = r.v_end - r.v_start;
                 for (int c = 0; c < uh; c += zf::kSumRowsHost) wl_sum.add(i, pl, (int)u, c, 1);
-                for (int c = 0; c < uh; c += zf::kStatRowsHost) (L.win == 5 ? wl_st5 : wl_st7).add(i, pl, (int)u, c, 1);
+                const int half = L.win / 2, srows = zf::stat_rows_host(L.win);
+                for (int c = -half; c < uh + half; c += srows) (L.win == 5 ? wl_st5 : wl_st7).add(i, pl, (int)u, c, 1);
                 wl_unit.add(i, pl, (int)u, 0, 1);
             }
             const int ss = pl ? 1 : 0, full = 64 >> ss, off = 8 >> ss;

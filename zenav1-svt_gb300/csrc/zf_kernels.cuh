@@ -29,6 +29,8 @@ int describe_cdef_frame(const zf_frame *f, FrameDesc *d);
 constexpr int kFinClusterHost = 8;  // k_cdef_finish: CTAs per frame (cluster size)
 constexpr int kFinThreadsHost = 512;
 constexpr int kSumRowsHost = 16;   // k_lr_sums rows per CTA
-constexpr int kStatRowsHost = 16;  // k_lr_stats rows per CTA
+// k_lr_stats<win>: rows per CTA over the unit's rows extended by win/2 on
+// both sides (one thread per (row, row offset) plus one per (row, window row))
+constexpr int stat_rows_host(int win) { return 256 / (3 * win - 1); }
 
 }  // namespace zf

@@ -79,24 +79,43 @@ __global__ void __launch_bounds__(256) k_lr_sums(FrameDesc *frames, const WorkIt
 }
 
 // ---------------------------------------------------------------------------
-// 2. compute_stats: M[k] += y_k x, H[k][l] += y_k y_l (l >= k), y the win x
-// win window of (dgd - avg) in column-major order (idx = col * win + row).
-// A CTA takes kStatRows rows of one unit. Work is split into jobs: one job
-// per pair of window columns (ci <= cj) holding the win x win block of H,
-// plus one job for M; each job is run by `groups` threads over interleaved
-// pixels.
+// 2. compute_stats: M[a] = sum y_a x, H[a][b] = sum y_a y_b (b >= a) over the
+// unit, y the win x win window of D = dgd - avg in column-major order
+// (index = col * win + row), x = src - avg (restoration.rs:567-632, :1738).
+//
+// Regrouping (exact integer sums). With window offsets s_a = (ra - h, ca - h)
+// and delta = s_b - s_a = (dr, dc), H[a][b] = sum over the unit rectangle
+// shifted by s_a of P[y][x] = D[y][x] * D[y + dr][x + dc]. For a fixed delta
+// all (a, b) pairs share P and differ only in the shift, so each thread takes
+// one image row y and one dr, slides a register window along the row
+// computing P for every dc at once, and gets the row sums over all shifted
+// column windows [sc, sc + uw) from a running prefix; a row contributes to
+// every vertical shift sr with y in [sr, sr + uh). M uses the same sliding
+// window with X in place of the second factor. Row sums of <= 392 products
+// of magnitude <= 1023^2 fit int32; everything is folded into int64.
+//
+// A CTA covers kLrRows(WIN) consecutive rows of the unit's vertical range
+// extended by h = WIN/2 on both sides (items: a = unit, b = first row).
 // ---------------------------------------------------------------------------
-constexpr int kStatRows = 16;
 constexpr int kMaxUnitW = 384 + 8;
 
 template <int WIN>
+struct StatGeom {
+    static constexpr int H = WIN / 2;
+    static constexpr int NDR = 2 * WIN - 1;             // dr in [-(WIN-1), WIN-1]
+    static constexpr int ROWS = 256 / (NDR + WIN);      // rows per CTA (stat_rows_host)
+    static constexpr int DROWS = ROWS + 2 * (WIN - 1);  // staged D rows
+    static constexpr int DCOLS = kMaxUnitW + 2 * H + WIN;
+};
+
+template <int WIN>
 __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkItem *items, int nitems) {
-    constexpr int HALF = WIN / 2;
-    constexpr int WIN2 = WIN * WIN;
-    constexpr int NJOBS = WIN * (WIN + 1) / 2 + 1;
-    __shared__ int16_t dgd[(kStatRows + 2 * HALF) * kMaxUnitW];
-    __shared__ int16_t src[kStatRows * kMaxUnitW];
-    __shared__ long long part[NJOBS * WIN2];
+    using G = StatGeom<WIN>;
+    constexpr int HALF = G::H, WIN2 = WIN * WIN;
+    __shared__ int16_t D[G::DROWS * G::DCOLS];
+    __shared__ int16_t X[G::ROWS * kMaxUnitW];
+    __shared__ unsigned long long Hs[WIN2 * WIN2];
+    __shared__ unsigned long long Ms[WIN2];
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
     FrameDesc &f = frames[wi.frame];
@@ -105,87 +124,122 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
     LrUnit &u = pl.units[wi.a];
     const int bd = f.bd, stride = plane_stride(f, wi.plane);
     const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
-    const int i0 = wi.b, i1 = min(uh, wi.b + kStatRows), nr = i1 - i0;
-    const int64_t npx = (int64_t)uw * uh;
-    const int avg = (int)((unsigned long long)u.sum / (unsigned long long)npx);
-    const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
-    const int dws = uw + 2 * HALF;  // staged dgd row width
-    for (int q = threadIdx.x; q < (nr + 2 * HALF) * dws; q += blockDim.x) {
-        const int rr = q / dws, cc = q - rr * dws;
-        const int y = clampi(r.v_start + i0 - HALF + rr, 0, pl.ph - 1);
-        const int x = clampi(r.h_start - HALF + cc, 0, pl.pw - 1);
-        dgd[q] = (int16_t)(ldpx(dg, (int64_t)y * stride + x, bd) - avg);
+    const int avg = (int)((unsigned long long)u.sum / (unsigned long long)((int64_t)uw * uh));
+    const uint8_t *dg = f.A[wi.plane], *sr_ = f.S[wi.plane];
+    // rows of this CTA in unit coordinates (extended range [-HALF, uh + HALF))
+    const int y0 = wi.b, y1 = min(uh + HALF, y0 + G::ROWS);
+    // D rows [y0 - (WIN-1), y1 + (WIN-1)) clamped, columns [-HALF, uw + HALF + WIN)
+    const int dy0 = y0 - (WIN - 1), dx0 = -HALF;
+    const int dcols = uw + 2 * HALF + WIN;
+    const int drows = (y1 - y0) + 2 * (WIN - 1);
+    for (int q = threadIdx.x; q < drows * dcols; q += blockDim.x) {
+        const int rr = q / dcols, cc = q - rr * dcols;
+        const int y = clampi(r.v_start + dy0 + rr, 0, pl.ph - 1);
+        const int x = clampi(r.h_start + dx0 + cc, 0, pl.pw - 1);
+        D[rr * G::DCOLS + cc] = (int16_t)(ldpx(dg, (int64_t)y * stride + x, bd) - avg);
     }
-    for (int q = threadIdx.x; q < nr * uw; q += blockDim.x) {
+    const int xi0 = max(y0, 0), xi1 = min(y1, uh);
+    for (int q = threadIdx.x; q < (xi1 - xi0) * uw; q += blockDim.x) {
         const int rr = q / uw, cc = q - rr * uw;
-        src[q] = (int16_t)(ldpx(sr, (int64_t)(r.v_start + i0 + rr) * stride + r.h_start + cc, bd) - avg);
+        X[rr * kMaxUnitW + cc] =
+            (int16_t)(ldpx(sr_, (int64_t)(r.v_start + xi0 + rr) * stride + r.h_start + cc, bd) - avg);
     }
-    for (int q = threadIdx.x; q < NJOBS * WIN2; q += blockDim.x) part[q] = 0;
+    for (int q = threadIdx.x; q < WIN2 * WIN2; q += blockDim.x) Hs[q] = 0;
+    if (threadIdx.x < WIN2) Ms[threadIdx.x] = 0;
     __syncthreads();
-    const int groups = blockDim.x / NJOBS;
-    const int job = threadIdx.x / groups, grp = threadIdx.x - job * groups;
-    if (job < NJOBS) {
-        int ci = 0, cj = 0;
-        const bool mjob = job == NJOBS - 1;
-        if (!mjob) {
-            int k = job;
-            while (k >= WIN - ci) {
-                k -= WIN - ci;
-                ++ci;
+    auto Dat = [&](int y, int x) -> int { return D[(y - dy0) * G::DCOLS + (x - dx0)]; };
+
+    const int nh = G::NDR * (y1 - y0);
+    const int t = threadIdx.x;
+    if (t < nh) {
+        // ---- H: one (row y, dr) per thread
+        const int dr = t % G::NDR - (WIN - 1);
+        const int y = y0 + t / G::NDR;
+        // the row and its partner must lie in the extended range
+        if (y + dr >= -HALF && y + dr < uh + HALF) {
+            const int dc0 = dr < 0 ? 1 : 0;  // dc = 0 only for dr >= 0
+            int pre[WIN], rs[WIN][WIN];      // rs[dc][sc + HALF]
+#pragma unroll
+            for (int k = 0; k < WIN; ++k) {
+                pre[k] = 0;
+#pragma unroll
+                for (int j = 0; j < WIN; ++j) rs[k][j] = 0;
             }
-            cj = ci + k;
-        }
-        int acc[WIN][WIN];
+            int win[WIN];  // D[y + dr][x + dc], dc = 0..WIN-1
 #pragma unroll
-        for (int a = 0; a < WIN; ++a)
+            for (int k = 0; k < WIN - 1; ++k) win[k + 1] = Dat(y + dr, -HALF + k);
+            // x runs over [-HALF, uw + HALF); prefix bookkeeping at the
+            // column-window starts (x = sc) and ends (x = sc + uw).
+            for (int x = -HALF; x < uw + HALF; ++x) {
 #pragma unroll
-            for (int b = 0; b < WIN; ++b) acc[a][b] = 0;
-        const int npix = nr * uw;
-        for (int q = grp; q < npix; q += groups) {
-            const int i = q / uw, j = q - i * uw;
-            // window row rr, column c: dgd[(i + rr) * dws + j + c]
-            if (mjob) {
-                const int x = src[i * uw + j];
+                for (int k = 0; k < WIN - 1; ++k) win[k] = win[k + 1];
+                win[WIN - 1] = Dat(y + dr, x + WIN - 1);
+                const bool edge = x < HALF + 1 || x >= uw - HALF;
+                if (edge) {
 #pragma unroll
-                for (int c = 0; c < WIN; ++c)
+                    for (int dc = 0; dc < WIN; ++dc)
 #pragma unroll
-                    for (int rr = 0; rr < WIN; ++rr) acc[c][rr] += dgd[(i + rr) * dws + j + c] * x;
-            } else {
-                int av[WIN], bv[WIN];
-#pragma unroll
-                for (int rr = 0; rr < WIN; ++rr) {
-                    av[rr] = dgd[(i + rr) * dws + j + ci];
-                    bv[rr] = dgd[(i + rr) * dws + j + cj];
+                        for (int sc = -HALF; sc <= HALF; ++sc) {
+                            if (sc + HALF + dc > WIN - 1) continue;  // cb = ca + dc < WIN
+                            if (x == sc) rs[dc][sc + HALF] -= pre[dc];
+                            if (x == sc + uw) rs[dc][sc + HALF] += pre[dc];
+                        }
                 }
+                const int a = Dat(y, x);
 #pragma unroll
-                for (int a = 0; a < WIN; ++a)
+                for (int dc = 0; dc < WIN; ++dc) pre[dc] += a * win[dc];
+            }
+            // x == uw + HALF ends the windows with sc = HALF
 #pragma unroll
-                    for (int b = 0; b < WIN; ++b) acc[a][b] += av[a] * bv[b];
+            for (int dc = 0; dc < WIN; ++dc)
+                if (HALF + HALF + dc <= WIN - 1) rs[dc][2 * HALF] += pre[dc];
+            // contributions: H[a][b], a = (ca, ra), b = (ca + dc, ra + dr)
+#pragma unroll
+            for (int dc = 0; dc < WIN; ++dc) {
+                if (dc < dc0) continue;
+#pragma unroll
+                for (int ca = 0; ca + dc < WIN; ++ca) {
+                    const int v = rs[dc][ca];
+                    if (v == 0) continue;
+                    for (int ra = max(0, -dr); ra < min(WIN, WIN - dr); ++ra) {
+                        const int sr = ra - HALF;
+                        if (y < sr || y >= sr + uh) continue;
+                        const int ia = ca * WIN + ra, ib = (ca + dc) * WIN + ra + dr;
+                        atomicAdd(&Hs[ia * WIN2 + ib], (unsigned long long)(long long)v);
+                    }
+                }
             }
         }
+    } else if (t < nh + WIN * (xi1 - xi0)) {
+        // ---- M: one (row i, ra) per thread
+        const int q = t - nh;
+        const int ra = q % WIN, i = xi0 + q / WIN;
+        const int yy = i + ra - HALF;
+        int acc[WIN];
+        int win[WIN];  // D[yy][j + ca - HALF], ca = 0..WIN-1
 #pragma unroll
-        for (int a = 0; a < WIN; ++a)
+        for (int k = 0; k < WIN; ++k) acc[k] = 0;
 #pragma unroll
-            for (int b = 0; b < WIN; ++b)
-                atomicAdd((unsigned long long *)&part[job * WIN2 + a * WIN + b],
-                          (unsigned long long)(long long)acc[a][b]);
+        for (int k = 0; k < WIN - 1; ++k) win[k + 1] = Dat(yy, -HALF + k);
+        const int16_t *xr = X + (i - xi0) * kMaxUnitW;
+        for (int j = 0; j < uw; ++j) {
+#pragma unroll
+            for (int k = 0; k < WIN - 1; ++k) win[k] = win[k + 1];
+            win[WIN - 1] = Dat(yy, j + HALF);
+            const int xv = xr[j];
+#pragma unroll
+            for (int ca = 0; ca < WIN; ++ca) acc[ca] += win[ca] * xv;
+        }
+#pragma unroll
+        for (int ca = 0; ca < WIN; ++ca)
+            atomicAdd(&Ms[ca * WIN + ra], (unsigned long long)(long long)acc[ca]);
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < NJOBS * WIN2; q += blockDim.x) {
-        const int jb = q / WIN2, a = (q / WIN) % WIN, b = q % WIN;
-        if (jb == NJOBS - 1) {
-            atomicAdd((unsigned long long *)&u.m[a * WIN + b], (unsigned long long)part[q]);
-        } else {
-            int ci = 0, k = jb;
-            while (k >= WIN - ci) {
-                k -= WIN - ci;
-                ++ci;
-            }
-            const int cj = ci + k;
-            const int kk = ci * WIN + a, ll = cj * WIN + b;
-            if (ll >= kk) atomicAdd((unsigned long long *)&u.h[kk * WIN2 + ll], (unsigned long long)part[q]);
-        }
+    for (int q = threadIdx.x; q < WIN2 * WIN2; q += blockDim.x) {
+        const int ia = q / WIN2, ib = q - ia * WIN2;
+        if (ib >= ia && Hs[q]) atomicAdd((unsigned long long *)&u.h[q], Hs[q]);
     }
+    if (threadIdx.x < WIN2 && Ms[threadIdx.x]) atomicAdd((unsigned long long *)&u.m[threadIdx.x], Ms[threadIdx.x]);
 }
 
 // ---------------------------------------------------------------------------
