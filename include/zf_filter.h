@@ -145,6 +145,13 @@ int32_t zf_sync(zf_ctx *ctx);
 /* The context's CUDA stream (a cudaStream_t), for callers that order their
  * own work or timing events against the library's launches. */
 void *zf_stream(const zf_ctx *ctx);
+/* Device memory the context holds now (its arena; grows to the largest
+ * batch seen, never shrinks by itself). No counterpart in the reference:
+ * the served request loop admits work against an HBM budget with it. */
+uint64_t zf_device_bytes(const zf_ctx *ctx);
+/* Release the context's arena (after synchronising its stream); the next
+ * call allocates again. No counterpart in the reference. */
+int32_t zf_trim(zf_ctx *ctx);
 
 /* Output array sizes for a frame (filter blocks, restoration units). */
 int32_t zf_query_sizes(const zf_frame *f, zf_sizes *out);

@@ -72,6 +72,10 @@ def lib():
     L.zf_stream.restype = C.c_void_p
     L.zf_launch_count.argtypes = [C.c_void_p]
     L.zf_launch_count.restype = C.c_uint64
+    L.zf_device_bytes.argtypes = [C.c_void_p]
+    L.zf_device_bytes.restype = C.c_uint64
+    L.zf_trim.argtypes = [C.c_void_p]
+    L.zf_trim.restype = C.c_int32
     L.zf_profile_enable.argtypes = [C.c_void_p, C.c_int32]
     L.zf_profile_reset.argtypes = [C.c_void_p]
     L.zf_profile_reset.restype = None
@@ -141,6 +145,14 @@ class Context:
 
     def launch_count(self):
         return lib().zf_launch_count(self.h)
+
+    def device_bytes(self):
+        """Device memory the context holds (its arena)."""
+        return lib().zf_device_bytes(self.h)
+
+    def trim(self):
+        """Release the arena (the next call allocates again)."""
+        self._check(lib().zf_trim(self.h))
 
     def profile(self, enable=True):
         self._check(lib().zf_profile_enable(self.h, 1 if enable else 0))

@@ -39,6 +39,13 @@ struct LrUnit {
     int32_t pad;
 };
 
+// Output record of a unit (the layout of zf_lr_unit in the C ABI).
+struct PackedUnit {
+    int16_t vf[8], hf[8];
+    uint8_t rtype;
+    uint8_t pad[7];
+};
+
 struct LrPlane {
     int on;              // plane searched
     int win;             // 5 or 7
@@ -49,6 +56,7 @@ struct LrPlane {
     int refine;          // finer_tile_search_wiener refinement (presets <= 3)
     UnitRect *rects;     // hunits*vunits
     LrUnit *units;       // hunits*vunits
+    PackedUnit *packed;  // hunits*vunits output records
 };
 
 struct CdefParams {

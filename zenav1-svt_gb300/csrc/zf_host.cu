@@ -26,6 +26,8 @@ using zf::LrUnit;
 using zf::UnitRect;
 using zf::WorkItem;
 
+static_assert(sizeof(zf::PackedUnit) == sizeof(zf_lr_unit), "unit record layout");
+
 struct zf_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -43,6 +45,11 @@ struct zf_ctx {
     };
     std::vector<Pending> pending;
     std::vector<zf_kernel_time> totals;
+    // pinned host staging: the batch's metadata image (descriptors, work
+    // lists, unit rectangles) goes up in one copy, the decisions come back
+    // in one copy
+    uint8_t *h_meta = nullptr, *h_out = nullptr;
+    size_t h_meta_cap = 0, h_out_cap = 0;
 };
 
 namespace {
@@ -325,9 +332,13 @@ struct Plan {
     int nfb = 0;
     size_t off_set[3][3];             // [set A/B/C][plane]
     size_t off_src[3];
-    size_t off_mi = 0, off_mse = 0, off_fbrow = 0, off_fbidx = 0, off_best = 0, off_stats = 0;
-    size_t off_ids = 0, off_rows32 = 0;
-    size_t off_rects[3], off_units[3];
+    size_t off_mi = 0, off_mse = 0, off_best = 0, off_ids = 0, off_rows32 = 0;
+    // relative to the batch's units region (zeroed with one memset)
+    size_t off_units[3];
+    // relative to the rectangles part of the metadata region
+    size_t off_rects[3];
+    // relative to the output region (read back with one copy)
+    size_t off_fbrow = 0, off_fbidx = 0, off_stats = 0, off_packed[3];
     std::vector<UnitRect> rects[3];
     int hunits[3], vunits[3];
     bool db_search = false;
@@ -358,7 +369,9 @@ bool lr_enabled(const zf_frame *f) {
     return f->enable_restoration && f->preset <= 6 && f->true_width >= 64 && f->true_height >= 64;
 }
 
-void plan_frame(Plan &p, const zf_frame *f, size_t &cursor) {
+// Offsets: per-frame device buffers at `cursor`; the unit accumulators,
+// rectangles and outputs in three batch-wide regions (ucur, rcur, ocur).
+void plan_frame(Plan &p, const zf_frame *f, size_t &cursor, size_t &ucur, size_t &rcur, size_t &ocur) {
     p.in = f;
     std::memset(&p.d, 0, sizeof(p.d));
     FrameDesc &d = p.d;
@@ -380,23 +393,24 @@ void plan_frame(Plan &p, const zf_frame *f, size_t &cursor) {
     p.nplanes = f->chroma_420 ? 3 : 1;
     p.pbytes[0] = (size_t)f->width * f->height * p.px;
     p.pbytes[1] = p.pbytes[2] = (size_t)(f->width / 2) * (f->height / 2) * p.px;
-    auto take = [&](size_t n) {
-        cursor = align_up(cursor, 256);
-        size_t o = cursor;
-        cursor += n;
+    auto take_in = [](size_t &c, size_t n) {
+        c = align_up(c, 256);
+        size_t o = c;
+        c += n;
         return o;
     };
+    auto take = [&](size_t n) { return take_in(cursor, n); };
     for (int s = 0; s < 3; ++s)
         for (int pl = 0; pl < 3; ++pl) p.off_set[s][pl] = pl < p.nplanes ? take(p.pbytes[pl]) : 0;
     for (int pl = 0; pl < 3; ++pl) p.off_src[pl] = pl < p.nplanes ? take(p.pbytes[pl]) : 0;
     p.off_mi = take((size_t)d.mi_cols * d.mi_rows * 4);
     p.off_mse = take((size_t)p.nfb * 2 * zf::kMaxCand * 8);
-    p.off_fbrow = take(p.nfb);
-    p.off_fbidx = take(p.nfb);
     p.off_best = take((size_t)p.nfb * 8);
     p.off_ids = take((size_t)p.nfb * 4);
     p.off_rows32 = take((size_t)p.nfb * 2 * zf::kMaxCand * 4);
-    p.off_stats = take(4 * 8);
+    p.off_fbrow = take_in(ocur, p.nfb);
+    p.off_fbidx = take_in(ocur, p.nfb);
+    p.off_stats = take_in(ocur, 4 * 8);
     cdef_policy(f, d.cdef);
     // Loop restoration (pipeline.rs:3225-3381).
     d.lr_on = lr_enabled(f) ? 1 : 0;
@@ -418,13 +432,14 @@ void plan_frame(Plan &p, const zf_frame *f, size_t &cursor) {
         L.vunits = p.vunits[pl];
         L.refine = f->preset <= 3;
         rest_units(pw, ph, ss, p.rects[pl]);
-        p.off_rects[pl] = take(p.rects[pl].size() * sizeof(UnitRect));
-        p.off_units[pl] = take(L.on ? p.rects[pl].size() * sizeof(LrUnit) : 0);
+        p.off_rects[pl] = take_in(rcur, p.rects[pl].size() * sizeof(UnitRect));
+        p.off_units[pl] = take_in(ucur, L.on ? p.rects[pl].size() * sizeof(LrUnit) : 0);
+        p.off_packed[pl] = take_in(ocur, L.on ? p.rects[pl].size() * sizeof(zf::PackedUnit) : 0);
     }
     p.db_search = f->preset <= 5;
 }
 
-void bind_pointers(Plan &p, uint8_t *base) {
+void bind_pointers(Plan &p, uint8_t *base, uint8_t *units, uint8_t *rects, uint8_t *out) {
     FrameDesc &d = p.d;
     for (int pl = 0; pl < 3; ++pl) {
         const bool on = pl < p.nplanes;
@@ -432,17 +447,36 @@ void bind_pointers(Plan &p, uint8_t *base) {
         d.B[pl] = on ? base + p.off_set[1][pl] : nullptr;
         d.C[pl] = on ? base + p.off_set[2][pl] : nullptr;
         d.S[pl] = on ? base + p.off_src[pl] : nullptr;
-        d.lr[pl].rects = (UnitRect *)(base + p.off_rects[pl]);
-        d.lr[pl].units = d.lr[pl].on ? (LrUnit *)(base + p.off_units[pl]) : nullptr;
+        d.lr[pl].rects = (UnitRect *)(rects + p.off_rects[pl]);
+        d.lr[pl].units = d.lr[pl].on ? (LrUnit *)(units + p.off_units[pl]) : nullptr;
+        d.lr[pl].packed = d.lr[pl].on ? (zf::PackedUnit *)(out + p.off_packed[pl]) : nullptr;
     }
     d.mi = (const uint32_t *)(base + p.off_mi);
     d.mse = (uint64_t *)(base + p.off_mse);
-    d.fb_row = base + p.off_fbrow;
-    d.fb_idx = base + p.off_fbidx;
+    d.fb_row = out + p.off_fbrow;
+    d.fb_idx = out + p.off_fbidx;
     d.cdef_best = (uint64_t *)(base + p.off_best);
     d.cdef_ids = (int *)(base + p.off_ids);
     d.cdef_rows32 = (uint32_t *)(base + p.off_rows32);
-    d.cdef_stats = (unsigned long long *)(base + p.off_stats);
+    d.cdef_stats = (unsigned long long *)(out + p.off_stats);
+}
+
+// Pinned host staging buffers (grow only).
+int ensure_host(zf_ctx *ctx, uint8_t *&buf, size_t &cap, size_t need) {
+    if (need <= cap) return ZF_OK;
+    if (buf) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFreeHost(buf);
+        buf = nullptr;
+        cap = 0;
+    }
+    const size_t c = align_up(need + need / 4, 1 << 16);
+    if (cudaHostAlloc((void **)&buf, c, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, ZF_ERR_ALLOC, "pinned host staging allocation failed");
+    }
+    cap = c;
+    return ZF_OK;
 }
 
 int ensure_arena(zf_ctx *ctx, size_t need) {
@@ -500,13 +534,6 @@ struct WorkList {
     }
 };
 
-int upload_list(zf_ctx *ctx, const WorkList &wl, uint8_t *dst) {
-    if (wl.items.empty()) return ZF_OK;
-    CU(cudaMemcpyAsync(dst, wl.items.data(), wl.items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
-                       ctx->stream));
-    return ZF_OK;
-}
-
 int launch_check(zf_ctx *ctx, const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(ctx, ZF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -525,10 +552,10 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     CU(cudaSetDevice(ctx->device));
     TRY(check_cancel(ctx));
     std::vector<Plan> plans((size_t)n);
-    size_t cursor = 0;
+    size_t cursor = 0, ucur = 0, rcur = 0, ocur = 0;
     for (int i = 0; i < n; ++i) {
         TRY(validate_frame(ctx, &frames[i]));
-        plan_frame(plans[i], &frames[i], cursor);
+        plan_frame(plans[i], &frames[i], cursor, ucur, rcur, ocur);
         plans[i].out = outs ? &outs[i] : nullptr;
     }
     // Work lists (host-known shapes).
@@ -559,58 +586,69 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             const int ss = pl ? 1 : 0, full = 64 >> ss, off = 8 >> ss;
             const int nstripes = (L.ph + off + full - 1) / full;
             const int ntiles = (L.pw + 63) / 64;
-            // unit of a (stripe, tile): rows and columns of the unit grid
-            for (int s = 0; s < nstripes; ++s) {
+            // unit of a (stripe, tile): the rectangles form a row-major
+            // hunits x vunits grid, so look the column up along the first
+            // row and the row along the first column
+            const std::vector<UnitRect> &R = p.rects[pl];
+            const int hu = p.hunits[pl], vu = p.vunits[pl];
+            std::vector<int> col((size_t)ntiles, -1);
+            for (int t = 0, c = 0; t < ntiles; ++t) {
+                const int x = t * 64;
+                while (c < hu && x >= R[c].h_end) ++c;
+                if (c < hu && x >= R[c].h_start) col[t] = c;
+            }
+            for (int s = 0, r = 0; s < nstripes; ++s) {
                 const int ys = std::max(0, s * full - off);
-                for (int t = 0; t < ntiles; ++t) {
-                    const int x = t * 64;
-                    int uidx = -1;
-                    for (size_t u = 0; u < p.rects[pl].size(); ++u) {
-                        const UnitRect &r = p.rects[pl][u];
-                        if (ys >= r.v_start && ys < r.v_end && x >= r.h_start && x < r.h_end) {
-                            uidx = (int)u;
-                            break;
-                        }
-                    }
-                    if (uidx >= 0) wl_apply.add(i, pl, uidx, (s << 16) | t, 1);
-                }
+                while (r < vu && ys >= R[(size_t)r * hu].v_end) ++r;
+                if (r >= vu || ys < R[(size_t)r * hu].v_start) continue;
+                for (int t = 0; t < ntiles; ++t)
+                    if (col[t] >= 0) wl_apply.add(i, pl, r * hu + col[t], (s << 16) | t, 1);
             }
         }
     }
-    const size_t desc_bytes = align_up((size_t)n * sizeof(FrameDesc), 256);
-    auto lsz = [](const WorkList &w) { return align_up(w.items.size() * sizeof(WorkItem) + 16, 256); };
-    const size_t o_desc = align_up(cursor, 256);
-    size_t c2 = o_desc + desc_bytes;
-    const size_t o_db = c2;
-    c2 += lsz(wl_db);
-    const size_t o_cs = c2;
-    c2 += lsz(wl_cs);
-    const size_t o_ca = c2;
-    c2 += lsz(wl_ca);
-    const size_t o_sum = c2;
-    c2 += lsz(wl_sum);
-    const size_t o_st5 = c2;
-    c2 += lsz(wl_st5);
-    const size_t o_st7 = c2;
-    c2 += lsz(wl_st7);
-    const size_t o_unit = c2;
-    c2 += lsz(wl_unit);
-    const size_t o_apply = c2;
-    c2 += lsz(wl_apply);
-    const size_t o_cf = c2;
-    c2 += align_up(cdef_frames.size() * 4 + 16, 256);
+    // Arena: per-frame buffers | unit accumulators | metadata image |
+    // deblock search scratch | outputs.
+    const size_t o_units = align_up(cursor, 256);
+    const size_t o_meta = align_up(o_units + ucur, 256);
+    size_t mcur = 0;
+    auto mtake = [&mcur](size_t b) {
+        mcur = align_up(mcur, 256);
+        const size_t o = mcur;
+        mcur += b + 16;
+        return o;
+    };
+    const size_t desc_bytes = (size_t)n * sizeof(FrameDesc);
+    const size_t m_desc = mtake(desc_bytes);
+    const WorkList *lists[8] = {&wl_db, &wl_cs, &wl_ca, &wl_sum, &wl_st5, &wl_st7, &wl_unit, &wl_apply};
+    size_t m_list[8];
+    for (int k = 0; k < 8; ++k) m_list[k] = mtake(lists[k]->items.size() * sizeof(WorkItem));
+    const size_t m_cf = mtake(cdef_frames.size() * 4);
+    const size_t m_rects = mtake(rcur);
+    const size_t meta_bytes = align_up(mcur, 256);
     // deblock search scratch: up to 3 slots per frame
+    size_t c2 = o_meta + meta_bytes;
     const size_t o_dbs_items = c2;
     c2 += align_up((size_t)n * 3 * 8 * sizeof(WorkItem) + 16, 256);
     const size_t o_dbs_lv = c2;
     c2 += align_up((size_t)n * 3 * 2 * 4, 256);
     const size_t o_dbs_sse = c2;
     c2 += align_up((size_t)n * 3 * 2 * 8, 256);
+    const size_t o_out = c2;
+    const size_t out_bytes = align_up(ocur, 256);
+    c2 += out_bytes;
     TRY(ensure_arena(ctx, c2));
+    const size_t hdesc = align_up(desc_bytes, 256);
+    TRY(ensure_host(ctx, ctx->h_meta, ctx->h_meta_cap, meta_bytes + hdesc));
+    TRY(ensure_host(ctx, ctx->h_out, ctx->h_out_cap, hdesc + out_bytes));
     uint8_t *base = ctx->arena;
     cudaStream_t st = ctx->stream;
-    for (auto &p : plans) bind_pointers(p, base);
-    FrameDesc *d_desc = (FrameDesc *)(base + o_desc);
+    for (auto &p : plans) bind_pointers(p, base, base + o_units, base + o_meta + m_rects, base + o_out);
+    FrameDesc *d_desc = (FrameDesc *)(base + o_meta + m_desc);
+    const size_t o_db = o_meta + m_list[0], o_cs = o_meta + m_list[1], o_ca = o_meta + m_list[2],
+                 o_sum = o_meta + m_list[3], o_st5 = o_meta + m_list[4], o_st7 = o_meta + m_list[5],
+                 o_unit = o_meta + m_list[6], o_apply = o_meta + m_list[7], o_cf = o_meta + m_cf;
+    // outputs start zeroed (statistics counters, fb_idx of skipped searches)
+    CU(cudaMemsetAsync(base + o_out, 0, out_bytes, st));
 
     // ---- inputs
     for (int i = 0; i < n; ++i) {
@@ -626,9 +664,8 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         TRY(copy_in(ctx, base + p.off_mi, f->mi, (size_t)p.d.mi_cols * p.d.mi_rows * 4, dev));
         for (int pl = 0; pl < 3; ++pl)
             if (!p.rects[pl].empty())
-                CU(cudaMemcpyAsync(base + p.off_rects[pl], p.rects[pl].data(), p.rects[pl].size() * sizeof(UnitRect),
-                                   cudaMemcpyHostToDevice, st));
-        CU(cudaMemsetAsync(base + p.off_stats, 0, 32, st));
+                std::memcpy(ctx->h_meta + m_rects + p.off_rects[pl], p.rects[pl].data(),
+                            p.rects[pl].size() * sizeof(UnitRect));
         // decisions the caller provides
         const zf_decisions *dec = p.out;
         if (run.lf_given) std::memcpy(p.d.lf, dec->lf, 4);
@@ -641,7 +678,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             std::memcpy(cp.uv_str, dec->cdef_uv, 8);
             if (cp.bits) {
                 if (!dec->cdef_fb_idx) return fail(ctx, ZF_ERR_ARG, "cdef_bits > 0 needs cdef_fb_idx");
-                CU(cudaMemcpyAsync(base + p.off_fbidx, dec->cdef_fb_idx, p.nfb, cudaMemcpyHostToDevice, st));
+                CU(cudaMemcpyAsync(base + o_out + p.off_fbidx, dec->cdef_fb_idx, p.nfb, cudaMemcpyHostToDevice, st));
             }
         }
         if (run.lr_given) {
@@ -690,11 +727,12 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 key_frame_levels(p.in->qindex, p.in->bit_depth, p.d.lf);
             }
         }
-        {
-            std::vector<FrameDesc> hd((size_t)n);
+        if (!slots.empty()) {
+            // the trial kernels read the descriptors (spare slot after the
+            // metadata image; the final image goes up after the search)
+            FrameDesc *hd = (FrameDesc *)(ctx->h_meta + meta_bytes);
             for (int i = 0; i < n; ++i) hd[i] = plans[i].d;
-            CU(cudaMemcpyAsync(d_desc, hd.data(), (size_t)n * sizeof(FrameDesc), cudaMemcpyHostToDevice, st));
-            CU(cudaStreamSynchronize(st));
+            CU(cudaMemcpyAsync(d_desc, hd, desc_bytes, cudaMemcpyHostToDevice, st));
         }
         bool chroma_phase = false;
         for (int guard = 0; guard < 256 && !slots.empty(); ++guard) {
@@ -765,22 +803,18 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             for (auto &s : slots) plans[s.frame].d.lf[1 + s.plane] = (uint8_t)s.hc.result;
     }
 
-    // ---- descriptors and work lists to the device
+    // ---- metadata image (descriptors, work lists, CDEF frames, unit
+    // rectangles) to the device in one copy
     {
-        std::vector<FrameDesc> hd((size_t)n);
+        uint8_t *hm = ctx->h_meta;
+        FrameDesc *hd = (FrameDesc *)(hm + m_desc);
         for (int i = 0; i < n; ++i) hd[i] = plans[i].d;
-        CU(cudaMemcpyAsync(d_desc, hd.data(), (size_t)n * sizeof(FrameDesc), cudaMemcpyHostToDevice, st));
+        for (int k = 0; k < 8; ++k)
+            if (!lists[k]->items.empty())
+                std::memcpy(hm + m_list[k], lists[k]->items.data(), lists[k]->items.size() * sizeof(WorkItem));
+        if (!cdef_frames.empty()) std::memcpy(hm + m_cf, cdef_frames.data(), cdef_frames.size() * 4);
+        CU(cudaMemcpyAsync(base + o_meta, hm, meta_bytes, cudaMemcpyHostToDevice, st));
     }
-    TRY(upload_list(ctx, wl_db, base + o_db));
-    TRY(upload_list(ctx, wl_cs, base + o_cs));
-    TRY(upload_list(ctx, wl_ca, base + o_ca));
-    TRY(upload_list(ctx, wl_sum, base + o_sum));
-    TRY(upload_list(ctx, wl_st5, base + o_st5));
-    TRY(upload_list(ctx, wl_st7, base + o_st7));
-    TRY(upload_list(ctx, wl_unit, base + o_unit));
-    TRY(upload_list(ctx, wl_apply, base + o_apply));
-    if (!cdef_frames.empty())
-        CU(cudaMemcpyAsync(base + o_cf, cdef_frames.data(), cdef_frames.size() * 4, cudaMemcpyHostToDevice, st));
 
     // ---- deblock apply: A -> B
     if (run.stages & STG_DB_APPLY) {
@@ -819,10 +853,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     }
     // ---- Wiener search on A
     if ((run.stages & STG_LR_SEARCH) && !run.lr_given) {
-        for (int i = 0; i < n; ++i)
-            for (int pl = 0; pl < 3; ++pl)
-                if (plans[i].d.lr[pl].on)
-                    CU(cudaMemsetAsync(plans[i].d.lr[pl].units, 0, plans[i].rects[pl].size() * sizeof(LrUnit), st));
+        if (ucur) CU(cudaMemsetAsync(base + o_units, 0, ucur, st));
         if (wl_sum.ctas) {
             { LaunchScope ls_(ctx, "k_lr_sums");
             zf::k_lr_sums<<<wl_sum.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_sum),
@@ -874,12 +905,8 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         }
     }
 
-    // ---- outputs
-    std::vector<FrameDesc> back((size_t)n);
-    CU(cudaMemcpyAsync(back.data(), d_desc, (size_t)n * sizeof(FrameDesc), cudaMemcpyDeviceToHost, st));
-    std::vector<std::vector<uint8_t>> fbidx((size_t)n), fbrow((size_t)n);
-    std::vector<std::vector<unsigned long long>> cst((size_t)n);
-    std::vector<std::vector<LrUnit>> units((size_t)n * 3);
+    // ---- outputs: planes to the caller, then the descriptors and the output
+    // region (fb_idx, fb_row, counters, unit records) in two copies
     for (int i = 0; i < n; ++i) {
         Plan &p = plans[i];
         const zf_frame *f = p.in;
@@ -887,26 +914,21 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         if (run.stages & (STG_DB_APPLY | STG_CDEF_APPLY | STG_LR_APPLY))
             for (int pl = 0; pl < p.nplanes; ++pl)
                 TRY(copy_out(ctx, f->rec[pl], base + p.off_set[run.rec_out][pl], p.pbytes[pl], dev));
-        fbidx[i].resize(p.nfb);
-        fbrow[i].resize(p.nfb);
-        cst[i].resize(4);
-        CU(cudaMemcpyAsync(fbidx[i].data(), base + p.off_fbidx, p.nfb, cudaMemcpyDeviceToHost, st));
-        CU(cudaMemcpyAsync(fbrow[i].data(), base + p.off_fbrow, p.nfb, cudaMemcpyDeviceToHost, st));
-        CU(cudaMemcpyAsync(cst[i].data(), base + p.off_stats, 32, cudaMemcpyDeviceToHost, st));
-        if (run.stages & STG_LR_SEARCH)
-            for (int pl = 0; pl < 3; ++pl)
-                if (p.d.lr[pl].on) {
-                    units[(size_t)i * 3 + pl].resize(p.rects[pl].size());
-                    CU(cudaMemcpyAsync(units[(size_t)i * 3 + pl].data(), p.d.lr[pl].units,
-                                       p.rects[pl].size() * sizeof(LrUnit), cudaMemcpyDeviceToHost, st));
-                }
     }
+    CU(cudaMemcpyAsync(ctx->h_out, d_desc, desc_bytes, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(ctx->h_out + hdesc, base + o_out, out_bytes, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     TRY(launch_check(ctx, "stream"));
     collect_profile(ctx);
+    const FrameDesc *back = (const FrameDesc *)ctx->h_out;
+    const uint8_t *ob = ctx->h_out + hdesc;
     for (int i = 0; i < n; ++i) {
         Plan &p = plans[i];
         const FrameDesc &b = back[i];
+        const uint8_t *fbidx = ob + p.off_fbidx, *fbrow = ob + p.off_fbrow;
+        const unsigned long long *cst = (const unsigned long long *)(ob + p.off_stats);
+        const bool searched = (run.stages & STG_LR_SEARCH) && !run.lr_given;
+        auto packed = [&](int pl) { return (const zf::PackedUnit *)(ob + p.off_packed[pl]); };
         zf_decisions *o = p.out;
         if (o) {
             if (run.stages & STG_DB_PICK) std::memcpy(o->lf, p.d.lf, 4);
@@ -918,9 +940,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 std::memcpy(o->cdef_y, b.cdef.y_str, 8);
                 std::memcpy(o->cdef_uv, b.cdef.uv_str, 8);
                 if (o->cdef_fb_idx)
-                    for (int k = 0; k < p.nfb; ++k) o->cdef_fb_idx[k] = b.cdef.bits ? fbidx[i][k] : 0;
+                    for (int k = 0; k < p.nfb; ++k) o->cdef_fb_idx[k] = b.cdef.bits ? fbidx[k] : 0;
             }
-            if ((run.stages & STG_LR_SEARCH) && !run.lr_given) {
+            if (searched) {
                 for (int pl = 0; pl < 3; ++pl) {
                     o->lr[pl].frame_rtype = b.lr[pl].on ? b.lr[pl].frame_rtype : ZF_RESTORE_NONE;
                     o->lr[pl].unit_size = 256;
@@ -928,19 +950,16 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                     o->lr[pl].vunits = p.vunits[pl];
                     if (!o->lr_units[pl]) continue;
                     const size_t nu = (size_t)p.hunits[pl] * p.vunits[pl];
-                    const std::vector<LrUnit> &uu = units[(size_t)i * 3 + pl];
+                    if (b.lr[pl].on) {
+                        std::memcpy(o->lr_units[pl], packed(pl), nu * sizeof(zf_lr_unit));
+                        continue;
+                    }
+                    static const int16_t def[8] = {3, -7, 15, -22, 15, -7, 3, 0};
                     for (size_t u = 0; u < nu; ++u) {
                         zf_lr_unit &lu = o->lr_units[pl][u];
                         std::memset(&lu, 0, sizeof(lu));
-                        if (uu.empty()) {
-                            static const int16_t def[8] = {3, -7, 15, -22, 15, -7, 3, 0};
-                            std::memcpy(lu.vfilter, def, 16);
-                            std::memcpy(lu.hfilter, def, 16);
-                            continue;
-                        }
-                        lu.rtype = (uint8_t)uu[u].rtype;
-                        std::memcpy(lu.vfilter, uu[u].vf, 16);
-                        std::memcpy(lu.hfilter, uu[u].hf, 16);
+                        std::memcpy(lu.vfilter, def, 16);
+                        std::memcpy(lu.hfilter, def, 16);
                     }
                 }
             }
@@ -948,15 +967,17 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         if (stats) {
             zf_stats &s = stats[i];
             std::memset(&s, 0, sizeof(s));
-            s.cdef_filtered_px = cst[i][0];
-            s.cdef_changed_px = cst[i][1];
+            s.cdef_filtered_px = cst[0];
+            s.cdef_changed_px = cst[1];
             int sbc = 0;
-            for (int k = 0; k < p.nfb; ++k) sbc += fbrow[i][k];
+            for (int k = 0; k < p.nfb; ++k) sbc += fbrow[k];
             s.cdef_sb_count = sbc;
             for (int pl = 0; pl < 3; ++pl) {
                 s.lr_frame_rtype[pl] = b.lr[pl].on ? b.lr[pl].frame_rtype : 0;
-                if (b.lr[pl].on && b.lr[pl].frame_rtype && !units[(size_t)i * 3 + pl].empty())
-                    for (auto &u : units[(size_t)i * 3 + pl]) s.lr_wiener_units += u.rtype == 1;
+                if (searched && b.lr[pl].on && b.lr[pl].frame_rtype) {
+                    const zf::PackedUnit *pu = packed(pl);
+                    for (size_t u = 0; u < p.rects[pl].size(); ++u) s.lr_wiener_units += pu[u].rtype == 1;
+                }
             }
         }
     }
@@ -1016,11 +1037,27 @@ void zf_destroy(zf_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->arena) cudaFree(ctx->arena);
+    if (ctx->h_meta) cudaFreeHost(ctx->h_meta);
+    if (ctx->h_out) cudaFreeHost(ctx->h_out);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
 
 const char *zf_last_error(const zf_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+uint64_t zf_device_bytes(const zf_ctx *ctx) { return ctx ? (uint64_t)ctx->arena_cap : 0; }
+
+int32_t zf_trim(zf_ctx *ctx) {
+    if (!ctx) return ZF_ERR_ARG;
+    CU(cudaSetDevice(ctx->device));
+    CU(cudaStreamSynchronize(ctx->stream));
+    if (ctx->arena) {
+        CU(cudaFree(ctx->arena));
+        ctx->arena = nullptr;
+        ctx->arena_cap = 0;
+    }
+    return ZF_OK;
+}
 
 int32_t zf_sync(zf_ctx *ctx) {
     if (!ctx) return ZF_ERR_ARG;
@@ -1033,8 +1070,17 @@ int32_t zf_query_sizes(const zf_frame *f, zf_sizes *out) {
     int e = validate_frame(nullptr, f);
     if (e) return e;
     Plan p;
-    size_t cursor = 0;
-    plan_frame(p, f, cursor);
+    size_t cursor = 0, ucur = 0, rcur = 0, ocur = 0;
+    plan_frame(p, f, cursor, ucur, rcur, ocur);
+    // work items (upper bound): per unit its sums / statistics row blocks
+    // and solve item, per plane the apply (stripe, tile) items
+    size_t items = 16;
+    for (int pl = 0; pl < 3; ++pl) {
+        const int ss = pl ? 1 : 0;
+        items += p.rects[pl].size() * (384 / 16 + 1 + 392 / 12 + 1 + 1);
+        items += (size_t)((p.d.lr[pl].ph + (8 >> ss)) / (64 >> ss) + 2) * ((p.d.lr[pl].pw + 63) / 64 + 1);
+    }
+    const size_t meta = align_up(sizeof(FrameDesc), 256) + items * sizeof(WorkItem) + 11 * 256 + rcur;
     std::memset(out, 0, sizeof(*out));
     out->nhfb = p.d.nhfb;
     out->nvfb = p.d.nvfb;
@@ -1043,7 +1089,8 @@ int32_t zf_query_sizes(const zf_frame *f, zf_sizes *out) {
         out->lr_vunits[pl] = p.vunits[pl];
     }
     out->lr_unit_size = 256;
-    out->device_bytes = cursor;
+    out->device_bytes = align_up(cursor, 256) + align_up(ucur, 256) + align_up(meta, 256) + align_up(ocur, 256) +
+                        3 * 1024;  // deblock search scratch
     return ZF_OK;
 }
 

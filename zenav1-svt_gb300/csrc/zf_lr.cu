@@ -804,7 +804,18 @@ __global__ void __launch_bounds__(32) k_lr_finish(FrameDesc *frames, int nframes
         pl.frame_rtype = frame_rtype;
     }
     __syncwarp();
-    for (int k = lane; k < n; k += 32) pl.units[k].rtype = frame_rtype ? U[k].pick : 0;
+    for (int k = lane; k < n; k += 32) {
+        const int rt = frame_rtype ? U[k].pick : 0;
+        pl.units[k].rtype = rt;
+        PackedUnit o;
+        for (int i = 0; i < 8; ++i) {
+            o.vf[i] = pl.units[k].vf[i];
+            o.hf[i] = pl.units[k].hf[i];
+        }
+        o.rtype = (uint8_t)rt;
+        for (int i = 0; i < 7; ++i) o.pad[i] = 0;
+        pl.packed[k] = o;
+    }
 }
 
 // ---------------------------------------------------------------------------
