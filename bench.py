@@ -12,6 +12,15 @@ Wiener search + apply).
          recon and geometry, D2H of the filtered recon and decisions inside
          the timed region).
 
+Two more keys on the same line (N=1 only):
+  batched  the 256-image mixed batch (sizes 64..2048, 8/10-bit) as one
+           zf_submit_batch per step vs one zf_filter_stage per image on the
+           same images (MPix/s each, their ratio, outputs identical),
+           plus the batch through host buffers.
+  served   Poisson arrivals at 50/200/800 req/s (sizes 128^2..6000x4000)
+           through the continuous-batching loop (serve.py): p50/p99 latency
+           and served MPix/s per rate.
+
 --impl reference times the reference algorithm on the host cores: the
 Rust reference cannot be built here, so this is the C++ oracle port, one
 thread per frame, on a bounded sample of the same workload.
@@ -48,6 +57,43 @@ def make_workload(w=W4K, h=H4K, idx=0):
     for i, (preset, qp) in enumerate(WORKLOAD):
         frames.append(synth.make_frame(synth.frame_seed(2, idx * 16 + i), w, h, 8, qp, preset, "power"))
     return frames
+
+
+def _gen_frame(job):
+    """One synthetic frame (runs in a spawned worker process)."""
+    ge._pkg()
+    from zenav1_svt_gb300 import synth
+    seed, w, h, bd, qp, preset, content = job
+    return synth.make_frame(seed, w, h, bd, qp, preset, content)
+
+
+def gen_frames(jobs):
+    """Frames for (seed, w, h, bd, qp, preset, content) jobs on all host cores."""
+    import multiprocessing as mp
+    procs = max(1, min(len(jobs), (os.cpu_count() or 2) - 1))
+    with mp.get_context("spawn").Pool(procs) as pool:
+        return pool.map(_gen_frame, jobs, chunksize=1)
+
+
+def batch_jobs(n):
+    ge._pkg()
+    from zenav1_svt_gb300 import synth
+    return [(synth.frame_seed(4, i), w, h, bd, qp, 6, "cosine")
+            for i, (w, h, bd, qp) in enumerate(synth.batch_specs(n))]
+
+
+def served_jobs(n):
+    ge._pkg()
+    from zenav1_svt_gb300 import synth
+    return [(synth.frame_seed(5, i), w, h, bd, qp, 6, "cosine")
+            for i, (w, h, bd, qp) in enumerate(synth.served_specs(n))]
+
+
+def stage_bytes(f):
+    """Mandatory bytes of one frame: recon in, source in, recon out (1.5
+    planes each at 1 or 2 bytes per sample) plus 4 bytes per 4x4 mi."""
+    b = 1 if f.bd == 8 else 2
+    return 3 * b * 1.5 * f.w * f.h + 4 * (f.w // 4) * (f.h // 4)
 
 
 # --------------------------------------------------------------------------
@@ -190,7 +236,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     ge.build()
     pkg = ge._pkg()
-    from zenav1_svt_gb300 import abi
+    from zenav1_svt_gb300 import abi, replicas
 
     frames = make_workload()
     mis = [pkg.pack_geom(f.geom) for f in frames]
@@ -252,12 +298,8 @@ def run_ours(args):
     clk = clocks.stop()
     px_step = sum(f.luma_px for f in frames)
     ms = float(np.mean(times))
-    t_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = world * px_step / (t_max / 1e3) / 1e6
+    t_max = replicas.max_over_ranks(ms, device=dev)  # replicas: the slowest rank's time
+    value = replicas.job_rate(px_step, world, t_max / 1e3) / 1e6
 
     # e2e: pinned host buffers through the C ABI
     h_src = [[torch.from_numpy(p.copy()).pin_memory() for p in f.src] for f in frames]
@@ -300,12 +342,8 @@ def run_ours(args):
         e1.record(stream)
         e1.synchronize()
         e_times.append(e0.elapsed_time(e1))
-    e_ms = float(np.mean(e_times))
-    if world > 1:
-        t = torch.tensor([e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e_ms = float(t.item())
-    e2e = world * px_step / (e_ms / 1e3) / 1e6
+    e_ms = replicas.max_over_ranks(float(np.mean(e_times)), device=dev)
+    e2e = replicas.job_rate(px_step, world, e_ms / 1e3) / 1e6
 
     # per-kernel device times (separate profiled pass, CUDA events per launch)
     restore()
@@ -347,11 +385,212 @@ def run_ours(args):
                 "roofline": roofline, "kernels": kernels, "clocks": clk}
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_sample()
+        if world == 1 and not args.no_batched:
+            line["batched"] = run_batched(args, ctx, stream, dev, gen_frames(batch_jobs(args.batch_n)))
+            print("batched:", json.dumps(line["batched"]), file=sys.stderr)
+        if world == 1 and not args.no_served:
+            line["served"] = run_served(args, local, gen_frames(served_jobs(32)))
         print(json.dumps(line))
     ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def run_batched(args, ctx, stream, dev, frames):
+    """The 256-image mixed batch (W, H ~ U[64, 2048], ~20 % odd, 70 % 8-bit,
+    qp ~ U[20, 50], preset 6): one zf_submit_batch call per step, against the
+    plain path (one zf_filter_stage call per image) on the same images.
+    Both device-resident; the batch also through host buffers (e2e)."""
+    import torch
+    pkg = ge._pkg()
+    from zenav1_svt_gb300 import abi
+    n = len(frames)
+    mis = [pkg.pack_geom(f.geom) for f in frames]
+    d_src = [[torch.from_numpy(p).to(dev) for p in f.src] for f in frames]
+    d_rec0 = [[torch.from_numpy(p).to(dev) for p in f.rec] for f in frames]
+    d_rec = [[x.clone() for x in r] for r in d_rec0]
+    d_mi = [torch.from_numpy(m.view(np.int32)).to(dev) for m in mis]
+    arr = (abi.ZfFrame * n)()
+    darr = (abi.ZfDecisions * n)()
+    st = (abi.ZfStats * n)()
+    decs = [abi.Decisions(f.w, f.h, f.true_w, f.true_h) for f in frames]
+    plain_decs = [abi.Decisions(f.w, f.h, f.true_w, f.true_h) for f in frames]
+    singles = []
+    for i, f in enumerate(frames):
+        arr[i] = abi.make_frame_struct(f, [x.data_ptr() for x in d_src[i]], [x.data_ptr() for x in d_rec[i]],
+                                       d_mi[i].data_ptr(), on_device=True)
+        darr[i] = decs[i].c
+        singles.append(abi.make_frame_struct(f, [x.data_ptr() for x in d_src[i]],
+                                             [x.data_ptr() for x in d_rec[i]], d_mi[i].data_ptr(),
+                                             on_device=True))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    px = sum(f.luma_px for f in frames)
+    mand = sum(stage_bytes(f) for f in frames)
+
+    def restore():
+        for r, r0 in zip(d_rec, d_rec0):
+            for a, b in zip(r, r0):
+                a.copy_(b)
+        flush.fill_(1)
+        torch.cuda.synchronize()
+
+    def timed(fn, steps):
+        out = []
+        for _ in range(steps):
+            restore()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return float(np.mean(out))
+
+    def batch():
+        ctx.submit_batch_raw(arr, n, darr, st)
+
+    one = abi.ZfStats()
+
+    def plain():
+        for s, d in zip(singles, plain_decs):
+            ctx.filter_stage_raw(s, d, one)
+
+    for _ in range(2):
+        restore()
+        batch()
+    l0 = ctx.launch_count()
+    b_ms = timed(batch, args.steps)
+    b_launches = (ctx.launch_count() - l0) // max(args.steps, 1)
+    out_batch = [[x.clone() for x in r] for r in d_rec]
+    for i in range(n):
+        decs[i].c = darr[i]
+    dec_batch = [d.as_dict() for d in decs]
+    restore()
+    plain()
+    p_ms = timed(plain, max(2, args.steps // 2))
+    same = all(torch.equal(a, b) for ra, rb in zip(out_batch, d_rec) for a, b in zip(ra, rb))
+    for a, d in zip(dec_batch, plain_decs):
+        b = d.as_dict()
+        same = same and a["lf"] == b["lf"] and a["cdef_y"] == b["cdef_y"] and a["cdef_uv"] == b["cdef_uv"] \
+            and a["cdef_bits"] == b["cdef_bits"] and bool((a["cdef_fb_idx"] == b["cdef_fb_idx"]).all()) \
+            and a["lr"] == b["lr"]
+    del out_batch
+
+    # e2e: the batch from pinned host buffers (H2D and D2H inside the call)
+    h_src = [[torch.from_numpy(p).pin_memory() for p in f.src] for f in frames]
+    h_rec0 = [f.rec for f in frames]
+    h_rec = [[torch.from_numpy(p.copy()).pin_memory() for p in f.rec] for f in frames]
+    h_mi = [torch.from_numpy(m.view(np.int32).copy()).pin_memory() for m in mis]
+    harr = (abi.ZfFrame * n)()
+    for i, f in enumerate(frames):
+        harr[i] = abi.make_frame_struct(f, [x.numpy() for x in h_src[i]], [x.numpy() for x in h_rec[i]],
+                                        h_mi[i].numpy())
+    h2d = sum(x.numel() * x.element_size() for r in h_rec for x in r) * 2 + sum(m.numel() * 4 for m in h_mi)
+    e_times = []
+    for k in range(2 + args.steps):
+        for r, r0 in zip(h_rec, h_rec0):
+            for a, b in zip(r, r0):
+                a.numpy()[...] = b
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.submit_batch_raw(harr, n, darr, st)
+        e1.record(stream)
+        e1.synchronize()
+        if k >= 2:
+            e_times.append(e0.elapsed_time(e1))
+    e_ms = float(np.mean(e_times))
+    peak = _peaks().get("hbm_gbs", 6800.0)
+    return {"workload": "256 images, W,H ~ U[64,2048] (~20% odd), 70% 8-bit / 30% 10-bit, qp ~ U[20,50], preset 6",
+            "images": n, "luma_mpix": round(px / 1e6, 3),
+            "batched_mpix_per_s": round(px / (b_ms / 1e3) / 1e6, 3), "batched_ms": round(b_ms, 3),
+            "launches_per_batch": int(b_launches),
+            "plain_mpix_per_s": round(px / (p_ms / 1e3) / 1e6, 3), "plain_ms": round(p_ms, 3),
+            "batched_over_plain": round(p_ms / b_ms, 3),
+            "batched_e2e_mpix_per_s": round(px / (e_ms / 1e3) / 1e6, 3),
+            "e2e_h2d_bytes": int(h2d), "e2e_d2h_bytes": int(h2d // 2),
+            "identical_to_plain": bool(same),
+            "stage_frac_of_hbm": round(mand / (b_ms / 1e3) / 1e9 / peak, 5),
+            "stage_bytes": int(mand)}
+
+
+def run_served(args, device, frames):
+    """Served requests: Poisson arrivals at 50 / 200 / 800 req/s, sizes
+    log-uniform 128^2 .. 6000x4000 (80 % 8-bit), preset 6, through the
+    continuous-batching loop (three worker contexts, 120 GB HBM budget).
+    Requests cycle through a pool of pre-generated images (pinned host
+    buffers); latency = completion - scheduled arrival."""
+    import copy
+    import torch
+    pkg = ge._pkg()
+    from zenav1_svt_gb300 import serve, synth
+    pool = []
+    for f in frames:
+        src = [torch.from_numpy(p).pin_memory().numpy() for p in f.src]
+        pool.append({"f": f, "src": src, "rec0": f.rec, "mi": pkg.pack_geom(f.geom), "slots": []})
+    executors = [serve.FilterExecutor(device) for _ in range(3)]
+    srv = serve.Server(executors, hbm_budget_bytes=120 << 30, max_batch=64, max_batch_px=48 << 20)
+    for e in pool:
+        r = serve.Request(e["f"], mi=e["mi"])
+        e["fp"] = executors[0].footprint(r)
+
+    def take(e):
+        for sl in e["slots"]:
+            if sl["req"] is None or sl["req"]._done.is_set():
+                return sl
+        sl = {"rec": [torch.from_numpy(p.copy()).pin_memory().numpy() for p in e["rec0"]], "req": None}
+        e["slots"].append(sl)
+        return sl
+
+    def request(k):
+        e = pool[k % len(pool)]
+        sl = take(e)
+        for a, b in zip(sl["rec"], e["rec0"]):
+            np.copyto(a, b)
+        fr = copy.copy(e["f"])
+        fr.src, fr.rec = e["src"], sl["rec"]
+        r = serve.Request(fr, mi=e["mi"], rid=k)
+        r.footprint = e["fp"]
+        sl["req"] = r
+        return r
+
+    # warm-up: one burst of the whole pool twice (arenas grow to batch size)
+    for _ in range(2):
+        for k in range(len(pool)):
+            srv.submit(request(k))
+        srv.drain(timeout=600)
+    out = {}
+    for rate in (50, 200, 800):
+        arrivals = synth.poisson_arrivals(rate, args.served_seconds, seed=rate)
+        reqs = []
+        t0 = time.perf_counter() + 0.02
+        for k, off in enumerate(arrivals):
+            r = request(k)
+            delay = t0 + off - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            reqs.append(srv.submit(r, arrival=t0 + off))
+        srv.drain(timeout=600)
+        s = serve.latency_summary(reqs)
+        s["offered_mpix_per_s"] = round(sum(r.luma_px for r in reqs) / args.served_seconds / 1e6, 3)
+        s["errors"] = sum(r.error is not None for r in reqs)
+        out["%d_req_s" % rate] = s
+    srv.close()
+    for e in executors:
+        e.close()
+    return {"workload": ("Poisson arrivals, sizes log-uniform 128^2..6000x4000, 80% 8-bit / 20% 10-bit, "
+                         "qp ~ U[18,45], preset 6; requests cycle a pool of {} images").format(len(pool)),
+            "seconds_per_rate": args.served_seconds, "workers": 3, "hbm_budget_gb": 120,
+            "peak_reserved_gb": round(srv.peak_reserved / 2 ** 30, 3), "rates": out}
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
 
 
 def run_profile(args):
@@ -400,6 +639,10 @@ def main():
     ap.add_argument("--pw", type=int, default=W4K)
     ap.add_argument("--ph", type=int, default=H4K)
     ap.add_argument("--nframes", type=int, default=4)
+    ap.add_argument("--no-batched", action="store_true", help="skip the 256-image batch")
+    ap.add_argument("--no-served", action="store_true", help="skip the served request loop")
+    ap.add_argument("--batch-n", type=int, default=256)
+    ap.add_argument("--served-seconds", type=float, default=4.0, help="arrival window per rate")
     args = ap.parse_args()
     if args.profile_run:
         return run_profile(args)

@@ -344,3 +344,29 @@ def workload_batch(n=256, max_dim=2048):
     for i, (w, h, bd, qp) in enumerate(batch_specs(n, max_dim=max_dim)):
         frames.append(make_frame(frame_seed(4, i), w, h, bd, qp, 6, "cosine"))
     return frames
+
+
+def served_specs(n=32, seed_cfg=5, max_w=6000, max_h=4000, min_dim=128):
+    """(w, h, bd, qp) for served requests: sizes log-uniform from
+    min_dim^2 to max_w x max_h, 80% 8-bit / 20% 10-bit, qp ~ U[18, 45],
+    preset 6."""
+    rng = np.random.default_rng(frame_seed(seed_cfg, 0x5E4E))
+    specs = []
+    for _ in range(n):
+        w = int(round(np.exp(rng.uniform(np.log(min_dim), np.log(max_w)))))
+        h = int(round(np.exp(rng.uniform(np.log(min_dim), np.log(max_h)))))
+        bd = 10 if rng.random() < 0.2 else 8
+        qp = int(rng.integers(18, 46))
+        specs.append((w, h, bd, qp))
+    return specs
+
+
+def poisson_arrivals(rate, seconds, seed):
+    """Arrival offsets (s) of a Poisson process of `rate` per second."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            return out
+        out.append(t)
