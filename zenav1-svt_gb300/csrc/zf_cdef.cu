@@ -43,61 +43,105 @@ __device__ __forceinline__ int adjust_strength(int strength, int var) {
     return var != 0 ? (strength * (4 + i) + 8) >> 4 : 0;
 }
 
-// cdef_find_dir (cdef.rs:143-198) on an 8x8 block at `img` (stride rs).
-__device__ void find_dir(const uint16_t *img, int rs, int coeff_shift, int *odir, int *ovar) {
-    int cost[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int partial[8][15];
+// cdef_find_dir (cdef.rs:143-198), split by direction pairs so that four
+// threads share one 8x8 block: pair 0 = directions (0, 4), 1 = (2, 6),
+// 2 = (1, 5), 3 = (3, 7). Each pass keeps at most 30 partial sums live.
+__host__ __device__ constexpr int kDiv(int n) { return n ? 840 / n : 0; }  // 840 / n
+
+template <int PAIR>
+__device__ __forceinline__ void dir_cost_pair(const uint16_t *img, int rs, int cs, int &ca, int &cb) {
+    constexpr int NB = (PAIR == 0) ? 15 : (PAIR == 1 ? 8 : 11);
+    int pa[NB], pb[NB];
 #pragma unroll
-    for (int a = 0; a < 8; ++a)
-#pragma unroll
-        for (int b = 0; b < 15; ++b) partial[a][b] = 0;
-    const int div[9] = {0, 840, 420, 280, 210, 168, 140, 120, 105};
+    for (int k = 0; k < NB; ++k) pa[k] = pb[k] = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            int x = ((int)img[i * rs + j] >> coeff_shift) - 128;
-            partial[0][i + j] += x;
-            partial[1][i + j / 2] += x;
-            partial[2][i] += x;
-            partial[3][3 + i - j / 2] += x;
-            partial[4][7 + i - j] += x;
-            partial[5][3 - i / 2 + j] += x;
-            partial[6][j] += x;
-            partial[7][i / 2 + j] += x;
+            const int x = ((int)img[i * rs + j] >> cs) - 128;
+            if (PAIR == 0) {
+                pa[i + j] += x;
+                pb[7 + i - j] += x;
+            } else if (PAIR == 1) {
+                pa[i] += x;
+                pb[j] += x;
+            } else if (PAIR == 2) {
+                pa[i + j / 2] += x;
+                pb[3 - i / 2 + j] += x;
+            } else {
+                pa[3 + i - j / 2] += x;
+                pb[i / 2 + j] += x;
+            }
         }
+    auto cost = [&](const int *p) {
+        int c = 0;
+        if (PAIR == 0) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        cost[2] += partial[2][i] * partial[2][i];
-        cost[6] += partial[6][i] * partial[6][i];
-    }
-    cost[2] *= div[8];
-    cost[6] *= div[8];
+            for (int i = 0; i < 7; ++i) c += (p[i] * p[i] + p[14 - i] * p[14 - i]) * kDiv(i + 1);
+            c += p[7] * p[7] * kDiv(8);
+        } else if (PAIR == 1) {
 #pragma unroll
-    for (int i = 0; i < 7; ++i) {
-        cost[0] += (partial[0][i] * partial[0][i] + partial[0][14 - i] * partial[0][14 - i]) * div[i + 1];
-        cost[4] += (partial[4][i] * partial[4][i] + partial[4][14 - i] * partial[4][14 - i]) * div[i + 1];
-    }
-    cost[0] += partial[0][7] * partial[0][7] * div[8];
-    cost[4] += partial[4][7] * partial[4][7] * div[8];
+            for (int i = 0; i < 8; ++i) c += p[i] * p[i];
+            c *= kDiv(8);
+        } else {
 #pragma unroll
-    for (int i = 1; i < 8; i += 2) {
+            for (int j = 0; j < 5; ++j) c += p[3 + j] * p[3 + j];
+            c *= kDiv(8);
 #pragma unroll
-        for (int j = 0; j < 5; ++j) cost[i] += partial[i][3 + j] * partial[i][3 + j];
-        cost[i] *= div[8];
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-            cost[i] += (partial[i][j] * partial[i][j] + partial[i][10 - j] * partial[i][10 - j]) * div[2 * j + 2];
-    }
-    int best_cost = 0, best_dir = 0;
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-        if (cost[i] > best_cost) {
-            best_cost = cost[i];
-            best_dir = i;
+            for (int j = 0; j < 3; ++j) c += (p[j] * p[j] + p[10 - j] * p[10 - j]) * kDiv(2 * j + 2);
         }
-    *odir = best_dir;
-    *ovar = (best_cost - cost[(best_dir + 4) & 7]) >> 10;
+        return c;
+    };
+    ca = cost(pa);
+    cb = cost(pb);
+}
+
+// Directions and variances of the blocks blist[0..nblk) of a region (block
+// b at region row (b >> 3) * 8 + 2, column (b & 7) * 8 + 2): four threads
+// per block (a 256-thread CTA: thread t takes pair t >> 6, block t & 63, so
+// each warp runs one pair), the per-direction costs meet in `cost`, then
+// one thread per block picks the best direction (strictly greater wins, the
+// lowest index on ties) and var = (best - cost of the orthogonal) >> 10.
+// Every thread of the CTA calls this.
+__device__ void find_dirs(const uint16_t *reg, int rs, int cs, const int *blist, int nblk, int (*cost)[8],
+                          int *sdir, int *svar) {
+    const int t = threadIdx.x, pair = t >> 6, k = t & 63;
+    if (k < nblk) {
+        const int b = blist[k];
+        const uint16_t *img = reg + ((b >> 3) * 8 + 2) * rs + (b & 7) * 8 + 2;
+        int ca, cb;
+        if (pair == 0) {
+            dir_cost_pair<0>(img, rs, cs, ca, cb);
+            cost[b][0] = ca;
+            cost[b][4] = cb;
+        } else if (pair == 1) {
+            dir_cost_pair<1>(img, rs, cs, ca, cb);
+            cost[b][2] = ca;
+            cost[b][6] = cb;
+        } else if (pair == 2) {
+            dir_cost_pair<2>(img, rs, cs, ca, cb);
+            cost[b][1] = ca;
+            cost[b][5] = cb;
+        } else {
+            dir_cost_pair<3>(img, rs, cs, ca, cb);
+            cost[b][3] = ca;
+            cost[b][7] = cb;
+        }
+    }
+    __syncthreads();
+    if (t < nblk) {
+        const int b = blist[t];
+        int best_cost = 0, best_dir = 0;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            if (cost[b][i] > best_cost) {
+                best_cost = cost[b][i];
+                best_dir = i;
+            }
+        sdir[b] = best_dir;
+        svar[b] = (best_cost - cost[b][(best_dir + 4) & 7]) >> 10;
+    }
+    __syncthreads();
 }
 
 // One output pixel of svt_cdef_filter_block_c: wrapping int16 tap sum,
@@ -181,15 +225,96 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v
     return s;  // valid in thread 0
 }
 
+// constrain with the damping shift precomputed: shift = max(0, damping -
+// msb(threshold)) (cdef.rs:113-120); threshold 0 gives 0 for any shift.
+__device__ __forceinline__ int constrain_s(int d, int thr, int shift) {
+    const int a = abs(d);
+    const int v = min(a, max(0, thr - (a >> shift)));
+    return d < 0 ? -v : v;
+}
+__device__ __forceinline__ int damp_shift(int thr, int damping) {
+    return thr ? max(0, damping - msb((unsigned)thr)) : 0;
+}
+
+// Region offsets of the taps of direction `dir` (row stride rs): primary
+// k = 0, 1, then the secondary directions dir + 2 and dir + 6, k = 0, 1.
+__device__ __forceinline__ void dir_offsets(int dir, int rs, int *o) {
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        o[k] = kDir[dir][k][0] * rs + kDir[dir][k][1];
+        o[2 + k] = kDir[(dir + 2) & 7][k][0] * rs + kDir[(dir + 2) & 7][k][1];
+        o[4 + k] = kDir[(dir + 6) & 7][k][0] * rs + kDir[(dir + 6) & 7][k][1];
+    }
+}
+
+// The 12 taps of one pixel as differences to x (read as int16, so the
+// sentinel is a large positive value), and the clamp range: min over x and
+// all taps, max over x and the taps that are not the sentinel.
+// d[0..3]: primary +k0, -k0, +k1, -k1; d[4..7]: secondary k0 (+2, -2, +6,
+// -6); d[8..11]: secondary k1.
+__device__ __forceinline__ void load_taps(const uint16_t *reg, int pos, const int *o, int x, int *d, int &mx,
+                                          int &mn) {
+    mx = x;
+    mn = x;
+    int q[12];
+    q[0] = pos + o[0]; q[1] = pos - o[0]; q[2] = pos + o[1]; q[3] = pos - o[1];
+    q[4] = pos + o[2]; q[5] = pos - o[2]; q[6] = pos + o[4]; q[7] = pos - o[4];
+    q[8] = pos + o[3]; q[9] = pos - o[3]; q[10] = pos + o[5]; q[11] = pos - o[5];
+#pragma unroll
+    for (int t = 0; t < 12; ++t) {
+        const uint16_t r = reg[q[t]];
+        const int v = (int16_t)r;
+        if (r != kVeryLarge) mx = max(mx, v);
+        mn = min(mn, v);
+        d[t] = v - x;
+    }
+}
+
+// Primary and secondary parts of the tap sum. The reference sums in
+// wrapping int16 (cdef.rs:965-1023); |sum| <= 2*(4+2)*60 + 12*16 = 912 for
+// every strength at 8 and 10 bits, so plain int sums are identical, and the
+// sum splits exactly into a primary part (per primary strength) and a
+// secondary part (per secondary strength).
+__device__ __forceinline__ int prim_sum(const int *d, int t, int shift, int cs) {
+    const int odd = (t >> cs) & 1;
+    const int w0 = odd ? 3 : 4, w1 = odd ? 3 : 2;
+    return w0 * (constrain_s(d[0], t, shift) + constrain_s(d[1], t, shift)) +
+           w1 * (constrain_s(d[2], t, shift) + constrain_s(d[3], t, shift));
+}
+__device__ __forceinline__ int sec_sum(const int *d, int s, int shift) {
+    return 2 * (constrain_s(d[4], s, shift) + constrain_s(d[5], s, shift) + constrain_s(d[6], s, shift) +
+                constrain_s(d[7], s, shift)) +
+           (constrain_s(d[8], s, shift) + constrain_s(d[9], s, shift) + constrain_s(d[10], s, shift) +
+            constrain_s(d[11], s, shift));
+}
+__device__ __forceinline__ int cdef_round(int x, int sum, int mn, int mx) {
+    return min(max(x + ((8 + sum - (sum < 0)) >> 4), mn), mx);
+}
+
 // Search: one CTA per filter block. Writes the fb's luma and joint-chroma
-// mse rows (cdef_search_still[_hbd]) and whether the fb has a row.
+// mse rows (cdef_search_still[_hbd], cdef.rs:1166-1568) and whether the fb
+// has a row.
+//
+// The candidate list of every preset is a grid: fp first-pass strengths
+// (primary p_i, secondary 0) followed by p_i x each of ns - 1 extra
+// secondary strengths (cdef_search_cfg_for_preset, cdef.rs:788-810). Per
+// pixel the kernel loads the taps once per direction set (the block's
+// direction for p_i != 0, direction 0 for p_i == 0), computes the primary
+// part once per p_i and the secondary part once per secondary strength, and
+// forms every candidate from the two parts. FPM x NSM bounds fp x ns.
+template <int FPM, int NSM>
 __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, const WorkItem *items, int nitems) {
+    constexpr int NCM = FPM * NSM;
     __shared__ uint16_t reg[CR * CR];
     __shared__ uint16_t src[64 * 64];
     __shared__ int sdir[64], svar[64];
-    __shared__ unsigned long long red[8];
+    __shared__ int dcost[64][8];
+    __shared__ int boff[64][6], boffc[64][6];
+    __shared__ int bpri[64][FPM];  // adjusted primary strength | damping shift << 16
     __shared__ int blist[64];
     __shared__ int nblk;
+    __shared__ uint32_t part[8][NCM];
+    __shared__ unsigned long long uvtot[FPM];
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
     const FrameDesc &f = frames[wi.frame];
@@ -197,6 +322,7 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
     const int fb = blockIdx.x - wi.cta_begin;
     const int fbr = fb / f.nhfb, fbc = fb - fbr * f.nhfb;
     const int bd = f.bd, cs = bd - 8;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t dl = fb_dlist(f, fbr, fbc);
     if (threadIdx.x == 0) {
         f.fb_row[fb] = dl != 0;
@@ -206,9 +332,24 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
         nblk = n;
     }
     if (dl == 0) return;
-    const int n_cand = cp.ncand;
+    const int n_cand = cp.ncand, fp = cp.first_pass_num, ns = n_cand / fp;
     uint64_t *row = f.mse + (int64_t)fb * 2 * n_cand;
-    const int damping = cp.damping;
+    const int dmp = cp.damping + cs;
+    int pri[FPM], sec[NSM], ssh[NSM];
+    bool any_zero = false;
+#pragma unroll
+    for (int i = 0; i < FPM; ++i) {
+        pri[i] = i < fp ? (cp.fs[i] / 4) << cs : 0;
+        any_zero = any_zero || (i < fp && pri[i] == 0);
+    }
+    sec[0] = 0;
+    ssh[0] = 0;
+#pragma unroll
+    for (int j = 1; j < NSM; ++j) {
+        const int s = j < ns ? cp.fs[fp + j - 1] % 4 : 0;
+        sec[j] = (s + (s == 3)) << cs;
+        ssh[j] = damp_shift(sec[j], dmp);
+    }
     // ---- luma
     const int x0 = fbc * 64, y0 = fbr * 64;
     load_region(f.B[0], bd, f.w, f.h, x0, y0, 64, reg);
@@ -217,43 +358,97 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
         src[i] = (x < f.w && y < f.h) ? (uint16_t)ldpx(f.S[0], (int64_t)y * f.w + x, bd) : 0;
     }
     __syncthreads();
+    find_dirs(reg, CR, cs, blist, nblk, dcost, sdir, svar);
     for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
-        const int b = blist[k], by = b >> 3, bx = b & 7;
-        find_dir(reg + (by * 8 + 2) * CR + bx * 8 + 2, CR, cs, &sdir[b], &svar[b]);
+        const int b = blist[k];
+        const int dir = sdir[b], var = svar[b];
+        dir_offsets(dir, CR, boff[b]);
+        dir_offsets(dir, CRC, boffc[b]);
+#pragma unroll
+        for (int i = 0; i < FPM; ++i) {
+            const int t = adjust_strength(pri[i], var);
+            bpri[b][i] = t | (damp_shift(t, dmp) << 16);
+        }
     }
     __syncthreads();
     const int sub = cp.sub_y;
-    const int rows_per = 8 / sub;  // sampled rows per 8x8 block
-    const int slots = nblk * rows_per * 8;
-    for (int gi = 0; gi < n_cand; ++gi) {
-        const int strength = cp.fs[gi];
-        const int pri = (strength / 4) << cs;
-        const int s = strength % 4;
-        const int sec = (s + (s == 3)) << cs;
-        const int dmp = damping + cs;
-        unsigned long long acc = 0;
-        for (int q = threadIdx.x; q < slots; q += blockDim.x) {
-            const int k = q / (rows_per * 8), rem = q - k * rows_per * 8;
-            const int i = (rem >> 3) * sub, j = rem & 7;
-            const int b = blist[k], by = b >> 3, bx = b & 7;
-            const int py = by * 8 + i, px = bx * 8 + j;
-            const int t = adjust_strength(pri, svar[b]);
-            const int y = cdef_px(reg, CR, (py + 2) * CR + px + 2, t, sec, pri ? sdir[b] : 0, dmp, dmp, cs);
-            const int e = (int)src[py * 64 + px] - y;
-            acc += (unsigned long long)((long long)e * e);
+    const int lgs = 6 - (__ffs(sub) - 1);  // sampled slots per 8x8 block: 64 / sub
+    const int slots = nblk << lgs;
+    uint32_t acc[NCM];
+#pragma unroll
+    for (int c = 0; c < NCM; ++c) acc[c] = 0;
+    for (int q = threadIdx.x; q < slots; q += blockDim.x) {
+        const int k = q >> lgs, rem = q & ((1 << lgs) - 1);
+        const int b = blist[k];
+        const int py = (b >> 3) * 8 + (rem >> 3) * sub, px = (b & 7) * 8 + (rem & 7);
+        const int pos = (py + 2) * CR + px + 2;
+        const int x = (int16_t)reg[pos], sv = src[py * 64 + px];
+        int d[12], mx, mn, S[NSM];
+        {  // block direction: candidates with p_i != 0
+            load_taps(reg, pos, boff[b], x, d, mx, mn);
+            S[0] = 0;
+#pragma unroll
+            for (int j = 1; j < NSM; ++j) S[j] = j < ns ? sec_sum(d, sec[j], ssh[j]) : 0;
+#pragma unroll
+            for (int i = 0; i < FPM; ++i) {
+                if (i >= fp || pri[i] == 0) continue;
+                const int tp = bpri[b][i];
+                const int P = prim_sum(d, tp & 0xffff, tp >> 16, cs);
+#pragma unroll
+                for (int j = 0; j < NSM; ++j) {
+                    if (j >= ns) continue;
+                    const int e = sv - cdef_round(x, P + S[j], mn, mx);
+                    acc[i * NSM + j] += (uint32_t)(e * e);
+                }
+            }
         }
-        unsigned long long tot = block_sum_u64(acc, red);
-        if (threadIdx.x == 0) row[gi] = (tot >> (2 * cs)) * (unsigned long long)sub;
+        if (any_zero) {  // direction 0: candidates with p_i == 0
+            const int o0[6] = {-1 * CR + 1, -2 * CR + 2, 0 * CR + 1, 0 * CR + 2, 1 * CR + 0, 2 * CR + 0};
+            load_taps(reg, pos, o0, x, d, mx, mn);
+#pragma unroll
+            for (int j = 1; j < NSM; ++j) S[j] = j < ns ? sec_sum(d, sec[j], ssh[j]) : 0;
+#pragma unroll
+            for (int i = 0; i < FPM; ++i) {
+                if (i >= fp || pri[i] != 0) continue;
+#pragma unroll
+                for (int j = 0; j < NSM; ++j) {
+                    if (j >= ns) continue;
+                    const int e = sv - cdef_round(x, S[j], mn, mx);
+                    acc[i * NSM + j] += (uint32_t)(e * e);
+                }
+            }
+        }
     }
-    // ---- chroma: U then V accumulate into the joint row
+    // per-warp partials (a lane holds <= 16 pixels of e^2 <= 1023^2: the
+    // warp total fits u32), then the fb total in u64
+#pragma unroll
+    for (int c = 0; c < NCM; ++c) {
+        uint32_t v = acc[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) part[warp][c] = v;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < NCM; c += blockDim.x) {
+        const int i = c / NSM, j = c - i * NSM;
+        if (i >= fp || j >= ns) continue;
+        unsigned long long tot = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += part[w][c];
+        const int gi = j == 0 ? i : fp + i * (ns - 1) + (j - 1);
+        row[gi] = (tot >> (2 * cs)) * (unsigned long long)sub;
+    }
+    // ---- chroma: U then V accumulate into the joint row (first-pass
+    // strengths only: secondary 0, primary not adjusted, damping - 1)
     if (!f.chroma) {
         if (threadIdx.x == 0)
             for (int gi = 0; gi < n_cand; ++gi) row[n_cand + gi] = 0;
         return;
     }
-    __shared__ unsigned long long uvacc[kMaxCand];
-    if (threadIdx.x == 0)
-        for (int gi = 0; gi < n_cand; ++gi) uvacc[gi] = 0;
+    if (threadIdx.x < FPM) uvtot[threadIdx.x] = 0;
+    const int cdmp = dmp - 1;
+    int csh[FPM];
+#pragma unroll
+    for (int i = 0; i < FPM; ++i) csh[i] = damp_shift(pri[i], cdmp);
     const int cw = f.w / 2, ch = f.h / 2, cx0 = fbc * 32, cy0 = fbr * 32;
     for (int p = 1; p <= 2; ++p) {
         __syncthreads();
@@ -263,30 +458,55 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
             src[i] = (x < cw && y < ch) ? (uint16_t)ldpx(f.S[p], (int64_t)y * cw + x, bd) : 0;
         }
         __syncthreads();
+        uint32_t cacc[FPM];
+#pragma unroll
+        for (int i = 0; i < FPM; ++i) cacc[i] = 0;
         const int cslots = nblk * 16;
-        for (int gi = 0; gi < cp.first_pass_num; ++gi) {
-            const int strength = cp.fs[gi];
-            const int pri = (strength / 4) << cs;
-            const int s = strength % 4;
-            const int sec = (s + (s == 3)) << cs;
-            const int dmp = damping + cs - 1;
-            unsigned long long acc = 0;
-            for (int q = threadIdx.x; q < cslots; q += blockDim.x) {
-                const int k = q >> 4, i = (q >> 2) & 3, j = q & 3;
-                const int b = blist[k], by = b >> 3, bx = b & 7;
-                const int py = by * 4 + i, px = bx * 4 + j;
-                const int y = cdef_px(reg, CRC, (py + 2) * CRC + px + 2, pri, sec, pri ? sdir[b] : 0, dmp, dmp, cs);
-                const int e = (int)src[py * 32 + px] - y;
-                acc += (unsigned long long)((long long)e * e);
+        for (int q = threadIdx.x; q < cslots; q += blockDim.x) {
+            const int k = q >> 4, b = blist[k];
+            const int py = (b >> 3) * 4 + ((q >> 2) & 3), px = (b & 7) * 4 + (q & 3);
+            const int pos = (py + 2) * CRC + px + 2;
+            const int x = (int16_t)reg[pos], sv = src[py * 32 + px];
+            int d[12], mx, mn;
+            load_taps(reg, pos, boffc[b], x, d, mx, mn);
+#pragma unroll
+            for (int i = 0; i < FPM; ++i) {
+                if (i >= fp) continue;
+                // primary 0 and secondary 0: every tap term is 0, the pixel is kept
+                const int y = pri[i] ? cdef_round(x, prim_sum(d, pri[i], csh[i], cs), mn, mx) : x;
+                const int e = sv - y;
+                cacc[i] += (uint32_t)(e * e);
             }
-            unsigned long long tot = block_sum_u64(acc, red);
-            if (threadIdx.x == 0) uvacc[gi] += (tot >> (2 * cs)) * (unsigned long long)cp.sub_uv;
+        }
+#pragma unroll
+        for (int i = 0; i < FPM; ++i) {
+            uint32_t v = cacc[i];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) part[warp][i] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < fp) {
+            unsigned long long tot = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += part[w][threadIdx.x];
+            uvtot[threadIdx.x] += (tot >> (2 * cs)) * (unsigned long long)cp.sub_uv;
         }
     }
-    if (threadIdx.x == 0) {
-        for (int gi = 0; gi < n_cand; ++gi)
-            row[n_cand + gi] = gi < cp.first_pass_num ? uvacc[gi] : 1040400ull * 64ull;
-    }
+    __syncthreads();
+    for (int gi = threadIdx.x; gi < n_cand; gi += blockDim.x)
+        row[n_cand + gi] = gi < fp ? uvtot[gi] : 1040400ull * 64ull;
+}
+
+// Launch the search instantiation covering fp x ns (the largest over the
+// batch's frames).
+cudaError_t launch_cdef_search(int fp, int ns, int ctas, cudaStream_t st, const FrameDesc *frames,
+                               const WorkItem *items, int nitems) {
+    if (fp <= 2 && ns <= 2) k_cdef_search<2, 2><<<ctas, 256, 0, st>>>(frames, items, nitems);
+    else if (fp <= 3 && ns <= 2) k_cdef_search<3, 2><<<ctas, 256, 0, st>>>(frames, items, nitems);
+    else if (fp <= 5 && ns <= 4) k_cdef_search<5, 4><<<ctas, 256, 0, st>>>(frames, items, nitems);
+    else if (fp <= 12 && ns <= 4) k_cdef_search<12, 4><<<ctas, 256, 0, st>>>(frames, items, nitems);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
 }
 
 // ---- finish: the joint strength search of one frame in one CTA ----------
@@ -507,6 +727,9 @@ __global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThread
 __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems) {
     __shared__ uint16_t reg[CR * CR];
     __shared__ int sdir[64], svar[64];
+    __shared__ int dcost[64][8];
+    __shared__ int blist[64];
+    __shared__ int nblk;
     __shared__ unsigned long long red[8];
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
@@ -542,10 +765,14 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     const int lvl_uv = (uvs / 4) << cs, sec_uv = ((uvs % 4) + ((uvs % 4) == 3)) << cs;
     const int damping = cp.damping + cs;
     load_region(f.B[0], bd, f.w, f.h, x0, y0, 64, reg);
+    if (threadIdx.x == 0) {
+        int n = 0;
+        for (int b = 0; b < 64; ++b)
+            if ((dl >> b) & 1) blist[n++] = b;
+        nblk = n;
+    }
     __syncthreads();
-    for (int b = threadIdx.x; b < 64; b += blockDim.x)
-        if ((dl >> b) & 1) find_dir(reg + ((b >> 3) * 8 + 2) * CR + (b & 7) * 8 + 2, CR, cs, &sdir[b], &svar[b]);
-    __syncthreads();
+    find_dirs(reg, CR, cs, blist, nblk, dcost, sdir, svar);
     unsigned long long filt = 0, changed = 0;
     const bool zero_y = lvl_y == 0 && sec_y == 0;
     for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
@@ -712,7 +939,9 @@ extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_de
         cudaMemcpyAsync(&sc->item, &item, sizeof(item), cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(&sc->frame_id, &frame_id, sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess)
         return ZF_ERR_CUDA;
-    k_cdef_search<<<nfb, 256, 0, st>>>(&sc->desc, &sc->item, 1);
+    if (launch_cdef_search(d.cdef.first_pass_num, d.cdef.ncand / d.cdef.first_pass_num, nfb, st, &sc->desc,
+                           &sc->item, 1) != cudaSuccess)
+        return ZF_ERR_CUDA;
     const int per_cta = (nfb + kFinCluster - 1) / kFinCluster * (2 * d.cdef.ncand + 1) * 4;  // < 48 KiB
     k_cdef_finish<<<kFinCluster, kFinThreads, per_cta, st>>>(&sc->desc, &sc->frame_id, per_cta);
     if (cudaGetLastError() != cudaSuccess) return ZF_ERR_CUDA;

@@ -826,9 +826,15 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     }
     // ---- CDEF search + finish on B
     if ((run.stages & STG_CDEF_SEARCH) && !cdef_frames.empty()) {
+        int fp = 1, ns = 1;
+        for (int fi : cdef_frames) {
+            const CdefParams &c = plans[fi].d.cdef;
+            fp = std::max(fp, c.first_pass_num);
+            ns = std::max(ns, c.ncand / c.first_pass_num);
+        }
         { LaunchScope ls_(ctx, "k_cdef_search");
-        zf::k_cdef_search<<<wl_cs.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_cs),
-                                                      (int)wl_cs.items.size()); }
+        CU(zf::launch_cdef_search(fp, ns, wl_cs.ctas, st, d_desc, (const WorkItem *)(base + o_cs),
+                                  (int)wl_cs.items.size())); }
         TRY(launch_check(ctx, "k_cdef_search"));
         { LaunchScope ls_(ctx, "k_cdef_finish");
         // dynamic shared memory for the compacted rows: the largest frame

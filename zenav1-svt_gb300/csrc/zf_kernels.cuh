@@ -11,7 +11,9 @@ __global__ void k_deblock_apply(const FrameDesc *frames, const WorkItem *items, 
 __global__ void k_deblock_sse(const FrameDesc *frames, const WorkItem *items, int nitems, const int *levels,
                               unsigned long long *sse);
 
-__global__ void k_cdef_search(const FrameDesc *frames, const WorkItem *items, int nitems);
+// CDEF search over a batch whose candidate grids are at most fp x ns.
+cudaError_t launch_cdef_search(int fp, int ns, int ctas, cudaStream_t st, const FrameDesc *frames,
+                               const WorkItem *items, int nitems);
 __global__ void k_cdef_finish(FrameDesc *frames, const int *frame_ids, int smem_bytes);
 __global__ void k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems);
 
