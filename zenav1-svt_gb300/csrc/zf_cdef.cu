@@ -517,39 +517,49 @@ __device__ __forceinline__ unsigned long long rdc(unsigned long long lambda, uns
     return ((rate * lambda + 256) >> 9) + (dist << 7);
 }
 
-// finish_cdef_rd + the per-fb index (cdef.rs:897-944, :1326-1344) for one
-// frame on a cluster of kFinCluster CTAs. The filter blocks are split into
-// kFinCluster contiguous ranges; each CTA compacts the rows of its range
-// (column-major u32: every per-filter-block mse is below 2^29 -- at most
-// 4096 px x 1023^2 >> 4 per plane, times sub <= 4 -- so the u32 copy is
-// lossless and a luma + chroma row sum fits u32) into its shared memory.
-// Each search_one_dual step (cdef.rs:824-862) sums its range into a local
-// partial, the cluster barrier publishes the partials, every CTA adds all
-// of them over distributed shared memory and takes the same argmin, so the
-// 75 sequential steps of the joint search stay in lockstep without a trip
-// to global memory.
+// finish_cdef_rd + the per-fb index (cdef.rs:897-944, :1326-1344).
+//
+// joint_strength_search_dual runs once per bit count i = 0..3 (nb = 1 << i
+// strengths: nb greedy search_one_dual steps, then 4 nb refinement steps)
+// and the four searches are independent, so each runs on its own cluster of
+// kFinCluster CTAs (critical path: the 40 steps of i = 3). The filter
+// blocks are split into kFinCluster contiguous ranges; each CTA compacts
+// the rows of its range (column-major u32: every per-filter-block mse is
+// below 2^29 -- at most 4096 px x 1023^2 >> 4 per plane, times sub <= 4 --
+// so the u32 copy is lossless and a luma + chroma row sum fits u32) into
+// its shared memory.
+//
+// One step: warp w sums pairs w, w + 16, ... over the CTA's rows (lanes
+// stride the rows, shuffle reduction), lane 0 writes the pair's partial to
+// a double-buffered array, one cluster barrier, then every warp adds the
+// cluster's partials over distributed shared memory and takes the argmin
+// itself (strict <, lowest pair index on ties), keeping its own copy of the
+// chosen strengths -- so a step has one barrier. The cluster that finishes
+// last (a counter in the frame descriptor) picks the bit count with the
+// lowest RD cost (strict <, in i order) and writes the per-fb indices.
 constexpr int kFinCluster = 8;
 constexpr int kFinThreads = 512;
+constexpr int kFinWarps = kFinThreads / 32;
+constexpr int kFinRowsPerLane = 8;  // register-cached best for up to 256 rows per CTA
 
-__global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThreads)
+__global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThreads, 1)
     k_cdef_finish(FrameDesc *frames, const int *frame_ids, int smem_bytes) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
-    extern __shared__ uint32_t dyn[];
-    __shared__ unsigned long long tot[kMaxCand * kMaxCand];   // this CTA's partial
-    __shared__ unsigned long long tsum[kMaxCand * kMaxCand];  // cluster-wide sum
-    __shared__ unsigned long long rv[32];
-    __shared__ int ri[32];
+    // dynamic: the double-buffered pair partials, then (when they fit) the
+    // compacted rows and their filter-block ids
+    extern __shared__ unsigned long long dyn64[];
+    __shared__ uint8_t wlev[kFinWarps][2][16];
     __shared__ int scan[kFinThreads];
-    __shared__ int lev0[17], lev1[17], blev0[8], blev1[8];
-    __shared__ int best_bits, local_sb;
-    __shared__ unsigned long long res_v;
+    __shared__ int local_sb, last_flag;
     const int rank = (int)cl.block_rank();
-    FrameDesc &f = frames[frame_ids[blockIdx.x / kFinCluster]];
+    const int cluster = blockIdx.x / kFinCluster;
+    const int level = cluster % kFinLevels;
+    FrameDesc &f = frames[frame_ids[cluster / kFinLevels]];
     CdefParams &cp = f.cdef;
     if (cp.mode != 1) return;  // uniform over the cluster
     const int nfb = f.nhfb * f.nvfb, n_cand = cp.ncand, n2 = 2 * n_cand, npairs = n_cand * n_cand;
-    const int T = blockDim.x, t = threadIdx.x;
+    const int T = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int fb0 = (int)((int64_t)nfb * rank / kFinCluster), fb1 = (int)((int64_t)nfb * (rank + 1) / kFinCluster);
     // compaction of this range's filter blocks with rows, in fb order
     const int span = fb1 - fb0, chunk = (span + T - 1) / T;
@@ -565,159 +575,187 @@ __global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThread
         __syncthreads();
     }
     const int sbr = scan[T - 1];
-    int pos = fb0 + scan[t] - cnt;
-    for (int fb = c0; fb < c1; ++fb)
-        if (f.fb_row[fb]) f.cdef_ids[pos++] = fb;
-    for (int fb = fb0 + t; fb < fb1; fb += T) f.fb_idx[fb] = 0;
+    unsigned long long *tot[2] = {dyn64, dyn64 + npairs};
+    uint32_t *dyn = reinterpret_cast<uint32_t *>(dyn64 + 2 * npairs);
+    const bool in_smem = (size_t)2 * npairs * 8 + (size_t)sbr * (n2 + 1) * 4 <= (size_t)smem_bytes;
+    uint32_t *R = in_smem ? dyn : f.cdef_rows32 + ((size_t)level * nfb + fb0) * n2;
+    int *ids = in_smem ? reinterpret_cast<int *>(dyn + (size_t)sbr * n2) : f.cdef_ids + (size_t)level * nfb + fb0;
+    {
+        int pos = scan[t] - cnt;
+        for (int fb = c0; fb < c1; ++fb)
+            if (f.fb_row[fb]) ids[pos++] = fb;
+    }
     if (t == 0) local_sb = sbr;
     cl.sync();
     int sb = 0;
     for (int r = 0; r < kFinCluster; ++r) sb += *cl.map_shared_rank(&local_sb, r);
     if (sb == 0) {  // every filter block all-skip: cdef.rs:282-288
-        if (rank == 0 && t == 0) {
-            cp.bits = 0;
-            cp.y_str[0] = 0;
-            cp.uv_str[0] = 0;
+        if (level == 0) {
+            for (int fb = fb0 + t; fb < fb1; fb += T) f.fb_idx[fb] = 0;
+            if (rank == 0 && t == 0) {
+                cp.bits = 0;
+                cp.y_str[0] = 0;
+                cp.uv_str[0] = 0;
+            }
         }
         cl.sync();
         return;
     }
-    const bool in_smem = (size_t)sbr * (n2 + 1) * 4 <= (size_t)smem_bytes;
-    uint32_t *R = in_smem ? dyn : f.cdef_rows32 + (size_t)fb0 * n2;
-    uint32_t *best = in_smem ? dyn + (size_t)sbr * n2 : reinterpret_cast<uint32_t *>(f.cdef_best) + fb0;
     for (int q = t; q < sbr * n2; q += T) {
         const int k = q / sbr, s = q - k * sbr;  // column-major: R[k * sbr + s]
-        R[q] = (uint32_t)f.mse[(int64_t)f.cdef_ids[fb0 + s] * n2 + k];
+        R[q] = (uint32_t)f.mse[(int64_t)ids[s] * n2 + k];
+    }
+    if (lane < 16) {
+        wlev[warp][0][lane] = 0;
+        wlev[warp][1][lane] = 0;
     }
     __syncthreads();
+    uint8_t *lev0 = wlev[warp][0], *lev1 = wlev[warp][1];
 
-    // One search_one_dual step over the whole frame.
+    int buf = 0;
+    // One search_one_dual step (cdef.rs:824-862) over the whole frame for
+    // strength slot nbs; returns the best total and records the pair.
     auto step = [&](int nbs) -> unsigned long long {
-        for (int p = t; p < npairs; p += T) tot[p] = 0;
-        for (int s = t; s < sbr; s += T) {
-            uint32_t b = 0xffffffffu;  // +infinity for an empty strength set
-            for (int gi = 0; gi < nbs; ++gi) {
-                const uint32_t c = R[lev0[gi] * sbr + s] + R[(n_cand + lev1[gi]) * sbr + s];
-                b = c < b ? c : b;
+        const bool cached = sbr <= 32 * kFinRowsPerLane;
+        uint32_t bst[kFinRowsPerLane];
+        if (cached) {
+#pragma unroll
+            for (int r = 0; r < kFinRowsPerLane; ++r) {
+                const int s = lane + 32 * r;
+                uint32_t b = 0xffffffffu;  // +infinity for an empty strength set
+                if (s < sbr)
+                    for (int gi = 0; gi < nbs; ++gi) {
+                        const uint32_t c = R[lev0[gi] * sbr + s] + R[(n_cand + lev1[gi]) * sbr + s];
+                        b = c < b ? c : b;
+                    }
+                bst[r] = b;
             }
-            best[s] = b;
         }
-        __syncthreads();
-        const int tpp = max(1, T / npairs);
-        for (int w = t; w < npairs * tpp; w += T) {
-            const int p = w / tpp, part = w - p * tpp;
+        for (int p = warp; p < npairs; p += kFinWarps) {
             const int j = p / n_cand, k = p - j * n_cand;
             const uint32_t *rj = R + (size_t)j * sbr, *rk = R + (size_t)(n_cand + k) * sbr;
             unsigned long long acc = 0;
-            for (int s = part; s < sbr; s += tpp) {
-                const uint32_t c = rj[s] + rk[s], b = best[s];
-                acc += c < b ? c : b;
+            if (cached) {
+#pragma unroll
+                for (int r = 0; r < kFinRowsPerLane; ++r) {
+                    const int s = lane + 32 * r;
+                    if (s < sbr) {
+                        const uint32_t c = rj[s] + rk[s];
+                        acc += c < bst[r] ? c : bst[r];
+                    }
+                }
+            } else {
+                for (int s = lane; s < sbr; s += 32) {
+                    uint32_t b = 0xffffffffu;
+                    for (int gi = 0; gi < nbs; ++gi) {
+                        const uint32_t c = R[lev0[gi] * sbr + s] + R[(n_cand + lev1[gi]) * sbr + s];
+                        b = c < b ? c : b;
+                    }
+                    const uint32_t c = rj[s] + rk[s];
+                    acc += c < b ? c : b;
+                }
             }
-            atomicAdd(&tot[p], acc);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+            if (lane == 0) tot[buf][p] = acc;
         }
-        cl.sync();  // partials complete everywhere
-        for (int p = t; p < npairs; p += T) {
-            unsigned long long v = 0;
-            for (int r = 0; r < kFinCluster; ++r) v += cl.map_shared_rank(tot, r)[p];
-            tsum[p] = v;
-        }
-        cl.sync();  // every CTA has read every partial before the next step
-        // argmin with strict < in (j, k) raster order: lowest index wins ties
+        cl.sync();  // partials of this step complete everywhere
         unsigned long long bv = ~0ull;
         int bi = 0x7fffffff;
-        for (int p = t; p < npairs; p += T) {
-            const unsigned long long v = tsum[p];
-            if (v < bv || (v == bv && p < bi)) {
+        for (int p = lane; p < npairs; p += 32) {
+            unsigned long long v = 0;
+            for (int r = 0; r < kFinCluster; ++r) v += cl.map_shared_rank(tot[buf], r)[p];
+            if (v < bv) {  // p increases along a lane: strict < keeps the lowest
                 bv = v;
                 bi = p;
             }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const unsigned long long ov = __shfl_down_sync(0xffffffffu, bv, o);
-            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+            const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
             if (ov < bv || (ov == bv && oi < bi)) {
                 bv = ov;
                 bi = oi;
             }
         }
-        if ((t & 31) == 0) {
-            rv[t >> 5] = bv;
-            ri[t >> 5] = bi;
+        if (bv >= (1ull << 63)) {  // best_tot starts at 1 << 63 with strict <
+            bi = 0;
+            bv = 1ull << 63;
         }
-        __syncthreads();
-        if (t == 0) {
-            unsigned long long v = ~0ull;
-            int idx = 0x7fffffff;
-            for (int w = 0; w < T / 32; ++w)
-                if (rv[w] < v || (rv[w] == v && ri[w] < idx)) {
-                    v = rv[w];
-                    idx = ri[w];
-                }
-            if (v >= (1ull << 63)) {  // best_tot starts at 1 << 63 with strict <
-                idx = 0;
-                v = 1ull << 63;
-            }
-            lev0[nbs] = idx / n_cand;
-            lev1[nbs] = idx % n_cand;
-            res_v = v;
+        if (lane == 0) {
+            lev0[nbs] = (uint8_t)(bi / n_cand);
+            lev1[nbs] = (uint8_t)(bi % n_cand);
         }
-        __syncthreads();
-        return res_v;
+        __syncwarp();
+        buf ^= 1;
+        return bv;
     };
 
-    unsigned long long best_cost = 1ull << 63;
-    if (t == 0) best_bits = 0;
-    for (int i = 0; i <= 3; ++i) {
-        const int nb = 1 << i;
-        if (t < 17) {
-            lev0[t] = 0;
-            lev1[t] = 0;
+    const int nb = 1 << level;
+    unsigned long long tt = 1ull << 63;
+    for (int s = 0; s < nb; ++s) tt = step(s);
+    for (int r = 0; r < 4 * nb; ++r) {
+        if (lane == 0)
+            for (int j = 0; j < nb - 1; ++j) {
+                lev0[j] = lev0[j + 1];
+                lev1[j] = lev1[j + 1];
+            }
+        __syncwarp();
+        tt = step(nb - 1);
+    }
+    // publish this bit count's result; the last cluster of the frame decides
+    if (rank == 0 && t == 0) {
+        const unsigned long long total_bits = (unsigned long long)sb * level + nb * 12;
+        f.fin_cost[level] = rdc(cp.lambda, total_bits << 9, tt * 16);
+        for (int k = 0; k < 8; ++k) {
+            f.fin_lev[level][k] = k < nb ? lev0[k] : 0;
+            f.fin_lev[level][8 + k] = k < nb ? lev1[k] : 0;
         }
-        __syncthreads();
-        unsigned long long tt = 1ull << 63;
-        for (int s = 0; s < nb; ++s) tt = step(s);
-        for (int r = 0; r < 4 * nb; ++r) {
-            if (t == 0)
-                for (int j = 0; j < nb - 1; ++j) {
-                    lev0[j] = lev0[j + 1];
-                    lev1[j] = lev1[j + 1];
-                }
-            __syncthreads();
-            tt = step(nb - 1);
-        }
-        const unsigned long long total_bits = (unsigned long long)sb * i + nb * 12;
-        const unsigned long long cost = rdc(cp.lambda, total_bits << 9, tt * 16);
-        if (cost < best_cost) {
-            best_cost = cost;
-            if (t == 0) {
-                best_bits = i;
-                for (int k = 0; k < nb; ++k) {
-                    blev0[k] = lev0[k];
-                    blev1[k] = lev1[k];
-                }
+        __threadfence();
+        last_flag = atomicAdd(&f.fin_done, 1) == kFinLevels - 1;
+    }
+    cl.sync();
+    const bool last = *cl.map_shared_rank(&last_flag, 0) != 0;
+    cl.sync();  // rank 0's shared memory must outlive every CTA's read of it
+    if (!last) return;
+    __threadfence();
+    __shared__ int best_bits;
+    __shared__ uint8_t blev[16];
+    if (t == 0) {
+        unsigned long long best_cost = 1ull << 63;
+        int bb = 0;
+        for (int i = 0; i < kFinLevels; ++i) {
+            const unsigned long long c = __ldcg(&f.fin_cost[i]);
+            if (c < best_cost) {
+                best_cost = c;
+                bb = i;
             }
         }
-        __syncthreads();
+        best_bits = bb;
+        for (int k = 0; k < 16; ++k) blev[k] = *(volatile uint8_t *)&f.fin_lev[bb][k];
     }
-    const int nb = 1 << best_bits;
+    __syncthreads();
+    const int bnb = 1 << best_bits;
+    for (int fb = fb0 + t; fb < fb1; fb += T) f.fb_idx[fb] = 0;
+    __syncthreads();
     for (int s = t; s < sbr; s += T) {
         int best_gi = 0;
         unsigned long long bst = ~0ull;
-        for (int gi = 0; gi < nb; ++gi) {
-            const unsigned long long c = (unsigned long long)R[blev0[gi] * sbr + s] + R[(n_cand + blev1[gi]) * sbr + s];
+        for (int gi = 0; gi < bnb; ++gi) {
+            const unsigned long long c = (unsigned long long)R[blev[gi] * sbr + s] + R[(n_cand + blev[8 + gi]) * sbr + s];
             if (c < bst) {
                 bst = c;
                 best_gi = gi;
             }
         }
-        f.fb_idx[f.cdef_ids[fb0 + s]] = (uint8_t)best_gi;
+        f.fb_idx[ids[s]] = (uint8_t)best_gi;
     }
     if (rank == 0 && t == 0) {
         cp.bits = best_bits;
         for (int gi = 0; gi < 8; ++gi) {
-            cp.y_str[gi] = gi < nb ? (uint8_t)cp.fs[blev0[gi]] : 0;
-            cp.uv_str[gi] = gi < nb ? (uint8_t)cp.fs[blev1[gi]] : 0;
+            cp.y_str[gi] = gi < bnb ? (uint8_t)cp.fs[blev[gi]] : 0;
+            cp.uv_str[gi] = gi < bnb ? (uint8_t)cp.fs[blev[8 + gi]] : 0;
         }
     }
 }
@@ -858,9 +896,8 @@ struct NoAllocScratch {
     int frame_id;
     int pad;
     uint64_t mse[kNoAllocMaxFb * 2 * kNoAllocMaxCand];
-    uint64_t best[kNoAllocMaxFb];
-    uint32_t rows32[kNoAllocMaxFb * 2 * kNoAllocMaxCand];
-    int ids[kNoAllocMaxFb];
+    uint32_t rows32[kFinLevels * kNoAllocMaxFb * 2 * kNoAllocMaxCand];
+    int ids[kFinLevels * kNoAllocMaxFb];
     uint8_t fb_row[kNoAllocMaxFb];
     uint8_t fb_idx[kNoAllocMaxFb];
 };
@@ -921,7 +958,6 @@ extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_de
     d.mse = sc->mse;
     d.fb_row = sc->fb_row;
     d.fb_idx = sc->fb_idx;
-    d.cdef_best = sc->best;
     d.cdef_ids = sc->ids;
     d.cdef_rows32 = sc->rows32;
     d.cdef_stats = nullptr;
@@ -942,8 +978,10 @@ extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_de
     if (launch_cdef_search(d.cdef.first_pass_num, d.cdef.ncand / d.cdef.first_pass_num, nfb, st, &sc->desc,
                            &sc->item, 1) != cudaSuccess)
         return ZF_ERR_CUDA;
-    const int per_cta = (nfb + kFinCluster - 1) / kFinCluster * (2 * d.cdef.ncand + 1) * 4;  // < 48 KiB
-    k_cdef_finish<<<kFinCluster, kFinThreads, per_cta, st>>>(&sc->desc, &sc->frame_id, per_cta);
+    // pair partials + compacted rows and ids: < 48 KiB for ncand <= 20 and nfb <= 2048
+    const int per_cta = 2 * d.cdef.ncand * d.cdef.ncand * 8 +
+                        (nfb + kFinCluster - 1) / kFinCluster * (2 * d.cdef.ncand + 1) * 4;
+    k_cdef_finish<<<kFinCluster * kFinLevels, kFinThreads, per_cta, st>>>(&sc->desc, &sc->frame_id, per_cta);
     if (cudaGetLastError() != cudaSuccess) return ZF_ERR_CUDA;
     FrameDesc back;
     if (cudaMemcpyAsync(&back, &sc->desc, sizeof(back), cudaMemcpyDeviceToHost, st) != cudaSuccess) return ZF_ERR_CUDA;

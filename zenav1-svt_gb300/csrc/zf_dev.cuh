@@ -59,6 +59,9 @@ struct LrPlane {
     PackedUnit *packed;  // hunits*vunits output records
 };
 
+// CDEF joint strength search: bit counts 0..3, one cluster each.
+constexpr int kFinLevels = 4;
+
 struct CdefParams {
     int mode;            // 0: off (nothing signaled), 1: search, 2: fixed pick
     int damping, bits;
@@ -88,10 +91,14 @@ struct FrameDesc {
     uint64_t *mse;          // nfb x 2 x ncand
     uint8_t *fb_row;        // nfb: fb has a non-skip 8x8
     uint8_t *fb_idx;        // nfb
-    uint64_t *cdef_best;    // nfb scratch for the joint search
-    int *cdef_ids;          // nfb: compacted filter-block ids with rows
-    uint32_t *cdef_rows32;  // nfb x 2 x ncand: compacted rows (global fallback)
+    int *cdef_ids;          // 4 x nfb: compacted filter-block ids with rows (global fallback)
+    uint32_t *cdef_rows32;  // 4 x nfb x 2 x ncand: compacted rows (global fallback)
     unsigned long long *cdef_stats;  // [filtered, changed, sb_count]
+    // joint strength search, one result per bit count 0..3 (zero on upload)
+    unsigned long long fin_cost[4];
+    uint8_t fin_lev[4][16];  // lev0[0..8) then lev1[0..8)
+    int fin_done;            // clusters finished
+    int fin_pad;
     // LR
     LrPlane lr[3];
     int64_t rdmult;

@@ -332,7 +332,7 @@ struct Plan {
     int nfb = 0;
     size_t off_set[3][3];             // [set A/B/C][plane]
     size_t off_src[3];
-    size_t off_mi = 0, off_mse = 0, off_best = 0, off_ids = 0, off_rows32 = 0;
+    size_t off_mi = 0, off_mse = 0, off_ids = 0, off_rows32 = 0;
     // relative to the batch's units region (zeroed with one memset)
     size_t off_units[3];
     // relative to the rectangles part of the metadata region
@@ -405,9 +405,8 @@ void plan_frame(Plan &p, const zf_frame *f, size_t &cursor, size_t &ucur, size_t
     for (int pl = 0; pl < 3; ++pl) p.off_src[pl] = pl < p.nplanes ? take(p.pbytes[pl]) : 0;
     p.off_mi = take((size_t)d.mi_cols * d.mi_rows * 4);
     p.off_mse = take((size_t)p.nfb * 2 * zf::kMaxCand * 8);
-    p.off_best = take((size_t)p.nfb * 8);
-    p.off_ids = take((size_t)p.nfb * 4);
-    p.off_rows32 = take((size_t)p.nfb * 2 * zf::kMaxCand * 4);
+    p.off_ids = take((size_t)zf::kFinLevels * p.nfb * 4);
+    p.off_rows32 = take((size_t)zf::kFinLevels * p.nfb * 2 * zf::kMaxCand * 4);
     p.off_fbrow = take_in(ocur, p.nfb);
     p.off_fbidx = take_in(ocur, p.nfb);
     p.off_stats = take_in(ocur, 4 * 8);
@@ -455,7 +454,6 @@ void bind_pointers(Plan &p, uint8_t *base, uint8_t *units, uint8_t *rects, uint8
     d.mse = (uint64_t *)(base + p.off_mse);
     d.fb_row = out + p.off_fbrow;
     d.fb_idx = out + p.off_fbidx;
-    d.cdef_best = (uint64_t *)(base + p.off_best);
     d.cdef_ids = (int *)(base + p.off_ids);
     d.cdef_rows32 = (uint32_t *)(base + p.off_rows32);
     d.cdef_stats = (unsigned long long *)(out + p.off_stats);
@@ -837,16 +835,20 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                                   (int)wl_cs.items.size())); }
         TRY(launch_check(ctx, "k_cdef_search"));
         { LaunchScope ls_(ctx, "k_cdef_finish");
-        // dynamic shared memory for the compacted rows: the largest frame
-        // of the batch, capped (frames that do not fit use global scratch)
-        size_t want = 0;
-        for (int fi : cdef_frames)
-            want = std::max(want, ((size_t)plans[fi].nfb + zf::kFinClusterHost - 1) / zf::kFinClusterHost *
-                                      (2 * plans[fi].d.cdef.ncand + 1) * 4);
-        const int smem = (int)std::min<size_t>(want, kFinishSmemCap);
+        // dynamic shared memory: the double-buffered pair partials (always)
+        // and the compacted rows of the largest frame of the batch, capped
+        // (frames whose rows do not fit use global scratch)
+        size_t want = 0, pairs = 0;
+        for (int fi : cdef_frames) {
+            const size_t nc = (size_t)plans[fi].d.cdef.ncand;
+            pairs = std::max(pairs, 2 * nc * nc * 8);
+            want = std::max(want, 2 * nc * nc * 8 + ((size_t)plans[fi].nfb + zf::kFinClusterHost - 1) /
+                                                         zf::kFinClusterHost * (2 * nc + 1) * 4);
+        }
+        const int smem = (int)std::max(pairs, std::min<size_t>(want, kFinishSmemCap));
         CU(cudaFuncSetAttribute(zf::k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinishSmemCap));
-        zf::k_cdef_finish<<<(int)cdef_frames.size() * zf::kFinClusterHost, zf::kFinThreadsHost, smem, st>>>(
-            d_desc, (const int *)(base + o_cf), smem); }
+        zf::k_cdef_finish<<<(int)cdef_frames.size() * zf::kFinClusterHost * zf::kFinLevels, zf::kFinThreadsHost,
+                            smem, st>>>(d_desc, (const int *)(base + o_cf), smem); }
         TRY(launch_check(ctx, "k_cdef_finish"));
         TRY(check_cancel(ctx));
     }

@@ -28,7 +28,7 @@ __global__ void k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems)
 // Fills dims and the CDEF policy of *d from a frame (host; zf_host.cu).
 int describe_cdef_frame(const zf_frame *f, FrameDesc *d);
 
-constexpr int kFinClusterHost = 8;  // k_cdef_finish: CTAs per frame (cluster size)
+constexpr int kFinClusterHost = 8;  // k_cdef_finish: CTAs per cluster
 constexpr int kFinThreadsHost = 512;
 constexpr int kSumRowsHost = 16;   // k_lr_sums rows per CTA
 // k_lr_stats<win>: rows per CTA over the unit's rows extended by win/2 on
