@@ -28,15 +28,6 @@ __constant__ int8_t kDir[8][2][2] = {
 
 __device__ __forceinline__ int msb(unsigned v) { return 31 - __clz(v); }
 
-// constrain (cdef.rs:113-120).
-__device__ __forceinline__ int constrain(int diff, int threshold, int damping) {
-    if (threshold == 0) return 0;
-    int shift = max(0, damping - msb((unsigned)threshold));
-    int ad = abs(diff);
-    int v = min(ad, max(0, threshold - (ad >> shift)));
-    return diff < 0 ? -v : v;
-}
-
 // adjust_strength (cdef.rs:125-136).
 __device__ __forceinline__ int adjust_strength(int strength, int var) {
     int i = (var >> 6) != 0 ? min(msb((unsigned)(var >> 6)), 12) : 0;
@@ -142,47 +133,6 @@ __device__ void find_dirs(const uint16_t *reg, int rs, int cs, const int *blist,
         svar[b] = (best_cost - cost[b][(best_dir + 4) & 7]) >> 10;
     }
     __syncthreads();
-}
-
-// One output pixel of svt_cdef_filter_block_c: wrapping int16 tap sum,
-// taps read as int16, the sentinel excluded from max only.
-__device__ __forceinline__ int cdef_px(const uint16_t *reg, int rs, int pos, int pri, int sec, int dir, int pdamp,
-                                       int sdamp, int coeff_shift) {
-    const int ptap0 = ((pri >> coeff_shift) & 1) ? 3 : 4, ptap1 = ((pri >> coeff_shift) & 1) ? 3 : 2;
-    const int x = (int16_t)reg[pos];
-    int16_t sum = 0;
-    int mx = x, mn = x;
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const int ptap = k ? ptap1 : ptap0, stap = k ? 1 : 2;
-        const int od = kDir[dir][k][0] * rs + kDir[dir][k][1];
-        const int o2 = kDir[(dir + 2) & 7][k][0] * rs + kDir[(dir + 2) & 7][k][1];
-        const int o6 = kDir[(dir + 6) & 7][k][0] * rs + kDir[(dir + 6) & 7][k][1];
-        const uint16_t r0 = reg[pos + od], r1 = reg[pos - od];
-        const int p0 = (int16_t)r0, p1 = (int16_t)r1;
-        sum = (int16_t)(sum + (int16_t)(ptap * constrain(p0 - x, pri, pdamp)));
-        sum = (int16_t)(sum + (int16_t)(ptap * constrain(p1 - x, pri, pdamp)));
-        if (r0 != kVeryLarge) mx = max(p0, mx);
-        if (r1 != kVeryLarge) mx = max(p1, mx);
-        mn = min(p0, mn);
-        mn = min(p1, mn);
-        const uint16_t t0 = reg[pos + o2], t1 = reg[pos - o2], t2 = reg[pos + o6], t3 = reg[pos - o6];
-        const int s0 = (int16_t)t0, s1 = (int16_t)t1, s2 = (int16_t)t2, s3 = (int16_t)t3;
-        if (t0 != kVeryLarge) mx = max(s0, mx);
-        if (t1 != kVeryLarge) mx = max(s1, mx);
-        if (t2 != kVeryLarge) mx = max(s2, mx);
-        if (t3 != kVeryLarge) mx = max(s3, mx);
-        mn = min(s0, mn);
-        mn = min(s1, mn);
-        mn = min(s2, mn);
-        mn = min(s3, mn);
-        sum = (int16_t)(sum + (int16_t)(stap * constrain(s0 - x, sec, sdamp)));
-        sum = (int16_t)(sum + (int16_t)(stap * constrain(s1 - x, sec, sdamp)));
-        sum = (int16_t)(sum + (int16_t)(stap * constrain(s2 - x, sec, sdamp)));
-        sum = (int16_t)(sum + (int16_t)(stap * constrain(s3 - x, sec, sdamp)));
-    }
-    const int y = x + ((8 + (int)sum - (int)(sum < 0)) >> 4);
-    return min(max(y, mn), mx);
 }
 
 // Stage a plane window [y0-2, y0+n+2) x [x0-2, x0+n+2) with the sentinel
@@ -766,6 +716,8 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     __shared__ uint16_t reg[CR * CR];
     __shared__ int sdir[64], svar[64];
     __shared__ int dcost[64][8];
+    __shared__ int boff[64][6], boffc[64][6];
+    __shared__ int bt[64];  // luma: adjusted primary strength | damping shift << 16
     __shared__ int blist[64];
     __shared__ int nblk;
     __shared__ unsigned long long red[8];
@@ -811,18 +763,30 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     }
     __syncthreads();
     find_dirs(reg, CR, cs, blist, nblk, dcost, sdir, svar);
+    for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
+        const int b = blist[k];
+        dir_offsets(lvl_y ? sdir[b] : 0, CR, boff[b]);
+        dir_offsets(lvl_uv ? sdir[b] : 0, CRC, boffc[b]);
+        const int t = adjust_strength(lvl_y, svar[b]);
+        bt[b] = t | (damp_shift(t, damping) << 16);
+    }
+    __syncthreads();
     unsigned long long filt = 0, changed = 0;
     const bool zero_y = lvl_y == 0 && sec_y == 0;
+    const int ssh_y = damp_shift(sec_y, damping);
     for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
-        const int py = i / 64, px = i & 63;
+        const int py = i >> 6, px = i & 63;
         if (py >= vsize || px >= hsize) continue;
         const int b = (py >> 3) * 8 + (px >> 3);
-        const int x = reg[(py + 2) * CR + px + 2];
+        const int pos = (py + 2) * CR + px + 2;
+        const int x = (int16_t)reg[pos];
         int y = x;
         if (!zero_y && ((dl >> b) & 1)) {
-            const int t = adjust_strength(lvl_y, svar[b]);
-            if (!(t == 0 && sec_y == 0)) {
-                y = cdef_px(reg, CR, (py + 2) * CR + px + 2, t, sec_y, lvl_y ? sdir[b] : 0, damping, damping, cs);
+            const int tp = bt[b], t = tp & 0xffff;
+            if (!(t == 0 && sec_y == 0)) {  // cdef.rs:444-448
+                int d[12], mx, mn;
+                load_taps(reg, pos, boff[b], x, d, mx, mn);
+                y = cdef_round(x, prim_sum(d, t, tp >> 16, cs) + sec_sum(d, sec_y, ssh_y), mn, mx);
                 filt += 1;
                 changed += y != x;
             }
@@ -831,20 +795,23 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     }
     if (f.chroma) {
         const bool zero_uv = lvl_uv == 0 && sec_uv == 0;
+        const int psh = damp_shift(lvl_uv, damping - 1), ssh = damp_shift(sec_uv, damping - 1);
         const int cw = f.w / 2, ch = f.h / 2, cx0 = x0 / 2, cy0 = y0 / 2;
         for (int p = 1; p <= 2; ++p) {
             __syncthreads();
             load_region(f.B[p], bd, cw, ch, cx0, cy0, 32, reg);
             __syncthreads();
             for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
-                const int py = i / 32, px = i & 31;
+                const int py = i >> 5, px = i & 31;
                 if (py >= vsize / 2 || px >= hsize / 2) continue;
                 const int b = (py >> 2) * 8 + (px >> 2);
-                const int x = reg[(py + 2) * CRC + px + 2];
+                const int pos = (py + 2) * CRC + px + 2;
+                const int x = (int16_t)reg[pos];
                 int y = x;
                 if (!zero_uv && ((dl >> b) & 1)) {
-                    y = cdef_px(reg, CRC, (py + 2) * CRC + px + 2, lvl_uv, sec_uv, lvl_uv ? sdir[b] : 0, damping - 1,
-                                damping - 1, cs);
+                    int d[12], mx, mn;
+                    load_taps(reg, pos, boffc[b], x, d, mx, mn);
+                    y = cdef_round(x, prim_sum(d, lvl_uv, psh, cs) + sec_sum(d, sec_uv, ssh), mn, mx);
                     filt += 1;
                     changed += y != x;
                 }

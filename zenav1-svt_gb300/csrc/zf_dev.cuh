@@ -30,6 +30,7 @@ struct LrUnit {
     unsigned long long sse_bot; // u32 at 10 bits, restoration.rs:1991-2036)
     int64_t sse_none;
     int64_t sse_wn;             // trial SSE, INT64_MAX when the score reverts
+    unsigned long long tw_blk, tw_rgt, tw_bot;  // tiled trial SSE parts (no refinement)
     int64_t score;
     int64_t m[49];              // M, raw sums (before the bit-depth divider)
     int64_t h[2401];            // H upper triangle, row-major win2 x win2

@@ -557,7 +557,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         plans[i].out = outs ? &outs[i] : nullptr;
     }
     // Work lists (host-known shapes).
-    WorkList wl_db, wl_cs, wl_ca, wl_sum, wl_st5, wl_st7, wl_unit, wl_apply;
+    WorkList wl_db, wl_cs, wl_ca, wl_sum, wl_st5, wl_st7, wl_unit, wl_apply, wl_trial, wl_tiles;
     std::vector<int> cdef_frames;
     for (int i = 0; i < n; ++i) {
         Plan &p = plans[i];
@@ -580,6 +580,12 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 const int half = L.win / 2, srows = zf::stat_rows_host(L.win);
                 for (int c = -half; c < uh + half; c += srows) (L.win == 5 ? wl_st5 : wl_st7).add(i, pl, (int)u, c, 1);
                 wl_unit.add(i, pl, (int)u, 0, 1);
+                if (L.refine) {
+                    wl_trial.add(i, pl, (int)u, 0, 1);  // one CTA per unit: the hill-climb is sequential
+                } else {
+                    const int tl = zf::kTrialTileHost, uw = r.h_end - r.h_start;
+                    wl_tiles.add(i, pl, (int)u, 0, ((uw + tl - 1) / tl) * ((uh + tl - 1) / tl));
+                }
             }
             const int ss = pl ? 1 : 0, full = 64 >> ss, off = 8 >> ss;
             const int nstripes = (L.ph + off + full - 1) / full;
@@ -617,9 +623,11 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     };
     const size_t desc_bytes = (size_t)n * sizeof(FrameDesc);
     const size_t m_desc = mtake(desc_bytes);
-    const WorkList *lists[8] = {&wl_db, &wl_cs, &wl_ca, &wl_sum, &wl_st5, &wl_st7, &wl_unit, &wl_apply};
-    size_t m_list[8];
-    for (int k = 0; k < 8; ++k) m_list[k] = mtake(lists[k]->items.size() * sizeof(WorkItem));
+    constexpr int kLists = 10;
+    const WorkList *lists[kLists] = {&wl_db,  &wl_cs,   &wl_ca,    &wl_sum,   &wl_st5,
+                                     &wl_st7, &wl_unit, &wl_apply, &wl_trial, &wl_tiles};
+    size_t m_list[kLists];
+    for (int k = 0; k < kLists; ++k) m_list[k] = mtake(lists[k]->items.size() * sizeof(WorkItem));
     const size_t m_cf = mtake(cdef_frames.size() * 4);
     const size_t m_rects = mtake(rcur);
     const size_t meta_bytes = align_up(mcur, 256);
@@ -644,7 +652,8 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     FrameDesc *d_desc = (FrameDesc *)(base + o_meta + m_desc);
     const size_t o_db = o_meta + m_list[0], o_cs = o_meta + m_list[1], o_ca = o_meta + m_list[2],
                  o_sum = o_meta + m_list[3], o_st5 = o_meta + m_list[4], o_st7 = o_meta + m_list[5],
-                 o_unit = o_meta + m_list[6], o_apply = o_meta + m_list[7], o_cf = o_meta + m_cf;
+                 o_unit = o_meta + m_list[6], o_apply = o_meta + m_list[7], o_trial = o_meta + m_list[8],
+                 o_tiles = o_meta + m_list[9], o_cf = o_meta + m_cf;
     // outputs start zeroed (statistics counters, fb_idx of skipped searches)
     CU(cudaMemsetAsync(base + o_out, 0, out_bytes, st));
 
@@ -807,7 +816,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         uint8_t *hm = ctx->h_meta;
         FrameDesc *hd = (FrameDesc *)(hm + m_desc);
         for (int i = 0; i < n; ++i) hd[i] = plans[i].d;
-        for (int k = 0; k < 8; ++k)
+        for (int k = 0; k < kLists; ++k)
             if (!lists[k]->items.empty())
                 std::memcpy(hm + m_list[k], lists[k]->items.data(), lists[k]->items.size() * sizeof(WorkItem));
         if (!cdef_frames.empty()) std::memcpy(hm + m_cf, cdef_frames.data(), cdef_frames.size() * 4);
@@ -883,10 +892,18 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             zf::k_lr_solve<<<wl_unit.ctas, 128, 0, st>>>(d_desc, (const WorkItem *)(base + o_unit),
                                                         (int)wl_unit.items.size()); }
             TRY(launch_check(ctx, "k_lr_solve"));
-            { LaunchScope ls_(ctx, "k_lr_trial");
-            zf::k_lr_trial<<<wl_unit.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_unit),
-                                                        (int)wl_unit.items.size()); }
-            TRY(launch_check(ctx, "k_lr_trial"));
+            if (wl_trial.ctas) {
+                { LaunchScope ls_(ctx, "k_lr_trial");
+                zf::k_lr_trial<<<wl_trial.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_trial),
+                                                             (int)wl_trial.items.size()); }
+                TRY(launch_check(ctx, "k_lr_trial"));
+            }
+            if (wl_tiles.ctas) {
+                { LaunchScope ls_(ctx, "k_lr_trial_tiles");
+                zf::k_lr_trial_tiles<<<wl_tiles.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_tiles),
+                                                                   (int)wl_tiles.items.size()); }
+                TRY(launch_check(ctx, "k_lr_trial_tiles"));
+            }
         }
         { LaunchScope ls_(ctx, "k_lr_finish");
         int max_units = 1;
@@ -1080,12 +1097,12 @@ int32_t zf_query_sizes(const zf_frame *f, zf_sizes *out) {
     Plan p;
     size_t cursor = 0, ucur = 0, rcur = 0, ocur = 0;
     plan_frame(p, f, cursor, ucur, rcur, ocur);
-    // work items (upper bound): per unit its sums / statistics row blocks
-    // and solve item, per plane the apply (stripe, tile) items
+    // work items (upper bound): per unit its sums / statistics row blocks,
+    // solve and trial items, per plane the apply (stripe, tile) items
     size_t items = 16;
     for (int pl = 0; pl < 3; ++pl) {
         const int ss = pl ? 1 : 0;
-        items += p.rects[pl].size() * (384 / 16 + 1 + 392 / 12 + 1 + 1);
+        items += p.rects[pl].size() * (384 / 16 + 1 + 392 / 12 + 1 + 1 + 1);
         items += (size_t)((p.d.lr[pl].ph + (8 >> ss)) / (64 >> ss) + 2) * ((p.d.lr[pl].pw + 63) / 64 + 1);
     }
     const size_t meta = align_up(sizeof(FrameDesc), 256) + items * sizeof(WorkItem) + 11 * 256 + rcur;

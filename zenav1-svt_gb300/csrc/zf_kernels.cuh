@@ -22,6 +22,8 @@ cudaError_t launch_lr_stats(int win, int ctas, cudaStream_t st, FrameDesc *frame
                             int nitems);
 __global__ void k_lr_solve(FrameDesc *frames, const WorkItem *items, int nitems);
 __global__ void k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems);
+__global__ void k_lr_trial_tiles(FrameDesc *frames, const WorkItem *items, int nitems);
+constexpr int kTrialTileHost = 64;  // k_lr_trial_tiles tile edge
 __global__ void k_lr_finish(FrameDesc *frames, int nframes);
 __global__ void k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems);
 

@@ -657,6 +657,83 @@ __global__ void __launch_bounds__(256) k_lr_trial(FrameDesc *frames, const WorkI
     }
 }
 
+// Trial SSE without refinement (presets >= 4), split over the unit's 64x64
+// tiles so that every unit's filter runs on many SMs at once: one CTA per
+// tile (items: a = unit, one item per unit, CTA offset = tile index in
+// raster order), the three sse_region parts accumulate into the unit and
+// k_lr_finish combines them.
+constexpr int TL = 64;
+
+__global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const WorkItem *items, int nitems) {
+    constexpr int SW = TL + 7;
+    __shared__ uint16_t stage[(TL + 7) * SW];
+    __shared__ uint16_t tmp[(TL + 7) * TL];
+    __shared__ unsigned long long red[24];
+    const int it = find_item(items, nitems, blockIdx.x);
+    const WorkItem wi = items[it];
+    const FrameDesc &f = frames[wi.frame];
+    const LrPlane &pl = f.lr[wi.plane];
+    LrUnit &u = pl.units[wi.a];
+    if (u.score > 0) return;  // the unit reverts to NONE: no trial
+    const UnitRect r = pl.rects[wi.a];
+    const int bd = f.bd, stride = plane_stride(f, wi.plane);
+    const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
+    const int dw = uw % 16, dh = uh % 16;
+    const int ntx = (uw + TL - 1) / TL;
+    const int tile = blockIdx.x - wi.cta_begin;
+    const int ty = (tile / ntx) * TL, tx = (tile % ntx) * TL;
+    const int th = min(TL, uh - ty), tw = min(TL, uw - tx);
+    const int y0 = r.v_start + ty, x0 = r.h_start + tx;
+    int16_t hf[8], vf[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        hf[k] = u.hf[k];
+        vf[k] = u.vf[k];
+    }
+    const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
+    for (int q = threadIdx.x; q < (th + 7) * (tw + 7); q += blockDim.x) {
+        const int rr = q / (tw + 7), cc = q - rr * (tw + 7);
+        const int y = clampi(y0 - 3 + rr, 0, pl.ph - 1), x = clampi(x0 - 3 + cc, 0, pl.pw - 1);
+        stage[rr * SW + cc] = (uint16_t)ldpx(dg, (int64_t)y * stride + x, bd);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < (th + 7) * tw; q += blockDim.x) {
+        const int rr = q / tw, cc = q - rr * tw;
+        int px[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) px[k] = stage[rr * SW + cc + k];
+        tmp[rr * TL + cc] = (uint16_t)wiener_h(px, hf, bd);
+    }
+    __syncthreads();
+    unsigned long long blk = 0, rgt = 0, bot = 0;
+    for (int q = threadIdx.x; q < th * tw; q += blockDim.x) {
+        const int rr = q / tw, cc = q - rr * tw;
+        const int i = ty + rr, j = tx + cc;
+        int tp[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) tp[k] = tmp[(rr + k) * TL + cc];
+        const int y = wiener_v(tp, vf, bd);
+        const int e = ldpx(sr, (int64_t)(y0 + rr) * stride + x0 + cc, bd) - y;
+        const unsigned long long e2 = (unsigned long long)((long long)e * e);
+        if (j >= uw - dw) rgt += e2;
+        else if (i >= uh - dh) bot += e2;
+        else blk += e2;
+    }
+    unsigned long long v[3] = {blk, rgt, bot};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+        if ((threadIdx.x & 31) == 0) red[k * 8 + (threadIdx.x >> 5)] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        unsigned long long s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x * 8 + w];
+        if (s) atomicAdd(threadIdx.x == 0 ? &u.tw_blk : threadIdx.x == 1 ? &u.tw_rgt : &u.tw_bot, s);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // 5. Frame RD (search_restoration_still_bd finish, restoration.rs:847-897):
 // one thread per (frame, plane); reference-chained count_wiener_bits and
@@ -759,7 +836,13 @@ __global__ void __launch_bounds__(32) k_lr_finish(FrameDesc *frames, int nframes
         const LrUnit &u = pl.units[k];
         RdUnit r;
         r.sse_none = u.sse_none;
-        r.sse_wn = u.sse_wn;
+        if (pl.refine) {
+            r.sse_wn = u.sse_wn;
+        } else {  // k_lr_trial_tiles parts, combined as sse_region_hbd does
+            r.sse_wn = u.score > 0 ? INT64_MAX
+                       : f.bd == 8 ? (int64_t)(u.tw_blk + u.tw_rgt + u.tw_bot)
+                                   : (int64_t)u.tw_blk + (int64_t)(uint32_t)u.tw_rgt + (int64_t)(uint32_t)u.tw_bot;
+        }
         for (int i = 0; i < 3; ++i) {
             r.v[i] = u.vf[i];
             r.h[i] = u.hf[i];
