@@ -249,7 +249,7 @@ __device__ __forceinline__ void plane_geom(const FrameDesc &f, int plane, int *p
     *ph = plane ? f.h / 2 : f.h;
 }
 
-// Apply: A -> B for one 64x64 tile. Plane gating of apply_deblock_frame
+// Apply: IN -> B for one 64x64 tile. Plane gating of apply_deblock_frame
 // (deblock.rs:951-967): both luma levels zero disables every plane; a chroma
 // plane needs its own level.
 __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, const WorkItem *items, int nitems) {
@@ -279,12 +279,12 @@ __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, 
             int y = t.y0 + i / DB_T, x = t.x0 + (i % DB_T);
             if (x < pw && y < ph) {
                 int64_t o = (int64_t)y * pw + x;
-                stpx(f.B[plane], o, bd, ldpx(f.A[plane], o, bd));
+                stpx(f.B[plane], o, bd, ldpx(f.IN[plane], o, bd));
             }
         }
         return;
     }
-    db_load(t, f.A[plane], reg);
+    db_load(t, f.IN[plane], reg);
     db_params(t, lv, lh, vl, hl);
     __syncthreads();
     db_filter(t, reg, vl, hl, lv, lh);
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
     const int tix = blockIdx.x - wi.cta_begin;
     DbTile t{&f, plane, pw, ph, (tix % tiles_x) * DB_T, (tix / tiles_x) * DB_T};
     const int bd = f.bd;
-    db_load(t, f.A[plane], pristine);
+    db_load(t, f.IN[plane], pristine);
     __syncthreads();
     for (int k = 0; k < 2; ++k) {
         const int lvl = levels[slot * 2 + k];

@@ -82,8 +82,10 @@ struct FrameDesc {
     int mi_cols, mi_rows;
     int nhfb, nvfb;
     uint8_t lf[4];          // deblock levels (written before the apply)
-    // Planes: A = input recon, later post-CDEF; B = post-deblock (pre-CDEF);
-    // C = post-LR (final). S = source.
+    // Planes: IN = input recon (read by the deblock passes only); B =
+    // post-deblock (pre-CDEF); A = post-CDEF; C = post-LR (final); S =
+    // source. IN may be A, or the caller's buffer, which may also be C.
+    uint8_t *IN[3];
     uint8_t *A[3], *B[3], *C[3];
     const uint8_t *S[3];
     const uint32_t *mi;

@@ -342,6 +342,7 @@ struct Plan {
     std::vector<UnitRect> rects[3];
     int hunits[3], vunits[3];
     bool db_search = false;
+    bool zero_copy = false;  // kernels read and write the caller's device planes directly
 };
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) & ~(a - 1); }
@@ -443,6 +444,7 @@ void bind_pointers(Plan &p, uint8_t *base, uint8_t *units, uint8_t *rects, uint8
     for (int pl = 0; pl < 3; ++pl) {
         const bool on = pl < p.nplanes;
         d.A[pl] = on ? base + p.off_set[0][pl] : nullptr;
+        d.IN[pl] = d.A[pl];
         d.B[pl] = on ? base + p.off_set[1][pl] : nullptr;
         d.C[pl] = on ? base + p.off_set[2][pl] : nullptr;
         d.S[pl] = on ? base + p.off_src[pl] : nullptr;
@@ -587,9 +589,16 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                     wl_tiles.add(i, pl, (int)u, 0, ((uw + tl - 1) / tl) * ((uh + tl - 1) / tl));
                 }
             }
+        }
+        // Wiener apply items: every (stripe, 64-px tile) of every plane's
+        // aligned canvas, plus the canvas rows below the true plane (stripe
+        // index nstripes); the kernel filters Wiener units and copies the rest
+        for (int pl = 0; pl < p.nplanes && (run.stages & STG_LR_APPLY); ++pl) {
+            const LrPlane &L = p.d.lr[pl];
             const int ss = pl ? 1 : 0, full = 64 >> ss, off = 8 >> ss;
             const int nstripes = (L.ph + off + full - 1) / full;
-            const int ntiles = (L.pw + 63) / 64;
+            const int ntiles = (L.stride + 63) / 64;
+            const int canvas_h = pl ? p.d.h / 2 : p.d.h;
             // unit of a (stripe, tile): the rectangles form a row-major
             // hunits x vunits grid, so look the column up along the first
             // row and the row along the first column
@@ -604,10 +613,12 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             for (int s = 0, r = 0; s < nstripes; ++s) {
                 const int ys = std::max(0, s * full - off);
                 while (r < vu && ys >= R[(size_t)r * hu].v_end) ++r;
-                if (r >= vu || ys < R[(size_t)r * hu].v_start) continue;
+                const bool row_ok = r < vu && ys >= R[(size_t)r * hu].v_start;
                 for (int t = 0; t < ntiles; ++t)
-                    if (col[t] >= 0) wl_apply.add(i, pl, r * hu + col[t], (s << 16) | t, 1);
+                    wl_apply.add(i, pl, (L.on && row_ok && col[t] >= 0) ? r * hu + col[t] : -1, (s << 16) | t, 1);
             }
+            if (canvas_h > L.ph)
+                for (int t = 0; t < ntiles; ++t) wl_apply.add(i, pl, -1, (nstripes << 16) | t, 1);
         }
     }
     // Arena: per-frame buffers | unit accumulators | metadata image |
@@ -663,12 +674,27 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         const zf_frame *f = p.in;
         const bool dev = f->planes_on_device != 0;
         const int set = run.rec_in;
-        for (int pl = 0; pl < p.nplanes; ++pl) {
-            TRY(copy_in(ctx, base + p.off_set[set][pl], f->rec[pl], p.pbytes[pl], dev));
-            TRY(copy_in(ctx, base + p.off_src[pl], f->src[pl], p.pbytes[pl], dev));
-            if (run.pre_cdef_in) TRY(copy_in(ctx, base + p.off_set[SET_B][pl], run.pre_cdef[pl], p.pbytes[pl], dev));
+        // Whole stage on device planes: the deblock passes read the caller's
+        // recon, the Wiener apply writes every pixel of it at the end (after
+        // the last read), and source and geometry are read in place.
+        p.zero_copy = dev && set == SET_A && run.rec_out == SET_C && !run.pre_cdef_in &&
+                      (run.stages & STG_DB_APPLY) && (run.stages & STG_LR_APPLY);
+        if (p.zero_copy) {
+            for (int pl = 0; pl < p.nplanes; ++pl) {
+                p.d.IN[pl] = static_cast<uint8_t *>(f->rec[pl]);
+                p.d.C[pl] = static_cast<uint8_t *>(f->rec[pl]);
+                p.d.S[pl] = static_cast<const uint8_t *>(f->src[pl]);
+            }
+            p.d.mi = f->mi;
+        } else {
+            for (int pl = 0; pl < p.nplanes; ++pl) {
+                TRY(copy_in(ctx, base + p.off_set[set][pl], f->rec[pl], p.pbytes[pl], dev));
+                TRY(copy_in(ctx, base + p.off_src[pl], f->src[pl], p.pbytes[pl], dev));
+                if (run.pre_cdef_in)
+                    TRY(copy_in(ctx, base + p.off_set[SET_B][pl], run.pre_cdef[pl], p.pbytes[pl], dev));
+            }
+            TRY(copy_in(ctx, base + p.off_mi, f->mi, (size_t)p.d.mi_cols * p.d.mi_rows * 4, dev));
         }
-        TRY(copy_in(ctx, base + p.off_mi, f->mi, (size_t)p.d.mi_cols * p.d.mi_rows * 4, dev));
         for (int pl = 0; pl < 3; ++pl)
             if (!p.rects[pl].empty())
                 std::memcpy(ctx->h_meta + m_rects + p.off_rects[pl], p.rects[pl].data(),
@@ -918,10 +944,6 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     }
     // ---- Wiener apply: A (+ B boundary lines) -> C
     if (run.stages & STG_LR_APPLY) {
-        for (int i = 0; i < n; ++i)
-            for (int pl = 0; pl < plans[i].nplanes; ++pl)
-                CU(cudaMemcpyAsync(base + plans[i].off_set[SET_C][pl], base + plans[i].off_set[SET_A][pl],
-                                   plans[i].pbytes[pl], cudaMemcpyDeviceToDevice, st));
         if (wl_apply.ctas) {
             { LaunchScope ls_(ctx, "k_lr_apply");
             zf::k_lr_apply<<<wl_apply.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_apply),
@@ -936,7 +958,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         Plan &p = plans[i];
         const zf_frame *f = p.in;
         const bool dev = f->planes_on_device != 0;
-        if (run.stages & (STG_DB_APPLY | STG_CDEF_APPLY | STG_LR_APPLY))
+        if ((run.stages & (STG_DB_APPLY | STG_CDEF_APPLY | STG_LR_APPLY)) && !p.zero_copy)
             for (int pl = 0; pl < p.nplanes; ++pl)
                 TRY(copy_out(ctx, f->rec[pl], base + p.off_set[run.rec_out][pl], p.pbytes[pl], dev));
     }

@@ -903,12 +903,15 @@ __global__ void __launch_bounds__(32) k_lr_finish(FrameDesc *frames, int nframes
 
 // ---------------------------------------------------------------------------
 // 6. Apply (apply_restoration_frame, restoration.rs:992-1052) with the
-// stripe boundaries of save_lr_boundaries: one CTA per (plane, stripe,
-// 64-px column tile), C = filtered, already holding a copy of A. Rows
+// stripe boundaries of save_lr_boundaries, writing every pixel of C: one CTA
+// per (plane, stripe, 64-px column tile) over the aligned canvas. Tiles of
+// Wiener units are filtered within the true plane and copied from A beyond
+// it; every other tile (unit NONE, frame NONE, plane not searched, and the
+// rows below the true plane: stripe index nstripes) is copied from A. Rows
 // above / below a stripe come from the post-deblock (pre-CDEF) plane B at
 // interior stripe edges (the only lines the single-tile apply reads) and
 // from the edge-replicated post-CDEF plane at the frame top / bottom.
-// items: a = unit index, b = stripe << 16 | column tile.
+// items: a = unit index (-1: copy only), b = stripe << 16 | column tile.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems) {
     constexpr int SW = TT_W + 7;
@@ -918,18 +921,31 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
     const WorkItem wi = items[blockIdx.x];
     const FrameDesc &f = frames[wi.frame];
     const LrPlane &pl = f.lr[wi.plane];
-    if (!pl.on || pl.frame_rtype == 0) return;
-    const LrUnit &u = pl.units[wi.a];
-    if (u.rtype != 1) return;
     const int ss = wi.plane ? 1 : 0;
     const int full = 64 >> ss, off = 8 >> ss;
     const int s = wi.b >> 16, ct = wi.b & 0xffff;
-    const int ys = max(0, s * full - off), ye = min(pl.ph, (s + 1) * full - off);
-    const int x0 = ct * TT_W, ncol = min(TT_W, pl.pw - x0);
-    const int nrow = ye - ys;
-    const bool copy_above = s > 0, copy_below = ye < pl.ph;
     const int bd = f.bd, stride = plane_stride(f, wi.plane);
+    const int canvas_h = wi.plane ? f.h / 2 : f.h;
+    const int nstripes = (pl.ph + off + full - 1) / full;
+    // rows of this item: a stripe of the true plane, or the canvas rows below it
+    const int ys = s < nstripes ? max(0, s * full - off) : pl.ph;
+    const int ye = s < nstripes ? min(pl.ph, (s + 1) * full - off) : canvas_h;
+    const int x0 = ct * TT_W, tw = min(TT_W, stride - x0);
     const uint8_t *post = f.A[wi.plane], *pre = f.B[wi.plane];
+    uint8_t *out = f.C[wi.plane];
+    const bool filter = s < nstripes && wi.a >= 0 && pl.on && pl.frame_rtype != 0 && pl.units[wi.a].rtype == 1;
+    // columns copied from A: all of them, or those beyond the true width
+    const int cx = filter ? min(tw, pl.pw - x0) : 0;
+    if (cx < tw)
+        for (int q = threadIdx.x; q < (ye - ys) * (tw - cx); q += blockDim.x) {
+            const int rr = q / (tw - cx), cc = cx + (q - rr * (tw - cx));
+            const int64_t o = (int64_t)(ys + rr) * stride + x0 + cc;
+            stpx(out, o, bd, ldpx(post, o, bd));
+        }
+    if (!filter) return;
+    const LrUnit &u = pl.units[wi.a];
+    const int ncol = cx, nrow = ye - ys;
+    const bool copy_above = s > 0, copy_below = ye < pl.ph;
     const int rows = nrow + 7;
     for (int q = threadIdx.x; q < rows * SW; q += blockDim.x) {
         const int rr = q / SW, cc = q - rr * SW;
@@ -971,7 +987,7 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
         int tp[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) tp[k] = tmp[(rr + k) * TT_W + cc];
-        stpx(f.C[wi.plane], (int64_t)(ys + rr) * stride + x0 + cc, bd, wiener_v(tp, u.vf, bd));
+        stpx(out, (int64_t)(ys + rr) * stride + x0 + cc, bd, wiener_v(tp, u.vf, bd));
     }
 }
 
