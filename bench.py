@@ -466,6 +466,14 @@ def run_batched(args, ctx, stream, dev, frames):
     for i in range(n):
         decs[i].c = darr[i]
     dec_batch = [d.as_dict() for d in decs]
+    # per-kernel device time of one batch (CUDA events per launch)
+    restore()
+    ctx.profile(True)
+    ctx.profile_reset()
+    batch()
+    ctx.sync()
+    b_kernels = {k: round(v[1], 4) for k, v in sorted(ctx.profile_read().items(), key=lambda kv: -kv[1][1])}
+    ctx.profile(False)
     restore()
     plain()
     p_ms = timed(plain, max(2, args.steps // 2))
@@ -506,7 +514,7 @@ def run_batched(args, ctx, stream, dev, frames):
     return {"workload": "256 images, W,H ~ U[64,2048] (~20% odd), 70% 8-bit / 30% 10-bit, qp ~ U[20,50], preset 6",
             "images": n, "luma_mpix": round(px / 1e6, 3),
             "batched_mpix_per_s": round(px / (b_ms / 1e3) / 1e6, 3), "batched_ms": round(b_ms, 3),
-            "launches_per_batch": int(b_launches),
+            "launches_per_batch": int(b_launches), "kernel_ms": b_kernels,
             "plain_mpix_per_s": round(px / (p_ms / 1e3) / 1e6, 3), "plain_ms": round(p_ms, 3),
             "batched_over_plain": round(p_ms / b_ms, 3),
             "batched_e2e_mpix_per_s": round(px / (e_ms / 1e3) / 1e6, 3),

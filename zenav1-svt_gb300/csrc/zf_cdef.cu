@@ -177,10 +177,11 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v
 
 // constrain with the damping shift precomputed: shift = max(0, damping -
 // msb(threshold)) (cdef.rs:113-120); threshold 0 gives 0 for any shift.
+// sign(d) * min(|d|, m) with m = max(0, thr - (|d| >> shift)) >= 0 is d
+// clamped to [-m, m].
 __device__ __forceinline__ int constrain_s(int d, int thr, int shift) {
-    const int a = abs(d);
-    const int v = min(a, max(0, thr - (a >> shift)));
-    return d < 0 ? -v : v;
+    const int m = max(0, thr - (abs(d) >> shift));
+    return min(max(d, -m), m);
 }
 __device__ __forceinline__ int damp_shift(int thr, int damping) {
     return thr ? max(0, damping - msb((unsigned)thr)) : 0;
@@ -202,6 +203,9 @@ __device__ __forceinline__ void dir_offsets(int dir, int rs, int *o) {
 // all taps, max over x and the taps that are not the sentinel.
 // d[0..3]: primary +k0, -k0, +k1, -k1; d[4..7]: secondary k0 (+2, -2, +6,
 // -6); d[8..11]: secondary k1.
+// EDGE = false: the region holds no sentinel (the filter block and its
+// 2-pixel reach lie inside the canvas), so the max needs no test.
+template <bool EDGE = true>
 __device__ __forceinline__ void load_taps(const uint16_t *reg, int pos, const int *o, int x, int *d, int &mx,
                                           int &mn) {
     mx = x;
@@ -214,10 +218,18 @@ __device__ __forceinline__ void load_taps(const uint16_t *reg, int pos, const in
     for (int t = 0; t < 12; ++t) {
         const uint16_t r = reg[q[t]];
         const int v = (int16_t)r;
-        if (r != kVeryLarge) mx = max(mx, v);
+        if (!EDGE || r != kVeryLarge) mx = max(mx, v);
         mn = min(mn, v);
         d[t] = v - x;
     }
+}
+
+// load_taps with the sentinel test only where the region can hold one
+// (a CTA-uniform branch).
+__device__ __forceinline__ void load_taps_at(bool edge, const uint16_t *reg, int pos, const int *o, int x, int *d,
+                                             int &mx, int &mn) {
+    if (edge) load_taps<true>(reg, pos, o, x, d, mx, mn);
+    else load_taps<false>(reg, pos, o, x, d, mx, mn);
 }
 
 // Primary and secondary parts of the tap sum. The reference sums in
@@ -324,6 +336,9 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
     const int sub = cp.sub_y;
     const int lgs = 6 - (__ffs(sub) - 1);  // sampled slots per 8x8 block: 64 / sub
     const int slots = nblk << lgs;
+    // the 2-pixel reach of the filter block inside the canvas: no sentinel
+    const bool edge_y = !(x0 >= 2 && y0 >= 2 && x0 + 66 <= f.w && y0 + 66 <= f.h);
+    const bool edge_uv = !(x0 >= 4 && y0 >= 4 && x0 / 2 + 34 <= f.w / 2 && y0 / 2 + 34 <= f.h / 2);
     uint32_t acc[NCM];
 #pragma unroll
     for (int c = 0; c < NCM; ++c) acc[c] = 0;
@@ -335,7 +350,7 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
         const int x = (int16_t)reg[pos], sv = src[py * 64 + px];
         int d[12], mx, mn, S[NSM];
         {  // block direction: candidates with p_i != 0
-            load_taps(reg, pos, boff[b], x, d, mx, mn);
+            load_taps_at(edge_y, reg, pos, boff[b], x, d, mx, mn);
             S[0] = 0;
 #pragma unroll
             for (int j = 1; j < NSM; ++j) S[j] = j < ns ? sec_sum(d, sec[j], ssh[j]) : 0;
@@ -354,7 +369,7 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
         }
         if (any_zero) {  // direction 0: candidates with p_i == 0
             const int o0[6] = {-1 * CR + 1, -2 * CR + 2, 0 * CR + 1, 0 * CR + 2, 1 * CR + 0, 2 * CR + 0};
-            load_taps(reg, pos, o0, x, d, mx, mn);
+            load_taps_at(edge_y, reg, pos, o0, x, d, mx, mn);
 #pragma unroll
             for (int j = 1; j < NSM; ++j) S[j] = j < ns ? sec_sum(d, sec[j], ssh[j]) : 0;
 #pragma unroll
@@ -418,7 +433,7 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
             const int pos = (py + 2) * CRC + px + 2;
             const int x = (int16_t)reg[pos], sv = src[py * 32 + px];
             int d[12], mx, mn;
-            load_taps(reg, pos, boffc[b], x, d, mx, mn);
+            load_taps_at(edge_uv, reg, pos, boffc[b], x, d, mx, mn);
 #pragma unroll
             for (int i = 0; i < FPM; ++i) {
                 if (i >= fp) continue;
@@ -772,6 +787,8 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     }
     __syncthreads();
     unsigned long long filt = 0, changed = 0;
+    const bool edge_y = !(x0 >= 2 && y0 >= 2 && x0 + 66 <= f.w && y0 + 66 <= f.h);
+    const bool edge_uv = !(x0 >= 4 && y0 >= 4 && x0 / 2 + 34 <= f.w / 2 && y0 / 2 + 34 <= f.h / 2);
     const bool zero_y = lvl_y == 0 && sec_y == 0;
     const int ssh_y = damp_shift(sec_y, damping);
     for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
@@ -785,7 +802,7 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
             const int tp = bt[b], t = tp & 0xffff;
             if (!(t == 0 && sec_y == 0)) {  // cdef.rs:444-448
                 int d[12], mx, mn;
-                load_taps(reg, pos, boff[b], x, d, mx, mn);
+                load_taps_at(edge_y, reg, pos, boff[b], x, d, mx, mn);
                 y = cdef_round(x, prim_sum(d, t, tp >> 16, cs) + sec_sum(d, sec_y, ssh_y), mn, mx);
                 filt += 1;
                 changed += y != x;
@@ -810,7 +827,7 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
                 int y = x;
                 if (!zero_uv && ((dl >> b) & 1)) {
                     int d[12], mx, mn;
-                    load_taps(reg, pos, boffc[b], x, d, mx, mn);
+                    load_taps_at(edge_uv, reg, pos, boffc[b], x, d, mx, mn);
                     y = cdef_round(x, prim_sum(d, lvl_uv, psh, cs) + sec_sum(d, sec_uv, ssh), mn, mx);
                     filt += 1;
                     changed += y != x;

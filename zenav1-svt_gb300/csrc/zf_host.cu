@@ -932,13 +932,17 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             }
         }
         { LaunchScope ls_(ctx, "k_lr_finish");
-        int max_units = 1;
+        // dynamic shared memory: 32 B per unit, plus the (unit, reference)
+        // pair table of planes with at most 200 units
+        size_t smem = 32;
         for (auto &p : plans)
-            for (int pl = 0; pl < 3; ++pl) max_units = std::max(max_units, p.hunits[pl] * p.vunits[pl]);
-        const int smem = max_units * 32;
+            for (int pl = 0; pl < 3; ++pl) {
+                const size_t nu = (size_t)p.hunits[pl] * p.vunits[pl], np = nu * (nu + 1) / 2;
+                smem = std::max(smem, nu * 32 + (np <= (size_t)zf::kLrPairMaxHost ? np * 4 : 0));
+            }
         if (smem > 48 * 1024)
-            CU(cudaFuncSetAttribute(zf::k_lr_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        zf::k_lr_finish<<<n * 3, 32, smem, st>>>(d_desc, n); }
+            CU(cudaFuncSetAttribute(zf::k_lr_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        zf::k_lr_finish<<<n * 3, zf::kLrFinThreadsHost, smem, st>>>(d_desc, n); }
         TRY(launch_check(ctx, "k_lr_finish"));
         TRY(check_cancel(ctx));
     }

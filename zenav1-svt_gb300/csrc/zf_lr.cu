@@ -790,7 +790,9 @@ __device__ int count_wiener_bits(int win, const int16_t *vf, const int16_t *hf, 
     return bits;
 }
 __device__ __forceinline__ double rdcost_dbl(int64_t rdmult, int64_t rate, int64_t dist) {
-    return __dadd_rn(__ddiv_rn(__dmul_rn((double)rate, (double)rdmult), 512.0), __dmul_rn((double)dist, 128.0));
+    // the reference divides by 512.0: scaling by 2^-9 is exact, so the
+    // multiplication gives the same double
+    return __dadd_rn(__dmul_rn(__dmul_rn((double)rate, (double)rdmult), 1.0 / 512.0), __dmul_rn((double)dist, 128.0));
 }
 
 // Per-unit RD inputs staged in shared memory (count_wiener_bits reads taps
@@ -815,24 +817,47 @@ __device__ int count_bits3(int win, const int16_t *v, const int16_t *h, const in
     return bits;
 }
 
-// One warp per (frame, plane): lanes stage the unit data, lane 0 walks the
-// units in order with the reference-filter chain, lanes write the picks.
-__global__ void __launch_bounds__(32) k_lr_finish(FrameDesc *frames, int nframes) {
+// Frame RD of one (frame, plane) per CTA (search_restoration_still,
+// restoration.rs:838-924). The unit walk is sequential only through the
+// reference filter of count_wiener_bits: the last unit chosen WIENER (or the
+// default taps). So every (unit k, reference j) pair -- j = -1 for the
+// default, else a unit before k -- is evaluated in parallel first: the bits
+// of k's taps against j's taps and whether WIENER beats NONE for k under
+// that reference. The walk then only looks pairs up. Planes with more units
+// than the pair table holds walk with the full evaluation per unit.
+constexpr int kLrFinThreads = 256;
+constexpr int kLrPairMax = 20100;  // units <= 200 (pair table of int32 in shared memory)
+
+__device__ __forceinline__ void unit_rd(const FrameDesc &f, const LrPlane &pl, const RdUnit &u,
+                                        const int16_t *rv, const int16_t *rh, int64_t &bits_wn, bool &pick) {
+    const int64_t cnt = count_bits3(pl.win, u.v, u.h, rv, rh);
+    bits_wn = 320 + (cnt << 9);
+    const int64_t bits_none = 768;
+    const double cn = rdcost_dbl(f.rdmult, bits_none >> 4, u.sse_none);
+    const double cw = rdcost_dbl(f.rdmult, bits_wn >> 4, u.sse_wn);
+    pick = cw < cn;
+}
+
+__global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, int nframes) {
     extern __shared__ unsigned char lr_dyn[];
-    RdUnit *U = reinterpret_cast<RdUnit *>(lr_dyn);
     __shared__ int frame_rtype;
+    __shared__ int64_t red[kLrFinThreads / 32];
     const int id = blockIdx.x;
     if (id >= nframes * 3) return;
     FrameDesc &f = frames[id / 3];
     LrPlane &pl = f.lr[id % 3];
-    const int lane = threadIdx.x;
+    const int t = threadIdx.x;
     if (!pl.on) {
-        if (lane == 0) pl.frame_rtype = 0;
+        if (t == 0) pl.frame_rtype = 0;
         return;
     }
     const int n = pl.hunits * pl.vunits;
+    const int npairs = n * (n + 1) / 2;
+    const bool table = npairs <= kLrPairMax;
+    RdUnit *U = reinterpret_cast<RdUnit *>(lr_dyn);
+    int32_t *PT = reinterpret_cast<int32_t *>(lr_dyn + (size_t)n * sizeof(RdUnit));
     int64_t part = 0;
-    for (int k = lane; k < n; k += 32) {
+    for (int k = t; k < n; k += blockDim.x) {
         const LrUnit &u = pl.units[k];
         RdUnit r;
         r.sse_none = u.sse_none;
@@ -853,11 +878,36 @@ __global__ void __launch_bounds__(32) k_lr_finish(FrameDesc *frames, int nframes
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
-    __syncwarp();
-    if (lane == 0) {
-        const double cost_none_frame = rdcost_dbl(f.rdmult, 0, part);
+    if ((t & 31) == 0) red[t >> 5] = part;
+    __syncthreads();
+    if (table) {
+        // pair (k, j), j in [-1, k): index k (k + 1) / 2 + j + 1; entry =
+        // bits_wn | pick << 30 (bits_wn < 2^16)
+        const int16_t dflt[3] = {3, -7, 15};
+        for (int idx = t; idx < npairs; idx += blockDim.x) {
+            int k = (int)((sqrtf(8.0f * (float)idx + 1.0f) - 1.0f) * 0.5f);
+            while (k * (k + 1) / 2 > idx) --k;
+            while ((k + 1) * (k + 2) / 2 <= idx) ++k;
+            const int j = idx - k * (k + 1) / 2 - 1;
+            const RdUnit &u = U[k];
+            if (u.sse_wn == INT64_MAX) {
+                PT[idx] = 0;
+                continue;
+            }
+            int64_t bw;
+            bool pk;
+            unit_rd(f, pl, u, j < 0 ? dflt : U[j].v, j < 0 ? dflt : U[j].h, bw, pk);
+            PT[idx] = (int32_t)bw | (pk ? 1 << 30 : 0);
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        int64_t total = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += red[w];
+        const double cost_none_frame = rdcost_dbl(f.rdmult, 0, total);
         int64_t bits_frame = 0, sse_frame = 0;
         int16_t rv[3] = {3, -7, 15}, rh[3] = {3, -7, 15};
+        int last = -1;
         for (int k = 0; k < n; ++k) {
             RdUnit &u = U[k];
             if (u.sse_wn == INT64_MAX) {
@@ -865,20 +915,26 @@ __global__ void __launch_bounds__(32) k_lr_finish(FrameDesc *frames, int nframes
                 sse_frame += u.sse_none;
                 continue;
             }
-            const int64_t cnt = count_bits3(pl.win, u.v, u.h, rv, rh);
-            const int64_t bits_wn = 320 + (cnt << 9), bits_none = 768;
-            const double cn = rdcost_dbl(f.rdmult, bits_none >> 4, u.sse_none);
-            const double cw = rdcost_dbl(f.rdmult, bits_wn >> 4, u.sse_wn);
-            if (cw < cn) {
+            int64_t bits_wn;
+            bool pick;
+            if (table) {
+                const int32_t e = PT[k * (k + 1) / 2 + last + 1];
+                bits_wn = e & 0xffff;
+                pick = (e >> 30) & 1;
+            } else {
+                unit_rd(f, pl, u, rv, rh, bits_wn, pick);
+            }
+            if (pick) {
                 u.pick = 1;
                 bits_frame += bits_wn;
                 sse_frame += u.sse_wn;
+                last = k;
                 for (int i = 0; i < 3; ++i) {
                     rv[i] = u.v[i];
                     rh[i] = u.h[i];
                 }
             } else {
-                bits_frame += bits_none;
+                bits_frame += 768;
                 sse_frame += u.sse_none;
             }
         }
@@ -886,8 +942,8 @@ __global__ void __launch_bounds__(32) k_lr_finish(FrameDesc *frames, int nframes
         frame_rtype = cost_wn_frame < cost_none_frame ? 1 : 0;
         pl.frame_rtype = frame_rtype;
     }
-    __syncwarp();
-    for (int k = lane; k < n; k += 32) {
+    __syncthreads();
+    for (int k = t; k < n; k += blockDim.x) {
         const int rt = frame_rtype ? U[k].pick : 0;
         pl.units[k].rtype = rt;
         PackedUnit o;
