@@ -608,8 +608,7 @@ def run_profile(args):
     ge.build()
     pkg = ge._pkg()
     from zenav1_svt_gb300 import abi, synth
-    frames = [synth.make_frame(synth.frame_seed(2, 100 + i), args.pw, args.ph, 8, qp, preset, "power")
-              for i, (preset, qp) in enumerate(WORKLOAD[:args.nframes])]
+    frames = make_workload(args.pw, args.ph)[:args.nframes]  # the timed frames (same seeds)
     ctx = pkg.Context(0)
     dev = torch.device("cuda", 0)
     keep, structs, pairs = [], [], []
