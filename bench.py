@@ -539,7 +539,10 @@ def run_served(args, device, frames):
         src = [torch.from_numpy(p).pin_memory().numpy() for p in f.src]
         pool.append({"f": f, "src": src, "rec0": f.rec, "mi": pkg.pack_geom(f.geom), "slots": []})
     executors = [serve.FilterExecutor(device) for _ in range(3)]
-    srv = serve.Server(executors, hbm_budget_bytes=120 << 30, max_batch=64, max_batch_px=48 << 20)
+    # every worker's arena sized up front for a full batch (48 MP at 10 bits
+    # needs < 1 GB), so no arena grows while requests are timed
+    srv = serve.Server(executors, hbm_budget_bytes=120 << 30, max_batch=64, max_batch_px=48 << 20,
+                       reserve_bytes=3 << 29)
     for e in pool:
         r = serve.Request(e["f"], mi=e["mi"])
         e["fp"] = executors[0].footprint(r)
@@ -591,7 +594,8 @@ def run_served(args, device, frames):
     return {"workload": ("Poisson arrivals, sizes log-uniform 128^2..6000x4000, 80% 8-bit / 20% 10-bit, "
                          "qp ~ U[18,45], preset 6; requests cycle a pool of {} images").format(len(pool)),
             "seconds_per_rate": args.served_seconds, "workers": 3, "hbm_budget_gb": 120,
-            "peak_reserved_gb": round(srv.peak_reserved / 2 ** 30, 3), "rates": out}
+            "peak_reserved_gb": round(srv.peak_reserved / 2 ** 30, 3), "arena_grows": srv.arena_grows,
+            "rates": out}
 
 
 def _peaks():

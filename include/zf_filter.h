@@ -152,6 +152,11 @@ uint64_t zf_device_bytes(const zf_ctx *ctx);
 /* Release the context's arena (after synchronising its stream); the next
  * call allocates again. No counterpart in the reference. */
 int32_t zf_trim(zf_ctx *ctx);
+/* Grow the arena to at least device_bytes and each pinned host staging
+ * buffer (metadata up, decisions down) to at least host_bytes now, so that
+ * later calls up to that size allocate nothing (allocation and release
+ * synchronise the device). No counterpart in the reference. */
+int32_t zf_reserve(zf_ctx *ctx, uint64_t device_bytes, uint64_t host_bytes);
 
 /* Output array sizes for a frame (filter blocks, restoration units). */
 int32_t zf_query_sizes(const zf_frame *f, zf_sizes *out);

@@ -76,6 +76,8 @@ def lib():
     L.zf_device_bytes.restype = C.c_uint64
     L.zf_trim.argtypes = [C.c_void_p]
     L.zf_trim.restype = C.c_int32
+    L.zf_reserve.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64]
+    L.zf_reserve.restype = C.c_int32
     L.zf_profile_enable.argtypes = [C.c_void_p, C.c_int32]
     L.zf_profile_reset.argtypes = [C.c_void_p]
     L.zf_profile_reset.restype = None
@@ -153,6 +155,10 @@ class Context:
     def trim(self):
         """Release the arena (the next call allocates again)."""
         self._check(lib().zf_trim(self.h))
+
+    def reserve(self, device_bytes, host_bytes=8 << 20):
+        """Grow the arena and the pinned staging buffers ahead of time."""
+        self._check(lib().zf_reserve(self.h, int(device_bytes), int(host_bytes)))
 
     def profile(self, enable=True):
         self._check(lib().zf_profile_enable(self.h, 1 if enable else 0))

@@ -10,6 +10,8 @@
 // canvas. Here a CTA owns one 64x64 filter block and stages exactly that
 // (plus the 2-pixel reach of the taps) in shared memory, so every pixel of
 // every candidate reads the same values as the reference's build_src.
+#include <algorithm>
+
 #include <cooperative_groups.h>
 
 #include "zf_dev.cuh"
@@ -723,6 +725,211 @@ __global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThread
             cp.uv_str[gi] = gi < bnb ? (uint8_t)cp.fs[blev[8 + gi]] : 0;
         }
     }
+}
+
+// The same joint search with one 1024-thread CTA per (frame, bit count),
+// for frames whose rows fit in one CTA's shared memory: no cluster
+// barriers, rows padded to a multiple of 4 (zero rows add 0) and read as
+// uint4. A step: the best of the fixed strengths per row into shared
+// memory; then warps take (pair, row chunk) tasks -- four rows per lane per
+// load, summed in u32 (each min < 2^30, four < 2^32) into a u64 -- and
+// write per-task partials; warp 0 adds the chunks of each pair and takes the
+// argmin (strict <, lowest pair index on ties). The last CTA of a frame
+// picks the bit count as the cluster form does.
+constexpr int kFin1Threads = 1024;
+constexpr int kFin1Warps = kFin1Threads / 32;
+
+__global__ void __launch_bounds__(kFin1Threads, 1) k_cdef_finish1(FrameDesc *frames, const int *frame_ids) {
+    extern __shared__ __align__(16) unsigned char fin1_dyn[];
+    __shared__ int scan[kFin1Threads];
+    __shared__ uint8_t lev[2][16];
+    __shared__ unsigned long long res_v;
+    __shared__ int last_flag, best_bits;
+    const int level = blockIdx.x % kFinLevels;
+    FrameDesc &f = frames[frame_ids[blockIdx.x / kFinLevels]];
+    CdefParams &cp = f.cdef;
+    if (cp.mode != 1) return;
+    const int nfb = f.nhfb * f.nvfb, n_cand = cp.ncand, n2 = 2 * n_cand, npairs = n_cand * n_cand;
+    const int T = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int chunk = (nfb + T - 1) / T;
+    const int c0 = min(nfb, t * chunk), c1 = min(nfb, t * chunk + chunk);
+    int cnt = 0;
+    for (int fb = c0; fb < c1; ++fb) cnt += f.fb_row[fb];
+    scan[t] = cnt;
+    __syncthreads();
+    for (int o = 1; o < T; o <<= 1) {
+        const int v = t >= o ? scan[t - o] : 0;
+        __syncthreads();
+        scan[t] += v;
+        __syncthreads();
+    }
+    const int sb = scan[T - 1];
+    if (sb == 0) {  // every filter block all-skip: cdef.rs:282-288
+        if (level == 0) {
+            for (int fb = t; fb < nfb; fb += T) f.fb_idx[fb] = 0;
+            if (t == 0) {
+                cp.bits = 0;
+                cp.y_str[0] = 0;
+                cp.uv_str[0] = 0;
+            }
+        }
+        return;
+    }
+    const int nq = (sb + 3) >> 2, s4 = nq * 4;  // rows padded to a multiple of 4
+    const int C = max(1, (4 * kFin1Warps + npairs - 1) / npairs);  // row chunks per pair
+    const int ntasks = npairs * C;
+    uint32_t *R = reinterpret_cast<uint32_t *>(fin1_dyn);  // R[k * s4 + s]
+    uint32_t *best = R + (size_t)n2 * s4;
+    unsigned long long *part = reinterpret_cast<unsigned long long *>(best + s4);
+    int *ids = reinterpret_cast<int *>(part + ntasks);
+    {
+        int pos = scan[t] - cnt;
+        for (int fb = c0; fb < c1; ++fb)
+            if (f.fb_row[fb]) ids[pos++] = fb;
+    }
+    __syncthreads();
+    for (int q = t; q < n2 * s4; q += T) {
+        const int k = q / s4, s = q - k * s4;
+        R[q] = s < sb ? (uint32_t)f.mse[(int64_t)ids[s] * n2 + k] : 0u;
+    }
+    if (t < 16) lev[0][t] = lev[1][t] = 0;
+    __syncthreads();
+    const uint4 *R4 = reinterpret_cast<const uint4 *>(R);
+    uint4 *best4 = reinterpret_cast<uint4 *>(best);
+
+    auto step = [&](int nbs) -> unsigned long long {
+        for (int q = t; q < nq; q += T) {
+            uint4 b = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+            for (int gi = 0; gi < nbs; ++gi) {
+                const uint4 a = R4[(size_t)lev[0][gi] * nq + q], c = R4[(size_t)(n_cand + lev[1][gi]) * nq + q];
+                b.x = min(b.x, a.x + c.x);
+                b.y = min(b.y, a.y + c.y);
+                b.z = min(b.z, a.z + c.z);
+                b.w = min(b.w, a.w + c.w);
+            }
+            best4[q] = b;
+        }
+        __syncthreads();
+        for (int task = warp; task < ntasks; task += kFin1Warps) {
+            const int p = task / C, c = task - p * C;
+            const int j = p / n_cand, k = p - j * n_cand;
+            const uint4 *rj = R4 + (size_t)j * nq, *rk = R4 + (size_t)(n_cand + k) * nq;
+            const int q0 = (int)((int64_t)nq * c / C), q1 = (int)((int64_t)nq * (c + 1) / C);
+            unsigned long long acc = 0;
+            for (int q = q0 + lane; q < q1; q += 32) {
+                const uint4 a = rj[q], b = rk[q], m = best4[q];
+                acc += (unsigned long long)(min(a.x + b.x, m.x) + min(a.y + b.y, m.y) + min(a.z + b.z, m.z) +
+                                            min(a.w + b.w, m.w));
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+            if (lane == 0) part[task] = acc;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long bv = ~0ull;
+            int bi = 0x7fffffff;
+            for (int p = lane; p < npairs; p += 32) {
+                unsigned long long v = 0;
+                for (int c = 0; c < C; ++c) v += part[p * C + c];
+                if (v < bv) {
+                    bv = v;
+                    bi = p;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov < bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (bv >= (1ull << 63)) {  // best_tot starts at 1 << 63 with strict <
+                bi = 0;
+                bv = 1ull << 63;
+            }
+            if (lane == 0) {
+                lev[0][nbs] = (uint8_t)(bi / n_cand);
+                lev[1][nbs] = (uint8_t)(bi % n_cand);
+                res_v = bv;
+            }
+        }
+        __syncthreads();
+        return res_v;
+    };
+
+    const int nb = 1 << level;
+    unsigned long long tt = 1ull << 63;
+    for (int s = 0; s < nb; ++s) tt = step(s);
+    for (int r = 0; r < 4 * nb; ++r) {
+        if (t == 0)
+            for (int j = 0; j < nb - 1; ++j) {
+                lev[0][j] = lev[0][j + 1];
+                lev[1][j] = lev[1][j + 1];
+            }
+        __syncthreads();
+        tt = step(nb - 1);
+    }
+    if (t == 0) {
+        const unsigned long long total_bits = (unsigned long long)sb * level + nb * 12;
+        f.fin_cost[level] = rdc(cp.lambda, total_bits << 9, tt * 16);
+        for (int k = 0; k < 8; ++k) {
+            f.fin_lev[level][k] = k < nb ? lev[0][k] : 0;
+            f.fin_lev[level][8 + k] = k < nb ? lev[1][k] : 0;
+        }
+        __threadfence();
+        last_flag = atomicAdd(&f.fin_done, 1) == kFinLevels - 1;
+    }
+    __syncthreads();
+    if (!last_flag) return;
+    __threadfence();
+    if (t == 0) {
+        unsigned long long best_cost = 1ull << 63;
+        int bb = 0;
+        for (int i = 0; i < kFinLevels; ++i) {
+            const unsigned long long c = __ldcg(&f.fin_cost[i]);
+            if (c < best_cost) {
+                best_cost = c;
+                bb = i;
+            }
+        }
+        best_bits = bb;
+        for (int k = 0; k < 16; ++k) lev[k >> 3][k & 7] = *(volatile uint8_t *)&f.fin_lev[bb][k];
+    }
+    __syncthreads();
+    const int bnb = 1 << best_bits;
+    for (int fb = t; fb < nfb; fb += T) f.fb_idx[fb] = 0;
+    __syncthreads();
+    for (int s = t; s < sb; s += T) {
+        int best_gi = 0;
+        unsigned long long bst = ~0ull;
+        for (int gi = 0; gi < bnb; ++gi) {
+            const unsigned long long c =
+                (unsigned long long)R[(size_t)lev[0][gi] * s4 + s] + R[(size_t)(n_cand + lev[1][gi]) * s4 + s];
+            if (c < bst) {
+                bst = c;
+                best_gi = gi;
+            }
+        }
+        f.fb_idx[ids[s]] = (uint8_t)best_gi;
+    }
+    if (t == 0) {
+        cp.bits = best_bits;
+        for (int gi = 0; gi < 8; ++gi) {
+            cp.y_str[gi] = gi < bnb ? (uint8_t)cp.fs[lev[0][gi]] : 0;
+            cp.uv_str[gi] = gi < bnb ? (uint8_t)cp.fs[lev[1][gi]] : 0;
+        }
+    }
+}
+
+// Shared memory k_cdef_finish1 needs for a frame (0 when it does not fit).
+int finish1_smem(int nfb, int ncand, int cap) {
+    const int64_t s4 = ((int64_t)nfb + 3) / 4 * 4, n2 = 2 * ncand, npairs = (int64_t)ncand * ncand;
+    const int64_t C = std::max<int64_t>(1, (4 * kFin1Warps + npairs - 1) / npairs);
+    const int64_t bytes = (n2 * s4 + s4) * 4 + npairs * C * 8 + (int64_t)nfb * 4;
+    return bytes <= cap ? (int)bytes : 0;
 }
 
 // ---- apply: one CTA per filter block, B (post-deblock) -> A -----------

@@ -347,8 +347,11 @@ struct Plan {
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) & ~(a - 1); }
 
-// Dynamic shared memory opted in for k_cdef_finish's compacted rows.
+// Dynamic shared memory opted in for k_cdef_finish's compacted rows, and
+// for the single-CTA form's rows, best column and partials.
 constexpr size_t kFinishSmemCap = 160 * 1024;
+constexpr int kFinish1SmemCap = 200 * 1024;
+constexpr int kFinish1MaxFb = 1024;  // filter blocks (a 2048x2048 frame)
 
 int validate_frame(zf_ctx *ctx, const zf_frame *f) {
     if (!f) return fail(ctx, ZF_ERR_ARG, "frame is NULL");
@@ -560,7 +563,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     }
     // Work lists (host-known shapes).
     WorkList wl_db, wl_cs, wl_ca, wl_sum, wl_st5, wl_st7, wl_unit, wl_apply, wl_trial, wl_tiles;
-    std::vector<int> cdef_frames;
+    std::vector<int> cdef_small, cdef_large;  // joint search: one CTA / cluster per bit count
     for (int i = 0; i < n; ++i) {
         Plan &p = plans[i];
         for (int pl = 0; pl < p.nplanes; ++pl) {
@@ -569,7 +572,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         }
         if (p.d.cdef.mode == 1 && !run.cdef_given) {
             wl_cs.add(i, 0, 0, 0, p.nfb);
-            cdef_frames.push_back(i);
+            const bool small = p.nfb <= kFinish1MaxFb &&
+                               zf::finish1_smem(p.nfb, p.d.cdef.ncand, kFinish1SmemCap) > 0;
+            (small ? cdef_small : cdef_large).push_back(i);
         }
         wl_ca.add(i, 0, 0, 0, p.nfb);
         for (int pl = 0; pl < 3; ++pl) {
@@ -621,6 +626,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 for (int t = 0; t < ntiles; ++t) wl_apply.add(i, pl, -1, (nstripes << 16) | t, 1);
         }
     }
+    std::vector<int> cdef_frames(cdef_small);
+    cdef_frames.insert(cdef_frames.end(), cdef_large.begin(), cdef_large.end());
+    const int n_small = (int)cdef_small.size();
     // Arena: per-frame buffers | unit accumulators | metadata image |
     // deblock search scratch | outputs.
     const size_t o_units = align_up(cursor, 256);
@@ -869,21 +877,40 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         CU(zf::launch_cdef_search(fp, ns, wl_cs.ctas, st, d_desc, (const WorkItem *)(base + o_cs),
                                   (int)wl_cs.items.size())); }
         TRY(launch_check(ctx, "k_cdef_search"));
-        { LaunchScope ls_(ctx, "k_cdef_finish");
-        // dynamic shared memory: the double-buffered pair partials (always)
-        // and the compacted rows of the largest frame of the batch, capped
-        // (frames whose rows do not fit use global scratch)
-        size_t want = 0, pairs = 0;
-        for (int fi : cdef_frames) {
-            const size_t nc = (size_t)plans[fi].d.cdef.ncand;
-            pairs = std::max(pairs, 2 * nc * nc * 8);
-            want = std::max(want, 2 * nc * nc * 8 + ((size_t)plans[fi].nfb + zf::kFinClusterHost - 1) /
-                                                         zf::kFinClusterHost * (2 * nc + 1) * 4);
+        // Joint search: frames of up to kFinish1MaxFb filter blocks whose rows
+        // fit one CTA's shared memory run one CTA per (frame, bit count);
+        // larger frames an 8-CTA cluster per (frame, bit count), which wins
+        // once the per-step row sums outweigh the cluster barrier.
+        // (cdef_frames lists the small frames first, n_small of them)
+        int smem1 = 0;
+        for (int k = 0; k < n_small; ++k) {
+            const Plan &pf = plans[cdef_frames[k]];
+            smem1 = std::max(smem1, zf::finish1_smem(pf.nfb, pf.d.cdef.ncand, kFinish1SmemCap));
         }
-        const int smem = (int)std::max(pairs, std::min<size_t>(want, kFinishSmemCap));
-        CU(cudaFuncSetAttribute(zf::k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinishSmemCap));
-        zf::k_cdef_finish<<<(int)cdef_frames.size() * zf::kFinClusterHost * zf::kFinLevels, zf::kFinThreadsHost,
-                            smem, st>>>(d_desc, (const int *)(base + o_cf), smem); }
+        const std::vector<int> small_f(cdef_frames.begin(), cdef_frames.begin() + n_small),
+            large_f(cdef_frames.begin() + n_small, cdef_frames.end());
+        { LaunchScope ls_(ctx, "k_cdef_finish");
+        if (!small_f.empty()) {
+            CU(cudaFuncSetAttribute(zf::k_cdef_finish1, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinish1SmemCap));
+            zf::k_cdef_finish1<<<(int)small_f.size() * zf::kFinLevels, zf::kFin1ThreadsHost, smem1, st>>>(
+                d_desc, (const int *)(base + o_cf));
+        }
+        if (!large_f.empty()) {
+            // dynamic shared memory: the double-buffered pair partials (always)
+            // and the compacted rows of the largest frame, capped (frames whose
+            // rows do not fit use global scratch)
+            size_t want = 0, pairs = 0;
+            for (int fi : large_f) {
+                const size_t nc = (size_t)plans[fi].d.cdef.ncand;
+                pairs = std::max(pairs, 2 * nc * nc * 8);
+                want = std::max(want, 2 * nc * nc * 8 + ((size_t)plans[fi].nfb + zf::kFinClusterHost - 1) /
+                                                             zf::kFinClusterHost * (2 * nc + 1) * 4);
+            }
+            const int smem = (int)std::max(pairs, std::min<size_t>(want, kFinishSmemCap));
+            CU(cudaFuncSetAttribute(zf::k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinishSmemCap));
+            zf::k_cdef_finish<<<(int)large_f.size() * zf::kFinClusterHost * zf::kFinLevels, zf::kFinThreadsHost,
+                                smem, st>>>(d_desc, (const int *)(base + o_cf) + small_f.size(), smem);
+        } }
         TRY(launch_check(ctx, "k_cdef_finish"));
         TRY(check_cancel(ctx));
     }
@@ -1107,6 +1134,15 @@ int32_t zf_trim(zf_ctx *ctx) {
         ctx->arena = nullptr;
         ctx->arena_cap = 0;
     }
+    return ZF_OK;
+}
+
+int32_t zf_reserve(zf_ctx *ctx, uint64_t device_bytes, uint64_t host_bytes) {
+    if (!ctx) return ZF_ERR_ARG;
+    CU(cudaSetDevice(ctx->device));
+    TRY(ensure_arena(ctx, (size_t)device_bytes));
+    TRY(ensure_host(ctx, ctx->h_meta, ctx->h_meta_cap, (size_t)host_bytes));
+    TRY(ensure_host(ctx, ctx->h_out, ctx->h_out_cap, (size_t)host_bytes));
     return ZF_OK;
 }
 

@@ -15,6 +15,10 @@ __global__ void k_deblock_sse(const FrameDesc *frames, const WorkItem *items, in
 cudaError_t launch_cdef_search(int fp, int ns, int ctas, cudaStream_t st, const FrameDesc *frames,
                                const WorkItem *items, int nitems);
 __global__ void k_cdef_finish(FrameDesc *frames, const int *frame_ids, int smem_bytes);
+__global__ void k_cdef_finish1(FrameDesc *frames, const int *frame_ids);
+// Dynamic shared memory of k_cdef_finish1 for a frame; 0 when over `cap`.
+int finish1_smem(int nfb, int ncand, int cap);
+constexpr int kFin1ThreadsHost = 1024;
 __global__ void k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems);
 
 __global__ void k_lr_sums(FrameDesc *frames, const WorkItem *items, int nitems);

@@ -108,6 +108,9 @@ class FilterExecutor:
     def device_bytes(self):
         return int(self.ctx.device_bytes())
 
+    def reserve(self, device_bytes):
+        self.ctx.reserve(device_bytes)
+
     def trim(self):
         self.ctx.trim()
 
@@ -131,7 +134,10 @@ class Server:
     """Continuous-batching loop over `executors` (one worker thread each)."""
 
     def __init__(self, executors, hbm_budget_bytes=120 << 30, max_batch=64, max_batch_px=32 << 20,
-                 clock=time.perf_counter):
+                 reserve_bytes=0, clock=time.perf_counter):
+        """reserve_bytes > 0: grow every worker's arena to that size up front
+        (growing an arena later releases the old one, which synchronises the
+        device and stalls every worker)."""
         if not executors:
             raise ValueError("need at least one executor")
         self.budget = int(hbm_budget_bytes)
@@ -145,8 +151,13 @@ class Server:
         self.batches = 0
         self.peak_reserved = 0
         self.completed = []
+        self.arena_grows = 0
+        if reserve_bytes * len(executors) > self.budget:
+            raise ValueError("reserved arenas exceed the HBM budget")
         self._disp = threading.Thread(target=self._dispatch_loop, name="zf-dispatch", daemon=True)
         for w in self.workers:
+            if reserve_bytes:
+                w.ex.reserve(reserve_bytes)
             w.held = w.ex.device_bytes()
             w.thread = threading.Thread(target=self._worker_loop, args=(w,), name="zf-worker%d" % w.idx,
                                         daemon=True)
@@ -269,6 +280,7 @@ class Server:
             t1 = self.clock()
             held = w.ex.device_bytes()
             with self.lock:
+                self.arena_grows += held > w.held
                 for r in batch:
                     r.t_start, r.t_done = t0, t1
                     r.error = err
@@ -288,10 +300,14 @@ def latency_summary(reqs):
     if not done:
         return {"requests": 0}
     lat = np.array([r.latency for r in done]) * 1e3
+    wait = np.array([r.t_start - r.arrival for r in done]) * 1e3
+    svc = np.array([r.t_done - r.t_start for r in done]) * 1e3
     t0 = min(r.arrival for r in done)
     t1 = max(r.t_done for r in done)
     px = sum(r.luma_px for r in done)
     return {"requests": len(done), "p50_ms": round(float(np.percentile(lat, 50)), 3),
             "p99_ms": round(float(np.percentile(lat, 99)), 3), "max_ms": round(float(lat.max()), 3),
+            "p99_queue_ms": round(float(np.percentile(wait, 99)), 3),
+            "p99_batch_ms": round(float(np.percentile(svc, 99)), 3),
             "mpix_per_s": round(px / max(t1 - t0, 1e-9) / 1e6, 3),
             "batches": len({(r.worker, r.batch) for r in done})}
