@@ -187,9 +187,47 @@ struct DbTile {
     int plane, pw, ph, x0, y0;
 };
 
+// Word-wide plane access. Plane rows start 4-byte aligned when the plane
+// base is (a row is a multiple of 4 bytes: luma width % 8 == 0, chroma
+// width % 4 == 0), tile columns start at multiples of 4 samples and plane
+// widths are multiples of 4, so a 4-byte word (4 u8 or 2 u16 samples) is
+// either wholly inside the plane or wholly outside.
+__device__ __forceinline__ bool word_ok(const void *p) { return ((uintptr_t)p & 3) == 0; }
+
+// Samples of a word as packed u16 pairs (lo, hi): 4 samples at 8 bits, 2 at 10.
+__device__ __forceinline__ void unpack_word(uint32_t v, int bd, uint16_t *o) {
+    if (bd == 8) {
+        *reinterpret_cast<uint32_t *>(o) = (v & 0xffu) | ((v & 0xff00u) << 8);
+        *reinterpret_cast<uint32_t *>(o + 2) = ((v >> 16) & 0xffu) | ((v >> 8) & 0xff0000u);
+    } else {
+        *reinterpret_cast<uint32_t *>(o) = v;
+    }
+}
+__device__ __forceinline__ uint32_t pack_word(const uint16_t *o, int bd) {
+    if (bd == 8) {
+        const uint32_t a = *reinterpret_cast<const uint32_t *>(o), b = *reinterpret_cast<const uint32_t *>(o + 2);
+        return (a & 0xffu) | ((a >> 8) & 0xff00u) | ((b & 0xffu) << 16) | ((b & 0xff0000u) << 8);
+    }
+    return *reinterpret_cast<const uint32_t *>(o);
+}
+__device__ __forceinline__ const uint32_t *word_at(const uint8_t *plane, int64_t sample, int bd) {
+    return reinterpret_cast<const uint32_t *>(plane + sample * (bd == 8 ? 1 : 2));
+}
+
 // Load the region of a tile into shared memory as u16.
 __device__ void db_load(const DbTile &t, const uint8_t *plane, uint16_t *reg) {
     const int bd = t.f->bd;
+    if (word_ok(plane)) {
+        const int spw = bd == 8 ? 4 : 2, wpr = DB_R / spw;
+        for (int i = threadIdx.x; i < DB_R * wpr; i += blockDim.x) {
+            const int ry = i / wpr, wx = i - ry * wpr;
+            const int y = t.y0 - DB_H + ry, x = t.x0 - DB_H + wx * spw;
+            uint32_t v = 0;
+            if (x >= 0 && x < t.pw && y >= 0 && y < t.ph) v = *word_at(plane, (int64_t)y * t.pw + x, bd);
+            unpack_word(v, bd, reg + ry * DB_R + wx * spw);
+        }
+        return;
+    }
     for (int i = threadIdx.x; i < DB_R * DB_R; i += blockDim.x) {
         int ry = i / DB_R, rx = i - ry * DB_R;
         int y = t.y0 - DB_H + ry, x = t.x0 - DB_H + rx;
@@ -253,7 +291,7 @@ __device__ __forceinline__ void plane_geom(const FrameDesc &f, int plane, int *p
 // (deblock.rs:951-967): both luma levels zero disables every plane; a chroma
 // plane needs its own level.
 __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, const WorkItem *items, int nitems) {
-    __shared__ uint16_t reg[DB_R * DB_R];
+    __shared__ __align__(16) uint16_t reg[DB_R * DB_R];
     __shared__ uint8_t vl[DB_BANDS * DB_EDGES], hl[(DB_T / 4) * DB_EDGES];
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
@@ -274,6 +312,19 @@ __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, 
         lv = lh = f.lf[1 + plane];
     }
     const int bd = f.bd;
+    const int spw = bd == 8 ? 4 : 2, wpr = DB_T / spw;
+    const bool words = word_ok(f.IN[plane]) && word_ok(f.B[plane]);
+    if (lv == 0 && lh == 0 && words) {  // copy-through, word-wide
+        for (int i = threadIdx.x; i < DB_T * wpr; i += blockDim.x) {
+            const int ty = i / wpr, wx = i - ty * wpr;
+            const int y = t.y0 + ty, x = t.x0 + wx * spw;
+            if (x < pw && y < ph) {
+                const int64_t o = (int64_t)y * pw + x;
+                *const_cast<uint32_t *>(word_at(f.B[plane], o, bd)) = *word_at(f.IN[plane], o, bd);
+            }
+        }
+        return;
+    }
     if (lv == 0 && lh == 0) {  // copy-through
         for (int i = threadIdx.x; i < DB_T * DB_T; i += blockDim.x) {
             int y = t.y0 + i / DB_T, x = t.x0 + (i % DB_T);
@@ -288,6 +339,16 @@ __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, 
     db_params(t, lv, lh, vl, hl);
     __syncthreads();
     db_filter(t, reg, vl, hl, lv, lh);
+    if (word_ok(f.B[plane])) {
+        for (int i = threadIdx.x; i < DB_T * wpr; i += blockDim.x) {
+            const int ty = i / wpr, wx = i - ty * wpr;
+            const int y = t.y0 + ty, x = t.x0 + wx * spw;
+            if (x < pw && y < ph)
+                *const_cast<uint32_t *>(word_at(f.B[plane], (int64_t)y * pw + x, bd)) =
+                    pack_word(reg + (ty + DB_H) * DB_R + DB_H + wx * spw, bd);
+        }
+        return;
+    }
     for (int i = threadIdx.x; i < DB_T * DB_T; i += blockDim.x) {
         int ty = i / DB_T, tx = i % DB_T;
         int y = t.y0 + ty, x = t.x0 + tx;
@@ -301,8 +362,8 @@ __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, 
 // plane) search slot; sse[slot * 2 + k] accumulates level levels[slot*2+k].
 __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, const WorkItem *items, int nitems,
                                                      const int *levels, unsigned long long *sse) {
-    __shared__ uint16_t reg[DB_R * DB_R];
-    __shared__ uint16_t pristine[DB_R * DB_R];
+    __shared__ __align__(16) uint16_t reg[DB_R * DB_R];
+    __shared__ __align__(16) uint16_t pristine[DB_R * DB_R];
     __shared__ uint8_t vl[DB_BANDS * DB_EDGES], hl[(DB_T / 4) * DB_EDGES];
     __shared__ unsigned long long part[8];
     const int it = find_item(items, nitems, blockIdx.x);
