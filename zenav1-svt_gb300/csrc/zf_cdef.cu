@@ -141,11 +141,21 @@ __device__ void find_dirs(const uint16_t *reg, int rs, int cs, const int *blist,
 // outside the aligned plane (build_src, cdef.rs:517-544).
 __device__ void load_region(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n, uint16_t *reg) {
     const int rs = n + 4;
-    for (int i = threadIdx.x; i < rs * rs; i += blockDim.x) {
-        int ry = i / rs, rx = i - ry * rs;
-        int y = y0 - 2 + ry, x = x0 - 2 + rx;
-        reg[i] = (x >= 0 && x < pw && y >= 0 && y < ph) ? (uint16_t)ldpx(plane, (int64_t)y * pw + x, bd) : kVeryLarge;
-    }
+    stage_window(
+        bd, pw, rs, x0 - 2, rs, false, kVeryLarge,
+        [&](int ry) {
+            const int y = y0 - 2 + ry;
+            return (y >= 0 && y < ph) ? row_ptr(plane, y, pw, bd) : (const uint8_t *)nullptr;
+        },
+        [&](int ry, int rx, int v) { reg[ry * rs + rx] = (uint16_t)v; });
+}
+
+// Stage the n x n source tile at (x0, y0), 0 outside the canvas.
+__device__ void load_src(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n, uint16_t *src) {
+    stage_window(
+        bd, pw, n, x0, n, false, 0,
+        [&](int ry) { return y0 + ry < ph ? row_ptr(plane, y0 + ry, pw, bd) : (const uint8_t *)nullptr; },
+        [&](int ry, int rx, int v) { src[ry * n + rx] = (uint16_t)v; });
 }
 
 // Non-skip 8x8 blocks of one filter block (the dlist, cdef.rs:1203-1213):
@@ -317,10 +327,7 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
     // ---- luma
     const int x0 = fbc * 64, y0 = fbr * 64;
     load_region(f.B[0], bd, f.w, f.h, x0, y0, 64, reg);
-    for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
-        int y = y0 + i / 64, x = x0 + (i & 63);
-        src[i] = (x < f.w && y < f.h) ? (uint16_t)ldpx(f.S[0], (int64_t)y * f.w + x, bd) : 0;
-    }
+    load_src(f.S[0], bd, f.w, f.h, x0, y0, 64, src);
     __syncthreads();
     find_dirs(reg, CR, cs, blist, nblk, dcost, sdir, svar);
     for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
@@ -420,10 +427,7 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
     for (int p = 1; p <= 2; ++p) {
         __syncthreads();
         load_region(f.B[p], bd, cw, ch, cx0, cy0, 32, reg);
-        for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
-            int y = cy0 + i / 32, x = cx0 + (i & 31);
-            src[i] = (x < cw && y < ch) ? (uint16_t)ldpx(f.S[p], (int64_t)y * cw + x, bd) : 0;
-        }
+        load_src(f.S[p], bd, cw, ch, cx0, cy0, 32, src);
         __syncthreads();
         uint32_t cacc[FPM];
 #pragma unroll
@@ -998,10 +1002,13 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     const bool edge_uv = !(x0 >= 4 && y0 >= 4 && x0 / 2 + 34 <= f.w / 2 && y0 / 2 + 34 <= f.h / 2);
     const bool zero_y = lvl_y == 0 && sec_y == 0;
     const int ssh_y = damp_shift(sec_y, damping);
-    for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
-        const int py = i >> 6, px = i & 63;
+    // a warp takes half an 8x8 block (4 rows x 8 columns), so whether the
+    // block is filtered is uniform over the warp
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int h = warp; h < 128; h += nwarps) {
+        const int b = h >> 1;
+        const int py = (b >> 3) * 8 + (h & 1) * 4 + (lane >> 3), px = (b & 7) * 8 + (lane & 7);
         if (py >= vsize || px >= hsize) continue;
-        const int b = (py >> 3) * 8 + (px >> 3);
         const int pos = (py + 2) * CR + px + 2;
         const int x = (int16_t)reg[pos];
         int y = x;
@@ -1025,10 +1032,11 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
             __syncthreads();
             load_region(f.B[p], bd, cw, ch, cx0, cy0, 32, reg);
             __syncthreads();
-            for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
-                const int py = i >> 5, px = i & 31;
+            // a warp takes two horizontally adjacent 4x4 blocks
+            for (int bp = warp; bp < 32; bp += nwarps) {
+                const int b = 2 * bp + (lane >> 4);
+                const int py = (b >> 3) * 4 + ((lane >> 2) & 3), px = (b & 7) * 4 + (lane & 3);
                 if (py >= vsize / 2 || px >= hsize / 2) continue;
-                const int b = (py >> 2) * 8 + (px >> 2);
                 const int pos = (py + 2) * CRC + px + 2;
                 const int x = (int16_t)reg[pos];
                 int y = x;

@@ -133,6 +133,60 @@ __device__ __forceinline__ int ldpx(const uint8_t *p, int64_t idx, int bd) {
 __device__ __forceinline__ void stpx(uint8_t *p, int64_t idx, int bd, int v) {
     if (bd == 8) p[idx] = (uint8_t)v; else reinterpret_cast<uint16_t *>(p)[idx] = (uint16_t)v;
 }
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Row pointer (sample 0 of row y) of a plane with `stride` samples per row.
+__device__ __forceinline__ const uint8_t *row_ptr(const uint8_t *plane, int64_t y, int stride, int bd) {
+    return plane + y * stride * (bd == 8 ? 1 : 2);
+}
+
+// ---- word-wide access ----------------------------------------------------
+// Planes are stored with rows of a multiple of 4 bytes (luma width % 8 == 0,
+// chroma width % 4 == 0), so when a plane base is 4-byte aligned every word
+// of 4 u8 or 2 u16 samples starting at a multiple of 4 (2) samples is one
+// aligned 32-bit access.
+__device__ __forceinline__ int word_samples(int bd) { return bd == 8 ? 4 : 2; }
+__device__ __forceinline__ int word_sample(uint32_t v, int k, int bd) {
+    return bd == 8 ? (int)((v >> (8 * k)) & 0xffu) : (int)((v >> (16 * k)) & 0xffffu);
+}
+__device__ __forceinline__ bool aligned4(const void *p) { return ((uintptr_t)p & 3) == 0; }
+__device__ __forceinline__ int floor_div(int a, int b) { return a >= 0 ? a / b : -((b - 1 - a) / b); }
+
+// Stage a window of a plane (all threads of the CTA call it): rows r in
+// [0, nrows) read the row pointers rowp(r) (nullptr: a row of `fill`),
+// columns x in [xa, xa + n). A column outside [0, pw) reads column
+// clamp(x, 0, pw - 1) when clamp_x, else gives `fill`. put(r, x - xa, v)
+// stores a sample. Each thread takes whole words: a word wholly inside
+// [0, pw) of an aligned row is one 32-bit load, other words go per sample.
+template <typename RowFn, typename PutFn>
+__device__ __forceinline__ void stage_window(int bd, int pw, int nrows, int xa, int n, bool clamp_x, int fill,
+                                             RowFn rowp, PutFn put) {
+    const int spw = word_samples(bd);
+    const int wa = floor_div(xa, spw), nw = floor_div(xa + n - 1, spw) - wa + 1;
+    for (int i = threadIdx.x; i < nrows * nw; i += blockDim.x) {
+        const int r = i / nw, w = i - r * nw;
+        const uint8_t *row = rowp(r);
+        const int x0 = (wa + w) * spw;
+        if (row && x0 >= 0 && x0 + spw <= pw && aligned4(row)) {
+            const uint32_t v = *reinterpret_cast<const uint32_t *>(row + (bd == 8 ? x0 : 2 * x0));
+            for (int k = 0; k < spw; ++k) {
+                const int x = x0 + k;
+                if (x >= xa && x < xa + n) put(r, x - xa, word_sample(v, k, bd));
+            }
+        } else {
+            for (int k = 0; k < spw; ++k) {
+                const int x = x0 + k;
+                if (x < xa || x >= xa + n) continue;
+                int v = fill;
+                if (row) {
+                    if (x >= 0 && x < pw) v = ldpx(row, x, bd);
+                    else if (clamp_x) v = ldpx(row, clampi(x, 0, pw - 1), bd);
+                }
+                put(r, x - xa, v);
+            }
+        }
+    }
+}
 
 // ---- packed geometry (zf_filter.h) --------------------------------------
 __device__ __forceinline__ int mi_bw(uint32_t r) { return 4 << (r & 7); }

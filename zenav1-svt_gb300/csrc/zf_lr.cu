@@ -26,7 +26,6 @@ namespace zf {
 constexpr int64_t kTapScale = 1 << 16;
 constexpr int kStep = 128;  // WIENER_FILT_STEP
 
-__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 __device__ __forceinline__ int plane_stride(const FrameDesc &f, int p) { return p ? f.w / 2 : f.w; }
 
@@ -50,16 +49,34 @@ __global__ void __launch_bounds__(256) k_lr_sums(FrameDesc *frames, const WorkIt
     const int i0 = wi.b, i1 = min(uh, wi.b + kSumRows);
     unsigned long long s = 0, blk = 0, rgt = 0, bot = 0;
     const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
-    for (int q = threadIdx.x; q < (i1 - i0) * uw; q += blockDim.x) {
-        const int i = i0 + q / uw, j = q % uw;
-        const int64_t o = (int64_t)(r.v_start + i) * stride + r.h_start + j;
-        const int d = ldpx(dg, o, bd);
-        const int e = ldpx(sr, o, bd) - d;
-        const unsigned long long e2 = (unsigned long long)((long long)e * e);
-        s += (unsigned long long)d;
-        if (j >= uw - dw) rgt += e2;
-        else if (i >= uh - dh) bot += e2;
-        else blk += e2;
+    // words of the unit rows (units start at multiples of 256 columns)
+    const int spw = word_samples(bd), nw = (uw + spw - 1) / spw;
+    for (int q = threadIdx.x; q < (i1 - i0) * nw; q += blockDim.x) {
+        const int i = i0 + q / nw, j0 = (q % nw) * spw, cnt = min(spw, uw - j0);
+        const uint8_t *drow = row_ptr(dg, r.v_start + i, stride, bd), *srow = row_ptr(sr, r.v_start + i, stride, bd);
+        const int x0 = r.h_start + j0;
+        int dv[4], sv[4];
+        if (cnt == spw && aligned4(drow) && aligned4(srow)) {
+            const uint32_t a = *reinterpret_cast<const uint32_t *>(drow + (bd == 8 ? x0 : 2 * x0));
+            const uint32_t b = *reinterpret_cast<const uint32_t *>(srow + (bd == 8 ? x0 : 2 * x0));
+            for (int k = 0; k < spw; ++k) {
+                dv[k] = word_sample(a, k, bd);
+                sv[k] = word_sample(b, k, bd);
+            }
+        } else {
+            for (int k = 0; k < cnt; ++k) {
+                dv[k] = ldpx(drow, x0 + k, bd);
+                sv[k] = ldpx(srow, x0 + k, bd);
+            }
+        }
+        for (int k = 0; k < cnt; ++k) {
+            const int j = j0 + k, d = dv[k], e = sv[k] - d;
+            const unsigned long long e2 = (unsigned long long)((long long)e * e);
+            s += (unsigned long long)d;
+            if (j >= uw - dw) rgt += e2;
+            else if (i >= uh - dh) bot += e2;
+            else blk += e2;
+        }
     }
     unsigned long long v[4] = {s, blk, rgt, bot};
 #pragma unroll
@@ -132,18 +149,15 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
     const int dy0 = y0 - (WIN - 1), dx0 = -HALF;
     const int dcols = uw + 2 * HALF + WIN;
     const int drows = (y1 - y0) + 2 * (WIN - 1);
-    for (int q = threadIdx.x; q < drows * dcols; q += blockDim.x) {
-        const int rr = q / dcols, cc = q - rr * dcols;
-        const int y = clampi(r.v_start + dy0 + rr, 0, pl.ph - 1);
-        const int x = clampi(r.h_start + dx0 + cc, 0, pl.pw - 1);
-        D[rr * G::DCOLS + cc] = (int16_t)(ldpx(dg, (int64_t)y * stride + x, bd) - avg);
-    }
+    stage_window(
+        bd, pl.pw, drows, r.h_start + dx0, dcols, true, 0,
+        [&](int rr) { return row_ptr(dg, clampi(r.v_start + dy0 + rr, 0, pl.ph - 1), stride, bd); },
+        [&](int rr, int cc, int v) { D[rr * G::DCOLS + cc] = (int16_t)(v - avg); });
     const int xi0 = max(y0, 0), xi1 = min(y1, uh);
-    for (int q = threadIdx.x; q < (xi1 - xi0) * uw; q += blockDim.x) {
-        const int rr = q / uw, cc = q - rr * uw;
-        X[rr * kMaxUnitW + cc] =
-            (int16_t)(ldpx(sr_, (int64_t)(r.v_start + xi0 + rr) * stride + r.h_start + cc, bd) - avg);
-    }
+    stage_window(
+        bd, pl.pw, xi1 - xi0, r.h_start, uw, true, 0,
+        [&](int rr) { return row_ptr(sr_, r.v_start + xi0 + rr, stride, bd); },
+        [&](int rr, int cc, int v) { X[rr * kMaxUnitW + cc] = (int16_t)(v - avg); });
     for (int q = threadIdx.x; q < WIN2 * WIN2; q += blockDim.x) Hs[q] = 0;
     if (threadIdx.x < WIN2) Ms[threadIdx.x] = 0;
     __syncthreads();
@@ -169,26 +183,46 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
 #pragma unroll
             for (int k = 0; k < WIN - 1; ++k) win[k + 1] = Dat(y + dr, -HALF + k);
             // x runs over [-HALF, uw + HALF); prefix bookkeeping at the
-            // column-window starts (x = sc) and ends (x = sc + uw).
-            for (int x = -HALF; x < uw + HALF; ++x) {
+            // column-window starts (x = sc) and ends (x = sc + uw), which
+            // all lie outside the middle range [HALF + 1, uw - HALF).
+            auto edge_step = [&](int x) {
 #pragma unroll
                 for (int k = 0; k < WIN - 1; ++k) win[k] = win[k + 1];
                 win[WIN - 1] = Dat(y + dr, x + WIN - 1);
-                const bool edge = x < HALF + 1 || x >= uw - HALF;
-                if (edge) {
 #pragma unroll
-                    for (int dc = 0; dc < WIN; ++dc)
+                for (int dc = 0; dc < WIN; ++dc)
 #pragma unroll
-                        for (int sc = -HALF; sc <= HALF; ++sc) {
-                            if (sc + HALF + dc > WIN - 1) continue;  // cb = ca + dc < WIN
-                            if (x == sc) rs[dc][sc + HALF] -= pre[dc];
-                            if (x == sc + uw) rs[dc][sc + HALF] += pre[dc];
-                        }
-                }
+                    for (int sc = -HALF; sc <= HALF; ++sc) {
+                        if (sc + HALF + dc > WIN - 1) continue;  // cb = ca + dc < WIN
+                        if (x == sc) rs[dc][sc + HALF] -= pre[dc];
+                        if (x == sc + uw) rs[dc][sc + HALF] += pre[dc];
+                    }
                 const int a = Dat(y, x);
 #pragma unroll
                 for (int dc = 0; dc < WIN; ++dc) pre[dc] += a * win[dc];
+            };
+            const int xm0 = HALF + 1, xm1 = max(xm0, uw - HALF);
+            int x = -HALF;
+            for (; x < xm0; ++x) edge_step(x);
+            {
+                // middle: the window rotates through registers (slot
+                // (u + dc) % WIN holds D[y + dr][x + u + dc]), no moves
+                int w[WIN];
+#pragma unroll
+                for (int k = 0; k < WIN - 1; ++k) w[k] = win[k + 1];
+                for (; x + WIN <= xm1; x += WIN) {
+#pragma unroll
+                    for (int u = 0; u < WIN; ++u) {
+                        w[(u + WIN - 1) % WIN] = Dat(y + dr, x + u + WIN - 1);
+                        const int a = Dat(y, x + u);
+#pragma unroll
+                        for (int dc = 0; dc < WIN; ++dc) pre[dc] += a * w[(u + dc) % WIN];
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < WIN - 1; ++k) win[k + 1] = w[k];
             }
+            for (; x < uw + HALF; ++x) edge_step(x);
             // x == uw + HALF ends the windows with sc = HALF
 #pragma unroll
             for (int dc = 0; dc < WIN; ++dc)
@@ -222,7 +256,25 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
 #pragma unroll
         for (int k = 0; k < WIN - 1; ++k) win[k + 1] = Dat(yy, -HALF + k);
         const int16_t *xr = X + (i - xi0) * kMaxUnitW;
-        for (int j = 0; j < uw; ++j) {
+        int j = 0;
+        {
+            // rotating window: slot (u + ca) % WIN holds D[yy][j + u + ca - HALF]
+            int w[WIN];
+#pragma unroll
+            for (int k = 0; k < WIN - 1; ++k) w[k] = win[k + 1];
+            for (; j + WIN <= uw; j += WIN) {
+#pragma unroll
+                for (int u = 0; u < WIN; ++u) {
+                    w[(u + WIN - 1) % WIN] = Dat(yy, j + u + HALF);
+                    const int xv = xr[j + u];
+#pragma unroll
+                    for (int ca = 0; ca < WIN; ++ca) acc[ca] += w[(u + ca) % WIN] * xv;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < WIN - 1; ++k) win[k + 1] = w[k];
+        }
+        for (; j < uw; ++j) {
 #pragma unroll
             for (int k = 0; k < WIN - 1; ++k) win[k] = win[k + 1];
             win[WIN - 1] = Dat(yy, j + HALF);
@@ -519,11 +571,10 @@ __device__ int64_t trial_sse(const FrameDesc &f, int plane, const LrPlane &pl, c
         for (int tx = 0; tx < uw; tx += TT_W) {
             const int y0 = r.v_start + ty, x0 = r.h_start + tx;
             __syncthreads();
-            for (int q = threadIdx.x; q < SH * SW; q += blockDim.x) {
-                const int rr = q / SW, cc = q - rr * SW;
-                const int y = clampi(y0 - 3 + rr, 0, pl.ph - 1), x = clampi(x0 - 3 + cc, 0, pl.pw - 1);
-                stage[q] = (uint16_t)ldpx(dg, (int64_t)y * stride + x, bd);
-            }
+            stage_window(
+                bd, pl.pw, SH, x0 - 3, SW, true, 0,
+                [&](int rr) { return row_ptr(dg, clampi(y0 - 3 + rr, 0, pl.ph - 1), stride, bd); },
+                [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
             __syncthreads();
             for (int q = threadIdx.x; q < SH * TT_W; q += blockDim.x) {
                 const int rr = q / TT_W, cc = q - rr * TT_W;
@@ -668,6 +719,7 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
     constexpr int SW = TL + 7;
     __shared__ uint16_t stage[(TL + 7) * SW];
     __shared__ uint16_t tmp[(TL + 7) * TL];
+    __shared__ uint16_t srct[TL * TL];
     __shared__ unsigned long long red[24];
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
@@ -691,11 +743,13 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         vf[k] = u.vf[k];
     }
     const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
-    for (int q = threadIdx.x; q < (th + 7) * (tw + 7); q += blockDim.x) {
-        const int rr = q / (tw + 7), cc = q - rr * (tw + 7);
-        const int y = clampi(y0 - 3 + rr, 0, pl.ph - 1), x = clampi(x0 - 3 + cc, 0, pl.pw - 1);
-        stage[rr * SW + cc] = (uint16_t)ldpx(dg, (int64_t)y * stride + x, bd);
-    }
+    stage_window(
+        bd, pl.pw, th + 7, x0 - 3, tw + 7, true, 0,
+        [&](int rr) { return row_ptr(dg, clampi(y0 - 3 + rr, 0, pl.ph - 1), stride, bd); },
+        [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
+    stage_window(
+        bd, pl.pw, th, x0, tw, true, 0, [&](int rr) { return row_ptr(sr, y0 + rr, stride, bd); },
+        [&](int rr, int cc, int v) { srct[rr * TL + cc] = (uint16_t)v; });
     __syncthreads();
     for (int q = threadIdx.x; q < (th + 7) * tw; q += blockDim.x) {
         const int rr = q / tw, cc = q - rr * tw;
@@ -713,7 +767,7 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
 #pragma unroll
         for (int k = 0; k < 8; ++k) tp[k] = tmp[(rr + k) * TL + cc];
         const int y = wiener_v(tp, vf, bd);
-        const int e = ldpx(sr, (int64_t)(y0 + rr) * stride + x0 + cc, bd) - y;
+        const int e = (int)srct[rr * TL + cc] - y;
         const unsigned long long e2 = (unsigned long long)((long long)e * e);
         if (j >= uw - dw) rgt += e2;
         else if (i >= uh - dh) bot += e2;
@@ -1003,10 +1057,8 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
     const int ncol = cx, nrow = ye - ys;
     const bool copy_above = s > 0, copy_below = ye < pl.ph;
     const int rows = nrow + 7;
-    for (int q = threadIdx.x; q < rows * SW; q += blockDim.x) {
-        const int rr = q / SW, cc = q - rr * SW;
+    auto row_of = [&](int rr) {
         const int y = ys - 3 + rr;
-        const int x = clampi(x0 - 3 + cc, 0, pl.pw - 1);
         const uint8_t *src = post;
         int yy;
         if (y < ys) {
@@ -1026,8 +1078,10 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
         } else {
             yy = y;
         }
-        stage[q] = (uint16_t)ldpx(src, (int64_t)yy * stride + x, bd);
-    }
+        return row_ptr(src, yy, stride, bd);
+    };
+    stage_window(bd, pl.pw, rows, x0 - 3, SW, true, 0, row_of,
+                 [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
     __syncthreads();
     for (int q = threadIdx.x; q < rows * TT_W; q += blockDim.x) {
         const int rr = q / TT_W, cc = q - rr * TT_W;
