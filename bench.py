@@ -223,8 +223,23 @@ def kernel_bytes(name, w, h, px):
         "k_lr_stats5": 2 * plane,
         "k_lr_stats7": 2 * plane,
         "k_lr_trial": 2 * plane,
+        "k_lr_trial_tiles": 2 * plane,
         "k_lr_apply": 2 * plane,
     }.get(name, 0.0)
+
+
+# DRAM bytes (read + write) per luma pixel of one launch, from one ncu
+# capture of each kernel on a 3840x2160 8-bit preset-6 frame
+# (profiles/top_kernels_4k_p6_frame.md); the roofline's `traffic` scales
+# them to the launch's frame.
+KERNEL_DRAM_BYTES_PER_PX = {
+    "k_cdef_apply": (14.068224e6 + 256.0) / (3840 * 2160),
+    "k_cdef_search": 26.512384e6 / (3840 * 2160),
+    "k_lr_stats5": 25.800704e6 / (3840 * 2160),
+    "k_cdef_finish": 0.229632e6 / (3840 * 2160),
+    "k_deblock_apply": (15.017472e6 + 0.326656e6) / (3840 * 2160),
+    "k_lr_trial_tiles": 24.95488e6 / (3840 * 2160),
+}
 
 
 def run_ours(args):
@@ -364,8 +379,13 @@ def run_ours(args):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
+    bpp = KERNEL_DRAM_BYTES_PER_PX.get(name)
+    traffic = int(bpp * np.mean([f.luma_px for f in frames])) if bpp else None
     roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 5), "traffic": None,
+                "frac": round(achieved / peak, 5), "traffic": traffic,
+                "algorithmic_bytes": int(bytes_per_launch),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 4K preset-6 launch, "
+                                  "scaled by luma pixels" if traffic else None,
                 "peak_source": "of measured" if "hbm_gbs" in peaks else "of fallback",
                 "stage_bytes_per_px": 4.75,
                 "stage_frac": round((4.75 * px_step / (ms / 1e3) / 1e9) / peak, 5)}
