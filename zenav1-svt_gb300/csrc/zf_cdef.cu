@@ -160,19 +160,27 @@ __device__ void load_src(const uint8_t *plane, int bd, int pw, int ph, int x0, i
 
 // Non-skip 8x8 blocks of one filter block (the dlist, cdef.rs:1203-1213):
 // bit (by*8+bx) of the returned mask; blocks past a partial fb are 0.
-__device__ uint64_t fb_dlist(const FrameDesc &f, int fbr, int fbc) {
+// Threads 0..63 test one block each, warp ballots meet in `part` (two
+// words); every thread of the CTA calls this and gets the mask.
+__device__ uint64_t fb_dlist(const FrameDesc &f, int fbr, int fbc, unsigned *part) {
     const int vsize = min(64, f.h - fbr * 64), hsize = min(64, f.w - fbc * 64);
-    uint64_t m = 0;
-    for (int by = 0; by < vsize / 8; ++by)
-        for (int bx = 0; bx < hsize / 8; ++bx) {
+    const int t = threadIdx.x;
+    bool nonskip = false;
+    if (t < 64) {
+        const int by = t >> 3, bx = t & 7;
+        if (by < vsize / 8 && bx < hsize / 8) {
             const int r = fbr * 16 + by * 2, c = fbc * 16 + bx * 2;
             bool all = true;
             for (int rr = r; rr < min(r + 2, f.mi_rows); ++rr)
                 for (int cc = c; cc < min(c + 2, f.mi_cols); ++cc)
                     all = all && mi_skip(f.mi[(int64_t)rr * f.mi_cols + cc]);
-            if (!all) m |= 1ull << (by * 8 + bx);
+            nonskip = !all;
         }
-    return m;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, nonskip);
+    if (t < 64 && (t & 31) == 0) part[t >> 5] = m;
+    __syncthreads();
+    return (uint64_t)part[0] | ((uint64_t)part[1] << 32);
 }
 
 __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v, unsigned long long *scratch) {
@@ -297,7 +305,8 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
     const int fbr = fb / f.nhfb, fbc = fb - fbr * f.nhfb;
     const int bd = f.bd, cs = bd - 8;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint64_t dl = fb_dlist(f, fbr, fbc);
+    __shared__ unsigned dl_part[2];
+    const uint64_t dl = fb_dlist(f, fbr, fbc, dl_part);
     if (threadIdx.x == 0) {
         f.fb_row[fb] = dl != 0;
         int n = 0;
@@ -958,7 +967,8 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     const int vsize = min(64, f.h - y0), hsize = min(64, f.w - x0);
     // Decoder do_cdef gate (cdef.rs:84-88).
     const bool any = cp.bits != 0 || cp.y_str[0] != 0 || (f.chroma && cp.uv_str[0] != 0);
-    const uint64_t dl_all = fb_dlist(f, fbr, fbc);
+    __shared__ unsigned dl_part[2];
+    const uint64_t dl_all = fb_dlist(f, fbr, fbc, dl_part);
     if (threadIdx.x == 0) f.fb_row[fb] = dl_all != 0;
     const uint64_t dl = any ? dl_all : 0;
     if (dl == 0) {  // copy-through
