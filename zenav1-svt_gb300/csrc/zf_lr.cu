@@ -373,41 +373,41 @@ __device__ void reduce_bins(int64_t (&bins)[NB], int n, int64_t *out) {
 }
 
 // One update_{a,b}_sep_sym (restoration.rs:849-909). `upd_a` selects which
-// factor is solved; `fix` is the other one.
+// factor is solved; `fix` is the other one. Every bin is a sum of
+// independently truncated terms, so the order of the sum is free: a thread
+// owns one bin pair q (the (k, l) of update_a, the (i, j) of update_b) and a
+// slice of the other pair index, and the 20 bins meet in shared memory
+// (`sbins`, zero on entry and on return).
 __device__ void update_sep_sym(bool upd_a, int win, const int64_t *M, const int64_t *H, const int32_t *fix,
-                               int32_t *outv, int64_t *sav, int64_t *sbv) {
+                               int32_t *outv, int64_t *sav, int64_t *sbv, unsigned long long *sbins) {
     const int win2 = win * win, h1 = (win >> 1) + 1;
-    int64_t bins[20];
-#pragma unroll
-    for (int k = 0; k < 20; ++k) bins[k] = 0;
-    // av terms
-    for (int t = threadIdx.x; t < win2; t += blockDim.x) {
-        const int i = t / win, j = t - i * win;
-        if (upd_a) bins[16 + wrap_index(j, win)] += M[i * win + j] * (int64_t)fix[i] / kTapScale;
-        else bins[16 + wrap_index(i, win)] += M[i * win + j] * (int64_t)fix[j] / kTapScale;
-    }
-    // bv terms
-    const int n4 = win2 * win2;
-    for (int t = threadIdx.x; t < n4; t += blockDim.x) {
-        const int i = t / (win * win2), r1 = t - i * win * win2;
-        const int j = r1 / win2, r2 = r1 - j * win2;
-        const int k = r2 / win, l = r2 - k * win;
-        if (upd_a) {
-            const int64_t hv = H[(int64_t)j * win * win2 + i * win + k * win2 + l];
-            bins[wrap_index(l, win) * 4 + wrap_index(k, win)] +=
-                hv * (int64_t)fix[i] / kTapScale * (int64_t)fix[j] / kTapScale;
-        } else {
-            const int64_t hv = H[(int64_t)i * win * win2 + j * win + k * win2 + l];
-            bins[wrap_index(j, win) * 4 + wrap_index(i, win)] +=
-                hv * (int64_t)fix[k] / kTapScale * (int64_t)fix[l] / kTapScale;
+    const int t = threadIdx.x, R = blockDim.x / win2;
+    if (t < R * win2) {
+        const int q = t % win2, sl = t / win2;
+        const int qa = q / win, qb = q - qa * win;
+        int64_t acc = 0;
+        for (int pp = sl; pp < win2; pp += R) {
+            const int pa = pp / win, pb = pp - pa * win;
+            // update_a: (i, j) = (pa, pb), (k, l) = (qa, qb); update_b: (i, j) =
+            // (qa, qb), (k, l) = (pa, pb); the two factors come from `fix`
+            const int64_t hv = upd_a ? H[pb * win * win2 + pa * win + qa * win2 + qb]
+                                     : H[qa * win * win2 + qb * win + pa * win2 + pb];
+            acc += hv * (int64_t)fix[pa] / kTapScale * (int64_t)fix[pb] / kTapScale;
         }
+        atomicAdd(&sbins[wrap_index(qb, win) * 4 + wrap_index(qa, win)], (unsigned long long)acc);
     }
-    __shared__ int64_t red[20];
-    reduce_bins<20>(bins, 20, red);
-    if (threadIdx.x == 0) {
-        for (int a = 0; a < h1; ++a) sav[a] = red[16 + a];
+    if (t < win) {  // av terms: t is j (update_a) or i (update_b)
+        int64_t acc = 0;
+        for (int o = 0; o < win; ++o)
+            acc += (upd_a ? M[o * win + t] : M[t * win + o]) * (int64_t)fix[o] / kTapScale;
+        atomicAdd(&sbins[16 + wrap_index(t, win)], (unsigned long long)acc);
+    }
+    __syncthreads();
+    if (t == 0) {
+        for (int a = 0; a < h1; ++a) sav[a] = (int64_t)sbins[16 + a];
         for (int a = 0; a < h1; ++a)
-            for (int b = 0; b < h1; ++b) sbv[a * h1 + b] = red[a * 4 + b];
+            for (int b = 0; b < h1; ++b) sbv[a * h1 + b] = (int64_t)sbins[a * 4 + b];
+        for (int k = 0; k < 20; ++k) sbins[k] = 0;
         normalize_and_solve(win, sav, sbv, outv);
     }
     __syncthreads();
@@ -447,14 +447,18 @@ __global__ void __launch_bounds__(128) k_lr_solve(FrameDesc *frames, const WorkI
     const LrPlane &pl = f.lr[wi.plane];
     LrUnit &u = pl.units[wi.a];
     const int win = pl.win, win2 = win * win;
-    const int64_t div = f.bd == 10 ? 4 : 1;
-    // Bit-depth divider on M and the upper triangle, then mirror
+    // Bit-depth divider on M and the upper triangle (truncating division by
+    // 4 at 10 bits, written as a shift with the sign correction), then mirror
     // (compute_stats_hbd, restoration.rs:1799-1806).
-    for (int k = threadIdx.x; k < win2; k += blockDim.x) M[k] = u.m[k] / div;
+    const bool hbd = f.bd == 10;
+    auto divd = [hbd](int64_t v) { return hbd ? (v + ((v >> 63) & 3)) >> 2 : v; };
+    __shared__ unsigned long long sbins[20];
+    if (threadIdx.x < 20) sbins[threadIdx.x] = 0;
+    for (int k = threadIdx.x; k < win2; k += blockDim.x) M[k] = divd(u.m[k]);
     for (int t = threadIdx.x; t < win2 * win2; t += blockDim.x) {
         const int k = t / win2, l = t - k * win2;
         if (l >= k) {
-            const int64_t v = u.h[t] / div;
+            const int64_t v = divd(u.h[t]);
             H[t] = v;
             H[l * win2 + k] = v;
         }
@@ -475,8 +479,8 @@ __global__ void __launch_bounds__(128) k_lr_solve(FrameDesc *frames, const WorkI
     }
     __syncthreads();
     for (int round = 1; round < 5; ++round) {
-        update_sep_sym(true, win, M, H, b, a, sav, sbv);
-        update_sep_sym(false, win, M, H, a, b, sav, sbv);
+        update_sep_sym(true, win, M, H, b, a, sav, sbv, sbins);
+        update_sep_sym(false, win, M, H, a, b, sav, sbv, sbins);
     }
     if (threadIdx.x == 0) {
         for (int i = 0; i < 8; ++i) {
