@@ -129,7 +129,7 @@ template <int WIN>
 __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkItem *items, int nitems) {
     using G = StatGeom<WIN>;
     constexpr int HALF = G::H, WIN2 = WIN * WIN;
-    __shared__ int16_t D[G::DROWS * G::DCOLS];
+    __shared__ __align__(16) int16_t D[G::DROWS * G::DCOLS];
     __shared__ int16_t X[G::ROWS * kMaxUnitW];
     __shared__ unsigned long long Hs[WIN2 * WIN2];
     __shared__ unsigned long long Ms[WIN2];
@@ -165,6 +165,15 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
 
     const int nh = G::NDR * (y1 - y0);
     const int t = threadIdx.x;
+    // Rows with every vertical shift valid (HALF <= y < uh - HALF) keep their
+    // row sums for a cross-row reduction; the others add theirs directly.
+    auto interior = [&](int yy) { return yy >= HALF && yy < uh - HALF; };
+    int rs[WIN][WIN];  // rs[dc][sc + HALF]
+    bool keep = false;
+#pragma unroll
+    for (int k = 0; k < WIN; ++k)
+#pragma unroll
+        for (int j = 0; j < WIN; ++j) rs[k][j] = 0;
     if (t < nh) {
         // ---- H: one (row y, dr) per thread
         const int dr = t % G::NDR - (WIN - 1);
@@ -172,13 +181,9 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
         // the row and its partner must lie in the extended range
         if (y + dr >= -HALF && y + dr < uh + HALF) {
             const int dc0 = dr < 0 ? 1 : 0;  // dc = 0 only for dr >= 0
-            int pre[WIN], rs[WIN][WIN];      // rs[dc][sc + HALF]
+            int pre[WIN];
 #pragma unroll
-            for (int k = 0; k < WIN; ++k) {
-                pre[k] = 0;
-#pragma unroll
-                for (int j = 0; j < WIN; ++j) rs[k][j] = 0;
-            }
+            for (int k = 0; k < WIN; ++k) pre[k] = 0;
             int win[WIN];  // D[y + dr][x + dc], dc = 0..WIN-1
 #pragma unroll
             for (int k = 0; k < WIN - 1; ++k) win[k + 1] = Dat(y + dr, -HALF + k);
@@ -228,9 +233,10 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
             for (int dc = 0; dc < WIN; ++dc)
                 if (HALF + HALF + dc <= WIN - 1) rs[dc][2 * HALF] += pre[dc];
             // contributions: H[a][b], a = (ca, ra), b = (ca + dc, ra + dr)
+            keep = interior(y);
 #pragma unroll
             for (int dc = 0; dc < WIN; ++dc) {
-                if (dc < dc0) continue;
+                if (dc < dc0 || keep) continue;
 #pragma unroll
                 for (int ca = 0; ca + dc < WIN; ++ca) {
                     const int v = rs[dc][ca];
@@ -285,6 +291,42 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
 #pragma unroll
         for (int ca = 0; ca < WIN; ++ca)
             atomicAdd(&Ms[ca * WIN + ra], (unsigned long long)(long long)acc[ca]);
+    }
+    __syncthreads();
+    // Interior rows: the row sums of each (dr, dc, ca) are added over the
+    // CTA's rows in shared memory (D is no longer read), then one atomic per
+    // H entry. RS[(row * NDR + dr index) * NE + e], e enumerating (dc, ca)
+    // with ca + dc < WIN.
+    {
+        constexpr int NE = WIN * (WIN + 1) / 2;
+        static_assert(G::ROWS * G::NDR * NE * 4 <= G::DROWS * G::DCOLS * 2, "row-sum buffer fits in D");
+        int *RS = reinterpret_cast<int *>(D);
+        if (keep) {
+            int e = 0;
+#pragma unroll
+            for (int dc = 0; dc < WIN; ++dc)
+#pragma unroll
+                for (int ca = 0; ca + dc < WIN; ++ca) RS[t * NE + e++] = rs[dc][ca];
+        }
+        __syncthreads();
+        for (int q = t; q < G::NDR * NE; q += blockDim.x) {
+            const int dri = q / NE, dr = dri - (WIN - 1);
+            int e = q - dri * NE, dc = 0;
+            while (e >= WIN - dc) {
+                e -= WIN - dc;
+                ++dc;
+            }
+            const int ca = e;
+            if (dr < 0 && dc == 0) continue;
+            long long acc = 0;
+            for (int r = 0; r < y1 - y0; ++r)
+                if (interior(y0 + r)) acc += RS[(r * G::NDR + dri) * NE + (q - dri * NE)];
+            if (acc == 0) continue;
+            for (int ra = max(0, -dr); ra < min(WIN, WIN - dr); ++ra) {
+                const int ia = ca * WIN + ra, ib = (ca + dc) * WIN + ra + dr;
+                atomicAdd(&Hs[ia * WIN2 + ib], (unsigned long long)acc);
+            }
+        }
     }
     __syncthreads();
     for (int q = threadIdx.x; q < WIN2 * WIN2; q += blockDim.x) {
