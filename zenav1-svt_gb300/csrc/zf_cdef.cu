@@ -521,6 +521,7 @@ constexpr int kFinCluster = 8;
 constexpr int kFinThreads = 512;
 constexpr int kFinWarps = kFinThreads / 32;
 constexpr int kFinRowsPerLane = 8;  // register-cached best for up to 256 rows per CTA
+constexpr int kFinPushPairs = 512;  // push partials to every rank up to this many pairs (64 KiB)
 
 __global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThreads, 1)
     k_cdef_finish(FrameDesc *frames, const int *frame_ids, int smem_bytes) {
@@ -555,9 +556,15 @@ __global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThread
         __syncthreads();
     }
     const int sbr = scan[T - 1];
-    unsigned long long *tot[2] = {dyn64, dyn64 + npairs};
-    uint32_t *dyn = reinterpret_cast<uint32_t *>(dyn64 + 2 * npairs);
-    const bool in_smem = (size_t)2 * npairs * 8 + (size_t)sbr * (n2 + 1) * 4 <= (size_t)smem_bytes;
+    // Pair partials. push: every CTA stores its partials into every rank's
+    // inbox[buf][rank][pair] before the barrier, so the sums read local
+    // shared memory; else (many pairs) each CTA keeps tot[buf][pair] and the
+    // sums read the other ranks' copies.
+    const bool push = npairs <= kFinPushPairs;
+    const int pslots = push ? kFinCluster * npairs : npairs;
+    unsigned long long *tot[2] = {dyn64, dyn64 + pslots};
+    uint32_t *dyn = reinterpret_cast<uint32_t *>(dyn64 + 2 * pslots);
+    const bool in_smem = (size_t)2 * pslots * 8 + (size_t)sbr * (n2 + 1) * 4 <= (size_t)smem_bytes;
     uint32_t *R = in_smem ? dyn : f.cdef_rows32 + ((size_t)level * nfb + fb0) * n2;
     int *ids = in_smem ? reinterpret_cast<int *>(dyn + (size_t)sbr * n2) : f.cdef_ids + (size_t)level * nfb + fb0;
     {
@@ -636,15 +643,22 @@ __global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThread
                 }
             }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-            if (lane == 0) tot[buf][p] = acc;
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (push) {
+                if (lane < kFinCluster) *cl.map_shared_rank(tot[buf] + rank * npairs + p, lane) = acc;
+            } else if (lane == 0) {
+                tot[buf][p] = acc;
+            }
         }
-        cl.sync();  // partials of this step complete everywhere
+        cl.sync();  // partials of this step complete (and delivered) everywhere
         unsigned long long bv = ~0ull;
         int bi = 0x7fffffff;
         for (int p = lane; p < npairs; p += 32) {
             unsigned long long v = 0;
-            for (int r = 0; r < kFinCluster; ++r) v += cl.map_shared_rank(tot[buf], r)[p];
+            if (push)
+                for (int r = 0; r < kFinCluster; ++r) v += tot[buf][r * npairs + p];
+            else
+                for (int r = 0; r < kFinCluster; ++r) v += cl.map_shared_rank(tot[buf], r)[p];
             if (v < bv) {  // p increases along a lane: strict < keeps the lowest
                 bv = v;
                 bi = p;
@@ -1187,9 +1201,14 @@ extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_de
     if (launch_cdef_search(d.cdef.first_pass_num, d.cdef.ncand / d.cdef.first_pass_num, nfb, st, &sc->desc,
                            &sc->item, 1) != cudaSuccess)
         return ZF_ERR_CUDA;
-    // pair partials + compacted rows and ids: < 48 KiB for ncand <= 20 and nfb <= 2048
-    const int per_cta = 2 * d.cdef.ncand * d.cdef.ncand * 8 +
+    // pair partials (an inbox per rank) + compacted rows and ids: at most
+    // 51 + 42 KiB for ncand <= 20 and nfb <= 2048
+    const int np = d.cdef.ncand * d.cdef.ncand;
+    const int per_cta = 2 * (np <= kFinPushPairs ? kFinCluster : 1) * np * 8 +
                         (nfb + kFinCluster - 1) / kFinCluster * (2 * d.cdef.ncand + 1) * 4;
+    if (per_cta > 48 * 1024 &&
+        cudaFuncSetAttribute(k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, per_cta) != cudaSuccess)
+        return ZF_ERR_CUDA;
     k_cdef_finish<<<kFinCluster * kFinLevels, kFinThreads, per_cta, st>>>(&sc->desc, &sc->frame_id, per_cta);
     if (cudaGetLastError() != cudaSuccess) return ZF_ERR_CUDA;
     FrameDesc back;

@@ -901,10 +901,12 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             // rows do not fit use global scratch)
             size_t want = 0, pairs = 0;
             for (int fi : large_f) {
-                const size_t nc = (size_t)plans[fi].d.cdef.ncand;
-                pairs = std::max(pairs, 2 * nc * nc * 8);
-                want = std::max(want, 2 * nc * nc * 8 + ((size_t)plans[fi].nfb + zf::kFinClusterHost - 1) /
-                                                             zf::kFinClusterHost * (2 * nc + 1) * 4);
+                const size_t nc = (size_t)plans[fi].d.cdef.ncand, np = nc * nc;
+                // double-buffered partials: an inbox per rank up to kFinPushPairs pairs
+                const size_t pb = 2 * (np <= (size_t)zf::kFinPushPairsHost ? zf::kFinClusterHost : 1) * np * 8;
+                pairs = std::max(pairs, pb);
+                want = std::max(want, pb + ((size_t)plans[fi].nfb + zf::kFinClusterHost - 1) /
+                                                zf::kFinClusterHost * (2 * nc + 1) * 4);
             }
             const int smem = (int)std::max(pairs, std::min<size_t>(want, kFinishSmemCap));
             CU(cudaFuncSetAttribute(zf::k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinishSmemCap));

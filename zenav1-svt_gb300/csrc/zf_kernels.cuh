@@ -19,6 +19,7 @@ __global__ void k_cdef_finish1(FrameDesc *frames, const int *frame_ids);
 // Dynamic shared memory of k_cdef_finish1 for a frame; 0 when over `cap`.
 int finish1_smem(int nfb, int ncand, int cap);
 constexpr int kFin1ThreadsHost = 1024;
+constexpr int kFinPushPairsHost = 512;  // k_cdef_finish: inbox per rank up to this many pairs
 __global__ void k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems);
 
 __global__ void k_lr_sums(FrameDesc *frames, const WorkItem *items, int nitems);
