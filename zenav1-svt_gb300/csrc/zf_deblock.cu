@@ -377,21 +377,40 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
     DbTile t{&f, plane, pw, ph, (tix % tiles_x) * DB_T, (tix / tiles_x) * DB_T};
     const int bd = f.bd;
     db_load(t, f.IN[plane], pristine);
+    // edge lengths do not depend on a nonzero level: computed once
+    if (levels[slot * 2] > 0 || levels[slot * 2 + 1] > 0) db_params(t, 1, 1, vl, hl);
     __syncthreads();
+    const int spw = bd == 8 ? 4 : 2, wpr = DB_T / spw;
+    const bool words = word_ok(f.S[plane]);
     for (int k = 0; k < 2; ++k) {
         const int lvl = levels[slot * 2 + k];
         if (lvl < 0) continue;
-        for (int i = threadIdx.x; i < DB_R * DB_R; i += blockDim.x) reg[i] = pristine[i];
-        if (lvl != 0) db_params(t, lvl, lvl, vl, hl);
+        for (int i = threadIdx.x; i < DB_R * DB_R / 2; i += blockDim.x)
+            reinterpret_cast<uint32_t *>(reg)[i] = reinterpret_cast<const uint32_t *>(pristine)[i];
         __syncthreads();
         if (lvl != 0) db_filter(t, reg, vl, hl, lvl, lvl);
         unsigned long long acc = 0;
-        for (int i = threadIdx.x; i < DB_T * DB_T; i += blockDim.x) {
-            int ty = i / DB_T, tx = i % DB_T;
-            int y = t.y0 + ty, x = t.x0 + tx;
-            if (x < pw && y < ph) {
-                int d = ldpx(f.S[plane], (int64_t)y * pw + x, bd) - (int)reg[(ty + DB_H) * DB_R + tx + DB_H];
-                acc += (unsigned long long)((long long)d * d);
+        if (words) {
+            for (int i = threadIdx.x; i < DB_T * wpr; i += blockDim.x) {
+                const int ty = i / wpr, wx = i - ty * wpr;
+                const int y = t.y0 + ty, x = t.x0 + wx * spw;
+                if (x < pw && y < ph) {
+                    const uint32_t sw = *word_at(f.S[plane], (int64_t)y * pw + x, bd);
+                    const uint16_t *rp = reg + (ty + DB_H) * DB_R + DB_H + wx * spw;
+                    for (int q = 0; q < spw; ++q) {
+                        const int d = word_sample(sw, q, bd) - (int)rp[q];
+                        acc += (unsigned long long)((long long)d * d);
+                    }
+                }
+            }
+        } else {
+            for (int i = threadIdx.x; i < DB_T * DB_T; i += blockDim.x) {
+                int ty = i / DB_T, tx = i % DB_T;
+                int y = t.y0 + ty, x = t.x0 + tx;
+                if (x < pw && y < ph) {
+                    int d = ldpx(f.S[plane], (int64_t)y * pw + x, bd) - (int)reg[(ty + DB_H) * DB_R + tx + DB_H];
+                    acc += (unsigned long long)((long long)d * d);
+                }
             }
         }
 #pragma unroll

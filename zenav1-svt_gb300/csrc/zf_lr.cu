@@ -900,22 +900,10 @@ __device__ __forceinline__ double rdcost_dbl(int64_t rdmult, int64_t rate, int64
 struct RdUnit {
     int64_t sse_none, sse_wn;
     int16_t v[3], h[3];
-    int16_t pick, pad;
+    int16_t pick;
+    int16_t thr;  // WIENER beats NONE iff the tap bits <= thr (-1: never)
 };
 
-__device__ int count_bits3(int win, const int16_t *v, const int16_t *h, const int16_t *rv, const int16_t *rh) {
-    auto tap = [](int f, int rf, int minv, int maxv, int k) {
-        return count_subexpfin(maxv - minv + 1, k, recenter_finite_nonneg(maxv - minv + 1, rf - minv, f - minv));
-    };
-    int bits = 0;
-    if (win == 7) bits += tap(v[0], rv[0], -5, 10, 1);
-    bits += tap(v[1], rv[1], -23, 8, 2);
-    bits += tap(v[2], rv[2], -17, 46, 3);
-    if (win == 7) bits += tap(h[0], rh[0], -5, 10, 1);
-    bits += tap(h[1], rh[1], -23, 8, 2);
-    bits += tap(h[2], rh[2], -17, 46, 3);
-    return bits;
-}
 
 // Frame RD of one (frame, plane) per CTA (search_restoration_still,
 // restoration.rs:838-924). The unit walk is sequential only through the
@@ -928,9 +916,42 @@ __device__ int count_bits3(int win, const int16_t *v, const int16_t *h, const in
 constexpr int kLrFinThreads = 256;
 constexpr int kLrPairMax = 20100;  // units <= 200 (pair table of int32 in shared memory)
 
+// Bits of one tap as a table over (reference, value) for the three tap
+// positions (ranges [-5, 10], [-23, 8], [-17, 46]; finalize_sym_filter and the
+// refinement keep taps inside them): count_wiener_bits becomes six lookups.
+constexpr int kTb0 = 16, kTb1 = 32, kTb2 = 64;
+struct TapBits {
+    uint8_t t0[kTb0 * kTb0], t1[kTb1 * kTb1], t2[kTb2 * kTb2];
+};
+__device__ void fill_tap_bits(TapBits &tb) {
+    for (int q = threadIdx.x; q < kTb0 * kTb0 + kTb1 * kTb1 + kTb2 * kTb2; q += blockDim.x) {
+        // entry [r * n + v]: reference tap r + minv, tap v + minv
+        int n, k, rel = q;
+        uint8_t *dst;
+        if (rel < kTb0 * kTb0) {
+            n = kTb0, k = 1, dst = tb.t0;
+        } else if ((rel -= kTb0 * kTb0) < kTb1 * kTb1) {
+            n = kTb1, k = 2, dst = tb.t1;
+        } else {
+            rel -= kTb1 * kTb1;
+            n = kTb2, k = 3, dst = tb.t2;
+        }
+        const int r = rel / n, v = rel - r * n;
+        dst[rel] = (uint8_t)count_subexpfin(n, k, recenter_finite_nonneg(n, r, v));
+    }
+}
+__device__ __forceinline__ int count_bits_tab(const TapBits &tb, int win, const int16_t *v, const int16_t *h,
+                                              const int16_t *rv, const int16_t *rh) {
+    int bits = tb.t1[(rv[1] + 23) * kTb1 + v[1] + 23] + tb.t2[(rv[2] + 17) * kTb2 + v[2] + 17] +
+               tb.t1[(rh[1] + 23) * kTb1 + h[1] + 23] + tb.t2[(rh[2] + 17) * kTb2 + h[2] + 17];
+    if (win == 7) bits += tb.t0[(rv[0] + 5) * kTb0 + v[0] + 5] + tb.t0[(rh[0] + 5) * kTb0 + h[0] + 5];
+    return bits;
+}
+
 __device__ __forceinline__ void unit_rd(const FrameDesc &f, const LrPlane &pl, const RdUnit &u,
-                                        const int16_t *rv, const int16_t *rh, int64_t &bits_wn, bool &pick) {
-    const int64_t cnt = count_bits3(pl.win, u.v, u.h, rv, rh);
+                                        const int16_t *rv, const int16_t *rh, const TapBits &tb, int64_t &bits_wn,
+                                        bool &pick) {
+    const int64_t cnt = count_bits_tab(tb, pl.win, u.v, u.h, rv, rh);
     bits_wn = 320 + (cnt << 9);
     const int64_t bits_none = 768;
     const double cn = rdcost_dbl(f.rdmult, bits_none >> 4, u.sse_none);
@@ -942,6 +963,7 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
     extern __shared__ unsigned char lr_dyn[];
     __shared__ int frame_rtype;
     __shared__ int64_t red[kLrFinThreads / 32];
+    __shared__ TapBits tb;
     const int id = blockIdx.x;
     if (id >= nframes * 3) return;
     FrameDesc &f = frames[id / 3];
@@ -954,6 +976,7 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
     const int n = pl.hunits * pl.vunits;
     const int npairs = n * (n + 1) / 2;
     const bool table = npairs <= kLrPairMax;
+    fill_tap_bits(tb);
     RdUnit *U = reinterpret_cast<RdUnit *>(lr_dyn);
     int32_t *PT = reinterpret_cast<int32_t *>(lr_dyn + (size_t)n * sizeof(RdUnit));
     int64_t part = 0;
@@ -973,6 +996,24 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
             r.h[i] = u.hf[i];
         }
         r.pick = 0;
+        // The WIENER cost grows with the tap bits and NONE's does not depend
+        // on them, so the pick is "bits <= thr": thr by bisection on the
+        // reference's own double comparison.
+        r.thr = -1;
+        if (r.sse_wn != INT64_MAX) {
+            const double cn = rdcost_dbl(f.rdmult, 768 >> 4, r.sse_none);
+            int lo = -1, hi = 64;  // pick(lo) holds (or lo = -1), pick(hi) does not
+            if (rdcost_dbl(f.rdmult, (320 + ((int64_t)hi << 9)) >> 4, r.sse_wn) < cn) {
+                lo = hi;  // beyond any count the taps can reach
+            } else {
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (rdcost_dbl(f.rdmult, (320 + ((int64_t)mid << 9)) >> 4, r.sse_wn) < cn) lo = mid;
+                    else hi = mid;
+                }
+            }
+            r.thr = (int16_t)lo;
+        }
         U[k] = r;
         part += u.sse_none;
     }
@@ -994,10 +1035,8 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
                 PT[idx] = 0;
                 continue;
             }
-            int64_t bw;
-            bool pk;
-            unit_rd(f, pl, u, j < 0 ? dflt : U[j].v, j < 0 ? dflt : U[j].h, bw, pk);
-            PT[idx] = (int32_t)bw | (pk ? 1 << 30 : 0);
+            const int cnt = count_bits_tab(tb, pl.win, u.v, u.h, j < 0 ? dflt : U[j].v, j < 0 ? dflt : U[j].h);
+            PT[idx] = (320 + (cnt << 9)) | (cnt <= u.thr ? 1 << 30 : 0);
         }
         __syncthreads();
     }
@@ -1022,7 +1061,7 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
                 bits_wn = e & 0xffff;
                 pick = (e >> 30) & 1;
             } else {
-                unit_rd(f, pl, u, rv, rh, bits_wn, pick);
+                unit_rd(f, pl, u, rv, rh, tb, bits_wn, pick);
             }
             if (pick) {
                 u.pick = 1;
