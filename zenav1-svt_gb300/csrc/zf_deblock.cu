@@ -219,8 +219,14 @@ __device__ void db_load(const DbTile &t, const uint8_t *plane, uint16_t *reg) {
     const int bd = t.f->bd;
     if (word_ok(plane)) {
         const int spw = bd == 8 ? 4 : 2, wpr = DB_R / spw;
-        for (int i = threadIdx.x; i < DB_R * wpr; i += blockDim.x) {
-            const int ry = i / wpr, wx = i - ry * wpr;
+        // flat over (row, word); row and word advance by blockDim.x's quotient
+        // and remainder
+        const int step_r = blockDim.x / wpr, step_w = blockDim.x - step_r * wpr;
+        for (int ry = threadIdx.x / wpr, wx = threadIdx.x - ry * wpr; ry < DB_R; ry += step_r, wx += step_w) {
+            if (wx >= wpr) {
+                wx -= wpr;
+                if (++ry >= DB_R) break;
+            }
             const int y = t.y0 - DB_H + ry, x = t.x0 - DB_H + wx * spw;
             uint32_t v = 0;
             if (x >= 0 && x < t.pw && y >= 0 && y < t.ph) v = *word_at(plane, (int64_t)y * t.pw + x, bd);
@@ -312,11 +318,11 @@ __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, 
         lv = lh = f.lf[1 + plane];
     }
     const int bd = f.bd;
-    const int spw = bd == 8 ? 4 : 2, wpr = DB_T / spw;
+    const int spw = bd == 8 ? 4 : 2, wpr = DB_T / spw, lgw = bd == 8 ? 4 : 5;  // wpr = 1 << lgw
     const bool words = word_ok(f.IN[plane]) && word_ok(f.B[plane]);
     if (lv == 0 && lh == 0 && words) {  // copy-through, word-wide
         for (int i = threadIdx.x; i < DB_T * wpr; i += blockDim.x) {
-            const int ty = i / wpr, wx = i - ty * wpr;
+            const int ty = i >> lgw, wx = i & (wpr - 1);
             const int y = t.y0 + ty, x = t.x0 + wx * spw;
             if (x < pw && y < ph) {
                 const int64_t o = (int64_t)y * pw + x;
@@ -341,7 +347,7 @@ __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, 
     db_filter(t, reg, vl, hl, lv, lh);
     if (word_ok(f.B[plane])) {
         for (int i = threadIdx.x; i < DB_T * wpr; i += blockDim.x) {
-            const int ty = i / wpr, wx = i - ty * wpr;
+            const int ty = i >> lgw, wx = i & (wpr - 1);
             const int y = t.y0 + ty, x = t.x0 + wx * spw;
             if (x < pw && y < ph)
                 *const_cast<uint32_t *>(word_at(f.B[plane], (int64_t)y * pw + x, bd)) =
@@ -380,7 +386,7 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
     // edge lengths do not depend on a nonzero level: computed once
     if (levels[slot * 2] > 0 || levels[slot * 2 + 1] > 0) db_params(t, 1, 1, vl, hl);
     __syncthreads();
-    const int spw = bd == 8 ? 4 : 2, wpr = DB_T / spw;
+    const int spw = bd == 8 ? 4 : 2, wpr = DB_T / spw, lgw = bd == 8 ? 4 : 5;  // wpr = 1 << lgw
     const bool words = word_ok(f.S[plane]);
     for (int k = 0; k < 2; ++k) {
         const int lvl = levels[slot * 2 + k];
@@ -392,7 +398,7 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
         unsigned long long acc = 0;
         if (words) {
             for (int i = threadIdx.x; i < DB_T * wpr; i += blockDim.x) {
-                const int ty = i / wpr, wx = i - ty * wpr;
+                const int ty = i >> lgw, wx = i & (wpr - 1);
                 const int y = t.y0 + ty, x = t.x0 + wx * spw;
                 if (x < pw && y < ph) {
                     const uint32_t sw = *word_at(f.S[plane], (int64_t)y * pw + x, bd);

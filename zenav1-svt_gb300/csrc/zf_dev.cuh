@@ -163,8 +163,16 @@ __device__ __forceinline__ void stage_window(int bd, int pw, int nrows, int xa, 
                                              RowFn rowp, PutFn put) {
     const int spw = word_samples(bd);
     const int wa = floor_div(xa, spw), nw = floor_div(xa + n - 1, spw) - wa + 1;
-    for (int i = threadIdx.x; i < nrows * nw; i += blockDim.x) {
-        const int r = i / nw, w = i - r * nw;
+    // flat over (row, word) pairs; the thread's row and word advance by the
+    // constant quotient and remainder of blockDim.x (one division per call)
+    const int step_r = blockDim.x / nw, step_w = blockDim.x - step_r * nw;
+    int r = threadIdx.x / nw, w = threadIdx.x - r * nw;
+    for (; r < nrows; r += step_r, w += step_w) {
+        if (w >= nw) {
+            w -= nw;
+            ++r;
+            if (r >= nrows) break;
+        }
         const uint8_t *row = rowp(r);
         const int x0 = (wa + w) * spw;
         if (row && x0 >= 0 && x0 + spw <= pw && aligned4(row)) {

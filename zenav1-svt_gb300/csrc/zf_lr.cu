@@ -51,8 +51,12 @@ __global__ void __launch_bounds__(256) k_lr_sums(FrameDesc *frames, const WorkIt
     const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
     // words of the unit rows (units start at multiples of 256 columns)
     const int spw = word_samples(bd), nw = (uw + spw - 1) / spw;
-    for (int q = threadIdx.x; q < (i1 - i0) * nw; q += blockDim.x) {
-        const int i = i0 + q / nw, j0 = (q % nw) * spw, cnt = min(spw, uw - j0);
+    const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    for (int q = threadIdx.x >> 5; q < (i1 - i0) * ((nw + 31) >> 5); q += nwarps) {
+        // warp per (row, 32-word segment), lanes over the words
+        const int segs = (nw + 31) >> 5, i = i0 + q / segs, w = (q - (q / segs) * segs) * 32 + lane;
+        if (w >= nw) continue;
+        const int j0 = w * spw, cnt = min(spw, uw - j0);
         const uint8_t *drow = row_ptr(dg, r.v_start + i, stride, bd), *srow = row_ptr(sr, r.v_start + i, stride, bd);
         const int x0 = r.h_start + j0;
         int dv[4], sv[4];
@@ -797,8 +801,10 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         bd, pl.pw, th, x0, tw, true, 0, [&](int rr) { return row_ptr(sr, y0 + rr, stride, bd); },
         [&](int rr, int cc, int v) { srct[rr * TL + cc] = (uint16_t)v; });
     __syncthreads();
-    for (int q = threadIdx.x; q < (th + 7) * tw; q += blockDim.x) {
-        const int rr = q / tw, cc = q - rr * tw;
+    // rows x 64 columns (TL), columns past the tile width skipped: no division
+    for (int q = threadIdx.x; q < (th + 7) * TL; q += blockDim.x) {
+        const int rr = q >> 6, cc = q & (TL - 1);
+        if (cc >= tw) continue;
         int px[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) px[k] = stage[rr * SW + cc + k];
@@ -806,8 +812,9 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
     }
     __syncthreads();
     unsigned long long blk = 0, rgt = 0, bot = 0;
-    for (int q = threadIdx.x; q < th * tw; q += blockDim.x) {
-        const int rr = q / tw, cc = q - rr * tw;
+    for (int q = threadIdx.x; q < th * TL; q += blockDim.x) {
+        const int rr = q >> 6, cc = q & (TL - 1);
+        if (cc >= tw) continue;
         const int i = ty + rr, j = tx + cc;
         int tp[8];
 #pragma unroll
