@@ -583,9 +583,10 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             for (size_t u = 0; u < p.rects[pl].size(); ++u) {
                 const UnitRect &r = p.rects[pl][u];
                 const int uh = r.v_end - r.v_start;
-                for (int c = 0; c < uh; c += zf::kSumRowsHost) wl_sum.add(i, pl, (int)u, c, 1);
+                // one item per unit; the CTA offset selects the row block
+                wl_sum.add(i, pl, (int)u, 0, (uh + zf::kSumRowsHost - 1) / zf::kSumRowsHost);
                 const int half = L.win / 2, srows = zf::stat_rows_host(L.win);
-                for (int c = -half; c < uh + half; c += srows) (L.win == 5 ? wl_st5 : wl_st7).add(i, pl, (int)u, c, 1);
+                (L.win == 5 ? wl_st5 : wl_st7).add(i, pl, (int)u, 0, (uh + 2 * half + srows - 1) / srows);
                 wl_unit.add(i, pl, (int)u, 0, 1);
                 if (L.refine) {
                     wl_trial.add(i, pl, (int)u, 0, 1);  // one CTA per unit: the hill-climb is sequential
@@ -604,26 +605,18 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             const int nstripes = (L.ph + off + full - 1) / full;
             const int ntiles = (L.stride + 63) / 64;
             const int canvas_h = pl ? p.d.h / 2 : p.d.h;
-            // unit of a (stripe, tile): the rectangles form a row-major
-            // hunits x vunits grid, so look the column up along the first
-            // row and the row along the first column
+            // one item per stripe (CTA offset = 64-px column tile); a = the
+            // stripe's row of the row-major hunits x vunits unit grid (-1:
+            // copy only), the kernel finds the column along that row
             const std::vector<UnitRect> &R = p.rects[pl];
             const int hu = p.hunits[pl], vu = p.vunits[pl];
-            std::vector<int> col((size_t)ntiles, -1);
-            for (int t = 0, c = 0; t < ntiles; ++t) {
-                const int x = t * 64;
-                while (c < hu && x >= R[c].h_end) ++c;
-                if (c < hu && x >= R[c].h_start) col[t] = c;
-            }
             for (int s = 0, r = 0; s < nstripes; ++s) {
                 const int ys = std::max(0, s * full - off);
                 while (r < vu && ys >= R[(size_t)r * hu].v_end) ++r;
                 const bool row_ok = r < vu && ys >= R[(size_t)r * hu].v_start;
-                for (int t = 0; t < ntiles; ++t)
-                    wl_apply.add(i, pl, (L.on && row_ok && col[t] >= 0) ? r * hu + col[t] : -1, (s << 16) | t, 1);
+                wl_apply.add(i, pl, (L.on && row_ok) ? r : -1, s, ntiles);
             }
-            if (canvas_h > L.ph)
-                for (int t = 0; t < ntiles; ++t) wl_apply.add(i, pl, -1, (nstripes << 16) | t, 1);
+            if (canvas_h > L.ph) wl_apply.add(i, pl, -1, nstripes, ntiles);
         }
     }
     std::vector<int> cdef_frames(cdef_small);

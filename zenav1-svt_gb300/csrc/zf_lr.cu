@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) k_lr_sums(FrameDesc *frames, const WorkIt
     const int bd = f.bd, stride = plane_stride(f, wi.plane);
     const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
     const int dw = uw % 16, dh = uh % 16;
-    const int i0 = wi.b, i1 = min(uh, wi.b + kSumRows);
+    const int i0 = (blockIdx.x - wi.cta_begin) * kSumRows, i1 = min(uh, i0 + kSumRows);
     unsigned long long s = 0, blk = 0, rgt = 0, bot = 0;
     const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
     // words of the unit rows (units start at multiples of 256 columns)
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
     const int avg = (int)((unsigned long long)u.sum / (unsigned long long)((int64_t)uw * uh));
     const uint8_t *dg = f.A[wi.plane], *sr_ = f.S[wi.plane];
     // rows of this CTA in unit coordinates (extended range [-HALF, uh + HALF))
-    const int y0 = wi.b, y1 = min(uh + HALF, y0 + G::ROWS);
+    const int y0 = -HALF + (blockIdx.x - wi.cta_begin) * G::ROWS, y1 = min(uh + HALF, y0 + G::ROWS);
     // D rows [y0 - (WIN-1), y1 + (WIN-1)) clamped, columns [-HALF, uw + HALF + WIN)
     const int dy0 = y0 - (WIN - 1), dx0 = -HALF;
     const int dcols = uw + 2 * HALF + WIN;
@@ -1120,12 +1120,12 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
     constexpr int MAXH = 64 + 7;
     __shared__ uint16_t stage[MAXH * SW];
     __shared__ uint16_t tmp[MAXH * TT_W];
-    const WorkItem wi = items[blockIdx.x];
+    const WorkItem wi = items[find_item(items, nitems, blockIdx.x)];
     const FrameDesc &f = frames[wi.frame];
     const LrPlane &pl = f.lr[wi.plane];
     const int ss = wi.plane ? 1 : 0;
     const int full = 64 >> ss, off = 8 >> ss;
-    const int s = wi.b >> 16, ct = wi.b & 0xffff;
+    const int s = wi.b, ct = blockIdx.x - wi.cta_begin;
     const int bd = f.bd, stride = plane_stride(f, wi.plane);
     const int canvas_h = wi.plane ? f.h / 2 : f.h;
     const int nstripes = (pl.ph + off + full - 1) / full;
@@ -1135,17 +1135,43 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
     const int x0 = ct * TT_W, tw = min(TT_W, stride - x0);
     const uint8_t *post = f.A[wi.plane], *pre = f.B[wi.plane];
     uint8_t *out = f.C[wi.plane];
-    const bool filter = s < nstripes && wi.a >= 0 && pl.on && pl.frame_rtype != 0 && pl.units[wi.a].rtype == 1;
+    // the unit of this tile: wi.a is its row of the unit grid (-1: copy only),
+    // the column is looked up along that row
+    __shared__ int s_unit, s_filter;
+    if (threadIdx.x == 0) {
+        int unit = -1;
+        if (wi.a >= 0 && pl.on) {
+            const UnitRect *urow = pl.rects + wi.a * pl.hunits;
+            for (int c = 0; c < pl.hunits; ++c)
+                if (x0 >= urow[c].h_start && x0 < urow[c].h_end) {
+                    unit = wi.a * pl.hunits + c;
+                    break;
+                }
+        }
+        s_unit = unit;
+        s_filter = s < nstripes && unit >= 0 && pl.frame_rtype != 0 && pl.units[unit].rtype == 1;
+    }
+    __syncthreads();
+    const int unit = s_unit;
+    const bool filter = s_filter != 0;
     // columns copied from A: all of them, or those beyond the true width
     const int cx = filter ? min(tw, pl.pw - x0) : 0;
-    if (cx < tw)
+    const int spw = word_samples(bd), nwr = tw / spw;  // tw is a multiple of 4 (plane widths are)
+    if (cx == 0 && aligned4(post) && aligned4(out)) {  // whole tile: word copies
+        for (int q = threadIdx.x; q < (ye - ys) * nwr; q += blockDim.x) {
+            const int rr = q / nwr, wx = q - rr * nwr;
+            const int64_t o = ((int64_t)(ys + rr) * stride + x0) * (bd == 8 ? 1 : 2) + wx * 4;
+            *reinterpret_cast<uint32_t *>(out + o) = *reinterpret_cast<const uint32_t *>(post + o);
+        }
+    } else if (cx < tw) {
         for (int q = threadIdx.x; q < (ye - ys) * (tw - cx); q += blockDim.x) {
             const int rr = q / (tw - cx), cc = cx + (q - rr * (tw - cx));
             const int64_t o = (int64_t)(ys + rr) * stride + x0 + cc;
             stpx(out, o, bd, ldpx(post, o, bd));
         }
+    }
     if (!filter) return;
-    const LrUnit &u = pl.units[wi.a];
+    const LrUnit &u = pl.units[unit];
     const int ncol = cx, nrow = ye - ys;
     const bool copy_above = s > 0, copy_below = ye < pl.ph;
     const int rows = nrow + 7;
