@@ -352,6 +352,20 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) & ~(a - 1); }
 constexpr size_t kFinishSmemCap = 160 * 1024;
 constexpr int kFinish1SmemCap = 200 * 1024;
 constexpr int kFinish1MaxFb = 1024;  // filter blocks (a 2048x2048 frame)
+// k_lr_finish: 32 B per unit plus the pair table of <= 200 units (or 32 B
+// per unit alone for larger planes; 4096 units at most)
+constexpr int kLrFinishSmemCap = 160 * 1024;
+
+// Opt the kernels with large dynamic shared memory in once per device
+// (a function attribute; set at context creation, not per call).
+cudaError_t set_kernel_attributes() {
+    cudaError_t e = cudaFuncSetAttribute(zf::k_cdef_finish1, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinish1SmemCap);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(zf::k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFinishSmemCap);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(zf::k_lr_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kLrFinishSmemCap);
+    return e;
+}
 
 int validate_frame(zf_ctx *ctx, const zf_frame *f) {
     if (!f) return fail(ctx, ZF_ERR_ARG, "frame is NULL");
@@ -884,7 +898,6 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             large_f(cdef_frames.begin() + n_small, cdef_frames.end());
         { LaunchScope ls_(ctx, "k_cdef_finish");
         if (!small_f.empty()) {
-            CU(cudaFuncSetAttribute(zf::k_cdef_finish1, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinish1SmemCap));
             zf::k_cdef_finish1<<<(int)small_f.size() * zf::kFinLevels, zf::kFin1ThreadsHost, smem1, st>>>(
                 d_desc, (const int *)(base + o_cf));
         }
@@ -902,7 +915,6 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                                                 zf::kFinClusterHost * (2 * nc + 1) * 4);
             }
             const int smem = (int)std::max(pairs, std::min<size_t>(want, kFinishSmemCap));
-            CU(cudaFuncSetAttribute(zf::k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinishSmemCap));
             zf::k_cdef_finish<<<(int)large_f.size() * zf::kFinClusterHost * zf::kFinLevels, zf::kFinThreadsHost,
                                 smem, st>>>(d_desc, (const int *)(base + o_cf) + small_f.size(), smem);
         } }
@@ -962,8 +974,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 const size_t nu = (size_t)p.hunits[pl] * p.vunits[pl], np = nu * (nu + 1) / 2;
                 smem = std::max(smem, nu * 32 + (np <= (size_t)zf::kLrPairMaxHost ? np * 4 : 0));
             }
-        if (smem > 48 * 1024)
-            CU(cudaFuncSetAttribute(zf::k_lr_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (smem > (size_t)kLrFinishSmemCap) return fail(ctx, ZF_ERR_UNSUPPORTED, "restoration unit table too large");
         zf::k_lr_finish<<<n * 3, zf::kLrFinThreadsHost, smem, st>>>(d_desc, n); }
         TRY(launch_check(ctx, "k_lr_finish"));
         TRY(check_cancel(ctx));
@@ -1096,7 +1107,8 @@ int32_t zf_create(zf_ctx **out, const zf_opts *opts) {
     c->device = opts ? opts->device : 0;
     c->budget = opts ? opts->hbm_budget_bytes : 0;
     c->cancel = opts ? opts->cancel_flag : nullptr;
-    if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        set_kernel_attributes() != cudaSuccess) {
         cudaGetLastError();
         delete c;
         return ZF_ERR_CUDA;
