@@ -416,6 +416,8 @@ def run_ours(args):
                 "roofline": roofline, "kernels": kernels, "clocks": clk}
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_sample()
+        if world == 1:
+            line["highres_10bit"] = run_highres10(args, ctx, stream, dev)
         if world == 1 and not args.no_batched:
             line["batched"] = run_batched(args, ctx, stream, dev, gen_frames(batch_jobs(args.batch_n)))
             print("batched:", json.dumps(line["batched"]), file=sys.stderr)
@@ -426,6 +428,43 @@ def run_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def run_highres10(args, ctx, stream, dev):
+    """The 10-bit high-resolution configuration: one 4096x3072 10-bit frame
+    (u16 planes), preset 2 (20 CDEF candidates, deblock level search,
+    Wiener refinement), qp 28; device-resident, one zf_filter_stage per
+    step, L2 flushed between steps."""
+    import torch
+    pkg = ge._pkg()
+    from zenav1_svt_gb300 import abi, synth
+    f = synth.make_frame(synth.frame_seed(3, 0), 4096, 3072, 10, 28, 2, "power10")
+    src = [torch.from_numpy(p).to(dev) for p in f.src]
+    rec0 = [torch.from_numpy(p).to(dev) for p in f.rec]
+    rec = [x.clone() for x in rec0]
+    m = torch.from_numpy(pkg.pack_geom(f.geom).view(np.int32)).to(dev)
+    s = abi.make_frame_struct(f, [x.data_ptr() for x in src], [x.data_ptr() for x in rec], m.data_ptr(),
+                              on_device=True)
+    d = abi.Decisions(f.w, f.h, f.true_w, f.true_h)
+    st = abi.ZfStats()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    times = []
+    for k in range(args.warmup + args.steps):
+        for a, b in zip(rec, rec0):
+            a.copy_(b)
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.filter_stage_raw(s, d, st)
+        e1.record(stream)
+        e1.synchronize()
+        if k >= args.warmup:
+            times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    return {"workload": "4096x3072 10-bit 4:2:0 (u16), preset 2, qp 28, device-resident",
+            "mpix_per_s": round(f.luma_px / (ms / 1e3) / 1e6, 3), "ms": round(ms, 3),
+            "lf": d.as_dict()["lf"], "cdef_bits": d.as_dict()["cdef_bits"]}
 
 
 def run_batched(args, ctx, stream, dev, frames):

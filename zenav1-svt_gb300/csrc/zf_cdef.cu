@@ -11,6 +11,7 @@
 // (plus the 2-pixel reach of the taps) in shared memory, so every pixel of
 // every candidate reads the same values as the reference's build_src.
 #include <algorithm>
+#include <mutex>
 
 #include <cooperative_groups.h>
 
@@ -501,9 +502,10 @@ __device__ __forceinline__ unsigned long long rdc(unsigned long long lambda, uns
 //
 // joint_strength_search_dual runs once per bit count i = 0..3 (nb = 1 << i
 // strengths: nb greedy search_one_dual steps, then 4 nb refinement steps)
-// and the four searches are independent, so each runs on its own cluster of
-// kFinCluster CTAs (critical path: the 40 steps of i = 3). The filter
-// blocks are split into kFinCluster contiguous ranges; each CTA compacts
+// and the four searches are independent, so each runs on its own cluster
+// (16 CTAs where the device allows it, else 8; critical path: the 40 steps
+// of i = 3). The filter blocks are split into one contiguous range per CTA;
+// each CTA compacts
 // the rows of its range (column-major u32: every per-filter-block mse is
 // below 2^29 -- at most 4096 px x 1023^2 >> 4 per plane, times sub <= 4 --
 // so the u32 copy is lossless and a luma + chroma row sum fits u32) into
@@ -517,13 +519,14 @@ __device__ __forceinline__ unsigned long long rdc(unsigned long long lambda, uns
 // chosen strengths -- so a step has one barrier. The cluster that finishes
 // last (a counter in the frame descriptor) picks the bit count with the
 // lowest RD cost (strict <, in i order) and writes the per-fb indices.
-constexpr int kFinCluster = 8;
+constexpr int kFinCluster = 8;      // portable cluster size (the fallback)
+constexpr int kFinClusterMax = 16;  // non-portable cluster size, where the device allows it
 constexpr int kFinThreads = 512;
 constexpr int kFinWarps = kFinThreads / 32;
 constexpr int kFinRowsPerLane = 8;  // register-cached best for up to 256 rows per CTA
 constexpr int kFinPushPairs = 512;  // push partials to every rank up to this many pairs (64 KiB)
 
-__global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThreads, 1)
+__global__ void __launch_bounds__(kFinThreads, 1)
     k_cdef_finish(FrameDesc *frames, const int *frame_ids, int smem_bytes) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
@@ -534,14 +537,15 @@ __global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThread
     __shared__ int scan[kFinThreads];
     __shared__ int local_sb, last_flag;
     const int rank = (int)cl.block_rank();
-    const int cluster = blockIdx.x / kFinCluster;
+    const int CL = (int)cl.num_blocks();  // cluster size chosen at launch (8 or 16)
+    const int cluster = blockIdx.x / CL;
     const int level = cluster % kFinLevels;
     FrameDesc &f = frames[frame_ids[cluster / kFinLevels]];
     CdefParams &cp = f.cdef;
     if (cp.mode != 1) return;  // uniform over the cluster
     const int nfb = f.nhfb * f.nvfb, n_cand = cp.ncand, n2 = 2 * n_cand, npairs = n_cand * n_cand;
     const int T = blockDim.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const int fb0 = (int)((int64_t)nfb * rank / kFinCluster), fb1 = (int)((int64_t)nfb * (rank + 1) / kFinCluster);
+    const int fb0 = (int)((int64_t)nfb * rank / CL), fb1 = (int)((int64_t)nfb * (rank + 1) / CL);
     // compaction of this range's filter blocks with rows, in fb order
     const int span = fb1 - fb0, chunk = (span + T - 1) / T;
     const int c0 = fb0 + min(span, t * chunk), c1 = fb0 + min(span, t * chunk + chunk);
@@ -561,7 +565,7 @@ __global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThread
     // shared memory; else (many pairs) each CTA keeps tot[buf][pair] and the
     // sums read the other ranks' copies.
     const bool push = npairs <= kFinPushPairs;
-    const int pslots = push ? kFinCluster * npairs : npairs;
+    const int pslots = push ? CL * npairs : npairs;
     unsigned long long *tot[2] = {dyn64, dyn64 + pslots};
     uint32_t *dyn = reinterpret_cast<uint32_t *>(dyn64 + 2 * pslots);
     const bool in_smem = (size_t)2 * pslots * 8 + (size_t)sbr * (n2 + 1) * 4 <= (size_t)smem_bytes;
@@ -575,7 +579,7 @@ __global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThread
     if (t == 0) local_sb = sbr;
     cl.sync();
     int sb = 0;
-    for (int r = 0; r < kFinCluster; ++r) sb += *cl.map_shared_rank(&local_sb, r);
+    for (int r = 0; r < CL; ++r) sb += *cl.map_shared_rank(&local_sb, r);
     if (sb == 0) {  // every filter block all-skip: cdef.rs:282-288
         if (level == 0) {
             for (int fb = fb0 + t; fb < fb1; fb += T) f.fb_idx[fb] = 0;
@@ -645,7 +649,7 @@ __global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThread
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (push) {
-                if (lane < kFinCluster) *cl.map_shared_rank(tot[buf] + rank * npairs + p, lane) = acc;
+                if (lane < CL) *cl.map_shared_rank(tot[buf] + rank * npairs + p, lane) = acc;
             } else if (lane == 0) {
                 tot[buf][p] = acc;
             }
@@ -656,9 +660,9 @@ __global__ void __cluster_dims__(kFinCluster, 1, 1) __launch_bounds__(kFinThread
         for (int p = lane; p < npairs; p += 32) {
             unsigned long long v = 0;
             if (push)
-                for (int r = 0; r < kFinCluster; ++r) v += tot[buf][r * npairs + p];
+                for (int r = 0; r < CL; ++r) v += tot[buf][r * npairs + p];
             else
-                for (int r = 0; r < kFinCluster; ++r) v += cl.map_shared_rank(tot[buf], r)[p];
+                for (int r = 0; r < CL; ++r) v += cl.map_shared_rank(tot[buf], r)[p];
             if (v < bv) {  // p increases along a lane: strict < keeps the lowest
                 bv = v;
                 bi = p;
@@ -951,6 +955,65 @@ __global__ void __launch_bounds__(kFin1Threads, 1) k_cdef_finish1(FrameDesc *fra
     }
 }
 
+// Launch k_cdef_finish for `nclusters` (frame, bit count) clusters of `cl`
+// CTAs (the cluster size is a launch attribute; 16 needs the non-portable
+// attribute, set once per device by finish_cluster_size).
+cudaError_t launch_cdef_finish(int nclusters, int cl, size_t smem, cudaStream_t st, FrameDesc *frames,
+                               const int *frame_ids, int smem_bytes) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nclusters * cl));
+    cfg.blockDim = dim3(kFinThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_cdef_finish, frames, frame_ids, smem_bytes);
+}
+
+// The cluster size for k_cdef_finish with `smem` dynamic bytes: 16 when the
+// device can co-schedule a 16-CTA cluster of this kernel, else 8.
+int finish_cluster_size(size_t smem) {
+    static std::mutex mu;
+    static int allowed = -1;                      // non-portable sizes opted in (per process)
+    static size_t last_smem = 0;
+    static int last_size = 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (last_size && last_smem == smem) return last_size;
+    if (allowed < 0) {
+        allowed = cudaFuncSetAttribute(k_cdef_finish, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                          cudaSuccess
+                      ? 1
+                      : 0;
+        cudaGetLastError();
+    }
+    last_smem = smem;
+    last_size = kFinCluster;
+    if (!allowed) return kFinCluster;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kFinClusterMax);
+    cfg.blockDim = dim3(kFinThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kFinClusterMax;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_cdef_finish, &cfg) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        return kFinCluster;
+    }
+    last_size = kFinClusterMax;
+    return kFinClusterMax;
+}
+
 // Shared memory k_cdef_finish1 needs for a frame (0 when it does not fit).
 int finish1_smem(int nfb, int ncand, int cap) {
     const int64_t s4 = ((int64_t)nfb + 3) / 4 * 4, n2 = 2 * ncand, npairs = (int64_t)ncand * ncand;
@@ -1204,12 +1267,13 @@ extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_de
     // pair partials (an inbox per rank) + compacted rows and ids: at most
     // 51 + 42 KiB for ncand <= 20 and nfb <= 2048
     const int np = d.cdef.ncand * d.cdef.ncand;
-    const int per_cta = 2 * (np <= kFinPushPairs ? kFinCluster : 1) * np * 8 +
-                        (nfb + kFinCluster - 1) / kFinCluster * (2 * d.cdef.ncand + 1) * 4;
+    const int CL = kFinCluster;
+    const int per_cta = 2 * (np <= kFinPushPairs ? CL : 1) * np * 8 + (nfb + CL - 1) / CL * (2 * d.cdef.ncand + 1) * 4;
     if (per_cta > 48 * 1024 &&
         cudaFuncSetAttribute(k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, per_cta) != cudaSuccess)
         return ZF_ERR_CUDA;
-    k_cdef_finish<<<kFinCluster * kFinLevels, kFinThreads, per_cta, st>>>(&sc->desc, &sc->frame_id, per_cta);
+    if (launch_cdef_finish(kFinLevels, CL, per_cta, st, &sc->desc, &sc->frame_id, per_cta) != cudaSuccess)
+        return ZF_ERR_CUDA;
     if (cudaGetLastError() != cudaSuccess) return ZF_ERR_CUDA;
     FrameDesc back;
     if (cudaMemcpyAsync(&back, &sc->desc, sizeof(back), cudaMemcpyDeviceToHost, st) != cudaSuccess) return ZF_ERR_CUDA;

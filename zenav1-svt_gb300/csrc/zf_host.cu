@@ -902,21 +902,28 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 d_desc, (const int *)(base + o_cf));
         }
         if (!large_f.empty()) {
-            // dynamic shared memory: the double-buffered pair partials (always)
-            // and the compacted rows of the largest frame, capped (frames whose
-            // rows do not fit use global scratch)
-            size_t want = 0, pairs = 0;
-            for (int fi : large_f) {
-                const size_t nc = (size_t)plans[fi].d.cdef.ncand, np = nc * nc;
-                // double-buffered partials: an inbox per rank up to kFinPushPairs pairs
-                const size_t pb = 2 * (np <= (size_t)zf::kFinPushPairsHost ? zf::kFinClusterHost : 1) * np * 8;
-                pairs = std::max(pairs, pb);
-                want = std::max(want, pb + ((size_t)plans[fi].nfb + zf::kFinClusterHost - 1) /
-                                                zf::kFinClusterHost * (2 * nc + 1) * 4);
+            // dynamic shared memory: the double-buffered pair partials (an
+            // inbox per rank up to kFinPushPairs pairs) and the compacted rows
+            // of the largest frame, capped (frames whose rows do not fit use
+            // global scratch). 16-CTA clusters where the device allows them.
+            auto need = [&](int cl) {
+                size_t want = 0, pairs = 0;
+                for (int fi : large_f) {
+                    const size_t nc = (size_t)plans[fi].d.cdef.ncand, np = nc * nc;
+                    const size_t pb = 2 * (np <= (size_t)zf::kFinPushPairsHost ? (size_t)cl : 1) * np * 8;
+                    pairs = std::max(pairs, pb);
+                    want = std::max(want, pb + ((size_t)plans[fi].nfb + cl - 1) / cl * (2 * nc + 1) * 4);
+                }
+                return std::max(pairs, std::min<size_t>(want, kFinishSmemCap));
+            };
+            int cl = zf::kFinClusterMaxHost;
+            size_t smem = need(cl);
+            if (zf::finish_cluster_size(smem) != cl) {
+                cl = zf::kFinClusterHost;
+                smem = need(cl);
             }
-            const int smem = (int)std::max(pairs, std::min<size_t>(want, kFinishSmemCap));
-            zf::k_cdef_finish<<<(int)large_f.size() * zf::kFinClusterHost * zf::kFinLevels, zf::kFinThreadsHost,
-                                smem, st>>>(d_desc, (const int *)(base + o_cf) + small_f.size(), smem);
+            CU(zf::launch_cdef_finish((int)large_f.size() * zf::kFinLevels, cl, smem, st, d_desc,
+                                      (const int *)(base + o_cf) + small_f.size(), (int)smem));
         } }
         TRY(launch_check(ctx, "k_cdef_finish"));
         TRY(check_cancel(ctx));

@@ -20,6 +20,12 @@ __global__ void k_cdef_finish1(FrameDesc *frames, const int *frame_ids);
 int finish1_smem(int nfb, int ncand, int cap);
 constexpr int kFin1ThreadsHost = 1024;
 constexpr int kFinPushPairsHost = 512;  // k_cdef_finish: inbox per rank up to this many pairs
+constexpr int kFinClusterMaxHost = 16;  // k_cdef_finish: non-portable cluster size when allowed
+// k_cdef_finish over `nclusters` clusters of `cl` CTAs (cluster size set at launch).
+cudaError_t launch_cdef_finish(int nclusters, int cl, size_t smem, cudaStream_t st, FrameDesc *frames,
+                               const int *frame_ids, int smem_bytes);
+// 16 when a 16-CTA cluster of k_cdef_finish with `smem` dynamic bytes fits the device, else 8.
+int finish_cluster_size(size_t smem);
 __global__ void k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems);
 
 __global__ void k_lr_sums(FrameDesc *frames, const WorkItem *items, int nitems);
