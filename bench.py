@@ -12,7 +12,9 @@ Wiener search + apply).
          recon and geometry, D2H of the filtered recon and decisions inside
          the timed region).
 
-Two more keys on the same line (N=1 only):
+More keys on the same line (N=1 only):
+  highres_10bit  one 4096x3072 10-bit preset-2 frame per step (u16 planes,
+           20 CDEF candidates, deblock level search, Wiener refinement).
   batched  the 256-image mixed batch (sizes 64..2048, 8/10-bit) as one
            zf_submit_batch per step vs one zf_filter_stage per image on the
            same images (MPix/s each, their ratio, outputs identical),
@@ -462,9 +464,18 @@ def run_highres10(args, ctx, stream, dev):
         if k >= args.warmup:
             times.append(e0.elapsed_time(e1))
     ms = float(np.mean(times))
+    for a, b in zip(rec, rec0):
+        a.copy_(b)
+    torch.cuda.synchronize()
+    ctx.profile(True)
+    ctx.profile_reset()
+    ctx.filter_stage_raw(s, d, st)
+    ctx.sync()
+    kern = {k: round(v[1], 4) for k, v in sorted(ctx.profile_read().items(), key=lambda kv: -kv[1][1])}
+    ctx.profile(False)
     return {"workload": "4096x3072 10-bit 4:2:0 (u16), preset 2, qp 28, device-resident",
             "mpix_per_s": round(f.luma_px / (ms / 1e3) / 1e6, 3), "ms": round(ms, 3),
-            "lf": d.as_dict()["lf"], "cdef_bits": d.as_dict()["cdef_bits"]}
+            "lf": d.as_dict()["lf"], "cdef_bits": d.as_dict()["cdef_bits"], "kernel_ms": kern}
 
 
 def run_batched(args, ctx, stream, dev, frames):
