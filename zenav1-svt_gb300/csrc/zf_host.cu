@@ -603,7 +603,8 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 (L.win == 5 ? wl_st5 : wl_st7).add(i, pl, (int)u, 0, (uh + 2 * half + srows - 1) / srows);
                 wl_unit.add(i, pl, (int)u, 0, 1);
                 if (L.refine) {
-                    wl_trial.add(i, pl, (int)u, 0, 1);  // one CTA per unit: the hill-climb is sequential
+                    // one cluster per unit: the hill-climb is sequential, its trials are not
+                    wl_trial.add(i, pl, (int)u, 0, zf::kTrialClusterHost);
                 } else {
                     const int tl = zf::kTrialTileHost, uw = r.h_end - r.h_start;
                     wl_tiles.add(i, pl, (int)u, 0, ((uw + tl - 1) / tl) * ((uh + tl - 1) / tl));

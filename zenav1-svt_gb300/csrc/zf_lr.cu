@@ -19,6 +19,8 @@
 // same exact value the reference's per-pixel int64 accumulation reaches.
 #include <climits>
 
+#include <cooperative_groups.h>
+
 #include "zf_dev.cuh"
 
 namespace zf {
@@ -609,16 +611,29 @@ __device__ __forceinline__ int wiener_v(const int *tp, const int16_t *vf, int bd
 
 // SSE of the unit filtered with `t` against the source; three parts as in
 // sse_region_hbd. Returns the combined value in thread 0 (all threads get it).
+// The refinement trial runs on a cluster of kTrialCluster CTAs per unit:
+// CTA `rank` filters tiles rank, rank + CL, ... of the unit, the partial SSE
+// parts are pushed into every rank's inbox (double-buffered) before one
+// cluster barrier, and every CTA forms the same total, so the hill-climb
+// decisions stay identical across the cluster.
+constexpr int kTrialCluster = 8;
+
 __device__ int64_t trial_sse(const FrameDesc &f, int plane, const LrPlane &pl, const UnitRect &r, const Taps &t,
-                             uint16_t *stage, uint16_t *tmp, unsigned long long *red) {
+                             uint16_t *stage, uint16_t *tmp, unsigned long long *red,
+                             unsigned long long (*inbox)[kTrialCluster][3], int &buf) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank(), CL = (int)cl.num_blocks();
     const int bd = f.bd, stride = plane_stride(f, plane);
     const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
     const int dw = uw % 16, dh = uh % 16;
     const uint8_t *dg = f.A[plane], *sr = f.S[plane];
     unsigned long long blk = 0, rgt = 0, bot = 0;
     constexpr int SW = TT_W + 7, SH = TT_H + 7;
-    for (int ty = 0; ty < uh; ty += TT_H) {
-        for (int tx = 0; tx < uw; tx += TT_W) {
+    const int ntx = (uw + TT_W - 1) / TT_W, ntiles = ntx * ((uh + TT_H - 1) / TT_H);
+    for (int tile = rank; tile < ntiles; tile += CL) {
+        {
+            const int ty = (tile / ntx) * TT_H, tx = (tile - (tile / ntx) * ntx) * TT_W;
             const int y0 = r.v_start + ty, x0 = r.h_start + tx;
             __syncthreads();
             stage_window(
@@ -659,29 +674,40 @@ __device__ int64_t trial_sse(const FrameDesc &f, int plane, const LrPlane &pl, c
         if ((threadIdx.x & 31) == 0) red[k * 8 + (threadIdx.x >> 5)] = v[k];
     }
     __syncthreads();
-    __shared__ int64_t res;
-    if (threadIdx.x == 0) {
-        unsigned long long s[3] = {0, 0, 0};
-        for (int k = 0; k < 3; ++k)
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s[k] += red[k * 8 + w];
-        res = bd == 8 ? (int64_t)(s[0] + s[1] + s[2]) : (int64_t)s[0] + (int64_t)(uint32_t)s[1] + (int64_t)(uint32_t)s[2];
+    __shared__ unsigned long long mine[3];
+    if (threadIdx.x < 3) {
+        unsigned long long s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x * 8 + w];
+        mine[threadIdx.x] = s;
     }
     __syncthreads();
-    return res;
+    if (threadIdx.x < CL)  // this CTA's parts into rank threadIdx.x's inbox
+        for (int k = 0; k < 3; ++k) *cl.map_shared_rank(&inbox[buf][rank][k], (int)threadIdx.x) = mine[k];
+    cl.sync();
+    unsigned long long sp[3] = {0, 0, 0};
+    for (int q = 0; q < CL; ++q)
+        for (int k = 0; k < 3; ++k) sp[k] += inbox[buf][q][k];
+    buf ^= 1;
+    return bd == 8 ? (int64_t)(sp[0] + sp[1] + sp[2])
+                   : (int64_t)sp[0] + (int64_t)(uint32_t)sp[1] + (int64_t)(uint32_t)sp[2];
 }
 
-__global__ void __launch_bounds__(256) k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems) {
+__global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256)
+    k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems) {
     __shared__ uint16_t stage[(TT_H + 7) * (TT_W + 7)];
     __shared__ uint16_t tmp[(TT_H + 7) * TT_W];
     __shared__ unsigned long long red[24];
+    __shared__ unsigned long long inbox[2][kTrialCluster][3];
     __shared__ Taps t;
-    const WorkItem wi = items[blockIdx.x];
+    int buf = 0;
+    const WorkItem wi = items[find_item(items, nitems, blockIdx.x)];
     FrameDesc &f = frames[wi.frame];
     const LrPlane &pl = f.lr[wi.plane];
     LrUnit &u = pl.units[wi.a];
     const UnitRect r = pl.rects[wi.a];
-    if (u.score > 0) {
-        if (threadIdx.x == 0) u.sse_wn = INT64_MAX;
+    const bool lead = cooperative_groups::this_cluster().block_rank() == 0;
+    if (u.score > 0) {  // uniform over the cluster (one unit)
+        if (lead && threadIdx.x == 0) u.sse_wn = INT64_MAX;
         return;
     }
     if (threadIdx.x < 8) {
@@ -689,7 +715,7 @@ __global__ void __launch_bounds__(256) k_lr_trial(FrameDesc *frames, const WorkI
         t.h[threadIdx.x] = u.hf[threadIdx.x];
     }
     __syncthreads();
-    int64_t err = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red);
+    int64_t err = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red, inbox, buf);
     if (pl.refine) {
         // use_refinement with max_one_refinement_step: one step size (4).
         const int plane_off = (7 - pl.win) >> 1;
@@ -708,7 +734,7 @@ __global__ void __launch_bounds__(256) k_lr_trial(FrameDesc *frames, const WorkI
                         fp[3] += 2 * s;
                     }
                     __syncthreads();
-                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red);
+                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red, inbox, buf);
                     if (e2 > err) {
                         __syncthreads();
                         if (threadIdx.x == 0) {
@@ -732,7 +758,7 @@ __global__ void __launch_bounds__(256) k_lr_trial(FrameDesc *frames, const WorkI
                         fp[3] -= 2 * s;
                     }
                     __syncthreads();
-                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red);
+                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red, inbox, buf);
                     if (e2 > err) {
                         __syncthreads();
                         if (threadIdx.x == 0) {
@@ -749,7 +775,7 @@ __global__ void __launch_bounds__(256) k_lr_trial(FrameDesc *frames, const WorkI
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (lead && threadIdx.x == 0) {
         u.sse_wn = err;
         for (int i = 0; i < 8; ++i) {
             u.vf[i] = t.v[i];
