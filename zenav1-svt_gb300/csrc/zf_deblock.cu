@@ -243,48 +243,74 @@ __device__ void db_load(const DbTile &t, const uint8_t *plane, uint16_t *reg) {
     }
 }
 
-// Edge lengths of a tile: vl[band][edge] for vertical edges over the region
-// rows, hl[col band][edge] for horizontal edges over the tile columns.
-__device__ void db_params(const DbTile &t, int lvl_v, int lvl_h, uint8_t *vl, uint8_t *hl) {
+// The filtering edges of a tile, bucketed by filter length (4, 6, 8, 14):
+// v[bucket][k] = band * DB_EDGES + edge for vertical edges over the region
+// rows, h[bucket][k] = column band * DB_EDGES + edge for horizontal edges
+// over the tile columns. Edges within a pass are independent, so each
+// bucket runs with every thread on one compile-time filter length.
+struct DbEdges {
+    uint16_t v[4][DB_BANDS * DB_EDGES];
+    uint16_t h[4][(DB_T / 4) * DB_EDGES];
+    int nv[4], nh[4];
+};
+__device__ __forceinline__ int len_bucket(int len) { return len == 4 ? 0 : len == 6 ? 1 : len == 8 ? 2 : 3; }
+
+// Every thread of the CTA calls this; the lists are complete after the
+// caller's next barrier.
+__device__ void db_params(const DbTile &t, int lvl_v, int lvl_h, DbEdges &E) {
     const FrameDesc &f = *t.f;
+    if (threadIdx.x < 4) E.nv[threadIdx.x] = E.nh[threadIdx.x] = 0;
+    __syncthreads();
     for (int i = threadIdx.x; i < DB_BANDS * DB_EDGES; i += blockDim.x) {
         int band = i / DB_EDGES, e = i - band * DB_EDGES;
         int y = t.y0 - DB_H + band * 4, x = t.x0 - 4 + e * 4;
         int len = 0;
         if (y >= 0 && y < t.ph && x >= 0 && x < t.pw) len = edge_len(f, true, x, y, t.plane, lvl_v);
-        vl[i] = (uint8_t)len;
+        if (len) {
+            const int bk = len_bucket(len);
+            E.v[bk][atomicAdd(&E.nv[bk], 1)] = (uint16_t)i;
+        }
     }
     for (int i = threadIdx.x; i < (DB_T / 4) * DB_EDGES; i += blockDim.x) {
         int cb = i / DB_EDGES, e = i - cb * DB_EDGES;
         int x = t.x0 + cb * 4, y = t.y0 - 4 + e * 4;
         int len = 0;
         if (y >= 0 && y < t.ph && x >= 0 && x < t.pw) len = edge_len(f, false, x, y, t.plane, lvl_h);
-        hl[i] = (uint8_t)len;
+        if (len) {
+            const int bk = len_bucket(len);
+            E.h[bk][atomicAdd(&E.nh[bk], 1)] = (uint16_t)i;
+        }
+    }
+}
+
+__device__ __forceinline__ void filter_bucket(int bk, uint16_t *p, int st, Thr t, int bd) {
+    switch (bk) {  // a constant length per call site after inlining
+        case 0: filter_line(p, st, 4, t, bd); break;
+        case 1: filter_line(p, st, 6, t, bd); break;
+        case 2: filter_line(p, st, 8, t, bd); break;
+        default: filter_line(p, st, 14, t, bd); break;
     }
 }
 
 // Both passes on the region in shared memory.
-__device__ void db_filter(const DbTile &t, uint16_t *reg, const uint8_t *vl, const uint8_t *hl, int lvl_v,
-                          int lvl_h) {
+__device__ void db_filter(const DbTile &t, uint16_t *reg, const DbEdges &E, int lvl_v, int lvl_h) {
     const int bd = t.f->bd, sharp = t.f->sharpness;
     const Thr tv = lf_thresholds(lvl_v, sharp), th = lf_thresholds(lvl_h, sharp);
-    for (int i = threadIdx.x; i < DB_BANDS * DB_EDGES * 4; i += blockDim.x) {
-        int be = i >> 2, line = i & 3;
-        int len = vl[be];
-        if (!len) continue;
-        int band = be / DB_EDGES, e = be - band * DB_EDGES;
-        int ry = band * 4 + line, rx = DB_H - 4 + e * 4;
-        filter_line(reg + ry * DB_R + rx, 1, len, tv, bd);
-    }
+    for (int bk = 0; bk < 4; ++bk)
+        for (int i = threadIdx.x; i < E.nv[bk] * 4; i += blockDim.x) {
+            const int be = E.v[bk][i >> 2], line = i & 3;
+            const int band = be / DB_EDGES, e = be - band * DB_EDGES;
+            const int ry = band * 4 + line, rx = DB_H - 4 + e * 4;
+            filter_bucket(bk, reg + ry * DB_R + rx, 1, tv, bd);
+        }
     __syncthreads();
-    for (int i = threadIdx.x; i < (DB_T / 4) * DB_EDGES * 4; i += blockDim.x) {
-        int be = i >> 2, line = i & 3;
-        int len = hl[be];
-        if (!len) continue;
-        int cb = be / DB_EDGES, e = be - cb * DB_EDGES;
-        int rx = DB_H + cb * 4 + line, ry = DB_H - 4 + e * 4;
-        filter_line(reg + ry * DB_R + rx, DB_R, len, th, bd);
-    }
+    for (int bk = 0; bk < 4; ++bk)
+        for (int i = threadIdx.x; i < E.nh[bk] * 4; i += blockDim.x) {
+            const int be = E.h[bk][i >> 2], line = i & 3;
+            const int cb = be / DB_EDGES, e = be - cb * DB_EDGES;
+            const int rx = DB_H + cb * 4 + line, ry = DB_H - 4 + e * 4;
+            filter_bucket(bk, reg + ry * DB_R + rx, DB_R, th, bd);
+        }
     __syncthreads();
 }
 
@@ -298,7 +324,7 @@ __device__ __forceinline__ void plane_geom(const FrameDesc &f, int plane, int *p
 // plane needs its own level.
 __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, const WorkItem *items, int nitems) {
     __shared__ __align__(16) uint16_t reg[DB_R * DB_R];
-    __shared__ uint8_t vl[DB_BANDS * DB_EDGES], hl[(DB_T / 4) * DB_EDGES];
+    __shared__ DbEdges edges;
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
     const FrameDesc &f = frames[wi.frame];
@@ -342,9 +368,9 @@ __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, 
         return;
     }
     db_load(t, f.IN[plane], reg);
-    db_params(t, lv, lh, vl, hl);
+    db_params(t, lv, lh, edges);
     __syncthreads();
-    db_filter(t, reg, vl, hl, lv, lh);
+    db_filter(t, reg, edges, lv, lh);
     if (word_ok(f.B[plane])) {
         for (int i = threadIdx.x; i < DB_T * wpr; i += blockDim.x) {
             const int ty = i >> lgw, wx = i & (wpr - 1);
@@ -370,7 +396,7 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
                                                      const int *levels, unsigned long long *sse) {
     __shared__ __align__(16) uint16_t reg[DB_R * DB_R];
     __shared__ __align__(16) uint16_t pristine[DB_R * DB_R];
-    __shared__ uint8_t vl[DB_BANDS * DB_EDGES], hl[(DB_T / 4) * DB_EDGES];
+    __shared__ DbEdges edges;
     __shared__ unsigned long long part[8];
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
@@ -384,7 +410,7 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
     const int bd = f.bd;
     db_load(t, f.IN[plane], pristine);
     // edge lengths do not depend on a nonzero level: computed once
-    if (levels[slot * 2] > 0 || levels[slot * 2 + 1] > 0) db_params(t, 1, 1, vl, hl);
+    if (levels[slot * 2] > 0 || levels[slot * 2 + 1] > 0) db_params(t, 1, 1, edges);
     __syncthreads();
     const int spw = bd == 8 ? 4 : 2, wpr = DB_T / spw, lgw = bd == 8 ? 4 : 5;  // wpr = 1 << lgw
     const bool words = word_ok(f.S[plane]);
@@ -394,7 +420,7 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
         for (int i = threadIdx.x; i < DB_R * DB_R / 2; i += blockDim.x)
             reinterpret_cast<uint32_t *>(reg)[i] = reinterpret_cast<const uint32_t *>(pristine)[i];
         __syncthreads();
-        if (lvl != 0) db_filter(t, reg, vl, hl, lvl, lvl);
+        if (lvl != 0) db_filter(t, reg, edges, lvl, lvl);
         unsigned long long acc = 0;
         if (words) {
             for (int i = threadIdx.x; i < DB_T * wpr; i += blockDim.x) {
