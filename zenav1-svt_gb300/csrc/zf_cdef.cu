@@ -955,6 +955,307 @@ __global__ void __launch_bounds__(kFin1Threads, 1) k_cdef_finish1(FrameDesc *fra
     }
 }
 
+// ---- finish for the small candidate sets (4 or 6 candidates: presets 4-6)
+//
+// One kJointThreads-thread CTA per (frame, bit count), no cluster. Thread t
+// owns the filter blocks t + r * kJointThreads (r < RPT) and their rows stay
+// in shared memory at R[k][r * kJointThreads + t]; a block without a row (or
+// past the frame) is a zero row, which adds 0 to every total, so rows need
+// no compaction. The costs of the strengths in the current set are a shift
+// register per owned row in registers: the best over the set (the reference's
+// per-row `best`) costs a few register mins, not a pass over the set.
+//
+// Bounds: a row's luma entry is below 2^28 (<= 4096 px x 1023^2 >> 4, or x
+// 255^2 at 8 bits, the subsampled sum times sub never exceeding the full
+// block) and its joint chroma entry below 2^27, so a pair cost is below
+// 3 * 2^27 and up to 5 rows per thread sum exactly in u32 -- two lanes of
+// such sums still fit u32, the first reduce stage stays 32-bit.
+//
+// One step: per thread the NC^2 pair totals over its rows (min(l + c, best)
+// by one add-min), a warp reduce-scatter that leaves each pair's warp sum in
+// a lane, one partial per (warp, pair) in shared memory, a barrier, the sums
+// and argmin in warp 0 (strict <, lowest pair index on ties), a barrier.
+constexpr int kJointThreads = 512;
+constexpr int kJointWarps = kJointThreads / 32;
+
+// Warp reduce-scatter of N u32 values held by every lane (N = 4, 16 or 32;
+// each value below 2^31): the sum over the warp of value i is written to
+// out[i] by the lanes that end up holding it.
+template <int N>
+__device__ __forceinline__ void warp_scatter_sum(const uint32_t *v, int lane, unsigned long long *out) {
+    static_assert(N == 4 || N == 16 || N == 32, "N");
+    constexpr int H = N / 2;
+    unsigned long long b[H];
+    int idx = 0;
+    {
+        const bool up = (lane & 16) != 0;
+#pragma unroll
+        for (int i = 0; i < H; ++i) {
+            const uint32_t s = up ? v[i] : v[i + H], k = up ? v[i + H] : v[i];
+            b[i] = (unsigned long long)(k + __shfl_xor_sync(0xffffffffu, s, 16));
+        }
+        if (up) idx += H;
+    }
+#pragma unroll
+    for (int st = 0; st < 4; ++st) {
+        const int o = 8 >> st, n = H >> st;  // values held before this stage
+        if (n > 1) {
+            const int h = n >> 1;
+            const bool up = (lane & o) != 0;
+#pragma unroll
+            for (int i = 0; i < h; ++i) {
+                const unsigned long long s = up ? b[i] : b[i + h], k = up ? b[i + h] : b[i];
+                b[i] = k + __shfl_xor_sync(0xffffffffu, s, o);
+            }
+            if (up) idx += h;
+        } else {
+            b[0] += __shfl_xor_sync(0xffffffffu, b[0], o);
+        }
+    }
+    out[idx] = b[0];  // lanes holding the same index write the same sum
+}
+
+// joint_strength_search_dual (cdef.rs:866-885) for nb = NB strengths over
+// the CTA's rows; returns the last step's total and leaves the strengths in
+// lev[0][0..NB) (luma) and lev[1][0..NB) (chroma).
+template <int NC, int RPT, int NB>
+__device__ __forceinline__ unsigned long long joint_search(const uint32_t *R, unsigned long long *part,
+                                                           uint8_t (*lev)[16], int *spick,
+                                                           unsigned long long *sres) {
+    constexpr int P = NC * NC, T = kJointThreads, S = T * RPT;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint32_t pc[RPT][NB];  // costs of the set's strengths, oldest first
+    uint32_t bg[RPT];      // greedy phase: best over the strengths picked so far
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        bg[r] = 0xffffffffu;
+#pragma unroll
+        for (int g = 0; g < NB; ++g) pc[r][g] = 0;
+    }
+    unsigned long long tt = 1ull << 63;
+    for (int step = 0; step < 5 * NB; ++step) {
+        const bool refine = step >= NB;
+        uint32_t acc[P];
+#pragma unroll
+        for (int p = 0; p < P; ++p) acc[p] = 0;
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) {
+            // refinement: the set is the newest NB - 1 strengths (the
+            // reference drops its oldest before the search)
+            uint32_t bst = bg[r];
+            if (refine) {
+                bst = 0xffffffffu;
+#pragma unroll
+                for (int g = 1; g < NB; ++g) bst = min(bst, pc[r][g]);
+            }
+            uint32_t rl[NC], rc[NC];
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                rl[k] = R[k * S + r * T + t];
+                rc[k] = R[(NC + k) * S + r * T + t];
+            }
+#pragma unroll
+            for (int j = 0; j < NC; ++j)
+#pragma unroll
+                for (int k = 0; k < NC; ++k) acc[j * NC + k] += __viaddmin_u32(rl[j], rc[k], bst);
+        }
+        if constexpr (P == 16) {
+            warp_scatter_sum<16>(acc, lane, part + warp * P);
+        } else {
+            warp_scatter_sum<32>(acc, lane, part + warp * P);
+            warp_scatter_sum<4>(acc + 32, lane, part + warp * P + 32);
+        }
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long bv = ~0ull;
+            int bi = 0x7fffffff;
+            for (int p = lane; p < P; p += 32) {
+                unsigned long long v = 0;
+#pragma unroll
+                for (int w = 0; w < kJointWarps; ++w) v += part[w * P + p];
+                if (v < bv) {  // p increases along a lane: strict < keeps the lowest
+                    bv = v;
+                    bi = p;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov < bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (bv >= (1ull << 63)) {  // best_tot starts at 1 << 63 with strict <
+                bi = 0;
+                bv = 1ull << 63;
+            }
+            if (lane == 0) {
+                *spick = bi;
+                *sres = bv;
+                const int slot = refine ? NB - 1 : step;
+                if (refine)
+                    for (int g = 0; g < NB - 1; ++g) {
+                        lev[0][g] = lev[0][g + 1];
+                        lev[1][g] = lev[1][g + 1];
+                    }
+                lev[0][slot] = (uint8_t)(bi / NC);
+                lev[1][slot] = (uint8_t)(bi % NC);
+            }
+        }
+        __syncthreads();
+        const int bi = *spick, j = bi / NC, k = bi - j * NC;
+        tt = *sres;
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) {
+            const uint32_t c = R[j * S + r * T + t] + R[(NC + k) * S + r * T + t];
+            bg[r] = min(bg[r], c);
+#pragma unroll
+            for (int g = 0; g + 1 < NB; ++g) pc[r][g] = pc[r][g + 1];
+            pc[r][NB - 1] = c;
+        }
+    }
+    return tt;
+}
+
+template <int NC, int RPT>
+__global__ void __launch_bounds__(kJointThreads, 1) k_cdef_joint(FrameDesc *frames, const int *frame_ids) {
+    extern __shared__ __align__(16) unsigned char joint_dyn[];
+    constexpr int T = kJointThreads, S = T * RPT, P = NC * NC;
+    __shared__ unsigned long long part[kJointWarps * P];
+    __shared__ uint8_t lev[2][16];
+    __shared__ unsigned long long res_v;
+    __shared__ int pick, last_flag, best_bits;
+    const int level = blockIdx.x % kFinLevels;
+    FrameDesc &f = frames[frame_ids[blockIdx.x / kFinLevels]];
+    CdefParams &cp = f.cdef;
+    if (cp.mode != 1) return;
+    const int nfb = f.nhfb * f.nvfb, n2 = 2 * NC, t = threadIdx.x;
+    uint32_t *R = reinterpret_cast<uint32_t *>(joint_dyn);  // R[k * S + slot]
+    int sb = 0;
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        const int fb = r * T + t;
+        const bool row = fb < nfb && f.fb_row[fb];
+        const uint64_t *m = f.mse + (int64_t)fb * n2;
+#pragma unroll
+        for (int k = 0; k < 2 * NC; ++k) R[k * S + fb] = row ? (uint32_t)m[k] : 0u;
+        sb += __syncthreads_count(row);
+    }
+    if (sb == 0) {  // every filter block all-skip: cdef.rs:282-288
+        if (level == 0) {
+            for (int fb = t; fb < nfb; fb += T) f.fb_idx[fb] = 0;
+            if (t == 0) {
+                cp.bits = 0;
+                cp.y_str[0] = 0;
+                cp.uv_str[0] = 0;
+            }
+        }
+        return;
+    }
+    if (t < 16) lev[0][t] = lev[1][t] = 0;
+    __syncthreads();
+    unsigned long long tt;
+    switch (level) {
+        case 0: tt = joint_search<NC, RPT, 1>(R, part, lev, &pick, &res_v); break;
+        case 1: tt = joint_search<NC, RPT, 2>(R, part, lev, &pick, &res_v); break;
+        case 2: tt = joint_search<NC, RPT, 4>(R, part, lev, &pick, &res_v); break;
+        default: tt = joint_search<NC, RPT, 8>(R, part, lev, &pick, &res_v); break;
+    }
+    const int nb = 1 << level;
+    if (t == 0) {
+        const unsigned long long total_bits = (unsigned long long)sb * level + nb * 12;
+        f.fin_cost[level] = rdc(cp.lambda, total_bits << 9, tt * 16);
+        for (int k = 0; k < 8; ++k) {
+            f.fin_lev[level][k] = k < nb ? lev[0][k] : 0;
+            f.fin_lev[level][8 + k] = k < nb ? lev[1][k] : 0;
+        }
+        __threadfence();
+        last_flag = atomicAdd(&f.fin_done, 1) == kFinLevels - 1;
+    }
+    __syncthreads();
+    if (!last_flag) return;
+    __threadfence();
+    if (t == 0) {
+        unsigned long long best_cost = 1ull << 63;
+        int bb = 0;
+        for (int i = 0; i < kFinLevels; ++i) {
+            const unsigned long long c = __ldcg(&f.fin_cost[i]);
+            if (c < best_cost) {
+                best_cost = c;
+                bb = i;
+            }
+        }
+        best_bits = bb;
+        for (int k = 0; k < 16; ++k) lev[k >> 3][k & 7] = *(volatile uint8_t *)&f.fin_lev[bb][k];
+    }
+    __syncthreads();
+    const int bnb = 1 << best_bits;
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        const int fb = r * T + t;
+        if (fb >= nfb) continue;
+        int best_gi = 0;
+        if (f.fb_row[fb]) {
+            unsigned long long bst = ~0ull;
+            for (int gi = 0; gi < bnb; ++gi) {
+                const unsigned long long c = (unsigned long long)R[lev[0][gi] * S + fb] + R[(NC + lev[1][gi]) * S + fb];
+                if (c < bst) {
+                    bst = c;
+                    best_gi = gi;
+                }
+            }
+        }
+        f.fb_idx[fb] = (uint8_t)best_gi;
+    }
+    if (t == 0) {
+        cp.bits = best_bits;
+        for (int gi = 0; gi < 8; ++gi) {
+            cp.y_str[gi] = gi < bnb ? (uint8_t)cp.fs[lev[0][gi]] : 0;
+            cp.uv_str[gi] = gi < bnb ? (uint8_t)cp.fs[lev[1][gi]] : 0;
+        }
+    }
+}
+
+// Rows per thread k_cdef_joint needs for a frame: 1, 2 or 4; 0 when the
+// frame is outside its range (other candidate counts, more filter blocks).
+int joint_rows_per_thread(int nfb, int ncand) {
+    if (ncand != 4 && ncand != 6) return 0;
+    for (int rpt = 1; rpt <= 4; rpt *= 2)
+        if (nfb <= rpt * kJointThreads) return rpt;
+    return 0;
+}
+
+size_t joint_smem(int ncand, int rpt) { return (size_t)2 * ncand * kJointThreads * rpt * 4; }
+
+cudaError_t launch_cdef_joint(int ncand, int rpt, int nframes, cudaStream_t st, FrameDesc *frames,
+                              const int *frame_ids) {
+    const size_t smem = joint_smem(ncand, rpt);
+    const dim3 grid((unsigned)(nframes * kFinLevels));
+#define ZF_JOINT(NC, RPT)                                                                              \
+    if (ncand == NC && rpt == RPT) {                                                                   \
+        k_cdef_joint<NC, RPT><<<grid, kJointThreads, smem, st>>>(frames, frame_ids);                   \
+        return cudaGetLastError();                                                                     \
+    }
+    ZF_JOINT(4, 1) ZF_JOINT(4, 2) ZF_JOINT(4, 4) ZF_JOINT(6, 1) ZF_JOINT(6, 2) ZF_JOINT(6, 4)
+#undef ZF_JOINT
+    return cudaErrorInvalidValue;
+}
+
+// Opt k_cdef_joint's instantiations into their dynamic shared memory.
+cudaError_t joint_set_attributes() {
+    cudaError_t e = cudaSuccess;
+#define ZF_JOINT_ATTR(NC, RPT)                                                                              \
+    if (e == cudaSuccess)                                                                                   \
+        e = cudaFuncSetAttribute(k_cdef_joint<NC, RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,        \
+                                 (int)joint_smem(NC, RPT));
+    ZF_JOINT_ATTR(4, 1) ZF_JOINT_ATTR(4, 2) ZF_JOINT_ATTR(4, 4) ZF_JOINT_ATTR(6, 1) ZF_JOINT_ATTR(6, 2)
+    ZF_JOINT_ATTR(6, 4)
+#undef ZF_JOINT_ATTR
+    return e;
+}
+
 // Launch k_cdef_finish for `nclusters` (frame, bit count) clusters of `cl`
 // CTAs (the cluster size is a launch attribute; 16 needs the non-portable
 // attribute, set once per device by finish_cluster_size).

@@ -352,6 +352,11 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) & ~(a - 1); }
 constexpr size_t kFinishSmemCap = 160 * 1024;
 constexpr int kFinish1SmemCap = 200 * 1024;
 constexpr int kFinish1MaxFb = 1024;  // filter blocks (a 2048x2048 frame)
+// k_cdef_joint launch groups: (4 or 6 candidates) x (1, 2 or 4 rows per thread)
+constexpr int kJointGroups = 6;
+int joint_group(int ncand, int rpt) { return (ncand == 6 ? 3 : 0) + (rpt == 4 ? 2 : rpt == 2 ? 1 : 0); }
+int joint_group_ncand(int g) { return g < 3 ? 4 : 6; }
+int joint_group_rpt(int g) { return 1 << (g % 3); }
 // k_lr_finish: 32 B per unit plus the pair table of <= 200 units (or 32 B
 // per unit alone for larger planes; 4096 units at most)
 constexpr int kLrFinishSmemCap = 160 * 1024;
@@ -364,6 +369,7 @@ cudaError_t set_kernel_attributes() {
         e = cudaFuncSetAttribute(zf::k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFinishSmemCap);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(zf::k_lr_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kLrFinishSmemCap);
+    if (e == cudaSuccess) e = zf::joint_set_attributes();
     return e;
 }
 
@@ -578,6 +584,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     // Work lists (host-known shapes).
     WorkList wl_db, wl_cs, wl_ca, wl_sum, wl_st5, wl_st7, wl_unit, wl_apply, wl_trial, wl_tiles;
     std::vector<int> cdef_small, cdef_large;  // joint search: one CTA / cluster per bit count
+    std::vector<int> cdef_joint[kJointGroups];  // register-row joint search, by (candidates, rows per thread)
     for (int i = 0; i < n; ++i) {
         Plan &p = plans[i];
         for (int pl = 0; pl < p.nplanes; ++pl) {
@@ -586,9 +593,11 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         }
         if (p.d.cdef.mode == 1 && !run.cdef_given) {
             wl_cs.add(i, 0, 0, 0, p.nfb);
+            const int rpt = zf::joint_rows_per_thread(p.nfb, p.d.cdef.ncand);
             const bool small = p.nfb <= kFinish1MaxFb &&
                                zf::finish1_smem(p.nfb, p.d.cdef.ncand, kFinish1SmemCap) > 0;
-            (small ? cdef_small : cdef_large).push_back(i);
+            if (rpt) cdef_joint[joint_group(p.d.cdef.ncand, rpt)].push_back(i);
+            else (small ? cdef_small : cdef_large).push_back(i);
         }
         wl_ca.add(i, 0, 0, 0, p.nfb);
         for (int pl = 0; pl < 3; ++pl) {
@@ -634,7 +643,12 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             if (canvas_h > L.ph) wl_apply.add(i, pl, -1, nstripes, ntiles);
         }
     }
-    std::vector<int> cdef_frames(cdef_small);
+    // finish frame ids: the joint groups in order, then the small frames,
+    // then the large ones
+    std::vector<int> cdef_frames;
+    for (const std::vector<int> &g : cdef_joint) cdef_frames.insert(cdef_frames.end(), g.begin(), g.end());
+    const int n_joint = (int)cdef_frames.size();
+    cdef_frames.insert(cdef_frames.end(), cdef_small.begin(), cdef_small.end());
     cdef_frames.insert(cdef_frames.end(), cdef_large.begin(), cdef_large.end());
     const int n_small = (int)cdef_small.size();
     // Arena: per-frame buffers | unit accumulators | metadata image |
@@ -885,22 +899,30 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         CU(zf::launch_cdef_search(fp, ns, wl_cs.ctas, st, d_desc, (const WorkItem *)(base + o_cs),
                                   (int)wl_cs.items.size())); }
         TRY(launch_check(ctx, "k_cdef_search"));
-        // Joint search: frames of up to kFinish1MaxFb filter blocks whose rows
-        // fit one CTA's shared memory run one CTA per (frame, bit count);
-        // larger frames an 8-CTA cluster per (frame, bit count), which wins
-        // once the per-step row sums outweigh the cluster barrier.
-        // (cdef_frames lists the small frames first, n_small of them)
+        // Joint search: frames with 4 or 6 candidates and up to 2048 filter
+        // blocks run k_cdef_joint, one CTA per (frame, bit count) and one
+        // launch per (candidates, rows per thread) group; other frames of up
+        // to kFinish1MaxFb filter blocks whose rows fit one CTA's shared
+        // memory run k_cdef_finish1; larger frames a cluster per (frame, bit
+        // count), which wins once the per-step row sums outweigh the cluster
+        // barrier. (cdef_frames lists the joint groups, then the small
+        // frames, then the large ones)
         int smem1 = 0;
-        for (int k = 0; k < n_small; ++k) {
+        for (int k = n_joint; k < n_joint + n_small; ++k) {
             const Plan &pf = plans[cdef_frames[k]];
             smem1 = std::max(smem1, zf::finish1_smem(pf.nfb, pf.d.cdef.ncand, kFinish1SmemCap));
         }
-        const std::vector<int> small_f(cdef_frames.begin(), cdef_frames.begin() + n_small),
-            large_f(cdef_frames.begin() + n_small, cdef_frames.end());
+        const std::vector<int> small_f(cdef_frames.begin() + n_joint, cdef_frames.begin() + n_joint + n_small),
+            large_f(cdef_frames.begin() + n_joint + n_small, cdef_frames.end());
         { LaunchScope ls_(ctx, "k_cdef_finish");
+        for (int g = 0, off = 0; g < kJointGroups; off += (int)cdef_joint[g].size(), ++g) {
+            if (cdef_joint[g].empty()) continue;
+            CU(zf::launch_cdef_joint(joint_group_ncand(g), joint_group_rpt(g), (int)cdef_joint[g].size(), st,
+                                     d_desc, (const int *)(base + o_cf) + off));
+        }
         if (!small_f.empty()) {
             zf::k_cdef_finish1<<<(int)small_f.size() * zf::kFinLevels, zf::kFin1ThreadsHost, smem1, st>>>(
-                d_desc, (const int *)(base + o_cf));
+                d_desc, (const int *)(base + o_cf) + n_joint);
         }
         if (!large_f.empty()) {
             // dynamic shared memory: the double-buffered pair partials (an
@@ -924,7 +946,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 smem = need(cl);
             }
             CU(zf::launch_cdef_finish((int)large_f.size() * zf::kFinLevels, cl, smem, st, d_desc,
-                                      (const int *)(base + o_cf) + small_f.size(), (int)smem));
+                                      (const int *)(base + o_cf) + n_joint + small_f.size(), (int)smem));
         } }
         TRY(launch_check(ctx, "k_cdef_finish"));
         TRY(check_cancel(ctx));

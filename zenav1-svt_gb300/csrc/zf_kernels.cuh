@@ -26,6 +26,14 @@ cudaError_t launch_cdef_finish(int nclusters, int cl, size_t smem, cudaStream_t 
                                const int *frame_ids, int smem_bytes);
 // 16 when a 16-CTA cluster of k_cdef_finish with `smem` dynamic bytes fits the device, else 8.
 int finish_cluster_size(size_t smem);
+// k_cdef_joint (one CTA per (frame, bit count), rows in registers' reach):
+// rows per thread for a frame (1, 2 or 4; 0 when the frame is outside its
+// range), the launch over `nframes` frames of one (ncand, rpt) group, and
+// the dynamic shared memory opt-in (once per device).
+int joint_rows_per_thread(int nfb, int ncand);
+cudaError_t launch_cdef_joint(int ncand, int rpt, int nframes, cudaStream_t st, FrameDesc *frames,
+                              const int *frame_ids);
+cudaError_t joint_set_attributes();
 __global__ void k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems);
 
 __global__ void k_lr_sums(FrameDesc *frames, const WorkItem *items, int nitems);
