@@ -24,7 +24,7 @@ struct UnitRect {
 
 // Per-unit Wiener state, written by the stats/solve/trial/finish kernels.
 struct LrUnit {
-    int64_t sum;                // sum of dgd over the unit (find_average numerator)
+    int64_t sum_src;            // sum of src over the unit
     unsigned long long sse_blk; // sse_region parts: 16x16 blocks, right strip,
     unsigned long long sse_rgt; // bottom strip (the strips are truncated to
     unsigned long long sse_bot; // u32 at 10 bits, restoration.rs:1991-2036)
@@ -32,8 +32,13 @@ struct LrUnit {
     int64_t sse_wn;             // trial SSE, INT64_MAX when the score reverts
     unsigned long long tw_blk, tw_rgt, tw_bot;  // tiled trial SSE parts (no refinement)
     int64_t score;
-    int64_t m[49];              // M, raw sums (before the bit-depth divider)
-    int64_t h[2401];            // H upper triangle, row-major win2 x win2
+    // Raw-sample sums (before the average correction and the bit-depth
+    // divider): M, the H upper triangle (row-major win2 x win2) and the dgd
+    // sums over the unit rectangle shifted by each window offset (the
+    // centre one is the find_average numerator).
+    int64_t m[49];
+    int64_t h[2401];
+    int64_t s[49];
     int32_t vd[7], hd[7];
     int16_t vf[8], hf[8];
     int32_t rtype;

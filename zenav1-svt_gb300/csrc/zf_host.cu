@@ -582,7 +582,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         plans[i].out = outs ? &outs[i] : nullptr;
     }
     // Work lists (host-known shapes).
-    WorkList wl_db, wl_cs, wl_ca, wl_sum, wl_st5, wl_st7, wl_unit, wl_apply, wl_trial, wl_tiles;
+    WorkList wl_db, wl_cs, wl_ca, wl_st5, wl_st7, wl_unit, wl_apply, wl_trial, wl_tiles;
     std::vector<int> cdef_small, cdef_large;  // joint search: one CTA / cluster per bit count
     std::vector<int> cdef_joint[kJointGroups];  // register-row joint search, by (candidates, rows per thread)
     for (int i = 0; i < n; ++i) {
@@ -607,7 +607,6 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 const UnitRect &r = p.rects[pl][u];
                 const int uh = r.v_end - r.v_start;
                 // one item per unit; the CTA offset selects the row block
-                wl_sum.add(i, pl, (int)u, 0, (uh + zf::kSumRowsHost - 1) / zf::kSumRowsHost);
                 const int half = L.win / 2, srows = zf::stat_rows_host(L.win);
                 (L.win == 5 ? wl_st5 : wl_st7).add(i, pl, (int)u, 0, (uh + 2 * half + srows - 1) / srows);
                 wl_unit.add(i, pl, (int)u, 0, 1);
@@ -664,9 +663,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     };
     const size_t desc_bytes = (size_t)n * sizeof(FrameDesc);
     const size_t m_desc = mtake(desc_bytes);
-    constexpr int kLists = 10;
-    const WorkList *lists[kLists] = {&wl_db,  &wl_cs,   &wl_ca,    &wl_sum,   &wl_st5,
-                                     &wl_st7, &wl_unit, &wl_apply, &wl_trial, &wl_tiles};
+    constexpr int kLists = 9;
+    const WorkList *lists[kLists] = {&wl_db,   &wl_cs,    &wl_ca,    &wl_st5,  &wl_st7,
+                                     &wl_unit, &wl_apply, &wl_trial, &wl_tiles};
     size_t m_list[kLists];
     for (int k = 0; k < kLists; ++k) m_list[k] = mtake(lists[k]->items.size() * sizeof(WorkItem));
     const size_t m_cf = mtake(cdef_frames.size() * 4);
@@ -692,9 +691,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     for (auto &p : plans) bind_pointers(p, base, base + o_units, base + o_meta + m_rects, base + o_out);
     FrameDesc *d_desc = (FrameDesc *)(base + o_meta + m_desc);
     const size_t o_db = o_meta + m_list[0], o_cs = o_meta + m_list[1], o_ca = o_meta + m_list[2],
-                 o_sum = o_meta + m_list[3], o_st5 = o_meta + m_list[4], o_st7 = o_meta + m_list[5],
-                 o_unit = o_meta + m_list[6], o_apply = o_meta + m_list[7], o_trial = o_meta + m_list[8],
-                 o_tiles = o_meta + m_list[9], o_cf = o_meta + m_cf;
+                 o_st5 = o_meta + m_list[3], o_st7 = o_meta + m_list[4], o_unit = o_meta + m_list[5],
+                 o_apply = o_meta + m_list[6], o_trial = o_meta + m_list[7], o_tiles = o_meta + m_list[8],
+                 o_cf = o_meta + m_cf;
     // outputs start zeroed (statistics counters, fb_idx of skipped searches)
     CU(cudaMemsetAsync(base + o_out, 0, out_bytes, st));
 
@@ -961,12 +960,6 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     // ---- Wiener search on A
     if ((run.stages & STG_LR_SEARCH) && !run.lr_given) {
         if (ucur) CU(cudaMemsetAsync(base + o_units, 0, ucur, st));
-        if (wl_sum.ctas) {
-            { LaunchScope ls_(ctx, "k_lr_sums");
-            zf::k_lr_sums<<<wl_sum.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_sum),
-                                                      (int)wl_sum.items.size()); }
-            TRY(launch_check(ctx, "k_lr_sums"));
-        }
         if (wl_st5.ctas) {
             LaunchScope ls5_(ctx, "k_lr_stats5");
             CU(zf::launch_lr_stats(5, wl_st5.ctas, st, d_desc, (const WorkItem *)(base + o_st5),

@@ -36,7 +36,6 @@ cudaError_t launch_cdef_joint(int ncand, int rpt, int nframes, cudaStream_t st, 
 cudaError_t joint_set_attributes();
 __global__ void k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems);
 
-__global__ void k_lr_sums(FrameDesc *frames, const WorkItem *items, int nitems);
 cudaError_t launch_lr_stats(int win, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
                             int nitems);
 __global__ void k_lr_solve(FrameDesc *frames, const WorkItem *items, int nitems);
@@ -54,7 +53,6 @@ int describe_cdef_frame(const zf_frame *f, FrameDesc *d);
 
 constexpr int kFinClusterHost = 8;  // k_cdef_finish: CTAs per cluster
 constexpr int kFinThreadsHost = 512;
-constexpr int kSumRowsHost = 16;   // k_lr_sums rows per CTA
 // k_lr_stats<win>: rows per CTA over the unit's rows extended by win/2 on
 // both sides (one thread per (row, row offset) plus one per (row, window row))
 constexpr int stat_rows_host(int win) { return 256 / (3 * win - 1); }

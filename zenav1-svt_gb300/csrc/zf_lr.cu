@@ -32,93 +32,43 @@ constexpr int kStep = 128;  // WIENER_FILT_STEP
 __device__ __forceinline__ int plane_stride(const FrameDesc &f, int p) { return p ? f.w / 2 : f.w; }
 
 // ---------------------------------------------------------------------------
-// 1. Per-unit sums: find_average numerator and sse_region(src, dgd).
-// items: a = unit, b = first row of the chunk (relative to v_start).
-// ---------------------------------------------------------------------------
-constexpr int kSumRows = 16;
-
-__global__ void __launch_bounds__(256) k_lr_sums(FrameDesc *frames, const WorkItem *items, int nitems) {
-    __shared__ unsigned long long red[4][8];
-    const int it = find_item(items, nitems, blockIdx.x);
-    const WorkItem wi = items[it];
-    FrameDesc &f = frames[wi.frame];
-    const LrPlane &pl = f.lr[wi.plane];
-    const UnitRect r = pl.rects[wi.a];
-    LrUnit &u = pl.units[wi.a];
-    const int bd = f.bd, stride = plane_stride(f, wi.plane);
-    const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
-    const int dw = uw % 16, dh = uh % 16;
-    const int i0 = (blockIdx.x - wi.cta_begin) * kSumRows, i1 = min(uh, i0 + kSumRows);
-    unsigned long long s = 0, blk = 0, rgt = 0, bot = 0;
-    const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
-    // words of the unit rows (units start at multiples of 256 columns)
-    const int spw = word_samples(bd), nw = (uw + spw - 1) / spw;
-    const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    for (int q = threadIdx.x >> 5; q < (i1 - i0) * ((nw + 31) >> 5); q += nwarps) {
-        // warp per (row, 32-word segment), lanes over the words
-        const int segs = (nw + 31) >> 5, i = i0 + q / segs, w = (q - (q / segs) * segs) * 32 + lane;
-        if (w >= nw) continue;
-        const int j0 = w * spw, cnt = min(spw, uw - j0);
-        const uint8_t *drow = row_ptr(dg, r.v_start + i, stride, bd), *srow = row_ptr(sr, r.v_start + i, stride, bd);
-        const int x0 = r.h_start + j0;
-        int dv[4], sv[4];
-        if (cnt == spw && aligned4(drow) && aligned4(srow)) {
-            const uint32_t a = *reinterpret_cast<const uint32_t *>(drow + (bd == 8 ? x0 : 2 * x0));
-            const uint32_t b = *reinterpret_cast<const uint32_t *>(srow + (bd == 8 ? x0 : 2 * x0));
-            for (int k = 0; k < spw; ++k) {
-                dv[k] = word_sample(a, k, bd);
-                sv[k] = word_sample(b, k, bd);
-            }
-        } else {
-            for (int k = 0; k < cnt; ++k) {
-                dv[k] = ldpx(drow, x0 + k, bd);
-                sv[k] = ldpx(srow, x0 + k, bd);
-            }
-        }
-        for (int k = 0; k < cnt; ++k) {
-            const int j = j0 + k, d = dv[k], e = sv[k] - d;
-            const unsigned long long e2 = (unsigned long long)((long long)e * e);
-            s += (unsigned long long)d;
-            if (j >= uw - dw) rgt += e2;
-            else if (i >= uh - dh) bot += e2;
-            else blk += e2;
-        }
-    }
-    unsigned long long v[4] = {s, blk, rgt, bot};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-        if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v[k];
-    }
-    __syncthreads();
-    if (threadIdx.x < 4) {
-        unsigned long long t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
-        unsigned long long *dst = threadIdx.x == 0 ? (unsigned long long *)&u.sum
-                                : threadIdx.x == 1 ? &u.sse_blk : threadIdx.x == 2 ? &u.sse_rgt : &u.sse_bot;
-        atomicAdd(dst, t);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// 2. compute_stats: M[a] = sum y_a x, H[a][b] = sum y_a y_b (b >= a) over the
-// unit, y the win x win window of D = dgd - avg in column-major order
-// (index = col * win + row), x = src - avg (restoration.rs:567-632, :1738).
+// 1. compute_stats on raw samples (restoration.rs:567-632 / :1738-1807), with
+// find_average (:198) and sse_region (:1666 / :1991) folded in.
 //
-// Regrouping (exact integer sums). With window offsets s_a = (ra - h, ca - h)
-// and delta = s_b - s_a = (dr, dc), H[a][b] = sum over the unit rectangle
-// shifted by s_a of P[y][x] = D[y][x] * D[y + dr][x + dc]. For a fixed delta
-// all (a, b) pairs share P and differ only in the shift, so each thread takes
-// one image row y and one dr, slides a register window along the row
-// computing P for every dc at once, and gets the row sums over all shifted
-// column windows [sc, sc + uw) from a running prefix; a row contributes to
-// every vertical shift sr with y in [sr, sr + uh). M uses the same sliding
-// window with X in place of the second factor. Row sums of <= 392 products
-// of magnitude <= 1023^2 fit int32; everything is folded into int64.
+// M[a] = sum y_a x and H[a][b] = sum y_a y_b (b >= a) over the unit, y the
+// win x win window of dgd - A in column-major order (index = col * win +
+// row), x = src - A, A = find_average(dgd). With d = dgd, s = src, n the
+// unit's pixel count and S_a = sum of d over the unit rectangle shifted by
+// the window offset of a, the integer identities
+//   H[a][b] = Hr[a][b] - A (S_a + S_b) + n A^2,
+//   M[a]    = Mr[a] - A (S_a + sum s) + n A^2
+// hold exactly, Hr and Mr being the same sums over the raw samples. So one
+// pass accumulates Hr, Mr, S (S_centre / n is A), sum s and the three
+// sse_region parts, and k_lr_solve applies the correction before the
+// bit-depth divider: the same integers the reference reaches.
+//
+// Regrouping of Hr (exact integer sums). With window offsets s_a = (ra - h,
+// ca - h) and delta = s_b - s_a = (dr, dc), Hr[a][b] = sum over the unit
+// rectangle shifted by s_a of P[y][x] = d[y][x] * d[y + dr][x + dc]. For a
+// fixed delta all (a, b) pairs share P and differ only in the shift, so each
+// thread takes one image row y and one dr, slides along the row computing P
+// for every dc at once, and gets the row sums over all shifted column
+// windows [sc, sc + uw) from a running prefix; a row contributes to every
+// vertical shift sr with y in [sr, sr + uh). Mr and the shift sums use the
+// same walk with s (and 1) in place of the second factor. Row sums of <= 396
+// products of magnitude <= 1023^2 fit int32; everything is folded into int64.
+//
+// 8-bit frames with the 5-tap window keep the staged rows as bytes, and the
+// middle of every row walk (where no column window starts or ends) takes
+// four columns per step: one 32-bit dot product of four byte products per
+// dc (the partner row's bytes for dc = 1..3 are byte permutes of two
+// aligned words).
 //
 // A CTA covers kLrRows(WIN) consecutive rows of the unit's vertical range
-// extended by h = WIN/2 on both sides (items: a = unit, b = first row).
+// extended by h = WIN/2 on both sides (items: a = unit, CTA offset = row
+// block). Threads [0, NDR * rows) walk (row, dr) for Hr; the next WIN * (unit
+// rows) walk (unit row i, ra) for Mr, the shift sums of row i + ra - h and,
+// for ra = h, sum s and the sse parts of row i.
 // ---------------------------------------------------------------------------
 constexpr int kMaxUnitW = 384 + 8;
 
@@ -129,16 +79,29 @@ struct StatGeom {
     static constexpr int ROWS = 256 / (NDR + WIN);      // rows per CTA (stat_rows_host)
     static constexpr int DROWS = ROWS + 2 * (WIN - 1);  // staged D rows
     static constexpr int DCOLS = kMaxUnitW + 2 * H + WIN;
+    static constexpr int DSB = (DCOLS + 3) / 4 * 4;     // byte layout: row stride (a multiple of 4)
+    static constexpr int XSB = (kMaxUnitW + 3) / 4 * 4;
 };
+
+__device__ __forceinline__ uint32_t ld_word(const uint8_t *p) { return *reinterpret_cast<const uint32_t *>(p); }
+
+// Bytes k..k+3 of the little-endian byte string w0 w1 (k = 0..4).
+template <int K>
+__device__ __forceinline__ uint32_t bytes_at(uint32_t w0, uint32_t w1) {
+    if constexpr (K == 0) return w0;
+    else if constexpr (K == 4) return w1;
+    else return __byte_perm(w0, w1, 0x3210 + 0x1111 * K);
+}
 
 template <int WIN>
 __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkItem *items, int nitems) {
     using G = StatGeom<WIN>;
     constexpr int HALF = G::H, WIN2 = WIN * WIN;
     __shared__ __align__(16) int16_t D[G::DROWS * G::DCOLS];
-    __shared__ int16_t X[G::ROWS * kMaxUnitW];
+    __shared__ __align__(16) int16_t X[G::ROWS * kMaxUnitW];
     __shared__ unsigned long long Hs[WIN2 * WIN2];
-    __shared__ unsigned long long Ms[WIN2];
+    __shared__ unsigned long long Ms[WIN2], Ss[WIN2], Es[4];  // Es: sum s, sse blocks, right, bottom
+    static_assert(G::DROWS * G::DSB <= (int)sizeof(D) && G::ROWS * G::XSB <= (int)sizeof(X), "byte layout fits");
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
     FrameDesc &f = frames[wi.frame];
@@ -147,10 +110,11 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
     LrUnit &u = pl.units[wi.a];
     const int bd = f.bd, stride = plane_stride(f, wi.plane);
     const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
-    const int avg = (int)((unsigned long long)u.sum / (unsigned long long)((int64_t)uw * uh));
+    const bool packed = WIN == 5 && bd == 8;
+    uint8_t *Db = reinterpret_cast<uint8_t *>(D), *Xb = reinterpret_cast<uint8_t *>(X);
     const uint8_t *dg = f.A[wi.plane], *sr_ = f.S[wi.plane];
     // rows of this CTA in unit coordinates (extended range [-HALF, uh + HALF))
-    const int y0 = -HALF + (blockIdx.x - wi.cta_begin) * G::ROWS, y1 = min(uh + HALF, y0 + G::ROWS);
+    const int y0 = -HALF + ((int)blockIdx.x - wi.cta_begin) * G::ROWS, y1 = min(uh + HALF, y0 + G::ROWS);
     // D rows [y0 - (WIN-1), y1 + (WIN-1)) clamped, columns [-HALF, uw + HALF + WIN)
     const int dy0 = y0 - (WIN - 1), dx0 = -HALF;
     const int dcols = uw + 2 * HALF + WIN;
@@ -158,16 +122,25 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
     stage_window(
         bd, pl.pw, drows, r.h_start + dx0, dcols, true, 0,
         [&](int rr) { return row_ptr(dg, clampi(r.v_start + dy0 + rr, 0, pl.ph - 1), stride, bd); },
-        [&](int rr, int cc, int v) { D[rr * G::DCOLS + cc] = (int16_t)(v - avg); });
+        [&](int rr, int cc, int v) {
+            if (packed) Db[rr * G::DSB + cc] = (uint8_t)v;
+            else D[rr * G::DCOLS + cc] = (int16_t)v;
+        });
     const int xi0 = max(y0, 0), xi1 = min(y1, uh);
     stage_window(
         bd, pl.pw, xi1 - xi0, r.h_start, uw, true, 0,
         [&](int rr) { return row_ptr(sr_, r.v_start + xi0 + rr, stride, bd); },
-        [&](int rr, int cc, int v) { X[rr * kMaxUnitW + cc] = (int16_t)(v - avg); });
+        [&](int rr, int cc, int v) {
+            if (packed) Xb[rr * G::XSB + cc] = (uint8_t)v;
+            else X[rr * kMaxUnitW + cc] = (int16_t)v;
+        });
     for (int q = threadIdx.x; q < WIN2 * WIN2; q += blockDim.x) Hs[q] = 0;
-    if (threadIdx.x < WIN2) Ms[threadIdx.x] = 0;
+    if (threadIdx.x < WIN2) Ms[threadIdx.x] = Ss[threadIdx.x] = 0;
+    if (threadIdx.x < 4) Es[threadIdx.x] = 0;
     __syncthreads();
-    auto Dat = [&](int y, int x) -> int { return D[(y - dy0) * G::DCOLS + (x - dx0)]; };
+    auto Dat = [&](int y, int x) -> int {
+        return packed ? (int)Db[(y - dy0) * G::DSB + (x - dx0)] : (int)D[(y - dy0) * G::DCOLS + (x - dx0)];
+    };
 
     const int nh = G::NDR * (y1 - y0);
     const int t = threadIdx.x;
@@ -181,7 +154,7 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
 #pragma unroll
         for (int j = 0; j < WIN; ++j) rs[k][j] = 0;
     if (t < nh) {
-        // ---- H: one (row y, dr) per thread
+        // ---- Hr: one (row y, dr) per thread
         const int dr = t % G::NDR - (WIN - 1);
         const int y = y0 + t / G::NDR;
         // the row and its partner must lie in the extended range
@@ -190,55 +163,102 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
             int pre[WIN];
 #pragma unroll
             for (int k = 0; k < WIN; ++k) pre[k] = 0;
-            int win[WIN];  // D[y + dr][x + dc], dc = 0..WIN-1
+            int win[WIN];  // d[y + dr][x + dc], dc = 0..WIN-1
 #pragma unroll
             for (int k = 0; k < WIN - 1; ++k) win[k + 1] = Dat(y + dr, -HALF + k);
             // x runs over [-HALF, uw + HALF); prefix bookkeeping at the
             // column-window starts (x = sc) and ends (x = sc + uw), which
             // all lie outside the middle range [HALF + 1, uw - HALF).
-            auto edge_step = [&](int x) {
+            auto step = [&](int x) {  // one column: window slide, products
 #pragma unroll
                 for (int k = 0; k < WIN - 1; ++k) win[k] = win[k + 1];
                 win[WIN - 1] = Dat(y + dr, x + WIN - 1);
-#pragma unroll
-                for (int dc = 0; dc < WIN; ++dc)
-#pragma unroll
-                    for (int sc = -HALF; sc <= HALF; ++sc) {
-                        if (sc + HALF + dc > WIN - 1) continue;  // cb = ca + dc < WIN
-                        if (x == sc) rs[dc][sc + HALF] -= pre[dc];
-                        if (x == sc + uw) rs[dc][sc + HALF] += pre[dc];
-                    }
                 const int a = Dat(y, x);
 #pragma unroll
                 for (int dc = 0; dc < WIN; ++dc) pre[dc] += a * win[dc];
             };
             const int xm0 = HALF + 1, xm1 = max(xm0, uw - HALF);
             int x = -HALF;
-            for (; x < xm0; ++x) edge_step(x);
-            {
-                // middle: the window rotates through registers (slot
-                // (u + dc) % WIN holds D[y + dr][x + u + dc]), no moves
-                int w[WIN];
+            if (uw >= 16) {
+                // head: x = sc starts the windows of sc (unrolled, so the
+                // bookkeeping is resolved at compile time)
 #pragma unroll
-                for (int k = 0; k < WIN - 1; ++k) w[k] = win[k + 1];
-                for (; x + WIN <= xm1; x += WIN) {
+                for (int k = 0; k < WIN; ++k) {
 #pragma unroll
-                    for (int u = 0; u < WIN; ++u) {
-                        w[(u + WIN - 1) % WIN] = Dat(y + dr, x + u + WIN - 1);
-                        const int a = Dat(y, x + u);
+                    for (int dc = 0; dc < WIN; ++dc)
+                        if (k + dc <= WIN - 1) rs[dc][k] -= pre[dc];
+                    step(k - HALF);
+                }
+                x = xm0;
+                if (packed) {
+                    if constexpr (WIN == 5) {
+                        // plain steps up to a word boundary of the byte rows
+                        // (x + HALF = 0 mod 4), then four columns per step
+                        constexpr int xs = HALF + 1 + ((4 - (2 * HALF + 1) % 4) & 3);
+                        for (; x < xs; ++x) step(x);
+                        const uint8_t *ra_ = Db + (y - dy0) * G::DSB + HALF, *rb_ = Db + (y + dr - dy0) * G::DSB + HALF;
+                        if (x + 4 <= xm1) {
+                            uint32_t w0 = ld_word(rb_ + x);
+                            for (; x + 4 <= xm1; x += 4) {
+                                const uint32_t a4 = ld_word(ra_ + x), w1 = ld_word(rb_ + x + 4);
+                                pre[0] = (int)__dp4a(a4, w0, (uint32_t)pre[0]);
+                                pre[1] = (int)__dp4a(a4, bytes_at<1>(w0, w1), (uint32_t)pre[1]);
+                                pre[2] = (int)__dp4a(a4, bytes_at<2>(w0, w1), (uint32_t)pre[2]);
+                                pre[3] = (int)__dp4a(a4, bytes_at<3>(w0, w1), (uint32_t)pre[3]);
+                                pre[4] = (int)__dp4a(a4, w1, (uint32_t)pre[4]);
+                                w0 = w1;
+                            }
+                            // the step's window: win[k + 1] = d[y + dr][x + k]
 #pragma unroll
-                        for (int dc = 0; dc < WIN; ++dc) pre[dc] += a * w[(u + dc) % WIN];
+                            for (int k = 0; k < WIN - 1; ++k) win[k + 1] = Dat(y + dr, x + k);
+                        }
                     }
+                } else {
+                    // middle: the window rotates through registers (slot
+                    // (u + dc) % WIN holds d[y + dr][x + u + dc]), no moves
+                    int w[WIN];
+#pragma unroll
+                    for (int k = 0; k < WIN - 1; ++k) w[k] = win[k + 1];
+                    for (; x + WIN <= xm1; x += WIN) {
+#pragma unroll
+                        for (int u = 0; u < WIN; ++u) {
+                            w[(u + WIN - 1) % WIN] = Dat(y + dr, x + u + WIN - 1);
+                            const int a = Dat(y, x + u);
+#pragma unroll
+                            for (int dc = 0; dc < WIN; ++dc) pre[dc] += a * w[(u + dc) % WIN];
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < WIN - 1; ++k) win[k + 1] = w[k];
+                }
+                for (; x < uw - HALF; ++x) step(x);
+                // tail: x = sc + uw ends the windows of sc; the last end
+                // (sc = HALF) is at x = uw + HALF, past the walk
+#pragma unroll
+                for (int k = 0; k < WIN; ++k) {
+#pragma unroll
+                    for (int dc = 0; dc < WIN; ++dc)
+                        if (k + dc <= WIN - 1) rs[dc][k] += pre[dc];
+                    if (k < WIN - 1) step(uw - HALF + k);
+                }
+            } else {
+                // narrow unit: starts and ends may interleave
+                for (; x < uw + HALF; ++x) {
+#pragma unroll
+                    for (int dc = 0; dc < WIN; ++dc)
+#pragma unroll
+                        for (int sc = -HALF; sc <= HALF; ++sc) {
+                            if (sc + HALF + dc > WIN - 1) continue;  // cb = ca + dc < WIN
+                            if (x == sc) rs[dc][sc + HALF] -= pre[dc];
+                            if (x == sc + uw) rs[dc][sc + HALF] += pre[dc];
+                        }
+                    step(x);
                 }
 #pragma unroll
-                for (int k = 0; k < WIN - 1; ++k) win[k + 1] = w[k];
+                for (int dc = 0; dc < WIN; ++dc)
+                    if (HALF + HALF + dc <= WIN - 1) rs[dc][2 * HALF] += pre[dc];
             }
-            for (; x < uw + HALF; ++x) edge_step(x);
-            // x == uw + HALF ends the windows with sc = HALF
-#pragma unroll
-            for (int dc = 0; dc < WIN; ++dc)
-                if (HALF + HALF + dc <= WIN - 1) rs[dc][2 * HALF] += pre[dc];
-            // contributions: H[a][b], a = (ca, ra), b = (ca + dc, ra + dr)
+            // contributions: Hr[a][b], a = (ca, ra), b = (ca + dc, ra + dr)
             keep = interior(y);
 #pragma unroll
             for (int dc = 0; dc < WIN; ++dc) {
@@ -257,46 +277,114 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
             }
         }
     } else if (t < nh + WIN * (xi1 - xi0)) {
-        // ---- M: one (row i, ra) per thread
+        // ---- Mr, shift sums, sum s and sse: one (unit row i, ra) per thread
         const int q = t - nh;
         const int ra = q % WIN, i = xi0 + q / WIN;
         const int yy = i + ra - HALF;
-        int acc[WIN];
-        int win[WIN];  // D[yy][j + ca - HALF], ca = 0..WIN-1
+        const bool centre = ra == HALF;
+        const int jr = uw - uw % 16;  // the right strip of sse_region
+        int acc[WIN];  // Mr[ca][ra] row parts
 #pragma unroll
         for (int k = 0; k < WIN; ++k) acc[k] = 0;
-#pragma unroll
-        for (int k = 0; k < WIN - 1; ++k) win[k + 1] = Dat(yy, -HALF + k);
-        const int16_t *xr = X + (i - xi0) * kMaxUnitW;
+        // c0 = sum of d[yy][j - HALF], j in [0, uw) (the ca = 0 column window)
+        unsigned c0 = 0, sx = 0, e_in = 0, e_rgt = 0;
         int j = 0;
-        {
-            // rotating window: slot (u + ca) % WIN holds D[yy][j + u + ca - HALF]
-            int w[WIN];
+        if (packed) {
+            if constexpr (WIN == 5) {
+                const uint8_t *rd = Db + (yy - dy0) * G::DSB;  // byte j + ca is d[yy][j + ca - HALF]
+                const uint8_t *rx = Xb + (i - xi0) * G::XSB;
+                const int uw4 = uw & ~3;
+                uint32_t w0 = ld_word(rd);
+                for (; j < uw4; j += 4) {
+                    const uint32_t w1 = ld_word(rd + j + 4), xv = ld_word(rx + j);
+                    const uint32_t d2 = bytes_at<2>(w0, w1);
+                    acc[0] = (int)__dp4a(w0, xv, (uint32_t)acc[0]);
+                    acc[1] = (int)__dp4a(bytes_at<1>(w0, w1), xv, (uint32_t)acc[1]);
+                    acc[2] = (int)__dp4a(d2, xv, (uint32_t)acc[2]);
+                    acc[3] = (int)__dp4a(bytes_at<3>(w0, w1), xv, (uint32_t)acc[3]);
+                    acc[4] = (int)__dp4a(w1, xv, (uint32_t)acc[4]);
+                    c0 = __dp4a(w0, 0x01010101u, c0);
+                    if (centre) {
+                        sx = __dp4a(xv, 0x01010101u, sx);
+                        const uint32_t e = __vabsdiffu4(xv, d2);
+                        if (j >= jr) e_rgt = __dp4a(e, e, e_rgt);
+                        else e_in = __dp4a(e, e, e_in);
+                    }
+                    w0 = w1;
+                }
+                for (; j < uw; ++j) {
+                    const int xv = rx[j];
 #pragma unroll
-            for (int k = 0; k < WIN - 1; ++k) w[k] = win[k + 1];
-            for (; j + WIN <= uw; j += WIN) {
-#pragma unroll
-                for (int u = 0; u < WIN; ++u) {
-                    w[(u + WIN - 1) % WIN] = Dat(yy, j + u + HALF);
-                    const int xv = xr[j + u];
-#pragma unroll
-                    for (int ca = 0; ca < WIN; ++ca) acc[ca] += w[(u + ca) % WIN] * xv;
+                    for (int ca = 0; ca < WIN; ++ca) acc[ca] += (int)rd[j + ca] * xv;
+                    c0 += rd[j];
+                    if (centre) {
+                        const int e = xv - (int)rd[j + HALF];
+                        sx += xv;
+                        if (j >= jr) e_rgt += e * e;
+                        else e_in += e * e;
+                    }
                 }
             }
+        } else {
+            int win[WIN];  // d[yy][j + ca - HALF], ca = 0..WIN-1
 #pragma unroll
-            for (int k = 0; k < WIN - 1; ++k) win[k + 1] = w[k];
+            for (int k = 0; k < WIN - 1; ++k) win[k + 1] = Dat(yy, -HALF + k);
+            const int16_t *xr = X + (i - xi0) * kMaxUnitW;
+            {
+                // rotating window: slot (u + ca) % WIN holds d[yy][j + u + ca - HALF]
+                int w[WIN];
+#pragma unroll
+                for (int k = 0; k < WIN - 1; ++k) w[k] = win[k + 1];
+                for (; j + WIN <= uw; j += WIN) {
+#pragma unroll
+                    for (int u = 0; u < WIN; ++u) {
+                        w[(u + WIN - 1) % WIN] = Dat(yy, j + u + HALF);
+                        const int xv = xr[j + u];
+#pragma unroll
+                        for (int ca = 0; ca < WIN; ++ca) acc[ca] += w[(u + ca) % WIN] * xv;
+                        c0 += w[u % WIN];
+                        if (centre) {
+                            const int e = xv - w[(u + HALF) % WIN];
+                            sx += xv;
+                            if (j + u >= jr) e_rgt += e * e;
+                            else e_in += e * e;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < WIN - 1; ++k) win[k + 1] = w[k];
+            }
+            for (; j < uw; ++j) {
+#pragma unroll
+                for (int k = 0; k < WIN - 1; ++k) win[k] = win[k + 1];
+                win[WIN - 1] = Dat(yy, j + HALF);
+                const int xv = xr[j];
+#pragma unroll
+                for (int ca = 0; ca < WIN; ++ca) acc[ca] += win[ca] * xv;
+                c0 += win[0];
+                if (centre) {
+                    const int e = xv - win[HALF];
+                    sx += xv;
+                    if (j >= jr) e_rgt += e * e;
+                    else e_in += e * e;
+                }
+            }
         }
-        for (; j < uw; ++j) {
 #pragma unroll
-            for (int k = 0; k < WIN - 1; ++k) win[k] = win[k + 1];
-            win[WIN - 1] = Dat(yy, j + HALF);
-            const int xv = xr[j];
+        for (int ca = 0; ca < WIN; ++ca) atomicAdd(&Ms[ca * WIN + ra], (unsigned long long)(long long)acc[ca]);
+        // column windows ca = 1..WIN-1 slide the ca = 0 one
+        unsigned long long cw = c0;
+        atomicAdd(&Ss[ra], cw);
 #pragma unroll
-            for (int ca = 0; ca < WIN; ++ca) acc[ca] += win[ca] * xv;
+        for (int ca = 1; ca < WIN; ++ca) {
+            cw = cw - (unsigned)Dat(yy, ca - 1 - HALF) + (unsigned)Dat(yy, ca - 1 - HALF + uw);
+            atomicAdd(&Ss[ca * WIN + ra], cw);
         }
-#pragma unroll
-        for (int ca = 0; ca < WIN; ++ca)
-            atomicAdd(&Ms[ca * WIN + ra], (unsigned long long)(long long)acc[ca]);
+        if (centre) {
+            atomicAdd(&Es[0], (unsigned long long)sx);
+            atomicAdd(&Es[i >= uh - uh % 16 ? 3 : 1], (unsigned long long)e_in);
+            atomicAdd(&Es[2], (unsigned long long)e_rgt);
+        }
     }
     __syncthreads();
     // Interior rows: the row sums of each (dr, dc, ca) are added over the
@@ -339,11 +427,19 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
         const int ia = q / WIN2, ib = q - ia * WIN2;
         if (ib >= ia && Hs[q]) atomicAdd((unsigned long long *)&u.h[q], Hs[q]);
     }
-    if (threadIdx.x < WIN2 && Ms[threadIdx.x]) atomicAdd((unsigned long long *)&u.m[threadIdx.x], Ms[threadIdx.x]);
+    if (threadIdx.x < WIN2) {
+        if (Ms[threadIdx.x]) atomicAdd((unsigned long long *)&u.m[threadIdx.x], Ms[threadIdx.x]);
+        if (Ss[threadIdx.x]) atomicAdd((unsigned long long *)&u.s[threadIdx.x], Ss[threadIdx.x]);
+    }
+    if (threadIdx.x < 4 && Es[threadIdx.x]) {
+        unsigned long long *dst = threadIdx.x == 0 ? (unsigned long long *)&u.sum_src
+                                : threadIdx.x == 1 ? &u.sse_blk : threadIdx.x == 2 ? &u.sse_rgt : &u.sse_bot;
+        atomicAdd(dst, Es[threadIdx.x]);
+    }
 }
 
 // ---------------------------------------------------------------------------
-// 3. Solve: wiener_decompose_sep_sym + finalize_sym_filter + compute_score
+// 2. Solve: wiener_decompose_sep_sym + finalize_sym_filter + compute_score
 // (restoration.rs:801-1056), one CTA per unit. The update_{a,b} sums are
 // sums of independently truncated terms, so threads split the terms and the
 // bins are reduced exactly.
@@ -495,27 +591,29 @@ __global__ void __launch_bounds__(128) k_lr_solve(FrameDesc *frames, const WorkI
     const LrPlane &pl = f.lr[wi.plane];
     LrUnit &u = pl.units[wi.a];
     const int win = pl.win, win2 = win * win;
-    // Bit-depth divider on M and the upper triangle (truncating division by
-    // 4 at 10 bits, written as a shift with the sign correction), then mirror
-    // (compute_stats_hbd, restoration.rs:1799-1806).
+    // The raw-sample sums corrected by the unit average A = find_average
+    // (restoration.rs:198: the centre shift sum over the pixel count), then
+    // the bit-depth divider on M and the upper triangle (truncating division
+    // by 4 at 10 bits, written as a shift with the sign correction), then
+    // mirrored (compute_stats_hbd, restoration.rs:1799-1806).
     const bool hbd = f.bd == 10;
     auto divd = [hbd](int64_t v) { return hbd ? (v + ((v >> 63) & 3)) >> 2 : v; };
+    const UnitRect rc = pl.rects[wi.a];
+    const int64_t n = (int64_t)(rc.h_end - rc.h_start) * (rc.v_end - rc.v_start);
+    const int ctr = (win >> 1) * win + (win >> 1);
+    const int64_t A = (int64_t)((unsigned long long)u.s[ctr] / (unsigned long long)n), nAA = n * A * A;
     __shared__ unsigned long long sbins[20];
     if (threadIdx.x < 20) sbins[threadIdx.x] = 0;
-    for (int k = threadIdx.x; k < win2; k += blockDim.x) M[k] = divd(u.m[k]);
+    for (int k = threadIdx.x; k < win2; k += blockDim.x) M[k] = divd(u.m[k] - A * (u.s[k] + u.sum_src) + nAA);
     for (int t = threadIdx.x; t < win2 * win2; t += blockDim.x) {
         const int k = t / win2, l = t - k * win2;
         if (l >= k) {
-            const int64_t v = divd(u.h[t]);
+            const int64_t v = divd(u.h[t] - A * (u.s[k] + u.s[l]) + nAA);
             H[t] = v;
             H[l * win2 + k] = v;
         }
     }
     if (threadIdx.x == 0) {
-        const int uw = pl.rects[wi.a].h_end - pl.rects[wi.a].h_start;
-        const int uh = pl.rects[wi.a].v_end - pl.rects[wi.a].v_start;
-        (void)uw;
-        (void)uh;
         if (f.bd == 8) u.sse_none = (int64_t)(u.sse_blk + u.sse_rgt + u.sse_bot);
         else u.sse_none = (int64_t)u.sse_blk + (int64_t)(uint32_t)u.sse_rgt + (int64_t)(uint32_t)u.sse_bot;
         const int off = (7 - win) >> 1;
@@ -582,7 +680,7 @@ __global__ void __launch_bounds__(128) k_lr_solve(FrameDesc *frames, const WorkI
 }
 
 // ---------------------------------------------------------------------------
-// 4. Trial filter + SSE (try_restoration_unit, restoration.rs:472-507) and
+// 3. Trial filter + SSE (try_restoration_unit, restoration.rs:472-507) and
 // the refinement hill-climb (finer_tile_search_wiener, :513-636). One CTA
 // per unit.
 // ---------------------------------------------------------------------------
@@ -868,7 +966,7 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
 }
 
 // ---------------------------------------------------------------------------
-// 5. Frame RD (search_restoration_still_bd finish, restoration.rs:847-897):
+// 4. Frame RD (search_restoration_still_bd finish, restoration.rs:847-897):
 // one thread per (frame, plane); reference-chained count_wiener_bits and
 // RDCOST_DBL in IEEE double without contraction.
 // ---------------------------------------------------------------------------
@@ -1130,7 +1228,7 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
 }
 
 // ---------------------------------------------------------------------------
-// 6. Apply (apply_restoration_frame, restoration.rs:992-1052) with the
+// 5. Apply (apply_restoration_frame, restoration.rs:992-1052) with the
 // stripe boundaries of save_lr_boundaries, writing every pixel of C: one CTA
 // per (plane, stripe, 64-px column tile) over the aligned canvas. Tiles of
 // Wiener units are filtered within the true plane and copied from A beyond
