@@ -60,6 +60,7 @@ struct LrPlane {
     int hunits, vunits;
     int frame_rtype;
     int refine;          // finer_tile_search_wiener refinement (presets <= 3)
+    int trial_out;       // the tiled trial writes its filtered pixels into C
     UnitRect *rects;     // hunits*vunits
     LrUnit *units;       // hunits*vunits
     PackedUnit *packed;  // hunits*vunits output records

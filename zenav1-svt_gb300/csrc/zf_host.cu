@@ -728,6 +728,15 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             if (!p.rects[pl].empty())
                 std::memcpy(ctx->h_meta + m_rects + p.off_rects[pl], p.rects[pl].data(),
                             p.rects[pl].size() * sizeof(UnitRect));
+        // The tiled Wiener trial (units without refinement) writes its
+        // filtered pixels into C when this call applies the search's
+        // decisions; the apply then recomputes only the rows next to
+        // interior stripe boundaries of Wiener units.
+        const bool trial_out = (run.stages & STG_LR_SEARCH) && !run.lr_given && (run.stages & STG_LR_APPLY);
+        for (int pl = 0; pl < 3; ++pl) {
+            LrPlane &L = p.d.lr[pl];
+            L.trial_out = trial_out && L.on && !L.refine ? 1 : 0;
+        }
         // decisions the caller provides
         const zf_decisions *dec = p.out;
         if (run.lf_given) std::memcpy(p.d.lf, dec->lf, 4);

@@ -891,9 +891,9 @@ constexpr int TL = 64;
 
 __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const WorkItem *items, int nitems) {
     constexpr int SW = TL + 7;
-    __shared__ uint16_t stage[(TL + 7) * SW];
-    __shared__ uint16_t tmp[(TL + 7) * TL];
-    __shared__ uint16_t srct[TL * TL];
+    __shared__ __align__(16) uint16_t stage[(TL + 7) * SW];
+    __shared__ __align__(16) uint16_t tmp[(TL + 7) * TL];
+    __shared__ __align__(16) uint16_t srct[TL * TL];
     __shared__ unsigned long long red[24];
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
@@ -917,38 +917,68 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         vf[k] = u.vf[k];
     }
     const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
+    const bool tout = pl.trial_out != 0;
+    uint8_t *outp = f.C[wi.plane];
+    const int ph = pl.ph;
     stage_window(
         bd, pl.pw, th + 7, x0 - 3, tw + 7, true, 0,
-        [&](int rr) { return row_ptr(dg, clampi(y0 - 3 + rr, 0, pl.ph - 1), stride, bd); },
+        [&](int rr) { return row_ptr(dg, clampi(y0 - 3 + rr, 0, ph - 1), stride, bd); },
         [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
     stage_window(
         bd, pl.pw, th, x0, tw, true, 0, [&](int rr) { return row_ptr(sr, y0 + rr, stride, bd); },
         [&](int rr, int cc, int v) { srct[rr * TL + cc] = (uint16_t)v; });
     __syncthreads();
-    // rows x 64 columns (TL), columns past the tile width skipped: no division
-    for (int q = threadIdx.x; q < (th + 7) * TL; q += blockDim.x) {
-        const int rr = q >> 6, cc = q & (TL - 1);
-        if (cc >= tw) continue;
-        int px[8];
+    // The solver's taps are symmetric (f[6 - k] = f[k], f[7] = 0), so each
+    // pass is 4 multiplies per output on pair sums, the centre tap carrying
+    // the 128 of wiener_convolve_add_src; a thread takes four outputs along
+    // the pass from 11 staged samples.
+    // horizontal: (th + 7) rows x 16 runs of four columns
+    {
+        const int c3 = 128 + hf[3], off = 1 << (bd + 6), lim = (1 << (bd + 5)) - 1;
+        for (int q = threadIdx.x; q < (th + 7) * (TL / 4); q += blockDim.x) {
+            const int rr = q >> 4, c0 = (q & 15) * 4;
+            if (c0 >= tw) continue;
+            const uint16_t *sp = stage + rr * SW + c0;
+            int p[11];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) px[k] = stage[rr * SW + cc + k];
-        tmp[rr * TL + cc] = (uint16_t)wiener_h(px, hf, bd);
+            for (int k = 0; k < 11; ++k) p[k] = sp[k];
+            uint32_t o[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int sum = p[j + 3] * c3 + hf[0] * (p[j] + p[j + 6]) + hf[1] * (p[j + 1] + p[j + 5]) +
+                                hf[2] * (p[j + 2] + p[j + 4]) + off;
+                o[j] = (uint32_t)clampi((sum + 4) >> 3, 0, lim);
+            }
+            *reinterpret_cast<uint2 *>(tmp + rr * TL + c0) = make_uint2(o[0] | o[1] << 16, o[2] | o[3] << 16);
+        }
     }
     __syncthreads();
+    // vertical: runs of four rows x 64 columns, SSE parts, trial output
     unsigned long long blk = 0, rgt = 0, bot = 0;
-    for (int q = threadIdx.x; q < th * TL; q += blockDim.x) {
-        const int rr = q >> 6, cc = q & (TL - 1);
-        if (cc >= tw) continue;
-        const int i = ty + rr, j = tx + cc;
-        int tp[8];
+    {
+        const int c3 = 128 + vf[3], off = -(1 << (bd + 10)), vmax = (1 << bd) - 1;
+        for (int q = threadIdx.x; q < ((th + 3) >> 2) * TL; q += blockDim.x) {
+            const int r0 = (q >> 6) * 4, cc = q & (TL - 1);
+            if (cc >= tw) continue;
+            int p[11];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) tp[k] = tmp[(rr + k) * TL + cc];
-        const int y = wiener_v(tp, vf, bd);
-        const int e = (int)srct[rr * TL + cc] - y;
-        const unsigned long long e2 = (unsigned long long)((long long)e * e);
-        if (j >= uw - dw) rgt += e2;
-        else if (i >= uh - dh) bot += e2;
-        else blk += e2;
+            for (int k = 0; k < 11; ++k) p[k] = tmp[(r0 + k) * TL + cc];
+            const int j = tx + cc;
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) {
+                const int rr = r0 + jj;
+                if (rr >= th) break;
+                const int sum = p[jj + 3] * c3 + vf[0] * (p[jj] + p[jj + 6]) + vf[1] * (p[jj + 1] + p[jj + 5]) +
+                                vf[2] * (p[jj + 2] + p[jj + 4]) + off;
+                const int y = clampi((sum + (1 << 10)) >> 11, 0, vmax);
+                if (tout) stpx(outp, (int64_t)(y0 + rr) * stride + x0 + cc, bd, y);
+                const int e = (int)srct[rr * TL + cc] - y;
+                const unsigned long long e2 = (unsigned long long)((long long)e * e);
+                if (j >= uw - dw) rgt += e2;
+                else if (ty + rr >= uh - dh) bot += e2;
+                else blk += e2;
+            }
+        }
     }
     unsigned long long v[3] = {blk, rgt, bot};
 #pragma unroll
@@ -962,6 +992,64 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         unsigned long long s = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x * 8 + w];
         if (s) atomicAdd(threadIdx.x == 0 ? &u.tw_blk : threadIdx.x == 1 ? &u.tw_rgt : &u.tw_bot, s);
+    }
+    if (!tout) return;
+    // The apply's pixels of this tile (apply_restoration_frame, restoration
+    // .rs:992-1052): equal to the trial's except within 3 rows of an interior
+    // stripe edge b (stripes of 64 rows, the first 8 shorter, halved for
+    // chroma), where the apply reads the post-deblock lines that
+    // save_lr_boundaries keeps: the upper stripe's rows b-3..b-1 take B[b]
+    // and B[min(b+1, ph-1)] in place of rows >= b, the lower stripe's rows
+    // b..b+2 take B[b-1] and B[b-2] in place of rows < b. Those rows are
+    // recomputed here with the same taps, so C ends final for a Wiener unit.
+    const int ssh = wi.plane ? 1 : 0, full = 64 >> ssh, soff = 8 >> ssh;
+    const int yA = y0 - 3;  // plane row of tmp row 0
+    const uint8_t *pre = f.B[wi.plane];
+    uint16_t *hb = srct;    // the four B rows after the horizontal pass
+    const int hc3 = 128 + hf[3], hoff = 1 << (bd + 6), hlim = (1 << (bd + 5)) - 1;
+    const int vc3 = 128 + vf[3], voff = -(1 << (bd + 10)), vmax = (1 << bd) - 1;
+    for (int si = max(1, (y0 + soff) / full);; ++si) {
+        const int b = si * full - soff;
+        if (b >= ph || b - 3 >= y0 + th) break;
+        if (b + 3 <= y0) continue;
+        __syncthreads();  // C rows of the main pass written; stage and hb free
+        // rows b - 2, b - 1, b, min(b + 1, ph - 1)
+        stage_window(
+            bd, pl.pw, 4, x0 - 3, tw + 7, true, 0,
+            [&](int rr) { return row_ptr(pre, rr < 3 ? b - 2 + rr : min(b + 1, ph - 1), stride, bd); },
+            [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
+        __syncthreads();
+        for (int q = threadIdx.x; q < 4 * (TL / 4); q += blockDim.x) {
+            const int rr = q >> 4, c0 = (q & 15) * 4;
+            if (c0 >= tw) continue;
+            const uint16_t *sp = stage + rr * SW + c0;
+            int p[11];
+#pragma unroll
+            for (int k = 0; k < 11; ++k) p[k] = sp[k];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int sum = p[j + 3] * hc3 + hf[0] * (p[j] + p[j + 6]) + hf[1] * (p[j + 1] + p[j + 5]) +
+                                hf[2] * (p[j + 2] + p[j + 4]) + hoff;
+                hb[rr * TL + c0 + j] = (uint16_t)clampi((sum + 4) >> 3, 0, hlim);
+            }
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < 6 * TL; q += blockDim.x) {
+            const int y = b - 3 + (q >> 6), cc = q & (TL - 1);
+            if (cc >= tw || y < y0 || y >= y0 + th) continue;
+            int tp[7];
+#pragma unroll
+            for (int k = 0; k < 7; ++k) {
+                const int t = y - 3 + k;
+                int row;  // index into tmp (A rows) or hb (B rows, marked by >= 1000)
+                if (y < b) row = t < b ? t - yA : 1000 + (t == b ? 2 : 3);
+                else row = t < b ? 1000 + (t == b - 1 ? 1 : 0) : t - yA;
+                tp[k] = row >= 1000 ? hb[(row - 1000) * TL + cc] : tmp[row * TL + cc];
+            }
+            const int sum = tp[3] * vc3 + vf[0] * (tp[0] + tp[6]) + vf[1] * (tp[1] + tp[5]) +
+                            vf[2] * (tp[2] + tp[4]) + voff;
+            stpx(outp, (int64_t)y * stride + x0 + cc, bd, clampi((sum + (1 << 10)) >> 11, 0, vmax));
+        }
     }
 }
 
@@ -1242,8 +1330,8 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
 __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems) {
     constexpr int SW = TT_W + 7;
     constexpr int MAXH = 64 + 7;
-    __shared__ uint16_t stage[MAXH * SW];
-    __shared__ uint16_t tmp[MAXH * TT_W];
+    __shared__ __align__(16) uint16_t stage[MAXH * SW];
+    __shared__ __align__(16) uint16_t tmp[MAXH * TT_W];
     const WorkItem wi = items[find_item(items, nitems, blockIdx.x)];
     const FrameDesc &f = frames[wi.frame];
     const LrPlane &pl = f.lr[wi.plane];
@@ -1296,51 +1384,72 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
     }
     if (!filter) return;
     const LrUnit &u = pl.units[unit];
-    const int ncol = cx, nrow = ye - ys;
+    int16_t hf[8], vf[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        hf[k] = u.hf[k];
+        vf[k] = u.vf[k];
+    }
+    const int ncol = cx;
     const bool copy_above = s > 0, copy_below = ye < pl.ph;
-    const int rows = nrow + 7;
-    auto row_of = [&](int rr) {
-        const int y = ys - 3 + rr;
-        const uint8_t *src = post;
-        int yy;
-        if (y < ys) {
-            if (copy_above) {
-                src = pre;
-                yy = y == ys - 1 ? ys - 1 : ys - 2;
+    // Output rows [rb, re) of the stripe: stage rows rb - 3 .. re + 3 with
+    // the stripe's boundary substitution, horizontal pass, vertical pass.
+    auto filter_rows = [&](int rb, int re) {
+        const int nrow = re - rb, rows = nrow + 7;
+        auto row_of = [&](int rr) {
+            const int y = rb - 3 + rr;
+            const uint8_t *src = post;
+            int yy;
+            if (y < ys) {
+                if (copy_above) {
+                    src = pre;
+                    yy = y == ys - 1 ? ys - 1 : ys - 2;
+                } else {
+                    yy = clampi(y, 0, pl.ph - 1);
+                }
+            } else if (y >= ye) {
+                if (copy_below) {
+                    src = pre;
+                    yy = y == ye ? ye : min(ye + 1, pl.ph - 1);
+                } else {
+                    yy = clampi(y, 0, pl.ph - 1);
+                }
             } else {
-                yy = clampi(y, 0, pl.ph - 1);
+                yy = y;
             }
-        } else if (y >= ye) {
-            if (copy_below) {
-                src = pre;
-                yy = y == ye ? ye : min(ye + 1, pl.ph - 1);
-            } else {
-                yy = clampi(y, 0, pl.ph - 1);
-            }
-        } else {
-            yy = y;
+            return row_ptr(src, yy, stride, bd);
+        };
+        __syncthreads();  // the previous band's reads of stage / tmp are done
+        stage_window(bd, pl.pw, rows, x0 - 3, SW, true, 0, row_of,
+                     [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
+        __syncthreads();
+        // four outputs per thread along each pass from 11 staged samples
+        for (int q = threadIdx.x; q < rows * (TT_W / 4); q += blockDim.x) {
+            const int rr = q >> 4, c0 = (q & 15) * 4;
+            int p[11];
+#pragma unroll
+            for (int k = 0; k < 11; ++k) p[k] = stage[rr * SW + c0 + k];
+            uint32_t o[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) o[j] = (uint32_t)wiener_h(p + j, hf, bd);
+            *reinterpret_cast<uint2 *>(tmp + rr * TT_W + c0) = make_uint2(o[0] | o[1] << 16, o[2] | o[3] << 16);
         }
-        return row_ptr(src, yy, stride, bd);
+        __syncthreads();
+        for (int q = threadIdx.x; q < ((nrow + 3) >> 2) * TT_W; q += blockDim.x) {
+            const int r0 = (q >> 6) * 4, cc = q & (TT_W - 1);
+            if (cc >= ncol) continue;
+            int p[11];
+#pragma unroll
+            for (int k = 0; k < 11; ++k) p[k] = tmp[(r0 + k) * TT_W + cc];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (r0 + j >= nrow) break;
+                stpx(out, (int64_t)(rb + r0 + j) * stride + x0 + cc, bd, wiener_v(p + j, vf, bd));
+            }
+        }
     };
-    stage_window(bd, pl.pw, rows, x0 - 3, SW, true, 0, row_of,
-                 [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
-    __syncthreads();
-    for (int q = threadIdx.x; q < rows * TT_W; q += blockDim.x) {
-        const int rr = q / TT_W, cc = q - rr * TT_W;
-        int px[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) px[k] = stage[rr * SW + cc + k];
-        tmp[q] = (uint16_t)wiener_h(px, u.hf, bd);
-    }
-    __syncthreads();
-    for (int q = threadIdx.x; q < nrow * TT_W; q += blockDim.x) {
-        const int rr = q / TT_W, cc = q - rr * TT_W;
-        if (cc >= ncol) continue;
-        int tp[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) tp[k] = tmp[(rr + k) * TT_W + cc];
-        stpx(out, (int64_t)(ys + rr) * stride + x0 + cc, bd, wiener_v(tp, u.vf, bd));
-    }
+    // a tiled-trial plane: the trial wrote this unit's final pixels
+    if (!pl.trial_out) filter_rows(ys, ye);
 }
 
 }  // namespace zf
