@@ -887,12 +887,23 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256)
 // tile (items: a = unit, one item per unit, CTA offset = tile index in
 // raster order), the three sse_region parts accumulate into the unit and
 // k_lr_finish combines them.
+//
+// When the plane's trial output is kept (trial_out), the tile also writes
+// the apply's pixels (apply_restoration_frame, restoration.rs:992-1052)
+// into C. They equal the trial's except within 3 rows of an interior stripe
+// edge b (stripes of 64 rows, the first 8 shorter, halved for chroma), where
+// the apply reads the post-deblock lines that save_lr_boundaries keeps: the
+// upper stripe's rows b-3..b-1 take B[b] and B[min(b+1, ph-1)] in place of
+// rows >= b, the lower stripe's rows b..b+2 take B[b-1] and B[b-2] in place
+// of rows < b. Those four B rows per edge are staged and filtered with the
+// tile's rows, so C ends final for a Wiener unit.
 constexpr int TL = 64;
+constexpr int kTileEdges = 3;  // stripe edges whose rows can meet a 64-row tile (stripes >= 32 rows)
 
 __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const WorkItem *items, int nitems) {
-    constexpr int SW = TL + 7;
-    __shared__ __align__(16) uint16_t stage[(TL + 7) * SW];
-    __shared__ __align__(16) uint16_t tmp[(TL + 7) * TL];
+    constexpr int SW = TL + 7, SR = TL + 7 + 4 * kTileEdges;
+    __shared__ __align__(16) uint16_t stage[SR * SW];
+    __shared__ __align__(16) uint16_t tmp[SR * TL];
     __shared__ __align__(16) uint16_t srct[TL * TL];
     __shared__ unsigned long long red[24];
     const int it = find_item(items, nitems, blockIdx.x);
@@ -916,13 +927,35 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         hf[k] = u.hf[k];
         vf[k] = u.vf[k];
     }
-    const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
+    const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane], *pre = f.B[wi.plane];
     const bool tout = pl.trial_out != 0;
     uint8_t *outp = f.C[wi.plane];
     const int ph = pl.ph;
+    // interior stripe edges whose rows b - 3 .. b + 2 meet the tile
+    int eb[kTileEdges], ne = 0;
+#pragma unroll
+    for (int e = 0; e < kTileEdges; ++e) eb[e] = INT_MIN / 2;
+    if (tout) {
+        const int ssh = wi.plane ? 1 : 0, full = 64 >> ssh, soff = 8 >> ssh;
+        for (int si = max(1, (y0 - 3 + soff) / full); ne < kTileEdges; ++si) {
+            const int b = si * full - soff;
+            if (b >= ph || b - 3 >= y0 + th) break;
+            if (b + 3 <= y0) continue;
+#pragma unroll
+            for (int e = 0; e < kTileEdges; ++e)
+                if (e == ne) eb[e] = b;
+            ++ne;
+        }
+    }
+    const int na = th + 7, rows = na + 4 * ne;  // A rows, then per edge B[b-2], B[b-1], B[b], B[min(b+1, ph-1)]
     stage_window(
-        bd, pl.pw, th + 7, x0 - 3, tw + 7, true, 0,
-        [&](int rr) { return row_ptr(dg, clampi(y0 - 3 + rr, 0, ph - 1), stride, bd); },
+        bd, pl.pw, rows, x0 - 3, tw + 7, true, 0,
+        [&](int rr) {
+            if (rr < na) return row_ptr(dg, clampi(y0 - 3 + rr, 0, ph - 1), stride, bd);
+            const int e = (rr - na) >> 2, k = (rr - na) & 3;
+            const int b = e == 0 ? eb[0] : e == 1 ? eb[1] : eb[2];
+            return row_ptr(pre, k < 3 ? b - 2 + k : min(b + 1, ph - 1), stride, bd);
+        },
         [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
     stage_window(
         bd, pl.pw, th, x0, tw, true, 0, [&](int rr) { return row_ptr(sr, y0 + rr, stride, bd); },
@@ -932,10 +965,10 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
     // pass is 4 multiplies per output on pair sums, the centre tap carrying
     // the 128 of wiener_convolve_add_src; a thread takes four outputs along
     // the pass from 11 staged samples.
-    // horizontal: (th + 7) rows x 16 runs of four columns
+    // horizontal: every staged row x 16 runs of four columns
     {
         const int c3 = 128 + hf[3], off = 1 << (bd + 6), lim = (1 << (bd + 5)) - 1;
-        for (int q = threadIdx.x; q < (th + 7) * (TL / 4); q += blockDim.x) {
+        for (int q = threadIdx.x; q < rows * (TL / 4); q += blockDim.x) {
             const int rr = q >> 4, c0 = (q & 15) * 4;
             if (c0 >= tw) continue;
             const uint16_t *sp = stage + rr * SW + c0;
@@ -953,32 +986,57 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         }
     }
     __syncthreads();
+    const int c3 = 128 + vf[3], voff = -(1 << (bd + 10)), vmax = (1 << bd) - 1;
+    auto vert = [&](const int *p) {
+        const int sum = p[3] * c3 + vf[0] * (p[0] + p[6]) + vf[1] * (p[1] + p[5]) + vf[2] * (p[2] + p[4]) + voff;
+        return clampi((sum + (1 << 10)) >> 11, 0, vmax);
+    };
+    auto edge_row = [&](int y) {  // y within 3 rows of a stripe edge of this tile
+        bool hit = false;
+#pragma unroll
+        for (int e = 0; e < kTileEdges; ++e) hit |= y >= eb[e] - 3 && y < eb[e] + 3;
+        return hit;
+    };
     // vertical: runs of four rows x 64 columns, SSE parts, trial output
     unsigned long long blk = 0, rgt = 0, bot = 0;
-    {
-        const int c3 = 128 + vf[3], off = -(1 << (bd + 10)), vmax = (1 << bd) - 1;
-        for (int q = threadIdx.x; q < ((th + 3) >> 2) * TL; q += blockDim.x) {
-            const int r0 = (q >> 6) * 4, cc = q & (TL - 1);
-            if (cc >= tw) continue;
-            int p[11];
+    for (int q = threadIdx.x; q < ((th + 3) >> 2) * TL; q += blockDim.x) {
+        const int r0 = (q >> 6) * 4, cc = q & (TL - 1);
+        if (cc >= tw) continue;
+        int p[11];
 #pragma unroll
-            for (int k = 0; k < 11; ++k) p[k] = tmp[(r0 + k) * TL + cc];
-            const int j = tx + cc;
+        for (int k = 0; k < 11; ++k) p[k] = tmp[(r0 + k) * TL + cc];
+        const int j = tx + cc;
 #pragma unroll
-            for (int jj = 0; jj < 4; ++jj) {
-                const int rr = r0 + jj;
-                if (rr >= th) break;
-                const int sum = p[jj + 3] * c3 + vf[0] * (p[jj] + p[jj + 6]) + vf[1] * (p[jj + 1] + p[jj + 5]) +
-                                vf[2] * (p[jj + 2] + p[jj + 4]) + off;
-                const int y = clampi((sum + (1 << 10)) >> 11, 0, vmax);
-                if (tout) stpx(outp, (int64_t)(y0 + rr) * stride + x0 + cc, bd, y);
-                const int e = (int)srct[rr * TL + cc] - y;
-                const unsigned long long e2 = (unsigned long long)((long long)e * e);
-                if (j >= uw - dw) rgt += e2;
-                else if (ty + rr >= uh - dh) bot += e2;
-                else blk += e2;
-            }
+        for (int jj = 0; jj < 4; ++jj) {
+            const int rr = r0 + jj;
+            if (rr >= th) break;
+            const int y = vert(p + jj);
+            if (tout && !edge_row(y0 + rr)) stpx(outp, (int64_t)(y0 + rr) * stride + x0 + cc, bd, y);
+            const int e = (int)srct[rr * TL + cc] - y;
+            const unsigned long long e2 = (unsigned long long)((long long)e * e);
+            if (j >= uw - dw) rgt += e2;
+            else if (ty + rr >= uh - dh) bot += e2;
+            else blk += e2;
         }
+    }
+    // the apply's rows at the stripe edges: tmp rows of A (index y - y0 + 3)
+    // or of the edge's B rows (index na + 4 e + k)
+    for (int q = threadIdx.x; q < ne * 6 * TL; q += blockDim.x) {
+        const int e = q / (6 * TL), k6 = (q >> 6) % 6, cc = q & (TL - 1);
+        const int b = e == 0 ? eb[0] : e == 1 ? eb[1] : eb[2];
+        const int y = b - 3 + k6;
+        if (cc >= tw || y < y0 || y >= y0 + th) continue;
+        const int bb = na + 4 * e;
+        int tp[7];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            const int t = y - 3 + k;
+            int row;
+            if (y < b) row = t < b ? t - y0 + 3 : bb + (t == b ? 2 : 3);
+            else row = t < b ? bb + (t == b - 1 ? 1 : 0) : t - y0 + 3;
+            tp[k] = tmp[row * TL + cc];
+        }
+        stpx(outp, (int64_t)y * stride + x0 + cc, bd, vert(tp));
     }
     unsigned long long v[3] = {blk, rgt, bot};
 #pragma unroll
@@ -992,64 +1050,6 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         unsigned long long s = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x * 8 + w];
         if (s) atomicAdd(threadIdx.x == 0 ? &u.tw_blk : threadIdx.x == 1 ? &u.tw_rgt : &u.tw_bot, s);
-    }
-    if (!tout) return;
-    // The apply's pixels of this tile (apply_restoration_frame, restoration
-    // .rs:992-1052): equal to the trial's except within 3 rows of an interior
-    // stripe edge b (stripes of 64 rows, the first 8 shorter, halved for
-    // chroma), where the apply reads the post-deblock lines that
-    // save_lr_boundaries keeps: the upper stripe's rows b-3..b-1 take B[b]
-    // and B[min(b+1, ph-1)] in place of rows >= b, the lower stripe's rows
-    // b..b+2 take B[b-1] and B[b-2] in place of rows < b. Those rows are
-    // recomputed here with the same taps, so C ends final for a Wiener unit.
-    const int ssh = wi.plane ? 1 : 0, full = 64 >> ssh, soff = 8 >> ssh;
-    const int yA = y0 - 3;  // plane row of tmp row 0
-    const uint8_t *pre = f.B[wi.plane];
-    uint16_t *hb = srct;    // the four B rows after the horizontal pass
-    const int hc3 = 128 + hf[3], hoff = 1 << (bd + 6), hlim = (1 << (bd + 5)) - 1;
-    const int vc3 = 128 + vf[3], voff = -(1 << (bd + 10)), vmax = (1 << bd) - 1;
-    for (int si = max(1, (y0 + soff) / full);; ++si) {
-        const int b = si * full - soff;
-        if (b >= ph || b - 3 >= y0 + th) break;
-        if (b + 3 <= y0) continue;
-        __syncthreads();  // C rows of the main pass written; stage and hb free
-        // rows b - 2, b - 1, b, min(b + 1, ph - 1)
-        stage_window(
-            bd, pl.pw, 4, x0 - 3, tw + 7, true, 0,
-            [&](int rr) { return row_ptr(pre, rr < 3 ? b - 2 + rr : min(b + 1, ph - 1), stride, bd); },
-            [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
-        __syncthreads();
-        for (int q = threadIdx.x; q < 4 * (TL / 4); q += blockDim.x) {
-            const int rr = q >> 4, c0 = (q & 15) * 4;
-            if (c0 >= tw) continue;
-            const uint16_t *sp = stage + rr * SW + c0;
-            int p[11];
-#pragma unroll
-            for (int k = 0; k < 11; ++k) p[k] = sp[k];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int sum = p[j + 3] * hc3 + hf[0] * (p[j] + p[j + 6]) + hf[1] * (p[j + 1] + p[j + 5]) +
-                                hf[2] * (p[j + 2] + p[j + 4]) + hoff;
-                hb[rr * TL + c0 + j] = (uint16_t)clampi((sum + 4) >> 3, 0, hlim);
-            }
-        }
-        __syncthreads();
-        for (int q = threadIdx.x; q < 6 * TL; q += blockDim.x) {
-            const int y = b - 3 + (q >> 6), cc = q & (TL - 1);
-            if (cc >= tw || y < y0 || y >= y0 + th) continue;
-            int tp[7];
-#pragma unroll
-            for (int k = 0; k < 7; ++k) {
-                const int t = y - 3 + k;
-                int row;  // index into tmp (A rows) or hb (B rows, marked by >= 1000)
-                if (y < b) row = t < b ? t - yA : 1000 + (t == b ? 2 : 3);
-                else row = t < b ? 1000 + (t == b - 1 ? 1 : 0) : t - yA;
-                tp[k] = row >= 1000 ? hb[(row - 1000) * TL + cc] : tmp[row * TL + cc];
-            }
-            const int sum = tp[3] * vc3 + vf[0] * (tp[0] + tp[6]) + vf[1] * (tp[1] + tp[5]) +
-                            vf[2] * (tp[2] + tp[4]) + voff;
-            stpx(outp, (int64_t)y * stride + x0 + cc, bd, clampi((sum + (1 << 10)) >> 11, 0, vmax));
-        }
     }
 }
 
