@@ -228,12 +228,11 @@ def kernel_bytes(name, w, h, px):
         "k_deblock_sse": 2 * plane,        # read recon + source
         "k_cdef_search": 2 * plane,        # read deblocked + source
         "k_cdef_apply": 2 * plane,         # read deblocked, write CDEF output
-        "k_lr_sums": 2 * plane,            # read post-CDEF + source
-        "k_lr_stats5": 2 * plane,
+        "k_lr_stats5": 2 * plane,          # read post-CDEF + source
         "k_lr_stats7": 2 * plane,
         "k_lr_trial": 2 * plane,
-        "k_lr_trial_tiles": 2 * plane,
-        "k_lr_apply": 2 * plane,
+        "k_lr_trial_tiles": 3 * plane,     # read post-CDEF + source, write the restored plane
+        "k_lr_apply": 2 * plane,           # at most: read post-CDEF, write restored (units without Wiener)
     }.get(name, 0.0)
 
 

@@ -1405,7 +1405,12 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
             if (!(t == 0 && sec_y == 0)) {  // cdef.rs:444-448
                 int d[12], mx, mn;
                 load_taps_at(edge_y, reg, pos, boff[b], x, d, mx, mn);
-                y = cdef_round(x, prim_sum(d, t, tp >> 16, cs) + sec_sum(d, sec_y, ssh_y), mn, mx);
+                // a zero strength constrains every tap to 0 (its taps still
+                // bound the clamp); t is uniform over the warp, sec_y over the CTA
+                int sum = 0;
+                if (t) sum += prim_sum(d, t, tp >> 16, cs);
+                if (sec_y) sum += sec_sum(d, sec_y, ssh_y);
+                y = cdef_round(x, sum, mn, mx);
                 filt += 1;
                 changed += y != x;
             }
@@ -1431,7 +1436,10 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
                 if (!zero_uv && ((dl >> b) & 1)) {
                     int d[12], mx, mn;
                     load_taps_at(edge_uv, reg, pos, boffc[b], x, d, mx, mn);
-                    y = cdef_round(x, prim_sum(d, lvl_uv, psh, cs) + sec_sum(d, sec_uv, ssh), mn, mx);
+                    int sum = 0;
+                    if (lvl_uv) sum += prim_sum(d, lvl_uv, psh, cs);
+                    if (sec_uv) sum += sec_sum(d, sec_uv, ssh);
+                    y = cdef_round(x, sum, mn, mx);
                     filt += 1;
                     changed += y != x;
                 }

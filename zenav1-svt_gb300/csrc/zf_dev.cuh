@@ -122,9 +122,14 @@ struct WorkItem {
     int cta_begin, ctas;
 };
 
-// Binary search for the work item owning blockIdx.x.
+// The work item owning CTA `cta`. A list of more than one item is followed
+// by a coarse index (written by the host): entry k is the item owning CTA
+// 32 k, then a last entry n - 1; the binary search runs between two
+// neighbouring entries (a few items at most), not over the whole list.
 __device__ __forceinline__ int find_item(const WorkItem *items, int n, int cta) {
-    int lo = 0, hi = n - 1;
+    if (n <= 1) return 0;
+    const int *coarse = reinterpret_cast<const int *>(items + n);
+    int lo = coarse[cta >> 5], hi = coarse[(cta >> 5) + 1];
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
         if (items[mid].cta_begin <= cta) lo = mid; else hi = mid - 1;

@@ -555,6 +555,23 @@ struct WorkList {
         items.push_back(w);
         ctas += n;
     }
+    // Coarse index stored after the items (find_item): entry k is the item
+    // owning CTA 32 k, then a last entry nitems - 1. One-item lists have none.
+    size_t coarse_count() const { return items.size() > 1 ? (size_t)(ctas + 31) / 32 + 1 : 0; }
+    size_t bytes() const { return items.size() * sizeof(WorkItem) + coarse_count() * sizeof(int); }
+    void write(uint8_t *dst) const {
+        std::memcpy(dst, items.data(), items.size() * sizeof(WorkItem));
+        const size_t nc = coarse_count();
+        if (!nc) return;
+        int *c = reinterpret_cast<int *>(dst + items.size() * sizeof(WorkItem));
+        size_t it = 0;
+        for (size_t k = 0; k + 1 < nc; ++k) {
+            const int cta = (int)(k * 32);
+            while (it + 1 < items.size() && items[it + 1].cta_begin <= cta) ++it;
+            c[k] = (int)it;
+        }
+        c[nc - 1] = (int)items.size() - 1;
+    }
 };
 
 int launch_check(zf_ctx *ctx, const char *what) {
@@ -667,14 +684,17 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     const WorkList *lists[kLists] = {&wl_db,   &wl_cs,    &wl_ca,    &wl_st5,  &wl_st7,
                                      &wl_unit, &wl_apply, &wl_trial, &wl_tiles};
     size_t m_list[kLists];
-    for (int k = 0; k < kLists; ++k) m_list[k] = mtake(lists[k]->items.size() * sizeof(WorkItem));
+    for (int k = 0; k < kLists; ++k) m_list[k] = mtake(lists[k]->bytes());
     const size_t m_cf = mtake(cdef_frames.size() * 4);
     const size_t m_rects = mtake(rcur);
     const size_t meta_bytes = align_up(mcur, 256);
-    // deblock search scratch: up to 3 slots per frame
+    // deblock search scratch: up to 3 slots per frame, each of at most the
+    // largest frame's luma tiles (items, then their coarse index)
+    size_t max_tiles = 1;
+    for (const Plan &p : plans) max_tiles = std::max(max_tiles, (size_t)((p.d.w + 63) / 64) * ((p.d.h + 63) / 64));
     size_t c2 = o_meta + meta_bytes;
     const size_t o_dbs_items = c2;
-    c2 += align_up((size_t)n * 3 * 8 * sizeof(WorkItem) + 16, 256);
+    c2 += align_up((size_t)n * 3 * sizeof(WorkItem) + ((size_t)n * 3 * max_tiles / 32 + 2) * sizeof(int) + 16, 256);
     const size_t o_dbs_lv = c2;
     c2 += align_up((size_t)n * 3 * 2 * 4, 256);
     const size_t o_dbs_sse = c2;
@@ -847,8 +867,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 continue;
             }
             if ((int)owner.size() > n * 3) return fail(ctx, ZF_ERR_UNSUPPORTED, "too many search slots");
-            CU(cudaMemcpyAsync(base + o_dbs_items, wl.items.data(), wl.items.size() * sizeof(WorkItem),
-                               cudaMemcpyHostToDevice, st));
+            std::vector<uint8_t> wl_img(wl.bytes());
+            wl.write(wl_img.data());
+            CU(cudaMemcpyAsync(base + o_dbs_items, wl_img.data(), wl_img.size(), cudaMemcpyHostToDevice, st));
             CU(cudaMemcpyAsync(base + o_dbs_lv, lv.data(), lv.size() * 4, cudaMemcpyHostToDevice, st));
             CU(cudaMemsetAsync(base + o_dbs_sse, 0, lv.size() * 8, st));
             { LaunchScope ls_(ctx, "k_deblock_sse");
@@ -881,8 +902,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         FrameDesc *hd = (FrameDesc *)(hm + m_desc);
         for (int i = 0; i < n; ++i) hd[i] = plans[i].d;
         for (int k = 0; k < kLists; ++k)
-            if (!lists[k]->items.empty())
-                std::memcpy(hm + m_list[k], lists[k]->items.data(), lists[k]->items.size() * sizeof(WorkItem));
+            if (!lists[k]->items.empty()) lists[k]->write(hm + m_list[k]);
         if (!cdef_frames.empty()) std::memcpy(hm + m_cf, cdef_frames.data(), cdef_frames.size() * 4);
         CU(cudaMemcpyAsync(base + o_meta, hm, meta_bytes, cudaMemcpyHostToDevice, st));
     }
@@ -1206,7 +1226,10 @@ int32_t zf_query_sizes(const zf_frame *f, zf_sizes *out) {
         items += p.rects[pl].size() * (384 / 16 + 1 + 392 / 12 + 1 + 1 + 1);
         items += (size_t)((p.d.lr[pl].ph + (8 >> ss)) / (64 >> ss) + 2) * ((p.d.lr[pl].pw + 63) / 64 + 1);
     }
-    const size_t meta = align_up(sizeof(FrameDesc), 256) + items * sizeof(WorkItem) + 11 * 256 + rcur;
+    // coarse item indices: one int per 32 CTAs of a list (a 64x64 region
+    // gives fewer than 64 CTAs over all lists) and two per list
+    const size_t coarse = ((size_t)64 * p.d.nhfb * p.d.nvfb / 32 + 2 * 16) * sizeof(int);
+    const size_t meta = align_up(sizeof(FrameDesc), 256) + items * sizeof(WorkItem) + coarse + 11 * 256 + rcur;
     std::memset(out, 0, sizeof(*out));
     out->nhfb = p.d.nhfb;
     out->nvfb = p.d.nvfb;
