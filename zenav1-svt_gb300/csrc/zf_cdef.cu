@@ -1133,16 +1133,35 @@ __global__ void __launch_bounds__(kJointThreads, 1) k_cdef_joint(FrameDesc *fram
     if (cp.mode != 1) return;
     const int nfb = f.nhfb * f.nvfb, n2 = 2 * NC, t = threadIdx.x;
     uint32_t *R = reinterpret_cast<uint32_t *>(joint_dyn);  // R[k * S + slot]
-    int sb = 0;
+    // rows of the owned blocks: every load issued before the stores, one
+    // barrier for the row count
+    __shared__ int s_rows;
+    if (t == 0) s_rows = 0;
+    int mine = 0;
+    {
+        bool row[RPT];
 #pragma unroll
-    for (int r = 0; r < RPT; ++r) {
-        const int fb = r * T + t;
-        const bool row = fb < nfb && f.fb_row[fb];
-        const uint64_t *m = f.mse + (int64_t)fb * n2;
+        for (int r = 0; r < RPT; ++r) {
+            const int fb = r * T + t;
+            row[r] = fb < nfb && f.fb_row[fb];
+            mine += row[r];
+        }
+        uint32_t v[RPT][2 * NC];
 #pragma unroll
-        for (int k = 0; k < 2 * NC; ++k) R[k * S + fb] = row ? (uint32_t)m[k] : 0u;
-        sb += __syncthreads_count(row);
+        for (int r = 0; r < RPT; ++r) {
+            const uint64_t *m = f.mse + (int64_t)(r * T + t) * n2;
+#pragma unroll
+            for (int k = 0; k < 2 * NC; ++k) v[r][k] = row[r] ? (uint32_t)m[k] : 0u;
+        }
+#pragma unroll
+        for (int r = 0; r < RPT; ++r)
+#pragma unroll
+            for (int k = 0; k < 2 * NC; ++k) R[k * S + r * T + t] = v[r][k];
     }
+    __syncthreads();
+    if (mine) atomicAdd(&s_rows, mine);
+    __syncthreads();
+    const int sb = s_rows;
     if (sb == 0) {  // every filter block all-skip: cdef.rs:282-288
         if (level == 0) {
             for (int fb = t; fb < nfb; fb += T) f.fb_idx[fb] = 0;

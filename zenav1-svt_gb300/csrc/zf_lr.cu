@@ -449,54 +449,79 @@ __device__ __forceinline__ int wrap_index(int i, int win) {
     return i >= h1 ? win - 1 - i : i;
 }
 
-__device__ bool linsolve(int n, int64_t *a, int stride, int64_t *b, int32_t *x) {
-    for (int k = 0; k < n - 1; ++k) {
-        for (int i = n - 1; i >= k + 1; --i) {
-            int64_t u = a[(i - 1) * stride + k], v = a[i * stride + k];
+// linsolve_wiener (restoration.rs:801-846) for N unknowns in registers
+// (N = 2 for the 5-tap window, 3 for the 7-tap one): the same pivoting and
+// the same truncating divisions in the same order; independent divisions
+// of one elimination step interleave in the instruction stream.
+template <int N>
+__device__ __forceinline__ bool linsolve_reg(int64_t (&a)[N][N], int64_t (&b)[N], int32_t (&x)[N]) {
+#pragma unroll
+    for (int k = 0; k < N - 1; ++k) {
+#pragma unroll
+        for (int i = N - 1; i >= k + 1; --i) {
+            const int64_t u = a[i - 1][k], v = a[i][k];
             if ((u < 0 ? -u : u) < (v < 0 ? -v : v)) {
-                for (int j = 0; j < n; ++j) {
-                    int64_t t = a[i * stride + j];
-                    a[i * stride + j] = a[(i - 1) * stride + j];
-                    a[(i - 1) * stride + j] = t;
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    const int64_t t = a[i][j];
+                    a[i][j] = a[i - 1][j];
+                    a[i - 1][j] = t;
                 }
-                int64_t t = b[i];
+                const int64_t t = b[i];
                 b[i] = b[i - 1];
                 b[i - 1] = t;
             }
         }
-        for (int i = k; i < n - 1; ++i) {
-            if (a[k * stride + k] == 0) return false;
-            const int64_t c = a[(i + 1) * stride + k], cd = a[k * stride + k];
-            for (int j = 0; j < n; ++j) a[(i + 1) * stride + j] -= c / 256 * a[k * stride + j] / cd * 256;
+        const int64_t cd = a[k][k];
+        if (cd == 0) return false;
+#pragma unroll
+        for (int i = k; i < N - 1; ++i) {
+            const int64_t c = a[i + 1][k];
+#pragma unroll
+            for (int j = 0; j < N; ++j) a[i + 1][j] -= c / 256 * a[k][j] / cd * 256;
             b[i + 1] -= c * b[k] / cd;
         }
     }
-    for (int i = n - 1; i >= 0; --i) {
-        if (a[i * stride + i] == 0) return false;
+#pragma unroll
+    for (int i = N - 1; i >= 0; --i) {
+        if (a[i][i] == 0) return false;
         int64_t c = 0;
-        for (int j = i + 1; j < n; ++j) c += a[i * stride + j] * (int64_t)x[j] / kTapScale;
-        x[i] = (int32_t)(kTapScale * (b[i] - c) / a[i * stride + i]);
+#pragma unroll
+        for (int j = i + 1; j < N; ++j) c += a[i][j] * (int64_t)x[j] / kTapScale;
+        x[i] = (int32_t)(kTapScale * (b[i] - c) / a[i][i]);
     }
     return true;
 }
 
-// normalize_and_solve (restoration.rs:913-941), one thread.
-__device__ void normalize_and_solve(int win, int64_t *av, int64_t *bv, int32_t *out) {
-    const int h1 = (win >> 1) + 1;
-    const int64_t ah = av[h1 - 1];
-    for (int i = 0; i < h1 - 1; ++i) av[i] -= ah * 2 + bv[i * h1 + h1 - 1] - 2 * bv[(h1 - 1) * h1 + (h1 - 1)];
-    for (int i = 0; i < h1 - 1; ++i)
-        for (int j = 0; j < h1 - 1; ++j)
-            bv[i * h1 + j] -= 2 * (bv[i * h1 + (h1 - 1)] + bv[(h1 - 1) * h1 + j] - 2 * bv[(h1 - 1) * h1 + (h1 - 1)]);
-    int32_t s[7] = {0, 0, 0, 0, 0, 0, 0};
-    if (linsolve(h1 - 1, bv, h1, av, s)) {
-        s[h1 - 1] = (int32_t)kTapScale;
-        for (int i = h1; i < win; ++i) {
-            s[i] = s[win - 1 - i];
-            s[h1 - 1] -= 2 * s[i];
-        }
-        for (int i = 0; i < win; ++i) out[i] = s[i];
+// normalize_and_solve (restoration.rs:913-941) in registers, one thread;
+// `out` (WIN taps) is written only when the system solves.
+template <int WIN>
+__device__ __forceinline__ void normalize_and_solve_reg(int64_t (&av)[WIN / 2 + 1], int64_t (&bv)[WIN / 2 + 1][WIN / 2 + 1],
+                                                        int32_t *out) {
+    constexpr int H1 = WIN / 2 + 1, N = H1 - 1;
+    const int64_t ah = av[H1 - 1], bc = bv[H1 - 1][H1 - 1];
+    int64_t a[N][N], b[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        b[i] = av[i] - (ah * 2 + bv[i][H1 - 1] - 2 * bc);
+#pragma unroll
+        for (int j = 0; j < N; ++j) a[i][j] = bv[i][j] - 2 * (bv[i][H1 - 1] + bv[H1 - 1][j] - 2 * bc);
     }
+    int32_t x[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) x[i] = 0;
+    if (!linsolve_reg<N>(a, b, x)) return;
+    int32_t sv[WIN];
+#pragma unroll
+    for (int i = 0; i < N; ++i) sv[i] = x[i];
+    sv[H1 - 1] = (int32_t)kTapScale;
+#pragma unroll
+    for (int i = H1; i < WIN; ++i) {
+        sv[i] = sv[WIN - 1 - i];
+        sv[H1 - 1] -= 2 * sv[i];
+    }
+#pragma unroll
+    for (int i = 0; i < WIN; ++i) out[i] = sv[i];
 }
 
 // Block-wide int64 sum of `n` per-thread bins into out[] (thread 0 valid).
@@ -516,43 +541,75 @@ __device__ void reduce_bins(int64_t (&bins)[NB], int n, int64_t *out) {
     __syncthreads();
 }
 
-// One update_{a,b}_sep_sym (restoration.rs:849-909). `upd_a` selects which
-// factor is solved; `fix` is the other one. Every bin is a sum of
-// independently truncated terms, so the order of the sum is free: a thread
-// owns one bin pair q (the (k, l) of update_a, the (i, j) of update_b) and a
-// slice of the other pair index, and the 20 bins meet in shared memory
-// (`sbins`, zero on entry and on return).
-__device__ void update_sep_sym(bool upd_a, int win, const int64_t *M, const int64_t *H, const int32_t *fix,
-                               int32_t *outv, int64_t *sav, int64_t *sbv, unsigned long long *sbins) {
-    const int win2 = win * win, h1 = (win >> 1) + 1;
-    const int t = threadIdx.x, R = blockDim.x / win2;
-    if (t < R * win2) {
-        const int q = t % win2, sl = t / win2;
-        const int qa = q / win, qb = q - qa * win;
+// One update_{a,b}_sep_sym (restoration.rs:849-909) for a WIN-tap window
+// on a 128-thread CTA. `upd_a` selects which factor is solved; `fix` is the
+// other one. Every bin is a sum of independently truncated terms, so the
+// order of the sum is free: a thread owns one bin pair q (the (k, l) of
+// update_a, the (i, j) of update_b) and a slice of the other pair index and
+// leaves its partial in `part` (plus one partial per av term); lanes of warp
+// 0 add the partials of one bin each (binq lists the pairs of a bin; no
+// atomics) and lane 0 solves in registers.
+template <int WIN>
+__device__ __forceinline__ void update_sep_sym(bool upd_a, const int64_t *M, const int64_t *H, const int32_t *fix,
+                                               int32_t *outv, int64_t *part, int64_t *binv,
+                                               const int8_t (*binq)[4]) {
+    constexpr int W2 = WIN * WIN, H1 = WIN / 2 + 1, R = 128 / W2, NPP = (W2 + R - 1) / R;
+    const int t = threadIdx.x;
+    if (t < R * W2) {
+        const int q = t % W2, sl = t / W2;
+        const int qa = q / WIN, qb = q - qa * WIN;
         int64_t acc = 0;
-        for (int pp = sl; pp < win2; pp += R) {
-            const int pa = pp / win, pb = pp - pa * win;
-            // update_a: (i, j) = (pa, pb), (k, l) = (qa, qb); update_b: (i, j) =
-            // (qa, qb), (k, l) = (pa, pb); the two factors come from `fix`
-            const int64_t hv = upd_a ? H[pb * win * win2 + pa * win + qa * win2 + qb]
-                                     : H[qa * win * win2 + qb * win + pa * win2 + pb];
-            acc += hv * (int64_t)fix[pa] / kTapScale * (int64_t)fix[pb] / kTapScale;
+#pragma unroll
+        for (int k = 0; k < NPP; ++k) {
+            const int pp = sl + k * R;
+            if (pp < W2) {
+                const int pa = pp / WIN, pb = pp - pa * WIN;
+                // update_a: (i, j) = (pa, pb), (k, l) = (qa, qb); update_b:
+                // (i, j) = (qa, qb), (k, l) = (pa, pb); factors from `fix`
+                const int64_t hv = upd_a ? H[pb * WIN * W2 + pa * WIN + qa * W2 + qb]
+                                         : H[qa * WIN * W2 + qb * WIN + pa * W2 + pb];
+                acc += hv * (int64_t)fix[pa] / kTapScale * (int64_t)fix[pb] / kTapScale;
+            }
         }
-        atomicAdd(&sbins[wrap_index(qb, win) * 4 + wrap_index(qa, win)], (unsigned long long)acc);
+        part[t] = acc;
     }
-    if (t < win) {  // av terms: t is j (update_a) or i (update_b)
+    if (t < WIN) {  // av terms: t is j (update_a) or i (update_b)
         int64_t acc = 0;
-        for (int o = 0; o < win; ++o)
-            acc += (upd_a ? M[o * win + t] : M[t * win + o]) * (int64_t)fix[o] / kTapScale;
-        atomicAdd(&sbins[16 + wrap_index(t, win)], (unsigned long long)acc);
+#pragma unroll
+        for (int o = 0; o < WIN; ++o)
+            acc += (upd_a ? M[o * WIN + t] : M[t * WIN + o]) * (int64_t)fix[o] / kTapScale;
+        part[R * W2 + t] = acc;
     }
     __syncthreads();
-    if (t == 0) {
-        for (int a = 0; a < h1; ++a) sav[a] = (int64_t)sbins[16 + a];
-        for (int a = 0; a < h1; ++a)
-            for (int b = 0; b < h1; ++b) sbv[a * h1 + b] = (int64_t)sbins[a * 4 + b];
-        for (int k = 0; k < 20; ++k) sbins[k] = 0;
-        normalize_and_solve(win, sav, sbv, outv);
+    if (t < 32) {
+        // lane t < H1^2: matrix bin t (wrap(qb) = t / H1, wrap(qa) = t % H1);
+        // lane H1^2 + a: vector bin a (wrap(term) = a)
+        if (t < H1 * H1 + H1) {
+            const bool vec = t >= H1 * H1;
+            const int row = vec ? 16 + t - H1 * H1 : t;
+            int64_t sum = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int q = binq[row][k];
+                if (q < 0) continue;
+                if (vec) sum += part[R * W2 + q];
+                else
+#pragma unroll
+                    for (int sl = 0; sl < R; ++sl) sum += part[sl * W2 + q];
+            }
+            binv[t] = sum;
+        }
+        __syncwarp();
+        if (t == 0) {
+            int64_t av[H1], bv[H1][H1];
+#pragma unroll
+            for (int i = 0; i < H1; ++i) {
+                av[i] = binv[H1 * H1 + i];
+#pragma unroll
+                for (int j = 0; j < H1; ++j) bv[i][j] = binv[i * H1 + j];
+            }
+            normalize_and_solve_reg<WIN>(av, bv, outv);
+        }
     }
     __syncthreads();
 }
@@ -579,18 +636,21 @@ __device__ void finalize_sym(int win, const int32_t *f, int16_t *fi) {
     fi[7] = 0;
 }
 
-// items: a = unit. One CTA (128 threads) per unit.
-__global__ void __launch_bounds__(128) k_lr_solve(FrameDesc *frames, const WorkItem *items, int nitems) {
-    __shared__ int64_t H[2401];
-    __shared__ int64_t M[49];
-    __shared__ int32_t a[7], b[7];
-    __shared__ int64_t sav[4], sbv[16];
+// One unit's solve (the WIN-tap window), 128 threads.
+template <int WIN>
+__device__ __forceinline__ void solve_unit(const FrameDesc &f, const LrPlane &pl, int unit) {
+    constexpr int W2 = WIN * WIN, H1 = WIN / 2 + 1, R = 128 / W2;
+    __shared__ int64_t H[W2 * W2];
+    __shared__ int64_t M[W2], Sv[W2];
+    __shared__ int32_t a[WIN], b[WIN];
+    __shared__ int64_t spart[128 + 8];
+    __shared__ int64_t binv[H1 * H1 + H1];
+    __shared__ int8_t binq[20][4];
     __shared__ int16_t vf[8], hf[8];
-    const WorkItem wi = items[blockIdx.x];
-    FrameDesc &f = frames[wi.frame];
-    const LrPlane &pl = f.lr[wi.plane];
-    LrUnit &u = pl.units[wi.a];
-    const int win = pl.win, win2 = win * win;
+    __shared__ int32_t ab[W2];
+    static_assert(R * W2 + WIN <= 128 + 8, "partials fit");
+    LrUnit &u = pl.units[unit];
+    const int t = threadIdx.x;
     // The raw-sample sums corrected by the unit average A = find_average
     // (restoration.rs:198: the centre shift sum over the pixel count), then
     // the bit-depth divider on M and the upper triangle (truncating division
@@ -598,46 +658,80 @@ __global__ void __launch_bounds__(128) k_lr_solve(FrameDesc *frames, const WorkI
     // mirrored (compute_stats_hbd, restoration.rs:1799-1806).
     const bool hbd = f.bd == 10;
     auto divd = [hbd](int64_t v) { return hbd ? (v + ((v >> 63) & 3)) >> 2 : v; };
-    const UnitRect rc = pl.rects[wi.a];
+    const UnitRect rc = pl.rects[unit];
     const int64_t n = (int64_t)(rc.h_end - rc.h_start) * (rc.v_end - rc.v_start);
-    const int ctr = (win >> 1) * win + (win >> 1);
+    constexpr int ctr = (WIN / 2) * WIN + WIN / 2;
     const int64_t A = (int64_t)((unsigned long long)u.s[ctr] / (unsigned long long)n), nAA = n * A * A;
-    __shared__ unsigned long long sbins[20];
-    if (threadIdx.x < 20) sbins[threadIdx.x] = 0;
-    for (int k = threadIdx.x; k < win2; k += blockDim.x) M[k] = divd(u.m[k] - A * (u.s[k] + u.sum_src) + nAA);
-    for (int t = threadIdx.x; t < win2 * win2; t += blockDim.x) {
-        const int k = t / win2, l = t - k * win2;
-        if (l >= k) {
-            const int64_t v = divd(u.h[t] - A * (u.s[k] + u.s[l]) + nAA);
-            H[t] = v;
-            H[l * win2 + k] = v;
-        }
+    if (t < W2) {
+        Sv[t] = u.s[t];
+        M[t] = divd(u.m[t] - A * (u.s[t] + u.sum_src) + nAA);
     }
-    if (threadIdx.x == 0) {
+    // bins of update_sep_sym: matrix bin a * H1 + b holds the pairs q =
+    // qa * WIN + qb with wrap(qb) = a, wrap(qa) = b (at most 4); vector bin a
+    // (row 16 + a) the terms o with wrap(o) = a (at most 2)
+    if (t < 20) {
+        int nq = 0;
+        int8_t lst[4] = {-1, -1, -1, -1};
+        if (t < H1 * H1) {
+            const int ra = t / H1, rb = t - ra * H1;
+            for (int qa = 0; qa < WIN; ++qa)
+                for (int qb = 0; qb < WIN; ++qb)
+                    if (wrap_index(qb, WIN) == ra && wrap_index(qa, WIN) == rb && nq < 4)
+                        lst[nq++] = (int8_t)(qa * WIN + qb);
+        } else if (t >= 16 && t < 16 + H1) {
+            for (int o = 0; o < WIN; ++o)
+                if (wrap_index(o, WIN) == t - 16 && nq < 4) lst[nq++] = (int8_t)o;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) binq[t][k] = lst[k];
+    }
+    if (t == 0) {
         if (f.bd == 8) u.sse_none = (int64_t)(u.sse_blk + u.sse_rgt + u.sse_bot);
         else u.sse_none = (int64_t)u.sse_blk + (int64_t)(uint32_t)u.sse_rgt + (int64_t)(uint32_t)u.sse_bot;
-        const int off = (7 - win) >> 1;
+        constexpr int off = (7 - WIN) >> 1;
         const int init[7] = {3, -7, 15, kStep - 2 * (3 - 7 + 15), 15, -7, 3};
-        for (int i = 0; i < win; ++i) {
+#pragma unroll
+        for (int i = 0; i < WIN; ++i) {
             a[i] = (int32_t)(kTapScale / kStep) * init[i + off];
             b[i] = a[i];
         }
     }
     __syncthreads();
-    for (int round = 1; round < 5; ++round) {
-        update_sep_sym(true, win, M, H, b, a, sav, sbv, sbins);
-        update_sep_sym(false, win, M, H, a, b, sav, sbv, sbins);
+    // H in chunks of five entries per thread, the loads issued first
+    for (int t0 = 0; t0 < W2 * W2; t0 += 5 * 128) {
+        int64_t hv[5];
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+            const int q = t0 + c * 128 + t;
+            hv[c] = q < W2 * W2 ? u.h[q] : 0;
+        }
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+            const int q = t0 + c * 128 + t;
+            if (q >= W2 * W2) break;
+            const int k = q / W2, l = q - k * W2;
+            if (l >= k) {
+                const int64_t v = divd(hv[c] - A * (Sv[k] + Sv[l]) + nAA);
+                H[q] = v;
+                H[l * W2 + k] = v;
+            }
+        }
     }
-    if (threadIdx.x == 0) {
+    __syncthreads();
+    for (int round = 1; round < 5; ++round) {
+        update_sep_sym<WIN>(true, M, H, b, a, spart, binv, binq);
+        update_sep_sym<WIN>(false, M, H, a, b, spart, binv, binq);
+    }
+    if (t == 0) {
         for (int i = 0; i < 8; ++i) {
             vf[i] = 0;
             hf[i] = 0;
         }
-        finalize_sym(win, a, vf);
-        finalize_sym(win, b, hf);
+        finalize_sym(WIN, a, vf);
+        finalize_sym(WIN, b, hf);
         for (int i = 0; i < 7; ++i) {
-            u.vd[i] = i < win ? a[i] : 0;
-            u.hd[i] = i < win ? b[i] : 0;
+            u.vd[i] = i < WIN ? a[i] : 0;
+            u.hd[i] = i < WIN ? b[i] : 0;
         }
         for (int i = 0; i < 8; ++i) {
             u.vf[i] = vf[i];
@@ -645,38 +739,40 @@ __global__ void __launch_bounds__(128) k_lr_solve(FrameDesc *frames, const WorkI
         }
     }
     __syncthreads();
-    // compute_score (restoration.rs:1009-1056).
-    __shared__ int32_t ab[49];
-    if (threadIdx.x == 0) {
-        int16_t av[7] = {0}, bv[7] = {0};
-        const int off = (7 - win) >> 1;
-        av[3] = kStep;
-        bv[3] = kStep;
-        for (int i = 0; i < 3; ++i) {
-            av[i] = vf[i];
-            av[6 - i] = vf[i];
-            bv[i] = hf[i];
-            bv[6 - i] = hf[i];
-            av[3] = (int16_t)(av[3] - 2 * av[i]);
-            bv[3] = (int16_t)(bv[3] - 2 * bv[i]);
-        }
-        for (int k = 0; k < win; ++k)
-            for (int l = 0; l < win; ++l) ab[k * win + l] = (int32_t)av[l + off] * (int32_t)bv[k + off];
+    // compute_score (restoration.rs:1009-1056): ab[k * WIN + l] = av[l + off]
+    // * bv[k + off], av / bv the symmetric 7-tap filters of vf / hf (centre
+    // 128 - 2 * the others).
+    if (t < W2) {
+        constexpr int off = (7 - WIN) >> 1;
+        auto tap7 = [](const int16_t *fl, int i) -> int32_t {
+            return i == 3 ? (int16_t)(kStep - 2 * (fl[0] + fl[1] + fl[2])) : fl[i < 3 ? i : 6 - i];
+        };
+        const int k = t / WIN, l = t - k * WIN;
+        ab[t] = tap7(vf, l + off) * tap7(hf, k + off);
     }
     __syncthreads();
     int64_t bins[2] = {0, 0};
-    for (int k = threadIdx.x; k < win2; k += blockDim.x) bins[0] += (int64_t)ab[k] * M[k] / kStep / kStep;
-    for (int t = threadIdx.x; t < win2 * win2; t += blockDim.x) {
-        const int k = t / win2, l = t - k * win2;
-        bins[1] += (int64_t)ab[k] * H[t] * (int64_t)ab[l] / kStep / kStep / kStep / kStep;
+    if (t < W2) bins[0] = (int64_t)ab[t] * M[t] / kStep / kStep;
+    for (int q = t; q < W2 * W2; q += 128) {
+        const int k = q / W2, l = q - k * W2;
+        bins[1] += (int64_t)ab[k] * H[q] * (int64_t)ab[l] / kStep / kStep / kStep / kStep;
     }
     __shared__ int64_t pq[2];
     reduce_bins<2>(bins, 2, pq);
-    if (threadIdx.x == 0) {
+    if (t == 0) {
         const int64_t score = pq[1] - 2 * pq[0];
-        const int64_t ip = M[win2 >> 1], iq = H[(win2 >> 1) * win2 + (win2 >> 1)];
+        const int64_t ip = M[W2 >> 1], iq = H[(W2 >> 1) * W2 + (W2 >> 1)];
         u.score = score - (iq - 2 * ip);
     }
+}
+
+// items: a = unit. One CTA (128 threads) per unit.
+__global__ void __launch_bounds__(128) k_lr_solve(FrameDesc *frames, const WorkItem *items, int nitems) {
+    const WorkItem wi = items[blockIdx.x];
+    const FrameDesc &f = frames[wi.frame];
+    const LrPlane &pl = f.lr[wi.plane];
+    if (pl.win == 5) solve_unit<5>(f, pl, wi.a);
+    else solve_unit<7>(f, pl, wi.a);
 }
 
 // ---------------------------------------------------------------------------
