@@ -43,7 +43,7 @@ __global__ void k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems)
 __global__ void k_lr_trial_tiles(FrameDesc *frames, const WorkItem *items, int nitems);
 constexpr int kTrialTileHost = 64;  // k_lr_trial_tiles tile edge
 constexpr int kTrialClusterHost = 8;  // k_lr_trial: CTAs per unit (cluster size)
-constexpr int kLrFinThreadsHost = 256;  // k_lr_finish CTA size
+constexpr int kLrFinThreadsHost = 1024;  // k_lr_finish CTA size
 constexpr int kLrPairMaxHost = 20100;   // k_lr_finish pair-table entries (units <= 200)
 __global__ void k_lr_finish(FrameDesc *frames, int nframes);
 __global__ void k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems);

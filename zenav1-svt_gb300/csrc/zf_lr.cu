@@ -1216,7 +1216,7 @@ struct RdUnit {
     int64_t sse_none, sse_wn;
     int16_t v[3], h[3];
     int16_t pick;
-    int16_t thr;  // WIENER beats NONE iff the tap bits <= thr (-1: never)
+    int16_t thr;  // WIENER beats NONE iff the tap bits <= thr (-1: never); after the walk, the WIENER bits
 };
 
 
@@ -1228,8 +1228,9 @@ struct RdUnit {
 // of k's taps against j's taps and whether WIENER beats NONE for k under
 // that reference. The walk then only looks pairs up. Planes with more units
 // than the pair table holds walk with the full evaluation per unit.
-constexpr int kLrFinThreads = 256;
+constexpr int kLrFinThreads = 1024;
 constexpr int kLrPairMax = 20100;  // units <= 200 (pair table of int32 in shared memory)
+constexpr int kLrPairUnits = 200;
 
 // Bits of one tap as a table over (reference, value) for the three tap
 // positions (ranges [-5, 10], [-23, 8], [-17, 46]; finalize_sym_filter and the
@@ -1336,22 +1337,108 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
     for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
     if ((t & 31) == 0) red[t >> 5] = part;
     __syncthreads();
+    // units with a trial (bit k of vmask), and each unit's taps packed for
+    // the pair table: bytes v1 + 23, v2 + 17, h1 + 23, h2 + 17, then v0 + 5,
+    // h0 + 5 (the tap tables' row / column offsets)
+    __shared__ unsigned vmask[(kLrPairUnits + 31) / 32];
+    __shared__ unsigned long long ptap[kLrPairUnits + 1];
     if (table) {
+        if (t < kLrPairUnits + 1) {
+            const int16_t dv[3] = {3, -7, 15};
+            const int16_t *v = t < n ? U[t].v : dv, *h = t < n ? U[t].h : dv;  // entry n: the default reference
+            ptap[t] = (unsigned long long)((v[1] + 23) | (v[2] + 17) << 8 | (h[1] + 23) << 16 | (h[2] + 17) << 24) |
+                      (unsigned long long)((v[0] + 5) | (h[0] + 5) << 8) << 32;
+        }
+        if (t < ((kLrPairUnits + 31) / 32) * 32) {
+            const unsigned m = __ballot_sync(0xffffffffu, t < n && U[t].sse_wn != INT64_MAX);
+            if ((t & 31) == 0) vmask[t >> 5] = m;
+        }
+        __syncthreads();
         // pair (k, j), j in [-1, k): index k (k + 1) / 2 + j + 1; entry =
-        // bits_wn | pick << 30 (bits_wn < 2^16)
-        const int16_t dflt[3] = {3, -7, 15};
-        for (int idx = t; idx < npairs; idx += blockDim.x) {
-            int k = (int)((sqrtf(8.0f * (float)idx + 1.0f) - 1.0f) * 0.5f);
-            while (k * (k + 1) / 2 > idx) --k;
-            while ((k + 1) * (k + 2) / 2 <= idx) ++k;
-            const int j = idx - k * (k + 1) / 2 - 1;
-            const RdUnit &u = U[k];
-            if (u.sse_wn == INT64_MAX) {
-                PT[idx] = 0;
+        // bits_wn | pick << 30 (bits_wn < 2^16). A warp per row k, lanes
+        // over j (the unit's taps broadcast, the references' consecutive).
+        const int lane = t & 31, warp = t >> 5, nw = blockDim.x >> 5;
+        for (int k = warp; k < n; k += nw) {
+            const int base = k * (k + 1) / 2 + 1;
+            if (!((vmask[k >> 5] >> (k & 31)) & 1)) {
+                for (int j = lane - 1; j < k; j += 32) PT[base + j] = 0;
                 continue;
             }
-            const int cnt = count_bits_tab(tb, pl.win, u.v, u.h, j < 0 ? dflt : U[j].v, j < 0 ? dflt : U[j].h);
-            PT[idx] = (320 + (cnt << 9)) | (cnt <= u.thr ? 1 << 30 : 0);
+            const unsigned long long pk = ptap[k];
+            const int thr = U[k].thr;
+            for (int j = lane - 1; j < k; j += 32) {
+                const unsigned long long pj = ptap[j < 0 ? n : j];
+                const unsigned a = (unsigned)pk, r = (unsigned)pj;
+                int cnt = tb.t1[(r & 0xff) * kTb1 + (a & 0xff)] + tb.t2[((r >> 8) & 0xff) * kTb2 + ((a >> 8) & 0xff)] +
+                          tb.t1[((r >> 16) & 0xff) * kTb1 + ((a >> 16) & 0xff)] + tb.t2[(r >> 24) * kTb2 + (a >> 24)];
+                if (pl.win == 7) {
+                    const unsigned a0 = (unsigned)(pk >> 32), r0 = (unsigned)(pj >> 32);
+                    cnt += tb.t0[(r0 & 0xff) * kTb0 + (a0 & 0xff)] + tb.t0[(r0 >> 8) * kTb0 + (a0 >> 8)];
+                }
+                PT[base + j] = (320 + (cnt << 9)) | (cnt <= thr ? 1 << 30 : 0);
+            }
+        }
+        __syncthreads();
+    }
+    // The walk (count_wiener_bits chained through the last WIENER unit's
+    // taps): with the pair table its only serial step is the lookup of
+    // (unit, last WIENER unit); each unit's pick and WIENER bits are recorded
+    // and the frame's bits and SSE are summed by all threads afterwards.
+    __shared__ int64_t fsum[2];
+    if (t == 0) {
+        if (table) {
+            int last = -1;
+            unsigned vm = 0;
+            for (int k = 0; k < n; ++k) {
+                if ((k & 31) == 0) vm = vmask[k >> 5];
+                if (!((vm >> (k & 31)) & 1)) continue;  // no trial: pick stays 0
+                const int32_t e = PT[k * (k + 1) / 2 + last + 1];
+                const bool pick = (e >> 30) & 1;
+                U[k].pick = pick ? 1 : 0;
+                U[k].thr = (int16_t)(e & 0xffff);  // the WIENER bits, read back below
+                last = pick ? k : last;
+            }
+        } else {
+            int16_t rv[3] = {3, -7, 15}, rh[3] = {3, -7, 15};
+            for (int k = 0; k < n; ++k) {
+                RdUnit &u = U[k];
+                if (u.sse_wn == INT64_MAX) continue;
+                int64_t bits_wn;
+                bool pick;
+                unit_rd(f, pl, u, rv, rh, tb, bits_wn, pick);
+                u.pick = pick ? 1 : 0;
+                u.thr = (int16_t)bits_wn;
+                if (pick)
+                    for (int i = 0; i < 3; ++i) {
+                        rv[i] = u.v[i];
+                        rh[i] = u.h[i];
+                    }
+            }
+        }
+    }
+    __syncthreads();
+    {
+        int64_t bsum = 0, ssum = 0;
+        for (int k = t; k < n; k += blockDim.x) {
+            const RdUnit &u = U[k];
+            if (u.pick) {
+                bsum += (uint16_t)u.thr;
+                ssum += u.sse_wn;
+            } else {
+                bsum += 768;
+                ssum += u.sse_none;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            bsum += __shfl_down_sync(0xffffffffu, bsum, o);
+            ssum += __shfl_down_sync(0xffffffffu, ssum, o);
+        }
+        if (t < 2) fsum[t] = 0;
+        __syncthreads();
+        if ((t & 31) == 0) {
+            atomicAdd((unsigned long long *)&fsum[0], (unsigned long long)bsum);
+            atomicAdd((unsigned long long *)&fsum[1], (unsigned long long)ssum);
         }
         __syncthreads();
     }
@@ -1359,40 +1446,7 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
         int64_t total = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += red[w];
         const double cost_none_frame = rdcost_dbl(f.rdmult, 0, total);
-        int64_t bits_frame = 0, sse_frame = 0;
-        int16_t rv[3] = {3, -7, 15}, rh[3] = {3, -7, 15};
-        int last = -1;
-        for (int k = 0; k < n; ++k) {
-            RdUnit &u = U[k];
-            if (u.sse_wn == INT64_MAX) {
-                bits_frame += 768;
-                sse_frame += u.sse_none;
-                continue;
-            }
-            int64_t bits_wn;
-            bool pick;
-            if (table) {
-                const int32_t e = PT[k * (k + 1) / 2 + last + 1];
-                bits_wn = e & 0xffff;
-                pick = (e >> 30) & 1;
-            } else {
-                unit_rd(f, pl, u, rv, rh, tb, bits_wn, pick);
-            }
-            if (pick) {
-                u.pick = 1;
-                bits_frame += bits_wn;
-                sse_frame += u.sse_wn;
-                last = k;
-                for (int i = 0; i < 3; ++i) {
-                    rv[i] = u.v[i];
-                    rh[i] = u.h[i];
-                }
-            } else {
-                bits_frame += 768;
-                sse_frame += u.sse_none;
-            }
-        }
-        const double cost_wn_frame = rdcost_dbl(f.rdmult, bits_frame >> 4, sse_frame);
+        const double cost_wn_frame = rdcost_dbl(f.rdmult, fsum[0] >> 4, fsum[1]);
         frame_rtype = cost_wn_frame < cost_none_frame ? 1 : 0;
         pl.frame_rtype = frame_rtype;
     }
