@@ -244,6 +244,47 @@ int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_decisions *ou
 
 /* --- Observability ------------------------------------------------------- */
 
+/* ---- Self-guided restoration (RESTORE_SGRPROJ) ---------------------------
+ * No counterpart in the reference encoder: it never searches or signals
+ * SGRPROJ (svtav1-dsp/src/restoration.rs:1280, svtav1-encoder/src/
+ * restoration.rs:8); the reference project documents the filter in
+ * specs/08-loop-filters.md:371-421. The filter is the AV1 specification's
+ * box filter and self-guided projection (section 7.17.3, Sgr_Params); the
+ * apply is decoder-exact (stripe-aware sample fetch). The search is this
+ * library's: for every restoration unit and every parameter set of the
+ * mask, the least-squares projection weights (solved exactly), then the SSE
+ * of the unit filtered with them; the set of the smallest SSE wins (the
+ * lowest set on ties). Units are the plane's 256-sample restoration units
+ * (count_units_in_tile per dimension, rows offset by 8 >> ss_y), row-major;
+ * the search filters each unit with samples clamped to the plane (no
+ * stripes), like the Wiener search. */
+typedef struct zf_sgr_plane {
+    int32_t bit_depth;          /* 8 or 10 (u8 or u16 samples) */
+    int32_t width, height;      /* plane dims; rows are width samples apart */
+    int32_t ss_y;               /* 1 for 4:2:0 chroma (32-row stripes, offset 4) */
+    int32_t on_device;          /* 1: the plane pointers are device pointers */
+    const void *dgd;            /* post-CDEF plane (filter input) */
+    const void *src;            /* source plane (search only) */
+    const void *pre_cdef;       /* post-deblock plane (apply only: stripe edges) */
+} zf_sgr_plane;
+
+typedef struct zf_sgr_unit {
+    int32_t set;                /* Sgr_Params index 0..15; -1: unit not filtered */
+    int32_t xqd[2];             /* weights w0, w1 (w2 = 128 - w0 - w1) */
+    int32_t pad;
+    int64_t sse;                /* search: SSE of the unit filtered with set, xqd */
+    int64_t sse_none;           /* search: SSE of the unfiltered unit */
+} zf_sgr_unit;
+
+/* Per-unit search over the sets of set_mask (bit k = set k, non-zero).
+ * nunits must be the plane's unit count. */
+int32_t zf_sgr_search(zf_ctx *ctx, const zf_sgr_plane *p, uint32_t set_mask, zf_sgr_unit *units,
+                      int32_t nunits);
+/* Decoder-exact apply into dst (width x height, same memory kind as the
+ * planes, distinct from dgd and pre_cdef); units with set < 0 are copied. */
+int32_t zf_sgr_apply(zf_ctx *ctx, const zf_sgr_plane *p, const zf_sgr_unit *units, int32_t nunits,
+                     void *dst);
+
 typedef struct zf_kernel_time {
     char name[32];
     uint64_t launches;

@@ -84,6 +84,10 @@ def lib():
                                       P(C.c_int16), P(C.c_int16), C.c_int32, C.c_int32, C.c_int32]
     L.zfo_sse_region.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     L.zfo_sse_region.restype = C.c_int64
+    L.zfo_sgr_search.argtypes = [C.c_int32] * 4 + [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+    L.zfo_sgr_apply.argtypes = [C.c_int32] * 4 + [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.zfo_sgr_box_filter.argtypes = [C.c_int32] * 3 + [C.c_void_p] + [C.c_int32] * 6 + [C.c_void_p]
+    L.zfo_sgr_params.argtypes = [C.c_int32, P(C.c_int32)]
     _lib = L
     return L
 
@@ -169,3 +173,47 @@ def lr_apply(fr, rec, pre_cdef, dec, border=BORDER_C):
     s = _frame(fr, rec)
     pre = (C.c_void_p * 3)(*[p.ctypes.data for p in pre_cdef])
     assert lib().zfo_lr_apply(C.byref(s), pre, C.byref(dec.c), border) == 0
+
+
+# Self-guided restoration (AV1 spec 7.17.3; the reference encoder has none).
+SGR_UNIT = np.dtype([("set", np.int32), ("w0", np.int32), ("w1", np.int32), ("pad", np.int32),
+                     ("sse", np.int64), ("sse_none", np.int64)])
+
+
+def sgr_units_shape(pw, ph):
+    L = lib()
+    return L.zfo_count_units_in_tile(256, pw) * L.zfo_count_units_in_tile(256, ph)
+
+
+def sgr_search(bd, dgd, src, ss=0, set_mask=0xFFFF):
+    """Per restoration unit of the plane: best set of the mask, weights, SSEs."""
+    ph, pw = dgd.shape
+    dgd, src = np.ascontiguousarray(dgd), np.ascontiguousarray(src)
+    units = np.zeros(sgr_units_shape(pw, ph), SGR_UNIT)
+    assert lib().zfo_sgr_search(bd, pw, ph, ss, dgd.ctypes.data, src.ctypes.data, set_mask, units.ctypes.data) == 0
+    return units
+
+
+def sgr_apply(bd, dgd, pre_cdef, units, ss=0):
+    """Decoder-exact SGRPROJ apply of one plane (units with set < 0 copy)."""
+    ph, pw = dgd.shape
+    dgd, pre_cdef = np.ascontiguousarray(dgd), np.ascontiguousarray(pre_cdef)
+    units = np.ascontiguousarray(units, SGR_UNIT)
+    out = np.empty_like(dgd)
+    assert lib().zfo_sgr_apply(bd, pw, ph, ss, dgd.ctypes.data, pre_cdef.ctypes.data, units.ctypes.data,
+                               out.ctypes.data) == 0
+    return out
+
+
+def sgr_box_filter(bd, dgd, set_, pass_, x, y, w, h):
+    ph, pw = dgd.shape
+    dgd = np.ascontiguousarray(dgd)
+    out = np.zeros((h, w), np.int32)
+    lib().zfo_sgr_box_filter(bd, pw, ph, dgd.ctypes.data, set_, pass_, x, y, w, h, out.ctypes.data)
+    return out
+
+
+def sgr_params(set_):
+    out = (C.c_int32 * 4)()
+    lib().zfo_sgr_params(set_, out)
+    return list(out)

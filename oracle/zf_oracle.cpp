@@ -2196,6 +2196,248 @@ static int filter_stage_t(const zf_frame *f, const Geom &g, zf_decisions *out, z
     return ZF_OK;
 }
 
+
+// ===========================================================================
+// Self-guided restoration (RESTORE_SGRPROJ). The reference encoder never
+// searches or signals it (DSP/restoration.rs:1280, ENC/restoration.rs:8), so
+// this restates the AV1 specification instead: the box filter process and
+// the self-guided filter process of section 7.17.3 (the reference project's
+// specs/08-loop-filters.md:371-421 describes the same steps), with the
+// decoder's stripe-aware sample fetch (get_source_sample, section 7.17.6).
+// The per-unit search (every parameter set of a mask, least-squares
+// projection weights solved exactly, SSE of the filtered unit) is this
+// library's own; nothing pins it to another encoder.
+// ===========================================================================
+constexpr int SGR_SGR_BITS = 8, SGR_RST_BITS = 4, SGR_PRJ_BITS = 7, SGR_MTABLE_BITS = 20, SGR_RECIP_BITS = 12;
+constexpr int SGR_XQD_MIN[2] = {-96, -32}, SGR_XQD_MAX[2] = {31, 95};
+
+// Sgr_Params (r0, eps0, r1, eps1) of the AV1 specification.
+constexpr int SGR_PARAMS[16][4] = {{2, 12, 1, 4},  {2, 15, 1, 6},  {2, 18, 1, 8},  {2, 21, 1, 9},
+                                   {2, 24, 1, 10}, {2, 29, 1, 11}, {2, 36, 1, 12}, {2, 45, 1, 13},
+                                   {2, 56, 1, 14}, {2, 68, 1, 15}, {0, 0, 1, 5},   {0, 0, 1, 8},
+                                   {0, 0, 1, 11},  {0, 0, 1, 14},  {2, 30, 0, 0},  {2, 75, 0, 0}};
+
+static inline i32 round2(i64 x, int n) { return n == 0 ? (i32)x : (i32)((x + ((i64)1 << (n - 1))) >> n); }
+
+// One pass of the box filter process: F[i][j] for the w x h block at (x, y)
+// (plane coordinates); fetch(x, y) is the sample source (decoder:
+// get_source_sample; search: the plane clamped to its edges), cdef(x, y)
+// the centre sample.
+template <typename Fetch, typename Cdef>
+static void sgr_box_filter(int bd, int set, int pass, int x, int y, int w, int h, Fetch &&fetch, Cdef &&cdef,
+                           std::vector<i32> &F) {
+    const int r = SGR_PARAMS[set][pass * 2], eps = SGR_PARAMS[set][pass * 2 + 1];
+    F.assign((size_t)w * h, 0);
+    if (r == 0) return;
+    const int n = (2 * r + 1) * (2 * r + 1);
+    const i64 n2e = (i64)n * n * eps;
+    const i64 s = (((i64)1 << SGR_MTABLE_BITS) + n2e / 2) / n2e;
+    const i64 one_over_n = (((i64)1 << SGR_RECIP_BITS) + n / 2) / n;
+    const int aw = w + 2, ah = h + 2;
+    std::vector<i32> A((size_t)aw * ah), B((size_t)aw * ah);
+    for (int i = -1; i < h + 1; ++i)
+        for (int j = -1; j < w + 1; ++j) {
+            i64 a = 0, b = 0;
+            for (int dy = -r; dy <= r; ++dy)
+                for (int dx = -r; dx <= r; ++dx) {
+                    const i64 c = fetch(x + j + dx, y + i + dy);
+                    a += c * c;
+                    b += c;
+                }
+            a = round2(a, 2 * (bd - 8));
+            const i64 d = round2(b, bd - 8);
+            const i64 p = std::max<i64>(0, a * n - d * d);
+            const i64 z = round2(p * s, SGR_MTABLE_BITS);
+            i64 a2;
+            if (z >= 255) a2 = 256;
+            else if (z == 0) a2 = 1;
+            else a2 = ((z << SGR_SGR_BITS) + z / 2) / (z + 1);
+            const i64 b2 = (((i64)1 << SGR_SGR_BITS) - a2) * b * one_over_n;
+            A[(size_t)(i + 1) * aw + (j + 1)] = (i32)a2;
+            B[(size_t)(i + 1) * aw + (j + 1)] = round2(b2, SGR_RECIP_BITS);
+        }
+    for (int i = 0; i < h; ++i) {
+        const int shift = (pass == 0 && ((y + i) & 1)) ? 4 : 5;
+        for (int j = 0; j < w; ++j) {
+            i64 a = 0, b = 0;
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    int weight;
+                    if (pass == 0) weight = ((y + i + dy) & 1) ? (dx == 0 ? 6 : 5) : 0;
+                    else weight = (dx == 0 || dy == 0) ? 4 : 3;
+                    a += weight * A[(size_t)(i + 1 + dy) * aw + (j + 1 + dx)];
+                    b += weight * B[(size_t)(i + 1 + dy) * aw + (j + 1 + dx)];
+                }
+            const i64 v = a * cdef(x + j, y + i) + b;
+            F[(size_t)i * w + j] = round2(v, SGR_SGR_BITS + shift - SGR_RST_BITS);
+        }
+    }
+}
+
+// The projection of the self-guided filter process: the restored sample
+// from the centre sample, the two pass outputs and the weights w0, w1.
+static inline int sgr_project(int set, int bd, int px, i32 f0, i32 f1, int w0, int w1) {
+    const int w2 = (1 << SGR_PRJ_BITS) - w0 - w1;
+    const i64 u = (i64)px << SGR_RST_BITS;
+    i64 v = (i64)w1 * u;
+    v += SGR_PARAMS[set][0] ? (i64)w0 * f0 : (i64)w0 * u;
+    v += SGR_PARAMS[set][2] ? (i64)w2 * f1 : (i64)w2 * u;
+    const i64 o = round2(v, SGR_RST_BITS + SGR_PRJ_BITS);
+    return (int)std::min<i64>(std::max<i64>(o, 0), (1 << bd) - 1);
+}
+
+// n * 128 / d rounded half away from zero (d > 0), exact.
+static inline i64 sgr_div_round(__int128 n, __int128 d) {
+    const __int128 q = n * 128;
+    return (i64)(q >= 0 ? (2 * q + d) / (2 * d) : -((-2 * q + d) / (2 * d)));
+}
+
+// Least-squares projection weights from the unit sums (f0 = flt0 - u,
+// f1 = flt1 - u, s = (src << 4) - u): x = argmin sum (s - x0 f0 - x1 f1)^2,
+// xq = round(128 x), then the signalled weights w0, w1 clamped to their
+// ranges the way the decoder rebuilds a missing pass's weight.
+static void sgr_weights(int set, const i64 sums[5], int w[2]) {
+    const i64 H00 = sums[0], H01 = sums[1], H11 = sums[2], C0 = sums[3], C1 = sums[4];
+    const int r0 = SGR_PARAMS[set][0], r1 = SGR_PARAMS[set][2];
+    i64 xq0 = 0, xq1 = 0;
+    if (r0 && r1) {
+        const __int128 det = (__int128)H00 * H11 - (__int128)H01 * H01;
+        if (det > 0) {
+            xq0 = sgr_div_round((__int128)H11 * C0 - (__int128)H01 * C1, det);
+            xq1 = sgr_div_round((__int128)H00 * C1 - (__int128)H01 * C0, det);
+        }
+    } else if (r0) {
+        if (H00 > 0) xq0 = sgr_div_round(C0, H00);
+    } else if (H11 > 0) {
+        xq1 = sgr_div_round(C1, H11);
+    }
+    auto clampw = [](i64 v, int k) { return (int)std::min<i64>(std::max<i64>(v, SGR_XQD_MIN[k]), SGR_XQD_MAX[k]); };
+    if (r0 && r1) {
+        w[0] = clampw(xq0, 0);
+        w[1] = clampw((1 << SGR_PRJ_BITS) - w[0] - xq1, 1);
+    } else if (r0) {
+        w[0] = clampw(xq0, 0);
+        w[1] = clampw((1 << SGR_PRJ_BITS) - w[0], 1);
+    } else {
+        w[0] = 0;
+        w[1] = clampw((1 << SGR_PRJ_BITS) - xq1, 1);
+    }
+}
+
+struct SgrUnitOut {
+    int set, w0, w1;
+    i64 sse, sse_none;
+};
+
+// Search one plane: for every restoration unit (foreach_rest_unit_in_tile
+// geometry) and every set of the mask, filter the unit with samples clamped
+// to the plane, solve the weights, filter with them and keep the set of the
+// smallest SSE (the lowest set index on ties).
+template <typename T>
+static void sgr_search_plane(int bd, int pw, int ph, int ss, const T *dgd, const T *src, u32 mask,
+                             std::vector<SgrUnitOut> &out) {
+    const int unit = 256, hunits = count_units_in_tile(unit, pw), vunits = count_units_in_tile(unit, ph);
+    out.assign((size_t)hunits * vunits, SgrUnitOut{-1, 0, 0, 0, 0});
+    auto fetch = [&](int x, int y) -> i64 {
+        x = std::min(std::max(x, 0), pw - 1);
+        y = std::min(std::max(y, 0), ph - 1);
+        return dgd[(i64)y * pw + x];
+    };
+    auto cdef = [&](int x, int y) -> i64 { return dgd[(i64)y * pw + x]; };
+    PixelRect rect{0, 0, pw, ph};
+    foreach_rest_unit_in_tile(rect, hunits, unit, ss, [&](const TileLimits &lim, int ui) {
+        const int x0 = lim.h_start, y0 = lim.v_start, w = lim.h_end - lim.h_start, h = lim.v_end - lim.v_start;
+        SgrUnitOut &o = out[(size_t)ui];
+        i64 sse_none = 0;
+        for (int i = 0; i < h; ++i)
+            for (int j = 0; j < w; ++j) {
+                const i64 e = (i64)src[(i64)(y0 + i) * pw + x0 + j] - dgd[(i64)(y0 + i) * pw + x0 + j];
+                sse_none += e * e;
+            }
+        o.sse_none = sse_none;
+        std::vector<i32> F0, F1;
+        for (int set = 0; set < 16; ++set) {
+            if (!((mask >> set) & 1)) continue;
+            sgr_box_filter(bd, set, 0, x0, y0, w, h, fetch, cdef, F0);
+            sgr_box_filter(bd, set, 1, x0, y0, w, h, fetch, cdef, F1);
+            const bool r0 = SGR_PARAMS[set][0] != 0, r1 = SGR_PARAMS[set][2] != 0;
+            i64 sums[5] = {0, 0, 0, 0, 0};
+            for (int i = 0; i < h; ++i)
+                for (int j = 0; j < w; ++j) {
+                    const i64 u = (i64)dgd[(i64)(y0 + i) * pw + x0 + j] << SGR_RST_BITS;
+                    const i64 sv = ((i64)src[(i64)(y0 + i) * pw + x0 + j] << SGR_RST_BITS) - u;
+                    const i64 f0 = r0 ? F0[(size_t)i * w + j] - u : 0, f1 = r1 ? F1[(size_t)i * w + j] - u : 0;
+                    sums[0] += f0 * f0;
+                    sums[1] += f0 * f1;
+                    sums[2] += f1 * f1;
+                    sums[3] += f0 * sv;
+                    sums[4] += f1 * sv;
+                }
+            int wt[2];
+            sgr_weights(set, sums, wt);
+            i64 sse = 0;
+            for (int i = 0; i < h; ++i)
+                for (int j = 0; j < w; ++j) {
+                    const int px = dgd[(i64)(y0 + i) * pw + x0 + j];
+                    const int v = sgr_project(set, bd, px, F0[(size_t)i * w + j], F1[(size_t)i * w + j], wt[0], wt[1]);
+                    const i64 e = (i64)src[(i64)(y0 + i) * pw + x0 + j] - v;
+                    sse += e * e;
+                }
+            if (o.set < 0 || sse < o.sse) {
+                o.set = set;
+                o.w0 = wt[0];
+                o.w1 = wt[1];
+                o.sse = sse;
+            }
+        }
+    });
+}
+
+// Decoder-exact apply of one plane (section 7.17: per 4x4 luma / 2x2 chroma
+// block, the block's stripe deciding where samples above and below come
+// from). Units with set < 0 keep the post-CDEF samples. The block walk is
+// done per stripe row range; the result does not depend on the block size
+// because every block lies in one stripe and one unit.
+template <typename T>
+static void sgr_apply_plane(int bd, int pw, int ph, int ss, const T *dgd, const T *pre, const SgrUnitOut *units,
+                            T *dst) {
+    const int unit = 256, hunits = count_units_in_tile(unit, pw), vunits = count_units_in_tile(unit, ph);
+    const int full = 64 >> ss, off = 8 >> ss;
+    std::vector<i32> F0, F1;
+    for (int ys = 0; ys < ph;) {
+        const int stripe = (ys + off) / full;
+        const int start = -off + stripe * full, end = start + full - 1;
+        const int ye = std::min(ph, end + 1);
+        auto fetch = [&](int x, int y) -> i64 {
+            x = std::min(std::max(x, 0), pw - 1);
+            y = std::min(std::max(y, 0), ph - 1);
+            if (y < start) return pre[(i64)std::max(start - 2, y) * pw + x];
+            if (y > end) return pre[(i64)std::min(end + 2, y) * pw + x];
+            return dgd[(i64)y * pw + x];
+        };
+        auto cdef = [&](int x, int y) -> i64 { return dgd[(i64)y * pw + x]; };
+        const int urow = std::min(vunits - 1, (ys + off) / unit);
+        for (int uc = 0; uc < hunits; ++uc) {
+            const int x0 = uc * unit, x1 = uc == hunits - 1 ? pw : (uc + 1) * unit;
+            const SgrUnitOut &u = units[(size_t)urow * hunits + uc];
+            if (u.set < 0) {
+                for (int y = ys; y < ye; ++y)
+                    for (int x = x0; x < x1; ++x) dst[(i64)y * pw + x] = dgd[(i64)y * pw + x];
+                continue;
+            }
+            sgr_box_filter(bd, u.set, 0, x0, ys, x1 - x0, ye - ys, fetch, cdef, F0);
+            sgr_box_filter(bd, u.set, 1, x0, ys, x1 - x0, ye - ys, fetch, cdef, F1);
+            for (int y = ys; y < ye; ++y)
+                for (int x = x0; x < x1; ++x) {
+                    const size_t k = (size_t)(y - ys) * (x1 - x0) + (x - x0);
+                    dst[(i64)y * pw + x] =
+                        (T)sgr_project(u.set, bd, dgd[(i64)y * pw + x], F0[k], F1[k], u.w0, u.w1);
+                }
+        }
+        ys = ye;
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -2424,6 +2666,68 @@ int64_t zfo_sse_region(const void *a, int32_t a_stride, const void *b, int32_t b
                        int32_t bd) {
     if (bd == 8) return sse_region((const u8 *)a, 0, a_stride, (const u8 *)b, 0, b_stride, w, h);
     return sse_region((const u16 *)a, 0, a_stride, (const u16 *)b, 0, b_stride, w, h);
+}
+
+
+int32_t zfo_sgr_search(int32_t bd, int32_t pw, int32_t ph, int32_t ss, const void *dgd, const void *src,
+                       uint32_t set_mask, zfo_sgr_unit *units) {
+    if ((bd != 8 && bd != 10) || pw <= 0 || ph <= 0) return ZF_ERR_ARG;
+    std::vector<SgrUnitOut> out;
+    if (bd == 8) sgr_search_plane(bd, pw, ph, ss, (const u8 *)dgd, (const u8 *)src, set_mask, out);
+    else sgr_search_plane(bd, pw, ph, ss, (const u16 *)dgd, (const u16 *)src, set_mask, out);
+    for (size_t k = 0; k < out.size(); ++k) {
+        units[k].set = out[k].set;
+        units[k].w0 = out[k].w0;
+        units[k].w1 = out[k].w1;
+        units[k].sse = out[k].sse;
+        units[k].sse_none = out[k].sse_none;
+    }
+    return ZF_OK;
+}
+
+int32_t zfo_sgr_apply(int32_t bd, int32_t pw, int32_t ph, int32_t ss, const void *dgd, const void *pre_cdef,
+                      const zfo_sgr_unit *units, void *dst) {
+    if ((bd != 8 && bd != 10) || pw <= 0 || ph <= 0) return ZF_ERR_ARG;
+    const size_t n = (size_t)count_units_in_tile(256, pw) * count_units_in_tile(256, ph);
+    std::vector<SgrUnitOut> u(n);
+    for (size_t k = 0; k < n; ++k) u[k] = SgrUnitOut{units[k].set, units[k].w0, units[k].w1, 0, 0};
+    if (bd == 8) sgr_apply_plane(bd, pw, ph, ss, (const u8 *)dgd, (const u8 *)pre_cdef, u.data(), (u8 *)dst);
+    else sgr_apply_plane(bd, pw, ph, ss, (const u16 *)dgd, (const u16 *)pre_cdef, u.data(), (u16 *)dst);
+    return ZF_OK;
+}
+
+/* One pass of the box filter on a w x h block at (x, y) of a plane, the
+ * samples clamped to the plane (the search's fetch). */
+void zfo_sgr_box_filter(int32_t bd, int32_t pw, int32_t ph, const void *dgd, int32_t set, int32_t pass, int32_t x,
+                        int32_t y, int32_t w, int32_t h, int32_t *out) {
+    std::vector<i32> F;
+    auto run = [&](auto *p) {
+        auto fetch = [&](int xx, int yy) -> i64 {
+            xx = std::min(std::max(xx, 0), pw - 1);
+            yy = std::min(std::max(yy, 0), ph - 1);
+            return p[(i64)yy * pw + xx];
+        };
+        auto cdef = [&](int xx, int yy) -> i64 { return p[(i64)yy * pw + xx]; };
+        sgr_box_filter(bd, set, pass, x, y, w, h, fetch, cdef, F);
+    };
+    if (bd == 8) run((const u8 *)dgd);
+    else run((const u16 *)dgd);
+    std::memcpy(out, F.data(), F.size() * sizeof(i32));
+}
+
+/* The (r0, s0, r1, s1) of a set: radii and the scale s computed from eps. */
+void zfo_sgr_params(int32_t set, int32_t out[4]) {
+    for (int pass = 0; pass < 2; ++pass) {
+        const int r = SGR_PARAMS[set][pass * 2], eps = SGR_PARAMS[set][pass * 2 + 1];
+        out[pass * 2] = r;
+        if (!r) {
+            out[pass * 2 + 1] = -1;
+            continue;
+        }
+        const int n = (2 * r + 1) * (2 * r + 1);
+        const i64 n2e = (i64)n * n * eps;
+        out[pass * 2 + 1] = (int32_t)((((i64)1 << SGR_MTABLE_BITS) + n2e / 2) / n2e);
+    }
 }
 
 }  // extern "C"

@@ -97,6 +97,21 @@ void zfo_wiener_convolve(const void *src, int64_t src_origin, int32_t src_stride
 int64_t zfo_sse_region(const void *a, int32_t a_stride, const void *b, int32_t b_stride,
                        int32_t w, int32_t h, int32_t bd);
 
+/* --- Self-guided restoration (AV1 spec 7.17.3; not in the reference) ---- */
+typedef struct zfo_sgr_unit {
+    int32_t set, w0, w1, pad;
+    int64_t sse, sse_none;
+} zfo_sgr_unit;
+/* Planes tight (stride = pw), u8 when bd == 8 else u16; units hunits*vunits
+ * of the 256-px restoration-unit grid, row-major. */
+int32_t zfo_sgr_search(int32_t bd, int32_t pw, int32_t ph, int32_t ss, const void *dgd, const void *src,
+                       uint32_t set_mask, zfo_sgr_unit *units);
+int32_t zfo_sgr_apply(int32_t bd, int32_t pw, int32_t ph, int32_t ss, const void *dgd, const void *pre_cdef,
+                      const zfo_sgr_unit *units, void *dst);
+void zfo_sgr_box_filter(int32_t bd, int32_t pw, int32_t ph, const void *dgd, int32_t set, int32_t pass, int32_t x,
+                        int32_t y, int32_t w, int32_t h, int32_t *out);
+void zfo_sgr_params(int32_t set, int32_t out[4]);
+
 #ifdef __cplusplus
 }
 #endif

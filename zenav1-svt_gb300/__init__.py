@@ -16,6 +16,8 @@ variants surface as ZfError with the reference's variant name):
                             apply_restoration_frame           (restoration.rs:938, :992)
   filter_stage              the whole stage (pipeline.rs:2886-3455)
   submit_batch              many frames, one launch per pass
+  sgr_search / sgr_apply    self-guided restoration (AV1 spec 7.17.3); the
+                            reference encoder never searches SGRPROJ
 
 There is no CPU fallback: every call runs the CUDA kernels, and loading
 fails loudly when the library has not been built.
@@ -83,7 +85,9 @@ def lib():
     L.zf_profile_reset.restype = None
     L.zf_profile_read.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
     L.zf_profile_read.restype = C.c_int32
-    for name in ("zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
+    L.zf_sgr_search.argtypes = [C.c_void_p, P(abi.ZfSgrPlane), C.c_uint32, C.c_void_p, C.c_int32]
+    L.zf_sgr_apply.argtypes = [C.c_void_p, P(abi.ZfSgrPlane), C.c_void_p, C.c_int32, C.c_void_p]
+    for name in ("zf_sgr_search", "zf_sgr_apply", "zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
                  "zf_submit_batch", "zf_deblock_pick", "zf_deblock_apply", "zf_cdef_search",
                  "zf_cdef_apply", "zf_lr_search", "zf_lr_apply"):
         getattr(L, name).restype = C.c_int32
@@ -249,6 +253,37 @@ class Context:
         s = abi.make_frame_struct(fr, fr.src, rec, mi)
         pre = (C.c_void_p * 3)(*[p.ctypes.data for p in pre_cdef])
         self._check(lib().zf_lr_apply(self.h, C.byref(s), pre, C.byref(dec.c)))
+
+    # -- self-guided restoration ------------------------------------------
+    @staticmethod
+    def _sgr_plane(bd, dgd, src=None, pre_cdef=None, ss_y=0, on_device=False):
+        """zf_sgr_plane over numpy arrays (host) or torch CUDA tensors
+        (on_device=True, data_ptr())."""
+        addr = (lambda a: None if a is None else a.data_ptr()) if on_device else \
+            (lambda a: None if a is None else a.ctypes.data)
+        h, w = dgd.shape
+        return abi.ZfSgrPlane(bd, w, h, ss_y, 1 if on_device else 0, addr(dgd), addr(src), addr(pre_cdef))
+
+    def sgr_search(self, bd, dgd, src, ss_y=0, set_mask=0xFFFF, on_device=False):
+        """Per restoration unit: the best set of the mask, its weights, the
+        SSE with it and without filtering (a SGR_UNIT record array)."""
+        h, w = dgd.shape
+        n = abi.count_units(w) * abi.count_units(h)
+        units = np.zeros(n, abi.SGR_UNIT)
+        p = self._sgr_plane(bd, dgd, src, None, ss_y, on_device)
+        self._check(lib().zf_sgr_search(self.h, C.byref(p), set_mask, units.ctypes.data, n))
+        return units
+
+    def sgr_apply(self, bd, dgd, pre_cdef, units, ss_y=0, dst=None, on_device=False):
+        """Decoder-exact SGRPROJ apply; returns dst (a new host array when
+        dst is None and the planes are host arrays)."""
+        units = np.ascontiguousarray(units, abi.SGR_UNIT)
+        if dst is None:
+            dst = np.empty_like(dgd)
+        p = self._sgr_plane(bd, dgd, None, pre_cdef, ss_y, on_device)
+        d = dst.data_ptr() if on_device else dst.ctypes.data
+        self._check(lib().zf_sgr_apply(self.h, C.byref(p), units.ctypes.data, len(units), d))
+        return dst
 
 
 def query_sizes(fr, mi=None):

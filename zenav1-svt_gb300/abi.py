@@ -58,6 +58,16 @@ class ZfOpts(C.Structure):
                 ("cancel_flag", C.POINTER(C.c_int32))]
 
 
+class ZfSgrPlane(C.Structure):
+    _fields_ = [("bit_depth", C.c_int32), ("width", C.c_int32), ("height", C.c_int32), ("ss_y", C.c_int32),
+                ("on_device", C.c_int32), ("dgd", C.c_void_p), ("src", C.c_void_p), ("pre_cdef", C.c_void_p)]
+
+
+# zf_sgr_unit as a numpy record (32 bytes)
+SGR_UNIT = np.dtype([("set", np.int32), ("w0", np.int32), ("w1", np.int32), ("pad", np.int32),
+                     ("sse", np.int64), ("sse_none", np.int64)])
+
+
 class ZfKernelTime(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double)]
 

@@ -370,6 +370,7 @@ cudaError_t set_kernel_attributes() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(zf::k_lr_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kLrFinishSmemCap);
     if (e == cudaSuccess) e = zf::joint_set_attributes();
+    if (e == cudaSuccess) e = zf::sgr_set_attributes();
     return e;
 }
 
@@ -1147,6 +1148,58 @@ int describe_cdef_frame(const zf_frame *f, FrameDesc *d) {
 }
 }  // namespace zf
 
+namespace {
+// ---- self-guided restoration entry points (zf_sgr.cu kernels) ------------
+int validate_sgr_plane(zf_ctx *ctx, const zf_sgr_plane *p, int32_t nunits, int *hunits, int *vunits) {
+    if (!ctx) return ZF_ERR_ARG;
+    if (!p) return fail(ctx, ZF_ERR_ARG, "plane is NULL");
+    if (p->bit_depth != 8 && p->bit_depth != 10) return fail(ctx, ZF_ERR_UNSUPPORTED, "bit_depth must be 8 or 10");
+    if (p->width <= 0 || p->height <= 0 || p->width > 16384 || p->height > 16384)
+        return fail(ctx, ZF_ERR_INVALID_DIMS, "plane dims must be in [1, 16384]");
+    if (p->ss_y != 0 && p->ss_y != 1) return fail(ctx, ZF_ERR_ARG, "ss_y must be 0 or 1");
+    if (!p->dgd) return fail(ctx, ZF_ERR_ARG, "missing dgd plane");
+    *hunits = count_units_in_tile(256, p->width);
+    *vunits = count_units_in_tile(256, p->height);
+    if (nunits != *hunits * *vunits) return fail(ctx, ZF_ERR_ARG, "nunits does not match the plane's unit grid");
+    return ZF_OK;
+}
+
+// The 64 x 32 tiles of every unit rectangle (search).
+void sgr_search_tiles(int pw, int ph, int ss, std::vector<zf::SgrTile> &tiles) {
+    std::vector<UnitRect> rects;
+    rest_units(pw, ph, ss, rects);
+    tiles.clear();
+    for (size_t u = 0; u < rects.size(); ++u) {
+        const UnitRect &r = rects[u];
+        for (int y = r.v_start; y < r.v_end; y += zf::kSgrTileHHost)
+            for (int x = r.h_start; x < r.h_end; x += zf::kSgrTileWHost)
+                tiles.push_back(zf::SgrTile{(int)u, x, y, std::min(zf::kSgrTileWHost, r.h_end - x),
+                                            std::min(zf::kSgrTileHHost, r.v_end - y), 1, 0, 0});
+    }
+}
+
+// The apply's tiles: every stripe (64 >> ss rows, offset 8 >> ss) split into
+// 32-row pieces, 64-column tiles inside each unit column; a tile's unit is
+// the decoder's (unit row from the stripe, unit column from x).
+void sgr_apply_tiles(int pw, int ph, int ss, int hunits, int vunits, std::vector<zf::SgrTile> &tiles) {
+    const int full = 64 >> ss, off = 8 >> ss;
+    tiles.clear();
+    for (int ys = 0; ys < ph;) {
+        const int stripe = (ys + off) / full, start = -off + stripe * full, end = start + full - 1;
+        const int ye = std::min(ph, end + 1);
+        const int urow = std::min(vunits - 1, (ys + off) / 256);
+        for (int y = ys; y < ye; y += zf::kSgrTileHHost)
+            for (int uc = 0; uc < hunits; ++uc) {
+                const int x0 = uc * 256, x1 = uc == hunits - 1 ? pw : (uc + 1) * 256;
+                for (int x = x0; x < x1; x += zf::kSgrTileWHost)
+                    tiles.push_back(zf::SgrTile{urow * hunits + uc, x, y, std::min(zf::kSgrTileWHost, x1 - x),
+                                                std::min(zf::kSgrTileHHost, ye - y), start, end, 0});
+            }
+        ys = ye;
+    }
+}
+}  // namespace
+
 extern "C" {
 
 int32_t zf_abi_version(void) { return ZF_ABI_VERSION; }
@@ -1352,6 +1405,141 @@ int32_t zf_lr_apply(zf_ctx *ctx, const zf_frame *f, const void *const pre_cdef[3
     zf_decisions dd = *d;
     Run r{STG_LR_APPLY, SET_A, SET_C, true, pre_cdef, false, false, true};
     return run_batch(ctx, f, 1, &dd, nullptr, r);
+}
+
+int32_t zf_sgr_search(zf_ctx *ctx, const zf_sgr_plane *p, uint32_t set_mask, zf_sgr_unit *units, int32_t nunits) {
+    int hu, vu;
+    TRY(validate_sgr_plane(ctx, p, nunits, &hu, &vu));
+    if (!p->src) return fail(ctx, ZF_ERR_ARG, "missing source plane");
+    if (!units) return fail(ctx, ZF_ERR_ARG, "units is NULL");
+    if ((set_mask & 0xFFFFu) == 0 || (set_mask >> 16)) return fail(ctx, ZF_ERR_ARG, "set_mask must select sets 0..15");
+    CU(cudaSetDevice(ctx->device));
+    TRY(check_cancel(ctx));
+    std::vector<int> sets;
+    for (int k = 0; k < 16; ++k)
+        if ((set_mask >> k) & 1) sets.push_back(k);
+    const int nsets = (int)sets.size();
+    std::vector<zf::SgrTile> tiles;
+    sgr_search_tiles(p->width, p->height, p->ss_y, tiles);
+    const size_t bps = p->bit_depth == 8 ? 1 : 2, pbytes = (size_t)p->width * p->height * bps;
+    const bool dev = p->on_device != 0;
+    // arena: [dgd, src copies (host planes)] | tiles | sets | acc | sse_none | out
+    size_t cur = 0;
+    auto take = [&cur](size_t b) {
+        const size_t o = align_up(cur, 256);
+        cur = o + b;
+        return o;
+    };
+    const size_t o_dgd = dev ? 0 : take(pbytes), o_src = dev ? 0 : take(pbytes);
+    const size_t o_tiles = take(tiles.size() * sizeof(zf::SgrTile)), o_sets = take(sets.size() * 4);
+    const size_t o_acc = take((size_t)nunits * nsets * sizeof(zf::SgrAcc)), o_none = take((size_t)nunits * 8);
+    const size_t o_out = take((size_t)nunits * sizeof(zf_sgr_unit));
+    TRY(ensure_arena(ctx, cur));
+    const size_t meta = align_up(tiles.size() * sizeof(zf::SgrTile), 256) + sets.size() * 4;
+    TRY(ensure_host(ctx, ctx->h_meta, ctx->h_meta_cap, meta));
+    TRY(ensure_host(ctx, ctx->h_out, ctx->h_out_cap, (size_t)nunits * sizeof(zf_sgr_unit)));
+    uint8_t *base = ctx->arena;
+    cudaStream_t st = ctx->stream;
+    zf::SgrPlaneDesc P{p->bit_depth, p->width, p->height, p->ss_y, nullptr, nullptr, nullptr, nullptr};
+    if (dev) {
+        P.dgd = static_cast<const uint8_t *>(p->dgd);
+        P.src = static_cast<const uint8_t *>(p->src);
+    } else {
+        TRY(copy_in(ctx, base + o_dgd, p->dgd, pbytes, false));
+        TRY(copy_in(ctx, base + o_src, p->src, pbytes, false));
+        P.dgd = base + o_dgd;
+        P.src = base + o_src;
+    }
+    const size_t h_sets = align_up(tiles.size() * sizeof(zf::SgrTile), 256);
+    std::memcpy(ctx->h_meta, tiles.data(), tiles.size() * sizeof(zf::SgrTile));
+    std::memcpy(ctx->h_meta + h_sets, sets.data(), sets.size() * 4);
+    CU(cudaMemcpyAsync(base + o_tiles, ctx->h_meta, tiles.size() * sizeof(zf::SgrTile), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(base + o_sets, ctx->h_meta + h_sets, sets.size() * 4, cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(base + o_acc, 0, o_out - o_acc, st));  // acc and sse_none start at zero
+    const zf::SgrTile *d_tiles = (const zf::SgrTile *)(base + o_tiles);
+    const int *d_sets = (const int *)(base + o_sets);
+    zf::SgrAcc *d_acc = (zf::SgrAcc *)(base + o_acc);
+    long long *d_none = (long long *)(base + o_none);
+    zf_sgr_unit *d_out = (zf_sgr_unit *)(base + o_out);
+    const size_t smem = zf::sgr_smem_bytes();
+    const int ntiles = (int)tiles.size(), nacc = nunits * nsets;
+    { LaunchScope ls_(ctx, "k_sgr_search");
+    zf::k_sgr_search<<<ntiles, 256, smem, st>>>(P, d_tiles, d_sets, nsets, d_acc, d_none, 0); }
+    TRY(launch_check(ctx, "k_sgr_search"));
+    { LaunchScope ls_(ctx, "k_sgr_solve");
+    zf::k_sgr_solve<<<(nacc + 127) / 128, 128, 0, st>>>(d_sets, nsets, d_acc, nacc); }
+    TRY(launch_check(ctx, "k_sgr_solve"));
+    { LaunchScope ls_(ctx, "k_sgr_search");
+    zf::k_sgr_search<<<ntiles, 256, smem, st>>>(P, d_tiles, d_sets, nsets, d_acc, d_none, 1); }
+    TRY(launch_check(ctx, "k_sgr_search"));
+    { LaunchScope ls_(ctx, "k_sgr_pick");
+    zf::k_sgr_pick<<<(nunits + 127) / 128, 128, 0, st>>>(d_sets, nsets, d_acc, d_none, d_out, nunits); }
+    TRY(launch_check(ctx, "k_sgr_pick"));
+    CU(cudaMemcpyAsync(ctx->h_out, d_out, (size_t)nunits * sizeof(zf_sgr_unit), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    TRY(launch_check(ctx, "stream"));
+    collect_profile(ctx);
+    std::memcpy(units, ctx->h_out, (size_t)nunits * sizeof(zf_sgr_unit));
+    return ZF_OK;
+}
+
+int32_t zf_sgr_apply(zf_ctx *ctx, const zf_sgr_plane *p, const zf_sgr_unit *units, int32_t nunits, void *dst) {
+    int hu, vu;
+    TRY(validate_sgr_plane(ctx, p, nunits, &hu, &vu));
+    if (!p->pre_cdef) return fail(ctx, ZF_ERR_ARG, "missing pre_cdef plane");
+    if (!units || !dst) return fail(ctx, ZF_ERR_ARG, "units or dst is NULL");
+    if (dst == p->dgd || dst == p->pre_cdef) return fail(ctx, ZF_ERR_ARG, "dst must not alias the input planes");
+    for (int u = 0; u < nunits; ++u) {
+        const zf_sgr_unit &x = units[u];
+        if (x.set < -1 || x.set > 15) return fail(ctx, ZF_ERR_ARG, "unit set out of range");
+        if (x.set >= 0 && (x.xqd[0] < -96 || x.xqd[0] > 31 || x.xqd[1] < -32 || x.xqd[1] > 95))
+            return fail(ctx, ZF_ERR_ARG, "unit weights out of range");
+    }
+    CU(cudaSetDevice(ctx->device));
+    TRY(check_cancel(ctx));
+    std::vector<zf::SgrTile> tiles;
+    sgr_apply_tiles(p->width, p->height, p->ss_y, hu, vu, tiles);
+    const size_t bps = p->bit_depth == 8 ? 1 : 2, pbytes = (size_t)p->width * p->height * bps;
+    const bool dev = p->on_device != 0;
+    size_t cur = 0;
+    auto take = [&cur](size_t b) {
+        const size_t o = align_up(cur, 256);
+        cur = o + b;
+        return o;
+    };
+    const size_t o_dgd = dev ? 0 : take(pbytes), o_pre = dev ? 0 : take(pbytes), o_dst = dev ? 0 : take(pbytes);
+    const size_t o_units = take((size_t)nunits * sizeof(zf_sgr_unit)), o_tiles = take(tiles.size() * sizeof(zf::SgrTile));
+    TRY(ensure_arena(ctx, cur));
+    const size_t h_tiles = align_up((size_t)nunits * sizeof(zf_sgr_unit), 256);
+    TRY(ensure_host(ctx, ctx->h_meta, ctx->h_meta_cap, h_tiles + tiles.size() * sizeof(zf::SgrTile)));
+    uint8_t *base = ctx->arena;
+    cudaStream_t st = ctx->stream;
+    zf::SgrPlaneDesc P{p->bit_depth, p->width, p->height, p->ss_y, nullptr, nullptr, nullptr, nullptr};
+    if (dev) {
+        P.dgd = static_cast<const uint8_t *>(p->dgd);
+        P.pre = static_cast<const uint8_t *>(p->pre_cdef);
+        P.dst = static_cast<uint8_t *>(dst);
+    } else {
+        TRY(copy_in(ctx, base + o_dgd, p->dgd, pbytes, false));
+        TRY(copy_in(ctx, base + o_pre, p->pre_cdef, pbytes, false));
+        P.dgd = base + o_dgd;
+        P.pre = base + o_pre;
+        P.dst = base + o_dst;
+    }
+    std::memcpy(ctx->h_meta, units, (size_t)nunits * sizeof(zf_sgr_unit));
+    std::memcpy(ctx->h_meta + h_tiles, tiles.data(), tiles.size() * sizeof(zf::SgrTile));
+    CU(cudaMemcpyAsync(base + o_units, ctx->h_meta, (size_t)nunits * sizeof(zf_sgr_unit), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(base + o_tiles, ctx->h_meta + h_tiles, tiles.size() * sizeof(zf::SgrTile),
+                       cudaMemcpyHostToDevice, st));
+    { LaunchScope ls_(ctx, "k_sgr_apply");
+    zf::k_sgr_apply<<<(int)tiles.size(), 256, zf::sgr_smem_bytes(), st>>>(
+        P, (const zf::SgrTile *)(base + o_tiles), (const zf_sgr_unit *)(base + o_units)); }
+    TRY(launch_check(ctx, "k_sgr_apply"));
+    if (!dev) TRY(copy_out(ctx, dst, base + o_dst, pbytes, false));
+    CU(cudaStreamSynchronize(st));
+    TRY(launch_check(ctx, "stream"));
+    collect_profile(ctx);
+    return ZF_OK;
 }
 
 }  // extern "C"

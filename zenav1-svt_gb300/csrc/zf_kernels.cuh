@@ -57,4 +57,32 @@ constexpr int kFinThreadsHost = 512;
 // both sides (one thread per (row, row offset) plus one per (row, window row))
 constexpr int stat_rows_host(int win) { return 256 / (3 * win - 1); }
 
+// ---- self-guided restoration (zf_sgr.cu) ----------------------------------
+constexpr int kSgrTileWHost = 64, kSgrTileHHost = 32;  // tile (columns x rows)
+struct SgrPlaneDesc {
+    int bd, pw, ph, ss;      // tight planes: rows are pw samples apart
+    const uint8_t *dgd;      // post-CDEF plane
+    const uint8_t *src;      // source (search)
+    const uint8_t *pre;      // post-deblock plane (apply: stripe-boundary rows)
+    uint8_t *dst;            // apply output
+};
+struct SgrTile {
+    int unit, x0, y0, w, h;
+    int stripe_start, stripe_end;  // apply: the tile's stripe rows
+    int pad;
+};
+struct SgrAcc {                // one (unit, set) of the search
+    long long sums[5];         // H00, H01, H11, C0, C1
+    long long sse;
+    int w[2];
+};
+__global__ void k_sgr_search(SgrPlaneDesc P, const SgrTile *tiles, const int *sets, int nsets, SgrAcc *acc,
+                             long long *sse_none, int phase);
+__global__ void k_sgr_solve(const int *sets, int nsets, SgrAcc *acc, int n);
+__global__ void k_sgr_pick(const int *sets, int nsets, const SgrAcc *acc, const long long *sse_none,
+                           zf_sgr_unit *out, int nunits);
+__global__ void k_sgr_apply(SgrPlaneDesc P, const SgrTile *tiles, const zf_sgr_unit *units);
+size_t sgr_smem_bytes();
+cudaError_t sgr_set_attributes();
+
 }  // namespace zf
