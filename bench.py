@@ -19,6 +19,9 @@ More keys on the same line (N=1 only):
            zf_submit_batch per step vs one zf_filter_stage per image on the
            same images (MPix/s each, their ratio, outputs identical),
            plus the batch through host buffers.
+  sgr      self-guided restoration on one 3840x2160 8-bit frame's three
+           planes: the per-unit search over all 16 parameter sets and the
+           decoder-exact apply (the reference encoder has no SGRPROJ).
   served   Poisson arrivals at 50/200/800 req/s (sizes 128^2..6000x4000)
            through the continuous-batching loop (serve.py): p50/p99 latency
            and served MPix/s per rate.
@@ -419,6 +422,7 @@ def run_ours(args):
             line["cpu_baseline"] = cpu_baseline_sample()
         if world == 1:
             line["highres_10bit"] = run_highres10(args, ctx, stream, dev)
+            line["sgr"] = run_sgr(args, ctx, stream, dev, frames[0])
         if world == 1 and not args.no_batched:
             line["batched"] = run_batched(args, ctx, stream, dev, gen_frames(batch_jobs(args.batch_n)))
             print("batched:", json.dumps(line["batched"]), file=sys.stderr)
@@ -475,6 +479,46 @@ def run_highres10(args, ctx, stream, dev):
     return {"workload": "4096x3072 10-bit 4:2:0 (u16), preset 2, qp 28, device-resident",
             "mpix_per_s": round(f.luma_px / (ms / 1e3) / 1e6, 3), "ms": round(ms, 3),
             "lf": d.as_dict()["lf"], "cdef_bits": d.as_dict()["cdef_bits"], "kernel_ms": kern}
+
+
+def run_sgr(args, ctx, stream, dev, f):
+    """Self-guided restoration of one 4K frame (Y, U, V): zf_sgr_search over
+    all 16 sets, then zf_sgr_apply with the picked units; device-resident
+    planes (the frame's recon stands in for the post-CDEF plane and for the
+    post-deblock stripe lines), CUDA-event timed, L2 flushed per step."""
+    import torch
+    dsrc = [torch.from_numpy(p.astype(np.int16) if p.dtype == np.uint16 else p).to(dev) for p in f.src]
+    ddgd = [torch.from_numpy(p.astype(np.int16) if p.dtype == np.uint16 else p).to(dev) for p in f.rec]
+    dout = [torch.empty_like(x) for x in ddgd]
+    bd = 8 if f.src[0].dtype == np.uint8 else 10
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step():
+        for pl in range(3):
+            u = ctx.sgr_search(bd, ddgd[pl], dsrc[pl], ss_y=1 if pl else 0, on_device=True)
+            ctx.sgr_apply(bd, ddgd[pl], ddgd[pl], u, ss_y=1 if pl else 0, dst=dout[pl], on_device=True)
+        return u
+
+    times = []
+    for k in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        if k >= args.warmup:
+            times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    ctx.profile(True)
+    ctx.profile_reset()
+    step()
+    ctx.sync()
+    kern = {k: round(v[1], 4) for k, v in sorted(ctx.profile_read().items(), key=lambda kv: -kv[1][1])}
+    ctx.profile(False)
+    return {"workload": "3840x2160 8-bit 4:2:0 (Y, U, V), SGRPROJ search over 16 sets + apply, device-resident",
+            "mpix_per_s": round(f.luma_px / (ms / 1e3) / 1e6, 3), "ms": round(ms, 3), "kernel_ms": kern}
 
 
 def run_batched(args, ctx, stream, dev, frames):
