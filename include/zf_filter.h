@@ -244,6 +244,27 @@ int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_decisions *ou
 
 /* --- Observability ------------------------------------------------------- */
 
+/* ---- Frame-header filter syntax ------------------------------------------
+ * The loop_filter_params(), cdef_params() and lr_params() fields of an
+ * uncompressed frame header for a frame's decisions, as the reference's
+ * write_key_frame_header writes them (svtav1-entropy/src/obu.rs:1268-1377;
+ * AV1 spec 5.9.11, 5.9.19, 5.9.20). Host code; no device work. */
+typedef struct zf_header_opts {
+    int32_t monochrome;         /* NumPlanes = 1 (no chroma levels, strengths or lr types) */
+    int32_t allow_intrabc;      /* 1: none of the three blocks is coded */
+    int32_t enable_restoration; /* sequence header enable_restoration */
+    int32_t sb_size;            /* 64 or 128 */
+    int32_t sharpness;          /* loop_filter_sharpness 0..7 */
+    int32_t pad;
+} zf_header_opts;
+
+/* Appends the fields MSB-first at bit *bit_pos of buf (cap bytes; bits past
+ * *bit_pos are overwritten, earlier ones kept) and advances *bit_pos. The
+ * chroma restoration unit size is d->lr[1].unit_size (lr_uv_shift is coded
+ * when it differs from luma's). */
+int32_t zf_write_filter_params(const zf_decisions *d, const zf_header_opts *o, uint8_t *buf, int32_t cap,
+                               int32_t *bit_pos);
+
 /* ---- Self-guided restoration (RESTORE_SGRPROJ) ---------------------------
  * No counterpart in the reference encoder: it never searches or signals
  * SGRPROJ (svtav1-dsp/src/restoration.rs:1280, svtav1-encoder/src/

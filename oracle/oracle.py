@@ -88,6 +88,8 @@ def lib():
     L.zfo_sgr_apply.argtypes = [C.c_int32] * 4 + [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.zfo_sgr_box_filter.argtypes = [C.c_int32] * 3 + [C.c_void_p] + [C.c_int32] * 6 + [C.c_void_p]
     L.zfo_sgr_params.argtypes = [C.c_int32, P(C.c_int32)]
+    L.zfo_write_filter_params.argtypes = [P(abi.ZfDecisions), P(abi.ZfHeaderOpts), C.c_void_p, C.c_int32,
+                                          P(C.c_int32)]
     _lib = L
     return L
 
@@ -217,3 +219,12 @@ def sgr_params(set_):
     out = (C.c_int32 * 4)()
     lib().zfo_sgr_params(set_, out)
     return list(out)
+
+
+def write_filter_params(dec, opts, nbytes=64):
+    """Bits of loop_filter_params / cdef_params / lr_params as a '0'/'1' string."""
+    buf = np.zeros(nbytes, np.uint8)
+    pos = C.c_int32(0)
+    rc = lib().zfo_write_filter_params(C.byref(dec), C.byref(opts), buf.ctypes.data, nbytes, C.byref(pos))
+    assert rc == 0, rc
+    return "".join(str((buf[i >> 3] >> (7 - (i & 7))) & 1) for i in range(pos.value))

@@ -2730,4 +2730,60 @@ void zfo_sgr_params(int32_t set, int32_t out[4]) {
     }
 }
 
+
+/* loop_filter_params(), cdef_params(), lr_params() of write_key_frame_header
+ * (ENT/obu.rs:1268-1377), appended MSB-first like BitWriter::write_bits
+ * (ENT/obu.rs:284-299). */
+int32_t zfo_write_filter_params(const zf_decisions *d, const zf_header_opts *o, uint8_t *buf, int32_t cap,
+                                int32_t *bit_pos) {
+    if (o->allow_intrabc) return ZF_OK;
+    std::vector<int> bits;
+    auto wb = [&](uint32_t value, int n) {
+        for (int i = n - 1; i >= 0; --i) bits.push_back((value >> i) & 1);
+    };
+    const bool mono = o->monochrome != 0;
+    wb(d->lf[0], 6);
+    wb(d->lf[1], 6);
+    if (!mono && (d->lf[0] != 0 || d->lf[1] != 0)) {
+        wb(d->lf[2], 6);
+        wb(d->lf[3], 6);
+    }
+    wb((uint32_t)o->sharpness, 3);
+    wb(0, 1);
+    wb((uint32_t)(d->cdef_damping - 3), 2);
+    wb(d->cdef_bits, 2);
+    for (int i = 0; i < (1 << d->cdef_bits); ++i) {
+        wb(d->cdef_y[i], 6);
+        if (!mono) wb(d->cdef_uv[i], 6);
+    }
+    if (o->enable_restoration) {
+        const int num_planes = mono ? 1 : 3;
+        bool all_none = true, chroma_none = true;
+        for (int p = 0; p < num_planes; ++p) {
+            const int t = d->lr[p].frame_rtype;
+            if (t != 0) {
+                all_none = false;
+                if (p > 0) chroma_none = false;
+            }
+            const bool b0 = t == 1 || t == 2, b1 = t == 2 || t == 3;
+            wb(b0, 1);
+            wb(b1, 1);
+        }
+        if (!all_none) {
+            if (o->sb_size == 64) wb(d->lr[0].unit_size > 64, 1);
+            if (d->lr[0].unit_size > 64) wb(d->lr[0].unit_size > 128, 1);
+        }
+        if (!chroma_none) wb(d->lr[1].unit_size != d->lr[0].unit_size, 1);
+    }
+    int pos = *bit_pos;
+    if ((size_t)((pos + (int)bits.size() + 7) / 8) > (size_t)cap) return ZF_ERR_ARG;
+    for (int b : bits) {
+        const uint8_t m = (uint8_t)(0x80u >> (pos & 7));
+        buf[pos >> 3] = b ? (uint8_t)(buf[pos >> 3] | m) : (uint8_t)(buf[pos >> 3] & ~m);
+        ++pos;
+    }
+    *bit_pos = pos;
+    return ZF_OK;
+}
+
 }  // extern "C"

@@ -111,6 +111,9 @@ int32_t zfo_sgr_apply(int32_t bd, int32_t pw, int32_t ph, int32_t ss, const void
 void zfo_sgr_box_filter(int32_t bd, int32_t pw, int32_t ph, const void *dgd, int32_t set, int32_t pass, int32_t x,
                         int32_t y, int32_t w, int32_t h, int32_t *out);
 void zfo_sgr_params(int32_t set, int32_t out[4]);
+/* Frame-header loop_filter / cdef / lr params (ENT/obu.rs:1268-1377). */
+int32_t zfo_write_filter_params(const zf_decisions *d, const zf_header_opts *o, uint8_t *buf, int32_t cap,
+                                int32_t *bit_pos);
 
 #ifdef __cplusplus
 }

@@ -87,7 +87,9 @@ def lib():
     L.zf_profile_read.restype = C.c_int32
     L.zf_sgr_search.argtypes = [C.c_void_p, P(abi.ZfSgrPlane), C.c_uint32, C.c_void_p, C.c_int32]
     L.zf_sgr_apply.argtypes = [C.c_void_p, P(abi.ZfSgrPlane), C.c_void_p, C.c_int32, C.c_void_p]
-    for name in ("zf_sgr_search", "zf_sgr_apply", "zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
+    L.zf_write_filter_params.argtypes = [P(ZfDecisions), P(abi.ZfHeaderOpts), C.c_void_p, C.c_int32,
+                                         P(C.c_int32)]
+    for name in ("zf_write_filter_params", "zf_sgr_search", "zf_sgr_apply", "zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
                  "zf_submit_batch", "zf_deblock_pick", "zf_deblock_apply", "zf_cdef_search",
                  "zf_cdef_apply", "zf_lr_search", "zf_lr_apply"):
         getattr(L, name).restype = C.c_int32
@@ -284,6 +286,19 @@ class Context:
         d = dst.data_ptr() if on_device else dst.ctypes.data
         self._check(lib().zf_sgr_apply(self.h, C.byref(p), units.ctypes.data, len(units), d))
         return dst
+
+
+def write_filter_params(dec, monochrome=False, allow_intrabc=False, enable_restoration=True, sb_size=64,
+                        sharpness=0, buf=None, bit_pos=0):
+    """Frame-header loop_filter_params / cdef_params / lr_params bits for a
+    ZfDecisions (zf_write_filter_params). Returns (buffer, end bit)."""
+    buf = np.zeros(64, np.uint8) if buf is None else buf
+    o = abi.ZfHeaderOpts(int(monochrome), int(allow_intrabc), int(enable_restoration), sb_size, sharpness, 0)
+    pos = C.c_int32(bit_pos)
+    rc = lib().zf_write_filter_params(C.byref(dec), C.byref(o), buf.ctypes.data, len(buf), C.byref(pos))
+    if rc != 0:
+        raise ZfError(rc, "zf_write_filter_params")
+    return buf, pos.value
 
 
 def query_sizes(fr, mi=None):

@@ -58,6 +58,11 @@ class ZfOpts(C.Structure):
                 ("cancel_flag", C.POINTER(C.c_int32))]
 
 
+class ZfHeaderOpts(C.Structure):
+    _fields_ = [("monochrome", C.c_int32), ("allow_intrabc", C.c_int32), ("enable_restoration", C.c_int32),
+                ("sb_size", C.c_int32), ("sharpness", C.c_int32), ("pad", C.c_int32)]
+
+
 class ZfSgrPlane(C.Structure):
     _fields_ = [("bit_depth", C.c_int32), ("width", C.c_int32), ("height", C.c_int32), ("ss_y", C.c_int32),
                 ("on_device", C.c_int32), ("dgd", C.c_void_p), ("src", C.c_void_p), ("pre_cdef", C.c_void_p)]

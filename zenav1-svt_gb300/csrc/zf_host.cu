@@ -1542,4 +1542,73 @@ int32_t zf_sgr_apply(zf_ctx *ctx, const zf_sgr_plane *p, const zf_sgr_unit *unit
     return ZF_OK;
 }
 
+// loop_filter_params / cdef_params / lr_params of write_key_frame_header
+// (svtav1-entropy/src/obu.rs:1268-1377): fixed-width fields, MSB first.
+int32_t zf_write_filter_params(const zf_decisions *d, const zf_header_opts *o, uint8_t *buf, int32_t cap,
+                               int32_t *bit_pos) {
+    if (!d || !o || !buf || !bit_pos || cap < 0 || *bit_pos < 0) return ZF_ERR_ARG;
+    if (o->allow_intrabc) return ZF_OK;  // spec 5.9.11 / 5.9.19 / 5.9.20 defaults, nothing coded
+    if (o->sharpness < 0 || o->sharpness > 7 || (o->sb_size != 64 && o->sb_size != 128)) return ZF_ERR_ARG;
+    const bool mono = o->monochrome != 0;
+    for (int k = 0; k < 4; ++k)
+        if (d->lf[k] > 63) return ZF_ERR_ARG;
+    if (d->cdef_damping < 3 || d->cdef_damping > 6 || d->cdef_bits > 3) return ZF_ERR_ARG;
+    int pos = *bit_pos;
+    bool overflow = false;
+    auto put = [&](uint32_t v, int n) {
+        for (int i = n - 1; i >= 0; --i) {
+            if ((pos >> 3) >= cap) {
+                overflow = true;
+                return;
+            }
+            const uint8_t m = (uint8_t)(0x80u >> (pos & 7));
+            buf[pos >> 3] = ((v >> i) & 1) ? (uint8_t)(buf[pos >> 3] | m) : (uint8_t)(buf[pos >> 3] & ~m);
+            ++pos;
+        }
+    };
+    // loop_filter_params()
+    put(d->lf[0], 6);
+    put(d->lf[1], 6);
+    if (!mono && (d->lf[0] || d->lf[1])) {
+        put(d->lf[2], 6);
+        put(d->lf[3], 6);
+    }
+    put((uint32_t)o->sharpness, 3);
+    put(0, 1);  // loop_filter_delta_enabled
+    // cdef_params()
+    put((uint32_t)(d->cdef_damping - 3), 2);
+    put(d->cdef_bits, 2);
+    for (int i = 0; i < (1 << d->cdef_bits); ++i) {
+        if (d->cdef_y[i] > 63 || d->cdef_uv[i] > 63) return ZF_ERR_ARG;
+        put(d->cdef_y[i], 6);
+        if (!mono) put(d->cdef_uv[i], 6);
+    }
+    // lr_params()
+    if (o->enable_restoration) {
+        const int np = mono ? 1 : 3;
+        bool all_none = true, chroma_none = true;
+        for (int p = 0; p < np; ++p) {
+            const int t = d->lr[p].frame_rtype;
+            if (t < 0 || t > 3) return ZF_ERR_ARG;
+            if (t) {
+                all_none = false;
+                if (p) chroma_none = false;
+            }
+            // lr_type pairs: NONE (0,0), WIENER (1,0), SGRPROJ (1,1), SWITCHABLE (0,1)
+            put(t == 1 || t == 2, 1);
+            put(t == 2 || t == 3, 1);
+        }
+        if (!all_none) {
+            const int us = d->lr[0].unit_size;
+            if ((us != 64 && us != 128 && us != 256) || us < o->sb_size) return ZF_ERR_ARG;
+            if (o->sb_size == 64) put(us > 64, 1);
+            if (us > 64) put(us > 128, 1);
+        }
+        if (!chroma_none) put(d->lr[1].unit_size != d->lr[0].unit_size, 1);
+    }
+    if (overflow) return ZF_ERR_ARG;
+    *bit_pos = pos;
+    return ZF_OK;
+}
+
 }  // extern "C"
