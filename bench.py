@@ -244,12 +244,13 @@ def kernel_bytes(name, w, h, px):
 # (profiles/top_kernels_4k_p6_frame.md); the roofline's `traffic` scales
 # them to the launch's frame.
 KERNEL_DRAM_BYTES_PER_PX = {
-    "k_cdef_apply": (14.068224e6 + 256.0) / (3840 * 2160),
-    "k_cdef_search": 26.512384e6 / (3840 * 2160),
-    "k_lr_stats5": 25.800704e6 / (3840 * 2160),
-    "k_cdef_finish": 0.229632e6 / (3840 * 2160),
-    "k_deblock_apply": (15.017472e6 + 0.326656e6) / (3840 * 2160),
-    "k_lr_trial_tiles": 24.95488e6 / (3840 * 2160),
+    "k_cdef_apply": 14.070016e6 / (3840 * 2160),
+    "k_cdef_search": 26.51392e6 / (3840 * 2160),
+    "k_lr_stats5": (25.926912e6 + 256.0) / (3840 * 2160),
+    "k_cdef_finish": 0.19712e6 / (3840 * 2160),
+    "k_deblock_apply": 14.565888e6 / (3840 * 2160),
+    "k_lr_trial_tiles": (25.97632e6 + 6144.0) / (3840 * 2160),
+    "k_lr_apply": 0.049664e6 / (3840 * 2160),
 }
 
 
