@@ -22,6 +22,10 @@ More keys on the same line (N=1 only):
   sgr      self-guided restoration on one 3840x2160 8-bit frame's three
            planes: the per-unit search over all 16 parameter sets and the
            decoder-exact apply (the reference encoder has no SGRPROJ).
+  post     the steps on either side of restoration on one 3840x2160 frame:
+           the film-grain estimate (an HBM-streaming reduction; achieved
+           GB/s against the measured copy peak) and the normative superres
+           upscale of the luma plane from the denominator-16 width.
   served   Poisson arrivals at 50/200/800 req/s (sizes 128^2..6000x4000)
            through the continuous-batching loop (serve.py): p50/p99 latency
            and served MPix/s per rate.
@@ -326,6 +330,24 @@ def run_ours(args):
     px_step = sum(f.luma_px for f in frames)
     ms = float(np.mean(times))
     t_max = replicas.max_over_ranks(ms, device=dev)  # replicas: the slowest rank's time
+
+    # the same step with each call's launches run as a CUDA graph (not the
+    # headline: a comparison of the two launch modes)
+    g_times = []
+    ctx.use_graphs(True)
+    for k in range(args.warmup + args.steps):
+        restore()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step_device()
+        e1.record(stream)
+        e1.synchronize()
+        if k >= args.warmup:
+            g_times.append(e0.elapsed_time(e1))
+    g_stats = ctx.graph_stats()
+    ctx.use_graphs(False)
+    graphs = {"ms_per_step": round(float(np.mean(g_times)), 3), "direct_ms_per_step": round(ms, 3),
+              "graph_launches": int(g_stats[0]), "updates": int(g_stats[1]), "instantiations": int(g_stats[2])}
     value = replicas.job_rate(px_step, world, t_max / 1e3) / 1e6
 
     # e2e: pinned host buffers through the C ABI
@@ -418,12 +440,13 @@ def run_ours(args):
                 "e2e": {"value": round(e2e, 3), "unit": "MPix/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e_ms, 3)},
                 "gpu_launches": int(launches),
-                "roofline": roofline, "kernels": kernels, "clocks": clk}
+                "roofline": roofline, "kernels": kernels, "clocks": clk, "graphs": graphs}
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_sample()
         if world == 1:
             line["highres_10bit"] = run_highres10(args, ctx, stream, dev)
             line["sgr"] = run_sgr(args, ctx, stream, dev, frames[0])
+            line["post"] = run_post(args, ctx, stream, dev, frames[0])
         if world == 1 and not args.no_batched:
             line["batched"] = run_batched(args, ctx, stream, dev, gen_frames(batch_jobs(args.batch_n)))
             print("batched:", json.dumps(line["batched"]), file=sys.stderr)
@@ -522,6 +545,54 @@ def run_sgr(args, ctx, stream, dev, f):
             "mpix_per_s": round(f.luma_px / (ms / 1e3) / 1e6, 3), "ms": round(ms, 3), "kernel_ms": kern}
 
 
+def run_post(args, ctx, stream, dev, f):
+    """Film-grain estimate (source vs recon, luma) and superres upscale
+    (denominator 16: 1920 -> 3840 columns, 2160 rows) on device planes,
+    CUDA-event timed per call, L2 flushed before each; the estimate's
+    algorithmic bytes are the two luma planes it reads."""
+    import torch
+    import ctypes as C
+    pkg = ge._pkg()
+    from zenav1_svt_gb300 import abi
+    L = pkg.lib()
+    h, w = f.src[0].shape
+    src = torch.from_numpy(f.src[0]).to(dev)
+    rec = torch.from_numpy(f.rec[0]).to(dev)
+    coded = L.zf_superres_scaled_size(w, 16)
+    small = torch.from_numpy(np.ascontiguousarray(f.rec[0][:, :coded])).to(dev)
+    up = torch.empty((h, w), dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    p = abi.ZfFilmGrain()
+
+    def timed(fn):
+        out = []
+        for k in range(args.warmup + args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            ctx.profile(True)
+            ctx.profile_reset()
+            fn()
+            ctx.sync()
+            prof = ctx.profile_read()
+            ctx.profile(False)
+            if k >= args.warmup:
+                out.append(sum(v[1] for v in prof.values()))
+        return float(np.mean(out))
+
+    ms_est = timed(lambda: ctx._check(L.zf_film_grain_estimate(ctx.h, src.data_ptr(), rec.data_ptr(), w, h, w, 1,
+                                                                C.byref(p))))
+    ms_up = timed(lambda: ctx._check(L.zf_superres_upscale(ctx.h, small.data_ptr(), coded, coded, up.data_ptr(), w,
+                                                            w, h, 8, 1)))
+    peak = _peaks().get("hbm_gbs")
+    gbs = 2 * w * h / (ms_est / 1e3) / 1e9
+    return {"workload": "3840x2160 8-bit luma: film-grain estimate; superres upscale %d -> %d columns" % (coded, w),
+            "film_grain_ms": round(ms_est, 4), "film_grain_gbs": round(gbs, 1),
+            "film_grain_frac_of_hbm": round(gbs / peak, 4) if peak else None,
+            "film_grain_noise_var": round(p.noise_var, 4), "apply_grain": bool(p.apply_grain),
+            "superres_ms": round(ms_up, 4),
+            "superres_gbs": round((coded + w) * h / (ms_up / 1e3) / 1e9, 1)}
+
+
 def run_batched(args, ctx, stream, dev, frames):
     """The 256-image mixed batch (W, H ~ U[64, 2048], ~20 % odd, 70 % 8-bit,
     qp ~ U[20, 50], preset 6): one zf_submit_batch call per step, against the
@@ -602,6 +673,15 @@ def run_batched(args, ctx, stream, dev, frames):
     restore()
     plain()
     p_ms = timed(plain, max(2, args.steps // 2))
+    # both forms again with every call's launches run as a CUDA graph
+    ctx.use_graphs(True)
+    restore()
+    plain()
+    pg_ms = timed(plain, max(2, args.steps // 2))
+    restore()
+    batch()
+    bg_ms = timed(batch, args.steps)
+    ctx.use_graphs(False)
     same = all(torch.equal(a, b) for ra, rb in zip(out_batch, d_rec) for a, b in zip(ra, rb))
     for a, d in zip(dec_batch, plain_decs):
         b = d.as_dict()
@@ -642,6 +722,7 @@ def run_batched(args, ctx, stream, dev, frames):
             "launches_per_batch": int(b_launches), "kernel_ms": b_kernels,
             "plain_mpix_per_s": round(px / (p_ms / 1e3) / 1e6, 3), "plain_ms": round(p_ms, 3),
             "batched_over_plain": round(p_ms / b_ms, 3),
+            "graphs": {"plain_ms": round(pg_ms, 3), "batched_ms": round(bg_ms, 3)},
             "batched_e2e_mpix_per_s": round(px / (e_ms / 1e3) / 1e6, 3),
             "e2e_h2d_bytes": int(h2d), "e2e_d2h_bytes": int(h2d // 2),
             "identical_to_plain": bool(same),

@@ -123,9 +123,11 @@ typedef struct zf_sizes {
     uint64_t device_bytes;      /* device footprint of one frame in flight */
 } zf_sizes;
 
+#define ZF_OPT_GRAPHS 1          /* zf_opts.flags: run each call's launch sequence as a CUDA graph */
+
 typedef struct zf_opts {
     int32_t device;             /* CUDA device ordinal */
-    int32_t pad;
+    int32_t flags;              /* ZF_OPT_* (0: launches issued directly on the stream) */
     uint64_t hbm_budget_bytes;  /* 0: no limit */
     volatile int32_t *cancel_flag; /* polled between passes; non-zero => ZF_ERR_CANCELLED */
 } zf_opts;
@@ -306,11 +308,59 @@ int32_t zf_sgr_search(zf_ctx *ctx, const zf_sgr_plane *p, uint32_t set_mask, zf_
 int32_t zf_sgr_apply(zf_ctx *ctx, const zf_sgr_plane *p, const zf_sgr_unit *units, int32_t nunits,
                      void *dst);
 
+/* ---- Steps on either side of loop restoration ------------------------------
+ * Superres: svtav1-dsp/src/superres.rs (scaled_size :140, the normative
+ * upscale of one plane with one tile column, upscale_normative_plane :252);
+ * the encoder upscales the post-CDEF recon with it before restoration
+ * (pipeline.rs superres hook). Film grain: svtav1-encoder/src/film_grain.rs
+ * (estimate_film_grain :74, run after the restoration apply at
+ * pipeline.rs:3484-3485; synthesize_grain :127, the matching add). */
+typedef struct zf_film_grain {
+    int32_t apply_grain;
+    uint16_t grain_seed;
+    uint8_t num_y_points, num_cb_points, num_cr_points;
+    uint8_t point_y_value[14], point_y_scaling[14];
+    uint8_t point_cb_value[10], point_cb_scaling[10];
+    uint8_t point_cr_value[10], point_cr_scaling[10];
+    int8_t ar_coeffs_y[24], ar_coeffs_cb[25], ar_coeffs_cr[25];
+    uint8_t ar_coeff_lag, ar_coeff_shift, grain_scale_shift;
+    uint8_t cb_mult, cb_luma_mult, cr_mult, cr_luma_mult;
+    uint8_t overlap_flag, clip_to_restricted_range, chroma_scaling_from_luma;
+    uint16_t cb_offset, cr_offset;
+    double noise_var;           /* the estimate's noise variance (not signalled) */
+} zf_film_grain;
+
+/* scaled_size: the coded (downscaled) dimension for a superres denominator
+ * 9..16 (8 or > 16: unchanged). Host only. */
+int32_t zf_superres_scaled_size(int32_t dim, int32_t denom);
+/* Normative horizontal upscale src_width -> dst_width of rows rows (u8 when
+ * bit_depth == 8, else u16 clipped to the bit depth; strides in samples). */
+int32_t zf_superres_upscale(zf_ctx *ctx, const void *src, int32_t src_width, int32_t src_stride, void *dst,
+                            int32_t dst_width, int32_t dst_stride, int32_t rows, int32_t bit_depth,
+                            int32_t on_device);
+/* Film-grain estimate from the u8 luma source and the filtered recon. */
+int32_t zf_film_grain_estimate(zf_ctx *ctx, const uint8_t *src, const uint8_t *recon, int32_t width,
+                               int32_t height, int32_t stride, int32_t on_device, zf_film_grain *out);
+/* Adds synthesize_grain's noise to a u8 plane in place. */
+int32_t zf_film_grain_synthesize(zf_ctx *ctx, uint8_t *frame, int32_t width, int32_t height, int32_t stride,
+                                 int32_t on_device, const zf_film_grain *p);
+
 typedef struct zf_kernel_time {
     char name[32];
     uint64_t launches;
     double total_ms;            /* CUDA-event time on the context's stream */
 } zf_kernel_time;
+
+/* CUDA graphs (no counterpart in the reference). enable != 0: every
+ * filter-stage / batch call captures its launch sequence after the deblock
+ * level search (metadata upload, kernels, decision readback) into a graph,
+ * updates the context's executable graph with it (instantiating a new one
+ * when the sequence's shape changed) and launches that; passes are then not
+ * separated by cancel checks (the flag is polled before and after).
+ * Ignored while event profiling is on. */
+int32_t zf_use_graphs(zf_ctx *ctx, int32_t enable);
+/* out[0] graph launches, out[1] in-place updates, out[2] instantiations. */
+int32_t zf_graph_stats(const zf_ctx *ctx, uint64_t out[3]);
 
 /* Kernel launches issued by this context since zf_create. */
 uint64_t zf_launch_count(const zf_ctx *ctx);

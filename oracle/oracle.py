@@ -88,6 +88,15 @@ def lib():
     L.zfo_sgr_apply.argtypes = [C.c_int32] * 4 + [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.zfo_sgr_box_filter.argtypes = [C.c_int32] * 3 + [C.c_void_p] + [C.c_int32] * 6 + [C.c_void_p]
     L.zfo_sgr_params.argtypes = [C.c_int32, P(C.c_int32)]
+    L.zfo_superres_scaled_size.argtypes = [C.c_int32, C.c_int32]
+    L.zfo_superres_upscale.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_int32,
+                                       C.c_int32, C.c_int32]
+    L.zfo_superres_upscale.restype = None
+    L.zfo_film_grain_estimate.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                          P(abi.ZfFilmGrain)]
+    L.zfo_film_grain_estimate.restype = None
+    L.zfo_film_grain_synthesize.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, P(abi.ZfFilmGrain)]
+    L.zfo_film_grain_synthesize.restype = None
     L.zfo_write_filter_params.argtypes = [P(abi.ZfDecisions), P(abi.ZfHeaderOpts), C.c_void_p, C.c_int32,
                                           P(C.c_int32)]
     _lib = L
@@ -228,3 +237,25 @@ def write_filter_params(dec, opts, nbytes=64):
     rc = lib().zfo_write_filter_params(C.byref(dec), C.byref(opts), buf.ctypes.data, nbytes, C.byref(pos))
     assert rc == 0, rc
     return "".join(str((buf[i >> 3] >> (7 - (i & 7))) & 1) for i in range(pos.value))
+
+
+def superres_upscale(src, dst_width, bd=8):
+    rows, w = src.shape
+    src = np.ascontiguousarray(src)
+    dst = np.empty((rows, dst_width), src.dtype)
+    lib().zfo_superres_upscale(src.ctypes.data, w, w, dst.ctypes.data, dst_width, dst_width, rows, bd)
+    return dst
+
+
+def film_grain_estimate(src, recon):
+    h, w = src.shape
+    p = abi.ZfFilmGrain()
+    lib().zfo_film_grain_estimate(np.ascontiguousarray(src).ctypes.data, np.ascontiguousarray(recon).ctypes.data,
+                                  w, h, w, C.byref(p))
+    return p
+
+
+def film_grain_synthesize(frame, params):
+    h, w = frame.shape
+    lib().zfo_film_grain_synthesize(frame.ctypes.data, w, h, w, C.byref(params))
+    return frame

@@ -2786,4 +2786,91 @@ int32_t zfo_write_filter_params(const zf_decisions *d, const zf_header_opts *o, 
     return ZF_OK;
 }
 
+
+/* ---- superres (DSP/superres.rs) ---------------------------------------- */
+int32_t zfo_superres_scaled_size(int32_t dim, int32_t denom) {
+    // calculate_scaled_size_helper (superres.rs:140-149)
+    if (denom != 8 && denom <= 16) {
+        const int min_dim = std::min(16, dim);
+        const int scaled = (dim * 8 + denom / 2) / denom;
+        return std::max(scaled, min_dim);
+    }
+    return dim;
+}
+
+/* upscale_normative_plane (superres.rs:252-275) with upscale_normative_row
+ * (:208-249) and TileColPad::FRAME; bd > 8 reads/writes u16 and clips to
+ * the bit depth. */
+void zfo_superres_upscale(const void *src, int32_t src_stride, int32_t src_width, void *dst, int32_t dst_stride,
+                          int32_t dst_width, int32_t rows, int32_t bd) {
+    const i32 x_step = ((src_width << 14) + dst_width / 2) / dst_width;  // upscale_convolve_step
+    const i32 err = dst_width * x_step - (src_width << 14);              // upscale_convolve_x0
+    const i32 x0r = (-((dst_width - src_width) << 13) + dst_width / 2) / dst_width + (1 << 7) - err / 2;
+    const i32 x0 = (i32)((u32)x0r & 16383u);
+    for (int r = 0; r < rows; ++r) {
+        i32 x_qn = x0;
+        for (int x = 0; x < dst_width; ++x) {
+            const i32 base = x_qn >> 14;
+            const int phase = (x_qn & 16383) >> 8;
+            i32 sum = 0;
+            for (int k = 0; k < 8; ++k) {
+                const i32 idx = base - 4 + k;
+                const i32 i = idx < 0 ? 0 : (idx >= src_width ? src_width - 1 : idx);
+                const i32 v = bd == 8 ? ((const u8 *)src)[(i64)r * src_stride + i]
+                                      : ((const u16 *)src)[(i64)r * src_stride + i];
+                sum += v * zf_superres_filter[phase][k];
+            }
+            const i32 o = std::min(std::max((sum + 64) >> 7, 0), (1 << bd) - 1);
+            if (bd == 8) ((u8 *)dst)[(i64)r * dst_stride + x] = (u8)o;
+            else ((u16 *)dst)[(i64)r * dst_stride + x] = (u16)o;
+            x_qn += x_step;
+        }
+    }
+}
+
+/* ---- film grain (ENC/film_grain.rs) ------------------------------------ */
+/* estimate_film_grain (film_grain.rs:74-119). */
+void zfo_film_grain_estimate(const uint8_t *source, const uint8_t *denoised, int32_t width, int32_t height,
+                             int32_t stride, zf_film_grain *p) {
+    std::memset(p, 0, sizeof(*p));
+    i64 noise_sum = 0, noise_sq_sum = 0;
+    const i64 n = (i64)width * height;
+    for (int r = 0; r < height; ++r)
+        for (int c = 0; c < width; ++c) {
+            const i32 noise = (i32)source[(i64)r * stride + c] - (i32)denoised[(i64)r * stride + c];
+            noise_sum += noise;
+            noise_sq_sum += (i64)(noise * noise);
+        }
+    const double mean = n > 0 ? (double)noise_sum / (double)n : 0.0;
+    const double noise_var = n > 0 ? (double)noise_sq_sum / (double)n - mean * mean : 0.0;
+    p->noise_var = noise_var;
+    if (noise_var < 4.0) return;
+    p->apply_grain = 1;
+    p->grain_seed = 42;
+    p->ar_coeff_lag = 0;
+    p->grain_scale_shift = 0;
+    p->overlap_flag = 1;
+    p->num_y_points = 2;
+    const double v = std::min(std::sqrt(noise_var) * 2.0, 255.0);
+    p->point_y_value[0] = 0;
+    p->point_y_scaling[0] = (u8)v;
+    p->point_y_value[1] = 255;
+    p->point_y_scaling[1] = (u8)v;
+}
+
+/* synthesize_grain (film_grain.rs:127-150). */
+void zfo_film_grain_synthesize(uint8_t *frame, int32_t width, int32_t height, int32_t stride,
+                               const zf_film_grain *p) {
+    if (!p->apply_grain || p->num_y_points == 0) return;
+    const i32 scaling = p->point_y_scaling[0];
+    u32 seed = p->grain_seed;
+    for (int r = 0; r < height; ++r)
+        for (int c = 0; c < width; ++c) {
+            seed = seed * 1103515245u + 12345u;
+            const i32 noise = ((i32)(seed >> 16) % (scaling * 2 + 1)) - scaling;
+            const i32 val = (i32)frame[(i64)r * stride + c] + noise;
+            frame[(i64)r * stride + c] = (u8)std::min(std::max(val, 0), 255);
+        }
+}
+
 }  // extern "C"

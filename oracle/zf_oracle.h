@@ -111,6 +111,14 @@ int32_t zfo_sgr_apply(int32_t bd, int32_t pw, int32_t ph, int32_t ss, const void
 void zfo_sgr_box_filter(int32_t bd, int32_t pw, int32_t ph, const void *dgd, int32_t set, int32_t pass, int32_t x,
                         int32_t y, int32_t w, int32_t h, int32_t *out);
 void zfo_sgr_params(int32_t set, int32_t out[4]);
+/* Superres and film grain (DSP/superres.rs, ENC/film_grain.rs). */
+int32_t zfo_superres_scaled_size(int32_t dim, int32_t denom);
+void zfo_superres_upscale(const void *src, int32_t src_stride, int32_t src_width, void *dst, int32_t dst_stride,
+                          int32_t dst_width, int32_t rows, int32_t bd);
+void zfo_film_grain_estimate(const uint8_t *source, const uint8_t *denoised, int32_t width, int32_t height,
+                             int32_t stride, zf_film_grain *p);
+void zfo_film_grain_synthesize(uint8_t *frame, int32_t width, int32_t height, int32_t stride,
+                               const zf_film_grain *p);
 /* Frame-header loop_filter / cdef / lr params (ENT/obu.rs:1268-1377). */
 int32_t zfo_write_filter_params(const zf_decisions *d, const zf_header_opts *o, uint8_t *buf, int32_t cap,
                                 int32_t *bit_pos);

@@ -16,6 +16,7 @@ Sources (paths relative to the reference project):
   rust/crates/svtav1-encoder/src/deblock.rs (tests)        closed-form levels
   rust/crates/svtav1-encoder/src/restoration.rs (tests)    RD constants
   rust/crates/svtav1-encoder/src/pd0.rs (doc comment)      lambda anchors
+  rust/crates/svtav1-dsp/src/superres.rs                  normative upscale filter (64 x 8)
 
 Usage: python tests/golden/gen_golden.py [REF_ROOT]
 """
@@ -123,6 +124,14 @@ def main():
         "ac10": _table(os.path.join(crates, "svtav1-encoder/src/bd10_qlookup_tables.rs"),
                        "pub static AC_QLOOKUP_10"),
     }
+
+    sr = open(os.path.join(crates, "svtav1-dsp/src/superres.rs")).read()
+    i = sr.index("RESIZE_FILTER_NORMATIVE")
+    j = sr.index("= [", sr.index("pub static RESIZE_FILTER_NORMATIVE"))
+    body = sr[j + 3:sr.index("];", j)]
+    taps = [int(x) for x in re.findall(r"-?\d+", body)]
+    assert len(taps) == 64 * 8, len(taps)
+    out["tables"]["superres_filter"] = [taps[k * 8:(k + 1) * 8] for k in range(64)]
 
     # Wiener captures. The two 64x64 cells carry their C recon inputs.
     lr = {}

@@ -89,7 +89,17 @@ def lib():
     L.zf_sgr_apply.argtypes = [C.c_void_p, P(abi.ZfSgrPlane), C.c_void_p, C.c_int32, C.c_void_p]
     L.zf_write_filter_params.argtypes = [P(ZfDecisions), P(abi.ZfHeaderOpts), C.c_void_p, C.c_int32,
                                          P(C.c_int32)]
-    for name in ("zf_write_filter_params", "zf_sgr_search", "zf_sgr_apply", "zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
+    L.zf_use_graphs.argtypes = [C.c_void_p, C.c_int32]
+    L.zf_graph_stats.argtypes = [C.c_void_p, P(C.c_uint64)]
+    L.zf_superres_scaled_size.argtypes = [C.c_int32, C.c_int32]
+    L.zf_superres_upscale.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
+                                      C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.zf_film_grain_estimate.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                         C.c_int32, P(abi.ZfFilmGrain)]
+    L.zf_film_grain_synthesize.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                           P(abi.ZfFilmGrain)]
+    for name in ("zf_use_graphs", "zf_graph_stats", "zf_superres_scaled_size", "zf_superres_upscale", "zf_film_grain_estimate",
+                 "zf_film_grain_synthesize", "zf_write_filter_params", "zf_sgr_search", "zf_sgr_apply", "zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
                  "zf_submit_batch", "zf_deblock_pick", "zf_deblock_apply", "zf_cdef_search",
                  "zf_cdef_apply", "zf_lr_search", "zf_lr_apply"):
         getattr(L, name).restype = C.c_int32
@@ -171,6 +181,16 @@ class Context:
 
     def profile_reset(self):
         lib().zf_profile_reset(self.h)
+
+    def use_graphs(self, enable=True):
+        """Run each call's launch sequence as a CUDA graph (zf_use_graphs)."""
+        self._check(lib().zf_use_graphs(self.h, 1 if enable else 0))
+
+    def graph_stats(self):
+        """(graph launches, in-place updates, instantiations)."""
+        out = (C.c_uint64 * 3)()
+        self._check(lib().zf_graph_stats(self.h, out))
+        return tuple(out)
 
     def profile_read(self):
         """{kernel name: (launches, total_ms)} measured with CUDA events."""
@@ -255,6 +275,31 @@ class Context:
         s = abi.make_frame_struct(fr, fr.src, rec, mi)
         pre = (C.c_void_p * 3)(*[p.ctypes.data for p in pre_cdef])
         self._check(lib().zf_lr_apply(self.h, C.byref(s), pre, C.byref(dec.c)))
+
+    # -- superres and film grain -----------------------------------------
+    def superres_upscale(self, src, dst_width, bit_depth=8):
+        """Normative horizontal upscale of a (rows, width) host plane."""
+        rows, w = src.shape
+        src = np.ascontiguousarray(src)
+        dst = np.empty((rows, dst_width), src.dtype)
+        self._check(lib().zf_superres_upscale(self.h, src.ctypes.data, w, w, dst.ctypes.data, dst_width,
+                                              dst_width, rows, bit_depth, 0))
+        return dst
+
+    def film_grain_estimate(self, src, recon):
+        h, w = src.shape
+        p = abi.ZfFilmGrain()
+        self._check(lib().zf_film_grain_estimate(self.h, np.ascontiguousarray(src).ctypes.data,
+                                                 np.ascontiguousarray(recon).ctypes.data, w, h, w, 0,
+                                                 C.byref(p)))
+        return p
+
+    def film_grain_synthesize(self, frame, params):
+        """Adds the grain to a (rows, width) u8 host plane in place."""
+        h, w = frame.shape
+        assert frame.flags.c_contiguous
+        self._check(lib().zf_film_grain_synthesize(self.h, frame.ctypes.data, w, h, w, 0, C.byref(params)))
+        return frame
 
     # -- self-guided restoration ------------------------------------------
     @staticmethod

@@ -54,13 +54,27 @@ class ZfSizes(C.Structure):
 
 
 class ZfOpts(C.Structure):
-    _fields_ = [("device", C.c_int32), ("pad", C.c_int32), ("hbm_budget_bytes", C.c_uint64),
+    _fields_ = [("device", C.c_int32), ("flags", C.c_int32), ("hbm_budget_bytes", C.c_uint64),
                 ("cancel_flag", C.POINTER(C.c_int32))]
 
 
 class ZfHeaderOpts(C.Structure):
     _fields_ = [("monochrome", C.c_int32), ("allow_intrabc", C.c_int32), ("enable_restoration", C.c_int32),
                 ("sb_size", C.c_int32), ("sharpness", C.c_int32), ("pad", C.c_int32)]
+
+
+class ZfFilmGrain(C.Structure):
+    _fields_ = [("apply_grain", C.c_int32), ("grain_seed", C.c_uint16), ("num_y_points", C.c_uint8),
+                ("num_cb_points", C.c_uint8), ("num_cr_points", C.c_uint8),
+                ("point_y_value", C.c_uint8 * 14), ("point_y_scaling", C.c_uint8 * 14),
+                ("point_cb_value", C.c_uint8 * 10), ("point_cb_scaling", C.c_uint8 * 10),
+                ("point_cr_value", C.c_uint8 * 10), ("point_cr_scaling", C.c_uint8 * 10),
+                ("ar_coeffs_y", C.c_int8 * 24), ("ar_coeffs_cb", C.c_int8 * 25), ("ar_coeffs_cr", C.c_int8 * 25),
+                ("ar_coeff_lag", C.c_uint8), ("ar_coeff_shift", C.c_uint8), ("grain_scale_shift", C.c_uint8),
+                ("cb_mult", C.c_uint8), ("cb_luma_mult", C.c_uint8), ("cr_mult", C.c_uint8),
+                ("cr_luma_mult", C.c_uint8), ("overlap_flag", C.c_uint8), ("clip_to_restricted_range", C.c_uint8),
+                ("chroma_scaling_from_luma", C.c_uint8), ("cb_offset", C.c_uint16), ("cr_offset", C.c_uint16),
+                ("noise_var", C.c_double)]
 
 
 class ZfSgrPlane(C.Structure):

@@ -50,6 +50,12 @@ struct zf_ctx {
     // in one copy
     uint8_t *h_meta = nullptr, *h_out = nullptr;
     size_t h_meta_cap = 0, h_out_cap = 0;
+    // CUDA graph mode: one executable graph, updated from each call's capture
+    bool graphs = false;
+    bool capturing = false;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<uint64_t> gsig;  // node kinds, kernel functions and cluster shapes of gexec's graph
+    uint64_t graph_launches = 0, graph_updates = 0, graph_instantiations = 0;
 };
 
 namespace {
@@ -523,6 +529,7 @@ int ensure_arena(zf_ctx *ctx, size_t need) {
 }
 
 int check_cancel(zf_ctx *ctx) {
+    if (ctx->capturing) return ZF_OK;  // polled again after the graph
     if (ctx->cancel && *ctx->cancel) {
         cudaStreamSynchronize(ctx->stream);
         return fail(ctx, ZF_ERR_CANCELLED, "cancelled");
@@ -586,6 +593,94 @@ int launch_check(zf_ctx *ctx, const char *what) {
         int r_ = (x);           \
         if (r_ != ZF_OK) return r_; \
     } while (0)
+
+// Ends an open stream capture on every exit path (the graph is discarded).
+struct CaptureGuard {
+    zf_ctx *ctx;
+    bool active = false;
+    ~CaptureGuard() {
+        if (!active) return;
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(ctx->stream, &g);
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        ctx->capturing = false;
+    }
+};
+
+// Ends the capture and launches it through the context's executable graph:
+// an in-place update when the captured sequence has the same shape as the
+// last one, a fresh instantiation otherwise.
+// The graph's shape for the update decision: per node its kind and, for a
+// kernel, its function and cluster dimensions (an update may change a
+// kernel's arguments, grid and shared memory, but the executable graph is
+// rebuilt when a function or a cluster shape differs).
+int graph_signature(zf_ctx *ctx, cudaGraph_t g, std::vector<uint64_t> &sig) {
+    size_t nn = 0;
+    CU(cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    CU(cudaGraphGetNodes(g, nodes.data(), &nn));
+    sig.clear();
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType t;
+        CU(cudaGraphNodeGetType(nd, &t));
+        sig.push_back((uint64_t)t);
+        if (t == cudaGraphNodeTypeKernel) {
+            cudaKernelNodeParams kp;
+            CU(cudaGraphKernelNodeGetParams(nd, &kp));
+            sig.push_back((uint64_t)(uintptr_t)kp.func);
+            cudaLaunchAttributeValue v;
+            std::memset(&v, 0, sizeof(v));
+            if (cudaGraphKernelNodeGetAttribute(nd, cudaLaunchAttributeClusterDimension, &v) != cudaSuccess) {
+                cudaGetLastError();
+                std::memset(&v, 0, sizeof(v));
+            }
+            sig.push_back((uint64_t)v.clusterDim.x << 32 | (uint64_t)v.clusterDim.y << 16 | v.clusterDim.z);
+        }
+    }
+    return ZF_OK;
+}
+
+int launch_captured(zf_ctx *ctx, CaptureGuard &cg) {
+    cudaGraph_t g = nullptr;
+    cg.active = false;
+    ctx->capturing = false;
+    CU(cudaStreamEndCapture(ctx->stream, &g));
+    std::vector<uint64_t> sig;
+    const int rc = graph_signature(ctx, g, sig);
+    if (rc != ZF_OK) {
+        cudaGraphDestroy(g);
+        return rc;
+    }
+    bool ok = false;
+    if (ctx->gexec && sig == ctx->gsig) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(ctx->gexec, g, &info) == cudaSuccess) {
+            ok = true;
+            ctx->graph_updates++;
+        } else {
+            cudaGetLastError();
+            cudaGraphExecDestroy(ctx->gexec);
+            ctx->gexec = nullptr;
+        }
+    }
+    if (!ok) {
+        if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+        ctx->gexec = nullptr;
+        ctx->gsig = sig;
+        const cudaError_t e = cudaGraphInstantiate(&ctx->gexec, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            ctx->gexec = nullptr;
+            return fail(ctx, ZF_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        }
+        ctx->graph_instantiations++;
+    }
+    cudaGraphDestroy(g);
+    CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
+    ctx->graph_launches++;
+    return ZF_OK;
+}
 
 int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf_stats *stats, const Run &run) {
     if (!ctx) return ZF_ERR_ARG;
@@ -896,6 +991,16 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             for (auto &s : slots) plans[s.frame].d.lf[1 + s.plane] = (uint8_t)s.hc.result;
     }
 
+    // ---- graph mode: everything from here to the decision readback is
+    // captured and launched as one graph
+    CaptureGuard cg{ctx};
+    const bool use_graph = ctx->graphs && !ctx->profiling;
+    if (use_graph) {
+        CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cg.active = true;
+        ctx->capturing = true;
+    }
+
     // ---- metadata image (descriptors, work lists, CDEF frames, unit
     // rectangles) to the device in one copy
     {
@@ -1042,8 +1147,11 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         }
     }
 
-    // ---- outputs: planes to the caller, then the descriptors and the output
-    // region (fb_idx, fb_row, counters, unit records) in two copies
+    // ---- outputs: the descriptors and the output region (fb_idx, fb_row,
+    // counters, unit records) in two copies, then the planes to the caller
+    CU(cudaMemcpyAsync(ctx->h_out, d_desc, desc_bytes, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(ctx->h_out + hdesc, base + o_out, out_bytes, cudaMemcpyDeviceToHost, st));
+    if (use_graph) TRY(launch_captured(ctx, cg));
     for (int i = 0; i < n; ++i) {
         Plan &p = plans[i];
         const zf_frame *f = p.in;
@@ -1052,10 +1160,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             for (int pl = 0; pl < p.nplanes; ++pl)
                 TRY(copy_out(ctx, f->rec[pl], base + p.off_set[run.rec_out][pl], p.pbytes[pl], dev));
     }
-    CU(cudaMemcpyAsync(ctx->h_out, d_desc, desc_bytes, cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(ctx->h_out + hdesc, base + o_out, out_bytes, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     TRY(launch_check(ctx, "stream"));
+    if (use_graph) TRY(check_cancel(ctx));
     collect_profile(ctx);
     const FrameDesc *back = (const FrameDesc *)ctx->h_out;
     const uint8_t *ob = ctx->h_out + hdesc;
@@ -1212,6 +1319,7 @@ int32_t zf_create(zf_ctx **out, const zf_opts *opts) {
     c->device = opts ? opts->device : 0;
     c->budget = opts ? opts->hbm_budget_bytes : 0;
     c->cancel = opts ? opts->cancel_flag : nullptr;
+    c->graphs = opts && (opts->flags & ZF_OPT_GRAPHS);
     if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         set_kernel_attributes() != cudaSuccess) {
         cudaGetLastError();
@@ -1229,6 +1337,7 @@ void zf_destroy(zf_ctx *ctx) {
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->h_meta) cudaFreeHost(ctx->h_meta);
     if (ctx->h_out) cudaFreeHost(ctx->h_out);
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -1327,6 +1436,20 @@ int32_t zf_pack_geom(int32_t mi_cols, int32_t mi_rows, const uint32_t *block_id,
 }
 
 uint64_t zf_launch_count(const zf_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int32_t zf_use_graphs(zf_ctx *ctx, int32_t enable) {
+    if (!ctx) return ZF_ERR_ARG;
+    ctx->graphs = enable != 0;
+    return ZF_OK;
+}
+
+int32_t zf_graph_stats(const zf_ctx *ctx, uint64_t out[3]) {
+    if (!ctx || !out) return ZF_ERR_ARG;
+    out[0] = ctx->graph_launches;
+    out[1] = ctx->graph_updates;
+    out[2] = ctx->graph_instantiations;
+    return ZF_OK;
+}
 
 void *zf_stream(const zf_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
@@ -1608,6 +1731,152 @@ int32_t zf_write_filter_params(const zf_decisions *d, const zf_header_opts *o, u
     }
     if (overflow) return ZF_ERR_ARG;
     *bit_pos = pos;
+    return ZF_OK;
+}
+
+// ---- superres upscale and film grain (zf_post.cu kernels) ----------------
+
+int32_t zf_superres_scaled_size(int32_t dim, int32_t denom) {
+    // calculate_scaled_size_helper (svtav1-dsp/src/superres.rs:140)
+    if (dim <= 0 || dim > 65535) return dim;
+    if (denom != 8 && denom <= 16) {
+        const int min_dim = std::min(16, dim);
+        const int scaled = (dim * 8 + denom / 2) / denom;
+        return std::max(scaled, min_dim);
+    }
+    return dim;
+}
+
+int32_t zf_superres_upscale(zf_ctx *ctx, const void *src, int32_t src_width, int32_t src_stride, void *dst,
+                            int32_t dst_width, int32_t dst_stride, int32_t rows, int32_t bit_depth,
+                            int32_t on_device) {
+    if (!ctx) return ZF_ERR_ARG;
+    if (!src || !dst) return fail(ctx, ZF_ERR_ARG, "src or dst is NULL");
+    if (bit_depth != 8 && bit_depth != 10) return fail(ctx, ZF_ERR_UNSUPPORTED, "bit_depth must be 8 or 10");
+    if (src_width <= 0 || dst_width < src_width || dst_width > 16384 || rows <= 0 || rows > 16384 ||
+        src_stride < src_width || dst_stride < dst_width)
+        return fail(ctx, ZF_ERR_INVALID_DIMS, "superres dims out of range");
+    CU(cudaSetDevice(ctx->device));
+    // upscale_convolve_step / upscale_convolve_x0 (superres.rs:117, :128)
+    const int x_step = ((src_width << 14) + dst_width / 2) / dst_width;
+    const int err = dst_width * x_step - (src_width << 14);
+    const int x0r = (-((dst_width - src_width) << 13) + dst_width / 2) / dst_width + (1 << 7) - err / 2;
+    const int x0 = (int)((uint32_t)x0r & 16383u);
+    const size_t bps = bit_depth == 8 ? 1 : 2;
+    const size_t sbytes = ((size_t)(rows - 1) * src_stride + src_width) * bps;
+    const size_t dbytes = ((size_t)(rows - 1) * dst_stride + dst_width) * bps;
+    const bool dev = on_device != 0;
+    const uint8_t *d_src = static_cast<const uint8_t *>(src);
+    uint8_t *d_dst = static_cast<uint8_t *>(dst);
+    if (!dev) {
+        TRY(ensure_arena(ctx, align_up(sbytes, 256) + dbytes));
+        TRY(copy_in(ctx, ctx->arena, src, sbytes, false));
+        d_src = ctx->arena;
+        d_dst = ctx->arena + align_up(sbytes, 256);
+    }
+    cudaStream_t st = ctx->stream;
+    { LaunchScope ls_(ctx, "k_superres_upscale");
+    zf::k_superres_upscale<<<rows, 256, src_width * bps, st>>>(d_src, src_width, src_stride, d_dst, dst_width,
+                                                                dst_stride, bit_depth, x_step, x0); }
+    TRY(launch_check(ctx, "k_superres_upscale"));
+    if (!dev) TRY(copy_out(ctx, dst, d_dst, dbytes, false));
+    CU(cudaStreamSynchronize(st));
+    TRY(launch_check(ctx, "stream"));
+    collect_profile(ctx);
+    return ZF_OK;
+}
+
+int32_t zf_film_grain_estimate(zf_ctx *ctx, const uint8_t *src, const uint8_t *recon, int32_t width,
+                               int32_t height, int32_t stride, int32_t on_device, zf_film_grain *out) {
+    if (!ctx) return ZF_ERR_ARG;
+    if (!src || !recon || !out) return fail(ctx, ZF_ERR_ARG, "NULL argument");
+    if (width < 0 || height < 0 || width > 65536 || height > 65536 || (height > 0 && stride < width))
+        return fail(ctx, ZF_ERR_INVALID_DIMS, "film grain dims out of range");
+    std::memset(out, 0, sizeof(*out));
+    long long sum = 0;
+    unsigned long long sq = 0;
+    const long long n = (long long)width * height;
+    if (n > 0) {
+        CU(cudaSetDevice(ctx->device));
+        const size_t bytes = (size_t)(height - 1) * stride + width;
+        const bool dev = on_device != 0;
+        const size_t o_sums = dev ? 0 : 2 * align_up(bytes, 256);
+        TRY(ensure_arena(ctx, o_sums + 16));
+        TRY(ensure_host(ctx, ctx->h_out, ctx->h_out_cap, 16));
+        const uint8_t *d_src = src, *d_rec = recon;
+        if (!dev) {
+            TRY(copy_in(ctx, ctx->arena, src, bytes, false));
+            TRY(copy_in(ctx, ctx->arena + align_up(bytes, 256), recon, bytes, false));
+            d_src = ctx->arena;
+            d_rec = ctx->arena + align_up(bytes, 256);
+        }
+        cudaStream_t st = ctx->stream;
+        unsigned long long *d_sums = (unsigned long long *)(ctx->arena + o_sums);
+        CU(cudaMemsetAsync(d_sums, 0, 16, st));
+        // contiguous aligned planes: one flat run over a grid of 8 CTAs per SM
+        // (rows_per_cta 0); otherwise row blocks
+        const bool flat = stride == width && ((reinterpret_cast<uintptr_t>(d_src) | reinterpret_cast<uintptr_t>(d_rec)) & 15) == 0;
+        const long long nchunk = (long long)width * height / 16;
+        const int rpc = flat ? 0 : std::max(1, (int)((long long)height * width / (152LL * 4 * 16384) + 1));
+        const int grid = flat ? (int)std::max(1LL, std::min(152LL * 8, (nchunk + 1023) / 1024)) : (height + rpc - 1) / rpc;
+        { LaunchScope ls_(ctx, "k_grain_sums");
+        zf::k_grain_sums<<<grid, 256, 0, st>>>(d_src, d_rec, width, height, stride, rpc, d_sums); }
+        TRY(launch_check(ctx, "k_grain_sums"));
+        CU(cudaMemcpyAsync(ctx->h_out, d_sums, 16, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        TRY(launch_check(ctx, "stream"));
+        collect_profile(ctx);
+        unsigned long long h[2];
+        std::memcpy(h, ctx->h_out, 16);
+        sum = (long long)h[0];
+        sq = h[1];
+    }
+    // estimate_film_grain (film_grain.rs:74-119): variance in f64, a flat
+    // two-point luma scaling curve when it reaches 4
+    const double var = n > 0 ? (double)sq / (double)n - ((double)sum / (double)n) * ((double)sum / (double)n) : 0.0;
+    out->noise_var = var;
+    if (var < 4.0) return ZF_OK;
+    out->apply_grain = 1;
+    out->grain_seed = 42;
+    out->overlap_flag = 1;
+    out->num_y_points = 2;
+    const double sc = std::min(std::sqrt(var) * 2.0, 255.0);
+    const uint8_t s8 = (uint8_t)sc;  // Rust `as u8` of a value in [0, 255]: truncation
+    out->point_y_value[0] = 0;
+    out->point_y_scaling[0] = s8;
+    out->point_y_value[1] = 255;
+    out->point_y_scaling[1] = s8;
+    return ZF_OK;
+}
+
+int32_t zf_film_grain_synthesize(zf_ctx *ctx, uint8_t *frame, int32_t width, int32_t height, int32_t stride,
+                                 int32_t on_device, const zf_film_grain *p) {
+    if (!ctx) return ZF_ERR_ARG;
+    if (!frame || !p) return fail(ctx, ZF_ERR_ARG, "NULL argument");
+    if (width < 0 || height < 0 || width > 65536 || height > 65536 || (height > 0 && stride < width))
+        return fail(ctx, ZF_ERR_INVALID_DIMS, "film grain dims out of range");
+    if (!p->apply_grain || p->num_y_points == 0 || width == 0 || height == 0) return ZF_OK;
+    CU(cudaSetDevice(ctx->device));
+    const size_t bytes = (size_t)(height - 1) * stride + width;
+    const bool dev = on_device != 0;
+    uint8_t *d = frame;
+    if (!dev) {
+        TRY(ensure_arena(ctx, bytes));
+        TRY(copy_in(ctx, ctx->arena, frame, bytes, false));
+        d = ctx->arena;
+    }
+    cudaStream_t st = ctx->stream;
+    const long long total = (long long)width * height;
+    const long long threads = (total + zf::kGrainRunHost - 1) / zf::kGrainRunHost;
+    { LaunchScope ls_(ctx, "k_grain_synth");
+    zf::k_grain_synth<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(d, width, height, stride,
+                                                                         (uint32_t)p->grain_seed,
+                                                                         (int)p->point_y_scaling[0]); }
+    TRY(launch_check(ctx, "k_grain_synth"));
+    if (!dev) TRY(copy_out(ctx, frame, d, bytes, false));
+    CU(cudaStreamSynchronize(st));
+    TRY(launch_check(ctx, "stream"));
+    collect_profile(ctx);
     return ZF_OK;
 }
 

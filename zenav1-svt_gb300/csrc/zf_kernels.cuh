@@ -85,4 +85,12 @@ __global__ void k_sgr_apply(SgrPlaneDesc P, const SgrTile *tiles, const zf_sgr_u
 size_t sgr_smem_bytes();
 cudaError_t sgr_set_attributes();
 
+// ---- superres upscale, film grain (zf_post.cu) ------------------------------
+__global__ void k_superres_upscale(const uint8_t *src, int src_w, int src_stride, uint8_t *dst, int dst_w,
+                                   int dst_stride, int bd, int x_step, int x0);
+__global__ void k_grain_sums(const uint8_t *src, const uint8_t *rec, int w, int h, int stride, int rows_per_cta,
+                             unsigned long long *out);
+__global__ void k_grain_synth(uint8_t *frame, int w, int h, int stride, uint32_t seed, int scaling);
+constexpr int kGrainRunHost = 32;  // k_grain_synth: pixels per thread
+
 }  // namespace zf
