@@ -124,6 +124,7 @@ typedef struct zf_sizes {
 } zf_sizes;
 
 #define ZF_OPT_GRAPHS 1          /* zf_opts.flags: run each call's launch sequence as a CUDA graph */
+#define ZF_OPT_NO_TMA 2          /* zf_opts.flags: stage the statistics rows with thread loads, not TMA */
 
 typedef struct zf_opts {
     int32_t device;             /* CUDA device ordinal */

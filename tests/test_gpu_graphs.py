@@ -46,3 +46,25 @@ def test_graph_mode_matches_direct_launches(pkg):
     finally:
         direct.close()
         graph.close()
+
+
+def test_tma_rows_match_thread_staging(pkg):
+    """The statistics kernel's TMA-loaded rows (8-bit planes with 16-byte
+    row pitch) give the same stage as thread-staged rows, including units at
+    every plane edge, odd true sizes and the zero-copy device path."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from zenav1_svt_gb300 import abi
+    a, b = pkg.Context(0), pkg.Context(0, flags=abi.OPT_NO_TMA)
+    try:
+        for k, (w, h, qp, preset) in enumerate([(1024, 576, 30, 6), (1000, 600, 44, 4), (517, 389, 36, 6),
+                                                 (640, 1152, 24, 6), (96, 64, 40, 6), (1018, 571, 34, 6)]):
+            fr = synth.make_frame(synth.frame_seed(15, k), w, h, 8, qp, preset, "power")
+            d0, s0, r0 = a.filter_stage(fr)
+            d1, s1, r1 = b.filter_stage(fr)
+            assert_same_decisions(d1, d0)
+            assert_same_planes(r1, r0)
+    finally:
+        a.close()
+        b.close()

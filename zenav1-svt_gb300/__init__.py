@@ -126,11 +126,13 @@ def stats_dict(s):
 class Context:
     """One CUDA stream + device arena (zf_create); not thread-safe."""
 
-    def __init__(self, device=0, hbm_budget_bytes=0, cancel_flag=None):
+    def __init__(self, device=0, hbm_budget_bytes=0, cancel_flag=None, flags=0):
+        """flags: abi.OPT_GRAPHS / abi.OPT_NO_TMA (zf_opts.flags)."""
         L = lib()
         self._cancel = cancel_flag
         opts = ZfOpts()
         opts.device = device
+        opts.flags = flags
         opts.hbm_budget_bytes = hbm_budget_bytes
         if cancel_flag is not None:
             opts.cancel_flag = C.cast(cancel_flag, C.POINTER(C.c_int32))

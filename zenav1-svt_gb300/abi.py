@@ -10,6 +10,7 @@ ERRORS = {
     -5: "CudaError", -6: "InvalidArgument", -7: "InvalidGeometry", -8: "Timeout",
 }
 RESTORE_NONE, RESTORE_WIENER = 0, 1
+OPT_GRAPHS, OPT_NO_TMA = 1, 2  # zf_opts.flags
 
 
 class ZfFrame(C.Structure):

@@ -64,7 +64,20 @@ struct LrPlane {
     UnitRect *rects;     // hunits*vunits
     LrUnit *units;       // hunits*vunits
     PackedUnit *packed;  // hunits*vunits output records
+    // Tensor maps (CUtensorMap, 128 B each, in the metadata image) of the
+    // post-CDEF and source planes for the statistics kernel's TMA loads:
+    // 4-byte elements over (stride / 4, ph), boxes of kTmaDBoxW x kTmaDBoxH
+    // (post-CDEF) and kTmaXBoxW x kTmaXBoxH (source). nullptr: the kernel
+    // stages with thread loads (10-bit, 7-tap, strides not a multiple of 16).
+    const void *tm_a, *tm_s;
 };
+
+// Statistics kernel TMA boxes (5-tap window, 8-bit): the post-CDEF window
+// of a CTA (26 rows = 18 rows + 8 halo rows) starting 16 bytes left of the
+// unit (its 2-column halo at byte 14), the source rows of a CTA (18); widths
+// cover a unit of up to 383 columns plus halos, in 4-byte elements.
+constexpr int kTmaDBoxW = 104, kTmaDBoxH = 26, kTmaXBoxW = 96, kTmaXBoxH = 18;
+constexpr int kTmaDLead = 14;  // byte of column -2 (the window's first) in a D row
 
 // CDEF joint strength search: bit counts 0..3, one cluster each.
 constexpr int kFinLevels = 4;
@@ -205,6 +218,48 @@ __device__ __forceinline__ void stage_window(int bd, int pw, int nrows, int xa, 
             }
         }
     }
+}
+
+// ---- TMA and mbarrier (inline PTX) ---------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(mbar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Waits for the mbarrier phase with an iteration limit; false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *mbar, uint32_t parity, uint32_t limit) {
+    for (uint32_t it = 0; it < limit; ++it)
+        if (mbar_try_wait(mbar, parity)) return true;
+    return false;
+}
+// The tensor map (written to global memory before the launch) is read
+// through the tensor-map proxy.
+__device__ __forceinline__ void tmap_acquire(const void *tmap) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tmap) : "memory");
+}
+// 2-D tiled TMA load of one box at element coordinates (x, y) into shared
+// memory (128-byte aligned), completing on mbar. x * element size must be a
+// multiple of 16 bytes; out-of-range elements read as zero.
+__device__ __forceinline__ void tma_load_2d(void *smem_dst, const void *tmap, int x, int y, uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(smem_dst)), "l"(tmap), "r"(x), "r"(y), "r"(smem_u32(mbar))
+        : "memory");
 }
 
 // ---- packed geometry (zf_filter.h) --------------------------------------

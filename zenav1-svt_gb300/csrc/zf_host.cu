@@ -15,6 +15,9 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "../../include/zf_av1_tables.h"
 #include "../../include/zf_filter.h"
 #include "zf_kernels.cuh"
@@ -53,6 +56,7 @@ struct zf_ctx {
     // CUDA graph mode: one executable graph, updated from each call's capture
     bool graphs = false;
     bool capturing = false;
+    bool tma = true;  // statistics kernel rows by TMA where the planes allow
     cudaGraphExec_t gexec = nullptr;
     std::vector<uint64_t> gsig;  // node kinds, kernel functions and cluster shapes of gexec's graph
     uint64_t graph_launches = 0, graph_updates = 0, graph_instantiations = 0;
@@ -594,6 +598,42 @@ int launch_check(zf_ctx *ctx, const char *what) {
         if (r_ != ZF_OK) return r_; \
     } while (0)
 
+// cuTensorMapEncodeTiled from the driver (looked up once; nullptr when the
+// driver does not provide it, and the kernels then stage with thread loads).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// A 2-D tensor map of an 8-bit plane as 4-byte elements (stride / 4 per
+// row, ph rows) with box_w x box_h boxes, zero fill outside. false when the
+// plane does not qualify (row pitch or base not 16-byte aligned) or the
+// encoder refuses it.
+bool encode_plane_map(void *out128, const uint8_t *plane, int stride, int ph, int box_w, int box_h) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || !plane || (stride & 15) || (reinterpret_cast<uintptr_t>(plane) & 15) || ph <= 0) return false;
+    alignas(64) CUtensorMap m;
+    const cuuint64_t dims[2] = {(cuuint64_t)stride / 4, (cuuint64_t)ph};
+    const cuuint64_t strides[1] = {(cuuint64_t)stride};
+    const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h}, estr[2] = {1, 1};
+    if (enc(&m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<uint8_t *>(plane), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    static_assert(sizeof(CUtensorMap) == 128, "tensor map size");
+    std::memcpy(out128, &m, 128);
+    return true;
+}
+
 // Ends an open stream capture on every exit path (the graph is discarded).
 struct CaptureGuard {
     zf_ctx *ctx;
@@ -783,6 +823,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     for (int k = 0; k < kLists; ++k) m_list[k] = mtake(lists[k]->bytes());
     const size_t m_cf = mtake(cdef_frames.size() * 4);
     const size_t m_rects = mtake(rcur);
+    const size_t m_tm = mtake((size_t)n * 3 * 256);  // per frame and plane: post-CDEF and source tensor maps
     const size_t meta_bytes = align_up(mcur, 256);
     // deblock search scratch: up to 3 slots per frame, each of at most the
     // largest frame's luma tiles (items, then their coarse index)
@@ -1006,6 +1047,19 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     {
         uint8_t *hm = ctx->h_meta;
         FrameDesc *hd = (FrameDesc *)(hm + m_desc);
+        // tensor maps of the 8-bit planes the 5-tap statistics read
+        for (int i = 0; i < n; ++i)
+            for (int pl = 0; pl < 3; ++pl) {
+                LrPlane &L = plans[i].d.lr[pl];
+                L.tm_a = L.tm_s = nullptr;
+                if (!ctx->tma || !L.on || L.win != 5 || plans[i].d.bd != 8) continue;
+                const size_t o = m_tm + ((size_t)i * 3 + pl) * 256;
+                if (encode_plane_map(hm + o, plans[i].d.A[pl], L.stride, L.ph, zf::kTmaDBoxW, zf::kTmaDBoxH) &&
+                    encode_plane_map(hm + o + 128, plans[i].d.S[pl], L.stride, L.ph, zf::kTmaXBoxW, zf::kTmaXBoxH)) {
+                    L.tm_a = base + o_meta + o;
+                    L.tm_s = base + o_meta + o + 128;
+                }
+            }
         for (int i = 0; i < n; ++i) hd[i] = plans[i].d;
         for (int k = 0; k < kLists; ++k)
             if (!lists[k]->items.empty()) lists[k]->write(hm + m_list[k]);
@@ -1171,6 +1225,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         const FrameDesc &b = back[i];
         const uint8_t *fbidx = ob + p.off_fbidx, *fbrow = ob + p.off_fbrow;
         const unsigned long long *cst = (const unsigned long long *)(ob + p.off_stats);
+        if (cst[3]) return fail(ctx, ZF_ERR_TIMEOUT, "a statistics tile load did not arrive within its wait limit");
         const bool searched = (run.stages & STG_LR_SEARCH) && !run.lr_given;
         auto packed = [&](int pl) { return (const zf::PackedUnit *)(ob + p.off_packed[pl]); };
         zf_decisions *o = p.out;
@@ -1320,6 +1375,7 @@ int32_t zf_create(zf_ctx **out, const zf_opts *opts) {
     c->budget = opts ? opts->hbm_budget_bytes : 0;
     c->cancel = opts ? opts->cancel_flag : nullptr;
     c->graphs = opts && (opts->flags & ZF_OPT_GRAPHS);
+    c->tma = !(opts && (opts->flags & ZF_OPT_NO_TMA));
     if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         set_kernel_attributes() != cudaSuccess) {
         cudaGetLastError();

@@ -18,6 +18,7 @@
 // pixels (products <= 1023^2, so no overflow) and folds them into int64, the
 // same exact value the reference's per-pixel int64 accumulation reaches.
 #include <climits>
+#include <type_traits>
 
 #include <cooperative_groups.h>
 
@@ -94,14 +95,19 @@ __device__ __forceinline__ uint32_t bytes_at(uint32_t w0, uint32_t w1) {
 }
 
 template <int WIN>
-__global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkItem *items, int nitems) {
+__global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *frames, const WorkItem *items, int nitems) {
     using G = StatGeom<WIN>;
     constexpr int HALF = G::H, WIN2 = WIN * WIN;
-    __shared__ __align__(16) int16_t D[G::DROWS * G::DCOLS];
-    __shared__ __align__(16) int16_t X[G::ROWS * kMaxUnitW];
+    __shared__ __align__(128) int16_t D[G::DROWS * G::DCOLS];
+    __shared__ __align__(128) int16_t X[G::ROWS * kMaxUnitW];
     __shared__ unsigned long long Hs[WIN2 * WIN2];
     __shared__ unsigned long long Ms[WIN2], Ss[WIN2], Es[4];  // Es: sum s, sse blocks, right, bottom
+    __shared__ __align__(8) uint64_t mbar;
     static_assert(G::DROWS * G::DSB <= (int)sizeof(D) && G::ROWS * G::XSB <= (int)sizeof(X), "byte layout fits");
+    static_assert(WIN != 5 || (kTmaDBoxH == G::DROWS && kTmaXBoxH == G::ROWS &&
+                               kTmaDBoxW * 4 * kTmaDBoxH <= (int)sizeof(D) && kTmaXBoxW * 4 * kTmaXBoxH <= (int)sizeof(X) &&
+                               kTmaDLead + kMaxUnitW + 2 * HALF + WIN <= kTmaDBoxW * 4 && kMaxUnitW <= kTmaXBoxW * 4 + 8),
+                  "TMA boxes cover the 5-tap windows");
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
     FrameDesc &f = frames[wi.frame];
@@ -119,27 +125,81 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
     const int dy0 = y0 - (WIN - 1), dx0 = -HALF;
     const int dcols = uw + 2 * HALF + WIN;
     const int drows = (y1 - y0) + 2 * (WIN - 1);
-    stage_window(
-        bd, pl.pw, drows, r.h_start + dx0, dcols, true, 0,
-        [&](int rr) { return row_ptr(dg, clampi(r.v_start + dy0 + rr, 0, pl.ph - 1), stride, bd); },
-        [&](int rr, int cc, int v) {
-            if (packed) Db[rr * G::DSB + cc] = (uint8_t)v;
-            else D[rr * G::DCOLS + cc] = (int16_t)v;
-        });
     const int xi0 = max(y0, 0), xi1 = min(y1, uh);
-    stage_window(
-        bd, pl.pw, xi1 - xi0, r.h_start, uw, true, 0,
-        [&](int rr) { return row_ptr(sr_, r.v_start + xi0 + rr, stride, bd); },
-        [&](int rr, int cc, int v) {
-            if (packed) Xb[rr * G::XSB + cc] = (uint8_t)v;
-            else X[rr * kMaxUnitW + cc] = (int16_t)v;
-        });
+    // 8-bit rows come by two TMA box loads when the plane has tensor maps:
+    // D rows of kTmaDBoxW * 4 bytes from 16 bytes left of the unit (column
+    // -2 at byte kTmaDLead), X rows of kTmaXBoxW * 4 bytes from the unit's
+    // first column; otherwise threads stage them (row pitch DSB / XSB).
+    const bool tma = packed && pl.tm_a != nullptr;
+    const int dpitch = tma ? kTmaDBoxW * 4 : G::DSB, dlead = tma ? kTmaDLead : 0;
+    const int xpitch = tma ? kTmaXBoxW * 4 : G::XSB;
+    if (tma) {
+        if (threadIdx.x == 0) {
+            mbar_init(&mbar, 1);
+            tmap_acquire(pl.tm_a);
+            tmap_acquire(pl.tm_s);
+            mbar_expect_tx(&mbar, (kTmaDBoxW * kTmaDBoxH + kTmaXBoxW * kTmaXBoxH) * 4);
+            tma_load_2d(Db, pl.tm_a, (r.h_start - 16) >> 2, r.v_start + dy0, &mbar);
+            tma_load_2d(Xb, pl.tm_s, r.h_start >> 2, r.v_start + xi0, &mbar);
+        }
+    } else {
+        stage_window(
+            bd, pl.pw, drows, r.h_start + dx0, dcols, true, 0,
+            [&](int rr) { return row_ptr(dg, clampi(r.v_start + dy0 + rr, 0, pl.ph - 1), stride, bd); },
+            [&](int rr, int cc, int v) {
+                if (packed) Db[rr * G::DSB + cc] = (uint8_t)v;
+                else D[rr * G::DCOLS + cc] = (int16_t)v;
+            });
+        stage_window(
+            bd, pl.pw, xi1 - xi0, r.h_start, uw, true, 0,
+            [&](int rr) { return row_ptr(sr_, r.v_start + xi0 + rr, stride, bd); },
+            [&](int rr, int cc, int v) {
+                if (packed) Xb[rr * G::XSB + cc] = (uint8_t)v;
+                else X[rr * kMaxUnitW + cc] = (int16_t)v;
+            });
+    }
     for (int q = threadIdx.x; q < WIN2 * WIN2; q += blockDim.x) Hs[q] = 0;
     if (threadIdx.x < WIN2) Ms[threadIdx.x] = Ss[threadIdx.x] = 0;
     if (threadIdx.x < 4) Es[threadIdx.x] = 0;
     __syncthreads();
+    if (tma) {
+        // bounded wait for both boxes; on a timeout the frame's error word is
+        // set, the copies in flight are waited for once more and the CTA ends
+        const bool late = !mbar_wait_bounded(&mbar, 0, 1u << 20);
+        if (__syncthreads_or(late)) {
+            if (threadIdx.x == 0) atomicOr(&f.cdef_stats[3], 1ull);
+            mbar_wait_bounded(&mbar, 0, 1u << 20);
+            return;
+        }
+        // The loads read zeros outside the tensor and the canvas padding
+        // beyond the true width: clamp columns, then rows, to the plane
+        // like the thread staging does.
+        const int gx_lo = r.h_start + dx0, gx_hi = gx_lo + dcols;
+        const int gy_lo = r.v_start + dy0, gy_hi = gy_lo + drows;
+        const int cl = max(0, -gx_lo), cr = max(0, gx_hi - pl.pw);
+        if (cl + cr) {
+            for (int q = threadIdx.x; q < drows * (cl + cr); q += blockDim.x) {
+                const int rr = q / (cl + cr), k = q - rr * (cl + cr);
+                const int gy = gy_lo + rr;
+                if (gy < 0 || gy >= pl.ph) continue;  // whole row copied below
+                uint8_t *row = Db + rr * dpitch + dlead;  // byte c <-> column c - HALF
+                if (k < cl) row[k] = row[-gx_lo];
+                else row[dcols - 1 - (k - cl)] = row[pl.pw - 1 - gx_lo];
+            }
+            __syncthreads();
+        }
+        if (gy_lo < 0 || gy_hi > pl.ph) {
+            for (int q = threadIdx.x; q < drows * dcols; q += blockDim.x) {
+                const int rr = q / dcols, c = q - rr * dcols;
+                const int gy = gy_lo + rr;
+                if (gy >= 0 && gy < pl.ph) continue;
+                Db[rr * dpitch + dlead + c] = Db[(clampi(gy, 0, pl.ph - 1) - gy_lo) * dpitch + dlead + c];
+            }
+            __syncthreads();
+        }
+    }
     auto Dat = [&](int y, int x) -> int {
-        return packed ? (int)Db[(y - dy0) * G::DSB + (x - dx0)] : (int)D[(y - dy0) * G::DCOLS + (x - dx0)];
+        return packed ? (int)Db[(y - dy0) * dpitch + (x - dx0) + dlead] : (int)D[(y - dy0) * G::DCOLS + (x - dx0)];
     };
 
     const int nh = G::NDR * (y1 - y0);
@@ -193,10 +253,11 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
                 if (packed) {
                     if constexpr (WIN == 5) {
                         // plain steps up to a word boundary of the byte rows
-                        // (x + HALF = 0 mod 4), then four columns per step
-                        constexpr int xs = HALF + 1 + ((4 - (2 * HALF + 1) % 4) & 3);
+                        // (x + HALF + row lead = 0 mod 4), then four columns per step
+                        const int xs = HALF + 1 + ((4 - ((2 * HALF + 1 + dlead) & 3)) & 3);
                         for (; x < xs; ++x) step(x);
-                        const uint8_t *ra_ = Db + (y - dy0) * G::DSB + HALF, *rb_ = Db + (y + dr - dy0) * G::DSB + HALF;
+                        const uint8_t *ra_ = Db + (y - dy0) * dpitch + dlead + HALF,
+                                      *rb_ = Db + (y + dr - dy0) * dpitch + dlead + HALF;
                         if (x + 4 <= xm1) {
                             uint32_t w0 = ld_word(rb_ + x);
                             for (; x + 4 <= xm1; x += 4) {
@@ -291,27 +352,40 @@ __global__ void __launch_bounds__(256) k_lr_stats(FrameDesc *frames, const WorkI
         int j = 0;
         if (packed) {
             if constexpr (WIN == 5) {
-                const uint8_t *rd = Db + (yy - dy0) * G::DSB;  // byte j + ca is d[yy][j + ca - HALF]
-                const uint8_t *rx = Xb + (i - xi0) * G::XSB;
+                const uint8_t *rd = Db + (yy - dy0) * dpitch + dlead;  // byte j + ca is d[yy][j + ca - HALF]
+                const uint8_t *rx = Xb + (i - xi0) * xpitch;
                 const int uw4 = uw & ~3;
-                uint32_t w0 = ld_word(rd);
-                for (; j < uw4; j += 4) {
-                    const uint32_t w1 = ld_word(rd + j + 4), xv = ld_word(rx + j);
-                    const uint32_t d2 = bytes_at<2>(w0, w1);
-                    acc[0] = (int)__dp4a(w0, xv, (uint32_t)acc[0]);
-                    acc[1] = (int)__dp4a(bytes_at<1>(w0, w1), xv, (uint32_t)acc[1]);
-                    acc[2] = (int)__dp4a(d2, xv, (uint32_t)acc[2]);
-                    acc[3] = (int)__dp4a(bytes_at<3>(w0, w1), xv, (uint32_t)acc[3]);
-                    acc[4] = (int)__dp4a(w1, xv, (uint32_t)acc[4]);
-                    c0 = __dp4a(w0, 0x01010101u, c0);
-                    if (centre) {
-                        sx = __dp4a(xv, 0x01010101u, sx);
-                        const uint32_t e = __vabsdiffu4(xv, d2);
-                        if (j >= jr) e_rgt = __dp4a(e, e, e_rgt);
-                        else e_in = __dp4a(e, e, e_in);
+                // four columns per step: the ca windows are bytes ca + sh .. ca + sh + 3
+                // of the aligned words from rd - sh (sh = 0 for thread-staged rows,
+                // 2 for the TMA rows whose column -2 sits at byte 14)
+                auto mwalk = [&](auto shc) {
+                    constexpr int SH = decltype(shc)::value;
+                    const uint8_t *ra = rd - SH;
+                    uint32_t w0 = ld_word(ra), w1 = ld_word(ra + 4);
+                    for (; j < uw4; j += 4) {
+                        const uint32_t w2 = ld_word(ra + j + 8), xv = ld_word(rx + j);
+                        const uint32_t e0 = bytes_at<SH>(w0, w1), e1 = bytes_at<SH + 1>(w0, w1);
+                        const uint32_t d2 = SH == 2 ? w1 : bytes_at<(SH + 2) & 3>(w0, w1);
+                        const uint32_t e3 = SH == 2 ? bytes_at<1>(w1, w2) : bytes_at<SH + 3>(w0, w1);
+                        const uint32_t e4 = SH == 2 ? bytes_at<2>(w1, w2) : w1;
+                        acc[0] = (int)__dp4a(e0, xv, (uint32_t)acc[0]);
+                        acc[1] = (int)__dp4a(e1, xv, (uint32_t)acc[1]);
+                        acc[2] = (int)__dp4a(d2, xv, (uint32_t)acc[2]);
+                        acc[3] = (int)__dp4a(e3, xv, (uint32_t)acc[3]);
+                        acc[4] = (int)__dp4a(e4, xv, (uint32_t)acc[4]);
+                        c0 = __dp4a(e0, 0x01010101u, c0);
+                        if (centre) {
+                            sx = __dp4a(xv, 0x01010101u, sx);
+                            const uint32_t e = __vabsdiffu4(xv, d2);
+                            if (j >= jr) e_rgt = __dp4a(e, e, e_rgt);
+                            else e_in = __dp4a(e, e, e_in);
+                        }
+                        w0 = w1;
+                        w1 = w2;
                     }
-                    w0 = w1;
-                }
+                };
+                if (dlead & 3) mwalk(std::integral_constant<int, 2>());
+                else mwalk(std::integral_constant<int, 0>());
                 for (; j < uw; ++j) {
                     const int xv = rx[j];
 #pragma unroll
