@@ -37,6 +37,16 @@ __device__ __forceinline__ int adjust_strength(int strength, int var) {
     return var != 0 ? (strength * (4 + i) + 8) >> 4 : 0;
 }
 
+// The search stores each block's variance as a code (0: var == 0, else
+// 1 + i with i the adjust_strength exponent) beside its direction; the
+// apply rebuilds the adjusted strength from it.
+__device__ __forceinline__ int var_code(int var) {
+    return var != 0 ? 1 + ((var >> 6) != 0 ? min(msb((unsigned)(var >> 6)), 12) : 0) : 0;
+}
+__device__ __forceinline__ int adjust_strength_code(int strength, int code) {
+    return code != 0 ? (strength * (3 + code) + 8) >> 4 : 0;
+}
+
 // cdef_find_dir (cdef.rs:143-198), split by direction pairs so that four
 // threads share one 8x8 block: pair 0 = directions (0, 4), 1 = (2, 6),
 // 2 = (1, 5), 3 = (3, 7). Each pass keeps at most 30 partial sums live.
@@ -296,8 +306,9 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
     __shared__ int bpri[64][FPM];  // adjusted primary strength | damping shift << 16
     __shared__ int blist[64];
     __shared__ int nblk;
-    __shared__ uint32_t part[8][NCM];
-    __shared__ unsigned long long uvtot[FPM];
+    __shared__ uint16_t regc[2][CRC * CRC];
+    __shared__ uint16_t srcc[2][32 * 32];
+    __shared__ uint32_t part[8][NCM + 2 * FPM];
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
     const FrameDesc &f = frames[wi.frame];
@@ -334,15 +345,23 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
         sec[j] = (s + (s == 3)) << cs;
         ssh[j] = damp_shift(sec[j], dmp);
     }
-    // ---- luma
+    // ---- every plane's window staged at once (luma, then U and V)
     const int x0 = fbc * 64, y0 = fbr * 64;
+    const int cw = f.w / 2, ch = f.h / 2, cx0 = fbc * 32, cy0 = fbr * 32;
     load_region(f.B[0], bd, f.w, f.h, x0, y0, 64, reg);
     load_src(f.S[0], bd, f.w, f.h, x0, y0, 64, src);
+    if (f.chroma)
+#pragma unroll 1
+        for (int p = 0; p < 2; ++p) {
+            load_region(f.B[p + 1], bd, cw, ch, cx0, cy0, 32, regc[p]);
+            load_src(f.S[p + 1], bd, cw, ch, cx0, cy0, 32, srcc[p]);
+        }
     __syncthreads();
     find_dirs(reg, CR, cs, blist, nblk, dcost, sdir, svar);
     for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
         const int b = blist[k];
         const int dir = sdir[b], var = svar[b];
+        if (f.cdir) f.cdir[(int64_t)fb * 64 + b] = (uint8_t)(dir | (var_code(var) << 3));
         dir_offsets(dir, CR, boff[b]);
         dir_offsets(dir, CRC, boffc[b]);
 #pragma unroll
@@ -412,70 +431,70 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) part[warp][c] = v;
     }
+    // ---- chroma: U and V accumulate into the joint row (first-pass
+    // strengths only: secondary 0, primary not adjusted, damping - 1)
+    if (f.chroma) {
+        const int cdmp = dmp - 1;
+        int csh[FPM];
+#pragma unroll
+        for (int i = 0; i < FPM; ++i) csh[i] = damp_shift(pri[i], cdmp);
+        const int cslots = nblk * 16;
+#pragma unroll 1
+        for (int p = 0; p < 2; ++p) {
+            uint32_t cacc[FPM];
+#pragma unroll
+            for (int i = 0; i < FPM; ++i) cacc[i] = 0;
+            for (int q = threadIdx.x; q < cslots; q += blockDim.x) {
+                const int k = q >> 4, b = blist[k];
+                const int py = (b >> 3) * 4 + ((q >> 2) & 3), px = (b & 7) * 4 + (q & 3);
+                const int pos = (py + 2) * CRC + px + 2;
+                const int x = (int16_t)regc[p][pos], sv = srcc[p][py * 32 + px];
+                int d[12], mx, mn;
+                load_taps_at(edge_uv, regc[p], pos, boffc[b], x, d, mx, mn);
+#pragma unroll
+                for (int i = 0; i < FPM; ++i) {
+                    if (i >= fp) continue;
+                    // primary 0 and secondary 0: every tap term is 0, the pixel is kept
+                    const int y = pri[i] ? cdef_round(x, prim_sum(d, pri[i], csh[i], cs), mn, mx) : x;
+                    const int e = sv - y;
+                    cacc[i] += (uint32_t)(e * e);
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < FPM; ++i) {
+                uint32_t v = cacc[i];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+                if (lane == 0) part[warp][NCM + p * FPM + i] = v;
+            }
+        }
+    }
     __syncthreads();
+    const int nw = (int)(blockDim.x >> 5);
     for (int c = threadIdx.x; c < NCM; c += blockDim.x) {
         const int i = c / NSM, j = c - i * NSM;
         if (i >= fp || j >= ns) continue;
         unsigned long long tot = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += part[w][c];
+        for (int w = 0; w < nw; ++w) tot += part[w][c];
         const int gi = j == 0 ? i : fp + i * (ns - 1) + (j - 1);
         row[gi] = (tot >> (2 * cs)) * (unsigned long long)sub;
     }
-    // ---- chroma: U then V accumulate into the joint row (first-pass
-    // strengths only: secondary 0, primary not adjusted, damping - 1)
-    if (!f.chroma) {
-        if (threadIdx.x == 0)
-            for (int gi = 0; gi < n_cand; ++gi) row[n_cand + gi] = 0;
-        return;
-    }
-    if (threadIdx.x < FPM) uvtot[threadIdx.x] = 0;
-    const int cdmp = dmp - 1;
-    int csh[FPM];
-#pragma unroll
-    for (int i = 0; i < FPM; ++i) csh[i] = damp_shift(pri[i], cdmp);
-    const int cw = f.w / 2, ch = f.h / 2, cx0 = fbc * 32, cy0 = fbr * 32;
-    for (int p = 1; p <= 2; ++p) {
-        __syncthreads();
-        load_region(f.B[p], bd, cw, ch, cx0, cy0, 32, reg);
-        load_src(f.S[p], bd, cw, ch, cx0, cy0, 32, src);
-        __syncthreads();
-        uint32_t cacc[FPM];
-#pragma unroll
-        for (int i = 0; i < FPM; ++i) cacc[i] = 0;
-        const int cslots = nblk * 16;
-        for (int q = threadIdx.x; q < cslots; q += blockDim.x) {
-            const int k = q >> 4, b = blist[k];
-            const int py = (b >> 3) * 4 + ((q >> 2) & 3), px = (b & 7) * 4 + (q & 3);
-            const int pos = (py + 2) * CRC + px + 2;
-            const int x = (int16_t)reg[pos], sv = src[py * 32 + px];
-            int d[12], mx, mn;
-            load_taps_at(edge_uv, reg, pos, boffc[b], x, d, mx, mn);
-#pragma unroll
-            for (int i = 0; i < FPM; ++i) {
-                if (i >= fp) continue;
-                // primary 0 and secondary 0: every tap term is 0, the pixel is kept
-                const int y = pri[i] ? cdef_round(x, prim_sum(d, pri[i], csh[i], cs), mn, mx) : x;
-                const int e = sv - y;
-                cacc[i] += (uint32_t)(e * e);
+    for (int gi = threadIdx.x; gi < n_cand; gi += blockDim.x) {
+        unsigned long long v = 0;
+        if (f.chroma) {
+            if (gi < fp) {
+                unsigned long long tu = 0, tv = 0;
+                for (int w = 0; w < nw; ++w) {
+                    tu += part[w][NCM + gi];
+                    tv += part[w][NCM + FPM + gi];
+                }
+                v = ((tu >> (2 * cs)) + (tv >> (2 * cs))) * (unsigned long long)cp.sub_uv;
+            } else {
+                v = 1040400ull * 64ull;
             }
         }
-#pragma unroll
-        for (int i = 0; i < FPM; ++i) {
-            uint32_t v = cacc[i];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if (lane == 0) part[warp][i] = v;
-        }
-        __syncthreads();
-        if (threadIdx.x < fp) {
-            unsigned long long tot = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += part[w][threadIdx.x];
-            uvtot[threadIdx.x] += (tot >> (2 * cs)) * (unsigned long long)cp.sub_uv;
-        }
+        row[n_cand + gi] = v;
     }
-    __syncthreads();
-    for (int gi = threadIdx.x; gi < n_cand; gi += blockDim.x)
-        row[n_cand + gi] = gi < fp ? uvtot[gi] : 1040400ull * 64ull;
 }
 
 // Launch the search instantiation covering fp x ns (the largest over the
@@ -1346,6 +1365,7 @@ int finish1_smem(int nfb, int ncand, int cap) {
 
 __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems) {
     __shared__ uint16_t reg[CR * CR];
+    __shared__ uint16_t regc[2][CRC * CRC];
     __shared__ int sdir[64], svar[64];
     __shared__ int dcost[64][8];
     __shared__ int boff[64][6], boffc[64][6];
@@ -1387,7 +1407,12 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     const int lvl_y = (ys / 4) << cs, sec_y = ((ys % 4) + ((ys % 4) == 3)) << cs;
     const int lvl_uv = (uvs / 4) << cs, sec_uv = ((uvs % 4) + ((uvs % 4) == 3)) << cs;
     const int damping = cp.damping + cs;
+    const int cw = f.w / 2, ch = f.h / 2, cx0 = x0 / 2, cy0 = y0 / 2;
+    // every plane's window staged at once (luma, then U and V)
     load_region(f.B[0], bd, f.w, f.h, x0, y0, 64, reg);
+    if (f.chroma)
+#pragma unroll 1
+        for (int p = 0; p < 2; ++p) load_region(f.B[p + 1], bd, cw, ch, cx0, cy0, 32, regc[p]);
     if (threadIdx.x == 0) {
         int n = 0;
         for (int b = 0; b < 64; ++b)
@@ -1395,12 +1420,23 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
         nblk = n;
     }
     __syncthreads();
-    find_dirs(reg, CR, cs, blist, nblk, dcost, sdir, svar);
+    // directions: from this call's search of the same B when it ran (a
+    // frame-uniform branch), else found here
+    const bool have_dirs = f.cdir_ok != 0;
+    if (!have_dirs) find_dirs(reg, CR, cs, blist, nblk, dcost, sdir, svar);
     for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
         const int b = blist[k];
-        dir_offsets(lvl_y ? sdir[b] : 0, CR, boff[b]);
-        dir_offsets(lvl_uv ? sdir[b] : 0, CRC, boffc[b]);
-        const int t = adjust_strength(lvl_y, svar[b]);
+        int dir, t;
+        if (have_dirs) {
+            const int c = f.cdir[(int64_t)fb * 64 + b];
+            dir = c & 7;
+            t = adjust_strength_code(lvl_y, c >> 3);
+        } else {
+            dir = sdir[b];
+            t = adjust_strength(lvl_y, svar[b]);
+        }
+        dir_offsets(lvl_y ? dir : 0, CR, boff[b]);
+        dir_offsets(lvl_uv ? dir : 0, CRC, boffc[b]);
         bt[b] = t | (damp_shift(t, damping) << 16);
     }
     __syncthreads();
@@ -1439,22 +1475,20 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     if (f.chroma) {
         const bool zero_uv = lvl_uv == 0 && sec_uv == 0;
         const int psh = damp_shift(lvl_uv, damping - 1), ssh = damp_shift(sec_uv, damping - 1);
-        const int cw = f.w / 2, ch = f.h / 2, cx0 = x0 / 2, cy0 = y0 / 2;
+#pragma unroll 1
         for (int p = 1; p <= 2; ++p) {
-            __syncthreads();
-            load_region(f.B[p], bd, cw, ch, cx0, cy0, 32, reg);
-            __syncthreads();
+            const uint16_t *rc = regc[p - 1];
             // a warp takes two horizontally adjacent 4x4 blocks
             for (int bp = warp; bp < 32; bp += nwarps) {
                 const int b = 2 * bp + (lane >> 4);
                 const int py = (b >> 3) * 4 + ((lane >> 2) & 3), px = (b & 7) * 4 + (lane & 3);
                 if (py >= vsize / 2 || px >= hsize / 2) continue;
                 const int pos = (py + 2) * CRC + px + 2;
-                const int x = (int16_t)reg[pos];
+                const int x = (int16_t)rc[pos];
                 int y = x;
                 if (!zero_uv && ((dl >> b) & 1)) {
                     int d[12], mx, mn;
-                    load_taps_at(edge_uv, reg, pos, boffc[b], x, d, mx, mn);
+                    load_taps_at(edge_uv, rc, pos, boffc[b], x, d, mx, mn);
                     int sum = 0;
                     if (lvl_uv) sum += prim_sum(d, lvl_uv, psh, cs);
                     if (sec_uv) sum += sec_sum(d, sec_uv, ssh);

@@ -116,11 +116,15 @@ struct FrameDesc {
     int *cdef_ids;          // 4 x nfb: compacted filter-block ids with rows (global fallback)
     uint32_t *cdef_rows32;  // 4 x nfb x 2 x ncand: compacted rows (global fallback)
     unsigned long long *cdef_stats;  // [filtered, changed, sb_count]
+    // nfb x 64: direction | variance code << 3 of every non-skip 8x8 luma
+    // block, written by the search (when not null) and read by the apply
+    // when cdir_ok
+    uint8_t *cdir;
     // joint strength search, one result per bit count 0..3 (zero on upload)
     unsigned long long fin_cost[4];
     uint8_t fin_lev[4][16];  // lev0[0..8) then lev1[0..8)
     int fin_done;            // clusters finished
-    int fin_pad;
+    int cdir_ok;             // this call's search wrote cdir from the apply's B
     // LR
     LrPlane lr[3];
     int64_t rdmult;

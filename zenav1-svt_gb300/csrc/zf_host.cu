@@ -342,7 +342,7 @@ struct Plan {
     int nfb = 0;
     size_t off_set[3][3];             // [set A/B/C][plane]
     size_t off_src[3];
-    size_t off_mi = 0, off_mse = 0, off_ids = 0, off_rows32 = 0;
+    size_t off_mi = 0, off_mse = 0, off_ids = 0, off_rows32 = 0, off_cdir = 0;
     // relative to the batch's units region (zeroed with one memset)
     size_t off_units[3];
     // relative to the rectangles part of the metadata region
@@ -442,6 +442,7 @@ void plan_frame(Plan &p, const zf_frame *f, size_t &cursor, size_t &ucur, size_t
     p.off_mse = take((size_t)p.nfb * 2 * zf::kMaxCand * 8);
     p.off_ids = take((size_t)zf::kFinLevels * p.nfb * 4);
     p.off_rows32 = take((size_t)zf::kFinLevels * p.nfb * 2 * zf::kMaxCand * 4);
+    p.off_cdir = take((size_t)p.nfb * 64);
     p.off_fbrow = take_in(ocur, p.nfb);
     p.off_fbidx = take_in(ocur, p.nfb);
     p.off_stats = take_in(ocur, 4 * 8);
@@ -492,6 +493,7 @@ void bind_pointers(Plan &p, uint8_t *base, uint8_t *units, uint8_t *rects, uint8
     d.fb_idx = out + p.off_fbidx;
     d.cdef_ids = (int *)(base + p.off_ids);
     d.cdef_rows32 = (uint32_t *)(base + p.off_rows32);
+    d.cdir = base + p.off_cdir;
     d.cdef_stats = (unsigned long long *)(out + p.off_stats);
 }
 
@@ -890,6 +892,10 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         // decisions; the apply then recomputes only the rows next to
         // interior stripe boundaries of Wiener units.
         const bool trial_out = (run.stages & STG_LR_SEARCH) && !run.lr_given && (run.stages & STG_LR_APPLY);
+        // The CDEF apply takes the luma directions from the search when the
+        // same call searches this frame (both read the same B).
+        p.d.cdir_ok = (run.stages & STG_CDEF_SEARCH) && (run.stages & STG_CDEF_APPLY) && !run.cdef_given &&
+                      p.d.cdef.mode == 1;
         for (int pl = 0; pl < 3; ++pl) {
             LrPlane &L = p.d.lr[pl];
             L.trial_out = trial_out && L.on && !L.refine ? 1 : 0;
