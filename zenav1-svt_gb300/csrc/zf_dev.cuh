@@ -79,6 +79,9 @@ struct LrPlane {
 constexpr int kTmaDBoxW = 104, kTmaDBoxH = 26, kTmaXBoxW = 96, kTmaXBoxH = 18;
 constexpr int kTmaDLead = 14;  // byte of column -2 (the window's first) in a D row
 
+// Restoration apply: 64-px column tiles of a stripe per CTA.
+constexpr int kApplyGroup = 8;
+
 // CDEF joint strength search: bit counts 0..3, one cluster each.
 constexpr int kFinLevels = 4;
 

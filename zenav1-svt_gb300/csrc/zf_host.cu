@@ -781,20 +781,21 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             const LrPlane &L = p.d.lr[pl];
             const int ss = pl ? 1 : 0, full = 64 >> ss, off = 8 >> ss;
             const int nstripes = (L.ph + off + full - 1) / full;
-            const int ntiles = (L.stride + 63) / 64;
+            const int ngroups = ((L.stride + 63) / 64 + zf::kApplyGroup - 1) / zf::kApplyGroup;
             const int canvas_h = pl ? p.d.h / 2 : p.d.h;
-            // one item per stripe (CTA offset = 64-px column tile); a = the
-            // stripe's row of the row-major hunits x vunits unit grid (-1:
-            // copy only), the kernel finds the column along that row
+            // one item per stripe (CTA offset = group of kApplyGroup
+            // 64-px column tiles); a = the stripe's row of the row-major
+            // hunits x vunits unit grid (-1: copy only), the kernel finds the
+            // column along that row
             const std::vector<UnitRect> &R = p.rects[pl];
             const int hu = p.hunits[pl], vu = p.vunits[pl];
             for (int s = 0, r = 0; s < nstripes; ++s) {
                 const int ys = std::max(0, s * full - off);
                 while (r < vu && ys >= R[(size_t)r * hu].v_end) ++r;
                 const bool row_ok = r < vu && ys >= R[(size_t)r * hu].v_start;
-                wl_apply.add(i, pl, (L.on && row_ok) ? r : -1, s, ntiles);
+                wl_apply.add(i, pl, (L.on && row_ok) ? r : -1, s, ngroups);
             }
-            if (canvas_h > L.ph) wl_apply.add(i, pl, -1, nstripes, ntiles);
+            if (canvas_h > L.ph) wl_apply.add(i, pl, -1, nstripes, ngroups);
         }
     }
     // finish frame ids: the joint groups in order, then the small frames,

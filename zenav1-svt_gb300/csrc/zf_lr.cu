@@ -1131,29 +1131,37 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         bd, pl.pw, th, x0, tw, true, 0, [&](int rr) { return row_ptr(sr, y0 + rr, stride, bd); },
         [&](int rr, int cc, int v) { srct[rr * TL + cc] = (uint16_t)v; });
     __syncthreads();
+    const bool t5 = hf[0] == 0 && vf[0] == 0;  // uniform over the CTA
     // The solver's taps are symmetric (f[6 - k] = f[k], f[7] = 0), so each
     // pass is 4 multiplies per output on pair sums, the centre tap carrying
     // the 128 of wiener_convolve_add_src; a thread takes four outputs along
     // the pass from 11 staged samples.
     // horizontal: every staged row x 16 runs of four columns
     {
+        // T5: the 5-tap window's outer taps are 0 (finalize_sym), so the
+        // four outputs need samples 1..8 of the 11 and no outer pair
         const int c3 = 128 + hf[3], off = 1 << (bd + 6), lim = (1 << (bd + 5)) - 1;
-        for (int q = threadIdx.x; q < rows * (TL / 4); q += blockDim.x) {
-            const int rr = q >> 4, c0 = (q & 15) * 4;
-            if (c0 >= tw) continue;
-            const uint16_t *sp = stage + rr * SW + c0;
-            int p[11];
+        auto hpass = [&](auto t5c) {
+            constexpr bool T5 = decltype(t5c)::value;
+            for (int q = threadIdx.x; q < rows * (TL / 4); q += blockDim.x) {
+                const int rr = q >> 4, c0 = (q & 15) * 4;
+                if (c0 >= tw) continue;
+                const uint16_t *sp = stage + rr * SW + c0;
+                int p[11];
 #pragma unroll
-            for (int k = 0; k < 11; ++k) p[k] = sp[k];
-            uint32_t o[4];
+                for (int k = T5 ? 1 : 0; k < (T5 ? 9 : 11); ++k) p[k] = sp[k];
+                uint32_t o[4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int sum = p[j + 3] * c3 + hf[0] * (p[j] + p[j + 6]) + hf[1] * (p[j + 1] + p[j + 5]) +
-                                hf[2] * (p[j + 2] + p[j + 4]) + off;
-                o[j] = (uint32_t)clampi((sum + 4) >> 3, 0, lim);
+                for (int j = 0; j < 4; ++j) {
+                    int sum = p[j + 3] * c3 + hf[1] * (p[j + 1] + p[j + 5]) + hf[2] * (p[j + 2] + p[j + 4]) + off;
+                    if (!T5) sum += hf[0] * (p[j] + p[j + 6]);
+                    o[j] = (uint32_t)clampi((sum + 4) >> 3, 0, lim);
+                }
+                *reinterpret_cast<uint2 *>(tmp + rr * TL + c0) = make_uint2(o[0] | o[1] << 16, o[2] | o[3] << 16);
             }
-            *reinterpret_cast<uint2 *>(tmp + rr * TL + c0) = make_uint2(o[0] | o[1] << 16, o[2] | o[3] << 16);
-        }
+        };
+        if (t5) hpass(std::true_type());
+        else hpass(std::false_type());
     }
     __syncthreads();
     const int c3 = 128 + vf[3], voff = -(1 << (bd + 10)), vmax = (1 << bd) - 1;
@@ -1167,28 +1175,43 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         for (int e = 0; e < kTileEdges; ++e) hit |= y >= eb[e] - 3 && y < eb[e] + 3;
         return hit;
     };
-    // vertical: runs of four rows x 64 columns, SSE parts, trial output
-    unsigned long long blk = 0, rgt = 0, bot = 0;
-    for (int q = threadIdx.x; q < ((th + 3) >> 2) * TL; q += blockDim.x) {
-        const int r0 = (q >> 6) * 4, cc = q & (TL - 1);
-        if (cc >= tw) continue;
-        int p[11];
+    // vertical: runs of four rows x 64 columns, SSE parts, trial output.
+    // A thread takes at most 16 pixels of a tile, each e^2 <= 1023^2, so
+    // its SSE parts fit u32.
+    uint32_t blk32 = 0, rgt32 = 0, bot32 = 0;
+    auto vpass = [&](auto t5c) {
+        constexpr bool T5 = decltype(t5c)::value;
+        for (int q = threadIdx.x; q < ((th + 3) >> 2) * TL; q += blockDim.x) {
+            const int r0 = (q >> 6) * 4, cc = q & (TL - 1);
+            if (cc >= tw) continue;
+            int p[11];
 #pragma unroll
-        for (int k = 0; k < 11; ++k) p[k] = tmp[(r0 + k) * TL + cc];
-        const int j = tx + cc;
+            for (int k = T5 ? 1 : 0; k < (T5 ? 9 : 11); ++k) p[k] = tmp[(r0 + k) * TL + cc];
+            const bool right = tx + cc >= uw - dw;
 #pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-            const int rr = r0 + jj;
-            if (rr >= th) break;
-            const int y = vert(p + jj);
-            if (tout && !edge_row(y0 + rr)) stpx(outp, (int64_t)(y0 + rr) * stride + x0 + cc, bd, y);
-            const int e = (int)srct[rr * TL + cc] - y;
-            const unsigned long long e2 = (unsigned long long)((long long)e * e);
-            if (j >= uw - dw) rgt += e2;
-            else if (ty + rr >= uh - dh) bot += e2;
-            else blk += e2;
+            for (int jj = 0; jj < 4; ++jj) {
+                const int rr = r0 + jj;
+                if (rr >= th) break;
+                int y;
+                if (T5) {
+                    const int *pp = p + jj;
+                    const int sum = pp[3] * c3 + vf[1] * (pp[1] + pp[5]) + vf[2] * (pp[2] + pp[4]) + voff;
+                    y = clampi((sum + (1 << 10)) >> 11, 0, vmax);
+                } else {
+                    y = vert(p + jj);
+                }
+                if (tout && !edge_row(y0 + rr)) stpx(outp, (int64_t)(y0 + rr) * stride + x0 + cc, bd, y);
+                const int e = (int)srct[rr * TL + cc] - y;
+                const uint32_t e2 = (uint32_t)(e * e);
+                if (right) rgt32 += e2;
+                else if (ty + rr >= uh - dh) bot32 += e2;
+                else blk32 += e2;
+            }
         }
-    }
+    };
+    if (t5) vpass(std::true_type());
+    else vpass(std::false_type());
+    unsigned long long blk = blk32, rgt = rgt32, bot = bot32;
     // the apply's rows at the stripe edges: tmp rows of A (index y - y0 + 3)
     // or of the edge's B rows (index na + 4 e + k)
     for (int q = threadIdx.x; q < ne * 6 * TL; q += blockDim.x) {
@@ -1542,39 +1565,45 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
 // ---------------------------------------------------------------------------
 // 5. Apply (apply_restoration_frame, restoration.rs:992-1052) with the
 // stripe boundaries of save_lr_boundaries, writing every pixel of C: one CTA
-// per (plane, stripe, 64-px column tile) over the aligned canvas. Tiles of
-// Wiener units are filtered within the true plane and copied from A beyond
-// it; every other tile (unit NONE, frame NONE, plane not searched, and the
-// rows below the true plane: stripe index nstripes) is copied from A. Rows
-// above / below a stripe come from the post-deblock (pre-CDEF) plane B at
-// interior stripe edges (the only lines the single-tile apply reads) and
-// from the edge-replicated post-CDEF plane at the frame top / bottom.
-// items: a = unit index (-1: copy only), b = stripe << 16 | column tile.
+// per (plane, stripe, group of kApplyGroup 64-px column tiles) over the
+// aligned canvas. Tiles of Wiener units are filtered within the true plane
+// and copied from A beyond it; every other tile (unit NONE, frame NONE,
+// plane not searched, and the rows below the true plane: stripe index
+// nstripes) is copied from A. Rows above / below a stripe come from the
+// post-deblock (pre-CDEF) plane B at interior stripe edges (the only lines
+// the single-tile apply reads) and from the edge-replicated post-CDEF plane
+// at the frame top / bottom. items: a = unit row (-1: copy only), b = stripe.
+// A CTA looks its tiles' units up at once and copies every copied part
+// before it filters (planes the tiled trial did not write), so a copy-only
+// group pays one barrier.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems) {
     constexpr int SW = TT_W + 7;
     constexpr int MAXH = 64 + 7;
     __shared__ __align__(16) uint16_t stage[MAXH * SW];
     __shared__ __align__(16) uint16_t tmp[MAXH * TT_W];
+    __shared__ int s_unit[kApplyGroup], s_filter[kApplyGroup];
     const WorkItem wi = items[find_item(items, nitems, blockIdx.x)];
     const FrameDesc &f = frames[wi.frame];
     const LrPlane &pl = f.lr[wi.plane];
     const int ss = wi.plane ? 1 : 0;
     const int full = 64 >> ss, off = 8 >> ss;
-    const int s = wi.b, ct = blockIdx.x - wi.cta_begin;
+    const int s = wi.b;
     const int bd = f.bd, stride = plane_stride(f, wi.plane);
     const int canvas_h = wi.plane ? f.h / 2 : f.h;
     const int nstripes = (pl.ph + off + full - 1) / full;
     // rows of this item: a stripe of the true plane, or the canvas rows below it
     const int ys = s < nstripes ? max(0, s * full - off) : pl.ph;
     const int ye = s < nstripes ? min(pl.ph, (s + 1) * full - off) : canvas_h;
-    const int x0 = ct * TT_W, tw = min(TT_W, stride - x0);
+    const int ntiles = (stride + TT_W - 1) / TT_W;
+    const int g0 = (blockIdx.x - wi.cta_begin) * kApplyGroup;
+    const int ntl = min(kApplyGroup, ntiles - g0);
     const uint8_t *post = f.A[wi.plane], *pre = f.B[wi.plane];
     uint8_t *out = f.C[wi.plane];
-    // the unit of this tile: wi.a is its row of the unit grid (-1: copy only),
-    // the column is looked up along that row
-    __shared__ int s_unit, s_filter;
-    if (threadIdx.x == 0) {
+    // the unit of each tile: wi.a is its row of the unit grid (-1: copy
+    // only), the column is looked up along that row, one thread per tile
+    if ((int)threadIdx.x < ntl) {
+        const int x0 = (g0 + (int)threadIdx.x) * TT_W;
         int unit = -1;
         if (wi.a >= 0 && pl.on) {
             const UnitRect *urow = pl.rects + wi.a * pl.hunits;
@@ -1584,41 +1613,49 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
                     break;
                 }
         }
-        s_unit = unit;
-        s_filter = s < nstripes && unit >= 0 && pl.frame_rtype != 0 && pl.units[unit].rtype == 1;
+        s_unit[threadIdx.x] = unit;
+        s_filter[threadIdx.x] = s < nstripes && unit >= 0 && pl.frame_rtype != 0 && pl.units[unit].rtype == 1;
     }
     __syncthreads();
-    const int unit = s_unit;
-    const bool filter = s_filter != 0;
-    // columns copied from A: all of them, or those beyond the true width
-    const int cx = filter ? min(tw, pl.pw - x0) : 0;
-    const int spw = word_samples(bd), nwr = tw / spw;  // tw is a multiple of 4 (plane widths are)
-    if (cx == 0 && aligned4(post) && aligned4(out)) {  // whole tile: word copies
-        for (int q = threadIdx.x; q < (ye - ys) * nwr; q += blockDim.x) {
-            const int rr = q / nwr, wx = q - rr * nwr;
-            const int64_t o = ((int64_t)(ys + rr) * stride + x0) * (bd == 8 ? 1 : 2) + wx * 4;
-            *reinterpret_cast<uint32_t *>(out + o) = *reinterpret_cast<const uint32_t *>(post + o);
-        }
-    } else if (cx < tw) {
-        for (int q = threadIdx.x; q < (ye - ys) * (tw - cx); q += blockDim.x) {
-            const int rr = q / (tw - cx), cc = cx + (q - rr * (tw - cx));
-            const int64_t o = (int64_t)(ys + rr) * stride + x0 + cc;
-            stpx(out, o, bd, ldpx(post, o, bd));
+    const int spw = word_samples(bd);
+    const bool words = aligned4(post) && aligned4(out);
+    // copied columns of each tile: all of them, or those beyond the true width
+    for (int k = 0; k < ntl; ++k) {
+        const int x0 = (g0 + k) * TT_W, tw = min(TT_W, stride - x0);
+        const int cx = s_filter[k] ? min(tw, pl.pw - x0) : 0;
+        if (cx == 0 && words) {  // whole tile: word copies (tw is a multiple of 4, as plane widths are)
+            const int nwr = tw / spw;
+            for (int q = threadIdx.x; q < (ye - ys) * nwr; q += blockDim.x) {
+                const int rr = q / nwr, wx = q - rr * nwr;
+                const int64_t o = ((int64_t)(ys + rr) * stride + x0) * (bd == 8 ? 1 : 2) + wx * 4;
+                *reinterpret_cast<uint32_t *>(out + o) = *reinterpret_cast<const uint32_t *>(post + o);
+            }
+        } else if (cx < tw) {
+            for (int q = threadIdx.x; q < (ye - ys) * (tw - cx); q += blockDim.x) {
+                const int rr = q / (tw - cx), cc = cx + (q - rr * (tw - cx));
+                const int64_t o = (int64_t)(ys + rr) * stride + x0 + cc;
+                stpx(out, o, bd, ldpx(post, o, bd));
+            }
         }
     }
-    if (!filter) return;
-    const LrUnit &u = pl.units[unit];
-    int16_t hf[8], vf[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        hf[k] = u.hf[k];
-        vf[k] = u.vf[k];
-    }
-    const int ncol = cx;
+    // a tiled-trial plane: the trial wrote its units' final pixels
+    if (pl.trial_out) return;
     const bool copy_above = s > 0, copy_below = ye < pl.ph;
-    // Output rows [rb, re) of the stripe: stage rows rb - 3 .. re + 3 with
-    // the stripe's boundary substitution, horizontal pass, vertical pass.
-    auto filter_rows = [&](int rb, int re) {
+    for (int k = 0; k < ntl; ++k) {
+        if (!s_filter[k]) continue;  // uniform over the CTA
+        const int x0 = (g0 + k) * TT_W, tw = min(TT_W, stride - x0);
+        const int ncol = min(tw, pl.pw - x0);
+        const LrUnit &u = pl.units[s_unit[k]];
+        int16_t hf[8], vf[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            hf[j] = u.hf[j];
+            vf[j] = u.vf[j];
+        }
+        // Output rows [rb, re) of the stripe: stage rows rb - 3 .. re + 3
+        // with the stripe's boundary substitution, horizontal pass, vertical
+        // pass.
+        const int rb = ys, re = ye;
         const int nrow = re - rb, rows = nrow + 7;
         auto row_of = [&](int rr) {
             const int y = rb - 3 + rr;
@@ -1643,7 +1680,7 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
             }
             return row_ptr(src, yy, stride, bd);
         };
-        __syncthreads();  // the previous band's reads of stage / tmp are done
+        __syncthreads();  // the previous tile's reads of stage / tmp are done
         stage_window(bd, pl.pw, rows, x0 - 3, SW, true, 0, row_of,
                      [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
         __syncthreads();
@@ -1652,7 +1689,7 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
             const int rr = q >> 4, c0 = (q & 15) * 4;
             int p[11];
 #pragma unroll
-            for (int k = 0; k < 11; ++k) p[k] = stage[rr * SW + c0 + k];
+            for (int j = 0; j < 11; ++j) p[j] = stage[rr * SW + c0 + j];
             uint32_t o[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) o[j] = (uint32_t)wiener_h(p + j, hf, bd);
@@ -1664,16 +1701,14 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
             if (cc >= ncol) continue;
             int p[11];
 #pragma unroll
-            for (int k = 0; k < 11; ++k) p[k] = tmp[(r0 + k) * TT_W + cc];
+            for (int j = 0; j < 11; ++j) p[j] = tmp[(r0 + j) * TT_W + cc];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 if (r0 + j >= nrow) break;
                 stpx(out, (int64_t)(rb + r0 + j) * stride + x0 + cc, bd, wiener_v(p + j, vf, bd));
             }
         }
-    };
-    // a tiled-trial plane: the trial wrote this unit's final pixels
-    if (!pl.trial_out) filter_rows(ys, ye);
+    }
 }
 
 }  // namespace zf
