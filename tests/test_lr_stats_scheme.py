@@ -1,12 +1,12 @@
 """The thread decomposition of k_lr_stats (zenav1-svt_gb300/csrc/zf_lr.cu),
-emulated on the CPU: CTAs of 256 / (3 win - 1) rows over the unit's rows
+emulated on the CPU: CTAs of 256 / (3 win) rows over the unit's rows
 extended by win/2; one thread per (row, row offset dr) building the row sums
 of d[y][x] * d[y+dr][x+dc] over every shifted column window from a running
 prefix (head and tail steps at the window starts and ends, the middle in
 plain steps or, for 8-bit rows with the 5-tap window, in four-column
-groups on word boundaries); one thread per (unit row, window row) for M,
-the window shift sums (a sliding column window) and, for the centre window
-row, the source sum and the three sse_region parts. The statistics are sums
+groups on word boundaries); one thread per (unit row, window row) for M and
+the window shift sums (a sliding column window); one thread per unit row
+for the source sum and the three sse_region parts. The statistics are sums
 of raw samples; the solve's average correction
     H = Hr - A (S_a + S_b) + n A^2,   M = Mr - A (S_a + sum s) + n A^2
 is applied here as k_lr_solve does. Checked against the direct definition
@@ -42,7 +42,7 @@ def emu(dfull, s, uw, uh, WIN, off, packed):
     HALF = WIN // 2
     W2 = WIN * WIN
     NDR = 2 * WIN - 1
-    ROWS = 256 // (NDR + WIN)
+    ROWS = 256 // (NDR + WIN + 1)
     H = np.zeros(W2 * W2, np.int64)
     M = np.zeros(W2, np.int64)
     S = np.zeros(W2, np.int64)
@@ -52,7 +52,7 @@ def emu(dfull, s, uw, uh, WIN, off, packed):
         y1 = min(uh + HALF, y0 + ROWS)
         xi0, xi1 = max(y0, 0), min(y1, uh)
         nh = NDR * (y1 - y0)
-        assert nh + WIN * (xi1 - xi0) <= 256
+        assert nh + (WIN + 1) * (xi1 - xi0) <= 256
         for t in range(nh):
             dr = t % NDR - (WIN - 1)
             y = y0 + t // NDR
@@ -137,22 +137,13 @@ def emu(dfull, s, uw, uh, WIN, off, packed):
             ra = q % WIN
             i = xi0 + q // WIN
             yy = i + ra - HALF
-            centre = ra == HALF
-            jr = uw - uw % 16
             acc = [0] * WIN
-            c0 = sx = e_in = e_rgt = 0
+            c0 = 0
             for j in range(uw):
                 xv = int(s[i, j])
                 for ca in range(WIN):
                     acc[ca] += Dat(yy, j + ca - HALF) * xv
                 c0 += Dat(yy, j - HALF)
-                if centre:
-                    e = xv - Dat(yy, j)
-                    sx += xv
-                    if j >= jr:
-                        e_rgt += e * e
-                    else:
-                        e_in += e * e
             for ca in range(WIN):
                 M[ca * WIN + ra] += acc[ca]
             cw = c0
@@ -160,10 +151,33 @@ def emu(dfull, s, uw, uh, WIN, off, packed):
             for ca in range(1, WIN):  # the column windows slide
                 cw = cw - Dat(yy, ca - 1 - HALF) + Dat(yy, ca - 1 - HALF + uw)
                 S[ca * WIN + ra] += cw
-            if centre:
-                E[0] += sx
-                E[3 if i >= uh - uh % 16 else 1] += e_in
-                E[2] += e_rgt
+        for i in range(xi0, xi1):  # sum s and the sse parts of unit row i
+            jr = uw - uw % 16
+            sx = e_in = e_rgt = 0
+            j = 0
+            if packed:  # four columns per step, then single columns
+                while j + 4 <= uw:
+                    for k in range(4):
+                        xv = int(s[i, j + k])
+                        e = xv - Dat(i, j + k)
+                        sx += xv
+                        if j >= jr:  # j and jr are multiples of 4
+                            e_rgt += e * e
+                        else:
+                            e_in += e * e
+                    j += 4
+            while j < uw:
+                xv = int(s[i, j])
+                e = xv - Dat(i, j)
+                sx += xv
+                if j >= jr:
+                    e_rgt += e * e
+                else:
+                    e_in += e * e
+                j += 1
+            E[0] += sx
+            E[3 if i >= uh - uh % 16 else 1] += e_in
+            E[2] += e_rgt
     # k_lr_solve's correction
     n = uw * uh
     ctr = HALF * WIN + HALF

@@ -54,8 +54,9 @@ int describe_cdef_frame(const zf_frame *f, FrameDesc *d);
 constexpr int kFinClusterHost = 8;  // k_cdef_finish: CTAs per cluster
 constexpr int kFinThreadsHost = 512;
 // k_lr_stats<win>: rows per CTA over the unit's rows extended by win/2 on
-// both sides (one thread per (row, row offset) plus one per (row, window row))
-constexpr int stat_rows_host(int win) { return 256 / (3 * win - 1); }
+// both sides (one thread per (row, row offset), one per (row, window row)
+// and one per row)
+constexpr int stat_rows_host(int win) { return 256 / (3 * win); }
 
 // ---- self-guided restoration (zf_sgr.cu) ----------------------------------
 constexpr int kSgrTileWHost = 64, kSgrTileHHost = 32;  // tile (columns x rows)

@@ -65,11 +65,13 @@ __device__ __forceinline__ int plane_stride(const FrameDesc &f, int p) { return 
 // dc (the partner row's bytes for dc = 1..3 are byte permutes of two
 // aligned words).
 //
-// A CTA covers kLrRows(WIN) consecutive rows of the unit's vertical range
-// extended by h = WIN/2 on both sides (items: a = unit, CTA offset = row
-// block). Threads [0, NDR * rows) walk (row, dr) for Hr; the next WIN * (unit
-// rows) walk (unit row i, ra) for Mr, the shift sums of row i + ra - h and,
-// for ra = h, sum s and the sse parts of row i.
+// A CTA covers ROWS consecutive rows of the unit's vertical range extended
+// by h = WIN/2 on both sides (items: a = unit, CTA offset = row block).
+// Threads [0, NDR * rows) walk (row, dr) for Hr; the next WIN * (unit rows)
+// walk (unit row i, ra) for Mr and the shift sums of row i + ra - h; the
+// next (unit rows) take sum s and the sse parts of row i. The three kinds of
+// walk take about the same time, so no warp waits long at the barrier after
+// them (the sse work inside the Mr walks made those warps the slowest).
 // ---------------------------------------------------------------------------
 constexpr int kMaxUnitW = 384 + 8;
 
@@ -77,7 +79,7 @@ template <int WIN>
 struct StatGeom {
     static constexpr int H = WIN / 2;
     static constexpr int NDR = 2 * WIN - 1;             // dr in [-(WIN-1), WIN-1]
-    static constexpr int ROWS = 256 / (NDR + WIN);      // rows per CTA (stat_rows_host)
+    static constexpr int ROWS = 256 / (NDR + WIN + 1);  // rows per CTA (stat_rows_host)
     static constexpr int DROWS = ROWS + 2 * (WIN - 1);  // staged D rows
     static constexpr int DCOLS = kMaxUnitW + 2 * H + WIN;
     static constexpr int DSB = (DCOLS + 3) / 4 * 4;     // byte layout: row stride (a multiple of 4)
@@ -338,17 +340,15 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
             }
         }
     } else if (t < nh + WIN * (xi1 - xi0)) {
-        // ---- Mr, shift sums, sum s and sse: one (unit row i, ra) per thread
+        // ---- Mr and shift sums: one (unit row i, ra) per thread
         const int q = t - nh;
         const int ra = q % WIN, i = xi0 + q / WIN;
         const int yy = i + ra - HALF;
-        const bool centre = ra == HALF;
-        const int jr = uw - uw % 16;  // the right strip of sse_region
         int acc[WIN];  // Mr[ca][ra] row parts
 #pragma unroll
         for (int k = 0; k < WIN; ++k) acc[k] = 0;
         // c0 = sum of d[yy][j - HALF], j in [0, uw) (the ca = 0 column window)
-        unsigned c0 = 0, sx = 0, e_in = 0, e_rgt = 0;
+        unsigned c0 = 0;
         int j = 0;
         if (packed) {
             if constexpr (WIN == 5) {
@@ -374,12 +374,6 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                         acc[3] = (int)__dp4a(e3, xv, (uint32_t)acc[3]);
                         acc[4] = (int)__dp4a(e4, xv, (uint32_t)acc[4]);
                         c0 = __dp4a(e0, 0x01010101u, c0);
-                        if (centre) {
-                            sx = __dp4a(xv, 0x01010101u, sx);
-                            const uint32_t e = __vabsdiffu4(xv, d2);
-                            if (j >= jr) e_rgt = __dp4a(e, e, e_rgt);
-                            else e_in = __dp4a(e, e, e_in);
-                        }
                         w0 = w1;
                         w1 = w2;
                     }
@@ -391,12 +385,6 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
 #pragma unroll
                     for (int ca = 0; ca < WIN; ++ca) acc[ca] += (int)rd[j + ca] * xv;
                     c0 += rd[j];
-                    if (centre) {
-                        const int e = xv - (int)rd[j + HALF];
-                        sx += xv;
-                        if (j >= jr) e_rgt += e * e;
-                        else e_in += e * e;
-                    }
                 }
             }
         } else {
@@ -417,12 +405,6 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
 #pragma unroll
                         for (int ca = 0; ca < WIN; ++ca) acc[ca] += w[(u + ca) % WIN] * xv;
                         c0 += w[u % WIN];
-                        if (centre) {
-                            const int e = xv - w[(u + HALF) % WIN];
-                            sx += xv;
-                            if (j + u >= jr) e_rgt += e * e;
-                            else e_in += e * e;
-                        }
                     }
                 }
 #pragma unroll
@@ -436,12 +418,6 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
 #pragma unroll
                 for (int ca = 0; ca < WIN; ++ca) acc[ca] += win[ca] * xv;
                 c0 += win[0];
-                if (centre) {
-                    const int e = xv - win[HALF];
-                    sx += xv;
-                    if (j >= jr) e_rgt += e * e;
-                    else e_in += e * e;
-                }
             }
         }
 #pragma unroll
@@ -454,11 +430,55 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
             cw = cw - (unsigned)Dat(yy, ca - 1 - HALF) + (unsigned)Dat(yy, ca - 1 - HALF + uw);
             atomicAdd(&Ss[ca * WIN + ra], cw);
         }
-        if (centre) {
-            atomicAdd(&Es[0], (unsigned long long)sx);
-            atomicAdd(&Es[i >= uh - uh % 16 ? 3 : 1], (unsigned long long)e_in);
-            atomicAdd(&Es[2], (unsigned long long)e_rgt);
+    } else if (t < nh + (WIN + 1) * (xi1 - xi0)) {
+        // ---- sum s and the sse_region parts of unit row i: one row per
+        // thread (d row i against the source row)
+        const int i = xi0 + (t - nh - WIN * (xi1 - xi0));
+        const int jr = uw - uw % 16;  // the right strip of sse_region
+        unsigned sx = 0, e_in = 0, e_rgt = 0;
+        int j = 0;
+        if (packed) {
+            const uint8_t *rd = Db + (i - dy0) * dpitch + dlead + HALF;  // byte j is d[i][j]
+            const uint8_t *rx = Xb + (i - xi0) * xpitch;
+            const int uw4 = uw & ~3;
+            // four columns per step (j and jr are multiples of 4, so a step
+            // lies on one side of the right strip); d words start on a word
+            // boundary for the TMA rows, two bytes into one otherwise
+            auto ewalk = [&](uint32_t xv, uint32_t dv) {
+                sx = __dp4a(xv, 0x01010101u, sx);
+                const uint32_t e = __vabsdiffu4(xv, dv);
+                if (j >= jr) e_rgt = __dp4a(e, e, e_rgt);
+                else e_in = __dp4a(e, e, e_in);
+            };
+            if (((dlead + HALF) & 3) == 0) {
+                for (; j < uw4; j += 4) ewalk(ld_word(rx + j), ld_word(rd + j));
+            } else {
+                const uint8_t *ra = rd - 2;
+                uint32_t w0 = ld_word(ra);
+                for (; j < uw4; j += 4) {
+                    const uint32_t w1 = ld_word(ra + j + 4);
+                    ewalk(ld_word(rx + j), bytes_at<2>(w0, w1));
+                    w0 = w1;
+                }
+            }
+            for (; j < uw; ++j) {
+                const int xv = rx[j], e = xv - (int)rd[j];
+                sx += xv;
+                if (j >= jr) e_rgt += e * e;
+                else e_in += e * e;
+            }
+        } else {
+            const int16_t *xr = X + (i - xi0) * kMaxUnitW;
+            for (; j < uw; ++j) {
+                const int xv = xr[j], e = xv - Dat(i, j);
+                sx += xv;
+                if (j >= jr) e_rgt += e * e;
+                else e_in += e * e;
+            }
         }
+        atomicAdd(&Es[0], (unsigned long long)sx);
+        atomicAdd(&Es[i >= uh - uh % 16 ? 3 : 1], (unsigned long long)e_in);
+        atomicAdd(&Es[2], (unsigned long long)e_rgt);
     }
     __syncthreads();
     // Interior rows: the row sums of each (dr, dc, ca) are added over the
