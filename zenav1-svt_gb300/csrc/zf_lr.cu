@@ -262,6 +262,9 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                                       *rb_ = Db + (y + dr - dy0) * dpitch + dlead + HALF;
                         if (x + 4 <= xm1) {
                             uint32_t w0 = ld_word(rb_ + x);
+                            // two steps per iteration: the next step's loads
+                            // issue before this step's products need theirs
+#pragma unroll 2
                             for (; x + 4 <= xm1; x += 4) {
                                 const uint32_t a4 = ld_word(ra_ + x), w1 = ld_word(rb_ + x + 4);
                                 pre[0] = (int)__dp4a(a4, w0, (uint32_t)pre[0]);
@@ -362,6 +365,7 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                     constexpr int SH = decltype(shc)::value;
                     const uint8_t *ra = rd - SH;
                     uint32_t w0 = ld_word(ra), w1 = ld_word(ra + 4);
+#pragma unroll 2
                     for (; j < uw4; j += 4) {
                         const uint32_t w2 = ld_word(ra + j + 8), xv = ld_word(rx + j);
                         const uint32_t e0 = bytes_at<SH>(w0, w1), e1 = bytes_at<SH + 1>(w0, w1);
@@ -451,10 +455,12 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                 else e_in = __dp4a(e, e, e_in);
             };
             if (((dlead + HALF) & 3) == 0) {
+#pragma unroll 2
                 for (; j < uw4; j += 4) ewalk(ld_word(rx + j), ld_word(rd + j));
             } else {
                 const uint8_t *ra = rd - 2;
                 uint32_t w0 = ld_word(ra);
+#pragma unroll 2
                 for (; j < uw4; j += 4) {
                     const uint32_t w1 = ld_word(ra + j + 4);
                     ewalk(ld_word(rx + j), bytes_at<2>(w0, w1));
