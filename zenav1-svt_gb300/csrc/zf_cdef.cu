@@ -1363,6 +1363,28 @@ int finish1_smem(int nfb, int ncand, int cap) {
 
 // ---- apply: one CTA per filter block, B (post-deblock) -> A -----------
 
+// Copy the n x n block at (x0, y0) of a pw x ph plane (clipped to it) from
+// src to dst: 4-byte words when both planes are word aligned (plane widths
+// and block columns are multiples of 4 samples, so a word never straddles
+// the plane's right edge), samples otherwise.
+__device__ void copy_block(const uint8_t *src, uint8_t *dst, int pw, int ph, int x0, int y0, int n, int bd) {
+    const int rows = min(n, ph - y0), cols = min(n, pw - x0);
+    if (aligned4(src) && aligned4(dst)) {
+        const int spw = word_samples(bd), wpr = cols / spw, bps = bd == 8 ? 1 : 2;
+        for (int q = threadIdx.x; q < rows * wpr; q += blockDim.x) {
+            const int ry = q / wpr, wx = q - ry * wpr;
+            const int64_t o = ((int64_t)(y0 + ry) * pw + x0) * bps + wx * 4;
+            *reinterpret_cast<uint32_t *>(dst + o) = *reinterpret_cast<const uint32_t *>(src + o);
+        }
+        return;
+    }
+    for (int q = threadIdx.x; q < rows * cols; q += blockDim.x) {
+        const int ry = q / cols, cx = q - ry * cols;
+        const int64_t o = (int64_t)(y0 + ry) * pw + x0 + cx;
+        stpx(dst, o, bd, ldpx(src, o, bd));
+    }
+}
+
 __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems) {
     __shared__ uint16_t reg[CR * CR];
     __shared__ uint16_t regc[2][CRC * CRC];
@@ -1389,17 +1411,9 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     if (threadIdx.x == 0) f.fb_row[fb] = dl_all != 0;
     const uint64_t dl = any ? dl_all : 0;
     if (dl == 0) {  // copy-through
-        for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
-            int y = y0 + i / 64, x = x0 + (i & 63);
-            if (x < f.w && y < f.h) stpx(f.A[0], (int64_t)y * f.w + x, bd, ldpx(f.B[0], (int64_t)y * f.w + x, bd));
-        }
+        copy_block(f.B[0], f.A[0], f.w, f.h, x0, y0, 64, bd);
         if (f.chroma)
-            for (int p = 1; p <= 2; ++p)
-                for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
-                    int y = y0 / 2 + i / 32, x = x0 / 2 + (i & 31);
-                    if (x < f.w / 2 && y < f.h / 2)
-                        stpx(f.A[p], (int64_t)y * (f.w / 2) + x, bd, ldpx(f.B[p], (int64_t)y * (f.w / 2) + x, bd));
-                }
+            for (int p = 1; p <= 2; ++p) copy_block(f.B[p], f.A[p], f.w / 2, f.h / 2, x0 / 2, y0 / 2, 32, bd);
         return;
     }
     const int sidx = cp.bits == 0 ? 0 : f.fb_idx[fb];
