@@ -75,8 +75,12 @@ struct LrPlane {
 // Statistics kernel TMA boxes (5-tap window, 8-bit): the post-CDEF window
 // of a CTA (25 rows = 17 rows + 8 halo rows) starting 16 bytes left of the
 // unit (its 2-column halo at byte 14), the source rows of a CTA (17); widths
-// cover a unit of up to 383 columns plus halos, in 4-byte elements.
-constexpr int kTmaDBoxW = 104, kTmaDBoxH = 25, kTmaXBoxW = 96, kTmaXBoxH = 17;
+// cover a unit of up to 383 columns plus halos, in 4-byte elements. A box
+// lands in shared memory with its width as the row pitch; the widths are
+// 12 and 4 (mod 32) words, so eight consecutive rows start in eight
+// different banks (the walks of a warp read the same column of up to a
+// dozen rows; a pitch of 0 mod 32 words put every row in one bank).
+constexpr int kTmaDBoxW = 108, kTmaDBoxH = 25, kTmaXBoxW = 100, kTmaXBoxH = 17;
 constexpr int kTmaDLead = 14;  // byte of column -2 (the window's first) in a D row
 
 // Restoration apply: 64-px column tiles of a stripe per CTA.
