@@ -363,6 +363,33 @@ int32_t zf_use_graphs(zf_ctx *ctx, int32_t enable);
 /* out[0] graph launches, out[1] in-place updates, out[2] instantiations. */
 int32_t zf_graph_stats(const zf_ctx *ctx, uint64_t out[3]);
 
+/* Launch settings of a context (no counterpart in the reference: they
+ * change how the stage runs on the GPU, never its results). */
+typedef struct zf_tune {
+    int32_t graphs;             /* 0/1: CUDA-graph launch mode (zf_use_graphs) */
+    int32_t stats_tma;          /* 0/1: Wiener statistics rows of 8-bit planes by TMA */
+    int32_t apply_group;        /* 64-px column tiles per restoration-apply CTA: 1..16 */
+    int32_t pad;
+    double ms;                  /* zf_autotune: mean device time of one call (else 0) */
+} zf_tune;
+int32_t zf_get_tune(const zf_ctx *ctx, zf_tune *out);
+/* ZF_ERR_ARG for a setting out of range. */
+int32_t zf_set_tune(zf_ctx *ctx, const zf_tune *t);
+/* Autotuner (no counterpart in the reference). Times every candidate
+ * setting (graphs x stats_tma x apply_group in {1, 2, 4, 8, 16}) on the
+ * caller's frames: one call per candidate to warm up, then `reps` timed
+ * calls (CUDA events on the context's stream), each of the whole filter
+ * stage on private copies of the frames' recon restored before every call
+ * (zf_filter_stage for n == 1, zf_submit_batch otherwise), so the caller's
+ * buffers are not written. Sets the fastest candidate on the context and
+ * writes it to *best; writes up to `max` candidates with their times to
+ * `cands` (may be NULL). Returns the number of candidates (>= 1) or a
+ * negative ZF_ERR_*. Allocates device memory for the copies (device
+ * frames) and runs O(candidates x reps) stage calls: a set-up step, not a
+ * per-frame one. */
+int32_t zf_autotune(zf_ctx *ctx, const zf_frame *frames, int32_t n, int32_t reps, zf_tune *best,
+                    zf_tune *cands, int32_t max);
+
 /* Kernel launches issued by this context since zf_create. */
 uint64_t zf_launch_count(const zf_ctx *ctx);
 /* enable != 0: bracket every kernel launch with CUDA events (adds a little

@@ -90,6 +90,10 @@ def lib():
     L.zf_write_filter_params.argtypes = [P(ZfDecisions), P(abi.ZfHeaderOpts), C.c_void_p, C.c_int32,
                                          P(C.c_int32)]
     L.zf_use_graphs.argtypes = [C.c_void_p, C.c_int32]
+    L.zf_get_tune.argtypes = [C.c_void_p, P(abi.ZfTune)]
+    L.zf_set_tune.argtypes = [C.c_void_p, P(abi.ZfTune)]
+    L.zf_autotune.argtypes = [C.c_void_p, P(ZfFrame), C.c_int32, C.c_int32, P(abi.ZfTune), P(abi.ZfTune),
+                              C.c_int32]
     L.zf_graph_stats.argtypes = [C.c_void_p, P(C.c_uint64)]
     L.zf_superres_scaled_size.argtypes = [C.c_int32, C.c_int32]
     L.zf_superres_upscale.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
@@ -98,7 +102,7 @@ def lib():
                                          C.c_int32, P(abi.ZfFilmGrain)]
     L.zf_film_grain_synthesize.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                            P(abi.ZfFilmGrain)]
-    for name in ("zf_use_graphs", "zf_graph_stats", "zf_superres_scaled_size", "zf_superres_upscale", "zf_film_grain_estimate",
+    for name in ("zf_get_tune", "zf_set_tune", "zf_autotune", "zf_use_graphs", "zf_graph_stats", "zf_superres_scaled_size", "zf_superres_upscale", "zf_film_grain_estimate",
                  "zf_film_grain_synthesize", "zf_write_filter_params", "zf_sgr_search", "zf_sgr_apply", "zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
                  "zf_submit_batch", "zf_deblock_pick", "zf_deblock_apply", "zf_cdef_search",
                  "zf_cdef_apply", "zf_lr_search", "zf_lr_apply"):
@@ -187,6 +191,27 @@ class Context:
     def use_graphs(self, enable=True):
         """Run each call's launch sequence as a CUDA graph (zf_use_graphs)."""
         self._check(lib().zf_use_graphs(self.h, 1 if enable else 0))
+
+    def get_tune(self):
+        """The context's launch settings (zf_get_tune) as a dict."""
+        t = abi.ZfTune()
+        self._check(lib().zf_get_tune(self.h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tune(self, graphs, stats_tma, apply_group):
+        """Set the launch settings (zf_set_tune)."""
+        t = abi.ZfTune(graphs, stats_tma, apply_group, 0, 0.0)
+        self._check(lib().zf_set_tune(self.h, C.byref(t)))
+
+    def autotune_raw(self, frames_arr, n, reps=3):
+        """zf_autotune over n ZfFrame structs: (best dict, [candidate dicts]).
+        The context keeps the best setting."""
+        best = abi.ZfTune()
+        cands = (abi.ZfTune * 32)()
+        rc = lib().zf_autotune(self.h, frames_arr, n, reps, C.byref(best), cands, 32)
+        if rc < 0:
+            self._check(rc)
+        return best.as_dict(), [cands[i].as_dict() for i in range(min(rc, 32))]
 
     def graph_stats(self):
         """(graph launches, in-place updates, instantiations)."""

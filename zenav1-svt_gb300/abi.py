@@ -54,6 +54,15 @@ class ZfSizes(C.Structure):
                 ("device_bytes", C.c_uint64)]
 
 
+class ZfTune(C.Structure):
+    _fields_ = [("graphs", C.c_int32), ("stats_tma", C.c_int32), ("apply_group", C.c_int32),
+                ("pad", C.c_int32), ("ms", C.c_double)]
+
+    def as_dict(self):
+        return {"graphs": self.graphs, "stats_tma": self.stats_tma, "apply_group": self.apply_group,
+                "ms": round(self.ms, 4)}
+
+
 class ZfOpts(C.Structure):
     _fields_ = [("device", C.c_int32), ("flags", C.c_int32), ("hbm_budget_bytes", C.c_uint64),
                 ("cancel_flag", C.POINTER(C.c_int32))]

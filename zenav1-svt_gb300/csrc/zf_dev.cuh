@@ -83,8 +83,9 @@ struct LrPlane {
 constexpr int kTmaDBoxW = 108, kTmaDBoxH = 25, kTmaXBoxW = 100, kTmaXBoxH = 17;
 constexpr int kTmaDLead = 14;  // byte of column -2 (the window's first) in a D row
 
-// Restoration apply: 64-px column tiles of a stripe per CTA.
-constexpr int kApplyGroup = 8;
+// Restoration apply: at most this many 64-px column tiles of a stripe per
+// CTA (the launch's group size is a kernel argument, 8 unless tuned).
+constexpr int kApplyGroupMax = 16;
 
 // CDEF joint strength search: bit counts 0..3, one cluster each.
 constexpr int kFinLevels = 4;

@@ -57,6 +57,7 @@ struct zf_ctx {
     bool graphs = false;
     bool capturing = false;
     bool tma = true;  // statistics kernel rows by TMA where the planes allow
+    int apply_group = 8;  // 64-px column tiles per restoration-apply CTA
     cudaGraphExec_t gexec = nullptr;
     std::vector<uint64_t> gsig;  // node kinds, kernel functions and cluster shapes of gexec's graph
     uint64_t graph_launches = 0, graph_updates = 0, graph_instantiations = 0;
@@ -781,9 +782,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             const LrPlane &L = p.d.lr[pl];
             const int ss = pl ? 1 : 0, full = 64 >> ss, off = 8 >> ss;
             const int nstripes = (L.ph + off + full - 1) / full;
-            const int ngroups = ((L.stride + 63) / 64 + zf::kApplyGroup - 1) / zf::kApplyGroup;
+            const int ngroups = ((L.stride + 63) / 64 + ctx->apply_group - 1) / ctx->apply_group;
             const int canvas_h = pl ? p.d.h / 2 : p.d.h;
-            // one item per stripe (CTA offset = group of kApplyGroup
+            // one item per stripe (CTA offset = group of ctx->apply_group
             // 64-px column tiles); a = the stripe's row of the row-major
             // hunits x vunits unit grid (-1: copy only), the kernel finds the
             // column along that row
@@ -1203,7 +1204,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         if (wl_apply.ctas) {
             { LaunchScope ls_(ctx, "k_lr_apply");
             zf::k_lr_apply<<<wl_apply.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_apply),
-                                                         (int)wl_apply.items.size()); }
+                                                         (int)wl_apply.items.size(), ctx->apply_group); }
             TRY(launch_check(ctx, "k_lr_apply"));
         }
     }
@@ -1504,6 +1505,148 @@ int32_t zf_use_graphs(zf_ctx *ctx, int32_t enable) {
     if (!ctx) return ZF_ERR_ARG;
     ctx->graphs = enable != 0;
     return ZF_OK;
+}
+
+int32_t zf_get_tune(const zf_ctx *ctx, zf_tune *out) {
+    if (!ctx || !out) return ZF_ERR_ARG;
+    std::memset(out, 0, sizeof(*out));
+    out->graphs = ctx->graphs ? 1 : 0;
+    out->stats_tma = ctx->tma ? 1 : 0;
+    out->apply_group = ctx->apply_group;
+    return ZF_OK;
+}
+
+int32_t zf_set_tune(zf_ctx *ctx, const zf_tune *t) {
+    if (!ctx || !t) return ZF_ERR_ARG;
+    if (t->graphs < 0 || t->graphs > 1 || t->stats_tma < 0 || t->stats_tma > 1 || t->apply_group < 1 ||
+        t->apply_group > zf::kApplyGroupMax)
+        return fail(ctx, ZF_ERR_ARG, "tune setting out of range");
+    ctx->graphs = t->graphs != 0;
+    ctx->tma = t->stats_tma != 0;
+    ctx->apply_group = t->apply_group;
+    return ZF_OK;
+}
+
+int32_t zf_autotune(zf_ctx *ctx, const zf_frame *frames, int32_t n, int32_t reps, zf_tune *best, zf_tune *cands,
+                    int32_t max) {
+    if (!ctx || !frames || n <= 0 || !best || reps < 1 || reps > 1000) return ZF_ERR_ARG;
+    for (int i = 0; i < n; ++i) TRY(validate_frame(ctx, &frames[i]));
+    CU(cudaSetDevice(ctx->device));
+    zf_tune saved;
+    zf_get_tune(ctx, &saved);
+    // private recon copies: `work` is what the calls filter, `orig` restores it
+    std::vector<zf_frame> fr(frames, frames + n);
+    std::vector<void *> dev_bufs;
+    std::vector<std::vector<uint8_t>> host_bufs;
+    struct Plane {
+        void *work;
+        const void *orig;
+        size_t bytes;
+        bool dev;
+    };
+    std::vector<Plane> planes;
+    auto cleanup = [&]() {
+        for (void *p : dev_bufs) cudaFree(p);
+        dev_bufs.clear();
+    };
+    for (int i = 0; i < n; ++i) {
+        const zf_frame &f = frames[i];
+        const size_t px = f.bit_depth == 8 ? 1 : 2;
+        for (int pl = 0; pl < (f.chroma_420 ? 3 : 1); ++pl) {
+            const size_t bytes = (pl ? (size_t)(f.width / 2) * (f.height / 2) : (size_t)f.width * f.height) * px;
+            Plane P{nullptr, f.rec[pl], bytes, f.planes_on_device != 0};
+            if (P.dev) {
+                void *w = nullptr, *o = nullptr;
+                if (cudaMalloc(&w, bytes) != cudaSuccess || cudaMalloc(&o, bytes) != cudaSuccess) {
+                    if (w) cudaFree(w);
+                    cudaGetLastError();
+                    cleanup();
+                    return fail(ctx, ZF_ERR_ALLOC, "autotune: no device memory for the frame copies");
+                }
+                dev_bufs.push_back(w);
+                dev_bufs.push_back(o);
+                if (cudaMemcpyAsync(o, f.rec[pl], bytes, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess) {
+                    cleanup();
+                    return fail(ctx, ZF_ERR_CUDA, "autotune: copy of the recon failed");
+                }
+                P.work = w;
+                P.orig = o;
+            } else {
+                host_bufs.emplace_back(bytes);
+                P.work = host_bufs.back().data();
+            }
+            fr[i].rec[pl] = P.work;
+            planes.push_back(P);
+        }
+    }
+    auto restore = [&]() -> bool {
+        for (const Plane &P : planes) {
+            if (P.dev) {
+                if (cudaMemcpyAsync(P.work, P.orig, P.bytes, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
+                    return false;
+            } else {
+                std::memcpy(P.work, P.orig, P.bytes);
+            }
+        }
+        return true;
+    };
+    std::vector<zf_decisions> outs((size_t)n);
+    auto call = [&]() -> int {
+        std::memset(outs.data(), 0, outs.size() * sizeof(zf_decisions));
+        return n == 1 ? zf_filter_stage(ctx, fr.data(), outs.data(), nullptr)
+                      : zf_submit_batch(ctx, fr.data(), n, outs.data(), nullptr);
+    };
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        cleanup();
+        return fail(ctx, ZF_ERR_CUDA, "autotune: event creation failed");
+    }
+    static const int kGroups[5] = {1, 2, 4, 8, 16};
+    int count = 0, rc = ZF_OK;
+    zf_tune win{};
+    win.ms = -1.0;
+    for (int g = 0; g < 2 && rc == ZF_OK; ++g)
+        for (int t = 0; t < 2 && rc == ZF_OK; ++t)
+            for (int k = 0; k < 5 && rc == ZF_OK; ++k) {
+                zf_tune c{};
+                c.graphs = g;
+                c.stats_tma = t;
+                c.apply_group = kGroups[k];
+                zf_set_tune(ctx, &c);
+                double total = 0.0;
+                for (int r = -1; r < reps && rc == ZF_OK; ++r) {  // r = -1: warm-up
+                    if (!restore()) {
+                        rc = fail(ctx, ZF_ERR_CUDA, "autotune: restoring the recon failed");
+                        break;
+                    }
+                    cudaEventRecord(e0, ctx->stream);
+                    rc = call();
+                    if (rc != ZF_OK) break;
+                    cudaEventRecord(e1, ctx->stream);
+                    float ms = 0.f;
+                    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+                        rc = fail(ctx, ZF_ERR_CUDA, "autotune: event timing failed");
+                        break;
+                    }
+                    if (r >= 0) total += ms;
+                }
+                if (rc != ZF_OK) break;
+                c.ms = total / reps;
+                if (cands && count < max) cands[count] = c;
+                ++count;
+                if (win.ms < 0 || c.ms < win.ms) win = c;  // strict: the earlier candidate wins ties
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamSynchronize(ctx->stream);
+    cleanup();
+    if (rc != ZF_OK) {
+        zf_set_tune(ctx, &saved);
+        return rc;
+    }
+    zf_set_tune(ctx, &win);
+    *best = win;
+    return count;
 }
 
 int32_t zf_graph_stats(const zf_ctx *ctx, uint64_t out[3]) {

@@ -46,7 +46,7 @@ constexpr int kTrialClusterHost = 8;  // k_lr_trial: CTAs per unit (cluster size
 constexpr int kLrFinThreadsHost = 1024;  // k_lr_finish CTA size
 constexpr int kLrPairMaxHost = 20100;   // k_lr_finish pair-table entries (units <= 200)
 __global__ void k_lr_finish(FrameDesc *frames, int nframes);
-__global__ void k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems);
+__global__ void k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems, int group);
 
 // Fills dims and the CDEF policy of *d from a frame (host; zf_host.cu).
 int describe_cdef_frame(const zf_frame *f, FrameDesc *d);

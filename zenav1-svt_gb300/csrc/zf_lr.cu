@@ -1591,7 +1591,7 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
 // ---------------------------------------------------------------------------
 // 5. Apply (apply_restoration_frame, restoration.rs:992-1052) with the
 // stripe boundaries of save_lr_boundaries, writing every pixel of C: one CTA
-// per (plane, stripe, group of kApplyGroup 64-px column tiles) over the
+// per (plane, stripe, group of `group` <= kApplyGroupMax 64-px column tiles) over the
 // aligned canvas. Tiles of Wiener units are filtered within the true plane
 // and copied from A beyond it; every other tile (unit NONE, frame NONE,
 // plane not searched, and the rows below the true plane: stripe index
@@ -1603,12 +1603,12 @@ __global__ void __launch_bounds__(kLrFinThreads) k_lr_finish(FrameDesc *frames, 
 // before it filters (planes the tiled trial did not write), so a copy-only
 // group pays one barrier.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems) {
+__global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems, int group) {
     constexpr int SW = TT_W + 7;
     constexpr int MAXH = 64 + 7;
     __shared__ __align__(16) uint16_t stage[MAXH * SW];
     __shared__ __align__(16) uint16_t tmp[MAXH * TT_W];
-    __shared__ int s_unit[kApplyGroup], s_filter[kApplyGroup];
+    __shared__ int s_unit[kApplyGroupMax], s_filter[kApplyGroupMax];
     const WorkItem wi = items[find_item(items, nitems, blockIdx.x)];
     const FrameDesc &f = frames[wi.frame];
     const LrPlane &pl = f.lr[wi.plane];
@@ -1622,8 +1622,8 @@ __global__ void __launch_bounds__(256) k_lr_apply(FrameDesc *frames, const WorkI
     const int ys = s < nstripes ? max(0, s * full - off) : pl.ph;
     const int ye = s < nstripes ? min(pl.ph, (s + 1) * full - off) : canvas_h;
     const int ntiles = (stride + TT_W - 1) / TT_W;
-    const int g0 = (blockIdx.x - wi.cta_begin) * kApplyGroup;
-    const int ntl = min(kApplyGroup, ntiles - g0);
+    const int g0 = (blockIdx.x - wi.cta_begin) * group;
+    const int ntl = min(group, ntiles - g0);
     const uint8_t *post = f.A[wi.plane], *pre = f.B[wi.plane];
     uint8_t *out = f.C[wi.plane];
     // the unit of each tile: wi.a is its row of the unit grid (-1: copy
