@@ -268,6 +268,48 @@ typedef struct zf_header_opts {
 int32_t zf_write_filter_params(const zf_decisions *d, const zf_header_opts *o, uint8_t *buf, int32_t cap,
                                int32_t *bit_pos);
 
+/* ---- Per-superblock restoration syntax -----------------------------------
+ * The coded elements of a superblock's loop-restoration syntax, in coding
+ * order, for the caller's range coder: what the reference's
+ * write_lr_for_sb (svtav1-encoder/src/restoration.rs:1127-1182) codes for
+ * every restoration unit whose top-left corner lies in the superblock
+ * (corners_in_sb, :1070-1106), with write_wiener_filter's subexponential
+ * tap coding against the running per-plane reference filter
+ * (svtav1-entropy/src/lr.rs:67-236; plane-based window: 7-tap luma, so a
+ * 5-tap luma solve codes TAP0 as 0; 5-tap chroma). Host code; no device
+ * work. The range coder itself (AomWriter) stays the caller's. */
+#define ZF_SYM_WIENER_RESTORE 1 /* one symbol on the adaptive wiener_restore CDF, value 0/1 */
+#define ZF_SYM_BITS 2           /* nbits equiprobable bits of value, most significant first
+                                   (write_literal; nbits 1 is write_bit) */
+typedef struct zf_lr_sym {
+    int32_t kind;               /* ZF_SYM_* */
+    int32_t nbits;              /* ZF_SYM_BITS: 1..16 */
+    uint32_t value;
+    int16_t plane, pad;
+    int32_t unit;               /* restoration unit (row-major in its plane) */
+} zf_lr_sym;
+/* Running reference filters of the three planes (C wiener_info[3]). */
+typedef struct zf_wiener_refs {
+    int16_t vfilter[3][8], hfilter[3][8];
+} zf_wiener_refs;
+/* The default filter in every plane: call at the first superblock of each
+ * tile (svt_av1_reset_loop_restoration). */
+void zf_wiener_refs_reset(zf_wiener_refs *r);
+/* corners_in_sb: 1 and out = {rcol0, rcol1, rrow0, rrow1} when units of a
+ * plane (unit_size, is_uv) have their corner in the superblock at
+ * (mi_row, mi_col) of sb_mi mi, else 0 (negative: bad argument). frame_w is
+ * the upscaled width under superres; sr_denom 9..16, or 0 for none. */
+int32_t zf_lr_corners_in_sb(int32_t unit_size, int32_t is_uv, int32_t mi_row, int32_t mi_col, int32_t sb_mi,
+                            int32_t frame_w, int32_t frame_h, int32_t sr_denom, int32_t out[4]);
+/* Appends the superblock's elements to out (capacity cap) and returns
+ * their count, updating refs as the coder would; ZF_ERR_ARG when out is
+ * too small (nothing written, refs unchanged). Planes whose frame_rtype is
+ * NONE code nothing; a WIENER plane codes, per unit, the restore flag and,
+ * when set, the taps (d->lr_units[plane] must hold the plane's units). */
+int32_t zf_lr_sb_syntax(const zf_decisions *d, int32_t mi_row, int32_t mi_col, int32_t sb_mi, int32_t frame_w,
+                        int32_t frame_h, int32_t monochrome, int32_t sr_denom, zf_wiener_refs *refs,
+                        zf_lr_sym *out, int32_t cap);
+
 /* ---- Self-guided restoration (RESTORE_SGRPROJ) ---------------------------
  * No counterpart in the reference encoder: it never searches or signals
  * SGRPROJ (svtav1-dsp/src/restoration.rs:1280, svtav1-encoder/src/

@@ -90,6 +90,11 @@ def lib():
     L.zf_write_filter_params.argtypes = [P(ZfDecisions), P(abi.ZfHeaderOpts), C.c_void_p, C.c_int32,
                                          P(C.c_int32)]
     L.zf_use_graphs.argtypes = [C.c_void_p, C.c_int32]
+    L.zf_wiener_refs_reset.argtypes = [P(abi.ZfWienerRefs)]
+    L.zf_wiener_refs_reset.restype = None
+    L.zf_lr_corners_in_sb.argtypes = [C.c_int32] * 8 + [P(C.c_int32)]
+    L.zf_lr_sb_syntax.argtypes = [P(ZfDecisions)] + [C.c_int32] * 7 + [P(abi.ZfWienerRefs), P(abi.ZfLrSym),
+                                                                     C.c_int32]
     L.zf_get_tune.argtypes = [C.c_void_p, P(abi.ZfTune)]
     L.zf_set_tune.argtypes = [C.c_void_p, P(abi.ZfTune)]
     L.zf_autotune.argtypes = [C.c_void_p, P(ZfFrame), C.c_int32, C.c_int32, P(abi.ZfTune), P(abi.ZfTune),
@@ -102,7 +107,7 @@ def lib():
                                          C.c_int32, P(abi.ZfFilmGrain)]
     L.zf_film_grain_synthesize.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                            P(abi.ZfFilmGrain)]
-    for name in ("zf_get_tune", "zf_set_tune", "zf_autotune", "zf_use_graphs", "zf_graph_stats", "zf_superres_scaled_size", "zf_superres_upscale", "zf_film_grain_estimate",
+    for name in ("zf_lr_corners_in_sb", "zf_lr_sb_syntax", "zf_get_tune", "zf_set_tune", "zf_autotune", "zf_use_graphs", "zf_graph_stats", "zf_superres_scaled_size", "zf_superres_upscale", "zf_film_grain_estimate",
                  "zf_film_grain_synthesize", "zf_write_filter_params", "zf_sgr_search", "zf_sgr_apply", "zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
                  "zf_submit_batch", "zf_deblock_pick", "zf_deblock_apply", "zf_cdef_search",
                  "zf_cdef_apply", "zf_lr_search", "zf_lr_apply"):

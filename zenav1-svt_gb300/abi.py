@@ -54,6 +54,18 @@ class ZfSizes(C.Structure):
                 ("device_bytes", C.c_uint64)]
 
 
+SYM_WIENER_RESTORE, SYM_BITS = 1, 2  # zf_lr_sym.kind
+
+
+class ZfLrSym(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("nbits", C.c_int32), ("value", C.c_uint32), ("plane", C.c_int16),
+                ("pad", C.c_int16), ("unit", C.c_int32)]
+
+
+class ZfWienerRefs(C.Structure):
+    _fields_ = [("vfilter", (C.c_int16 * 8) * 3), ("hfilter", (C.c_int16 * 8) * 3)]
+
+
 class ZfTune(C.Structure):
     _fields_ = [("graphs", C.c_int32), ("stats_tma", C.c_int32), ("apply_group", C.c_int32),
                 ("pad", C.c_int32), ("ms", C.c_double)]

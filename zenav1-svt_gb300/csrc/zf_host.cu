@@ -1871,6 +1871,159 @@ int32_t zf_sgr_apply(zf_ctx *ctx, const zf_sgr_plane *p, const zf_sgr_unit *unit
     return ZF_OK;
 }
 
+// ---- per-superblock restoration syntax ----------------------------------
+
+void zf_wiener_refs_reset(zf_wiener_refs *r) {
+    if (!r) return;
+    static const int16_t def[8] = {3, -7, 15, -22, 15, -7, 3, 0};  // WIENER_DEFAULT taps
+    for (int p = 0; p < 3; ++p) {
+        std::memcpy(r->vfilter[p], def, sizeof(def));
+        std::memcpy(r->hfilter[p], def, sizeof(def));
+    }
+}
+
+// corners_in_sb (svtav1-encoder/src/restoration.rs:1070-1106): the unit
+// range whose top-left corners fall in the superblock; under superres the
+// horizontal mi -> pixel mapping carries the denominator over
+// SCALE_NUMERATOR = 8.
+int32_t zf_lr_corners_in_sb(int32_t unit_size, int32_t is_uv, int32_t mi_row, int32_t mi_col, int32_t sb_mi,
+                            int32_t frame_w, int32_t frame_h, int32_t sr_denom, int32_t out[4]) {
+    if (!out || (unit_size != 32 && unit_size != 64 && unit_size != 128 && unit_size != 256) || mi_row < 0 ||
+        mi_col < 0 || sb_mi <= 0 || frame_w <= 0 || frame_h <= 0 || (sr_denom != 0 && (sr_denom < 9 || sr_denom > 16)))
+        return ZF_ERR_ARG;
+    const int ss = is_uv ? 1 : 0;
+    const int tile_w = (frame_w + ss) >> ss, tile_h = (frame_h + ss) >> ss;
+    const int horz = count_units_in_tile(unit_size, tile_w), vert = count_units_in_tile(unit_size, tile_h);
+    const int mi_size = 4 >> ss;
+    const int mi_to_num_x = sr_denom ? mi_size * sr_denom : mi_size;
+    const int denom_x = sr_denom ? unit_size * 8 : unit_size;
+    const int rnd_x = denom_x - 1, rnd_y = unit_size - 1;
+    const int rcol0 = (mi_col * mi_to_num_x + rnd_x) / denom_x;
+    const int rrow0 = (mi_row * mi_size + rnd_y) / unit_size;
+    const int rcol1 = std::min(((mi_col + sb_mi) * mi_to_num_x + rnd_x) / denom_x, horz);
+    const int rrow1 = std::min(((mi_row + sb_mi) * mi_size + rnd_y) / unit_size, vert);
+    if (!(rcol0 < rcol1 && rrow0 < rrow1)) return 0;
+    out[0] = rcol0;
+    out[1] = rcol1;
+    out[2] = rrow0;
+    out[3] = rrow1;
+    return 1;
+}
+
+namespace {
+// The bit-level steps of write_primitive_quniform / _subexpfin /
+// _refsubexpfin (svtav1-entropy/src/lr.rs:40-145), emitted as elements.
+struct SymOut {
+    std::vector<zf_lr_sym> v;
+    int plane = 0, unit = 0;
+    void bits(uint32_t value, int n) {
+        if (n <= 0) return;  // a zero-width literal codes nothing
+        zf_lr_sym s{};
+        s.kind = ZF_SYM_BITS;
+        s.nbits = n;
+        s.value = value;
+        s.plane = (int16_t)plane;
+        s.unit = unit;
+        v.push_back(s);
+    }
+};
+int msb_u32(uint32_t n) { return 31 - __builtin_clz(n); }
+uint16_t recenter_nonneg_h(uint16_t r, uint16_t v) {
+    if (v > (r << 1)) return v;
+    if (v >= r) return (uint16_t)((v - r) << 1);
+    return (uint16_t)(((r - v) << 1) - 1);
+}
+uint16_t recenter_finite_nonneg_h(uint16_t n, uint16_t r, uint16_t v) {
+    if ((r << 1) <= n) return recenter_nonneg_h(r, v);
+    return recenter_nonneg_h((uint16_t)(n - 1 - r), (uint16_t)(n - 1 - v));
+}
+void quniform(SymOut &o, int n, int v) {
+    if (n <= 1) return;
+    const int l = msb_u32((uint32_t)(n - 1)) + 1, m = (1 << l) - n;
+    if (v < m) {
+        o.bits((uint32_t)v, l - 1);
+    } else {
+        o.bits((uint32_t)(m + ((v - m) >> 1)), l - 1);
+        o.bits((uint32_t)((v - m) & 1), 1);
+    }
+}
+void subexpfin(SymOut &o, int n, int k, int v) {
+    int i = 0, mk = 0;
+    for (;;) {
+        const int b = i ? k + i - 1 : k, a = 1 << b;
+        if (n <= mk + 3 * a) {
+            quniform(o, n - mk, v - mk);
+            return;
+        }
+        const bool t = v >= mk + a;
+        o.bits(t ? 1u : 0u, 1);
+        if (!t) {
+            o.bits((uint32_t)(v - mk), b);
+            return;
+        }
+        ++i;
+        mk += a;
+    }
+}
+// write_wiener_filter (svtav1-entropy/src/lr.rs:154-236) against the
+// plane's reference, which then becomes this filter.
+void wiener_filter_syms(SymOut &o, int win, const int16_t *vf, const int16_t *hf, int16_t *rvf, int16_t *rhf) {
+    static const int kMin[3] = {-5, -23, -17}, kMax[3] = {10, 8, 46}, kK[3] = {1, 2, 3};
+    auto tap = [&](const int16_t *f, const int16_t *rf, int idx) {
+        const int n = kMax[idx] - kMin[idx] + 1;
+        subexpfin(o, n, kK[idx],
+                  recenter_finite_nonneg_h((uint16_t)n, (uint16_t)(rf[idx] - kMin[idx]), (uint16_t)(f[idx] - kMin[idx])));
+    };
+    if (win == 7) tap(vf, rvf, 0);
+    tap(vf, rvf, 1);
+    tap(vf, rvf, 2);
+    if (win == 7) tap(hf, rhf, 0);
+    tap(hf, rhf, 1);
+    tap(hf, rhf, 2);
+    std::memcpy(rvf, vf, 16);
+    std::memcpy(rhf, hf, 16);
+}
+}  // namespace
+
+// write_lr_for_sb (svtav1-encoder/src/restoration.rs:1127-1182).
+int32_t zf_lr_sb_syntax(const zf_decisions *d, int32_t mi_row, int32_t mi_col, int32_t sb_mi, int32_t frame_w,
+                        int32_t frame_h, int32_t monochrome, int32_t sr_denom, zf_wiener_refs *refs,
+                        zf_lr_sym *out, int32_t cap) {
+    if (!d || !refs || (!out && cap > 0) || cap < 0) return ZF_ERR_ARG;
+    zf_wiener_refs r = *refs;
+    SymOut o;
+    for (int pl = 0; pl < (monochrome ? 1 : 3); ++pl) {
+        const zf_lr_plane &P = d->lr[pl];
+        if (P.frame_rtype == 0) continue;  // RESTORE_NONE: corners_in_sb is None
+        if (P.frame_rtype != 1 || !d->lr_units[pl]) return ZF_ERR_ARG;  // only WIENER frame types are coded here
+        int32_t c[4];
+        const int e = zf_lr_corners_in_sb(P.unit_size, pl > 0, mi_row, mi_col, sb_mi, frame_w, frame_h, sr_denom, c);
+        if (e < 0) return e;
+        if (e == 0) continue;
+        if (c[1] > P.hunits || c[3] > P.vunits) return ZF_ERR_ARG;
+        o.plane = pl;
+        for (int rrow = c[2]; rrow < c[3]; ++rrow)
+            for (int rcol = c[0]; rcol < c[1]; ++rcol) {
+                const int unit = rcol + rrow * P.hunits;
+                const zf_lr_unit &u = d->lr_units[pl][unit];
+                const bool used = u.rtype != 0;
+                o.unit = unit;
+                zf_lr_sym s{};
+                s.kind = ZF_SYM_WIENER_RESTORE;
+                s.value = used ? 1u : 0u;
+                s.plane = (int16_t)pl;
+                s.unit = unit;
+                o.v.push_back(s);
+                if (used)
+                    wiener_filter_syms(o, pl ? 5 : 7, u.vfilter, u.hfilter, r.vfilter[pl], r.hfilter[pl]);
+            }
+    }
+    if ((int64_t)o.v.size() > cap) return ZF_ERR_ARG;
+    if (!o.v.empty()) std::memcpy(out, o.v.data(), o.v.size() * sizeof(zf_lr_sym));
+    *refs = r;
+    return (int32_t)o.v.size();
+}
+
 // loop_filter_params / cdef_params / lr_params of write_key_frame_header
 // (svtav1-entropy/src/obu.rs:1268-1377): fixed-width fields, MSB first.
 int32_t zf_write_filter_params(const zf_decisions *d, const zf_header_opts *o, uint8_t *buf, int32_t cap,
