@@ -105,6 +105,13 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
     __shared__ unsigned long long Hs[WIN2 * WIN2];
     __shared__ unsigned long long Ms[WIN2], Ss[WIN2], Es[4];  // Es: sum s, sse blocks, right, bottom
     __shared__ __align__(8) uint64_t mbar;
+    // 5-tap window: each (unit row, window row) walk stores its Mr row parts
+    // and shift sums, and each sse walk its four sums, in a slot of its own
+    // (no shared-memory atomics, which serialised the lanes of a warp on the
+    // same few words); they are summed over the rows after the walks.
+    constexpr int SR = WIN == 5 ? G::ROWS : 1;
+    __shared__ int Mrow[SR][WIN2];
+    __shared__ unsigned Srow[SR][WIN2], Erow[SR][4];
     static_assert(G::DROWS * G::DSB <= (int)sizeof(D) && G::ROWS * G::XSB <= (int)sizeof(X), "byte layout fits");
     static_assert(WIN != 5 || (kTmaDBoxH == G::DROWS && kTmaXBoxH == G::ROWS &&
                                kTmaDBoxW * 4 * kTmaDBoxH <= (int)sizeof(D) && kTmaXBoxW * 4 * kTmaXBoxH <= (int)sizeof(X) &&
@@ -424,15 +431,29 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                 c0 += win[0];
             }
         }
-#pragma unroll
-        for (int ca = 0; ca < WIN; ++ca) atomicAdd(&Ms[ca * WIN + ra], (unsigned long long)(long long)acc[ca]);
         // column windows ca = 1..WIN-1 slide the ca = 0 one
-        unsigned long long cw = c0;
-        atomicAdd(&Ss[ra], cw);
+        if constexpr (WIN == 5) {
+            const int rr = i - xi0;
+            unsigned cw = c0;
+            Srow[rr][ra] = cw;
 #pragma unroll
-        for (int ca = 1; ca < WIN; ++ca) {
-            cw = cw - (unsigned)Dat(yy, ca - 1 - HALF) + (unsigned)Dat(yy, ca - 1 - HALF + uw);
-            atomicAdd(&Ss[ca * WIN + ra], cw);
+            for (int ca = 0; ca < WIN; ++ca) {
+                Mrow[rr][ca * WIN + ra] = acc[ca];
+                if (ca) {
+                    cw = cw - (unsigned)Dat(yy, ca - 1 - HALF) + (unsigned)Dat(yy, ca - 1 - HALF + uw);
+                    Srow[rr][ca * WIN + ra] = cw;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int ca = 0; ca < WIN; ++ca) atomicAdd(&Ms[ca * WIN + ra], (unsigned long long)(long long)acc[ca]);
+            unsigned long long cw = c0;
+            atomicAdd(&Ss[ra], cw);
+#pragma unroll
+            for (int ca = 1; ca < WIN; ++ca) {
+                cw = cw - (unsigned)Dat(yy, ca - 1 - HALF) + (unsigned)Dat(yy, ca - 1 - HALF + uw);
+                atomicAdd(&Ss[ca * WIN + ra], cw);
+            }
         }
     } else if (t < nh + (WIN + 1) * (xi1 - xi0)) {
         // ---- sum s and the sse_region parts of unit row i: one row per
@@ -482,9 +503,17 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                 else e_in += e * e;
             }
         }
-        atomicAdd(&Es[0], (unsigned long long)sx);
-        atomicAdd(&Es[i >= uh - uh % 16 ? 3 : 1], (unsigned long long)e_in);
-        atomicAdd(&Es[2], (unsigned long long)e_rgt);
+        if constexpr (WIN == 5) {
+            const bool bottom = i >= uh - uh % 16;
+            Erow[i - xi0][0] = sx;
+            Erow[i - xi0][1] = bottom ? 0u : e_in;
+            Erow[i - xi0][2] = e_rgt;
+            Erow[i - xi0][3] = bottom ? e_in : 0u;
+        } else {
+            atomicAdd(&Es[0], (unsigned long long)sx);
+            atomicAdd(&Es[i >= uh - uh % 16 ? 3 : 1], (unsigned long long)e_in);
+            atomicAdd(&Es[2], (unsigned long long)e_rgt);
+        }
     }
     __syncthreads();
     // Interior rows: the row sums of each (dr, dc, ca) are added over the
@@ -495,6 +524,21 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
         constexpr int NE = WIN * (WIN + 1) / 2;
         static_assert(G::ROWS * G::NDR * NE * 4 <= G::DROWS * G::DCOLS * 2, "row-sum buffer fits in D");
         int *RS = reinterpret_cast<int *>(D);
+        if constexpr (WIN == 5) {
+            // the row slots of the (row, window row) and sse walks: 25 Mr
+            // entries, 25 shift sums, 4 sse / source sums, over the unit rows
+            // of this CTA (each entry of Ms / Ss / Es is written here only)
+            const int nr = xi1 - xi0, q = (int)blockDim.x - 1 - t;  // the highest threads
+            if (q < 2 * WIN2 + 4) {
+                long long a = 0;
+                for (int r = 0; r < nr; ++r)
+                    a += q < WIN2 ? (long long)Mrow[r][q] : q < 2 * WIN2 ? (long long)Srow[r][q - WIN2]
+                                                                         : (long long)Erow[r][q - 2 * WIN2];
+                if (q < WIN2) Ms[q] = (unsigned long long)a;
+                else if (q < 2 * WIN2) Ss[q - WIN2] = (unsigned long long)a;
+                else Es[q - 2 * WIN2] = (unsigned long long)a;
+            }
+        }
         if (keep) {
             int e = 0;
 #pragma unroll
