@@ -213,9 +213,9 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
 
     const int nh = G::NDR * (y1 - y0);
     const int t = threadIdx.x;
-    // Rows with every vertical shift valid (HALF <= y < uh - HALF) keep their
-    // row sums for a cross-row reduction; the others add theirs directly.
-    auto interior = [&](int yy) { return yy >= HALF && yy < uh - HALF; };
+    // Every row's sums go through the cross-row reduction; rows with every
+    // vertical shift valid (HALF <= y < uh - HALF) add to all of them.
+    const bool all_interior = y0 >= HALF && y1 <= uh - HALF;
     int rs[WIN][WIN];  // rs[dc][sc + HALF]
     bool keep = false;
 #pragma unroll
@@ -223,7 +223,9 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
 #pragma unroll
         for (int j = 0; j < WIN; ++j) rs[k][j] = 0;
     if (t < nh) {
-        // ---- Hr: one (row y, dr) per thread
+        // ---- Hr: one (row y, dr) per thread; every such thread keeps its
+        // row sums (zeros when the partner row is outside the range)
+        keep = true;
         const int dr = t % G::NDR - (WIN - 1);
         const int y = y0 + t / G::NDR;
         // the row and its partner must lie in the extended range
@@ -332,22 +334,7 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                     if (HALF + HALF + dc <= WIN - 1) rs[dc][2 * HALF] += pre[dc];
             }
             // contributions: Hr[a][b], a = (ca, ra), b = (ca + dc, ra + dr)
-            keep = interior(y);
-#pragma unroll
-            for (int dc = 0; dc < WIN; ++dc) {
-                if (dc < dc0 || keep) continue;
-#pragma unroll
-                for (int ca = 0; ca + dc < WIN; ++ca) {
-                    const int v = rs[dc][ca];
-                    if (v == 0) continue;
-                    for (int ra = max(0, -dr); ra < min(WIN, WIN - dr); ++ra) {
-                        const int sr = ra - HALF;
-                        if (y < sr || y >= sr + uh) continue;
-                        const int ia = ca * WIN + ra, ib = (ca + dc) * WIN + ra + dr;
-                        atomicAdd(&Hs[ia * WIN2 + ib], (unsigned long long)(long long)v);
-                    }
-                }
-            }
+            (void)dc0;  // dc = 0 of a negative dr is dropped in the cross-row sums
         }
     } else if (t < nh + WIN * (xi1 - xi0)) {
         // ---- Mr and shift sums: one (unit row i, ra) per thread
@@ -516,10 +503,12 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
         }
     }
     __syncthreads();
-    // Interior rows: the row sums of each (dr, dc, ca) are added over the
-    // CTA's rows in shared memory (D is no longer read), then one atomic per
-    // H entry. RS[(row * NDR + dr index) * NE + e], e enumerating (dc, ca)
-    // with ca + dc < WIN.
+    // The row sums of each (dr, dc, ca) are added over the CTA's rows in
+    // shared memory (D is no longer read), then one atomic per H entry (per
+    // vertical shift when some row of the CTA lies within HALF of the unit's
+    // top or bottom, where a row reaches only some shifts).
+    // RS[(row * NDR + dr index) * NE + e], e enumerating (dc, ca) with
+    // ca + dc < WIN.
     {
         constexpr int NE = WIN * (WIN + 1) / 2;
         static_assert(G::ROWS * G::NDR * NE * 4 <= G::DROWS * G::DCOLS * 2, "row-sum buffer fits in D");
@@ -556,13 +545,32 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
             }
             const int ca = e;
             if (dr < 0 && dc == 0) continue;
-            long long acc = 0;
-            for (int r = 0; r < y1 - y0; ++r)
-                if (interior(y0 + r)) acc += RS[(r * G::NDR + dri) * NE + (q - dri * NE)];
-            if (acc == 0) continue;
-            for (int ra = max(0, -dr); ra < min(WIN, WIN - dr); ++ra) {
-                const int ia = ca * WIN + ra, ib = (ca + dc) * WIN + ra + dr;
-                atomicAdd(&Hs[ia * WIN2 + ib], (unsigned long long)acc);
+            const int ra0 = max(0, -dr), ra1 = min(WIN, WIN - dr);
+            if (all_interior) {  // every vertical shift holds every row
+                long long acc = 0;
+                for (int r = 0; r < y1 - y0; ++r) acc += RS[(r * G::NDR + dri) * NE + (q - dri * NE)];
+                if (acc == 0) continue;
+                for (int ra = ra0; ra < ra1; ++ra) {
+                    const int ia = ca * WIN + ra, ib = (ca + dc) * WIN + ra + dr;
+                    atomicAdd(&Hs[ia * WIN2 + ib], (unsigned long long)acc);
+                }
+            } else {  // a row adds to the vertical shifts sr = ra - HALF whose window [sr, sr + uh) holds it
+                long long acc[WIN];
+#pragma unroll
+                for (int k = 0; k < WIN; ++k) acc[k] = 0;
+                for (int r = 0; r < y1 - y0; ++r) {
+                    const long long v = RS[(r * G::NDR + dri) * NE + (q - dri * NE)];
+                    const int y = y0 + r;
+#pragma unroll
+                    for (int ra = 0; ra < WIN; ++ra)
+                        if (ra >= ra0 && ra < ra1 && y >= ra - HALF && y < ra - HALF + uh) acc[ra] += v;
+                }
+#pragma unroll
+                for (int ra = 0; ra < WIN; ++ra) {
+                    if (ra < ra0 || ra >= ra1 || acc[ra] == 0) continue;
+                    const int ia = ca * WIN + ra, ib = (ca + dc) * WIN + ra + dr;
+                    atomicAdd(&Hs[ia * WIN2 + ib], (unsigned long long)acc[ra]);
+                }
             }
         }
     }
