@@ -1241,6 +1241,22 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         if (t5) hpass(std::true_type());
         else hpass(std::false_type());
     }
+    // Rows of the tile the vertical pass writes (tout, not within 3 rows of
+    // a stripe edge) and rows in the unit's bottom strip, as bit masks over
+    // the tile's <= 64 rows (one ballot per 32 rows).
+    __shared__ uint32_t s_rows[4];
+    if (threadIdx.x < 64) {
+        const int rr = threadIdx.x;
+        bool near_edge = false;
+#pragma unroll
+        for (int e = 0; e < kTileEdges; ++e) near_edge |= y0 + rr >= eb[e] - 3 && y0 + rr < eb[e] + 3;
+        const unsigned mw = __ballot_sync(0xffffffffu, rr < th && tout && !near_edge);
+        const unsigned mb = __ballot_sync(0xffffffffu, rr < th && ty + rr >= uh - dh);
+        if ((threadIdx.x & 31) == 0) {
+            s_rows[threadIdx.x >> 5] = mw;
+            s_rows[2 + (threadIdx.x >> 5)] = mb;
+        }
+    }
     __syncthreads();
     const int c3 = 128 + vf[3], voff = -(1 << (bd + 10)), vmax = (1 << bd) - 1;
     auto vert = [&](const int *p) {
@@ -1253,6 +1269,8 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         for (int e = 0; e < kTileEdges; ++e) hit |= y >= eb[e] - 3 && y < eb[e] + 3;
         return hit;
     };
+    const uint64_t write_rows = s_rows[0] | ((uint64_t)s_rows[1] << 32);
+    const uint64_t bottom_rows = s_rows[2] | ((uint64_t)s_rows[3] << 32);
     // vertical: runs of four rows x 64 columns, SSE parts, trial output.
     // A thread takes at most 16 pixels of a tile, each e^2 <= 1023^2, so
     // its SSE parts fit u32.
@@ -1278,11 +1296,11 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
                 } else {
                     y = vert(p + jj);
                 }
-                if (tout && !edge_row(y0 + rr)) stpx(outp, (int64_t)(y0 + rr) * stride + x0 + cc, bd, y);
+                if ((write_rows >> rr) & 1) stpx(outp, (int64_t)(y0 + rr) * stride + x0 + cc, bd, y);
                 const int e = (int)srct[rr * TL + cc] - y;
                 const uint32_t e2 = (uint32_t)(e * e);
                 if (right) rgt32 += e2;
-                else if (ty + rr >= uh - dh) bot32 += e2;
+                else if ((bottom_rows >> rr) & 1) bot32 += e2;
                 else blk32 += e2;
             }
         }
