@@ -1394,7 +1394,7 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     __shared__ int bt[64];  // luma: adjusted primary strength | damping shift << 16
     __shared__ int blist[64];
     __shared__ int nblk;
-    __shared__ unsigned long long red[8];
+    __shared__ uint32_t s_count;  // filtered | changed << 16 (8-bit counters)
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
     const FrameDesc &f = frames[wi.frame];
@@ -1407,6 +1407,7 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     // Decoder do_cdef gate (cdef.rs:84-88).
     const bool any = cp.bits != 0 || cp.y_str[0] != 0 || (f.chroma && cp.uv_str[0] != 0);
     __shared__ unsigned dl_part[2];
+    if (threadIdx.x == 0) s_count = 0;  // ordered before its adds by the barriers below
     const uint64_t dl_all = fb_dlist(f, fbr, fbc, dl_part);
     if (threadIdx.x == 0) f.fb_row[fb] = dl_all != 0;
     const uint64_t dl = any ? dl_all : 0;
@@ -1454,7 +1455,7 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
         bt[b] = t | (damp_shift(t, damping) << 16);
     }
     __syncthreads();
-    unsigned long long filt = 0, changed = 0;
+    uint32_t filt = 0, changed = 0;
     const bool edge_y = !(x0 >= 2 && y0 >= 2 && x0 + 66 <= f.w && y0 + 66 <= f.h);
     const bool edge_uv = !(x0 >= 4 && y0 >= 4 && x0 / 2 + 34 <= f.w / 2 && y0 / 2 + 34 <= f.h / 2);
     const bool zero_y = lvl_y == 0 && sec_y == 0;
@@ -1515,11 +1516,16 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
         }
     }
     if (bd == 8 && f.cdef_stats) {
-        unsigned long long a = block_sum_u64(filt, red);
-        unsigned long long c = block_sum_u64(changed, red);
+        // a thread filters at most 24 pixels, a CTA at most 6144: both
+        // counts fit 16 bits of one word through the warp and CTA sums
+        uint32_t v = (uint32_t)filt | ((uint32_t)changed << 16);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) atomicAdd(&s_count, v);
+        __syncthreads();
         if (threadIdx.x == 0) {
-            atomicAdd(&f.cdef_stats[0], a);
-            atomicAdd(&f.cdef_stats[1], c);
+            atomicAdd(&f.cdef_stats[0], (unsigned long long)(s_count & 0xffffu));
+            atomicAdd(&f.cdef_stats[1], (unsigned long long)(s_count >> 16));
         }
     }
 }
