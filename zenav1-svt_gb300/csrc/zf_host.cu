@@ -738,7 +738,8 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         plans[i].out = outs ? &outs[i] : nullptr;
     }
     // Work lists (host-known shapes).
-    WorkList wl_db, wl_cs, wl_ca, wl_st5, wl_st7, wl_unit, wl_apply, wl_trial, wl_tiles;
+    // statistics: 5-tap 8-bit, 5-tap 10-bit (one kernel instantiation each), 7-tap
+    WorkList wl_db, wl_cs, wl_ca, wl_st5, wl_st7, wl_unit, wl_apply, wl_trial, wl_tiles, wl_st5h;
     std::vector<int> cdef_small, cdef_large;  // joint search: one CTA / cluster per bit count
     std::vector<int> cdef_joint[kJointGroups];  // register-row joint search, by (candidates, rows per thread)
     for (int i = 0; i < n; ++i) {
@@ -764,7 +765,8 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 const int uh = r.v_end - r.v_start;
                 // one item per unit; the CTA offset selects the row block
                 const int half = L.win / 2, srows = zf::stat_rows_host(L.win);
-                (L.win == 5 ? wl_st5 : wl_st7).add(i, pl, (int)u, 0, (uh + 2 * half + srows - 1) / srows);
+                (L.win == 5 ? (p.d.bd == 8 ? wl_st5 : wl_st5h) : wl_st7)
+                    .add(i, pl, (int)u, 0, (uh + 2 * half + srows - 1) / srows);
                 wl_unit.add(i, pl, (int)u, 0, 1);
                 if (L.refine) {
                     // one cluster per unit: the hill-climb is sequential, its trials are not
@@ -820,9 +822,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     };
     const size_t desc_bytes = (size_t)n * sizeof(FrameDesc);
     const size_t m_desc = mtake(desc_bytes);
-    constexpr int kLists = 9;
-    const WorkList *lists[kLists] = {&wl_db,   &wl_cs,    &wl_ca,    &wl_st5,  &wl_st7,
-                                     &wl_unit, &wl_apply, &wl_trial, &wl_tiles};
+    constexpr int kLists = 10;
+    const WorkList *lists[kLists] = {&wl_db,   &wl_cs,    &wl_ca,    &wl_st5,   &wl_st7,
+                                     &wl_unit, &wl_apply, &wl_trial, &wl_tiles, &wl_st5h};
     size_t m_list[kLists];
     for (int k = 0; k < kLists; ++k) m_list[k] = mtake(lists[k]->bytes());
     const size_t m_cf = mtake(cdef_frames.size() * 4);
@@ -854,7 +856,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     const size_t o_db = o_meta + m_list[0], o_cs = o_meta + m_list[1], o_ca = o_meta + m_list[2],
                  o_st5 = o_meta + m_list[3], o_st7 = o_meta + m_list[4], o_unit = o_meta + m_list[5],
                  o_apply = o_meta + m_list[6], o_trial = o_meta + m_list[7], o_tiles = o_meta + m_list[8],
-                 o_cf = o_meta + m_cf;
+                 o_st5h = o_meta + m_list[9], o_cf = o_meta + m_cf;
     // outputs start zeroed (statistics counters, fb_idx of skipped searches)
     CU(cudaMemsetAsync(base + o_out, 0, out_bytes, st));
 
@@ -1159,12 +1161,17 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         if (ucur) CU(cudaMemsetAsync(base + o_units, 0, ucur, st));
         if (wl_st5.ctas) {
             LaunchScope ls5_(ctx, "k_lr_stats5");
-            CU(zf::launch_lr_stats(5, wl_st5.ctas, st, d_desc, (const WorkItem *)(base + o_st5),
+            CU(zf::launch_lr_stats(5, 8, wl_st5.ctas, st, d_desc, (const WorkItem *)(base + o_st5),
                                    (int)wl_st5.items.size()));
+        }
+        if (wl_st5h.ctas) {
+            LaunchScope ls5h_(ctx, "k_lr_stats5");
+            CU(zf::launch_lr_stats(5, 10, wl_st5h.ctas, st, d_desc, (const WorkItem *)(base + o_st5h),
+                                   (int)wl_st5h.items.size()));
         }
         if (wl_st7.ctas) {
             LaunchScope ls7_(ctx, "k_lr_stats7");
-            CU(zf::launch_lr_stats(7, wl_st7.ctas, st, d_desc, (const WorkItem *)(base + o_st7),
+            CU(zf::launch_lr_stats(7, 0, wl_st7.ctas, st, d_desc, (const WorkItem *)(base + o_st7),
                                    (int)wl_st7.items.size()));
         }
         if (wl_unit.ctas) {
@@ -1455,7 +1462,7 @@ int32_t zf_query_sizes(const zf_frame *f, zf_sizes *out) {
     // coarse item indices: one int per 32 CTAs of a list (a 64x64 region
     // gives fewer than 64 CTAs over all lists) and two per list
     const size_t coarse = ((size_t)64 * p.d.nhfb * p.d.nvfb / 32 + 2 * 16) * sizeof(int);
-    const size_t meta = align_up(sizeof(FrameDesc), 256) + items * sizeof(WorkItem) + coarse + 11 * 256 + rcur;
+    const size_t meta = align_up(sizeof(FrameDesc), 256) + items * sizeof(WorkItem) + coarse + 12 * 256 + rcur;
     std::memset(out, 0, sizeof(*out));
     out->nhfb = p.d.nhfb;
     out->nvfb = p.d.nvfb;

@@ -36,7 +36,7 @@ cudaError_t launch_cdef_joint(int ncand, int rpt, int nframes, cudaStream_t st, 
 cudaError_t joint_set_attributes();
 __global__ void k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems);
 
-cudaError_t launch_lr_stats(int win, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
+cudaError_t launch_lr_stats(int win, int bd, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
                             int nitems);
 __global__ void k_lr_solve(FrameDesc *frames, const WorkItem *items, int nitems);
 __global__ void k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems);

@@ -96,7 +96,10 @@ __device__ __forceinline__ uint32_t bytes_at(uint32_t w0, uint32_t w1) {
     else return __byte_perm(w0, w1, 0x3210 + 0x1111 * K);
 }
 
-template <int WIN>
+// BD = 8 or 10: every frame of the launch has that bit depth, and only that
+// path is compiled (the 8-bit byte walks or the 16-bit scalar walks; one
+// kernel holding both took instruction-cache misses); BD = 0: either.
+template <int WIN, int BD>
 __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *frames, const WorkItem *items, int nitems) {
     using G = StatGeom<WIN>;
     constexpr int HALF = G::H, WIN2 = WIN * WIN;
@@ -125,7 +128,7 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
     LrUnit &u = pl.units[wi.a];
     const int bd = f.bd, stride = plane_stride(f, wi.plane);
     const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
-    const bool packed = WIN == 5 && bd == 8;
+    const bool packed = BD ? (WIN == 5 && BD == 8) : (WIN == 5 && bd == 8);
     uint8_t *Db = reinterpret_cast<uint8_t *>(D), *Xb = reinterpret_cast<uint8_t *>(X);
     const uint8_t *dg = f.A[wi.plane], *sr_ = f.S[wi.plane];
     // rows of this CTA in unit coordinates (extended range [-HALF, uh + HALF))
@@ -1813,10 +1816,12 @@ namespace zf {
 // Host-side launcher: the templated kernel is instantiated and launched in
 // this translation unit (whole-program compilation cannot launch a template
 // instantiation owned by another unit).
-cudaError_t launch_lr_stats(int win, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
+cudaError_t launch_lr_stats(int win, int bd, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
                             int nitems) {
-    if (win == 5) k_lr_stats<5><<<ctas, 256, 0, st>>>(frames, items, nitems);
-    else k_lr_stats<7><<<ctas, 256, 0, st>>>(frames, items, nitems);
+    if (win == 5 && bd == 8) k_lr_stats<5, 8><<<ctas, 256, 0, st>>>(frames, items, nitems);
+    else if (win == 5 && bd == 10) k_lr_stats<5, 10><<<ctas, 256, 0, st>>>(frames, items, nitems);
+    else if (win == 5) return cudaErrorInvalidValue;  // bit depths are 8 or 10
+    else k_lr_stats<7, 0><<<ctas, 256, 0, st>>>(frames, items, nitems);
     return cudaGetLastError();
 }
 }  // namespace zf
