@@ -233,7 +233,6 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
         const int y = y0 + t / G::NDR;
         // the row and its partner must lie in the extended range
         if (y + dr >= -HALF && y + dr < uh + HALF) {
-            const int dc0 = dr < 0 ? 1 : 0;  // dc = 0 only for dr >= 0
             int pre[WIN];
 #pragma unroll
             for (int k = 0; k < WIN; ++k) pre[k] = 0;
@@ -336,8 +335,9 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                 for (int dc = 0; dc < WIN; ++dc)
                     if (HALF + HALF + dc <= WIN - 1) rs[dc][2 * HALF] += pre[dc];
             }
-            // contributions: Hr[a][b], a = (ca, ra), b = (ca + dc, ra + dr)
-            (void)dc0;  // dc = 0 of a negative dr is dropped in the cross-row sums
+            // rs goes to the cross-row reduction after the walks, which adds
+            // it to Hr[a][b], a = (ca, ra), b = (ca + dc, ra + dr) (dc = 0 of
+            // a negative dr mirrors a positive dr and is dropped there)
         }
     } else if (t < nh + WIN * (xi1 - xi0)) {
         // ---- Mr and shift sums: one (unit row i, ra) per thread
