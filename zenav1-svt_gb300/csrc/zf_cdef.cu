@@ -150,7 +150,8 @@ __device__ void find_dirs(const uint16_t *reg, int rs, int cs, const int *blist,
 
 // Stage a plane window [y0-2, y0+n+2) x [x0-2, x0+n+2) with the sentinel
 // outside the aligned plane (build_src, cdef.rs:517-544).
-__device__ void load_region(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n, uint16_t *reg) {
+__device__ __noinline__ void load_region(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n,
+                                         uint16_t *reg) {
     const int rs = n + 4;
     stage_window(
         bd, pw, rs, x0 - 2, rs, false, kVeryLarge,
@@ -162,7 +163,8 @@ __device__ void load_region(const uint8_t *plane, int bd, int pw, int ph, int x0
 }
 
 // Stage the n x n source tile at (x0, y0), 0 outside the canvas.
-__device__ void load_src(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n, uint16_t *src) {
+__device__ __noinline__ void load_src(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n,
+                                      uint16_t *src) {
     stage_window(
         bd, pw, n, x0, n, false, 0,
         [&](int ry) { return y0 + ry < ph ? row_ptr(plane, y0 + ry, pw, bd) : (const uint8_t *)nullptr; },
