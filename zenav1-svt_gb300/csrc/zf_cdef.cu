@@ -1365,6 +1365,18 @@ int finish1_smem(int nfb, int ncand, int cap) {
 
 // ---- apply: one CTA per filter block, B (post-deblock) -> A -----------
 
+// Out-of-line copies of the direction search and the skip mask for the
+// apply, where they run once per filter block beside the hot filter loop
+// (inlined there they crowd it out of the instruction cache; the search
+// keeps them inlined, which measured faster for it).
+__device__ __noinline__ void find_dirs_ool(const uint16_t *reg, int rs, int cs, const int *blist, int nblk,
+                                           int (*cost)[8], int *sdir, int *svar) {
+    find_dirs(reg, rs, cs, blist, nblk, cost, sdir, svar);
+}
+__device__ __noinline__ uint64_t fb_dlist_ool(const FrameDesc &f, int fbr, int fbc, unsigned *part) {
+    return fb_dlist(f, fbr, fbc, part);
+}
+
 // Copy the n x n block at (x0, y0) of a pw x ph plane (clipped to it) from
 // src to dst: 4-byte words when both planes are word aligned (plane widths
 // and block columns are multiples of 4 samples, so a word never straddles
@@ -1410,7 +1422,7 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     const bool any = cp.bits != 0 || cp.y_str[0] != 0 || (f.chroma && cp.uv_str[0] != 0);
     __shared__ unsigned dl_part[2];
     if (threadIdx.x == 0) s_count = 0;  // ordered before its adds by the barriers below
-    const uint64_t dl_all = fb_dlist(f, fbr, fbc, dl_part);
+    const uint64_t dl_all = fb_dlist_ool(f, fbr, fbc, dl_part);
     if (threadIdx.x == 0) f.fb_row[fb] = dl_all != 0;
     const uint64_t dl = any ? dl_all : 0;
     if (dl == 0) {  // copy-through
@@ -1440,7 +1452,7 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     // directions: from this call's search of the same B when it ran (a
     // frame-uniform branch), else found here
     const bool have_dirs = f.cdir_ok != 0;
-    if (!have_dirs) find_dirs(reg, CR, cs, blist, nblk, dcost, sdir, svar);
+    if (!have_dirs) find_dirs_ool(reg, CR, cs, blist, nblk, dcost, sdir, svar);
     for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
         const int b = blist[k];
         int dir, t;
