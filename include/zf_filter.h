@@ -199,6 +199,16 @@ int32_t zf_submit_batch(zf_ctx *ctx, const zf_frame *frames, int32_t n,
  * pre-deblock rec; writes lf[4]. */
 int32_t zf_deblock_pick(zf_ctx *ctx, const zf_frame *f, uint8_t lf[4]);
 
+/* The trial of the deblock level search for a table of levels:
+ * try_filter_plane (deblock.rs:228-293) for each levels[k] (0..63; luma
+ * filters both edge directions at the level, as the search's dir = 2 does),
+ * i.e. the SSE between the source plane and the pre-deblock plane filtered
+ * at that level, over the full aligned plane. n <= 64; the whole table runs
+ * as one launch (the level search itself uses the same trials, several
+ * levels per launch). rec is not modified. */
+int32_t zf_deblock_sse_table(zf_ctx *ctx, const zf_frame *f, int32_t plane, const int32_t *levels, int32_t n,
+                             int64_t *sse);
+
 /* deblock::apply_deblock_frame[_hbd] (deblock.rs:938, :976): rec in place. */
 int32_t zf_deblock_apply(zf_ctx *ctx, const zf_frame *f, const uint8_t lf[4]);
 
@@ -206,6 +216,18 @@ int32_t zf_deblock_apply(zf_ctx *ctx, const zf_frame *f, const uint8_t lf[4]);
  * (cdef.rs:1166, :1374), the all-skip outcome (cdef.rs:282) or the qp
  * closed form (cdef.rs:151). Reads src and the post-deblock rec. */
 int32_t zf_cdef_search(zf_ctx *ctx, const zf_frame *f, zf_decisions *out);
+
+/* zf_cdef_search plus the search's per-filter-block mse rows, the values
+ * the reference's SVTAV1_CDEF_DBG dump prints (cdef_search_still[_hbd],
+ * cdef.rs:1166-1322): for filter block fb (raster order) with a non-skip
+ * 8x8, mse[fb * 2 * ncand + gi] is the luma SSE of candidate gi and
+ * mse[fb * 2 * ncand + ncand + gi] the joint U+V one, in candidate-slot
+ * order; has_row[fb] = 1 for those blocks, 0 for all-skip ones (whose rows
+ * are left untouched). mse must hold nhfb * nvfb * 2 * 48 entries and
+ * has_row nhfb * nvfb (either may be NULL); *ncand gets the candidate
+ * count, 0 when no search ran (presets >= 7: has_row is then all 0). */
+int32_t zf_cdef_search_rows(zf_ctx *ctx, const zf_frame *f, zf_decisions *out, uint64_t *mse, uint8_t *has_row,
+                            int32_t *ncand);
 
 /* cdef::apply_cdef_frame[_hbd] (cdef.rs:343, :556): rec in place (the
  * pre-CDEF snapshot is taken internally). */
@@ -226,26 +248,53 @@ int32_t zf_lr_apply(zf_ctx *ctx, const zf_frame *f, const void *const pre_cdef[3
  * Allocation-free CDEF strength search. No counterpart in the reference: it
  * computes the same decisions as zf_cdef_search, for callers that cannot
  * allocate device memory once running (an encoder loop that reserves all
- * memory at start-up, code running while a stream capture is open, a
- * process on a fully reserved GPU slice). It needs no zf_ctx and calls no
- * allocator: its scratch is a static device array of about 1 MiB that every
- * GPU loading the library keeps until exit.
+ * memory at start-up, code running while another component holds a stream
+ * capture open on a different stream, during which cudaMalloc is not
+ * allowed, a process on a fully reserved GPU slice). It needs no zf_ctx and
+ * calls no allocator: its scratch is a static device array of about 1.9 MiB
+ * (mse rows 640 KiB, compacted rows 1.25 MiB, ids 32 KiB) that every GPU
+ * loading the library keeps until exit.
  *  - f must have planes_on_device = 1: rec = post-deblock planes, src, mi
  *    are device pointers; out (and out->cdef_fb_idx) are host memory.
  *  - stream is a cudaStream_t (NULL: the legacy default stream); the call
- *    returns after synchronising it.
+ *    returns after synchronising it. The stream itself must not be capturing
+ *    (nor be the legacy stream while another stream captures in global
+ *    mode): such calls return ZF_ERR_UNSUPPORTED.
  *  - Limits: at most 2048 64x64 filter blocks (3840x2160 has 2040) ->
  *    ZF_ERR_INVALID_DIMS beyond; at most 20 candidate strengths (presets
  *    1..6; preset 0) -> ZF_ERR_UNSUPPORTED. Presets >= 7 return the qp
  *    closed form without device work.
- *  - The first call on a device looks up the array's device address with
- *    that device current; make that first call before any stream capture.
+ *  - The first call on a device (and the first after the device's context
+ *    was reset) looks up the array's device address with that device
+ *    current; make that first call before any stream capture.
  *  - All calls share the one array: calls that overlap on the GPU (other
  *    streams, other host threads) race and must be serialised by the caller.
  */
 int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_decisions *out);
 
 /* --- Observability ------------------------------------------------------- */
+
+/* Search trace, the counterpart of the reference's debug dumps
+ * SVTAV1_DLFDBG (deblock.rs:274-276, :406-408), SVTAV1_CDEF_DBG
+ * (cdef.rs:1296-1322) and SVTAV1_LR_DBG (restoration.rs:768-842), in the
+ * same line formats so that a trace of this library and one of the
+ * reference (or of a CPU restatement of it) diff line by line:
+ *   DLF_TRY plane= lvl0= lvl1= w= h= sse=      every level the hill-climb
+ *                                              evaluated, in climb order
+ *   DLF_PICK plane= dir= level= sse=
+ *   RS_CDEF_FB fbr= fbc= Y=[..] UV=[..]        per filter block with a row
+ *   RS_CDEF_SUM sb_count= fs=[..] Ysum=[..] UVsum=[..]
+ *   RS_CDEF_PICK bits= lev0=[..] lev1=[..]
+ *   LRNONE plane= unit= lim=[h0,h1,v0,v1] sse=  every unit, then per unit
+ *   LRWNSCORE plane= unit= score=
+ *   LRWNSEG plane= unit= sse_wn= v=[7 taps] h=[7 taps]   (score <= 0)
+ * (the reference's LRWNSOLVE and per-step LRSTEP lines are not produced:
+ * the refinement runs on the device without a per-step record). A batch
+ * call writes "ZF_FRAME index= w= h=" before each frame's lines. path
+ * "-" is stderr, NULL or "" stops tracing; the environment variable
+ * ZF_TRACE=<path> turns it on at zf_create. Tracing synchronises and reads
+ * the search buffers back after every call: a diagnostic mode. */
+int32_t zf_trace(zf_ctx *ctx, const char *path);
 
 /* ---- Frame-header filter syntax ------------------------------------------
  * The loop_filter_params(), cdef_params() and lr_params() fields of an

@@ -53,6 +53,9 @@ def lib():
     L.zfo_filter_stage.argtypes = [P(abi.ZfFrame), P(ZfoGeom), P(abi.ZfDecisions), P(abi.ZfStats), C.c_int32]
     L.zfo_deblock_pick.argtypes = [P(abi.ZfFrame), P(ZfoGeom), P(C.c_uint8)]
     L.zfo_deblock_apply.argtypes = [P(abi.ZfFrame), P(ZfoGeom), P(C.c_uint8)]
+    L.zfo_deblock_sse_table.argtypes = [P(abi.ZfFrame), P(ZfoGeom), C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
+    L.zfo_trace.argtypes = [C.c_char_p]
+    L.zfo_trace.restype = None
     L.zfo_cdef_search.argtypes = [P(abi.ZfFrame), P(ZfoGeom), P(abi.ZfDecisions), C.c_void_p, C.c_void_p,
                                   P(C.c_int32)]
     L.zfo_cdef_apply.argtypes = [P(abi.ZfFrame), P(ZfoGeom), P(abi.ZfDecisions), P(abi.ZfStats)]
@@ -138,6 +141,22 @@ def deblock_pick(fr, rec):
     lf = (C.c_uint8 * 4)()
     assert lib().zfo_deblock_pick(C.byref(s), C.byref(g), lf) == 0
     return list(lf)
+
+
+def deblock_sse_table(fr, plane, levels, rec=None):
+    """try_filter_plane's SSE of one plane at each level (int64 array)."""
+    rec = fr.rec if rec is None else rec
+    g = geom_struct(fr.geom)
+    s = _frame(fr, rec)
+    lv = np.ascontiguousarray(levels, np.int32)
+    out = np.zeros(len(lv), np.int64)
+    assert lib().zfo_deblock_sse_table(C.byref(s), C.byref(g), plane, lv.ctypes.data, len(lv), out.ctypes.data) == 0
+    return out
+
+
+def trace(path):
+    """Write the search trace lines to path (None stops)."""
+    lib().zfo_trace(None if path is None else path.encode())
 
 
 def deblock_apply(fr, rec, lf):

@@ -15,8 +15,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "../include/zf_av1_tables.h"
@@ -31,6 +33,20 @@ using u8 = uint8_t;
 using u16 = uint16_t;
 using u32 = uint32_t;
 using u64 = uint64_t;
+
+// Search trace (zfo_trace): the reference's SVTAV1_DLFDBG / SVTAV1_CDEF_DBG
+// / SVTAV1_LR_DBG lines (ENC/deblock.rs:274-276, :406-408; ENC/cdef.rs:
+// 1296-1322; ENC/restoration.rs:768-842), written where the reference
+// prints them.
+static FILE *g_trace = nullptr;
+template <typename T> static std::string list_str(const T *v, int n) {
+    std::string s = "[";
+    for (int i = 0; i < n; ++i) {
+        if (i) s += ", ";
+        s += std::to_string(v[i]);
+    }
+    return s + "]";
+}
 
 template <typename T> static inline T clampv(T v, T lo, T hi) { return v < lo ? lo : (v > hi ? hi : v); }
 static inline i32 iabs(i32 v) { return v < 0 ? -v : v; }
@@ -585,17 +601,31 @@ template <typename T>
 static void pick_levels_full_search(const T *const src[3], const T *const rec[3], int w, int h, bool chroma,
                                     const Geom &g, int conv_th, int sharpness, int bd, u8 out[4]) {
     std::vector<T> scratch;
+    i64 errs[3][64];
     auto try_plane = [&](int plane, int lvl) -> i64 {
         int pw = plane ? w / 2 : w, ph = plane ? h / 2 : h, ss = plane ? 1 : 0;
         scratch.assign(rec[plane], rec[plane] + (size_t)pw * ph);
         if (lvl != 0) filter_plane(scratch.data(), pw, pw, ph, plane, ss, lvl, lvl, g, sharpness, bd);
-        return plane_sse(src[plane], scratch.data(), pw, ph);
+        const i64 sse = plane_sse(src[plane], scratch.data(), pw, ph);
+        errs[plane][lvl] = sse;
+        if (g_trace)
+            std::fprintf(g_trace, "DLF_TRY plane=%d lvl0=%d lvl1=%d w=%d h=%d sse=%lld\n", plane, lvl, lvl, pw, ph,
+                         (long long)sse);
+        return sse;
+    };
+    auto pick_line = [&](int plane, int lvl) {
+        if (g_trace)
+            std::fprintf(g_trace, "DLF_PICK plane=%d dir=%d level=%d sse=%lld\n", plane, plane ? 0 : 2, lvl,
+                         (long long)errs[plane][lvl]);
     };
     int fy = search_filter_level([&](int l) { return try_plane(0, l); }, conv_th);
+    pick_line(0, fy);
     int fu = 0, fv = 0;
     if (fy != 0 && chroma) {
         fu = search_filter_level([&](int l) { return try_plane(1, l); }, conv_th);
+        pick_line(1, fu);
         fv = search_filter_level([&](int l) { return try_plane(2, l); }, conv_th);
+        pick_line(2, fv);
     }
     out[0] = (u8)fy;
     out[1] = (u8)fy;
@@ -1110,6 +1140,22 @@ static bool cdef_search_still(const CdefSearchCfg &cfg, const T *const rec[3], c
     std::vector<int> lev0, lev1;
     int bits = finish_cdef_rd(mse, n_cand, qindex, bd, lev0, lev1);
     int nb = 1 << bits;
+    if (g_trace) {
+        std::vector<u64> ysum(n_cand, 0), uvsum(n_cand, 0);
+        for (size_t i = 0; i < fb_addr.size(); ++i) {
+            std::fprintf(g_trace, "RS_CDEF_FB fbr=%d fbc=%d Y=%s UV=%s\n", fb_addr[i].first, fb_addr[i].second,
+                         list_str(mse[i].data(), n_cand).c_str(), list_str(mse[i].data() + n_cand, n_cand).c_str());
+            for (int gi = 0; gi < n_cand; ++gi) {
+                ysum[gi] += mse[i][gi];
+                uvsum[gi] += mse[i][n_cand + gi];
+            }
+        }
+        std::fprintf(g_trace, "RS_CDEF_SUM sb_count=%d fs=%s Ysum=%s UVsum=%s\n", (int)mse.size(),
+                     list_str(cfg.fs.data(), n_cand).c_str(), list_str(ysum.data(), n_cand).c_str(),
+                     list_str(uvsum.data(), n_cand).c_str());
+        std::fprintf(g_trace, "RS_CDEF_PICK bits=%d lev0=%s lev1=%s\n", bits, list_str(lev0.data(), nb).c_str(),
+                     list_str(lev1.data(), nb).c_str());
+    }
     pick->fb_idx.assign((size_t)nvfb * nhfb, 0);
     for (size_t i = 0; i < fb_addr.size(); ++i) {
         int best_gi = 0;
@@ -1883,6 +1929,9 @@ static void search_restoration(const WnCtrls &c, const T *const src[3], const T 
         foreach_rest_unit_in_tile(rect, hunits, unit_size, ss, [&](const TileLimits &lim, int ui) {
             sse_none[ui] = sse_region(s, (i64)lim.v_start * pw + lim.h_start, pw, r, (i64)lim.v_start * pw + lim.h_start,
                                       pw, lim.h_end - lim.h_start, lim.v_end - lim.v_start);
+            if (g_trace)
+                std::fprintf(g_trace, "LRNONE plane=%d unit=%d lim=[%d,%d,%d,%d] sse=%lld\n", plane, ui, lim.h_start,
+                             lim.h_end, lim.v_start, lim.v_end, (long long)sse_none[ui]);
         });
         foreach_rest_unit_in_tile(rect, hunits, unit_size, ss, [&](const TileLimits &lim, int ui) {
             int win2 = win * win;
@@ -1896,11 +1945,15 @@ static void search_restoration(const WnCtrls &c, const T *const src[3], const T 
             finalize_sym_filter(win, vd, wi.vfilter);
             finalize_sym_filter(win, hd, wi.hfilter);
             i64 score = compute_score(win, m.data(), hh.data(), wi.vfilter, wi.hfilter);
+            if (g_trace) std::fprintf(g_trace, "LRWNSCORE plane=%d unit=%d score=%lld\n", plane, ui, (long long)score);
             if (score > 0) {
                 sse_wn[ui] = INT64_MAX;
                 return;
             }
             i64 e = finer_tile_search_wiener(c, dgd, trial, s, pw, lim, rect, ss, wi, win, bd);
+            if (g_trace)
+                std::fprintf(g_trace, "LRWNSEG plane=%d unit=%d sse_wn=%lld v=%s h=%s\n", plane, ui, (long long)e,
+                             list_str(wi.vfilter, 7).c_str(), list_str(wi.hfilter, 7).c_str());
             sse_wn[ui] = e;
             wiener[ui] = wi;
         });
@@ -2458,6 +2511,34 @@ int32_t zfo_deblock_pick(const zf_frame *f, const zfo_geom *g, uint8_t lf[4]) {
     if (e) return e;
     Geom G = make_geom(f, g);
     return f->bit_depth == 8 ? deblock_pick_t<u8>(f, G, lf) : deblock_pick_t<u16>(f, G, lf);
+}
+
+void zfo_trace(const char *path) {
+    if (g_trace && g_trace != stderr) std::fclose(g_trace);
+    g_trace = nullptr;
+    if (!path || !*path) return;
+    g_trace = std::strcmp(path, "-") == 0 ? stderr : std::fopen(path, "w");
+}
+
+int32_t zfo_deblock_sse_table(const zf_frame *f, const zfo_geom *g, int32_t plane, const int32_t *levels, int32_t n,
+                              int64_t *sse) {
+    int e = validate(f);
+    if (e) return e;
+    Geom G = make_geom(f, g);
+    const int pw = plane ? f->width / 2 : f->width, ph = plane ? f->height / 2 : f->height, ss = plane ? 1 : 0;
+    for (int k = 0; k < n; ++k) {
+        const int lvl = levels[k];
+        if (f->bit_depth == 8) {
+            std::vector<u8> sc((const u8 *)f->rec[plane], (const u8 *)f->rec[plane] + (size_t)pw * ph);
+            if (lvl) filter_plane(sc.data(), pw, pw, ph, plane, ss, lvl, lvl, G, f->sharpness, 8);
+            sse[k] = plane_sse((const u8 *)f->src[plane], sc.data(), pw, ph);
+        } else {
+            std::vector<u16> sc((const u16 *)f->rec[plane], (const u16 *)f->rec[plane] + (size_t)pw * ph);
+            if (lvl) filter_plane(sc.data(), pw, pw, ph, plane, ss, lvl, lvl, G, f->sharpness, f->bit_depth);
+            sse[k] = plane_sse((const u16 *)f->src[plane], sc.data(), pw, ph);
+        }
+    }
+    return ZF_OK;
 }
 
 int32_t zfo_deblock_apply(const zf_frame *f, const zfo_geom *g, const uint8_t lf[4]) {

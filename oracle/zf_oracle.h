@@ -39,6 +39,14 @@ int32_t zfo_filter_stage(const zf_frame *f, const zfo_geom *g, zf_decisions *out
 /* Per-call-site pieces, same meaning as the zf_* functions. */
 int32_t zfo_deblock_pick(const zf_frame *f, const zfo_geom *g, uint8_t lf[4]);
 int32_t zfo_deblock_apply(const zf_frame *f, const zfo_geom *g, const uint8_t lf[4]);
+/* try_filter_plane (ENC/deblock.rs:228-293) of one plane at each of n
+ * levels (lvl0 = lvl1 = level): SSE vs the source over the aligned plane. */
+int32_t zfo_deblock_sse_table(const zf_frame *f, const zfo_geom *g, int32_t plane, const int32_t *levels, int32_t n,
+                              int64_t *sse);
+/* Search trace in the reference's debug-dump line formats (path "-" is
+ * stderr; NULL or "" stops): DLF_TRY / DLF_PICK, RS_CDEF_FB / RS_CDEF_SUM /
+ * RS_CDEF_PICK, LRNONE / LRWNSCORE / LRWNSEG. Process-wide. */
+void zfo_trace(const char *path);
 /* mse_out (optional): per filter block in raster order, 2*ncand u64
  * ([luma row][joint uv row]); rows of all-skip fbs are left untouched and
  * fb_has_row[fb] (optional) says which ones were written. */

@@ -1,13 +1,15 @@
 """zf_cdef_search_noalloc: the allocation-free CDEF strength search.
 
 Callers that cannot allocate device memory once running (an encoder loop
-that reserves everything at start-up, code running under an open stream
-capture, a process on a fully reserved GPU slice) use this entry point; it
+that reserves everything at start-up, code running while another stream is
+being captured, a process on a fully reserved GPU slice) use this entry
+point; it
 keeps its scratch in a static device array instead of a context arena. These
 tests call it through the C ABI and check it against the existing
-zf_cdef_search entry point -- the integer decisions must be identical -- on
-two calls in a row (the shared static scratch keeps the previous call's
-contents, which must not leak into the next result).
+zf_cdef_search entry point and the oracle -- the integer decisions must be
+identical -- on two calls in a row per frame (the shared static scratch
+keeps the previous call's contents, which must not leak into the next
+result).
 
 This file is collected last so that a run stopping at the first failure has
 already run every other test.
@@ -48,19 +50,53 @@ def _same(a, b):
     assert (a["cdef_fb_idx"] == b["cdef_fb_idx"]).all()
 
 
-def test_noalloc_search_matches_cdef_search_twice(pkg, ctx):
+NOALLOC_FRAMES = [
+    # (seed, w, h, bd, qp, preset, content): 4 candidates (single CTA rows),
+    # 6 candidates, 20 candidates (preset 2), and the largest frame the
+    # scratch takes (3840x2160: 2040 filter blocks, the 8-CTA cluster's
+    # biggest per-CTA share of rows) at presets 4 and 2
+    (synth.frame_seed(12, 1), 1000, 600, 8, 44, 6, "cosine"),
+    (synth.frame_seed(12, 2), 512, 384, 10, 30, 4, "power10"),
+    (synth.frame_seed(12, 3), 640, 480, 8, 30, 2, "cosine"),
+    (synth.frame_seed(2, 1), 3840, 2160, 8, 40, 4, "power"),
+    (synth.frame_seed(2, 5), 3840, 2160, 8, 28, 2, "power"),
+]
+
+
+def test_noalloc_search_matches_cdef_search_twice(pkg, ctx, oracle):
+    """Each frame searched twice in a row through the allocation-free entry
+    point: equal to zf_cdef_search and to the oracle both times."""
     L = _bind(pkg)
-    frames = [synth.make_frame(synth.frame_seed(12, 1), 1000, 600, 8, 44, 6, "cosine"),
-              synth.make_frame(synth.frame_seed(12, 2), 512, 384, 10, 30, 4, "power10")]
-    for fr in frames:
+    for args in NOALLOC_FRAMES:
+        fr = synth.make_frame(*args)
         mi = pkg.pack_geom(fr.geom)
         want = ctx.cdef_search_still(fr, fr.copy_rec(), mi=mi).as_dict()
+        ref = oracle.cdef_search(fr, fr.copy_rec())[0].as_dict()
+        _same(want, ref)
         s, keep = _on_device(fr, mi)
-        got = abi.Decisions(fr.w, fr.h, fr.true_w, fr.true_h)
-        rc = L.zf_cdef_search_noalloc(None, C.byref(s), C.byref(got.c))
-        assert rc == 0, rc
-        _same(got.as_dict(), want)
+        for _ in range(2):
+            got = abi.Decisions(fr.w, fr.h, fr.true_w, fr.true_h)
+            rc = L.zf_cdef_search_noalloc(None, C.byref(s), C.byref(got.c))
+            assert rc == 0, rc
+            _same(got.as_dict(), want)
+            _same(got.as_dict(), ref)
         del keep
+
+
+def test_noalloc_refuses_a_capturing_stream(pkg):
+    """The call synchronises its stream, so a stream under capture is
+    refused instead of being invalidated."""
+    import torch
+    L = _bind(pkg)
+    fr = synth.make_frame(*NOALLOC_FRAMES[0])
+    s, keep = _on_device(fr, pkg.pack_geom(fr.geom))
+    side = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    d = abi.Decisions(fr.w, fr.h, fr.true_w, fr.true_h)
+    with torch.cuda.graph(g, stream=side):
+        rc = L.zf_cdef_search_noalloc(C.c_void_p(side.cuda_stream), C.byref(s), C.byref(d.c))
+    assert rc == -3  # UnsupportedConfig
+    del keep
 
 
 def test_noalloc_rejects_frames_beyond_its_limits(pkg):

@@ -66,6 +66,10 @@ def lib():
     L.zf_submit_batch.argtypes = [C.c_void_p, P(ZfFrame), C.c_int32, P(ZfDecisions), P(ZfStats)]
     L.zf_deblock_pick.argtypes = [C.c_void_p, P(ZfFrame), P(C.c_uint8)]
     L.zf_deblock_apply.argtypes = [C.c_void_p, P(ZfFrame), P(C.c_uint8)]
+    L.zf_deblock_sse_table.argtypes = [C.c_void_p, P(ZfFrame), C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
+    L.zf_cdef_search_rows.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions), C.c_void_p, C.c_void_p,
+                                      P(C.c_int32)]
+    L.zf_trace.argtypes = [C.c_void_p, C.c_char_p]
     L.zf_cdef_search.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions)]
     L.zf_cdef_apply.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions), P(ZfStats)]
     L.zf_lr_search.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions)]
@@ -110,6 +114,7 @@ def lib():
     for name in ("zf_lr_corners_in_sb", "zf_lr_sb_syntax", "zf_get_tune", "zf_set_tune", "zf_autotune", "zf_use_graphs", "zf_graph_stats", "zf_superres_scaled_size", "zf_superres_upscale", "zf_film_grain_estimate",
                  "zf_film_grain_synthesize", "zf_write_filter_params", "zf_sgr_search", "zf_sgr_apply", "zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
                  "zf_submit_batch", "zf_deblock_pick", "zf_deblock_apply", "zf_cdef_search",
+                 "zf_deblock_sse_table", "zf_cdef_search_rows", "zf_trace",
                  "zf_cdef_apply", "zf_lr_search", "zf_lr_apply"):
         getattr(L, name).restype = C.c_int32
     _lib = L
@@ -274,6 +279,37 @@ class Context:
         lf = (C.c_uint8 * 4)()
         self._check(lib().zf_deblock_pick(self.h, C.byref(s), lf))
         return list(lf)
+
+    def deblock_sse_table(self, fr, plane, levels, rec=None, mi=None):
+        """try_filter_plane's SSE of one plane at each level, one launch
+        (zf_deblock_sse_table); rec is the pre-deblock recon."""
+        mi = pack_geom(fr.geom) if mi is None else mi
+        rec = fr.rec if rec is None else rec
+        s = abi.make_frame_struct(fr, fr.src, rec, mi)
+        lv = np.ascontiguousarray(levels, np.int32)
+        out = np.zeros(len(lv), np.int64)
+        self._check(lib().zf_deblock_sse_table(self.h, C.byref(s), plane, lv.ctypes.data, len(lv),
+                                               out.ctypes.data))
+        return out
+
+    def cdef_search_rows(self, fr, rec, mi=None):
+        """zf_cdef_search_rows on the post-deblock recon: (Decisions, mse rows
+        [nfb, 2 * ncand] or None, has_row [nfb])."""
+        mi = pack_geom(fr.geom) if mi is None else mi
+        s = abi.make_frame_struct(fr, fr.src, rec, mi)
+        d = Decisions(fr.w, fr.h, fr.true_w, fr.true_h)
+        nfb = d.nhfb * d.nvfb
+        flat = np.zeros(nfb * 2 * 48, np.uint64)
+        has = np.zeros(nfb, np.uint8)
+        nc = C.c_int32()
+        self._check(lib().zf_cdef_search_rows(self.h, C.byref(s), C.byref(d.c), flat.ctypes.data, has.ctypes.data,
+                                              C.byref(nc)))
+        n = nc.value
+        return d, (flat[:nfb * 2 * n].reshape(nfb, 2 * n) if n else None), has
+
+    def trace(self, path):
+        """Search trace lines to path ("-" stderr, None stops): zf_trace."""
+        self._check(lib().zf_trace(self.h, None if path is None else path.encode()))
 
     def apply_deblock_frame(self, fr, rec, lf, mi=None):
         mi = pack_geom(fr.geom) if mi is None else mi

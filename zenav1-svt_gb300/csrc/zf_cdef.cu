@@ -13,6 +13,8 @@
 #include <algorithm>
 #include <mutex>
 
+#include <cuda.h>
+
 #include <cooperative_groups.h>
 
 #include "zf_dev.cuh"
@@ -1552,14 +1554,16 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
 // Some callers cannot allocate device memory once they are running: an
 // encoder loop that reserves every byte at start-up and must not touch the
 // allocator per frame, code that runs while another component holds a
-// stream capture open (cudaMalloc is not allowed then), or a process on a
-// GPU slice whose memory is already fully reserved. For them this entry
-// point runs the same two kernels as zf_cdef_search, with all scratch in the
-// file-scope array below instead of a context arena. The array is modest
-// (about 1 MiB) and every GPU that loads the library holds it until the
-// process exits. Limits: at most kNoAllocMaxFb 64x64 filter blocks (a
-// 3840x2160 frame has 2040) and at most kNoAllocMaxCand candidate strengths
-// (presets 1..6; preset 0's 48 candidates are rejected).
+// stream capture open on a different stream (cudaMalloc is not allowed
+// then), or a process on a GPU slice whose memory is already fully
+// reserved. For them this entry point runs the same two kernels as
+// zf_cdef_search, with all scratch in the file-scope array below instead of
+// a context arena. The array is sizeof(NoAllocScratch), about 1.9 MiB
+// (mse rows 640 KiB, compacted rows 1.25 MiB, ids 32 KiB), and every GPU
+// that loads the library holds it until the process exits. Limits: at most
+// kNoAllocMaxFb 64x64 filter blocks (a 3840x2160 frame has 2040) and at
+// most kNoAllocMaxCand candidate strengths (presets 1..6; preset 0's 48
+// candidates are rejected).
 // ===========================================================================
 
 #include <mutex>
@@ -1584,13 +1588,37 @@ struct NoAllocScratch {
     uint8_t fb_idx[kNoAllocMaxFb];
 };
 
+static_assert(sizeof(NoAllocScratch) < 2u * 1024 * 1024, "allocation-free scratch stays below 2 MiB");
+
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
-// Device address of g_noalloc_scratch per device, looked up on the first
-// call made with that device current.
+// Device address of g_noalloc_scratch, looked up with cudaGetSymbolAddress
+// on the first call made with a device current and again whenever that
+// device's current context changed since (a cudaDeviceReset or any other
+// teardown of the primary context reloads the module at a new address).
 constexpr int kMaxDevices = 64;
-static NoAllocScratch *g_noalloc_addr[kMaxDevices];
+struct NoAllocAddr {
+    CUcontext ctx;
+    NoAllocScratch *ptr;
+};
+static NoAllocAddr g_noalloc_addr[kMaxDevices];
 static std::mutex g_noalloc_mu;
+
+// cuCtxGetCurrent from the driver (the library links the runtime only).
+static CUresult current_context(CUcontext *out) {
+    using Fn = CUresult (*)(CUcontext *);
+    static Fn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<Fn>(p);
+    }();
+    return fn ? fn(out) : CUDA_ERROR_NOT_FOUND;
+}
 }  // namespace zf
 
 extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_decisions *out) {
@@ -1617,20 +1645,35 @@ extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_de
     if (d.cdef.ncand > kNoAllocMaxCand) return ZF_ERR_UNSUPPORTED;  // preset 0
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return ZF_ERR_CUDA;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // The call synchronises its stream and copies from host stack memory, so
+    // it cannot be recorded into a graph: refuse a stream that is capturing
+    // (or the legacy stream while another stream captures in global mode).
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return ZF_ERR_UNSUPPORTED;
+    }
     NoAllocScratch *sc;
     {
         std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_addr[dev]) {
+        CUcontext cur = nullptr;
+        if (current_context(&cur) != CUDA_SUCCESS) cur = nullptr;
+        NoAllocAddr &a = g_noalloc_addr[dev];
+        if (!a.ptr || !cur || a.ctx != cur) {
             void *p = nullptr;
             if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
                 cudaGetLastError();
+                a.ptr = nullptr;
                 return ZF_ERR_CUDA;
             }
-            g_noalloc_addr[dev] = static_cast<NoAllocScratch *>(p);
+            // the runtime may have created the primary context just now
+            if (!cur && current_context(&cur) != CUDA_SUCCESS) cur = nullptr;
+            a.ctx = cur;
+            a.ptr = static_cast<NoAllocScratch *>(p);
         }
-        sc = g_noalloc_addr[dev];
+        sc = a.ptr;
     }
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     for (int p = 0; p < 3; ++p) {
         const bool on = p == 0 || f->chroma_420;
         d.B[p] = on ? (uint8_t *)f->rec[p] : nullptr;

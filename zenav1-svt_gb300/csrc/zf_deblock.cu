@@ -390,10 +390,12 @@ __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, 
 
 // Level search: SSE(source, plane filtered at level L in both directions)
 // over the full aligned plane (try_filter_plane, deblock.rs:228-293), for
-// up to two candidate levels per launch. items[].a = index of the (frame,
-// plane) search slot; sse[slot * 2 + k] accumulates level levels[slot*2+k].
+// up to kDbLevels candidate levels per (frame, plane) slot and launch: the
+// tile and its halo are staged once and filtered at every level of the
+// slot. items[].a = slot index; levels[slot * nl + k] (< 0: unused) and
+// sse[slot * nl + k] the SSE accumulated for it.
 __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, const WorkItem *items, int nitems,
-                                                     const int *levels, unsigned long long *sse) {
+                                                     const int *levels, int nl, unsigned long long *sse) {
     __shared__ __align__(16) uint16_t reg[DB_R * DB_R];
     __shared__ __align__(16) uint16_t pristine[DB_R * DB_R];
     __shared__ DbEdges edges;
@@ -410,12 +412,14 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
     const int bd = f.bd;
     db_load(t, f.IN[plane], pristine);
     // edge lengths do not depend on a nonzero level: computed once
-    if (levels[slot * 2] > 0 || levels[slot * 2 + 1] > 0) db_params(t, 1, 1, edges);
+    bool any = false;
+    for (int k = 0; k < nl; ++k) any = any || levels[slot * nl + k] > 0;
+    if (any) db_params(t, 1, 1, edges);
     __syncthreads();
     const int spw = bd == 8 ? 4 : 2, wpr = DB_T / spw, lgw = bd == 8 ? 4 : 5;  // wpr = 1 << lgw
     const bool words = word_ok(f.S[plane]);
-    for (int k = 0; k < 2; ++k) {
-        const int lvl = levels[slot * 2 + k];
+    for (int k = 0; k < nl; ++k) {
+        const int lvl = levels[slot * nl + k];
         if (lvl < 0) continue;
         for (int i = threadIdx.x; i < DB_R * DB_R / 2; i += blockDim.x)
             reinterpret_cast<uint32_t *>(reg)[i] = reinterpret_cast<const uint32_t *>(pristine)[i];
@@ -452,7 +456,7 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
         if (threadIdx.x == 0) {
             unsigned long long s = 0;
             for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += part[w];
-            atomicAdd(&sse[slot * 2 + k], s);
+            atomicAdd(&sse[slot * nl + k], s);
         }
         __syncthreads();
     }

@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -58,6 +59,10 @@ struct zf_ctx {
     bool capturing = false;
     bool tma = true;  // statistics kernel rows by TMA where the planes allow
     int apply_group = 8;  // 64-px column tiles per restoration-apply CTA
+    // search trace (zf_trace / ZF_TRACE): one text line per trial, filter
+    // block and restoration unit in the reference's debug-dump formats
+    FILE *trace = nullptr;
+    bool trace_owned = false;
     cudaGraphExec_t gexec = nullptr;
     std::vector<uint64_t> gsig;  // node kinds, kernel functions and cluster shapes of gexec's graph
     uint64_t graph_launches = 0, graph_updates = 0, graph_instantiations = 0;
@@ -121,6 +126,19 @@ enum : unsigned {
 // Where the caller's rec[] goes in, and which plane set comes back out.
 enum PlaneSet { SET_A = 0, SET_B = 1, SET_C = 2 };
 
+// zf_deblock_sse_table's request: SSE of one plane at each of n levels.
+struct DbTable {
+    int plane, n;
+    const int32_t *levels;
+    int64_t *sse;
+};
+// zf_cdef_search_rows' outputs (caller arrays; see the header).
+struct CdefRows {
+    uint64_t *mse;
+    uint8_t *has_row;
+    int32_t *ncand;
+};
+
 struct Run {
     unsigned stages;
     PlaneSet rec_in;
@@ -130,6 +148,8 @@ struct Run {
     bool lf_given;          // decisions provided by the caller
     bool cdef_given;
     bool lr_given;
+    DbTable *table = nullptr;    // zf_deblock_sse_table: trials of the caller's levels
+    CdefRows *rows = nullptr;    // zf_cdef_search_rows: the search's mse rows
 };
 
 int fail(zf_ctx *ctx, int code, const std::string &msg) {
@@ -277,13 +297,15 @@ void rest_units(int pw, int ph, int ss, std::vector<UnitRect> &out) {
 // The deblock level hill-climb of search_filter_level (deblock.rs:307-411)
 // replayed over the SSEs measured so far: returns the levels that the next
 // step needs (both candidates of a step are requested together), or marks
-// the search done.
+// the search done. The state where it stopped (mid level, step, direction)
+// is left in the fields for speculate().
 struct HillClimb {
     int64_t err[64];
     bool have[64];
     int conv_th = 0;
     bool done = false;
     int result = 0;
+    int at_mid = 0, at_step = 4, at_dir = 0;
     HillClimb() {
         for (int i = 0; i < 64; ++i) {
             err[i] = 0;
@@ -291,10 +313,12 @@ struct HillClimb {
         }
     }
     int needs(int out[2]) {
+        at_mid = 0;
+        at_step = 4;
+        at_dir = 0;
         if (!have[0]) {
             out[0] = 0;
-            out[1] = 4;
-            return 2;
+            return 1;
         }
         int dir = 0, mid = 0, step = 4, best = 0, conv = 0;
         int64_t best_err = err[0];
@@ -306,7 +330,12 @@ struct HillClimb {
             int n = 0;
             if (need_lo && !have[lo]) out[n++] = lo;
             if (need_hi && !have[hi]) out[n++] = hi;
-            if (n) return n;
+            if (n) {
+                at_mid = mid;
+                at_step = step;
+                at_dir = dir;
+                return n;
+            }
             if (need_lo && err[lo] < best_err + bias) {
                 if (err[lo] < best_err) best_err = err[lo];
                 best = lo;
@@ -329,7 +358,85 @@ struct HillClimb {
         result = best;
         return 0;
     }
+    // The levels the finished climb evaluated, in the order
+    // search_filter_level calls try_filter_frame.
+    void trial_order(std::vector<int> &out) const {
+        out.clear();
+        bool seen[64] = {};
+        auto visit = [&](int l) {
+            if (!seen[l]) out.push_back(l);
+            seen[l] = true;
+        };
+        visit(0);
+        int dir = 0, mid = 0, step = 4, best = 0, conv = 0;
+        int64_t best_err = err[0];
+        while (step > 0) {
+            const int hi = std::min(mid + step, 63), lo = std::max(mid - step, 0);
+            int64_t bias = (best_err >> (15 - (mid / 8))) * (int64_t)step;
+            bias >>= 1;
+            if (dir <= 0 && lo != mid) {
+                visit(lo);
+                if (err[lo] < best_err + bias) {
+                    if (err[lo] < best_err) best_err = err[lo];
+                    best = lo;
+                }
+            }
+            if (dir >= 0 && hi != mid) {
+                visit(hi);
+                if (err[hi] < best_err - bias) {
+                    best_err = err[hi];
+                    best = hi;
+                }
+            }
+            if (best == mid) {
+                conv += 1;
+                if (conv == conv_th) step = 0;
+                else step /= 2;
+                dir = 0;
+            } else {
+                dir = best < mid ? -1 : 1;
+                mid = best;
+            }
+        }
+    }
 };
+
+// Levels to evaluate in one trial launch for a climb that needs `need`:
+// the needed levels, then speculatively the levels the next steps may ask
+// for -- the continuation of the climb at its current step in the needed
+// directions (mid +- 2 step, +- 3 step, ...) and, when the climb refines
+// after converging (conv_th != 1), the half and quarter steps around the
+// current mid. Only the needed levels decide anything; the others are cached
+// SSEs that save a launch and a host round trip when the climb reaches them.
+void speculate(const HillClimb &hc, const int *need, int m, int cap, std::vector<int> &lv) {
+    lv.clear();
+    bool in[64] = {};
+    auto add = [&](int l) {
+        if ((int)lv.size() >= cap || l < 0 || l > 63 || in[l] || hc.have[l]) return;
+        in[l] = true;
+        lv.push_back(l);
+    };
+    for (int k = 0; k < m; ++k) add(need[k]);
+    const int mid = hc.at_mid, step = hc.at_step;
+    bool up = false, down = false;
+    for (int k = 0; k < m; ++k) {
+        up = up || need[k] > mid || (need[k] == 0 && mid == 0);
+        down = down || need[k] < mid;
+    }
+    for (int k = 1; k <= 16 && (int)lv.size() < cap; ++k) {
+        if (up) add(mid + k * step);
+        if (down) add(mid - k * step);
+        if (hc.conv_th != 1 && k == 2) {
+            add(mid + step / 2);
+            add(mid - step / 2);
+        }
+        if (hc.conv_th != 1 && k == 3) {
+            add(mid + step / 4);
+            add(mid - step / 4);
+        }
+        if (!up && !down) break;
+    }
+}
 
 // ---- per-frame plan -------------------------------------------------------
 
@@ -725,12 +832,118 @@ int launch_captured(zf_ctx *ctx, CaptureGuard &cg) {
     return ZF_OK;
 }
 
+// Rust {:?} of a slice: "[a, b, c]".
+template <typename T> std::string list_str(const T *v, int n) {
+    std::string s = "[";
+    for (int i = 0; i < n; ++i) {
+        if (i) s += ", ";
+        s += std::to_string(v[i]);
+    }
+    return s + "]";
+}
+
+// After a call: the CDEF search's mse rows for zf_cdef_search_rows, and the
+// search trace lines (the reference's SVTAV1_CDEF_DBG and SVTAV1_LR_DBG
+// dumps, cdef.rs:1296-1322, restoration.rs:768-842) read back from the
+// arena. Debug and diff aids only: they synchronise and copy.
+int search_records(zf_ctx *ctx, std::vector<Plan> &plans, const FrameDesc *back, const uint8_t *ob, const Run &run,
+                   std::vector<std::vector<std::string>> &p_trace) {
+    const int n = (int)plans.size();
+    cudaStream_t st = ctx->stream;
+    for (int i = 0; i < n; ++i) {
+        Plan &p = plans[i];
+        const FrameDesc &b = back[i];
+        const bool cdef_searched = (run.stages & STG_CDEF_SEARCH) && !run.cdef_given && p.d.cdef.mode == 1;
+        const int nc = p.d.cdef.ncand;
+        const uint8_t *fbrow = ob + p.off_fbrow;
+        std::vector<uint64_t> mse;
+        if (cdef_searched) {
+            mse.resize((size_t)p.nfb * 2 * nc);
+            CU(cudaMemcpyAsync(mse.data(), p.d.mse, mse.size() * 8, cudaMemcpyDeviceToHost, st));
+            CU(cudaStreamSynchronize(st));
+        }
+        if (run.rows && i == 0) {
+            *run.rows->ncand = cdef_searched ? nc : 0;
+            for (int fb = 0; fb < p.nfb; ++fb) {
+                const bool has = cdef_searched && fbrow[fb];
+                if (run.rows->has_row) run.rows->has_row[fb] = has ? 1 : 0;
+                if (run.rows->mse && has) std::memcpy(run.rows->mse + (size_t)fb * 2 * nc, &mse[(size_t)fb * 2 * nc], 2 * nc * 8);
+            }
+        }
+        if (!ctx->trace) continue;
+        std::vector<std::string> &T = p_trace[i];
+        if (cdef_searched) {
+            std::vector<uint64_t> ysum(nc, 0), uvsum(nc, 0);
+            int sbc = 0;
+            for (int fb = 0; fb < p.nfb; ++fb) {
+                if (!fbrow[fb]) continue;
+                const uint64_t *r = &mse[(size_t)fb * 2 * nc];
+                T.push_back("RS_CDEF_FB fbr=" + std::to_string(fb / p.d.nhfb) + " fbc=" + std::to_string(fb % p.d.nhfb) +
+                            " Y=" + list_str(r, nc) + " UV=" + list_str(r + nc, nc));
+                for (int g = 0; g < nc; ++g) {
+                    ysum[g] += r[g];
+                    uvsum[g] += r[nc + g];
+                }
+                ++sbc;
+            }
+            if (sbc) {
+                T.push_back("RS_CDEF_SUM sb_count=" + std::to_string(sbc) + " fs=" + list_str(p.d.cdef.fs, nc) +
+                            " Ysum=" + list_str(ysum.data(), nc) + " UVsum=" + list_str(uvsum.data(), nc));
+                const int bits = b.cdef.bits, nb = 1 << bits;
+                int l0[8], l1[8];
+                for (int k = 0; k < nb; ++k) {
+                    l0[k] = b.fin_lev[bits][k];
+                    l1[k] = b.fin_lev[bits][8 + k];
+                }
+                T.push_back("RS_CDEF_PICK bits=" + std::to_string(bits) + " lev0=" + list_str(l0, nb) +
+                            " lev1=" + list_str(l1, nb));
+            }
+        }
+        const bool lr_searched = (run.stages & STG_LR_SEARCH) && !run.lr_given;
+        for (int pl = 0; lr_searched && pl < 3; ++pl) {
+            const LrPlane &L = p.d.lr[pl];
+            if (!L.on) continue;
+            const size_t nu = p.rects[pl].size();
+            std::vector<LrUnit> U(nu);
+            CU(cudaMemcpyAsync(U.data(), L.units, nu * sizeof(LrUnit), cudaMemcpyDeviceToHost, st));
+            CU(cudaStreamSynchronize(st));
+            for (size_t u = 0; u < nu; ++u) {
+                const UnitRect &r = p.rects[pl][u];
+                T.push_back("LRNONE plane=" + std::to_string(pl) + " unit=" + std::to_string(u) + " lim=[" +
+                            std::to_string(r.h_start) + "," + std::to_string(r.h_end) + "," + std::to_string(r.v_start) +
+                            "," + std::to_string(r.v_end) + "] sse=" + std::to_string(U[u].sse_none));
+            }
+            for (size_t u = 0; u < nu; ++u) {
+                const LrUnit &x = U[u];
+                T.push_back("LRWNSCORE plane=" + std::to_string(pl) + " unit=" + std::to_string(u) +
+                            " score=" + std::to_string(x.score));
+                if (x.score > 0) continue;
+                const int64_t sse = L.refine ? x.sse_wn
+                                    : p.d.bd == 8 ? (int64_t)(x.tw_blk + x.tw_rgt + x.tw_bot)
+                                                  : (int64_t)x.tw_blk + (int64_t)(uint32_t)x.tw_rgt +
+                                                        (int64_t)(uint32_t)x.tw_bot;
+                T.push_back("LRWNSEG plane=" + std::to_string(pl) + " unit=" + std::to_string(u) + " sse_wn=" +
+                            std::to_string(sse) + " v=" + list_str(x.vf, 7) + " h=" + list_str(x.hf, 7));
+            }
+        }
+    }
+    if (ctx->trace) {
+        for (int i = 0; i < n; ++i) {
+            if (n > 1) std::fprintf(ctx->trace, "ZF_FRAME index=%d w=%d h=%d\n", i, plans[i].d.tw, plans[i].d.th);
+            for (const std::string &l : p_trace[i]) std::fprintf(ctx->trace, "%s\n", l.c_str());
+        }
+        std::fflush(ctx->trace);
+    }
+    return ZF_OK;
+}
+
 int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf_stats *stats, const Run &run) {
     if (!ctx) return ZF_ERR_ARG;
     if (n <= 0 || !frames) return fail(ctx, ZF_ERR_ARG, "empty batch");
     CU(cudaSetDevice(ctx->device));
     TRY(check_cancel(ctx));
     std::vector<Plan> plans((size_t)n);
+    std::vector<std::vector<std::string>> p_trace((size_t)n);  // trace lines per frame
     size_t cursor = 0, ucur = 0, rcur = 0, ocur = 0;
     for (int i = 0; i < n; ++i) {
         TRY(validate_frame(ctx, &frames[i]));
@@ -831,17 +1044,19 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     const size_t m_rects = mtake(rcur);
     const size_t m_tm = mtake((size_t)n * 3 * 256);  // per frame and plane: post-CDEF and source tensor maps
     const size_t meta_bytes = align_up(mcur, 256);
-    // deblock search scratch: up to 3 slots per frame, each of at most the
-    // largest frame's luma tiles (items, then their coarse index)
+    // deblock search scratch: up to 3 slots per frame (8 for a table of
+    // all 64 levels), each of at most the largest frame's luma tiles
+    // (items, then their coarse index), kDbLevels levels and SSEs per slot
     size_t max_tiles = 1;
     for (const Plan &p : plans) max_tiles = std::max(max_tiles, (size_t)((p.d.w + 63) / 64) * ((p.d.h + 63) / 64));
     size_t c2 = o_meta + meta_bytes;
+    const size_t db_slots = std::max<size_t>((size_t)n * 3, (64 + zf::kDbLevels - 1) / zf::kDbLevels);
     const size_t o_dbs_items = c2;
-    c2 += align_up((size_t)n * 3 * sizeof(WorkItem) + ((size_t)n * 3 * max_tiles / 32 + 2) * sizeof(int) + 16, 256);
+    c2 += align_up(db_slots * sizeof(WorkItem) + (db_slots * max_tiles / 32 + 2) * sizeof(int) + 16, 256);
     const size_t o_dbs_lv = c2;
-    c2 += align_up((size_t)n * 3 * 2 * 4, 256);
+    c2 += align_up(db_slots * zf::kDbLevels * 4, 256);
     const size_t o_dbs_sse = c2;
-    c2 += align_up((size_t)n * 3 * 2 * 8, 256);
+    c2 += align_up(db_slots * zf::kDbLevels * 8, 256);
     const size_t o_out = c2;
     const size_t out_bytes = align_up(ocur, 256);
     c2 += out_bytes;
@@ -948,7 +1163,66 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         }
     }
 
-    // ---- deblock level pick (presets <= 5: device SSE trials + host hill-climb)
+    // ---- deblock level pick (presets <= 5: device SSE trials + host
+    // hill-climb), or the caller's table of trial levels
+    // Trials: one launch evaluates every slot (frame, plane, up to
+    // kDbLevels levels) over all tiles of its plane.
+    struct TrialSlot {
+        int frame, plane;
+        std::vector<int> levels;
+        std::vector<int64_t> sse;
+    };
+    auto run_trials = [&](std::vector<TrialSlot> &ts) -> int {
+        WorkList wl;
+        std::vector<int> lv(ts.size() * zf::kDbLevels, -1);
+        for (size_t k = 0; k < ts.size(); ++k) {
+            const Plan &p = plans[ts[k].frame];
+            for (size_t j = 0; j < ts[k].levels.size(); ++j) lv[k * zf::kDbLevels + j] = ts[k].levels[j];
+            const int pw = ts[k].plane ? p.d.w / 2 : p.d.w, ph = ts[k].plane ? p.d.h / 2 : p.d.h;
+            wl.add(ts[k].frame, ts[k].plane, (int)k, 0, ((pw + 63) / 64) * ((ph + 63) / 64));
+        }
+        if (ts.size() > db_slots) return fail(ctx, ZF_ERR_UNSUPPORTED, "too many search slots");
+        std::vector<uint8_t> wl_img(wl.bytes());
+        wl.write(wl_img.data());
+        CU(cudaMemcpyAsync(base + o_dbs_items, wl_img.data(), wl_img.size(), cudaMemcpyHostToDevice, st));
+        CU(cudaMemcpyAsync(base + o_dbs_lv, lv.data(), lv.size() * 4, cudaMemcpyHostToDevice, st));
+        CU(cudaMemsetAsync(base + o_dbs_sse, 0, lv.size() * 8, st));
+        { LaunchScope ls_(ctx, "k_deblock_sse");
+        zf::k_deblock_sse<<<wl.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_dbs_items),
+                                                   (int)wl.items.size(), (const int *)(base + o_dbs_lv),
+                                                   zf::kDbLevels, (unsigned long long *)(base + o_dbs_sse)); }
+        TRY(launch_check(ctx, "k_deblock_sse"));
+        std::vector<unsigned long long> sse(lv.size());
+        CU(cudaMemcpyAsync(sse.data(), base + o_dbs_sse, sse.size() * 8, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        TRY(check_cancel(ctx));
+        for (size_t k = 0; k < ts.size(); ++k) {
+            ts[k].sse.resize(ts[k].levels.size());
+            for (size_t j = 0; j < ts[k].levels.size(); ++j)
+                ts[k].sse[j] = (int64_t)sse[k * zf::kDbLevels + j];
+        }
+        return ZF_OK;
+    };
+    if ((run.stages & STG_DB_PICK) || run.table) {
+        // the trial kernels read the descriptors (spare slot after the
+        // metadata image; the final image goes up after the search)
+        FrameDesc *hd = (FrameDesc *)(ctx->h_meta + meta_bytes);
+        for (int i = 0; i < n; ++i) hd[i] = plans[i].d;
+        CU(cudaMemcpyAsync(d_desc, hd, desc_bytes, cudaMemcpyHostToDevice, st));
+    }
+    if (run.table) {
+        // zf_deblock_sse_table: the caller's levels of one plane, kDbLevels
+        // per slot, one launch
+        std::vector<TrialSlot> ts;
+        for (int k = 0; k < run.table->n; k += zf::kDbLevels) {
+            TrialSlot t{0, run.table->plane, {}, {}};
+            for (int j = k; j < std::min(run.table->n, k + zf::kDbLevels); ++j) t.levels.push_back(run.table->levels[j]);
+            ts.push_back(t);
+        }
+        TRY(run_trials(ts));
+        for (size_t k = 0; k < ts.size(); ++k)
+            for (size_t j = 0; j < ts[k].levels.size(); ++j) run.table->sse[k * zf::kDbLevels + j] = ts[k].sse[j];
+    }
     if (run.stages & STG_DB_PICK) {
         struct Slot {
             int frame, plane;
@@ -965,17 +1239,26 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 key_frame_levels(p.in->qindex, p.in->bit_depth, p.d.lf);
             }
         }
-        if (!slots.empty()) {
-            // the trial kernels read the descriptors (spare slot after the
-            // metadata image; the final image goes up after the search)
-            FrameDesc *hd = (FrameDesc *)(ctx->h_meta + meta_bytes);
-            for (int i = 0; i < n; ++i) hd[i] = plans[i].d;
-            CU(cudaMemcpyAsync(d_desc, hd, desc_bytes, cudaMemcpyHostToDevice, st));
-        }
+        // trace lines of the climbs (try_filter_plane / search_filter_level)
+        auto trace_climb = [&](const Slot &s) {
+            if (!ctx->trace) return;
+            const Plan &p = plans[s.frame];
+            const int pw = s.plane ? p.d.w / 2 : p.d.w, ph = s.plane ? p.d.h / 2 : p.d.h;
+            std::vector<int> order;
+            s.hc.trial_order(order);
+            char line[160];
+            for (int l : order) {
+                std::snprintf(line, sizeof(line), "DLF_TRY plane=%d lvl0=%d lvl1=%d w=%d h=%d sse=%lld", s.plane, l, l,
+                              pw, ph, (long long)s.hc.err[l]);
+                p_trace[s.frame].push_back(line);
+            }
+            std::snprintf(line, sizeof(line), "DLF_PICK plane=%d dir=%d level=%d sse=%lld", s.plane, s.plane ? 0 : 2,
+                          s.hc.result, (long long)s.hc.err[s.hc.result]);
+            p_trace[s.frame].push_back(line);
+        };
         bool chroma_phase = false;
         for (int guard = 0; guard < 256 && !slots.empty(); ++guard) {
-            WorkList wl;
-            std::vector<int> lv;
+            std::vector<TrialSlot> ts;
             std::vector<int> owner;
             for (size_t k = 0; k < slots.size(); ++k) {
                 Slot &s = slots[k];
@@ -983,18 +1266,16 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 int need[2];
                 const int m = s.hc.needs(need);
                 if (m == 0) continue;
-                const int slot = (int)owner.size();
+                TrialSlot t{s.frame, s.plane, {}, {}};
+                speculate(s.hc, need, m, s.hc.have[0] ? zf::kDbLevels : 4, t.levels);
+                ts.push_back(t);
                 owner.push_back((int)k);
-                lv.push_back(need[0]);
-                lv.push_back(m > 1 ? need[1] : -1);
-                const Plan &p = plans[s.frame];
-                const int pw = s.plane ? p.d.w / 2 : p.d.w, ph = s.plane ? p.d.h / 2 : p.d.h;
-                wl.add(s.frame, s.plane, slot, 0, ((pw + 63) / 64) * ((ph + 63) / 64));
             }
             if (owner.empty()) {
                 bool all_done = true;
                 for (auto &s : slots) all_done = all_done && s.hc.done;
                 if (!all_done) return fail(ctx, ZF_ERR_UNSUPPORTED, "deblock search stalled");
+                for (auto &s : slots) trace_climb(s);
                 if (chroma_phase) break;
                 // luma finished: record levels, start chroma where luma > 0
                 std::vector<Slot> next;
@@ -1013,27 +1294,12 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 chroma_phase = true;
                 continue;
             }
-            if ((int)owner.size() > n * 3) return fail(ctx, ZF_ERR_UNSUPPORTED, "too many search slots");
-            std::vector<uint8_t> wl_img(wl.bytes());
-            wl.write(wl_img.data());
-            CU(cudaMemcpyAsync(base + o_dbs_items, wl_img.data(), wl_img.size(), cudaMemcpyHostToDevice, st));
-            CU(cudaMemcpyAsync(base + o_dbs_lv, lv.data(), lv.size() * 4, cudaMemcpyHostToDevice, st));
-            CU(cudaMemsetAsync(base + o_dbs_sse, 0, lv.size() * 8, st));
-            { LaunchScope ls_(ctx, "k_deblock_sse");
-            zf::k_deblock_sse<<<wl.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_dbs_items),
-                                                       (int)wl.items.size(), (const int *)(base + o_dbs_lv),
-                                                       (unsigned long long *)(base + o_dbs_sse)); }
-            TRY(launch_check(ctx, "k_deblock_sse"));
-            std::vector<unsigned long long> sse(lv.size());
-            CU(cudaMemcpyAsync(sse.data(), base + o_dbs_sse, sse.size() * 8, cudaMemcpyDeviceToHost, st));
-            CU(cudaStreamSynchronize(st));
-            TRY(check_cancel(ctx));
-            for (size_t sl = 0; sl < owner.size(); ++sl) {
-                Slot &s = slots[owner[sl]];
-                for (int k = 0; k < 2; ++k) {
-                    const int l = lv[sl * 2 + k];
-                    if (l < 0) continue;
-                    s.hc.err[l] = (int64_t)sse[sl * 2 + k];
+            TRY(run_trials(ts));
+            for (size_t k = 0; k < owner.size(); ++k) {
+                Slot &s = slots[owner[k]];
+                for (size_t j = 0; j < ts[k].levels.size(); ++j) {
+                    const int l = ts[k].levels[j];
+                    s.hc.err[l] = ts[k].sse[j];
                     s.hc.have[l] = true;
                 }
             }
@@ -1295,6 +1561,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             }
         }
     }
+    if (run.rows || ctx->trace) TRY(search_records(ctx, plans, back, ob, run, p_trace));
     return ZF_OK;
 }
 
@@ -1397,6 +1664,7 @@ int32_t zf_create(zf_ctx **out, const zf_opts *opts) {
         delete c;
         return ZF_ERR_CUDA;
     }
+    if (const char *tp = std::getenv("ZF_TRACE")) zf_trace(c, tp);
     *out = c;
     return ZF_OK;
 }
@@ -1410,7 +1678,24 @@ void zf_destroy(zf_ctx *ctx) {
     if (ctx->h_out) cudaFreeHost(ctx->h_out);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->trace_owned) std::fclose(ctx->trace);
     delete ctx;
+}
+
+int32_t zf_trace(zf_ctx *ctx, const char *path) {
+    if (!ctx) return ZF_ERR_ARG;
+    if (ctx->trace_owned) std::fclose(ctx->trace);
+    ctx->trace = nullptr;
+    ctx->trace_owned = false;
+    if (!path || !*path) return ZF_OK;
+    if (std::strcmp(path, "-") == 0) {
+        ctx->trace = stderr;
+        return ZF_OK;
+    }
+    ctx->trace = std::fopen(path, "w");
+    if (!ctx->trace) return fail(ctx, ZF_ERR_ARG, std::string("cannot open trace file ") + path);
+    ctx->trace_owned = true;
+    return ZF_OK;
 }
 
 const char *zf_last_error(const zf_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
@@ -1708,6 +1993,19 @@ int32_t zf_deblock_pick(zf_ctx *ctx, const zf_frame *f, uint8_t lf[4]) {
     return e;
 }
 
+int32_t zf_deblock_sse_table(zf_ctx *ctx, const zf_frame *f, int32_t plane, const int32_t *levels, int32_t n,
+                             int64_t *sse) {
+    if (!ctx) return ZF_ERR_ARG;
+    if (!levels || !sse || n <= 0 || n > 64) return fail(ctx, ZF_ERR_ARG, "levels: 1..64 entries required");
+    for (int k = 0; k < n; ++k)
+        if (levels[k] < 0 || levels[k] > 63) return fail(ctx, ZF_ERR_ARG, "level out of range 0..63");
+    if (!f || plane < 0 || plane > 2 || (plane > 0 && !f->chroma_420)) return fail(ctx, ZF_ERR_ARG, "bad plane");
+    DbTable t{plane, n, levels, sse};
+    Run r{0, SET_A, SET_A, false, nullptr, false, false, false};
+    r.table = &t;
+    return run_batch(ctx, f, 1, nullptr, nullptr, r);
+}
+
 int32_t zf_deblock_apply(zf_ctx *ctx, const zf_frame *f, const uint8_t lf[4]) {
     if (!lf) return fail(ctx, ZF_ERR_ARG, "lf is NULL");
     zf_decisions d;
@@ -1720,6 +2018,15 @@ int32_t zf_deblock_apply(zf_ctx *ctx, const zf_frame *f, const uint8_t lf[4]) {
 int32_t zf_cdef_search(zf_ctx *ctx, const zf_frame *f, zf_decisions *out) {
     if (!out) return fail(ctx, ZF_ERR_ARG, "decisions is NULL");
     Run r{STG_CDEF_SEARCH, SET_B, SET_B, false, nullptr, false, false, false};
+    return run_batch(ctx, f, 1, out, nullptr, r);
+}
+
+int32_t zf_cdef_search_rows(zf_ctx *ctx, const zf_frame *f, zf_decisions *out, uint64_t *mse, uint8_t *has_row,
+                            int32_t *ncand) {
+    if (!out || !ncand) return fail(ctx, ZF_ERR_ARG, "decisions or ncand is NULL");
+    CdefRows rows{mse, has_row, ncand};
+    Run r{STG_CDEF_SEARCH, SET_B, SET_B, false, nullptr, false, false, false};
+    r.rows = &rows;
     return run_batch(ctx, f, 1, out, nullptr, r);
 }
 

@@ -8,7 +8,9 @@
 namespace zf {
 
 __global__ void k_deblock_apply(const FrameDesc *frames, const WorkItem *items, int nitems);
-__global__ void k_deblock_sse(const FrameDesc *frames, const WorkItem *items, int nitems, const int *levels,
+// levels per (frame, plane) slot in one k_deblock_sse launch (at most)
+constexpr int kDbLevels = 8;
+__global__ void k_deblock_sse(const FrameDesc *frames, const WorkItem *items, int nitems, const int *levels, int nl,
                               unsigned long long *sse);
 
 // CDEF search over a batch whose candidate grids are at most fp x ns.

@@ -215,6 +215,61 @@ def synth_recon(rng, src, geom, qindex, bd, plane):
     return _to_plane(rec, bd)
 
 
+def _tx_blocks(geom, plane):
+    """Transform blocks of a plane as (origin y, origin x, height, width)
+    arrays in that plane's samples: the luma TX grid for plane 0, the 4:2:0
+    chroma TX of each block (max(bw/2, 4) x max(bh/2, 4)) for planes 1, 2."""
+    mi_rows, mi_cols = geom.mi_rows, geom.mi_cols
+    my, mx = np.mgrid[0:mi_rows, 0:mi_cols]
+    if plane == 0:
+        tw = geom.tw.astype(np.int64) // 4
+        th = geom.th.astype(np.int64) // 4
+        px = 4
+    else:
+        tw = np.maximum(geom.bw.astype(np.int64) // 8, 1) * 2
+        th = np.maximum(geom.bh.astype(np.int64) // 8, 1) * 2
+        px = 2
+    ox, oy = mx & ~(tw - 1), my & ~(th - 1)
+    first = (mx == ox) & (my == oy)
+    return oy[first] * px, ox[first] * px, th[first] * px, tw[first] * px, first
+
+
+def synth_recon_quant(rng, src, geom, qindex, bd, plane):
+    """Quantised-transform recon: every transform block of the plane is
+    replaced by the inverse 2-D DCT of its quantised orthonormal DCT
+    (step = AC quantiser / 8, on the plane's own bit-depth scale, rounding
+    with a small dead zone). Skipped blocks keep only their quantised DC (a
+    flat block, as an all-zero residual on a DC prediction gives). This is
+    the blocky, band-limited recon the deblock level search and CDEF exist
+    for: filtering it lowers the error against the source."""
+    from scipy.fft import dctn, idctn
+    tab = AC_QLOOKUP_8 if bd == 8 else AC_QLOOKUP_10
+    step = max(tab[qindex] / 8.0, 1.0)
+    h, w = src.shape
+    base = src.astype(np.float64)
+    out = base.copy()
+    y0, x0, bh, bw, first = _tx_blocks(geom, plane)
+    skip_first = geom.skip.astype(bool)[first]
+    shapes = {}
+    for i in range(len(y0)):
+        shapes.setdefault((int(bh[i]), int(bw[i])), []).append(i)
+    for (th, tw), idx in shapes.items():
+        idx = np.asarray(idx)
+        yy = y0[idx][:, None, None] + np.arange(th)[None, :, None]
+        xx = x0[idx][:, None, None] + np.arange(tw)[None, None, :]
+        yy, xx = np.broadcast_arrays(yy, xx)
+        ok = (yy < h) & (xx < w)
+        yy, xx = np.minimum(yy, h - 1), np.minimum(xx, w - 1)
+        blk = base[yy, xx]
+        c = dctn(blk, type=2, norm="ortho", axes=(1, 2))
+        q = np.sign(c) * np.floor(np.abs(c) / step + 0.35)
+        sk = skip_first[idx]
+        q[sk, :, :] = np.where(np.arange(th)[:, None] + np.arange(tw)[None, :] == 0, q[sk, :, :], 0.0)
+        rec = idctn(q * step, type=2, norm="ortho", axes=(1, 2))
+        out[yy[ok], xx[ok]] = rec[ok]
+    return _to_plane(out, bd)
+
+
 AC_QLOOKUP_8 = None
 AC_QLOOKUP_10 = None
 
@@ -270,7 +325,11 @@ def qp_to_qindex(qp):
     return 249 if qp == 62 else 255
 
 
-def make_frame(seed, true_w, true_h, bd, qp, preset, content="cosine", chroma=True, skip_prob=None):
+def make_frame(seed, true_w, true_h, bd, qp, preset, content="cosine", chroma=True, skip_prob=None,
+               recon="quant"):
+    """One frame's stage inputs. recon: "quant" (quantised-transform recon,
+    synth_recon_quant) or "offset" (source + per-TX offset + noise,
+    synth_recon)."""
     _load_tables()
     rng = np.random.default_rng(seed)
     w, h = align8(true_w), align8(true_h)
@@ -290,7 +349,12 @@ def make_frame(seed, true_w, true_h, bd, qp, preset, content="cosine", chroma=Tr
     src = [_to_plane(y, bd), _to_plane(u, bd), _to_plane(v, bd)]
     qindex = qp_to_qindex(qp)
     geom = random_geometry(rng, w, h, qp, skip_prob=skip_prob)
-    rec = [synth_recon(rng, src[p], geom, qindex, bd, p) for p in range(3)]
+    if recon == "quant":
+        rec = [synth_recon_quant(rng, src[p], geom, qindex, bd, p) for p in range(3)]
+    elif recon == "offset":
+        rec = [synth_recon(rng, src[p], geom, qindex, bd, p) for p in range(3)]
+    else:
+        raise ValueError(recon)
     if not chroma:
         src = [src[0], np.zeros((h // 2, w // 2), src[0].dtype), np.zeros((h // 2, w // 2), src[0].dtype)]
         rec = [rec[0], np.zeros_like(src[1]), np.zeros_like(src[2])]
@@ -339,11 +403,14 @@ def batch_specs(n=256, seed_cfg=4, max_dim=2048):
     return specs
 
 
+def batch_frame(i, spec):
+    """Image i of the mixed batch with its (w, h, bd, qp) spec."""
+    w, h, bd, qp = spec
+    return make_frame(frame_seed(4, i), w, h, bd, qp, 6, "cosine")
+
+
 def workload_batch(n=256, max_dim=2048):
-    frames = []
-    for i, (w, h, bd, qp) in enumerate(batch_specs(n, max_dim=max_dim)):
-        frames.append(make_frame(frame_seed(4, i), w, h, bd, qp, 6, "cosine"))
-    return frames
+    return [batch_frame(i, sp) for i, sp in enumerate(batch_specs(n, max_dim=max_dim))]
 
 
 def served_specs(n=32, seed_cfg=5, max_w=6000, max_h=4000, min_dim=128):
