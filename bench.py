@@ -51,6 +51,8 @@ import numpy as np  # noqa: E402
 import __graft_entry__ as ge  # noqa: E402
 
 METRIC = "byte-exact filter-stage MPix/s on 1 GB300, batched vs plain; p50/p99 latency"
+DATA = ("synthetic (seeded 1/f^2 fields + shapes + noise; synthetic MD geometry; quantised-transform "
+        "recon stand-in)")
 WORKLOAD = [(4, 24), (4, 40), (6, 24), (6, 40)]  # (preset, qp)
 W4K, H4K = 3840, 2160
 
@@ -60,12 +62,15 @@ def env_rank():
 
 
 def make_workload(w=W4K, h=H4K, idx=0):
+    """The four frames of the plain per-image workload (synth.workload_4k:
+    the frames the full-size parity tests pin against the oracle); other
+    sizes for profiling runs use the same seeds."""
     ge._pkg()
     from zenav1_svt_gb300 import synth
-    frames = []
-    for i, (preset, qp) in enumerate(WORKLOAD):
-        frames.append(synth.make_frame(synth.frame_seed(2, idx * 16 + i), w, h, 8, qp, preset, "power"))
-    return frames
+    if (w, h) == (W4K, H4K):
+        return [synth.workload_4k(preset, qp, idx) for preset, qp in WORKLOAD]
+    return [synth.make_frame(synth.frame_seed(2, idx * 16 + preset * 2 + (qp > 30)), w, h, 8, qp, preset, "power")
+            for preset, qp in WORKLOAD]
 
 
 def _gen_frame(job):
@@ -159,6 +164,14 @@ class ClockSampler:
 # --------------------------------------------------------------------------
 # reference arm: the oracle port on host cores
 # --------------------------------------------------------------------------
+def ours_config(nframes, world=1):
+    """The `config` of the plain workload, shared by both arms' lines."""
+    return {"workload": "plain per-image 3840x2160 8-bit 4:2:0, presets {4,6} x qp {24,40}",
+            "frames_per_step": nframes,
+            "l2": "GPU arm: flushed between steps (256 MB write); CPU arm: not applicable",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -166,17 +179,12 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.lib()
-    # bounded sample of the workload on every host core: one 3840x544 frame
-    # per core (the four presets/qps of the 4K workload, further seeds of the
-    # same content generator), one host thread per frame -- the reference
-    # stage is single-threaded per frame
-    cores = os.cpu_count() or 1
-    nf = max(4, cores)
-    frames = []
-    for k in range((nf + 3) // 4):
-        frames += make_workload(W4K, 544, idx=k)
-    frames = frames[:nf]
+    # the same four 3840x2160 frames as the GPU arm's step, one host thread
+    # per frame: the reference stage is single-threaded per frame, so a step
+    # of four frames keeps four cores busy
+    frames = make_workload()
     px = sum(f.luma_px for f in frames)
+    cores = os.cpu_count() or 1
 
     def step():
         recs = [f.copy_rec() for f in frames]
@@ -196,13 +204,11 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "MPix/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(tot / len(times) * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-            "data": "synthetic (seeded 1/f^2 fields + shapes + noise; synthetic MD geometry and recon)",
-            "config": {"workload": "3840x544 sample of the 4K plain workload, presets {4,6} x qp {24,40}",
-                       "frames_per_step": len(frames)},
+            "data": DATA, "config": ours_config(len(frames), world),
             "cpu_baseline": {"value": round(value, 3), "unit": "MPix/s", "cores": min(cores, len(frames)),
                              "kind": "port",
-                             "sample": "%d frames 3840x544 per step, one host thread per frame (C++ oracle port)"
-                                       % len(frames)},
+                             "sample": "the GPU arm's four 3840x2160 frames per step, one host thread per frame "
+                                       "(C++ oracle port; %d host cores)" % cores},
             "e2e": {"value": round(value, 3), "unit": "MPix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -244,8 +250,8 @@ def kernel_bytes(name, w, h, px):
 
 
 # DRAM bytes (read + write) per luma pixel of one launch, from one ncu
-# capture of each kernel on a 3840x2160 8-bit preset-6 frame
-# (profiles/top_kernels_4k_p6_frame.md); the roofline's `traffic` scales
+# capture of each kernel on a 3840x2160 8-bit preset-6 frame (the committed
+# summary of the top kernels' captures); the roofline's `traffic` scales
 # them to the launch's frame.
 KERNEL_DRAM_BYTES_PER_PX = {
     "k_cdef_apply": 14.070016e6 / (3840 * 2160),
@@ -433,10 +439,7 @@ def run_ours(args):
         line = {"metric": METRIC, "value": round(value, 3), "unit": "MPix/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_max, 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
-                "data": "synthetic (seeded 1/f^2 fields + shapes + noise; synthetic MD geometry and recon)",
-                "config": {"workload": "plain per-image 3840x2160 8-bit 4:2:0, presets {4,6} x qp {24,40}",
-                           "frames_per_step": len(frames), "l2": "flushed between steps (256 MB write)",
-                           "parallelism": "replicas" if world > 1 else "single"},
+                "data": DATA, "config": ours_config(len(frames), world),
                 "e2e": {"value": round(e2e, 3), "unit": "MPix/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e_ms, 3)},
                 "gpu_launches": int(launches),
@@ -444,6 +447,7 @@ def run_ours(args):
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_sample()
         if world == 1:
+            line["plain_512"] = run_plain512(args, ctx, stream, dev)
             line["highres_10bit"] = run_highres10(args, ctx, stream, dev)
             line["sgr"] = run_sgr(args, ctx, stream, dev, frames[0])
             line["post"] = run_post(args, ctx, stream, dev, frames[0])
@@ -459,6 +463,72 @@ def run_ours(args):
     return 0
 
 
+def run_plain512(args, ctx, stream, dev):
+    """The plain drop-in configuration: one 512x512 8-bit still, preset 6,
+    qp 32 (closed-form deblock levels, 4 CDEF candidates), one
+    zf_filter_stage per step: device-resident (L2 flushed between steps) and
+    from pinned host buffers (copies inside the timed call), with the
+    oracle's single-core time on the same frame beside it."""
+    import torch
+    pkg = ge._pkg()
+    from zenav1_svt_gb300 import abi, synth
+    f = synth.workload_plain_512()
+    mi = pkg.pack_geom(f.geom)
+    src = [torch.from_numpy(p).to(dev) for p in f.src]
+    rec0 = [torch.from_numpy(p).to(dev) for p in f.rec]
+    rec = [x.clone() for x in rec0]
+    m = torch.from_numpy(mi.view(np.int32)).to(dev)
+    s = abi.make_frame_struct(f, [x.data_ptr() for x in src], [x.data_ptr() for x in rec], m.data_ptr(),
+                              on_device=True)
+    h_src = [torch.from_numpy(p.copy()).pin_memory() for p in f.src]
+    h_rec = [torch.from_numpy(p.copy()).pin_memory() for p in f.rec]
+    h_mi = torch.from_numpy(mi.view(np.int32).copy()).pin_memory()
+    hs = abi.make_frame_struct(f, [x.numpy() for x in h_src], [x.numpy() for x in h_rec], h_mi.numpy())
+    d = abi.Decisions(f.w, f.h, f.true_w, f.true_h)
+    st = abi.ZfStats()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def timed(struct, restore):
+        out = []
+        for k in range(args.warmup + max(args.steps, 10)):
+            restore()
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.filter_stage_raw(struct, d, st)
+            e1.record(stream)
+            e1.synchronize()
+            if k >= args.warmup:
+                out.append(e0.elapsed_time(e1))
+        return float(np.mean(out)), float(np.percentile(out, 99))
+
+    def restore_dev():
+        for a, b in zip(rec, rec0):
+            a.copy_(b)
+
+    def restore_host():
+        for a, b in zip(h_rec, f.rec):
+            a.numpy()[...] = b
+
+    ms, p99 = timed(s, restore_dev)
+    e_ms, e_p99 = timed(hs, restore_host)
+    out = {"workload": "512x512 8-bit 4:2:0, preset 6, qp 32 (one frame per step)",
+           "mpix_per_s": round(f.luma_px / (ms / 1e3) / 1e6, 3), "ms": round(ms, 4), "p99_ms": round(p99, 4),
+           "e2e_mpix_per_s": round(f.luma_px / (e_ms / 1e3) / 1e6, 3), "e2e_ms": round(e_ms, 4),
+           "e2e_p99_ms": round(e_p99, 4), "lf": d.as_dict()["lf"], "cdef_bits": d.as_dict()["cdef_bits"]}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        t0 = time.perf_counter()
+        for _ in range(5):
+            oracle.filter_stage(f)
+        cpu_ms = (time.perf_counter() - t0) / 5 * 1e3
+        out["cpu_oracle_ms"] = round(cpu_ms, 3)
+        out["cpu_oracle_mpix_per_s"] = round(f.luma_px / (cpu_ms / 1e3) / 1e6, 3)
+    return out
+
+
 def run_highres10(args, ctx, stream, dev):
     """The 10-bit high-resolution configuration: one 4096x3072 10-bit frame
     (u16 planes), preset 2 (20 CDEF candidates, deblock level search,
@@ -467,7 +537,7 @@ def run_highres10(args, ctx, stream, dev):
     import torch
     pkg = ge._pkg()
     from zenav1_svt_gb300 import abi, synth
-    f = synth.make_frame(synth.frame_seed(3, 0), 4096, 3072, 10, 28, 2, "power10")
+    f = synth.workload_10bit_4096()
     src = [torch.from_numpy(p).to(dev) for p in f.src]
     rec0 = [torch.from_numpy(p).to(dev) for p in f.rec]
     rec = [x.clone() for x in rec0]

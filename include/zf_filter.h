@@ -481,6 +481,15 @@ int32_t zf_set_tune(zf_ctx *ctx, const zf_tune *t);
 int32_t zf_autotune(zf_ctx *ctx, const zf_frame *frames, int32_t n, int32_t reps, zf_tune *best,
                     zf_tune *cands, int32_t max);
 
+/* Iteration limit of the one device-side wait of the stage (the Wiener
+ * statistics kernel waiting for its TMA tile loads); 0 restores the
+ * default (2^20 iterations of mbarrier try_wait, far beyond any real
+ * load). A CTA that gives up drains its loads, records the timeout and the
+ * call returns ZF_ERR_TIMEOUT; the context stays usable. A small limit
+ * makes the wait give up on purpose: that is how the timeout path is
+ * tested. No counterpart in the reference. */
+int32_t zf_set_wait_limit(zf_ctx *ctx, uint32_t iterations);
+
 /* Kernel launches issued by this context since zf_create. */
 uint64_t zf_launch_count(const zf_ctx *ctx);
 /* enable != 0: bracket every kernel launch with CUDA events (adds a little

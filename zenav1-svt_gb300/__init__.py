@@ -70,6 +70,7 @@ def lib():
     L.zf_cdef_search_rows.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions), C.c_void_p, C.c_void_p,
                                       P(C.c_int32)]
     L.zf_trace.argtypes = [C.c_void_p, C.c_char_p]
+    L.zf_set_wait_limit.argtypes = [C.c_void_p, C.c_uint32]
     L.zf_cdef_search.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions)]
     L.zf_cdef_apply.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions), P(ZfStats)]
     L.zf_lr_search.argtypes = [C.c_void_p, P(ZfFrame), P(ZfDecisions)]
@@ -114,7 +115,7 @@ def lib():
     for name in ("zf_lr_corners_in_sb", "zf_lr_sb_syntax", "zf_get_tune", "zf_set_tune", "zf_autotune", "zf_use_graphs", "zf_graph_stats", "zf_superres_scaled_size", "zf_superres_upscale", "zf_film_grain_estimate",
                  "zf_film_grain_synthesize", "zf_write_filter_params", "zf_sgr_search", "zf_sgr_apply", "zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
                  "zf_submit_batch", "zf_deblock_pick", "zf_deblock_apply", "zf_cdef_search",
-                 "zf_deblock_sse_table", "zf_cdef_search_rows", "zf_trace",
+                 "zf_deblock_sse_table", "zf_cdef_search_rows", "zf_trace", "zf_set_wait_limit",
                  "zf_cdef_apply", "zf_lr_search", "zf_lr_apply"):
         getattr(L, name).restype = C.c_int32
     _lib = L
@@ -306,6 +307,10 @@ class Context:
                                               C.byref(nc)))
         n = nc.value
         return d, (flat[:nfb * 2 * n].reshape(nfb, 2 * n) if n else None), has
+
+    def set_wait_limit(self, iterations):
+        """Iteration limit of the statistics kernel's TMA wait (0: default)."""
+        self._check(lib().zf_set_wait_limit(self.h, int(iterations)))
 
     def trace(self, path):
         """Search trace lines to path ("-" stderr, None stops): zf_trace."""

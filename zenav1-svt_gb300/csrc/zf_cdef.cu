@@ -1708,9 +1708,16 @@ extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_de
     const int np = d.cdef.ncand * d.cdef.ncand;
     const int CL = kFinCluster;
     const int per_cta = 2 * (np <= kFinPushPairs ? CL : 1) * np * 8 + (nfb + CL - 1) / CL * (2 * d.cdef.ncand + 1) * 4;
-    if (per_cta > 48 * 1024 &&
-        cudaFuncSetAttribute(k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, per_cta) != cudaSuccess)
-        return ZF_ERR_CUDA;
+    // raise the kernel's dynamic shared memory opt-in when this launch needs
+    // more, never lower it: the attribute is per function and device, and a
+    // context set it to its own cap at creation
+    if (per_cta > 48 * 1024) {
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, k_cdef_finish) != cudaSuccess) return ZF_ERR_CUDA;
+        if (per_cta > fa.maxDynamicSharedSizeBytes &&
+            cudaFuncSetAttribute(k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, per_cta) != cudaSuccess)
+            return ZF_ERR_CUDA;
+    }
     if (launch_cdef_finish(kFinLevels, CL, per_cta, st, &sc->desc, &sc->frame_id, per_cta) != cudaSuccess)
         return ZF_ERR_CUDA;
     if (cudaGetLastError() != cudaSuccess) return ZF_ERR_CUDA;

@@ -137,6 +137,9 @@ struct FrameDesc {
     LrPlane lr[3];
     int64_t rdmult;
     int lr_on;
+    // iterations of the statistics kernel's bounded wait for its TMA boxes
+    // (zf_set_wait_limit); a CTA that gives up sets cdef_stats[3]
+    uint32_t wait_limit;
 };
 
 // One entry of a launch work list: a tile of a frame/plane, owning CTAs
@@ -253,6 +256,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity) {
         : "memory");
     return done != 0;
 }
+// Iterations of the drain wait after a timed-out wait: the copies already
+// issued always complete, so this is long (seconds) but still bounded.
+constexpr uint32_t kDrainWaitLimit = 1u << 26;
 // Waits for the mbarrier phase with an iteration limit; false when it gave up.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *mbar, uint32_t parity, uint32_t limit) {
     for (uint32_t it = 0; it < limit; ++it)

@@ -58,6 +58,7 @@ struct zf_ctx {
     bool graphs = false;
     bool capturing = false;
     bool tma = true;  // statistics kernel rows by TMA where the planes allow
+    uint32_t wait_limit = 1u << 20;  // statistics kernel's TMA wait (iterations)
     int apply_group = 8;  // 64-px column tiles per restoration-apply CTA
     // search trace (zf_trace / ZF_TRACE): one text line per trial, filter
     // block and restoration unit in the reference's debug-dump formats
@@ -949,6 +950,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         TRY(validate_frame(ctx, &frames[i]));
         plan_frame(plans[i], &frames[i], cursor, ucur, rcur, ocur);
         plans[i].out = outs ? &outs[i] : nullptr;
+        plans[i].d.wait_limit = ctx->wait_limit;
     }
     // Work lists (host-known shapes).
     // statistics: 5-tap 8-bit, 5-tap 10-bit (one kernel instantiation each), 7-tap
@@ -1680,6 +1682,12 @@ void zf_destroy(zf_ctx *ctx) {
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->trace_owned) std::fclose(ctx->trace);
     delete ctx;
+}
+
+int32_t zf_set_wait_limit(zf_ctx *ctx, uint32_t iterations) {
+    if (!ctx) return ZF_ERR_ARG;
+    ctx->wait_limit = iterations ? iterations : 1u << 20;
+    return ZF_OK;
 }
 
 int32_t zf_trace(zf_ctx *ctx, const char *path) {

@@ -175,12 +175,15 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
     if (threadIdx.x < 4) Es[threadIdx.x] = 0;
     __syncthreads();
     if (tma) {
-        // bounded wait for both boxes; on a timeout the frame's error word is
-        // set, the copies in flight are waited for once more and the CTA ends
-        const bool late = !mbar_wait_bounded(&mbar, 0, 1u << 20);
+        // bounded wait for both boxes (f.wait_limit iterations); on a
+        // timeout the frame's error word is set, the copies already issued
+        // are drained (they always land; the drain wait is long but bounded)
+        // so that no box is still arriving in shared memory when the CTA ends
+        const bool late = !mbar_wait_bounded(&mbar, 0, f.wait_limit);
         if (__syncthreads_or(late)) {
             if (threadIdx.x == 0) atomicOr(&f.cdef_stats[3], 1ull);
-            mbar_wait_bounded(&mbar, 0, 1u << 20);
+            mbar_wait_bounded(&mbar, 0, kDrainWaitLimit);
+            __syncthreads();
             return;
         }
         // The loads read zeros outside the tensor and the canvas padding
