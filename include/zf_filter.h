@@ -482,9 +482,9 @@ int32_t zf_autotune(zf_ctx *ctx, const zf_frame *frames, int32_t n, int32_t reps
                     zf_tune *cands, int32_t max);
 
 /* Iteration limit of the one device-side wait of the stage (the Wiener
- * statistics kernel waiting for its TMA tile loads); 0 restores the
- * default (2^20 iterations of mbarrier try_wait, far beyond any real
- * load). A CTA that gives up drains its loads, records the timeout and the
+ * statistics kernel waiting for its TMA tile loads), in steps of about
+ * 100 ns (mbarrier try_wait with a suspend-time hint); 0 restores the
+ * default of 2^20 steps, far beyond any real load. A CTA that gives up drains its loads, records the timeout and the
  * call returns ZF_ERR_TIMEOUT; the context stays usable. A small limit
  * makes the wait give up on purpose: that is how the timeout path is
  * tested. No counterpart in the reference. */

@@ -256,9 +256,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity) {
         : "memory");
     return done != 0;
 }
+// try_wait with an explicit suspend-time hint: the thread waits at most
+// about `ns` nanoseconds for the phase before the call returns false.
+__device__ __forceinline__ bool mbar_try_wait_ns(uint64_t *mbar, uint32_t parity, uint32_t ns) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(mbar)), "r"(parity), "r"(ns)
+        : "memory");
+    return done != 0;
+}
+// Waits for the phase in steps of about `ns` nanoseconds, at most `limit`
+// steps; false when it gave up.
+__device__ __forceinline__ bool mbar_wait_timed(uint64_t *mbar, uint32_t parity, uint32_t limit, uint32_t ns) {
+    for (uint32_t it = 0; it < limit; ++it)
+        if (mbar_try_wait_ns(mbar, parity, ns)) return true;
+    return false;
+}
 // Iterations of the drain wait after a timed-out wait: the copies already
 // issued always complete, so this is long (seconds) but still bounded.
 constexpr uint32_t kDrainWaitLimit = 1u << 26;
+// Suspend-time hint of one step of the statistics kernel's first wait.
+constexpr uint32_t kWaitStepNs = 100;
 // Waits for the mbarrier phase with an iteration limit; false when it gave up.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *mbar, uint32_t parity, uint32_t limit) {
     for (uint32_t it = 0; it < limit; ++it)

@@ -175,11 +175,12 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
     if (threadIdx.x < 4) Es[threadIdx.x] = 0;
     __syncthreads();
     if (tma) {
-        // bounded wait for both boxes (f.wait_limit iterations); on a
+        // bounded wait for both boxes (f.wait_limit steps of about
+        // kWaitStepNs nanoseconds: 2^20 steps, ~0.1 s, by default); on a
         // timeout the frame's error word is set, the copies already issued
         // are drained (they always land; the drain wait is long but bounded)
         // so that no box is still arriving in shared memory when the CTA ends
-        const bool late = !mbar_wait_bounded(&mbar, 0, f.wait_limit);
+        const bool late = !mbar_wait_timed(&mbar, 0, f.wait_limit, kWaitStepNs);
         if (__syncthreads_or(late)) {
             if (threadIdx.x == 0) atomicOr(&f.cdef_stats[3], 1ull);
             mbar_wait_bounded(&mbar, 0, kDrainWaitLimit);
