@@ -484,11 +484,14 @@ int32_t zf_autotune(zf_ctx *ctx, const zf_frame *frames, int32_t n, int32_t reps
 /* Iteration limit of the one device-side wait of the stage (the Wiener
  * statistics kernel waiting for its TMA tile loads), in steps of about
  * 100 ns (mbarrier try_wait with a suspend-time hint); 0 restores the
- * default of 2^20 steps, far beyond any real load. A CTA that gives up drains its loads, records the timeout and the
- * call returns ZF_ERR_TIMEOUT; the context stays usable. A small limit
- * makes the wait give up on purpose: that is how the timeout path is
- * tested. No counterpart in the reference. */
+ * default of 2^20 steps, far beyond any real load. A CTA that gives up
+ * drains its loads, records the timeout and the call returns
+ * ZF_ERR_TIMEOUT; the context stays usable. No counterpart in the
+ * reference. */
 int32_t zf_set_wait_limit(zf_ctx *ctx, uint32_t iterations);
+/* zf_set_wait_limit value under which the wait gives up before its first
+ * step, as if the loads never arrived: the test of the timeout path. */
+#define ZF_WAIT_GIVE_UP 0xFFFFFFFFu
 
 /* Kernel launches issued by this context since zf_create. */
 uint64_t zf_launch_count(const zf_ctx *ctx);

@@ -5,11 +5,12 @@
   call with Cancelled and writes no output; once the flag is cleared the
   same context runs the frame bit-exact against the oracle.
 - The one device-side wait of the stage (the Wiener statistics kernel
-  waiting for its TMA tile loads) has an iteration limit. A limit of one
-  iteration makes it give up on purpose: the call returns Timeout, the CTAs
-  drain their loads before they end, and the same context then runs the
-  frame with the default limit bit-exact against the oracle. Nothing faults,
-  traps or hangs: the kernels return and the host reads the status.
+  waiting for its TMA tile loads) has an iteration limit. ZF_WAIT_GIVE_UP
+  makes it give up before its first step, as if the loads never arrived:
+  the call returns Timeout, the CTAs drain their loads before they end, and
+  the same context then runs the frame with the default limit bit-exact
+  against the oracle. Nothing faults, traps or hangs: the kernels return and
+  the host reads the status.
 """
 import ctypes as C
 
@@ -47,7 +48,7 @@ def test_cancel_flag_refuses_then_recovers(pkg, oracle):
 def test_statistics_wait_limit_times_out_and_context_recovers(ctx, pkg, oracle):
     # 8-bit, 16-aligned planes: the statistics rows come by TMA
     fr = synth.make_frame(synth.frame_seed(13, 2), 1024, 768, 8, 30, 6, "cosine")
-    ctx.set_wait_limit(1)
+    ctx.set_wait_limit(0xFFFFFFFF)  # ZF_WAIT_GIVE_UP: give up before the first step
     try:
         with pytest.raises(pkg.ZfError) as e:
             ctx.filter_stage(fr)

@@ -398,6 +398,7 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
                                                      const int *levels, int nl, unsigned long long *sse) {
     __shared__ __align__(16) uint16_t reg[DB_R * DB_R];
     __shared__ __align__(16) uint16_t pristine[DB_R * DB_R];
+    __shared__ __align__(16) uint16_t srct[DB_T * DB_T];  // the source tile, staged once for every level
     __shared__ DbEdges edges;
     __shared__ unsigned long long part[8];
     const int it = find_item(items, nitems, blockIdx.x);
@@ -411,13 +412,30 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
     DbTile t{&f, plane, pw, ph, (tix % tiles_x) * DB_T, (tix / tiles_x) * DB_T};
     const int bd = f.bd;
     db_load(t, f.IN[plane], pristine);
+    // the tile's source samples (0 outside the plane: such positions are
+    // skipped by the sum below), word-wide where the plane allows
+    const int spw = bd == 8 ? 4 : 2, wpr = DB_T / spw, lgw = bd == 8 ? 4 : 5;  // wpr = 1 << lgw
+    if (word_ok(f.S[plane])) {
+        for (int i = threadIdx.x; i < DB_T * wpr; i += blockDim.x) {
+            const int ty = i >> lgw, wx = i & (wpr - 1);
+            const int y = t.y0 + ty, x = t.x0 + wx * spw;
+            const uint32_t v = (x < pw && y < ph) ? *word_at(f.S[plane], (int64_t)y * pw + x, bd) : 0u;
+            unpack_word(v, bd, srct + ty * DB_T + wx * spw);
+        }
+    } else {
+        for (int i = threadIdx.x; i < DB_T * DB_T; i += blockDim.x) {
+            const int ty = i / DB_T, tx = i % DB_T, y = t.y0 + ty, x = t.x0 + tx;
+            srct[i] = (uint16_t)((x < pw && y < ph) ? ldpx(f.S[plane], (int64_t)y * pw + x, bd) : 0);
+        }
+    }
     // edge lengths do not depend on a nonzero level: computed once
     bool any = false;
     for (int k = 0; k < nl; ++k) any = any || levels[slot * nl + k] > 0;
     if (any) db_params(t, 1, 1, edges);
     __syncthreads();
-    const int spw = bd == 8 ? 4 : 2, wpr = DB_T / spw, lgw = bd == 8 ? 4 : 5;  // wpr = 1 << lgw
-    const bool words = word_ok(f.S[plane]);
+    // rows and columns of the tile inside the plane (pw, ph are multiples of
+    // 4; two samples per word of the u16 rows)
+    const int rows = min(DB_T, ph - t.y0), pairs = min(DB_T, pw - t.x0) >> 1;
     for (int k = 0; k < nl; ++k) {
         const int lvl = levels[slot * nl + k];
         if (lvl < 0) continue;
@@ -426,27 +444,13 @@ __global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, co
         __syncthreads();
         if (lvl != 0) db_filter(t, reg, edges, lvl, lvl);
         unsigned long long acc = 0;
-        if (words) {
-            for (int i = threadIdx.x; i < DB_T * wpr; i += blockDim.x) {
-                const int ty = i >> lgw, wx = i & (wpr - 1);
-                const int y = t.y0 + ty, x = t.x0 + wx * spw;
-                if (x < pw && y < ph) {
-                    const uint32_t sw = *word_at(f.S[plane], (int64_t)y * pw + x, bd);
-                    const uint16_t *rp = reg + (ty + DB_H) * DB_R + DB_H + wx * spw;
-                    for (int q = 0; q < spw; ++q) {
-                        const int d = word_sample(sw, q, bd) - (int)rp[q];
-                        acc += (unsigned long long)((long long)d * d);
-                    }
-                }
-            }
-        } else {
-            for (int i = threadIdx.x; i < DB_T * DB_T; i += blockDim.x) {
-                int ty = i / DB_T, tx = i % DB_T;
-                int y = t.y0 + ty, x = t.x0 + tx;
-                if (x < pw && y < ph) {
-                    int d = ldpx(f.S[plane], (int64_t)y * pw + x, bd) - (int)reg[(ty + DB_H) * DB_R + tx + DB_H];
-                    acc += (unsigned long long)((long long)d * d);
-                }
+        for (int i = threadIdx.x; i < DB_T * (DB_T / 2); i += blockDim.x) {
+            const int ty = i >> 5, px = i & 31;
+            if (ty < rows && px < pairs) {
+                const uint32_t sv = reinterpret_cast<const uint32_t *>(srct + ty * DB_T)[px];
+                const uint32_t rv = reinterpret_cast<const uint32_t *>(reg + (ty + DB_H) * DB_R + DB_H)[px];
+                const int d0 = (int)(sv & 0xffffu) - (int)(rv & 0xffffu), d1 = (int)(sv >> 16) - (int)(rv >> 16);
+                acc += (unsigned long long)(uint32_t)(d0 * d0 + d1 * d1);
             }
         }
 #pragma unroll

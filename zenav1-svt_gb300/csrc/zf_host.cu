@@ -1229,12 +1229,13 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         struct Slot {
             int frame, plane;
             HillClimb hc;
+            int launches = 0;
         };
         std::vector<Slot> slots;
         for (int i = 0; i < n; ++i) {
             Plan &p = plans[i];
             if (p.db_search) {
-                Slot s{i, 0, HillClimb()};
+                Slot s{i, 0, HillClimb(), 0};
                 s.hc.conv_th = p.in->preset <= 3 ? 0 : 1;
                 slots.push_back(s);
             } else {
@@ -1268,8 +1269,11 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 int need[2];
                 const int m = s.hc.needs(need);
                 if (m == 0) continue;
+                // four levels in each of a climb's first two launches (most
+                // climbs end within them), kDbLevels in later ones
                 TrialSlot t{s.frame, s.plane, {}, {}};
-                speculate(s.hc, need, m, s.hc.have[0] ? zf::kDbLevels : 4, t.levels);
+                speculate(s.hc, need, m, s.launches < 2 ? 4 : zf::kDbLevels, t.levels);
+                s.launches++;
                 ts.push_back(t);
                 owner.push_back((int)k);
             }
@@ -1287,7 +1291,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                     p.d.lf[2] = p.d.lf[3] = 0;
                     if (s.hc.result != 0 && p.nplanes == 3)
                         for (int pl = 1; pl <= 2; ++pl) {
-                            Slot c{s.frame, pl, HillClimb()};
+                            Slot c{s.frame, pl, HillClimb(), 0};
                             c.hc.conv_th = s.hc.conv_th;
                             next.push_back(c);
                         }
