@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
         // timeout the frame's error word is set, the copies already issued
         // are drained (they always land; the drain wait is long but bounded)
         // so that no box is still arriving in shared memory when the CTA ends
-        const uint32_t lim = f.wait_limit == ZF_WAIT_GIVE_UP ? 0u : f.wait_limit;  // give up at once: a test
+        const uint32_t lim = f.wait_limit == 0xFFFFFFFFu ? 0u : f.wait_limit;  // ZF_WAIT_GIVE_UP: a test
         const bool late = !mbar_wait_timed(&mbar, 0, lim, kWaitStepNs);
         if (__syncthreads_or(late)) {
             if (threadIdx.x == 0) atomicOr(&f.cdef_stats[3], 1ull);
