@@ -789,7 +789,7 @@ def run_batched(args, ctx, stream, dev, frames):
     # setting on private copies of the recon); the context goes back to the
     # default setting afterwards
     best, cands = ctx.autotune_raw(arr, n, reps=2)
-    dflt = [c for c in cands if (c["graphs"], c["stats_tma"], c["apply_group"]) == (0, 1, 8)]
+    dflt = [c for c in cands if (c["graphs"], c["stats_tma"], c["apply_group"], c["stats_tc"]) == (0, 1, 8, 1)]
     ctx.set_tune(0, 1, 8)
     tune = {"best": best, "default_ms": dflt[0]["ms"] if dflt else None, "candidates": len(cands)}
     peak = _peaks().get("hbm_gbs", 6800.0)

@@ -460,7 +460,7 @@ typedef struct zf_tune {
     int32_t graphs;             /* 0/1: CUDA-graph launch mode (zf_use_graphs) */
     int32_t stats_tma;          /* 0/1: Wiener statistics rows of 8-bit planes by TMA */
     int32_t apply_group;        /* 64-px column tiles per restoration-apply CTA: 1..16 */
-    int32_t pad;
+    int32_t stats_tc;           /* 0/1: Wiener statistics of 8-bit planes on the tensor cores */
     double ms;                  /* zf_autotune: mean device time of one call (else 0) */
 } zf_tune;
 int32_t zf_get_tune(const zf_ctx *ctx, zf_tune *out);

@@ -202,3 +202,27 @@ def test_trace_env_and_batch_frames(pkg, tmp_path):
     lines = open(path).read().splitlines()
     assert [l for l in lines if l.startswith("ZF_FRAME")] == [
         "ZF_FRAME index=%d w=%d h=%d" % (k, f.true_w, f.true_h) for k, f in enumerate(frames)]
+
+
+def test_saturated_samples_stay_exact(ctx, oracle):
+    """Samples at 0 and 255 only (every centred product at its 2^14 bound):
+    the tensor-core statistics' fp32 chains stay exact, and the whole stage
+    matches the oracle, with the tensor-core and the CUDA-core statistics."""
+    rng = np.random.default_rng(77)
+    fr = frame(9, 384, 256, 8, 36, 6, "cosine")
+    for p in range(3):
+        h, w = fr.src[p].shape
+        blocks = rng.integers(0, 2, size=(h // 4 + 1, w // 4 + 1)).astype(np.uint8) * 255
+        fr.src[p] = np.ascontiguousarray(np.repeat(np.repeat(blocks, 4, 0), 4, 1)[:h, :w])
+        fr.rec[p] = np.where(rng.random((h, w)) < 0.5, 0, 255).astype(np.uint8)
+    do, so, ro = oracle.filter_stage(fr)
+    before = ctx.get_tune()
+    try:
+        for tc in (1, 0):
+            ctx.set_tune(before["graphs"], before["stats_tma"], before["apply_group"], tc)
+            dg, sg, rg = ctx.filter_stage(fr)
+            assert_same_decisions(dg, do)
+            assert_same_planes(rg, ro)
+            assert sg == so
+    finally:
+        ctx.set_tune(before["graphs"], before["stats_tma"], before["apply_group"], before["stats_tc"])

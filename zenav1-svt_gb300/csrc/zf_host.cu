@@ -58,6 +58,7 @@ struct zf_ctx {
     bool graphs = false;
     bool capturing = false;
     bool tma = true;  // statistics kernel rows by TMA where the planes allow
+    bool stats_tc = true;  // statistics of 8-bit 5-tap planes on the tensor cores (k_lr_stats_tc)
     uint32_t wait_limit = 1u << 20;  // statistics kernel's TMA wait (iterations)
     int apply_group = 8;  // 64-px column tiles per restoration-apply CTA
     // search trace (zf_trace / ZF_TRACE): one text line per trial, filter
@@ -488,6 +489,9 @@ cudaError_t set_kernel_attributes() {
         e = cudaFuncSetAttribute(zf::k_cdef_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFinishSmemCap);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(zf::k_lr_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, kLrFinishSmemCap);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(zf::k_lr_stats_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)zf::lr_stats_tc_smem());
     if (e == cudaSuccess) e = zf::joint_set_attributes();
     if (e == cudaSuccess) e = zf::sgr_set_attributes();
     return e;
@@ -954,7 +958,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     }
     // Work lists (host-known shapes).
     // statistics: 5-tap 8-bit, 5-tap 10-bit (one kernel instantiation each), 7-tap
-    WorkList wl_db, wl_cs, wl_ca, wl_st5, wl_st7, wl_unit, wl_apply, wl_trial, wl_tiles, wl_st5h;
+    WorkList wl_db, wl_cs, wl_ca, wl_st5, wl_st7, wl_unit, wl_apply, wl_trial, wl_tiles, wl_st5h, wl_stc;
     std::vector<int> cdef_small, cdef_large;  // joint search: one CTA / cluster per bit count
     std::vector<int> cdef_joint[kJointGroups];  // register-row joint search, by (candidates, rows per thread)
     for (int i = 0; i < n; ++i) {
@@ -980,8 +984,14 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 const int uh = r.v_end - r.v_start;
                 // one item per unit; the CTA offset selects the row block
                 const int half = L.win / 2, srows = zf::stat_rows_host(L.win);
-                (L.win == 5 ? (p.d.bd == 8 ? wl_st5 : wl_st5h) : wl_st7)
-                    .add(i, pl, (int)u, 0, (uh + 2 * half + srows - 1) / srows);
+                if (L.win == 5 && p.d.bd == 8 && ctx->stats_tc) {
+                    // tensor-core statistics: one CTA per band of output rows
+                    const int tr = zf::lr_stats_tc_rows();
+                    wl_stc.add(i, pl, (int)u, 0, (uh + tr - 1) / tr);
+                } else {
+                    (L.win == 5 ? (p.d.bd == 8 ? wl_st5 : wl_st5h) : wl_st7)
+                        .add(i, pl, (int)u, 0, (uh + 2 * half + srows - 1) / srows);
+                }
                 wl_unit.add(i, pl, (int)u, 0, 1);
                 if (L.refine) {
                     // one cluster per unit: the hill-climb is sequential, its trials are not
@@ -1037,9 +1047,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     };
     const size_t desc_bytes = (size_t)n * sizeof(FrameDesc);
     const size_t m_desc = mtake(desc_bytes);
-    constexpr int kLists = 10;
-    const WorkList *lists[kLists] = {&wl_db,   &wl_cs,    &wl_ca,    &wl_st5,   &wl_st7,
-                                     &wl_unit, &wl_apply, &wl_trial, &wl_tiles, &wl_st5h};
+    constexpr int kLists = 11;
+    const WorkList *lists[kLists] = {&wl_db,   &wl_cs,    &wl_ca,    &wl_st5,   &wl_st7,  &wl_unit,
+                                     &wl_apply, &wl_trial, &wl_tiles, &wl_st5h, &wl_stc};
     size_t m_list[kLists];
     for (int k = 0; k < kLists; ++k) m_list[k] = mtake(lists[k]->bytes());
     const size_t m_cf = mtake(cdef_frames.size() * 4);
@@ -1073,7 +1083,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     const size_t o_db = o_meta + m_list[0], o_cs = o_meta + m_list[1], o_ca = o_meta + m_list[2],
                  o_st5 = o_meta + m_list[3], o_st7 = o_meta + m_list[4], o_unit = o_meta + m_list[5],
                  o_apply = o_meta + m_list[6], o_trial = o_meta + m_list[7], o_tiles = o_meta + m_list[8],
-                 o_st5h = o_meta + m_list[9], o_cf = o_meta + m_cf;
+                 o_st5h = o_meta + m_list[9], o_stc = o_meta + m_list[10], o_cf = o_meta + m_cf;
     // outputs start zeroed (statistics counters, fb_idx of skipped searches)
     CU(cudaMemsetAsync(base + o_out, 0, out_bytes, st));
 
@@ -1435,6 +1445,12 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             LaunchScope ls5_(ctx, "k_lr_stats5");
             CU(zf::launch_lr_stats(5, 8, wl_st5.ctas, st, d_desc, (const WorkItem *)(base + o_st5),
                                    (int)wl_st5.items.size()));
+        }
+        if (wl_stc.ctas) {
+            LaunchScope lt_(ctx, "k_lr_stats_tc");
+            zf::k_lr_stats_tc<<<wl_stc.ctas, 128, zf::lr_stats_tc_smem(), st>>>(
+                d_desc, (const WorkItem *)(base + o_stc), (int)wl_stc.items.size());
+            TRY(launch_check(ctx, "k_lr_stats_tc"));
         }
         if (wl_st5h.ctas) {
             LaunchScope ls5h_(ctx, "k_lr_stats5");
@@ -1817,17 +1833,19 @@ int32_t zf_get_tune(const zf_ctx *ctx, zf_tune *out) {
     out->graphs = ctx->graphs ? 1 : 0;
     out->stats_tma = ctx->tma ? 1 : 0;
     out->apply_group = ctx->apply_group;
+    out->stats_tc = ctx->stats_tc ? 1 : 0;
     return ZF_OK;
 }
 
 int32_t zf_set_tune(zf_ctx *ctx, const zf_tune *t) {
     if (!ctx || !t) return ZF_ERR_ARG;
     if (t->graphs < 0 || t->graphs > 1 || t->stats_tma < 0 || t->stats_tma > 1 || t->apply_group < 1 ||
-        t->apply_group > zf::kApplyGroupMax)
+        t->apply_group > zf::kApplyGroupMax || t->stats_tc < 0 || t->stats_tc > 1)
         return fail(ctx, ZF_ERR_ARG, "tune setting out of range");
     ctx->graphs = t->graphs != 0;
     ctx->tma = t->stats_tma != 0;
     ctx->apply_group = t->apply_group;
+    ctx->stats_tc = t->stats_tc != 0;
     return ZF_OK;
 }
 
@@ -1905,17 +1923,25 @@ int32_t zf_autotune(zf_ctx *ctx, const zf_frame *frames, int32_t n, int32_t reps
         cleanup();
         return fail(ctx, ZF_ERR_CUDA, "autotune: event creation failed");
     }
+    // candidates: graphs x statistics form (tensor cores; CUDA cores with
+    // TMA rows; CUDA cores with thread-staged rows) x apply column tiles
     static const int kGroups[5] = {1, 2, 4, 8, 16};
+    std::vector<zf_tune> grid;
+    for (int g = 0; g < 2; ++g)
+        for (int form = 0; form < 3; ++form)
+            for (int k = 0; k < 5; ++k) {
+                zf_tune c{};
+                c.graphs = g;
+                c.stats_tc = form == 0 ? 1 : 0;
+                c.stats_tma = form == 2 ? 0 : 1;
+                c.apply_group = kGroups[k];
+                grid.push_back(c);
+            }
     int count = 0, rc = ZF_OK;
     zf_tune win{};
     win.ms = -1.0;
-    for (int g = 0; g < 2 && rc == ZF_OK; ++g)
-        for (int t = 0; t < 2 && rc == ZF_OK; ++t)
-            for (int k = 0; k < 5 && rc == ZF_OK; ++k) {
-                zf_tune c{};
-                c.graphs = g;
-                c.stats_tma = t;
-                c.apply_group = kGroups[k];
+    for (size_t ci = 0; ci < grid.size() && rc == ZF_OK; ++ci) {
+                zf_tune c = grid[ci];
                 zf_set_tune(ctx, &c);
                 double total = 0.0;
                 for (int r = -1; r < reps && rc == ZF_OK; ++r) {  // r = -1: warm-up

@@ -8,6 +8,12 @@
 namespace zf {
 
 __global__ void k_deblock_apply(const FrameDesc *frames, const WorkItem *items, int nitems);
+// Wiener statistics of 8-bit 5-tap planes on the tensor cores
+// (zf_lr_tc.cu): 128 threads, lr_stats_tc_smem() dynamic shared memory,
+// one CTA per band of lr_stats_tc_rows() output rows of a unit.
+__global__ void k_lr_stats_tc(FrameDesc *frames, const WorkItem *items, int nitems);
+size_t lr_stats_tc_smem();
+int lr_stats_tc_rows();
 // levels per (frame, plane) slot in one k_deblock_sse launch (at most)
 constexpr int kDbLevels = 8;
 __global__ void k_deblock_sse(const FrameDesc *frames, const WorkItem *items, int nitems, const int *levels, int nl,
