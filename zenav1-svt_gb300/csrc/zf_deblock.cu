@@ -70,75 +70,90 @@ __device__ __forceinline__ void filter4(int mask, int hev, int *w, int bd) {
 }
 
 // One line of one edge. `p` points at q0 in shared memory, `st` is the tap
-// step (1 for vertical edges, the row pitch for horizontal edges).
+// step (1 for vertical edges, the row pitch for horizontal edges). The
+// filter mask is computed from the inner taps first: a line whose mask fails
+// is left as it is (every branch of the reference then writes back the
+// values it read), so it loads nothing more and stores nothing; otherwise
+// only the samples a branch changes are stored.
 __device__ __forceinline__ void filter_line(uint16_t *p, int st, int len, Thr t, int bd) {
-    int w[14];
-    const int half = len >> 1;
-#pragma unroll
-    for (int k = 0; k < 14; ++k)
-        if (k < len) w[k] = p[(k - half) * st];
     const int sh = bd - 8;
     const int lim = t.lim << sh, blim = t.mblim << sh, thr = t.hev << sh, one = 1 << sh;
     auto ad = [](int a, int b) { return a > b ? a - b : b - a; };
+    auto at = [&](int k) -> int { return p[k * st]; };        // k: offset from q0
+    auto put = [&](int k, int v) { p[k * st] = (uint16_t)v; };
     if (len == 4) {
-        int p1 = w[0], p0 = w[1], q0 = w[2], q1 = w[3];
-        bool m = ad(p1, p0) <= lim && ad(q1, q0) <= lim && ad(p0, q0) * 2 + ad(p1, q1) / 2 <= blim;
-        int hev = (ad(p1, p0) > thr || ad(q1, q0) > thr) ? -1 : 0;
-        filter4(m ? -1 : 0, hev, w, bd);
+        int w[4] = {at(-2), at(-1), at(0), at(1)};
+        const int p1 = w[0], p0 = w[1], q0 = w[2], q1 = w[3];
+        const bool m = ad(p1, p0) <= lim && ad(q1, q0) <= lim && ad(p0, q0) * 2 + ad(p1, q1) / 2 <= blim;
+        if (!m) return;
+        const int hev = (ad(p1, p0) > thr || ad(q1, q0) > thr) ? -1 : 0;
+        filter4(-1, hev, w, bd);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) put(k - 2, w[k]);
     } else if (len == 6) {
-        int p2 = w[0], p1 = w[1], p0 = w[2], q0 = w[3], q1 = w[4], q2 = w[5];
-        bool m = ad(p2, p1) <= lim && ad(p1, p0) <= lim && ad(q1, q0) <= lim && ad(q2, q1) <= lim &&
-                 ad(p0, q0) * 2 + ad(p1, q1) / 2 <= blim;
-        bool flat = ad(p1, p0) <= one && ad(q1, q0) <= one && ad(p2, p0) <= one && ad(q2, q0) <= one;
-        if (flat && m) {
+        int w[6] = {at(-3), at(-2), at(-1), at(0), at(1), at(2)};
+        const int p2 = w[0], p1 = w[1], p0 = w[2], q0 = w[3], q1 = w[4], q2 = w[5];
+        const bool m = ad(p2, p1) <= lim && ad(p1, p0) <= lim && ad(q1, q0) <= lim && ad(q2, q1) <= lim &&
+                       ad(p0, q0) * 2 + ad(p1, q1) / 2 <= blim;
+        if (!m) return;
+        const bool flat = ad(p1, p0) <= one && ad(q1, q0) <= one && ad(p2, p0) <= one && ad(q2, q0) <= one;
+        if (flat) {
             w[1] = (p2 * 3 + p1 * 2 + p0 * 2 + q0 + 4) >> 3;
             w[2] = (p2 + p1 * 2 + p0 * 2 + q0 * 2 + q1 + 4) >> 3;
             w[3] = (p1 + p0 * 2 + q0 * 2 + q1 * 2 + q2 + 4) >> 3;
             w[4] = (p0 + q0 * 2 + q1 * 2 + q2 * 3 + 4) >> 3;
         } else {
-            int hev = (ad(p1, p0) > thr || ad(q1, q0) > thr) ? -1 : 0;
-            filter4(m ? -1 : 0, hev, w + 1, bd);
+            const int hev = (ad(p1, p0) > thr || ad(q1, q0) > thr) ? -1 : 0;
+            filter4(-1, hev, w + 1, bd);
         }
+#pragma unroll
+        for (int k = 1; k < 5; ++k) put(k - 3, w[k]);
     } else {
-        int *v = len == 8 ? w : w + 3;  // the [p3..q3] window
-        int p3 = v[0], p2 = v[1], p1 = v[2], p0 = v[3], q0 = v[4], q1 = v[5], q2 = v[6], q3 = v[7];
-        bool m = ad(p3, p2) <= lim && ad(p2, p1) <= lim && ad(p1, p0) <= lim && ad(q1, q0) <= lim &&
-                 ad(q2, q1) <= lim && ad(q3, q2) <= lim && ad(p0, q0) * 2 + ad(p1, q1) / 2 <= blim;
-        bool flat = ad(p1, p0) <= one && ad(q1, q0) <= one && ad(p2, p0) <= one && ad(q2, q0) <= one &&
-                    ad(p3, p0) <= one && ad(q3, q0) <= one;
-        bool flat2 = false;
-        if (len == 14)
-            flat2 = ad(w[1], p0) <= one && ad(w[12], q0) <= one && ad(w[2], p0) <= one && ad(w[11], q0) <= one &&
-                    ad(w[0], p0) <= one && ad(w[13], q0) <= one;
-        if (len == 14 && flat2 && flat && m) {
-            int p6 = w[0], p5 = w[1], p4 = w[2], q4 = w[11], q5 = w[12], q6 = w[13];
-            w[1] = (p6 * 7 + p5 * 2 + p4 * 2 + p3 + p2 + p1 + p0 + q0 + 8) >> 4;
-            w[2] = (p6 * 5 + p5 * 2 + p4 * 2 + p3 * 2 + p2 + p1 + p0 + q0 + q1 + 8) >> 4;
-            w[3] = (p6 * 4 + p5 + p4 * 2 + p3 * 2 + p2 * 2 + p1 + p0 + q0 + q1 + q2 + 8) >> 4;
-            w[4] = (p6 * 3 + p5 + p4 + p3 * 2 + p2 * 2 + p1 * 2 + p0 + q0 + q1 + q2 + q3 + 8) >> 4;
-            w[5] = (p6 * 2 + p5 + p4 + p3 + p2 * 2 + p1 * 2 + p0 * 2 + q0 + q1 + q2 + q3 + q4 + 8) >> 4;
-            w[6] = (p6 + p5 + p4 + p3 + p2 + p1 * 2 + p0 * 2 + q0 * 2 + q1 + q2 + q3 + q4 + q5 + 8) >> 4;
-            w[7] = (p5 + p4 + p3 + p2 + p1 + p0 * 2 + q0 * 2 + q1 * 2 + q2 + q3 + q4 + q5 + q6 + 8) >> 4;
-            w[8] = (p4 + p3 + p2 + p1 + p0 + q0 * 2 + q1 * 2 + q2 * 2 + q3 + q4 + q5 + q6 * 2 + 8) >> 4;
-            w[9] = (p3 + p2 + p1 + p0 + q0 + q1 * 2 + q2 * 2 + q3 * 2 + q4 + q5 + q6 * 3 + 8) >> 4;
-            w[10] = (p2 + p1 + p0 + q0 + q1 + q2 * 2 + q3 * 2 + q4 * 2 + q5 + q6 * 4 + 8) >> 4;
-            w[11] = (p1 + p0 + q0 + q1 + q2 + q3 * 2 + q4 * 2 + q5 * 2 + q6 * 5 + 8) >> 4;
-            w[12] = (p0 + q0 + q1 + q2 + q3 + q4 * 2 + q5 * 2 + q6 * 7 + 8) >> 4;
-        } else if (flat && m) {
-            v[1] = (p3 + p3 + p3 + 2 * p2 + p1 + p0 + q0 + 4) >> 3;
-            v[2] = (p3 + p3 + p2 + 2 * p1 + p0 + q0 + q1 + 4) >> 3;
-            v[3] = (p3 + p2 + p1 + 2 * p0 + q0 + q1 + q2 + 4) >> 3;
-            v[4] = (p2 + p1 + p0 + 2 * q0 + q1 + q2 + q3 + 4) >> 3;
-            v[5] = (p1 + p0 + q0 + 2 * q1 + q2 + q3 + q3 + 4) >> 3;
-            v[6] = (p0 + q0 + q1 + 2 * q2 + q3 + q3 + q3 + 4) >> 3;
+        // the [p3..q3] window first; the outer taps of the 14-tap filter
+        // only when the line is flat
+        int v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = at(k - 4);
+        const int p3 = v[0], p2 = v[1], p1 = v[2], p0 = v[3], q0 = v[4], q1 = v[5], q2 = v[6], q3 = v[7];
+        const bool m = ad(p3, p2) <= lim && ad(p2, p1) <= lim && ad(p1, p0) <= lim && ad(q1, q0) <= lim &&
+                       ad(q2, q1) <= lim && ad(q3, q2) <= lim && ad(p0, q0) * 2 + ad(p1, q1) / 2 <= blim;
+        if (!m) return;
+        const bool flat = ad(p1, p0) <= one && ad(q1, q0) <= one && ad(p2, p0) <= one && ad(q2, q0) <= one &&
+                          ad(p3, p0) <= one && ad(q3, q0) <= one;
+        if (len == 14 && flat) {
+            const int p6 = at(-7), p5 = at(-6), p4 = at(-5), q4 = at(4), q5 = at(5), q6 = at(6);
+            const bool flat2 = ad(p5, p0) <= one && ad(q5, q0) <= one && ad(p4, p0) <= one && ad(q4, q0) <= one &&
+                               ad(p6, p0) <= one && ad(q6, q0) <= one;
+            if (flat2) {
+                put(-6, (p6 * 7 + p5 * 2 + p4 * 2 + p3 + p2 + p1 + p0 + q0 + 8) >> 4);
+                put(-5, (p6 * 5 + p5 * 2 + p4 * 2 + p3 * 2 + p2 + p1 + p0 + q0 + q1 + 8) >> 4);
+                put(-4, (p6 * 4 + p5 + p4 * 2 + p3 * 2 + p2 * 2 + p1 + p0 + q0 + q1 + q2 + 8) >> 4);
+                put(-3, (p6 * 3 + p5 + p4 + p3 * 2 + p2 * 2 + p1 * 2 + p0 + q0 + q1 + q2 + q3 + 8) >> 4);
+                put(-2, (p6 * 2 + p5 + p4 + p3 + p2 * 2 + p1 * 2 + p0 * 2 + q0 + q1 + q2 + q3 + q4 + 8) >> 4);
+                put(-1, (p6 + p5 + p4 + p3 + p2 + p1 * 2 + p0 * 2 + q0 * 2 + q1 + q2 + q3 + q4 + q5 + 8) >> 4);
+                put(0, (p5 + p4 + p3 + p2 + p1 + p0 * 2 + q0 * 2 + q1 * 2 + q2 + q3 + q4 + q5 + q6 + 8) >> 4);
+                put(1, (p4 + p3 + p2 + p1 + p0 + q0 * 2 + q1 * 2 + q2 * 2 + q3 + q4 + q5 + q6 * 2 + 8) >> 4);
+                put(2, (p3 + p2 + p1 + p0 + q0 + q1 * 2 + q2 * 2 + q3 * 2 + q4 + q5 + q6 * 3 + 8) >> 4);
+                put(3, (p2 + p1 + p0 + q0 + q1 + q2 * 2 + q3 * 2 + q4 * 2 + q5 + q6 * 4 + 8) >> 4);
+                put(4, (p1 + p0 + q0 + q1 + q2 + q3 * 2 + q4 * 2 + q5 * 2 + q6 * 5 + 8) >> 4);
+                put(5, (p0 + q0 + q1 + q2 + q3 + q4 * 2 + q5 * 2 + q6 * 7 + 8) >> 4);
+                return;
+            }
+        }
+        if (flat) {
+            put(-3, (p3 + p3 + p3 + 2 * p2 + p1 + p0 + q0 + 4) >> 3);
+            put(-2, (p3 + p3 + p2 + 2 * p1 + p0 + q0 + q1 + 4) >> 3);
+            put(-1, (p3 + p2 + p1 + 2 * p0 + q0 + q1 + q2 + 4) >> 3);
+            put(0, (p2 + p1 + p0 + 2 * q0 + q1 + q2 + q3 + 4) >> 3);
+            put(1, (p1 + p0 + q0 + 2 * q1 + q2 + q3 + q3 + 4) >> 3);
+            put(2, (p0 + q0 + q1 + 2 * q2 + q3 + q3 + q3 + 4) >> 3);
         } else {
-            int hev = (ad(p1, p0) > thr || ad(q1, q0) > thr) ? -1 : 0;
-            filter4(m ? -1 : 0, hev, v + 2, bd);
+            const int hev = (ad(p1, p0) > thr || ad(q1, q0) > thr) ? -1 : 0;
+            filter4(-1, hev, v + 2, bd);
+#pragma unroll
+            for (int k = 2; k < 6; ++k) put(k - 4, v[k]);
         }
     }
-#pragma unroll
-    for (int k = 0; k < 14; ++k)
-        if (k < len) p[(k - half) * st] = (uint16_t)w[k];
 }
 
 // Transform dims of a packed mi for a plane: luma TX grid, or the chroma TX
@@ -322,7 +337,7 @@ __device__ __forceinline__ void plane_geom(const FrameDesc &f, int plane, int *p
 // Apply: IN -> B for one 64x64 tile. Plane gating of apply_deblock_frame
 // (deblock.rs:951-967): both luma levels zero disables every plane; a chroma
 // plane needs its own level.
-__global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, const WorkItem *items, int nitems) {
+__global__ void __launch_bounds__(256, 5) k_deblock_apply(const FrameDesc *frames, const WorkItem *items, int nitems) {
     __shared__ __align__(16) uint16_t reg[DB_R * DB_R];
     __shared__ DbEdges edges;
     const int it = find_item(items, nitems, blockIdx.x);
@@ -394,7 +409,7 @@ __global__ void __launch_bounds__(256) k_deblock_apply(const FrameDesc *frames, 
 // tile and its halo are staged once and filtered at every level of the
 // slot. items[].a = slot index; levels[slot * nl + k] (< 0: unused) and
 // sse[slot * nl + k] the SSE accumulated for it.
-__global__ void __launch_bounds__(256) k_deblock_sse(const FrameDesc *frames, const WorkItem *items, int nitems,
+__global__ void __launch_bounds__(256, 5) k_deblock_sse(const FrameDesc *frames, const WorkItem *items, int nitems,
                                                      const int *levels, int nl, unsigned long long *sse) {
     __shared__ __align__(16) uint16_t reg[DB_R * DB_R];
     __shared__ __align__(16) uint16_t pristine[DB_R * DB_R];
