@@ -264,6 +264,36 @@ KERNEL_DRAM_BYTES_PER_PX = {
 }
 
 
+# Warp instructions executed per luma pixel of the plain 4K step, per
+# kernel (ncu smsp__inst_executed.sum summed over the kernel's launches in
+# one pass of the bench's four frames, divided by their luma pixels). The
+# issue roofline of these integer-instruction-bound kernels: achieved warp
+# instructions per second (these counts over the bench's own CUDA-event
+# times of the same step) against the issue peak, four warp instructions
+# per clock per SM at the SM clock sampled during the timed region.
+KERNEL_WARP_INST_PER_PX = {}
+
+
+def issue_roofline(prof, frames, sm_count, sm_mhz):
+    """int_frac of the three kernels with the largest device time in one step."""
+    if not KERNEL_WARP_INST_PER_PX or not sm_mhz:
+        return None
+    peak = 4.0 * sm_count * sm_mhz * 1e6  # warp instructions per second
+    px_step = float(sum(f.luma_px for f in frames))
+    out = []
+    for name, (nl, ms) in sorted(prof.items(), key=lambda kv: -kv[1][1]):
+        ipp = KERNEL_WARP_INST_PER_PX.get(name)
+        if ipp is None or ms <= 0:
+            continue
+        achieved = ipp * px_step / (ms / 1e3)
+        out.append({"kernel": name, "warp_inst_per_px": round(ipp, 4), "achieved_winst_per_s": round(achieved, 1),
+                    "peak_winst_per_s": round(peak, 1), "int_frac": round(achieved / peak, 4)})
+        if len(out) == 3:
+            break
+    return {"unit": "warp instructions/s", "peak": "4 warp instructions/clock/SM x %d SMs x %.0f MHz (sampled)"
+            % (sm_count, sm_mhz), "kernels": out}
+
+
 def run_ours(args):
     import torch
     rank, world, local = env_rank()
@@ -444,6 +474,11 @@ def run_ours(args):
                         "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e_ms, 3)},
                 "gpu_launches": int(launches),
                 "roofline": roofline, "kernels": kernels, "clocks": clk, "graphs": graphs}
+        sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+        ir = issue_roofline(prof, frames, sm_count, clk.get("sm_mhz"))
+        if ir:
+            line["roofline"]["int"] = ir
+            line["roofline"]["int_frac"] = {k["kernel"]: k["int_frac"] for k in ir["kernels"]}
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_sample()
         if world == 1:
@@ -789,7 +824,7 @@ def run_batched(args, ctx, stream, dev, frames):
     # setting on private copies of the recon); the context goes back to the
     # default setting afterwards
     best, cands = ctx.autotune_raw(arr, n, reps=2)
-    dflt = [c for c in cands if (c["graphs"], c["stats_tma"], c["apply_group"], c["stats_tc"]) == (0, 1, 8, 1)]
+    dflt = [c for c in cands if (c["graphs"], c["stats_tma"], c["apply_group"], c["stats_tc"]) == (0, 1, 8, 0)]
     ctx.set_tune(0, 1, 8)
     tune = {"best": best, "default_ms": dflt[0]["ms"] if dflt else None, "candidates": len(cands)}
     peak = _peaks().get("hbm_gbs", 6800.0)
@@ -857,7 +892,7 @@ def run_served(args, device, frames):
         srv.drain(timeout=600)
     out = {}
     import gc
-    for rate in (50, 200, 800):
+    for rate in args.served_rates:
         arrivals = synth.poisson_arrivals(rate, args.served_seconds, seed=rate)
         reqs = []
         # no collector pauses inside the measured window (a full collection
@@ -904,6 +939,9 @@ def run_profile(args):
     from zenav1_svt_gb300 import abi, synth
     frames = make_workload(args.pw, args.ph)[:args.nframes]  # the timed frames (same seeds)
     ctx = pkg.Context(0)
+    if args.stats_tc:
+        t = ctx.get_tune()
+        ctx.set_tune(t["graphs"], t["stats_tma"], t["apply_group"], 1)
     dev = torch.device("cuda", 0)
     keep, structs, pairs = [], [], []
     for f in frames:
@@ -940,10 +978,12 @@ def main():
     ap.add_argument("--pw", type=int, default=W4K)
     ap.add_argument("--ph", type=int, default=H4K)
     ap.add_argument("--nframes", type=int, default=4)
+    ap.add_argument("--stats-tc", action="store_true", help="profile run: tensor-core Wiener statistics")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-image batch")
     ap.add_argument("--no-served", action="store_true", help="skip the served request loop")
     ap.add_argument("--batch-n", type=int, default=256)
     ap.add_argument("--served-seconds", type=float, default=4.0, help="arrival window per rate")
+    ap.add_argument("--served-rates", type=int, nargs="+", default=[50, 200, 800], help="arrival rates (req/s)")
     args = ap.parse_args()
     if args.profile_run:
         return run_profile(args)

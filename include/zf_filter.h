@@ -460,7 +460,8 @@ typedef struct zf_tune {
     int32_t graphs;             /* 0/1: CUDA-graph launch mode (zf_use_graphs) */
     int32_t stats_tma;          /* 0/1: Wiener statistics rows of 8-bit planes by TMA */
     int32_t apply_group;        /* 64-px column tiles per restoration-apply CTA: 1..16 */
-    int32_t stats_tc;           /* 0/1: Wiener statistics of 8-bit planes on the tensor cores */
+    int32_t stats_tc;           /* 0/1: Wiener statistics of 8-bit planes on the tensor cores
+                                   (default 0: the CUDA-core form measured faster) */
     double ms;                  /* zf_autotune: mean device time of one call (else 0) */
 } zf_tune;
 int32_t zf_get_tune(const zf_ctx *ctx, zf_tune *out);
@@ -482,7 +483,8 @@ int32_t zf_autotune(zf_ctx *ctx, const zf_frame *frames, int32_t n, int32_t reps
                     zf_tune *cands, int32_t max);
 
 /* Iteration limit of the one device-side wait of the stage (the Wiener
- * statistics kernel waiting for its TMA tile loads), in steps of about
+ * statistics kernels waiting for their TMA tile loads or, in the tensor-
+ * core form, for their MMAs), in steps of about
  * 100 ns (mbarrier try_wait with a suspend-time hint); 0 restores the
  * default of 2^20 steps, far beyond any real load. A CTA that gives up
  * drains its loads, records the timeout and the call returns

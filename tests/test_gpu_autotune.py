@@ -45,7 +45,7 @@ def test_every_setting_gives_the_same_bytes(ctx):
     frames = _frames()
     before = ctx.get_tune()
     try:
-        ctx.set_tune(0, 1, 8, 0)  # the CUDA-core statistics as the reference setting
+        ctx.set_tune(0, 1, 8, 0)  # the default setting as the reference
         ref = ctx.submit_batch(frames)
         for setting in ((0, 0, 1, 0), (1, 1, 16, 1), (0, 1, 2, 0), (1, 0, 3, 1), (0, 1, 8, 1)):
             ctx.set_tune(*setting)

@@ -45,9 +45,14 @@ def test_cancel_flag_refuses_then_recovers(pkg, oracle):
         c.close()
 
 
-def test_statistics_wait_limit_times_out_and_context_recovers(ctx, pkg, oracle):
+@pytest.mark.parametrize("stats_tc", [0, 1], ids=["tma_rows", "tensor_core_mma"])
+def test_statistics_wait_limit_times_out_and_context_recovers(ctx, pkg, oracle, stats_tc):
+    """Both statistics forms: the CUDA-core kernel waits for its TMA tile
+    loads, the tensor-core kernel for its MMAs."""
     # 8-bit, 16-aligned planes: the statistics rows come by TMA
     fr = synth.make_frame(synth.frame_seed(13, 2), 1024, 768, 8, 30, 6, "cosine")
+    before = ctx.get_tune()
+    ctx.set_tune(before["graphs"], 1, before["apply_group"], stats_tc)
     ctx.set_wait_limit(0xFFFFFFFF)  # ZF_WAIT_GIVE_UP: give up before the first step
     try:
         with pytest.raises(pkg.ZfError) as e:
@@ -55,8 +60,11 @@ def test_statistics_wait_limit_times_out_and_context_recovers(ctx, pkg, oracle):
         assert e.value.kind == "Timeout"
     finally:
         ctx.set_wait_limit(0)
-    do, so, ro = oracle.filter_stage(fr)
-    dg, sg, rg = ctx.filter_stage(fr)
-    assert_same_decisions(dg, do)
-    assert_same_planes(rg, ro)
-    assert sg == so
+    try:
+        do, so, ro = oracle.filter_stage(fr)
+        dg, sg, rg = ctx.filter_stage(fr)
+        assert_same_decisions(dg, do)
+        assert_same_planes(rg, ro)
+        assert sg == so
+    finally:
+        ctx.set_tune(before["graphs"], before["stats_tma"], before["apply_group"], before["stats_tc"])

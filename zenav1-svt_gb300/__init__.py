@@ -209,7 +209,7 @@ class Context:
         self._check(lib().zf_get_tune(self.h, C.byref(t)))
         return t.as_dict()
 
-    def set_tune(self, graphs, stats_tma, apply_group, stats_tc=1):
+    def set_tune(self, graphs, stats_tma, apply_group, stats_tc=0):
         """Set the launch settings (zf_set_tune)."""
         t = abi.ZfTune(graphs, stats_tma, apply_group, stats_tc, 0.0)
         self._check(lib().zf_set_tune(self.h, C.byref(t)))

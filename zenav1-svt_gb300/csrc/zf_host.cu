@@ -58,7 +58,7 @@ struct zf_ctx {
     bool graphs = false;
     bool capturing = false;
     bool tma = true;  // statistics kernel rows by TMA where the planes allow
-    bool stats_tc = true;  // statistics of 8-bit 5-tap planes on the tensor cores (k_lr_stats_tc)
+    bool stats_tc = false;  // statistics of 8-bit 5-tap planes on the tensor cores (k_lr_stats_tc)
     uint32_t wait_limit = 1u << 20;  // statistics kernel's TMA wait (iterations)
     int apply_group = 8;  // 64-px column tiles per restoration-apply CTA
     // search trace (zf_trace / ZF_TRACE): one text line per trial, filter

@@ -61,7 +61,6 @@ constexpr int THREADS = 128;
 constexpr uint32_t TMEM_COLS = 128;      // sets 0 and 1 at columns 0 and 64, N = 40 each
 // instruction descriptor: D f32, A and B f16, both K-major, N = 40, M = 64
 constexpr uint32_t IDESC = (1u << 4) | ((40u >> 3) << 17) | ((64u >> 4) << 24);
-constexpr uint32_t kMmaWaitLimit = 1u << 22;
 
 struct Smem {
     uint8_t stream[STREAM];
@@ -172,7 +171,7 @@ __global__ void __launch_bounds__(lrtc::THREADS, 3) k_lr_stats_tc(FrameDesc *fra
         // 1. e = d - 128 over the band's window rows and the tile's columns
         //    (-2 .. TW + 2), coordinates clamped to the plane
         const int er = rows + 4;
-#pragma unroll 1
+#pragma unroll 4
         for (int i = t; i < er * (TW + 4); i += THREADS) {
             const int yy = i / (TW + 4), xx = i - yy * (TW + 4);
             const int gy = clampi(ur.v_start + y0 - 2 + yy, 0, pl.ph - 1);
@@ -182,7 +181,7 @@ __global__ void __launch_bounds__(lrtc::THREADS, 3) k_lr_stats_tc(FrameDesc *fra
         __syncthreads();
         // 2. s - 128 at the output pixels (0 past the tile's valid columns),
         //    sum s and the sse_region parts
-#pragma unroll 1
+#pragma unroll 4
         for (int i = t; i < rows * TW; i += THREADS) {
             const int yy = i / TW, xx = i - yy * TW;
             int sv = 0;
@@ -252,9 +251,11 @@ __global__ void __launch_bounds__(lrtc::THREADS, 3) k_lr_stats_tc(FrameDesc *fra
                          : "memory");
         }
         // 5. bounded wait for the MMAs (the stream and the accumulators are
-        //    reused after it); on a timeout the frame's error word is set and
-        //    the MMAs are waited for once more before the CTA frees its columns
-        const bool late = !mbar_wait_bounded(&S.mbar, phase, kMmaWaitLimit);
+        //    reused after it; the context's wait limit, in ~100 ns steps); on
+        //    a timeout the frame's error word is set and the MMAs are waited
+        //    for once more before the CTA frees its tensor-memory columns
+        const uint32_t lim = f.wait_limit == 0xFFFFFFFFu ? 0u : f.wait_limit;  // ZF_WAIT_GIVE_UP: a test
+        const bool late = !mbar_wait_timed(&S.mbar, phase, lim, kWaitStepNs);
         if (__syncthreads_or(late)) {
             if (t == 0) atomicOr(&f.cdef_stats[3], 2ull);
             mbar_wait_bounded(&S.mbar, phase, kDrainWaitLimit);
