@@ -1157,7 +1157,9 @@ constexpr int TL = 64;
 constexpr int kTileEdges = 3;  // stripe edges whose rows can meet a 64-row tile (stripes >= 32 rows)
 
 __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const WorkItem *items, int nitems) {
-    constexpr int SW = TL + 7, SR = TL + 7 + 4 * kTileEdges;
+    // staged rows of TL + 7 samples at a pitch of TL + 8 (8-byte aligned
+    // rows: the horizontal pass reads each run with three 8-byte loads)
+    constexpr int SW = TL + 8, SR = TL + 7 + 4 * kTileEdges;
     __shared__ __align__(16) uint16_t stage[SR * SW];
     __shared__ __align__(16) uint16_t tmp[SR * TL];
     __shared__ __align__(16) uint16_t srct[TL * TL];
@@ -1232,10 +1234,16 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
             for (int q = threadIdx.x; q < rows * (TL / 4); q += blockDim.x) {
                 const int rr = q >> 4, c0 = (q & 15) * 4;
                 if (c0 >= tw) continue;
-                const uint16_t *sp = stage + rr * SW + c0;
-                int p[11];
+                const uint2 *sp = reinterpret_cast<const uint2 *>(stage + rr * SW + c0);
+                int p[12];
 #pragma unroll
-                for (int k = T5 ? 1 : 0; k < (T5 ? 9 : 11); ++k) p[k] = sp[k];
+                for (int k = 0; k < 3; ++k) {
+                    const uint2 w = sp[k];
+                    p[4 * k] = (int)(w.x & 0xffffu);
+                    p[4 * k + 1] = (int)(w.x >> 16);
+                    p[4 * k + 2] = (int)(w.y & 0xffffu);
+                    p[4 * k + 3] = (int)(w.y >> 16);
+                }
                 uint32_t o[4];
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
@@ -1271,44 +1279,72 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         const int sum = p[3] * c3 + vf[0] * (p[0] + p[6]) + vf[1] * (p[1] + p[5]) + vf[2] * (p[2] + p[4]) + voff;
         return clampi((sum + (1 << 10)) >> 11, 0, vmax);
     };
-    auto edge_row = [&](int y) {  // y within 3 rows of a stripe edge of this tile
-        bool hit = false;
-#pragma unroll
-        for (int e = 0; e < kTileEdges; ++e) hit |= y >= eb[e] - 3 && y < eb[e] + 3;
-        return hit;
-    };
     const uint64_t write_rows = s_rows[0] | ((uint64_t)s_rows[1] << 32);
     const uint64_t bottom_rows = s_rows[2] | ((uint64_t)s_rows[3] << 32);
-    // vertical: runs of four rows x 64 columns, SSE parts, trial output.
-    // A thread takes at most 16 pixels of a tile, each e^2 <= 1023^2, so
-    // its SSE parts fit u32.
+    // vertical: each thread takes four adjacent columns of one row (seven
+    // 8-byte loads of tmp, pair sums of two columns per 32-bit add), its
+    // SSE parts and one packed store of the trial output. A thread takes at
+    // most 16 pixels of a tile, each e^2 <= 1023^2, so its SSE parts fit
+    // u32. tmp values are < 2^15, so two packed 16-bit lanes add without
+    // carrying into each other.
     uint32_t blk32 = 0, rgt32 = 0, bot32 = 0;
+    // plane rows and tile columns keep 4-sample groups word aligned when
+    // the plane base is (an arena plane always is; a caller's may not be)
+    const bool out_aligned = ((uintptr_t)outp & (bd == 8 ? 3u : 7u)) == 0;
     auto vpass = [&](auto t5c) {
         constexpr bool T5 = decltype(t5c)::value;
-        for (int q = threadIdx.x; q < ((th + 3) >> 2) * TL; q += blockDim.x) {
-            const int r0 = (q >> 6) * 4, cc = q & (TL - 1);
-            if (cc >= tw) continue;
-            int p[11];
+        for (int q = threadIdx.x; q < th * (TL / 4); q += blockDim.x) {
+            const int rr = q >> 4, c0 = (q & 15) * 4;
+            if (c0 >= tw) continue;
+            uint2 v[7];
 #pragma unroll
-            for (int k = T5 ? 1 : 0; k < (T5 ? 9 : 11); ++k) p[k] = tmp[(r0 + k) * TL + cc];
-            const bool right = tx + cc >= uw - dw;
-#pragma unroll
-            for (int jj = 0; jj < 4; ++jj) {
-                const int rr = r0 + jj;
-                if (rr >= th) break;
-                int y;
-                if (T5) {
-                    const int *pp = p + jj;
-                    const int sum = pp[3] * c3 + vf[1] * (pp[1] + pp[5]) + vf[2] * (pp[2] + pp[4]) + voff;
-                    y = clampi((sum + (1 << 10)) >> 11, 0, vmax);
+            for (int k = T5 ? 1 : 0; k < (T5 ? 6 : 7); ++k)
+                v[k] = *reinterpret_cast<const uint2 *>(tmp + (rr + k) * TL + c0);
+            // packed pair sums (columns c0, c0 + 1 in .x; c0 + 2, c0 + 3 in .y)
+            const uint32_t p1x = v[1].x + v[5].x, p1y = v[1].y + v[5].y;
+            const uint32_t p2x = v[2].x + v[4].x, p2y = v[2].y + v[4].y;
+            uint32_t p0x = 0, p0y = 0;
+            if (!T5) {
+                p0x = v[0].x + v[6].x;
+                p0y = v[0].y + v[6].y;
+            }
+            auto lo = [](uint32_t w) { return (int)(w & 0xffffu); };
+            auto hi = [](uint32_t w) { return (int)(w >> 16); };
+            auto out = [&](int c, int p1, int p2, int p0) {
+                int sum = c * c3 + vf[1] * p1 + vf[2] * p2 + voff;
+                if (!T5) sum += vf[0] * p0;
+                return clampi((sum + (1 << 10)) >> 11, 0, vmax);
+            };
+            int y[4];
+            y[0] = out(lo(v[3].x), lo(p1x), lo(p2x), lo(p0x));
+            y[1] = out(hi(v[3].x), hi(p1x), hi(p2x), hi(p0x));
+            y[2] = out(lo(v[3].y), lo(p1y), lo(p2y), lo(p0y));
+            y[3] = out(hi(v[3].y), hi(p1y), hi(p2y), hi(p0y));
+            const int nq = min(4, tw - c0);
+            if ((write_rows >> rr) & 1) {
+                const int64_t o = (int64_t)(y0 + rr) * stride + x0 + c0;
+                if (nq == 4 && !out_aligned) {
+                    for (int j = 0; j < 4; ++j) stpx(outp, o + j, bd, y[j]);
+                } else if (nq == 4 && bd == 8) {
+                    *reinterpret_cast<uint32_t *>(outp + o) =
+                        (uint32_t)y[0] | (uint32_t)y[1] << 8 | (uint32_t)y[2] << 16 | (uint32_t)y[3] << 24;
+                } else if (nq == 4) {
+                    *reinterpret_cast<uint2 *>(outp + o * 2) =
+                        make_uint2((uint32_t)y[0] | (uint32_t)y[1] << 16, (uint32_t)y[2] | (uint32_t)y[3] << 16);
                 } else {
-                    y = vert(p + jj);
+                    for (int j = 0; j < nq; ++j) stpx(outp, o + j, bd, y[j]);
                 }
-                if ((write_rows >> rr) & 1) stpx(outp, (int64_t)(y0 + rr) * stride + x0 + cc, bd, y);
-                const int e = (int)srct[rr * TL + cc] - y;
+            }
+            const uint2 sv = *reinterpret_cast<const uint2 *>(srct + rr * TL + c0);
+            const int sx[4] = {lo(sv.x), hi(sv.x), lo(sv.y), hi(sv.y)};
+            const bool bottom = (bottom_rows >> rr) & 1;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (j >= nq) break;
+                const int e = sx[j] - y[j];
                 const uint32_t e2 = (uint32_t)(e * e);
-                if (right) rgt32 += e2;
-                else if ((bottom_rows >> rr) & 1) bot32 += e2;
+                if (tx + c0 + j >= uw - dw) rgt32 += e2;
+                else if (bottom) bot32 += e2;
                 else blk32 += e2;
             }
         }
