@@ -937,7 +937,12 @@ def run_profile(args):
     ge.build()
     pkg = ge._pkg()
     from zenav1_svt_gb300 import abi, synth
-    frames = make_workload(args.pw, args.ph)[:args.nframes]  # the timed frames (same seeds)
+    if args.workload == "highres10":
+        frames = [synth.workload_10bit_4096()]
+    elif args.workload == "batch":
+        frames = synth.workload_batch(n=args.batch_n)
+    else:
+        frames = make_workload(args.pw, args.ph)[:args.nframes]  # the timed frames (same seeds)
     ctx = pkg.Context(0)
     if args.stats_tc:
         t = ctx.get_tune()
@@ -979,6 +984,8 @@ def main():
     ap.add_argument("--ph", type=int, default=H4K)
     ap.add_argument("--nframes", type=int, default=4)
     ap.add_argument("--stats-tc", action="store_true", help="profile run: tensor-core Wiener statistics")
+    ap.add_argument("--workload", default="plain4k", choices=["plain4k", "highres10", "batch"],
+                    help="profile run: the frames to run (one zf_filter_stage per frame)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-image batch")
     ap.add_argument("--no-served", action="store_true", help="skip the served request loop")
     ap.add_argument("--batch-n", type=int, default=256)

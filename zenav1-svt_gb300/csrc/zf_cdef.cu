@@ -547,7 +547,6 @@ constexpr int kFinClusterMax = 16;  // non-portable cluster size, where the devi
 constexpr int kFinThreads = 512;
 constexpr int kFinWarps = kFinThreads / 32;
 constexpr int kFinRowsPerLane = 8;  // register-cached best for up to 256 rows per CTA
-constexpr int kFinPushPairs = 512;  // push partials to every rank up to this many pairs (64 KiB)
 
 __global__ void __launch_bounds__(kFinThreads, 1)
     k_cdef_finish(FrameDesc *frames, const int *frame_ids, int smem_bytes) {
@@ -583,13 +582,16 @@ __global__ void __launch_bounds__(kFinThreads, 1)
         __syncthreads();
     }
     const int sbr = scan[T - 1];
-    // Pair partials. push: every CTA stores its partials into every rank's
-    // inbox[buf][rank][pair] before the barrier, so the sums read local
-    // shared memory; else (many pairs) each CTA keeps tot[buf][pair] and the
-    // sums read the other ranks' copies.
-    const bool push = npairs <= kFinPushPairs;
-    const int pslots = push ? CL * npairs : npairs;
+    // Pair partials, reduce-scatter: pair p is owned by rank p % CL; every
+    // CTA stores its partial of p into the owner's inbox[buf][src rank][p /
+    // CL] (one remote store per pair), the owners sum their pairs and take
+    // the argmin over them, and the CL (best, pair) results are gathered
+    // into every rank (one remote store per rank).
+    const int owned = (npairs + CL - 1) / CL;
+    const int pslots = CL * owned;
     unsigned long long *tot[2] = {dyn64, dyn64 + pslots};
+    __shared__ unsigned long long g_bv[2][kFinClusterMax];
+    __shared__ int g_bi[2][kFinClusterMax];
     uint32_t *dyn = reinterpret_cast<uint32_t *>(dyn64 + 2 * pslots);
     const bool in_smem = (size_t)2 * pslots * 8 + (size_t)sbr * (n2 + 1) * 4 <= (size_t)smem_bytes;
     uint32_t *R = in_smem ? dyn : f.cdef_rows32 + ((size_t)level * nfb + fb0) * n2;
@@ -671,26 +673,41 @@ __global__ void __launch_bounds__(kFinThreads, 1)
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (push) {
-                if (lane < CL) *cl.map_shared_rank(tot[buf] + rank * npairs + p, lane) = acc;
-            } else if (lane == 0) {
-                tot[buf][p] = acc;
+            if (lane == 0) *cl.map_shared_rank(tot[buf] + rank * owned + p / CL, p % CL) = acc;
+        }
+        cl.sync();  // partials of this step delivered to their owners
+        // warp 0: the argmin over this rank's pairs p = rank + CL k, then the
+        // (best, pair) into every rank's gather slot
+        if (warp == 0) {
+            unsigned long long bv = ~0ull;
+            int bi = 0x7fffffff;
+            for (int k = lane; k < owned; k += 32) {
+                const int p = rank + CL * k;
+                if (p >= npairs) break;
+                unsigned long long v = 0;
+                for (int r = 0; r < CL; ++r) v += tot[buf][r * owned + k];
+                if (v < bv) {  // p increases along a lane: strict < keeps the lowest
+                    bv = v;
+                    bi = p;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov < bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (lane < CL) {
+                *cl.map_shared_rank(&g_bv[buf][rank], lane) = bv;
+                *cl.map_shared_rank(&g_bi[buf][rank], lane) = bi;
             }
         }
-        cl.sync();  // partials of this step complete (and delivered) everywhere
-        unsigned long long bv = ~0ull;
-        int bi = 0x7fffffff;
-        for (int p = lane; p < npairs; p += 32) {
-            unsigned long long v = 0;
-            if (push)
-                for (int r = 0; r < CL; ++r) v += tot[buf][r * npairs + p];
-            else
-                for (int r = 0; r < CL; ++r) v += cl.map_shared_rank(tot[buf], r)[p];
-            if (v < bv) {  // p increases along a lane: strict < keeps the lowest
-                bv = v;
-                bi = p;
-            }
-        }
+        cl.sync();  // every rank's best delivered everywhere
+        unsigned long long bv = lane < CL ? g_bv[buf][lane] : ~0ull;
+        int bi = lane < CL ? g_bi[buf][lane] : 0x7fffffff;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
@@ -1707,7 +1724,7 @@ extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_de
     // 51 + 42 KiB for ncand <= 20 and nfb <= 2048
     const int np = d.cdef.ncand * d.cdef.ncand;
     const int CL = kFinCluster;
-    const int per_cta = 2 * (np <= kFinPushPairs ? CL : 1) * np * 8 + (nfb + CL - 1) / CL * (2 * d.cdef.ncand + 1) * 4;
+    const int per_cta = (int)fin_pair_bytes(np, CL) + (nfb + CL - 1) / CL * (2 * d.cdef.ncand + 1) * 4;
     // raise the kernel's dynamic shared memory opt-in when this launch needs
     // more, never lower it: the attribute is per function and device, and a
     // context set it to its own cap at creation

@@ -142,6 +142,12 @@ struct FrameDesc {
     uint32_t wait_limit;
 };
 
+// k_cdef_finish (joint strength search on a cluster): bytes of the double-buffered pair partials per CTA (each
+// rank owns ceil(npairs / cl) pairs and receives one partial per rank)
+__host__ __device__ constexpr size_t fin_pair_bytes(int npairs, int cl) {
+    return 2 * (size_t)cl * (size_t)((npairs + cl - 1) / cl) * 8;
+}
+
 // One entry of a launch work list: a tile of a frame/plane, owning CTAs
 // [cta_begin, cta_begin + ctas).
 struct WorkItem {

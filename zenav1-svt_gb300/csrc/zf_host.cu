@@ -1405,15 +1405,15 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 d_desc, (const int *)(base + o_cf) + n_joint);
         }
         if (!large_f.empty()) {
-            // dynamic shared memory: the double-buffered pair partials (an
-            // inbox per rank up to kFinPushPairs pairs) and the compacted rows
+            // dynamic shared memory: the double-buffered pair partials (each
+            // rank's inbox for the pairs it owns) and the compacted rows
             // of the largest frame, capped (frames whose rows do not fit use
             // global scratch). 16-CTA clusters where the device allows them.
             auto need = [&](int cl) {
                 size_t want = 0, pairs = 0;
                 for (int fi : large_f) {
                     const size_t nc = (size_t)plans[fi].d.cdef.ncand, np = nc * nc;
-                    const size_t pb = 2 * (np <= (size_t)zf::kFinPushPairsHost ? (size_t)cl : 1) * np * 8;
+                    const size_t pb = zf::fin_pair_bytes((int)np, cl);
                     pairs = std::max(pairs, pb);
                     want = std::max(want, pb + ((size_t)plans[fi].nfb + cl - 1) / cl * (2 * nc + 1) * 4);
                 }

@@ -27,7 +27,6 @@ __global__ void k_cdef_finish1(FrameDesc *frames, const int *frame_ids);
 // Dynamic shared memory of k_cdef_finish1 for a frame; 0 when over `cap`.
 int finish1_smem(int nfb, int ncand, int cap);
 constexpr int kFin1ThreadsHost = 1024;
-constexpr int kFinPushPairsHost = 512;  // k_cdef_finish: inbox per rank up to this many pairs
 constexpr int kFinClusterMaxHost = 16;  // k_cdef_finish: non-portable cluster size when allowed
 // k_cdef_finish over `nclusters` clusters of `cl` CTAs (cluster size set at launch).
 cudaError_t launch_cdef_finish(int nclusters, int cl, size_t smem, cudaStream_t st, FrameDesc *frames,
