@@ -234,18 +234,24 @@ __device__ void db_load(const DbTile &t, const uint8_t *plane, uint16_t *reg) {
     const int bd = t.f->bd;
     if (word_ok(plane)) {
         const int spw = bd == 8 ? 4 : 2, wpr = DB_R / spw;
-        // flat over (row, word); row and word advance by blockDim.x's quotient
-        // and remainder
-        const int step_r = blockDim.x / wpr, step_w = blockDim.x - step_r * wpr;
-        for (int ry = threadIdx.x / wpr, wx = threadIdx.x - ry * wpr; ry < DB_R; ry += step_r, wx += step_w) {
-            if (wx >= wpr) {
-                wx -= wpr;
-                if (++ry >= DB_R) break;
+        // flat over (row, word), four words per thread at a time: their
+        // loads are issued before any is unpacked, so the latencies overlap
+        const int total = DB_R * wpr;
+        for (int i0 = threadIdx.x; i0 < total; i0 += 4 * blockDim.x) {
+            uint32_t v[4];
+            int off[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int i = i0 + j * blockDim.x;
+                const int ry = i / wpr, wx = i - ry * wpr;
+                const int y = t.y0 - DB_H + ry, x = t.x0 - DB_H + wx * spw;
+                off[j] = i < total ? ry * DB_R + wx * spw : -1;
+                v[j] = 0;
+                if (i < total && x >= 0 && x < t.pw && y >= 0 && y < t.ph) v[j] = *word_at(plane, (int64_t)y * t.pw + x, bd);
             }
-            const int y = t.y0 - DB_H + ry, x = t.x0 - DB_H + wx * spw;
-            uint32_t v = 0;
-            if (x >= 0 && x < t.pw && y >= 0 && y < t.ph) v = *word_at(plane, (int64_t)y * t.pw + x, bd);
-            unpack_word(v, bd, reg + ry * DB_R + wx * spw);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (off[j] >= 0) unpack_word(v[j], bd, reg + off[j]);
         }
         return;
     }

@@ -203,7 +203,10 @@ __device__ __forceinline__ int floor_div(int a, int b) { return a >= 0 ? a / b :
 // clamp(x, 0, pw - 1) when clamp_x, else gives `fill`. put(r, x - xa, v)
 // stores a sample. Each thread takes whole words: a word wholly inside
 // [0, pw) of an aligned row is one 32-bit load, other words go per sample.
-template <typename RowFn, typename PutFn>
+// A thread's words are taken B at a time: the B loads are issued before
+// any of them is stored, so their latencies overlap (B = 1 for kernels
+// whose registers are already scarce).
+template <int B = 4, typename RowFn, typename PutFn>
 __device__ __forceinline__ void stage_window(int bd, int pw, int nrows, int xa, int n, bool clamp_x, int fill,
                                              RowFn rowp, PutFn put) {
     const int spw = word_samples(bd);
@@ -212,30 +215,52 @@ __device__ __forceinline__ void stage_window(int bd, int pw, int nrows, int xa, 
     // constant quotient and remainder of blockDim.x (one division per call)
     const int step_r = blockDim.x / nw, step_w = blockDim.x - step_r * nw;
     int r = threadIdx.x / nw, w = threadIdx.x - r * nw;
-    for (; r < nrows; r += step_r, w += step_w) {
-        if (w >= nw) {
-            w -= nw;
-            ++r;
-            if (r >= nrows) break;
-        }
-        const uint8_t *row = rowp(r);
-        const int x0 = (wa + w) * spw;
-        if (row && x0 >= 0 && x0 + spw <= pw && aligned4(row)) {
-            const uint32_t v = *reinterpret_cast<const uint32_t *>(row + (bd == 8 ? x0 : 2 * x0));
-            for (int k = 0; k < spw; ++k) {
-                const int x = x0 + k;
-                if (x >= xa && x < xa + n) put(r, x - xa, word_sample(v, k, bd));
-            }
-        } else {
-            for (int k = 0; k < spw; ++k) {
-                const int x = x0 + k;
-                if (x < xa || x >= xa + n) continue;
-                int v = fill;
-                if (row) {
-                    if (x >= 0 && x < pw) v = ldpx(row, x, bd);
-                    else if (clamp_x) v = ldpx(row, clampi(x, 0, pw - 1), bd);
+    while (r < nrows) {
+        int rr[B], x0s[B];
+        uint32_t v[B];
+        bool fast[B];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            rr[j] = r < nrows ? r : -1;
+            x0s[j] = (wa + w) * spw;
+            fast[j] = false;
+            v[j] = 0;
+            if (rr[j] >= 0) {
+                const uint8_t *row = rowp(r);
+                const int x0 = x0s[j];
+                if (row && x0 >= 0 && x0 + spw <= pw && aligned4(row)) {
+                    v[j] = *reinterpret_cast<const uint32_t *>(row + (bd == 8 ? x0 : 2 * x0));
+                    fast[j] = true;
                 }
-                put(r, x - xa, v);
+                r += step_r;
+                w += step_w;
+                if (w >= nw) {
+                    w -= nw;
+                    ++r;
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            if (rr[j] < 0) continue;
+            const int x0 = x0s[j];
+            if (fast[j]) {
+                for (int k = 0; k < spw; ++k) {
+                    const int x = x0 + k;
+                    if (x >= xa && x < xa + n) put(rr[j], x - xa, word_sample(v[j], k, bd));
+                }
+            } else {
+                const uint8_t *row = rowp(rr[j]);
+                for (int k = 0; k < spw; ++k) {
+                    const int x = x0 + k;
+                    if (x < xa || x >= xa + n) continue;
+                    int vv = fill;
+                    if (row) {
+                        if (x >= 0 && x < pw) vv = ldpx(row, x, bd);
+                        else if (clamp_x) vv = ldpx(row, clampi(x, 0, pw - 1), bd);
+                    }
+                    put(rr[j], x - xa, vv);
+                }
             }
         }
     }

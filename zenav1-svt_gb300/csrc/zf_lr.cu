@@ -155,14 +155,14 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
             tma_load_2d(Xb, pl.tm_s, r.h_start >> 2, r.v_start + xi0, &mbar);
         }
     } else {
-        stage_window(
+        stage_window<1>(
             bd, pl.pw, drows, r.h_start + dx0, dcols, true, 0,
             [&](int rr) { return row_ptr(dg, clampi(r.v_start + dy0 + rr, 0, pl.ph - 1), stride, bd); },
             [&](int rr, int cc, int v) {
                 if (packed) Db[rr * G::DSB + cc] = (uint8_t)v;
                 else D[rr * G::DCOLS + cc] = (int16_t)v;
             });
-        stage_window(
+        stage_window<1>(
             bd, pl.pw, xi1 - xi0, r.h_start, uw, true, 0,
             [&](int rr) { return row_ptr(sr_, r.v_start + xi0 + rr, stride, bd); },
             [&](int rr, int cc, int v) {
@@ -990,7 +990,7 @@ __device__ int64_t trial_sse(const FrameDesc &f, int plane, const LrPlane &pl, c
             const int ty = (tile / ntx) * TT_H, tx = (tile - (tile / ntx) * ntx) * TT_W;
             const int y0 = r.v_start + ty, x0 = r.h_start + tx;
             __syncthreads();
-            stage_window(
+            stage_window<1>(
                 bd, pl.pw, SH, x0 - 3, SW, true, 0,
                 [&](int rr) { return row_ptr(dg, clampi(y0 - 3 + rr, 0, pl.ph - 1), stride, bd); },
                 [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
