@@ -155,7 +155,7 @@ __device__ void find_dirs(const uint16_t *reg, int rs, int cs, const int *blist,
 __device__ __noinline__ void load_region(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n,
                                          uint16_t *reg) {
     const int rs = n + 4;
-    stage_window(
+    stage_window<1>(
         bd, pw, rs, x0 - 2, rs, false, kVeryLarge,
         [&](int ry) {
             const int y = y0 - 2 + ry;
@@ -167,7 +167,7 @@ __device__ __noinline__ void load_region(const uint8_t *plane, int bd, int pw, i
 // Stage the n x n source tile at (x0, y0), 0 outside the canvas.
 __device__ __noinline__ void load_src(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n,
                                       uint16_t *src) {
-    stage_window(
+    stage_window<1>(
         bd, pw, n, x0, n, false, 0,
         [&](int ry) { return y0 + ry < ph ? row_ptr(plane, y0 + ry, pw, bd) : (const uint8_t *)nullptr; },
         [&](int ry, int rx, int v) { src[ry * n + rx] = (uint16_t)v; });
