@@ -482,6 +482,8 @@ def run_ours(args):
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_sample()
         if world == 1:
+            restore()  # the tuner copies the pre-deblock recon it is given
+            line["autotune_4k"] = run_autotune_4k(ctx, frames, structs)
             line["plain_512"] = run_plain512(args, ctx, stream, dev)
             line["highres_10bit"] = run_highres10(args, ctx, stream, dev)
             line["sgr"] = run_sgr(args, ctx, stream, dev, frames[0])
@@ -496,6 +498,27 @@ def run_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def run_autotune_4k(ctx, frames, structs):
+    """The autotuner on each 4K frame of the plain workload alone
+    (zf_filter_stage per setting, the frame's recon restored before every
+    call): the setting it keeps against the default, per frame."""
+    pkg = ge._pkg()
+    from zenav1_svt_gb300 import abi
+    default = (0, 1, 8, 0, 64, 8)
+    keys = ("graphs", "stats_tma", "apply_group", "stats_tc", "trial_tile", "db_levels")
+    out = []
+    for f, s in zip(frames, structs):
+        one = (abi.ZfFrame * 1)()
+        one[0] = s
+        best, cands = ctx.autotune_raw(one, 1, reps=3)
+        dflt = [c for c in cands if tuple(c[k] for k in keys) == default]
+        out.append({"frame": "preset %d qp %d" % (f.preset, {96: 24, 160: 40}.get(f.qindex, f.qindex)),
+                    "best": {k: best[k] for k in keys}, "best_ms": best["ms"],
+                    "default_ms": dflt[0]["ms"] if dflt else None, "settings_timed": len(cands)})
+        ctx.set_tune(*default)
+    return out
 
 
 def run_plain512(args, ctx, stream, dev):
@@ -824,8 +847,10 @@ def run_batched(args, ctx, stream, dev, frames):
     # setting on private copies of the recon); the context goes back to the
     # default setting afterwards
     best, cands = ctx.autotune_raw(arr, n, reps=2)
-    dflt = [c for c in cands if (c["graphs"], c["stats_tma"], c["apply_group"], c["stats_tc"]) == (0, 1, 8, 0)]
-    ctx.set_tune(0, 1, 8)
+    default = (0, 1, 8, 0, 64, 8)  # graphs, stats_tma, apply_group, stats_tc, trial_tile, db_levels
+    keys = ("graphs", "stats_tma", "apply_group", "stats_tc", "trial_tile", "db_levels")
+    dflt = [c for c in cands if tuple(c[k] for k in keys) == default]
+    ctx.set_tune(*default)
     tune = {"best": best, "default_ms": dflt[0]["ms"] if dflt else None, "candidates": len(cands)}
     peak = _peaks().get("hbm_gbs", 6800.0)
     return {"workload": "256 images, W,H ~ U[64,2048] (~20% odd), 70% 8-bit / 30% 10-bit, qp ~ U[20,50], preset 6",

@@ -462,22 +462,28 @@ typedef struct zf_tune {
     int32_t apply_group;        /* 64-px column tiles per restoration-apply CTA: 1..16 */
     int32_t stats_tc;           /* 0/1: Wiener statistics of 8-bit planes on the tensor cores
                                    (default 0: the CUDA-core form measured faster) */
+    int32_t trial_tile;         /* Wiener trial tile edge without refinement: 32 or 64 (default) */
+    int32_t db_levels;          /* deblock level trials per launch of the level search after a
+                                   climb's first two launches: 2..8 (default 8) */
     double ms;                  /* zf_autotune: mean device time of one call (else 0) */
 } zf_tune;
 int32_t zf_get_tune(const zf_ctx *ctx, zf_tune *out);
 /* ZF_ERR_ARG for a setting out of range. */
 int32_t zf_set_tune(zf_ctx *ctx, const zf_tune *t);
-/* Autotuner (no counterpart in the reference). Times every candidate
- * setting (graphs x stats_tma x apply_group in {1, 2, 4, 8, 16}) on the
- * caller's frames: one call per candidate to warm up, then `reps` timed
- * calls (CUDA events on the context's stream), each of the whole filter
+/* Autotuner (no counterpart in the reference). Coordinate descent from the
+ * context's current setting: each knob in turn -- graphs, the statistics
+ * form (CUDA cores with TMA rows / with thread-staged rows / tensor cores),
+ * apply_group in {1, 2, 4, 8, 16}, trial_tile in {64, 32}, db_levels in
+ * {8, 4, 2} -- takes every value with the other knobs at the best setting
+ * so far; a setting is timed once (one warm-up call, then `reps` calls timed
+ * with CUDA events on the context's stream), each call the whole filter
  * stage on private copies of the frames' recon restored before every call
  * (zf_filter_stage for n == 1, zf_submit_batch otherwise), so the caller's
- * buffers are not written. Sets the fastest candidate on the context and
- * writes it to *best; writes up to `max` candidates with their times to
- * `cands` (may be NULL). Returns the number of candidates (>= 1) or a
+ * buffers are not written. Sets the fastest setting on the context and
+ * writes it to *best; writes up to `max` timed settings with their times to
+ * `cands` (may be NULL). Returns the number of settings timed (>= 1) or a
  * negative ZF_ERR_*. Allocates device memory for the copies (device
- * frames) and runs O(candidates x reps) stage calls: a set-up step, not a
+ * frames) and runs O(settings x reps) stage calls: a set-up step, not a
  * per-frame one. */
 int32_t zf_autotune(zf_ctx *ctx, const zf_frame *frames, int32_t n, int32_t reps, zf_tune *best,
                     zf_tune *cands, int32_t max);

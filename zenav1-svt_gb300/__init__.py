@@ -209,10 +209,14 @@ class Context:
         self._check(lib().zf_get_tune(self.h, C.byref(t)))
         return t.as_dict()
 
-    def set_tune(self, graphs, stats_tma, apply_group, stats_tc=0):
+    def set_tune(self, graphs, stats_tma, apply_group, stats_tc=0, trial_tile=64, db_levels=8):
         """Set the launch settings (zf_set_tune)."""
-        t = abi.ZfTune(graphs, stats_tma, apply_group, stats_tc, 0.0)
+        t = abi.ZfTune(graphs, stats_tma, apply_group, stats_tc, trial_tile, db_levels, 0.0)
         self._check(lib().zf_set_tune(self.h, C.byref(t)))
+
+    def set_tune_dict(self, t):
+        """zf_set_tune from a get_tune()-style dict."""
+        self.set_tune(t["graphs"], t["stats_tma"], t["apply_group"], t["stats_tc"], t["trial_tile"], t["db_levels"])
 
     def autotune_raw(self, frames_arr, n, reps=3):
         """zf_autotune over n ZfFrame structs: (best dict, [candidate dicts]).

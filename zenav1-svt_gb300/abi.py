@@ -68,11 +68,13 @@ class ZfWienerRefs(C.Structure):
 
 class ZfTune(C.Structure):
     _fields_ = [("graphs", C.c_int32), ("stats_tma", C.c_int32), ("apply_group", C.c_int32),
-                ("stats_tc", C.c_int32), ("ms", C.c_double)]
+                ("stats_tc", C.c_int32), ("trial_tile", C.c_int32), ("db_levels", C.c_int32),
+                ("ms", C.c_double)]
 
     def as_dict(self):
         return {"graphs": self.graphs, "stats_tma": self.stats_tma, "apply_group": self.apply_group,
-                "stats_tc": self.stats_tc, "ms": round(self.ms, 4)}
+                "stats_tc": self.stats_tc, "trial_tile": self.trial_tile, "db_levels": self.db_levels,
+                "ms": round(self.ms, 4)}
 
 
 class ZfOpts(C.Structure):

@@ -59,6 +59,8 @@ struct zf_ctx {
     bool capturing = false;
     bool tma = true;  // statistics kernel rows by TMA where the planes allow
     bool stats_tc = false;  // statistics of 8-bit 5-tap planes on the tensor cores (k_lr_stats_tc)
+    int trial_tile = 64;    // k_lr_trial_tiles tile edge (32 or 64)
+    int db_levels = 8;      // deblock level trials per launch after a climb's first two launches
     uint32_t wait_limit = 1u << 20;  // statistics kernel's TMA wait (iterations)
     int apply_group = 8;  // 64-px column tiles per restoration-apply CTA
     // search trace (zf_trace / ZF_TRACE): one text line per trial, filter
@@ -997,7 +999,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                     // one cluster per unit: the hill-climb is sequential, its trials are not
                     wl_trial.add(i, pl, (int)u, 0, zf::kTrialClusterHost);
                 } else {
-                    const int tl = zf::kTrialTileHost, uw = r.h_end - r.h_start;
+                    const int tl = ctx->trial_tile, uw = r.h_end - r.h_start;
                     wl_tiles.add(i, pl, (int)u, 0, ((uw + tl - 1) / tl) * ((uh + tl - 1) / tl));
                 }
             }
@@ -1280,9 +1282,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 const int m = s.hc.needs(need);
                 if (m == 0) continue;
                 // four levels in each of a climb's first two launches (most
-                // climbs end within them), kDbLevels in later ones
+                // climbs end within them), ctx->db_levels in later ones
                 TrialSlot t{s.frame, s.plane, {}, {}};
-                speculate(s.hc, need, m, s.launches < 2 ? 4 : zf::kDbLevels, t.levels);
+                speculate(s.hc, need, m, s.launches < 2 ? std::min(4, ctx->db_levels) : ctx->db_levels, t.levels);
                 s.launches++;
                 ts.push_back(t);
                 owner.push_back((int)k);
@@ -1475,8 +1477,8 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             }
             if (wl_tiles.ctas) {
                 { LaunchScope ls_(ctx, "k_lr_trial_tiles");
-                zf::k_lr_trial_tiles<<<wl_tiles.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_tiles),
-                                                                   (int)wl_tiles.items.size()); }
+                CU(zf::launch_lr_trial_tiles(ctx->trial_tile, wl_tiles.ctas, st, d_desc,
+                                             (const WorkItem *)(base + o_tiles), (int)wl_tiles.items.size())); }
                 TRY(launch_check(ctx, "k_lr_trial_tiles"));
             }
         }
@@ -1834,18 +1836,23 @@ int32_t zf_get_tune(const zf_ctx *ctx, zf_tune *out) {
     out->stats_tma = ctx->tma ? 1 : 0;
     out->apply_group = ctx->apply_group;
     out->stats_tc = ctx->stats_tc ? 1 : 0;
+    out->trial_tile = ctx->trial_tile;
+    out->db_levels = ctx->db_levels;
     return ZF_OK;
 }
 
 int32_t zf_set_tune(zf_ctx *ctx, const zf_tune *t) {
     if (!ctx || !t) return ZF_ERR_ARG;
     if (t->graphs < 0 || t->graphs > 1 || t->stats_tma < 0 || t->stats_tma > 1 || t->apply_group < 1 ||
-        t->apply_group > zf::kApplyGroupMax || t->stats_tc < 0 || t->stats_tc > 1)
+        t->apply_group > zf::kApplyGroupMax || t->stats_tc < 0 || t->stats_tc > 1 ||
+        (t->trial_tile != 32 && t->trial_tile != 64) || t->db_levels < 2 || t->db_levels > zf::kDbLevels)
         return fail(ctx, ZF_ERR_ARG, "tune setting out of range");
     ctx->graphs = t->graphs != 0;
     ctx->tma = t->stats_tma != 0;
     ctx->apply_group = t->apply_group;
     ctx->stats_tc = t->stats_tc != 0;
+    ctx->trial_tile = t->trial_tile;
+    ctx->db_levels = t->db_levels;
     return ZF_OK;
 }
 
@@ -1923,49 +1930,67 @@ int32_t zf_autotune(zf_ctx *ctx, const zf_frame *frames, int32_t n, int32_t reps
         cleanup();
         return fail(ctx, ZF_ERR_CUDA, "autotune: event creation failed");
     }
-    // candidates: graphs x statistics form (tensor cores; CUDA cores with
-    // TMA rows; CUDA cores with thread-staged rows) x apply column tiles
+    // Coordinate descent from the context's current setting: each knob in
+    // turn takes every value with the others at the best so far -- graphs,
+    // the statistics form (CUDA cores with TMA rows, CUDA cores with thread
+    // staging, tensor cores), the restoration-apply column tiles per CTA, the
+    // Wiener trial tile edge, the deblock trial levels per launch. A setting
+    // timed once is not timed again.
     static const int kGroups[5] = {1, 2, 4, 8, 16};
-    std::vector<zf_tune> grid;
-    for (int g = 0; g < 2; ++g)
-        for (int form = 0; form < 3; ++form)
-            for (int k = 0; k < 5; ++k) {
-                zf_tune c{};
-                c.graphs = g;
-                c.stats_tc = form == 0 ? 1 : 0;
-                c.stats_tma = form == 2 ? 0 : 1;
-                c.apply_group = kGroups[k];
-                grid.push_back(c);
-            }
     int count = 0, rc = ZF_OK;
-    zf_tune win{};
+    zf_tune win = saved;
     win.ms = -1.0;
-    for (size_t ci = 0; ci < grid.size() && rc == ZF_OK; ++ci) {
-                zf_tune c = grid[ci];
-                zf_set_tune(ctx, &c);
-                double total = 0.0;
-                for (int r = -1; r < reps && rc == ZF_OK; ++r) {  // r = -1: warm-up
-                    if (!restore()) {
-                        rc = fail(ctx, ZF_ERR_CUDA, "autotune: restoring the recon failed");
-                        break;
-                    }
-                    cudaEventRecord(e0, ctx->stream);
-                    rc = call();
-                    if (rc != ZF_OK) break;
-                    cudaEventRecord(e1, ctx->stream);
-                    float ms = 0.f;
-                    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
-                        rc = fail(ctx, ZF_ERR_CUDA, "autotune: event timing failed");
-                        break;
-                    }
-                    if (r >= 0) total += ms;
-                }
-                if (rc != ZF_OK) break;
-                c.ms = total / reps;
-                if (cands && count < max) cands[count] = c;
-                ++count;
-                if (win.ms < 0 || c.ms < win.ms) win = c;  // strict: the earlier candidate wins ties
+    std::vector<zf_tune> timed;
+    auto same = [](const zf_tune &a, const zf_tune &b) {
+        return a.graphs == b.graphs && a.stats_tma == b.stats_tma && a.apply_group == b.apply_group &&
+               a.stats_tc == b.stats_tc && a.trial_tile == b.trial_tile && a.db_levels == b.db_levels;
+    };
+    auto evaluate = [&](zf_tune c) -> int {
+        for (const zf_tune &d : timed)
+            if (same(d, c)) {
+                if (win.ms < 0 || d.ms < win.ms) win = d;
+                return ZF_OK;
             }
+        zf_set_tune(ctx, &c);
+        double total = 0.0;
+        for (int r = -1; r < reps; ++r) {  // r = -1: warm-up
+            if (!restore()) return fail(ctx, ZF_ERR_CUDA, "autotune: restoring the recon failed");
+            cudaEventRecord(e0, ctx->stream);
+            const int e = call();
+            if (e != ZF_OK) return e;
+            cudaEventRecord(e1, ctx->stream);
+            float ms = 0.f;
+            if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+                return fail(ctx, ZF_ERR_CUDA, "autotune: event timing failed");
+            if (r >= 0) total += ms;
+        }
+        c.ms = total / reps;
+        timed.push_back(c);
+        if (cands && count < max) cands[count] = c;
+        ++count;
+        if (win.ms < 0 || c.ms < win.ms) win = c;  // strict: the earlier candidate wins ties
+        return ZF_OK;
+    };
+    for (int knob = 0; knob < 5 && rc == ZF_OK; ++knob) {
+        const zf_tune base = win;
+        const int nv = knob == 0 ? 2 : knob == 1 ? 3 : knob == 2 ? 5 : knob == 3 ? 2 : 3;
+        for (int v = 0; v < nv && rc == ZF_OK; ++v) {
+            zf_tune c = base;
+            if (knob == 0) {
+                c.graphs = v;
+            } else if (knob == 1) {
+                c.stats_tc = v == 2 ? 1 : 0;
+                c.stats_tma = v == 1 ? 0 : 1;
+            } else if (knob == 2) {
+                c.apply_group = kGroups[v];
+            } else if (knob == 3) {
+                c.trial_tile = v == 0 ? 64 : 32;
+            } else {
+                c.db_levels = v == 0 ? 8 : v == 1 ? 4 : 2;
+            }
+            rc = evaluate(c);
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaStreamSynchronize(ctx->stream);

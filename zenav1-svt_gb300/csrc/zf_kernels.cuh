@@ -47,8 +47,9 @@ cudaError_t launch_lr_stats(int win, int bd, int ctas, cudaStream_t st, FrameDes
                             int nitems);
 __global__ void k_lr_solve(FrameDesc *frames, const WorkItem *items, int nitems);
 __global__ void k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems);
-__global__ void k_lr_trial_tiles(FrameDesc *frames, const WorkItem *items, int nitems);
-constexpr int kTrialTileHost = 64;  // k_lr_trial_tiles tile edge
+// k_lr_trial_tiles<tl> (tile edge 32 or 64) over `ctas` tiles.
+cudaError_t launch_lr_trial_tiles(int tl, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
+                                  int nitems);
 constexpr int kTrialClusterHost = 8;  // k_lr_trial: CTAs per unit (cluster size)
 constexpr int kLrFinThreadsHost = 1024;  // k_lr_finish CTA size
 constexpr int kLrPairMaxHost = 20100;   // k_lr_finish pair-table entries (units <= 200)

@@ -1153,10 +1153,12 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256)
 // rows >= b, the lower stripe's rows b..b+2 take B[b-1] and B[b-2] in place
 // of rows < b. Those four B rows per edge are staged and filtered with the
 // tile's rows, so C ends final for a Wiener unit.
-constexpr int TL = 64;
-constexpr int kTileEdges = 3;  // stripe edges whose rows can meet a 64-row tile (stripes >= 32 rows)
+constexpr int kTileEdges = 3;  // stripe edges whose rows can meet a tile of <= 64 rows (stripes >= 32 rows)
 
+// TL: tile edge (32 or 64), a launch setting (zf_tune.trial_tile).
+template <int TL>
 __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const WorkItem *items, int nitems) {
+    constexpr int QPR = TL / 4, LQ = TL == 64 ? 4 : 3;  // four-sample runs per row, log2
     // staged rows of TL + 7 samples at a pitch of TL + 8 (8-byte aligned
     // rows: the horizontal pass reads each run with three 8-byte loads)
     constexpr int SW = TL + 8, SR = TL + 7 + 4 * kTileEdges;
@@ -1232,7 +1234,7 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         auto hpass = [&](auto t5c) {
             constexpr bool T5 = decltype(t5c)::value;
             for (int q = threadIdx.x; q < rows * (TL / 4); q += blockDim.x) {
-                const int rr = q >> 4, c0 = (q & 15) * 4;
+                const int rr = q >> LQ, c0 = (q & (QPR - 1)) * 4;
                 if (c0 >= tw) continue;
                 const uint2 *sp = reinterpret_cast<const uint2 *>(stage + rr * SW + c0);
                 int p[12];
@@ -1294,7 +1296,7 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
     auto vpass = [&](auto t5c) {
         constexpr bool T5 = decltype(t5c)::value;
         for (int q = threadIdx.x; q < th * (TL / 4); q += blockDim.x) {
-            const int rr = q >> 4, c0 = (q & 15) * 4;
+            const int rr = q >> LQ, c0 = (q & (QPR - 1)) * 4;
             if (c0 >= tw) continue;
             uint2 v[7];
 #pragma unroll
@@ -1355,7 +1357,7 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
     // the apply's rows at the stripe edges: tmp rows of A (index y - y0 + 3)
     // or of the edge's B rows (index na + 4 e + k)
     for (int q = threadIdx.x; q < ne * 6 * TL; q += blockDim.x) {
-        const int e = q / (6 * TL), k6 = (q >> 6) % 6, cc = q & (TL - 1);
+        const int e = q / (6 * TL), k6 = (q / TL) % 6, cc = q & (TL - 1);
         const int b = e == 0 ? eb[0] : e == 1 ? eb[1] : eb[2];
         const int y = b - 3 + k6;
         if (cc >= tw || y < y0 || y >= y0 + th) continue;
@@ -1857,6 +1859,14 @@ namespace zf {
 // Host-side launcher: the templated kernel is instantiated and launched in
 // this translation unit (whole-program compilation cannot launch a template
 // instantiation owned by another unit).
+cudaError_t launch_lr_trial_tiles(int tl, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
+                                  int nitems) {
+    if (tl == 32) k_lr_trial_tiles<32><<<ctas, 256, 0, st>>>(frames, items, nitems);
+    else if (tl == 64) k_lr_trial_tiles<64><<<ctas, 256, 0, st>>>(frames, items, nitems);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_lr_stats(int win, int bd, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
                             int nitems) {
     if (win == 5 && bd == 8) k_lr_stats<5, 8><<<ctas, 256, 0, st>>>(frames, items, nitems);
