@@ -266,12 +266,20 @@ KERNEL_DRAM_BYTES_PER_PX = {
 
 # Warp instructions executed per luma pixel of the plain 4K step, per
 # kernel (ncu smsp__inst_executed.sum summed over the kernel's launches in
-# one pass of the bench's four frames, divided by their luma pixels). The
+# one pass of the bench's four frames, divided by their luma pixels; the
+# committed summary of the instruction-mix capture gives the command). The
 # issue roofline of these integer-instruction-bound kernels: achieved warp
 # instructions per second (these counts over the bench's own CUDA-event
 # times of the same step) against the issue peak, four warp instructions
 # per clock per SM at the SM clock sampled during the timed region.
-KERNEL_WARP_INST_PER_PX = {}
+KERNEL_WARP_INST_PER_PX = {
+    "k_deblock_sse": 18.1571,
+    "k_deblock_apply": 5.3884,
+    "k_cdef_search": 11.9243,
+    "k_cdef_apply": 5.8323,
+    "k_lr_stats5": 5.8570,
+    "k_lr_trial_tiles": 8.2514,
+}
 
 
 def issue_roofline(prof, frames, sm_count, sm_mhz):
