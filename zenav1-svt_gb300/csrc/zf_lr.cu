@@ -973,7 +973,7 @@ __device__ __forceinline__ int wiener_v(const int *tp, const int16_t *vf, int bd
 constexpr int kTrialCluster = 8;
 
 __device__ int64_t trial_sse(const FrameDesc &f, int plane, const LrPlane &pl, const UnitRect &r, const Taps &t,
-                             uint16_t *stage, uint16_t *tmp, unsigned long long *red,
+                             uint16_t *stage, uint16_t *tmp, uint16_t *srct, unsigned long long *red,
                              unsigned long long (*inbox)[kTrialCluster][3], int &buf) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
@@ -982,38 +982,91 @@ __device__ int64_t trial_sse(const FrameDesc &f, int plane, const LrPlane &pl, c
     const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
     const int dw = uw % 16, dh = uh % 16;
     const uint8_t *dg = f.A[plane], *sr = f.S[plane];
-    unsigned long long blk = 0, rgt = 0, bot = 0;
-    constexpr int SW = TT_W + 7, SH = TT_H + 7;
+    // The taps are symmetric (f[6 - k] = f[k], f[7] = 0: the solve and every
+    // refinement step keep them so), so each pass is four multiplies per
+    // output on pair sums, the centre tap carrying the 128 of
+    // wiener_convolve_add_src; a thread takes four outputs per pass. With
+    // both outer taps 0 (every 5-tap window: the refinement starts at tap 1)
+    // the outer pair is dropped.
+    int hf[4], vf[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        hf[k] = t.h[k];
+        vf[k] = t.v[k];
+    }
+    const bool t5 = hf[0] == 0 && vf[0] == 0;  // uniform over the cluster
+    const int hc3 = 128 + hf[3], hoff = 1 << (bd + 6), hlim = (1 << (bd + 5)) - 1;
+    const int vc3 = 128 + vf[3], voff = -(1 << (bd + 10)), vmax = (1 << bd) - 1;
+    uint32_t blk = 0, rgt = 0, bot = 0;  // a thread's parts of one trial: <= 9 tiles x 8 pixels of e^2 <= 1023^2
+    constexpr int SW = TT_W + 8, SH = TT_H + 7;  // staged rows 8-byte aligned
     const int ntx = (uw + TT_W - 1) / TT_W, ntiles = ntx * ((uh + TT_H - 1) / TT_H);
     for (int tile = rank; tile < ntiles; tile += CL) {
-        {
-            const int ty = (tile / ntx) * TT_H, tx = (tile - (tile / ntx) * ntx) * TT_W;
-            const int y0 = r.v_start + ty, x0 = r.h_start + tx;
-            __syncthreads();
-            stage_window<1>(
-                bd, pl.pw, SH, x0 - 3, SW, true, 0,
-                [&](int rr) { return row_ptr(dg, clampi(y0 - 3 + rr, 0, pl.ph - 1), stride, bd); },
-                [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
-            __syncthreads();
-            for (int q = threadIdx.x; q < SH * TT_W; q += blockDim.x) {
-                const int rr = q / TT_W, cc = q - rr * TT_W;
-                int px[8];
+        const int ty = (tile / ntx) * TT_H, tx = (tile - (tile / ntx) * ntx) * TT_W;
+        const int y0 = r.v_start + ty, x0 = r.h_start + tx;
+        const int th = min(TT_H, uh - ty), tw = min(TT_W, uw - tx);
+        __syncthreads();
+        stage_window<1>(
+            bd, pl.pw, SH, x0 - 3, TT_W + 7, true, 0,
+            [&](int rr) { return row_ptr(dg, clampi(y0 - 3 + rr, 0, pl.ph - 1), stride, bd); },
+            [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
+        stage_window<1>(
+            bd, pl.pw, th, x0, tw, true, 0, [&](int rr) { return row_ptr(sr, y0 + rr, stride, bd); },
+            [&](int rr, int cc, int v) { srct[rr * TT_W + cc] = (uint16_t)v; });
+        __syncthreads();
+        // horizontal: every staged row x 16 runs of four columns
+        for (int q = threadIdx.x; q < SH * (TT_W / 4); q += blockDim.x) {
+            const int rr = q >> 4, c0 = (q & 15) * 4;
+            if (c0 >= tw) continue;
+            const uint2 *sp = reinterpret_cast<const uint2 *>(stage + rr * SW + c0);
+            int p[12];
 #pragma unroll
-                for (int k = 0; k < 8; ++k) px[k] = stage[rr * SW + cc + k];
-                tmp[q] = (uint16_t)wiener_h(px, t.h, bd);
+            for (int k = 0; k < 3; ++k) {
+                const uint2 w = sp[k];
+                p[4 * k] = (int)(w.x & 0xffffu);
+                p[4 * k + 1] = (int)(w.x >> 16);
+                p[4 * k + 2] = (int)(w.y & 0xffffu);
+                p[4 * k + 3] = (int)(w.y >> 16);
             }
-            __syncthreads();
-            for (int q = threadIdx.x; q < TT_H * TT_W; q += blockDim.x) {
-                const int rr = q / TT_W, cc = q - rr * TT_W;
-                const int i = ty + rr, j = tx + cc;
-                if (i >= uh || j >= uw) continue;
-                int tp[8];
+            uint32_t o[4];
 #pragma unroll
-                for (int k = 0; k < 8; ++k) tp[k] = tmp[(rr + k) * TT_W + cc];
-                const int y = wiener_v(tp, t.v, bd);
-                const int e = ldpx(sr, (int64_t)(y0 + rr) * stride + x0 + cc, bd) - y;
-                const unsigned long long e2 = (unsigned long long)((long long)e * e);
-                if (j >= uw - dw) rgt += e2;
+            for (int j = 0; j < 4; ++j) {
+                int sum = p[j + 3] * hc3 + hf[1] * (p[j + 1] + p[j + 5]) + hf[2] * (p[j + 2] + p[j + 4]) + hoff;
+                if (!t5) sum += hf[0] * (p[j] + p[j + 6]);
+                o[j] = (uint32_t)clampi((sum + 4) >> 3, 0, hlim);
+            }
+            *reinterpret_cast<uint2 *>(tmp + rr * TT_W + c0) = make_uint2(o[0] | o[1] << 16, o[2] | o[3] << 16);
+        }
+        __syncthreads();
+        // vertical: four columns of one row per thread, packed pair sums
+        // (tmp values are < 2^15), the SSE parts against the staged source
+        for (int q = threadIdx.x; q < th * (TT_W / 4); q += blockDim.x) {
+            const int rr = q >> 4, c0 = (q & 15) * 4;
+            if (c0 >= tw) continue;
+            uint2 v[7];
+#pragma unroll
+            for (int k = 0; k < 7; ++k)
+                v[k] = (t5 && (k == 0 || k == 6)) ? make_uint2(0, 0)
+                                                  : *reinterpret_cast<const uint2 *>(tmp + (rr + k) * TT_W + c0);
+            const uint32_t p1x = v[1].x + v[5].x, p1y = v[1].y + v[5].y;
+            const uint32_t p2x = v[2].x + v[4].x, p2y = v[2].y + v[4].y;
+            const uint32_t p0x = v[0].x + v[6].x, p0y = v[0].y + v[6].y;
+            auto lo = [](uint32_t w) { return (int)(w & 0xffffu); };
+            auto hi = [](uint32_t w) { return (int)(w >> 16); };
+            auto out = [&](int c, int a1, int a2, int a0) {
+                const int sum = c * vc3 + vf[1] * a1 + vf[2] * a2 + vf[0] * a0 + voff;
+                return clampi((sum + (1 << 10)) >> 11, 0, vmax);
+            };
+            const int y[4] = {out(lo(v[3].x), lo(p1x), lo(p2x), lo(p0x)), out(hi(v[3].x), hi(p1x), hi(p2x), hi(p0x)),
+                              out(lo(v[3].y), lo(p1y), lo(p2y), lo(p0y)), out(hi(v[3].y), hi(p1y), hi(p2y), hi(p0y))};
+            const uint2 sv = *reinterpret_cast<const uint2 *>(srct + rr * TT_W + c0);
+            const int sx[4] = {lo(sv.x), hi(sv.x), lo(sv.y), hi(sv.y)};
+            const int i = ty + rr, nq = min(4, tw - c0);
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) {
+                if (jj >= nq) break;
+                const int e = sx[jj] - y[jj];
+                const uint32_t e2 = (uint32_t)(e * e);
+                if (tx + c0 + jj >= uw - dw) rgt += e2;
                 else if (i >= uh - dh) bot += e2;
                 else blk += e2;
             }
@@ -1048,8 +1101,9 @@ __device__ int64_t trial_sse(const FrameDesc &f, int plane, const LrPlane &pl, c
 
 __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256)
     k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems) {
-    __shared__ uint16_t stage[(TT_H + 7) * (TT_W + 7)];
-    __shared__ uint16_t tmp[(TT_H + 7) * TT_W];
+    __shared__ __align__(16) uint16_t stage[(TT_H + 7) * (TT_W + 8)];
+    __shared__ __align__(16) uint16_t tmp[(TT_H + 7) * TT_W];
+    __shared__ __align__(16) uint16_t srct[TT_H * TT_W];
     __shared__ unsigned long long red[24];
     __shared__ unsigned long long inbox[2][kTrialCluster][3];
     __shared__ Taps t;
@@ -1069,7 +1123,7 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256)
         t.h[threadIdx.x] = u.hf[threadIdx.x];
     }
     __syncthreads();
-    int64_t err = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red, inbox, buf);
+    int64_t err = trial_sse(f, wi.plane, pl, r, t, stage, tmp, srct, red, inbox, buf);
     if (pl.refine) {
         // use_refinement with max_one_refinement_step: one step size (4).
         const int plane_off = (7 - pl.win) >> 1;
@@ -1088,7 +1142,7 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256)
                         fp[3] += 2 * s;
                     }
                     __syncthreads();
-                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red, inbox, buf);
+                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, srct, red, inbox, buf);
                     if (e2 > err) {
                         __syncthreads();
                         if (threadIdx.x == 0) {
@@ -1112,7 +1166,7 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256)
                         fp[3] -= 2 * s;
                     }
                     __syncthreads();
-                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, red, inbox, buf);
+                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, srct, red, inbox, buf);
                     if (e2 > err) {
                         __syncthreads();
                         if (threadIdx.x == 0) {
