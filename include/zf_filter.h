@@ -359,6 +359,63 @@ int32_t zf_lr_sb_syntax(const zf_decisions *d, int32_t mi_row, int32_t mi_col, i
                         int32_t frame_h, int32_t monochrome, int32_t sr_denom, zf_wiener_refs *refs,
                         zf_lr_sym *out, int32_t cap);
 
+/* ---- Tile symbol coder: the filter syntax as bytes ------------------------
+ * AV1's multi-symbol arithmetic coder (the encoder side of the AV1 spec's
+ * symbol decoding process, 8.2.2-8.2.6), in place of the reference's
+ * AomWriter over OdEcEnc (svtav1-entropy/src/writer.rs:18-80,
+ * range_coder.rs:24-300): the same interval arithmetic, CDF adaptation
+ * (cdf.rs:64-82) and final flush, so the same symbols give the same bytes.
+ * The caller's entropy walk codes its own symbols through it and, at the
+ * filter stage's places, the restoration units of each superblock
+ * (zf_ec_lr_sb, at the superblock's start, write_lr_for_sb) and the
+ * cdef_idx literal of each 64x64 filter block (zf_ec_cdef_block, after the
+ * skip flag of every coded block). Host code; no device work. */
+typedef struct zf_ec zf_ec;
+zf_ec *zf_ec_create(void);                 /* NULL when out of host memory */
+void zf_ec_destroy(zf_ec *ec);
+void zf_ec_reset(zf_ec *ec);               /* an empty stream (OdEcEnc::reset) */
+/* encode_bool_q15: bit with probability f / 32768 of a one (0 < f < 32768) */
+int32_t zf_ec_bool(zf_ec *ec, int32_t bit, uint32_t f);
+/* write_literal: nbits (0..32) equiprobable bits, most significant first */
+int32_t zf_ec_literal(zf_ec *ec, uint32_t value, int32_t nbits);
+/* write_symbol / write_cdf: symbol s of nsyms (2..16) under the inverse CDF
+ * icdf (C layout, nsyms + 1 entries: icdf[nsyms - 1] = 0, the adaptation
+ * counter at icdf[nsyms]); adapt != 0 updates icdf as the decoder will. */
+int32_t zf_ec_symbol(zf_ec *ec, int32_t s, uint16_t *icdf, int32_t nsyms, int32_t adapt);
+/* OdEcEnc::tell: bits used so far, the terminating bit included */
+int32_t zf_ec_tell(const zf_ec *ec);
+/* OdEcEnc::done: the stream's bytes into out (cap bytes); returns their
+ * count, ZF_ERR_ARG when cap is too small. The coder stays usable: more
+ * symbols may follow, and a later call returns the longer stream. */
+int32_t zf_ec_done(zf_ec *ec, uint8_t *out, int32_t cap);
+/* The default wiener_restore (use_wiener) CDF of a tile: {32768 - 11570, 0, 0}. */
+void zf_wiener_restore_cdf_init(uint16_t cdf[3]);
+/* Codes elements from zf_lr_sb_syntax: restore flags on wiener_cdf (adapted),
+ * bits as literals. ZF_ERR_ARG on a malformed element (nothing coded). */
+int32_t zf_ec_lr_syms(zf_ec *ec, const zf_lr_sym *syms, int32_t n, uint16_t wiener_cdf[3]);
+/* zf_lr_sb_syntax for the superblock, coded at once: returns the element
+ * count (refs and wiener_cdf advanced) or a negative code (nothing coded). */
+int32_t zf_ec_lr_sb(zf_ec *ec, const zf_decisions *d, int32_t mi_row, int32_t mi_col, int32_t sb_mi, int32_t frame_w,
+                    int32_t frame_h, int32_t monochrome, int32_t sr_denom, zf_wiener_refs *refs,
+                    uint16_t wiener_cdf[3]);
+/* Per-superblock cdef_idx state (the reference's CdefSbState,
+ * svtav1-encoder/src/pipeline.rs:3965-3980; C cdef_transmitted[4]). */
+typedef struct zf_cdef_sb {
+    int32_t bits;                /* cdef_bits: 0 codes nothing */
+    int32_t sb128;               /* 128x128 superblock: four filter blocks */
+    uint8_t strengths[4];        /* strength index per 64x64 quadrant (TL, TR, BL, BR) */
+    uint8_t transmitted[4];
+} zf_cdef_sb;
+/* At each superblock's start (superblock row/column sb_row, sb_col of
+ * sb_size 64 or 128): reads the quadrants' indices from d->cdef_fb_idx
+ * (pipeline.rs:2707-2745). */
+int32_t zf_cdef_sb_begin(const zf_decisions *d, int32_t sb_row, int32_t sb_col, int32_t sb_size, zf_cdef_sb *st);
+/* After a coded block's skip flag (block at luma sample block_x, block_y):
+ * the first non-skip block of each 64x64 filter block codes that filter
+ * block's index as cdef_bits literal bits (pipeline.rs:4995-5017; C
+ * write_cdef; spec read_cdef). Returns the bits coded (0 or cdef_bits). */
+int32_t zf_ec_cdef_block(zf_ec *ec, zf_cdef_sb *st, int32_t block_x, int32_t block_y, int32_t skip);
+
 /* ---- Self-guided restoration (RESTORE_SGRPROJ) ---------------------------
  * No counterpart in the reference encoder: it never searches or signals
  * SGRPROJ (svtav1-dsp/src/restoration.rs:1280, svtav1-encoder/src/

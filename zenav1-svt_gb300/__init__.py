@@ -100,6 +100,24 @@ def lib():
     L.zf_lr_corners_in_sb.argtypes = [C.c_int32] * 8 + [P(C.c_int32)]
     L.zf_lr_sb_syntax.argtypes = [P(ZfDecisions)] + [C.c_int32] * 7 + [P(abi.ZfWienerRefs), P(abi.ZfLrSym),
                                                                      C.c_int32]
+    L.zf_ec_create.argtypes = []
+    L.zf_ec_create.restype = C.c_void_p
+    L.zf_ec_destroy.argtypes = [C.c_void_p]
+    L.zf_ec_destroy.restype = None
+    L.zf_ec_reset.argtypes = [C.c_void_p]
+    L.zf_ec_reset.restype = None
+    L.zf_ec_bool.argtypes = [C.c_void_p, C.c_int32, C.c_uint32]
+    L.zf_ec_literal.argtypes = [C.c_void_p, C.c_uint32, C.c_int32]
+    L.zf_ec_symbol.argtypes = [C.c_void_p, C.c_int32, P(C.c_uint16), C.c_int32, C.c_int32]
+    L.zf_ec_tell.argtypes = [C.c_void_p]
+    L.zf_ec_done.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
+    L.zf_wiener_restore_cdf_init.argtypes = [P(C.c_uint16)]
+    L.zf_wiener_restore_cdf_init.restype = None
+    L.zf_ec_lr_syms.argtypes = [C.c_void_p, P(abi.ZfLrSym), C.c_int32, P(C.c_uint16)]
+    L.zf_ec_lr_sb.argtypes = [C.c_void_p, P(ZfDecisions)] + [C.c_int32] * 7 + [P(abi.ZfWienerRefs),
+                                                                             P(C.c_uint16)]
+    L.zf_cdef_sb_begin.argtypes = [P(ZfDecisions), C.c_int32, C.c_int32, C.c_int32, P(abi.ZfCdefSb)]
+    L.zf_ec_cdef_block.argtypes = [C.c_void_p, P(abi.ZfCdefSb), C.c_int32, C.c_int32, C.c_int32]
     L.zf_get_tune.argtypes = [C.c_void_p, P(abi.ZfTune)]
     L.zf_set_tune.argtypes = [C.c_void_p, P(abi.ZfTune)]
     L.zf_autotune.argtypes = [C.c_void_p, P(ZfFrame), C.c_int32, C.c_int32, P(abi.ZfTune), P(abi.ZfTune),
@@ -116,7 +134,8 @@ def lib():
                  "zf_film_grain_synthesize", "zf_write_filter_params", "zf_sgr_search", "zf_sgr_apply", "zf_create", "zf_sync", "zf_query_sizes", "zf_pack_geom", "zf_filter_stage",
                  "zf_submit_batch", "zf_deblock_pick", "zf_deblock_apply", "zf_cdef_search",
                  "zf_deblock_sse_table", "zf_cdef_search_rows", "zf_trace", "zf_set_wait_limit",
-                 "zf_cdef_apply", "zf_lr_search", "zf_lr_apply"):
+                 "zf_cdef_apply", "zf_lr_search", "zf_lr_apply", "zf_ec_bool", "zf_ec_literal", "zf_ec_symbol",
+                 "zf_ec_tell", "zf_ec_done", "zf_ec_lr_syms", "zf_ec_lr_sb", "zf_cdef_sb_begin", "zf_ec_cdef_block"):
         getattr(L, name).restype = C.c_int32
     _lib = L
     return L
@@ -421,6 +440,69 @@ def write_filter_params(dec, monochrome=False, allow_intrabc=False, enable_resto
     if rc != 0:
         raise ZfError(rc, "zf_write_filter_params")
     return buf, pos.value
+
+
+class RangeCoder:
+    """The tile symbol coder (zf_ec_*): AV1's arithmetic coder, with the
+    filter stage's per-superblock restoration syntax and cdef_idx literals."""
+
+    def __init__(self):
+        self._ec = lib().zf_ec_create()
+        if not self._ec:
+            raise MemoryError("zf_ec_create")
+        self.wiener_cdf = (C.c_uint16 * 3)()
+        lib().zf_wiener_restore_cdf_init(self.wiener_cdf)
+        self.refs = abi.ZfWienerRefs()
+        lib().zf_wiener_refs_reset(C.byref(self.refs))
+
+    def __del__(self):
+        if getattr(self, "_ec", None):
+            lib().zf_ec_destroy(self._ec)
+            self._ec = None
+
+    def _chk(self, rc, what):
+        if rc < 0:
+            raise ZfError(rc, what)
+        return rc
+
+    def bool(self, bit, f=16384):
+        self._chk(lib().zf_ec_bool(self._ec, int(bit), int(f)), "zf_ec_bool")
+
+    def literal(self, value, nbits):
+        self._chk(lib().zf_ec_literal(self._ec, int(value), int(nbits)), "zf_ec_literal")
+
+    def symbol(self, s, icdf, adapt=True):
+        """icdf: a ctypes uint16 array of nsyms + 1 entries (C layout), updated in place when adapt."""
+        self._chk(lib().zf_ec_symbol(self._ec, int(s), icdf, len(icdf) - 1, int(adapt)), "zf_ec_symbol")
+
+    def tell(self):
+        return lib().zf_ec_tell(self._ec)
+
+    def done(self):
+        n = (self.tell() + 7) // 8
+        buf = np.zeros(max(n, 1), np.uint8)
+        n = self._chk(lib().zf_ec_done(self._ec, buf.ctypes.data, len(buf)), "zf_ec_done")
+        return bytes(buf[:n])
+
+    def lr_sb(self, dec, mi_row, mi_col, sb_mi, frame_w, frame_h, monochrome=False, sr_denom=0):
+        """Codes the restoration units whose corner lies in the superblock
+        (at its start); returns the element count."""
+        return self._chk(lib().zf_ec_lr_sb(self._ec, C.byref(dec), mi_row, mi_col, sb_mi, frame_w, frame_h,
+                                           int(monochrome), sr_denom, C.byref(self.refs), self.wiener_cdf),
+                         "zf_ec_lr_sb")
+
+    @staticmethod
+    def cdef_sb(dec, sb_row, sb_col, sb_size=64):
+        st = abi.ZfCdefSb()
+        rc = lib().zf_cdef_sb_begin(C.byref(dec), sb_row, sb_col, sb_size, C.byref(st))
+        if rc < 0:
+            raise ZfError(rc, "zf_cdef_sb_begin")
+        return st
+
+    def cdef_block(self, st, block_x, block_y, skip):
+        """After a coded block's skip flag; returns the cdef_idx bits coded."""
+        return self._chk(lib().zf_ec_cdef_block(self._ec, C.byref(st), block_x, block_y, int(skip)),
+                         "zf_ec_cdef_block")
 
 
 def query_sizes(fr, mi=None):

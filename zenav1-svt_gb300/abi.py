@@ -66,6 +66,11 @@ class ZfWienerRefs(C.Structure):
     _fields_ = [("vfilter", (C.c_int16 * 8) * 3), ("hfilter", (C.c_int16 * 8) * 3)]
 
 
+class ZfCdefSb(C.Structure):
+    _fields_ = [("bits", C.c_int32), ("sb128", C.c_int32), ("strengths", C.c_uint8 * 4),
+                ("transmitted", C.c_uint8 * 4)]
+
+
 class ZfTune(C.Structure):
     _fields_ = [("graphs", C.c_int32), ("stats_tma", C.c_int32), ("apply_group", C.c_int32),
                 ("stats_tc", C.c_int32), ("trial_tile", C.c_int32), ("db_levels", C.c_int32),
