@@ -494,6 +494,9 @@ cudaError_t set_kernel_attributes() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(zf::k_lr_stats_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)zf::lr_stats_tc_smem());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(zf::k_lr_trial, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)zf::lr_trial_smem(zf::kTrialMaxTilesHost));
     if (e == cudaSuccess) e = zf::joint_set_attributes();
     if (e == cudaSuccess) e = zf::sgr_set_attributes();
     return e;
@@ -961,6 +964,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     // Work lists (host-known shapes).
     // statistics: 5-tap 8-bit, 5-tap 10-bit (one kernel instantiation each), 7-tap
     WorkList wl_db, wl_cs, wl_ca, wl_st5, wl_st7, wl_unit, wl_apply, wl_trial, wl_tiles, wl_st5h, wl_stc;
+    int trial_tiles = 1;  // k_lr_trial: the most tiles one CTA of a unit's cluster stages
     std::vector<int> cdef_small, cdef_large;  // joint search: one CTA / cluster per bit count
     std::vector<int> cdef_joint[kJointGroups];  // register-row joint search, by (candidates, rows per thread)
     for (int i = 0; i < n; ++i) {
@@ -998,6 +1002,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 if (L.refine) {
                     // one cluster per unit: the hill-climb is sequential, its trials are not
                     wl_trial.add(i, pl, (int)u, 0, zf::kTrialClusterHost);
+                    trial_tiles = std::max(trial_tiles, zf::lr_trial_tiles_per_cta(r.h_end - r.h_start, uh));
                 } else {
                     const int tl = ctx->trial_tile, uw = r.h_end - r.h_start;
                     wl_tiles.add(i, pl, (int)u, 0, ((uw + tl - 1) / tl) * ((uh + tl - 1) / tl));
@@ -1471,8 +1476,10 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             TRY(launch_check(ctx, "k_lr_solve"));
             if (wl_trial.ctas) {
                 { LaunchScope ls_(ctx, "k_lr_trial");
-                zf::k_lr_trial<<<wl_trial.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_trial),
-                                                             (int)wl_trial.items.size()); }
+                if (trial_tiles > zf::kTrialMaxTilesHost)
+                    return fail(ctx, ZF_ERR_UNSUPPORTED, "a restoration unit exceeds the refinement trial's tiles");
+                zf::k_lr_trial<<<wl_trial.ctas, 256, zf::lr_trial_smem(trial_tiles), st>>>(
+                    d_desc, (const WorkItem *)(base + o_trial), (int)wl_trial.items.size(), trial_tiles); }
                 TRY(launch_check(ctx, "k_lr_trial"));
             }
             if (wl_tiles.ctas) {
@@ -1530,6 +1537,8 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         const FrameDesc &b = back[i];
         const uint8_t *fbidx = ob + p.off_fbidx, *fbrow = ob + p.off_fbrow;
         const unsigned long long *cst = (const unsigned long long *)(ob + p.off_stats);
+        if (cst[3] & 4)
+            return fail(ctx, ZF_ERR_CUDA, "a refinement trial unit needed more tiles than its shared memory holds");
         if (cst[3]) return fail(ctx, ZF_ERR_TIMEOUT, "a statistics tile load did not arrive within its wait limit");
         const bool searched = (run.stages & STG_LR_SEARCH) && !run.lr_given;
         auto packed = [&](int pl) { return (const zf::PackedUnit *)(ob + p.off_packed[pl]); };

@@ -46,7 +46,11 @@ __global__ void k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitem
 cudaError_t launch_lr_stats(int win, int bd, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
                             int nitems);
 __global__ void k_lr_solve(FrameDesc *frames, const WorkItem *items, int nitems);
-__global__ void k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems);
+// max_tiles: tiles per CTA its dynamic shared memory (lr_trial_smem) holds.
+__global__ void k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems, int max_tiles);
+size_t lr_trial_smem(int max_tiles);
+__host__ __device__ int lr_trial_tiles_per_cta(int uw, int uh);
+constexpr int kTrialMaxTilesHost = 9;  // a unit of at most 383 x 383: 6 x 12 tiles of 64 x 32 over 8 CTAs
 // k_lr_trial_tiles<tl> (tile edge 32 or 64) over `ctas` tiles.
 cudaError_t launch_lr_trial_tiles(int tl, int ctas, cudaStream_t st, FrameDesc *frames, const WorkItem *items,
                                   int nitems);

@@ -964,24 +964,34 @@ __device__ __forceinline__ int wiener_v(const int *tp, const int16_t *vf, int bd
 }
 
 // SSE of the unit filtered with `t` against the source; three parts as in
-// sse_region_hbd. Returns the combined value in thread 0 (all threads get it).
+// sse_region_hbd. Returns the combined value (every thread gets it).
 // The refinement trial runs on a cluster of kTrialCluster CTAs per unit:
-// CTA `rank` filters tiles rank, rank + CL, ... of the unit, the partial SSE
-// parts are pushed into every rank's inbox (double-buffered) before one
-// cluster barrier, and every CTA forms the same total, so the hill-climb
-// decisions stay identical across the cluster.
+// CTA `rank` owns tiles rank, rank + CL, ... of the unit. It stages their
+// dgd windows and source tiles in shared memory once, before the first
+// trial (the samples do not change between trials, only the taps), so a
+// trial is the two filter passes over shared memory: the horizontal pass of
+// tile k and the vertical pass of tile k - 1 share one barrier (two
+// horizontal-pass buffers). The partial SSE parts are pushed into every
+// rank's inbox (double-buffered) before one cluster barrier, and every CTA
+// forms the same total, so the hill-climb decisions stay identical across
+// the cluster.
 constexpr int kTrialCluster = 8;
+constexpr int TRIAL_SW = TT_W + 8, TRIAL_SH = TT_H + 7;  // staged window rows 8-byte aligned
+constexpr int TRIAL_WIN = TRIAL_SH * TRIAL_SW, TRIAL_SRC = TT_H * TT_W, TRIAL_TMP = TRIAL_SH * TT_W;
 
-__device__ int64_t trial_sse(const FrameDesc &f, int plane, const LrPlane &pl, const UnitRect &r, const Taps &t,
-                             uint16_t *stage, uint16_t *tmp, uint16_t *srct, unsigned long long *red,
-                             unsigned long long (*inbox)[kTrialCluster][3], int &buf) {
+struct TrialTiles {
+    const uint16_t *win, *src;  // [n][TRIAL_WIN], [n][TRIAL_SRC]
+    uint16_t *tmp;              // [2][TRIAL_TMP]
+    int n, ntx, rank, CL;
+};
+
+__device__ int64_t trial_sse(const FrameDesc &f, const UnitRect &r, const Taps &t, const TrialTiles &T,
+                             unsigned long long *red, unsigned long long (*inbox)[kTrialCluster][3], int &buf) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
-    const int rank = (int)cl.block_rank(), CL = (int)cl.num_blocks();
-    const int bd = f.bd, stride = plane_stride(f, plane);
+    const int bd = f.bd;
     const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
     const int dw = uw % 16, dh = uh % 16;
-    const uint8_t *dg = f.A[plane], *sr = f.S[plane];
     // The taps are symmetric (f[6 - k] = f[k], f[7] = 0: the solve and every
     // refinement step keep them so), so each pass is four multiplies per
     // output on pair sums, the centre tap carrying the 128 of
@@ -998,82 +1008,83 @@ __device__ int64_t trial_sse(const FrameDesc &f, int plane, const LrPlane &pl, c
     const int hc3 = 128 + hf[3], hoff = 1 << (bd + 6), hlim = (1 << (bd + 5)) - 1;
     const int vc3 = 128 + vf[3], voff = -(1 << (bd + 10)), vmax = (1 << bd) - 1;
     uint32_t blk = 0, rgt = 0, bot = 0;  // a thread's parts of one trial: <= 9 tiles x 8 pixels of e^2 <= 1023^2
-    constexpr int SW = TT_W + 8, SH = TT_H + 7;  // staged rows 8-byte aligned
-    const int ntx = (uw + TT_W - 1) / TT_W, ntiles = ntx * ((uh + TT_H - 1) / TT_H);
-    for (int tile = rank; tile < ntiles; tile += CL) {
-        const int ty = (tile / ntx) * TT_H, tx = (tile - (tile / ntx) * ntx) * TT_W;
-        const int y0 = r.v_start + ty, x0 = r.h_start + tx;
-        const int th = min(TT_H, uh - ty), tw = min(TT_W, uw - tx);
-        __syncthreads();
-        stage_window<1>(
-            bd, pl.pw, SH, x0 - 3, TT_W + 7, true, 0,
-            [&](int rr) { return row_ptr(dg, clampi(y0 - 3 + rr, 0, pl.ph - 1), stride, bd); },
-            [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
-        stage_window<1>(
-            bd, pl.pw, th, x0, tw, true, 0, [&](int rr) { return row_ptr(sr, y0 + rr, stride, bd); },
-            [&](int rr, int cc, int v) { srct[rr * TT_W + cc] = (uint16_t)v; });
-        __syncthreads();
-        // horizontal: every staged row x 16 runs of four columns
-        for (int q = threadIdx.x; q < SH * (TT_W / 4); q += blockDim.x) {
-            const int rr = q >> 4, c0 = (q & 15) * 4;
-            if (c0 >= tw) continue;
-            const uint2 *sp = reinterpret_cast<const uint2 *>(stage + rr * SW + c0);
-            int p[12];
+    for (int k = 0; k <= T.n; ++k) {
+        if (k < T.n) {
+            // horizontal pass of tile k: every staged row x 16 runs of four columns
+            const int tile = T.rank + k * T.CL;
+            const int tw = min(TT_W, uw - (tile % T.ntx) * TT_W);
+            const uint16_t *stage = T.win + k * TRIAL_WIN;
+            uint16_t *tmp = T.tmp + (k & 1) * TRIAL_TMP;
+            for (int q = threadIdx.x; q < TRIAL_SH * (TT_W / 4); q += blockDim.x) {
+                const int rr = q >> 4, c0 = (q & 15) * 4;
+                if (c0 >= tw) continue;
+                const uint2 *sp = reinterpret_cast<const uint2 *>(stage + rr * TRIAL_SW + c0);
+                int p[12];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const uint2 w = sp[k];
-                p[4 * k] = (int)(w.x & 0xffffu);
-                p[4 * k + 1] = (int)(w.x >> 16);
-                p[4 * k + 2] = (int)(w.y & 0xffffu);
-                p[4 * k + 3] = (int)(w.y >> 16);
-            }
-            uint32_t o[4];
+                for (int j = 0; j < 3; ++j) {
+                    const uint2 w = sp[j];
+                    p[4 * j] = (int)(w.x & 0xffffu);
+                    p[4 * j + 1] = (int)(w.x >> 16);
+                    p[4 * j + 2] = (int)(w.y & 0xffffu);
+                    p[4 * j + 3] = (int)(w.y >> 16);
+                }
+                uint32_t o[4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                int sum = p[j + 3] * hc3 + hf[1] * (p[j + 1] + p[j + 5]) + hf[2] * (p[j + 2] + p[j + 4]) + hoff;
-                if (!t5) sum += hf[0] * (p[j] + p[j + 6]);
-                o[j] = (uint32_t)clampi((sum + 4) >> 3, 0, hlim);
-            }
-            *reinterpret_cast<uint2 *>(tmp + rr * TT_W + c0) = make_uint2(o[0] | o[1] << 16, o[2] | o[3] << 16);
-        }
-        __syncthreads();
-        // vertical: four columns of one row per thread, packed pair sums
-        // (tmp values are < 2^15), the SSE parts against the staged source
-        for (int q = threadIdx.x; q < th * (TT_W / 4); q += blockDim.x) {
-            const int rr = q >> 4, c0 = (q & 15) * 4;
-            if (c0 >= tw) continue;
-            uint2 v[7];
-#pragma unroll
-            for (int k = 0; k < 7; ++k)
-                v[k] = (t5 && (k == 0 || k == 6)) ? make_uint2(0, 0)
-                                                  : *reinterpret_cast<const uint2 *>(tmp + (rr + k) * TT_W + c0);
-            const uint32_t p1x = v[1].x + v[5].x, p1y = v[1].y + v[5].y;
-            const uint32_t p2x = v[2].x + v[4].x, p2y = v[2].y + v[4].y;
-            const uint32_t p0x = v[0].x + v[6].x, p0y = v[0].y + v[6].y;
-            auto lo = [](uint32_t w) { return (int)(w & 0xffffu); };
-            auto hi = [](uint32_t w) { return (int)(w >> 16); };
-            auto out = [&](int c, int a1, int a2, int a0) {
-                const int sum = c * vc3 + vf[1] * a1 + vf[2] * a2 + vf[0] * a0 + voff;
-                return clampi((sum + (1 << 10)) >> 11, 0, vmax);
-            };
-            const int y[4] = {out(lo(v[3].x), lo(p1x), lo(p2x), lo(p0x)), out(hi(v[3].x), hi(p1x), hi(p2x), hi(p0x)),
-                              out(lo(v[3].y), lo(p1y), lo(p2y), lo(p0y)), out(hi(v[3].y), hi(p1y), hi(p2y), hi(p0y))};
-            const uint2 sv = *reinterpret_cast<const uint2 *>(srct + rr * TT_W + c0);
-            const int sx[4] = {lo(sv.x), hi(sv.x), lo(sv.y), hi(sv.y)};
-            const int i = ty + rr, nq = min(4, tw - c0);
-#pragma unroll
-            for (int jj = 0; jj < 4; ++jj) {
-                if (jj >= nq) break;
-                const int e = sx[jj] - y[jj];
-                const uint32_t e2 = (uint32_t)(e * e);
-                if (tx + c0 + jj >= uw - dw) rgt += e2;
-                else if (i >= uh - dh) bot += e2;
-                else blk += e2;
+                for (int j = 0; j < 4; ++j) {
+                    int sum = p[j + 3] * hc3 + hf[1] * (p[j + 1] + p[j + 5]) + hf[2] * (p[j + 2] + p[j + 4]) + hoff;
+                    if (!t5) sum += hf[0] * (p[j] + p[j + 6]);
+                    o[j] = (uint32_t)clampi((sum + 4) >> 3, 0, hlim);
+                }
+                *reinterpret_cast<uint2 *>(tmp + rr * TT_W + c0) = make_uint2(o[0] | o[1] << 16, o[2] | o[3] << 16);
             }
         }
+        if (k > 0) {
+            // vertical pass of tile k - 1: four columns of one row per
+            // thread, packed pair sums (tmp values are < 2^15), the SSE
+            // parts against the staged source
+            const int tile = T.rank + (k - 1) * T.CL;
+            const int ty = (tile / T.ntx) * TT_H, tx = (tile % T.ntx) * TT_W;
+            const int th = min(TT_H, uh - ty), tw = min(TT_W, uw - tx);
+            const uint16_t *tmp = T.tmp + ((k - 1) & 1) * TRIAL_TMP;
+            const uint16_t *srct = T.src + (k - 1) * TRIAL_SRC;
+            for (int q = threadIdx.x; q < th * (TT_W / 4); q += blockDim.x) {
+                const int rr = q >> 4, c0 = (q & 15) * 4;
+                if (c0 >= tw) continue;
+                uint2 v[7];
+#pragma unroll
+                for (int j = 0; j < 7; ++j)
+                    v[j] = (t5 && (j == 0 || j == 6)) ? make_uint2(0, 0)
+                                                      : *reinterpret_cast<const uint2 *>(tmp + (rr + j) * TT_W + c0);
+                const uint32_t p1x = v[1].x + v[5].x, p1y = v[1].y + v[5].y;
+                const uint32_t p2x = v[2].x + v[4].x, p2y = v[2].y + v[4].y;
+                const uint32_t p0x = v[0].x + v[6].x, p0y = v[0].y + v[6].y;
+                auto lo = [](uint32_t w) { return (int)(w & 0xffffu); };
+                auto hi = [](uint32_t w) { return (int)(w >> 16); };
+                auto out = [&](int c, int a1, int a2, int a0) {
+                    const int sum = c * vc3 + vf[1] * a1 + vf[2] * a2 + vf[0] * a0 + voff;
+                    return clampi((sum + (1 << 10)) >> 11, 0, vmax);
+                };
+                const int y[4] = {out(lo(v[3].x), lo(p1x), lo(p2x), lo(p0x)),
+                                  out(hi(v[3].x), hi(p1x), hi(p2x), hi(p0x)),
+                                  out(lo(v[3].y), lo(p1y), lo(p2y), lo(p0y)),
+                                  out(hi(v[3].y), hi(p1y), hi(p2y), hi(p0y))};
+                const uint2 sv = *reinterpret_cast<const uint2 *>(srct + rr * TT_W + c0);
+                const int sx[4] = {lo(sv.x), hi(sv.x), lo(sv.y), hi(sv.y)};
+                const int i = ty + rr, nq = min(4, tw - c0);
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj) {
+                    if (jj >= nq) break;
+                    const int e = sx[jj] - y[jj];
+                    const uint32_t e2 = (uint32_t)(e * e);
+                    if (tx + c0 + jj >= uw - dw) rgt += e2;
+                    else if (i >= uh - dh) bot += e2;
+                    else blk += e2;
+                }
+            }
+        }
+        __syncthreads();
     }
     unsigned long long v[3] = {blk, rgt, bot};
-    __syncthreads();
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
 #pragma unroll
@@ -1088,22 +1099,30 @@ __device__ int64_t trial_sse(const FrameDesc &f, int plane, const LrPlane &pl, c
         mine[threadIdx.x] = s;
     }
     __syncthreads();
-    if (threadIdx.x < CL)  // this CTA's parts into rank threadIdx.x's inbox
-        for (int k = 0; k < 3; ++k) *cl.map_shared_rank(&inbox[buf][rank][k], (int)threadIdx.x) = mine[k];
+    if (threadIdx.x < T.CL)  // this CTA's parts into rank threadIdx.x's inbox
+        for (int k = 0; k < 3; ++k) *cl.map_shared_rank(&inbox[buf][T.rank][k], (int)threadIdx.x) = mine[k];
     cl.sync();
     unsigned long long sp[3] = {0, 0, 0};
-    for (int q = 0; q < CL; ++q)
+    for (int q = 0; q < T.CL; ++q)
         for (int k = 0; k < 3; ++k) sp[k] += inbox[buf][q][k];
     buf ^= 1;
     return bd == 8 ? (int64_t)(sp[0] + sp[1] + sp[2])
                    : (int64_t)sp[0] + (int64_t)(uint32_t)sp[1] + (int64_t)(uint32_t)sp[2];
 }
 
-__global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256)
-    k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems) {
-    __shared__ __align__(16) uint16_t stage[(TT_H + 7) * (TT_W + 8)];
-    __shared__ __align__(16) uint16_t tmp[(TT_H + 7) * TT_W];
-    __shared__ __align__(16) uint16_t srct[TT_H * TT_W];
+size_t lr_trial_smem(int max_tiles) {
+    return (size_t)max_tiles * (TRIAL_WIN + TRIAL_SRC) * 2 + 2 * TRIAL_TMP * 2;
+}
+__host__ __device__ int lr_trial_tiles_per_cta(int uw, int uh) {
+    return (((uw + TT_W - 1) / TT_W) * ((uh + TT_H - 1) / TT_H) + kTrialCluster - 1) / kTrialCluster;
+}
+
+// max_tiles: the tiles per CTA the dynamic shared memory holds
+// (lr_trial_smem); a unit needing more sets cdef_stats[3] bit 2 and is
+// skipped by its whole cluster.
+__global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256, 3)
+    k_lr_trial(FrameDesc *frames, const WorkItem *items, int nitems, int max_tiles) {
+    extern __shared__ __align__(16) uint16_t trial_dyn[];
     __shared__ unsigned long long red[24];
     __shared__ unsigned long long inbox[2][kTrialCluster][3];
     __shared__ Taps t;
@@ -1113,17 +1132,51 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256)
     const LrPlane &pl = f.lr[wi.plane];
     LrUnit &u = pl.units[wi.a];
     const UnitRect r = pl.rects[wi.a];
-    const bool lead = cooperative_groups::this_cluster().block_rank() == 0;
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const bool lead = cl.block_rank() == 0;
     if (u.score > 0) {  // uniform over the cluster (one unit)
         if (lead && threadIdx.x == 0) u.sse_wn = INT64_MAX;
         return;
+    }
+    const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
+    if (lr_trial_tiles_per_cta(uw, uh) > max_tiles) {  // uniform over the cluster
+        if (lead && threadIdx.x == 0) atomicOr(&f.cdef_stats[3], 4ull);
+        return;
+    }
+    TrialTiles T;
+    T.rank = (int)cl.block_rank();
+    T.CL = (int)cl.num_blocks();
+    T.ntx = (uw + TT_W - 1) / TT_W;
+    const int ntiles = T.ntx * ((uh + TT_H - 1) / TT_H);
+    T.n = T.rank < ntiles ? (ntiles - T.rank + T.CL - 1) / T.CL : 0;
+    T.win = trial_dyn;
+    T.src = trial_dyn + max_tiles * TRIAL_WIN;
+    T.tmp = trial_dyn + max_tiles * (TRIAL_WIN + TRIAL_SRC);
+    {
+        const int bd = f.bd, stride = plane_stride(f, wi.plane);
+        const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
+        for (int k = 0; k < T.n; ++k) {
+            const int tile = T.rank + k * T.CL;
+            const int ty = (tile / T.ntx) * TT_H, tx = (tile % T.ntx) * TT_W;
+            const int y0 = r.v_start + ty, x0 = r.h_start + tx;
+            const int th = min(TT_H, uh - ty), tw = min(TT_W, uw - tx);
+            uint16_t *stage = trial_dyn + k * TRIAL_WIN, *srct = trial_dyn + max_tiles * TRIAL_WIN + k * TRIAL_SRC;
+            stage_window<4>(
+                bd, pl.pw, TRIAL_SH, x0 - 3, TT_W + 7, true, 0,
+                [&](int rr) { return row_ptr(dg, clampi(y0 - 3 + rr, 0, pl.ph - 1), stride, bd); },
+                [&](int rr, int cc, int v) { stage[rr * TRIAL_SW + cc] = (uint16_t)v; });
+            stage_window<4>(
+                bd, pl.pw, th, x0, tw, true, 0, [&](int rr) { return row_ptr(sr, y0 + rr, stride, bd); },
+                [&](int rr, int cc, int v) { srct[rr * TT_W + cc] = (uint16_t)v; });
+        }
     }
     if (threadIdx.x < 8) {
         t.v[threadIdx.x] = u.vf[threadIdx.x];
         t.h[threadIdx.x] = u.hf[threadIdx.x];
     }
     __syncthreads();
-    int64_t err = trial_sse(f, wi.plane, pl, r, t, stage, tmp, srct, red, inbox, buf);
+    int64_t err = trial_sse(f, r, t, T, red, inbox, buf);
     if (pl.refine) {
         // use_refinement with max_one_refinement_step: one step size (4).
         const int plane_off = (7 - pl.win) >> 1;
@@ -1142,7 +1195,7 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256)
                         fp[3] += 2 * s;
                     }
                     __syncthreads();
-                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, srct, red, inbox, buf);
+                    const int64_t e2 = trial_sse(f, r, t, T, red, inbox, buf);
                     if (e2 > err) {
                         __syncthreads();
                         if (threadIdx.x == 0) {
@@ -1166,7 +1219,7 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256)
                         fp[3] -= 2 * s;
                     }
                     __syncthreads();
-                    const int64_t e2 = trial_sse(f, wi.plane, pl, r, t, stage, tmp, srct, red, inbox, buf);
+                    const int64_t e2 = trial_sse(f, r, t, T, red, inbox, buf);
                     if (e2 > err) {
                         __syncthreads();
                         if (threadIdx.x == 0) {
