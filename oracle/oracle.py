@@ -139,7 +139,8 @@ def stage_decisions(fr):
     """The oracle's whole-stage decisions as an abi.Decisions (the
     zf_decisions struct with its caller arrays), for the syntax writers."""
     g = geom_struct(fr.geom)
-    s = _frame(fr, fr.copy_rec())
+    rec = fr.copy_rec()  # held here: the frame struct only points at it
+    s = _frame(fr, rec)
     d = abi.Decisions(fr.w, fr.h, fr.true_w, fr.true_h)
     st = abi.ZfStats()
     assert lib().zfo_filter_stage(C.byref(s), C.byref(g), C.byref(d.c), C.byref(st), BORDER_C) == 0
