@@ -11,7 +11,9 @@ through the C ABI against the oracle, bit-exact on every plane and decision.
   10-bit and odd-size images;
 - a 6000x4000 preset-6 frame, the served workload's largest size: 3818
   filter blocks with 4 candidates, beyond the register-row joint search, so
-  the joint strength search runs on the cluster form;
+  the joint strength search runs on the cluster form (a warp per pair);
+- a 2560x1664 preset-0 frame: 1040 filter blocks at 48 candidates, the
+  cluster form's pair-per-thread step (the 4096x3072 frame takes it at 20);
 - the 4K frame with device-resident planes filtered in place (zero copy).
 
 The oracle needs ~2-20 s per frame on one host core.
@@ -31,6 +33,9 @@ FULL = [
     ("4k_p6_q40", lambda: synth.workload_4k(6, 40)),
     ("4096x3072_bd10_p2_q28", synth.workload_10bit_4096),
     ("6000x4000_p6_q30", lambda: synth.make_frame(synth.frame_seed(5, 6000), 6000, 4000, 8, 30, 6, "cosine")),
+    # 1040 filter blocks at 48 candidates (2304 strength pairs): the cluster
+    # joint search's pair-per-thread step at its widest
+    ("2560x1664_p0_q36", lambda: synth.make_frame(synth.frame_seed(7, 2560), 2560, 1664, 8, 36, 0, "cosine")),
 ]
 
 

@@ -24,6 +24,20 @@ namespace zf {
 constexpr uint16_t kVeryLarge = 0x7f7f;
 constexpr int CR = 68;  // luma region edge: 64 + 2 * 2 halo
 constexpr int CRC = 36; // chroma region edge: 32 + 2 * 2
+// Row pitches in 2-byte samples. At presets <= 5 a warp reads 4 rows x 8
+// columns of one luma 8x8 block, every lane at the same tap offset: with
+// 38 words per row those rows start 6 banks apart, so the 4-word row
+// segments (5 words at an odd offset) of the 32 lanes fall in distinct
+// banks (the region's own 34 words put the rows 2 banks apart: a 2-way
+// conflict on every tap read). At preset 6 (every fourth row) a warp reads
+// rows 0 and 4 of two adjacent blocks, 24 banks apart at this pitch. The
+// direction search's 8 rows x 4 blocks of a warp stay 2-way, as before.
+// The source tiles read one sample per lane: 36 words per row (64 samples
+// were 32 words, every row in the same banks: 4-way); the chroma windows
+// keep 18 words per row, their source tiles take the same.
+constexpr int CRP = 76;
+constexpr int SRCP = 72;
+constexpr int SRCCP = 36;
 
 // Cdef_Directions (AV1 spec 7.15.3) as (dy, dx).
 __constant__ int8_t kDir[8][2][2] = {
@@ -153,7 +167,7 @@ __device__ void find_dirs(const uint16_t *reg, int rs, int cs, const int *blist,
 // Stage a plane window [y0-2, y0+n+2) x [x0-2, x0+n+2) with the sentinel
 // outside the aligned plane (build_src, cdef.rs:517-544).
 __device__ __noinline__ void load_region(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n,
-                                         uint16_t *reg) {
+                                         uint16_t *reg, int pitch) {
     const int rs = n + 4;
     stage_window<1>(
         bd, pw, rs, x0 - 2, rs, false, kVeryLarge,
@@ -161,16 +175,16 @@ __device__ __noinline__ void load_region(const uint8_t *plane, int bd, int pw, i
             const int y = y0 - 2 + ry;
             return (y >= 0 && y < ph) ? row_ptr(plane, y, pw, bd) : (const uint8_t *)nullptr;
         },
-        [&](int ry, int rx, int v) { reg[ry * rs + rx] = (uint16_t)v; });
+        [&](int ry, int rx, int v) { reg[ry * pitch + rx] = (uint16_t)v; });
 }
 
 // Stage the n x n source tile at (x0, y0), 0 outside the canvas.
 __device__ __noinline__ void load_src(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n,
-                                      uint16_t *src) {
+                                      uint16_t *src, int pitch) {
     stage_window<1>(
         bd, pw, n, x0, n, false, 0,
         [&](int ry) { return y0 + ry < ph ? row_ptr(plane, y0 + ry, pw, bd) : (const uint8_t *)nullptr; },
-        [&](int ry, int rx, int v) { src[ry * n + rx] = (uint16_t)v; });
+        [&](int ry, int rx, int v) { src[ry * pitch + rx] = (uint16_t)v; });
 }
 
 // Non-skip 8x8 blocks of one filter block (the dlist, cdef.rs:1203-1213):
@@ -302,8 +316,8 @@ __device__ __forceinline__ int cdef_round(int x, int sum, int mn, int mx) {
 template <int FPM, int NSM>
 __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, const WorkItem *items, int nitems) {
     constexpr int NCM = FPM * NSM;
-    __shared__ uint16_t reg[CR * CR];
-    __shared__ uint16_t src[64 * 64];
+    __shared__ uint16_t reg[CR * CRP];
+    __shared__ uint16_t src[64 * SRCP];
     __shared__ int sdir[64], svar[64];
     __shared__ int dcost[64][8];
     __shared__ int boff[64][6], boffc[64][6];
@@ -311,7 +325,7 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
     __shared__ int blist[64];
     __shared__ int nblk;
     __shared__ uint16_t regc[2][CRC * CRC];
-    __shared__ uint16_t srcc[2][32 * 32];
+    __shared__ uint16_t srcc[2][32 * SRCCP];
     __shared__ uint32_t part[8][NCM + 2 * FPM];
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
@@ -352,21 +366,21 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
     // ---- every plane's window staged at once (luma, then U and V)
     const int x0 = fbc * 64, y0 = fbr * 64;
     const int cw = f.w / 2, ch = f.h / 2, cx0 = fbc * 32, cy0 = fbr * 32;
-    load_region(f.B[0], bd, f.w, f.h, x0, y0, 64, reg);
-    load_src(f.S[0], bd, f.w, f.h, x0, y0, 64, src);
+    load_region(f.B[0], bd, f.w, f.h, x0, y0, 64, reg, CRP);
+    load_src(f.S[0], bd, f.w, f.h, x0, y0, 64, src, SRCP);
     if (f.chroma)
 #pragma unroll 1
         for (int p = 0; p < 2; ++p) {
-            load_region(f.B[p + 1], bd, cw, ch, cx0, cy0, 32, regc[p]);
-            load_src(f.S[p + 1], bd, cw, ch, cx0, cy0, 32, srcc[p]);
+            load_region(f.B[p + 1], bd, cw, ch, cx0, cy0, 32, regc[p], CRC);
+            load_src(f.S[p + 1], bd, cw, ch, cx0, cy0, 32, srcc[p], SRCCP);
         }
     __syncthreads();
-    find_dirs(reg, CR, cs, blist, nblk, dcost, sdir, svar);
+    find_dirs(reg, CRP, cs, blist, nblk, dcost, sdir, svar);
     for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
         const int b = blist[k];
         const int dir = sdir[b], var = svar[b];
         if (f.cdir) f.cdir[(int64_t)fb * 64 + b] = (uint8_t)(dir | (var_code(var) << 3));
-        dir_offsets(dir, CR, boff[b]);
+        dir_offsets(dir, CRP, boff[b]);
         dir_offsets(dir, CRC, boffc[b]);
 #pragma unroll
         for (int i = 0; i < FPM; ++i) {
@@ -388,8 +402,8 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
         const int k = q >> lgs, rem = q & ((1 << lgs) - 1);
         const int b = blist[k];
         const int py = (b >> 3) * 8 + (rem >> 3) * sub, px = (b & 7) * 8 + (rem & 7);
-        const int pos = (py + 2) * CR + px + 2;
-        const int x = (int16_t)reg[pos], sv = src[py * 64 + px];
+        const int pos = (py + 2) * CRP + px + 2;
+        const int x = (int16_t)reg[pos], sv = src[py * SRCP + px];
         int d[12], mx, mn, S[NSM];
         {  // block direction: candidates with p_i != 0
             load_taps_at(edge_y, reg, pos, boff[b], x, d, mx, mn);
@@ -410,7 +424,7 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
             }
         }
         if (any_zero) {  // direction 0: candidates with p_i == 0
-            const int o0[6] = {-1 * CR + 1, -2 * CR + 2, 0 * CR + 1, 0 * CR + 2, 1 * CR + 0, 2 * CR + 0};
+            const int o0[6] = {-1 * CRP + 1, -2 * CRP + 2, 0 * CRP + 1, 0 * CRP + 2, 1 * CRP + 0, 2 * CRP + 0};
             load_taps_at(edge_y, reg, pos, o0, x, d, mx, mn);
 #pragma unroll
             for (int j = 1; j < NSM; ++j) S[j] = j < ns ? sec_sum(d, sec[j], ssh[j]) : 0;
@@ -452,7 +466,7 @@ __global__ void __launch_bounds__(256) k_cdef_search(const FrameDesc *frames, co
                 const int k = q >> 4, b = blist[k];
                 const int py = (b >> 3) * 4 + ((q >> 2) & 3), px = (b & 7) * 4 + (q & 3);
                 const int pos = (py + 2) * CRC + px + 2;
-                const int x = (int16_t)regc[p][pos], sv = srcc[p][py * 32 + px];
+                const int x = (int16_t)regc[p][pos], sv = srcc[p][py * SRCCP + px];
                 int d[12], mx, mn;
                 load_taps_at(edge_uv, regc[p], pos, boffc[b], x, d, mx, mn);
 #pragma unroll
@@ -547,6 +561,10 @@ constexpr int kFinClusterMax = 16;  // non-portable cluster size, where the devi
 constexpr int kFinThreads = 512;
 constexpr int kFinWarps = kFinThreads / 32;
 constexpr int kFinRowsPerLane = 8;  // register-cached best for up to 256 rows per CTA
+// Pair-per-thread steps: frames with at least kFinWideMinPairs strength
+// pairs (20 or 48 candidates) and at most kFinBstMax rows per CTA.
+constexpr int kFinWideMinPairs = 256;
+constexpr int kFinBstMax = 512;
 
 __global__ void __launch_bounds__(kFinThreads, 1)
     k_cdef_finish(FrameDesc *frames, const int *frame_ids, int smem_bytes) {
@@ -593,9 +611,17 @@ __global__ void __launch_bounds__(kFinThreads, 1)
     __shared__ unsigned long long g_bv[2][kFinClusterMax];
     __shared__ int g_bi[2][kFinClusterMax];
     uint32_t *dyn = reinterpret_cast<uint32_t *>(dyn64 + 2 * pslots);
-    const bool in_smem = (size_t)2 * pslots * 8 + (size_t)sbr * (n2 + 1) * 4 <= (size_t)smem_bytes;
+    // rows in shared memory take an odd column stride where it fits (the
+    // pair-per-thread step reads 20 or 48 columns at one row per lane: an
+    // odd stride puts them in distinct banks); the global fallback keeps
+    // the stride its slice was sized for
+    const size_t pbytes = (size_t)2 * pslots * 8;
+    const bool in_smem = pbytes + (size_t)sbr * (n2 + 1) * 4 <= (size_t)smem_bytes;
+    const int sbp = in_smem && !(sbr & 1) && pbytes + ((size_t)(sbr + 1) * n2 + sbr) * 4 <= (size_t)smem_bytes
+                        ? sbr + 1
+                        : sbr;
     uint32_t *R = in_smem ? dyn : f.cdef_rows32 + ((size_t)level * nfb + fb0) * n2;
-    int *ids = in_smem ? reinterpret_cast<int *>(dyn + (size_t)sbr * n2) : f.cdef_ids + (size_t)level * nfb + fb0;
+    int *ids = in_smem ? reinterpret_cast<int *>(dyn + (size_t)sbp * n2) : f.cdef_ids + (size_t)level * nfb + fb0;
     {
         int pos = scan[t] - cnt;
         for (int fb = c0; fb < c1; ++fb)
@@ -618,8 +644,8 @@ __global__ void __launch_bounds__(kFinThreads, 1)
         return;
     }
     for (int q = t; q < sbr * n2; q += T) {
-        const int k = q / sbr, s = q - k * sbr;  // column-major: R[k * sbr + s]
-        R[q] = (uint32_t)f.mse[(int64_t)ids[s] * n2 + k];
+        const int k = q / sbr, s = q - k * sbr;  // column-major: R[k * sbp + s]
+        R[k * sbp + s] = (uint32_t)f.mse[(int64_t)ids[s] * n2 + k];
     }
     if (lane < 16) {
         wlev[warp][0][lane] = 0;
@@ -631,8 +657,44 @@ __global__ void __launch_bounds__(kFinThreads, 1)
     int buf = 0;
     // One search_one_dual step (cdef.rs:824-862) over the whole frame for
     // strength slot nbs; returns the best total and records the pair.
+    __shared__ uint32_t bsts[kFinBstMax];
+    const bool wide = npairs >= kFinWideMinPairs && sbr <= kFinBstMax;
     auto step = [&](int nbs) -> unsigned long long {
-        const bool cached = sbr <= 32 * kFinRowsPerLane;
+        if (wide) {
+            // the best of the fixed strengths per row, then one pair per
+            // thread over all of the CTA's rows: no cross-lane reduction
+            for (int s = t; s < sbr; s += T) {
+                uint32_t b = 0xffffffffu;  // +infinity for an empty strength set
+                for (int gi = 0; gi < nbs; ++gi) {
+                    const uint32_t c = R[lev0[gi] * sbp + s] + R[(n_cand + lev1[gi]) * sbp + s];
+                    b = c < b ? c : b;
+                }
+                bsts[s] = b;
+            }
+            __syncthreads();
+            for (int p = t; p < npairs; p += T) {
+                const int j = p / n_cand, k = p - j * n_cand;
+                const uint32_t *rj = R + (size_t)j * sbp, *rk = R + (size_t)(n_cand + k) * sbp;
+                unsigned long long acc = 0;
+                int s = 0;
+                // four rows per u32 partial: each min is below 2^30
+                for (; s + 4 <= sbr; s += 4) {
+                    uint32_t m = 0;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const uint32_t c = rj[s + u] + rk[s + u], b = bsts[s + u];
+                        m += c < b ? c : b;
+                    }
+                    acc += m;
+                }
+                for (; s < sbr; ++s) {
+                    const uint32_t c = rj[s] + rk[s], b = bsts[s];
+                    acc += c < b ? c : b;
+                }
+                *cl.map_shared_rank(tot[buf] + rank * owned + p / CL, p % CL) = acc;
+            }
+        }
+        const bool cached = !wide && sbr <= 32 * kFinRowsPerLane;
         uint32_t bst[kFinRowsPerLane];
         if (cached) {
 #pragma unroll
@@ -641,15 +703,15 @@ __global__ void __launch_bounds__(kFinThreads, 1)
                 uint32_t b = 0xffffffffu;  // +infinity for an empty strength set
                 if (s < sbr)
                     for (int gi = 0; gi < nbs; ++gi) {
-                        const uint32_t c = R[lev0[gi] * sbr + s] + R[(n_cand + lev1[gi]) * sbr + s];
+                        const uint32_t c = R[lev0[gi] * sbp + s] + R[(n_cand + lev1[gi]) * sbp + s];
                         b = c < b ? c : b;
                     }
                 bst[r] = b;
             }
         }
-        for (int p = warp; p < npairs; p += kFinWarps) {
+        for (int p = warp; p < npairs && !wide; p += kFinWarps) {
             const int j = p / n_cand, k = p - j * n_cand;
-            const uint32_t *rj = R + (size_t)j * sbr, *rk = R + (size_t)(n_cand + k) * sbr;
+            const uint32_t *rj = R + (size_t)j * sbp, *rk = R + (size_t)(n_cand + k) * sbp;
             unsigned long long acc = 0;
             if (cached) {
 #pragma unroll
@@ -664,7 +726,7 @@ __global__ void __launch_bounds__(kFinThreads, 1)
                 for (int s = lane; s < sbr; s += 32) {
                     uint32_t b = 0xffffffffu;
                     for (int gi = 0; gi < nbs; ++gi) {
-                        const uint32_t c = R[lev0[gi] * sbr + s] + R[(n_cand + lev1[gi]) * sbr + s];
+                        const uint32_t c = R[lev0[gi] * sbp + s] + R[(n_cand + lev1[gi]) * sbp + s];
                         b = c < b ? c : b;
                     }
                     const uint32_t c = rj[s] + rk[s];
@@ -781,7 +843,7 @@ __global__ void __launch_bounds__(kFinThreads, 1)
         int best_gi = 0;
         unsigned long long bst = ~0ull;
         for (int gi = 0; gi < bnb; ++gi) {
-            const unsigned long long c = (unsigned long long)R[blev[gi] * sbr + s] + R[(n_cand + blev[8 + gi]) * sbr + s];
+            const unsigned long long c = (unsigned long long)R[blev[gi] * sbp + s] + R[(n_cand + blev[8 + gi]) * sbp + s];
             if (c < bst) {
                 bst = c;
                 best_gi = gi;
@@ -1419,7 +1481,7 @@ __device__ void copy_block(const uint8_t *src, uint8_t *dst, int pw, int ph, int
 }
 
 __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const WorkItem *items, int nitems) {
-    __shared__ uint16_t reg[CR * CR];
+    __shared__ uint16_t reg[CR * CRP];
     __shared__ uint16_t regc[2][CRC * CRC];
     __shared__ int sdir[64], svar[64];
     __shared__ int dcost[64][8];
@@ -1457,10 +1519,10 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     const int damping = cp.damping + cs;
     const int cw = f.w / 2, ch = f.h / 2, cx0 = x0 / 2, cy0 = y0 / 2;
     // every plane's window staged at once (luma, then U and V)
-    load_region(f.B[0], bd, f.w, f.h, x0, y0, 64, reg);
+    load_region(f.B[0], bd, f.w, f.h, x0, y0, 64, reg, CRP);
     if (f.chroma)
 #pragma unroll 1
-        for (int p = 0; p < 2; ++p) load_region(f.B[p + 1], bd, cw, ch, cx0, cy0, 32, regc[p]);
+        for (int p = 0; p < 2; ++p) load_region(f.B[p + 1], bd, cw, ch, cx0, cy0, 32, regc[p], CRC);
     if (threadIdx.x == 0) {
         int n = 0;
         for (int b = 0; b < 64; ++b)
@@ -1471,7 +1533,7 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
     // directions: from this call's search of the same B when it ran (a
     // frame-uniform branch), else found here
     const bool have_dirs = f.cdir_ok != 0;
-    if (!have_dirs) find_dirs_ool(reg, CR, cs, blist, nblk, dcost, sdir, svar);
+    if (!have_dirs) find_dirs_ool(reg, CRP, cs, blist, nblk, dcost, sdir, svar);
     for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
         const int b = blist[k];
         int dir, t;
@@ -1483,7 +1545,7 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
             dir = sdir[b];
             t = adjust_strength(lvl_y, svar[b]);
         }
-        dir_offsets(lvl_y ? dir : 0, CR, boff[b]);
+        dir_offsets(lvl_y ? dir : 0, CRP, boff[b]);
         dir_offsets(lvl_uv ? dir : 0, CRC, boffc[b]);
         bt[b] = t | (damp_shift(t, damping) << 16);
     }
@@ -1500,7 +1562,7 @@ __global__ void __launch_bounds__(256) k_cdef_apply(FrameDesc *frames, const Wor
         const int b = h >> 1;
         const int py = (b >> 3) * 8 + (h & 1) * 4 + (lane >> 3), px = (b & 7) * 8 + (lane & 7);
         if (py >= vsize || px >= hsize) continue;
-        const int pos = (py + 2) * CR + px + 2;
+        const int pos = (py + 2) * CRP + px + 2;
         const int x = (int16_t)reg[pos];
         int y = x;
         if (!zero_y && ((dl >> b) & 1)) {
@@ -1720,11 +1782,12 @@ extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_de
     if (launch_cdef_search(d.cdef.first_pass_num, d.cdef.ncand / d.cdef.first_pass_num, nfb, st, &sc->desc,
                            &sc->item, 1) != cudaSuccess)
         return ZF_ERR_CUDA;
-    // pair partials (an inbox per rank) + compacted rows and ids: at most
-    // 51 + 42 KiB for ncand <= 20 and nfb <= 2048
+    // pair partials (an inbox per rank) + compacted rows (an odd column
+    // stride) and ids: at most 51 + 42 KiB for ncand <= 20 and nfb <= 2048
     const int np = d.cdef.ncand * d.cdef.ncand;
     const int CL = kFinCluster;
-    const int per_cta = (int)fin_pair_bytes(np, CL) + (nfb + CL - 1) / CL * (2 * d.cdef.ncand + 1) * 4;
+    const int rows = (nfb + CL - 1) / CL;
+    const int per_cta = (int)fin_pair_bytes(np, CL) + (rows + 1) * 2 * d.cdef.ncand * 4 + rows * 4;
     // raise the kernel's dynamic shared memory opt-in when this launch needs
     // more, never lower it: the attribute is per function and device, and a
     // context set it to its own cap at creation

@@ -29,6 +29,11 @@ namespace zf {
 constexpr int DB_T = 64;             // output tile edge
 constexpr int DB_H = 12;             // halo
 constexpr int DB_R = DB_T + 2 * DB_H;  // region edge (88)
+// Region row pitch in 2-byte samples: 45 words. In the vertical-edge pass a
+// warp filters 8 edges (2 words apart) x 4 lines of each; their 32 words
+// cannot all fall in distinct banks, and 45 words per row keep it at 2-way
+// (the region's own 44 words: up to 3-way). Rows stay 4-byte aligned.
+constexpr int DB_P = DB_R + 2;
 constexpr int DB_BANDS = DB_R / 4;   // 22 four-row bands in the region
 constexpr int DB_EDGES = 19;         // edges at tile origin -4 .. +68
 
@@ -245,7 +250,7 @@ __device__ void db_load(const DbTile &t, const uint8_t *plane, uint16_t *reg) {
                 const int i = i0 + j * blockDim.x;
                 const int ry = i / wpr, wx = i - ry * wpr;
                 const int y = t.y0 - DB_H + ry, x = t.x0 - DB_H + wx * spw;
-                off[j] = i < total ? ry * DB_R + wx * spw : -1;
+                off[j] = i < total ? ry * DB_P + wx * spw : -1;
                 v[j] = 0;
                 if (i < total && x >= 0 && x < t.pw && y >= 0 && y < t.ph) v[j] = *word_at(plane, (int64_t)y * t.pw + x, bd);
             }
@@ -260,7 +265,7 @@ __device__ void db_load(const DbTile &t, const uint8_t *plane, uint16_t *reg) {
         int y = t.y0 - DB_H + ry, x = t.x0 - DB_H + rx;
         int v = 0;
         if (x >= 0 && x < t.pw && y >= 0 && y < t.ph) v = ldpx(plane, (int64_t)y * t.pw + x, bd);
-        reg[i] = (uint16_t)v;
+        reg[ry * DB_P + rx] = (uint16_t)v;
     }
 }
 
@@ -269,11 +274,24 @@ __device__ void db_load(const DbTile &t, const uint8_t *plane, uint16_t *reg) {
 // rows, h[bucket][k] = column band * DB_EDGES + edge for horizontal edges
 // over the tile columns. Edges within a pass are independent, so each
 // bucket runs with every thread on one compile-time filter length.
+// Buckets 0 and 1 share one array (bucket 0 from the front, bucket 1 from
+// the back), buckets 2 and 3 another: a pass has at most one entry per
+// edge, so each pair fits. Horizontal entries are edge * 16 + column band:
+// listed band-minor, the 8 segments of a warp are 8 adjacent column bands
+// of one edge row (16 consecutive words: no bank conflict); listed
+// edge-minor they were rows 4 apart, 0 or 16 banks apart (4-way).
+constexpr int DB_NV = DB_BANDS * DB_EDGES, DB_NH = (DB_T / 4) * DB_EDGES;
 struct DbEdges {
-    uint16_t v[4][DB_BANDS * DB_EDGES];
-    uint16_t h[4][(DB_T / 4) * DB_EDGES];
+    uint16_t v[2][DB_NV];
+    uint16_t h[2][DB_NH];
     int nv[4], nh[4];
 };
+__device__ __forceinline__ uint16_t &edge_slot(uint16_t (*lists)[DB_NV], int bk, int k) {
+    return lists[bk >> 1][(bk & 1) ? DB_NV - 1 - k : k];
+}
+__device__ __forceinline__ uint16_t &edge_slot(uint16_t (*lists)[DB_NH], int bk, int k) {
+    return lists[bk >> 1][(bk & 1) ? DB_NH - 1 - k : k];
+}
 __device__ __forceinline__ int len_bucket(int len) { return len == 4 ? 0 : len == 6 ? 1 : len == 8 ? 2 : 3; }
 
 // Every thread of the CTA calls this; the lists are complete after the
@@ -289,17 +307,17 @@ __device__ void db_params(const DbTile &t, int lvl_v, int lvl_h, DbEdges &E) {
         if (y >= 0 && y < t.ph && x >= 0 && x < t.pw) len = edge_len(f, true, x, y, t.plane, lvl_v);
         if (len) {
             const int bk = len_bucket(len);
-            E.v[bk][atomicAdd(&E.nv[bk], 1)] = (uint16_t)i;
+            edge_slot(E.v, bk, atomicAdd(&E.nv[bk], 1)) = (uint16_t)i;
         }
     }
-    for (int i = threadIdx.x; i < (DB_T / 4) * DB_EDGES; i += blockDim.x) {
-        int cb = i / DB_EDGES, e = i - cb * DB_EDGES;
+    for (int i = threadIdx.x; i < DB_NH; i += blockDim.x) {
+        int e = i >> 4, cb = i & 15;
         int x = t.x0 + cb * 4, y = t.y0 - 4 + e * 4;
         int len = 0;
         if (y >= 0 && y < t.ph && x >= 0 && x < t.pw) len = edge_len(f, false, x, y, t.plane, lvl_h);
         if (len) {
             const int bk = len_bucket(len);
-            E.h[bk][atomicAdd(&E.nh[bk], 1)] = (uint16_t)i;
+            edge_slot(E.h, bk, atomicAdd(&E.nh[bk], 1)) = (uint16_t)i;
         }
     }
 }
@@ -319,18 +337,18 @@ __device__ void db_filter(const DbTile &t, uint16_t *reg, const DbEdges &E, int 
     const Thr tv = lf_thresholds(lvl_v, sharp), th = lf_thresholds(lvl_h, sharp);
     for (int bk = 0; bk < 4; ++bk)
         for (int i = threadIdx.x; i < E.nv[bk] * 4; i += blockDim.x) {
-            const int be = E.v[bk][i >> 2], line = i & 3;
+            const int be = edge_slot(const_cast<uint16_t (*)[DB_NV]>(E.v), bk, i >> 2), line = i & 3;
             const int band = be / DB_EDGES, e = be - band * DB_EDGES;
             const int ry = band * 4 + line, rx = DB_H - 4 + e * 4;
-            filter_bucket(bk, reg + ry * DB_R + rx, 1, tv, bd);
+            filter_bucket(bk, reg + ry * DB_P + rx, 1, tv, bd);
         }
     __syncthreads();
     for (int bk = 0; bk < 4; ++bk)
         for (int i = threadIdx.x; i < E.nh[bk] * 4; i += blockDim.x) {
-            const int be = E.h[bk][i >> 2], line = i & 3;
-            const int cb = be / DB_EDGES, e = be - cb * DB_EDGES;
+            const int be = edge_slot(const_cast<uint16_t (*)[DB_NH]>(E.h), bk, i >> 2), line = i & 3;
+            const int e = be >> 4, cb = be & 15;
             const int rx = DB_H + cb * 4 + line, ry = DB_H - 4 + e * 4;
-            filter_bucket(bk, reg + ry * DB_R + rx, DB_R, th, bd);
+            filter_bucket(bk, reg + ry * DB_P + rx, DB_P, th, bd);
         }
     __syncthreads();
 }
@@ -344,7 +362,7 @@ __device__ __forceinline__ void plane_geom(const FrameDesc &f, int plane, int *p
 // (deblock.rs:951-967): both luma levels zero disables every plane; a chroma
 // plane needs its own level.
 __global__ void __launch_bounds__(256, 5) k_deblock_apply(const FrameDesc *frames, const WorkItem *items, int nitems) {
-    __shared__ __align__(16) uint16_t reg[DB_R * DB_R];
+    __shared__ __align__(16) uint16_t reg[DB_R * DB_P];
     __shared__ DbEdges edges;
     const int it = find_item(items, nitems, blockIdx.x);
     const WorkItem wi = items[it];
@@ -398,14 +416,14 @@ __global__ void __launch_bounds__(256, 5) k_deblock_apply(const FrameDesc *frame
             const int y = t.y0 + ty, x = t.x0 + wx * spw;
             if (x < pw && y < ph)
                 *const_cast<uint32_t *>(word_at(f.B[plane], (int64_t)y * pw + x, bd)) =
-                    pack_word(reg + (ty + DB_H) * DB_R + DB_H + wx * spw, bd);
+                    pack_word(reg + (ty + DB_H) * DB_P + DB_H + wx * spw, bd);
         }
         return;
     }
     for (int i = threadIdx.x; i < DB_T * DB_T; i += blockDim.x) {
         int ty = i / DB_T, tx = i % DB_T;
         int y = t.y0 + ty, x = t.x0 + tx;
-        if (x < pw && y < ph) stpx(f.B[plane], (int64_t)y * pw + x, bd, reg[(ty + DB_H) * DB_R + tx + DB_H]);
+        if (x < pw && y < ph) stpx(f.B[plane], (int64_t)y * pw + x, bd, reg[(ty + DB_H) * DB_P + tx + DB_H]);
     }
 }
 
@@ -417,8 +435,8 @@ __global__ void __launch_bounds__(256, 5) k_deblock_apply(const FrameDesc *frame
 // sse[slot * nl + k] the SSE accumulated for it.
 __global__ void __launch_bounds__(256, 5) k_deblock_sse(const FrameDesc *frames, const WorkItem *items, int nitems,
                                                      const int *levels, int nl, unsigned long long *sse) {
-    __shared__ __align__(16) uint16_t reg[DB_R * DB_R];
-    __shared__ __align__(16) uint16_t pristine[DB_R * DB_R];
+    __shared__ __align__(16) uint16_t reg[DB_R * DB_P];
+    __shared__ __align__(16) uint16_t pristine[DB_R * DB_P];
     __shared__ __align__(16) uint16_t srct[DB_T * DB_T];  // the source tile, staged once for every level
     __shared__ DbEdges edges;
     __shared__ unsigned long long part[8];
@@ -460,7 +478,7 @@ __global__ void __launch_bounds__(256, 5) k_deblock_sse(const FrameDesc *frames,
     for (int k = 0; k < nl; ++k) {
         const int lvl = levels[slot * nl + k];
         if (lvl < 0) continue;
-        for (int i = threadIdx.x; i < DB_R * DB_R / 2; i += blockDim.x)
+        for (int i = threadIdx.x; i < DB_R * DB_P / 2; i += blockDim.x)
             reinterpret_cast<uint32_t *>(reg)[i] = reinterpret_cast<const uint32_t *>(pristine)[i];
         __syncthreads();
         if (lvl != 0) db_filter(t, reg, edges, lvl, lvl);
@@ -469,7 +487,7 @@ __global__ void __launch_bounds__(256, 5) k_deblock_sse(const FrameDesc *frames,
             const int ty = i >> 5, px = i & 31;
             if (ty < rows && px < pairs) {
                 const uint32_t sv = reinterpret_cast<const uint32_t *>(srct + ty * DB_T)[px];
-                const uint32_t rv = reinterpret_cast<const uint32_t *>(reg + (ty + DB_H) * DB_R + DB_H)[px];
+                const uint32_t rv = reinterpret_cast<const uint32_t *>(reg + (ty + DB_H) * DB_P + DB_H)[px];
                 const int d0 = (int)(sv & 0xffffu) - (int)(rv & 0xffffu), d1 = (int)(sv >> 16) - (int)(rv >> 16);
                 acc += (unsigned long long)(uint32_t)(d0 * d0 + d1 * d1);
             }

@@ -1287,9 +1287,22 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 const int m = s.hc.needs(need);
                 if (m == 0) continue;
                 // four levels in each of a climb's first two launches (most
-                // climbs end within them), ctx->db_levels in later ones
+                // climbs end within them), ctx->db_levels in later ones. A
+                // refining climb (conv_th != 1) on a plane of >= 512 tiles
+                // takes at most two levels a launch: it converges through
+                // half and quarter steps, so deeper speculation is wasted as
+                // often as not, and there a level costs about as much as the
+                // host round trip it may save (a 4096x3072 10-bit preset-2
+                // frame: 3.65 ms at two levels a launch, 4.0 ms at eight;
+                // a 4K climb that only continues upwards, conv_th 1, gains
+                // from eight: 1.22 against 1.45 ms).
+                const Plan &sp = plans[s.frame];
+                const int spw = s.plane ? sp.d.w / 2 : sp.d.w, sph = s.plane ? sp.d.h / 2 : sp.d.h;
+                const bool big = ((spw + 63) / 64) * ((sph + 63) / 64) >= 512;
+                int cap = s.launches < 2 ? std::min(4, ctx->db_levels) : ctx->db_levels;
+                if (s.hc.conv_th != 1 && big) cap = std::min(cap, 2);
                 TrialSlot t{s.frame, s.plane, {}, {}};
-                speculate(s.hc, need, m, s.launches < 2 ? std::min(4, ctx->db_levels) : ctx->db_levels, t.levels);
+                speculate(s.hc, need, m, cap, t.levels);
                 s.launches++;
                 ts.push_back(t);
                 owner.push_back((int)k);
@@ -1422,7 +1435,9 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                     const size_t nc = (size_t)plans[fi].d.cdef.ncand, np = nc * nc;
                     const size_t pb = zf::fin_pair_bytes((int)np, cl);
                     pairs = std::max(pairs, pb);
-                    want = std::max(want, pb + ((size_t)plans[fi].nfb + cl - 1) / cl * (2 * nc + 1) * 4);
+                    // rows (+ one padding row per column: the odd stride) and ids
+                    const size_t rows = ((size_t)plans[fi].nfb + cl - 1) / cl;
+                    want = std::max(want, pb + (rows + 1) * 2 * nc * 4 + rows * 4);
                 }
                 return std::max(pairs, std::min<size_t>(want, kFinishSmemCap));
             };

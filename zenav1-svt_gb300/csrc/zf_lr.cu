@@ -1071,14 +1071,30 @@ __device__ int64_t trial_sse(const FrameDesc &f, const UnitRect &r, const Taps &
                 const uint2 sv = *reinterpret_cast<const uint2 *>(srct + rr * TT_W + c0);
                 const int sx[4] = {lo(sv.x), hi(sv.x), lo(sv.y), hi(sv.y)};
                 const int i = ty + rr, nq = min(4, tw - c0);
+                // the four columns share their sse_region part unless the
+                // right strip starts inside them (a unit width not a
+                // multiple of 4)
+                const int xc = tx + c0, xr = uw - dw;
+                uint32_t e2s = 0;
+                if (xc + nq <= xr || xc >= xr) {
 #pragma unroll
-                for (int jj = 0; jj < 4; ++jj) {
-                    if (jj >= nq) break;
-                    const int e = sx[jj] - y[jj];
-                    const uint32_t e2 = (uint32_t)(e * e);
-                    if (tx + c0 + jj >= uw - dw) rgt += e2;
-                    else if (i >= uh - dh) bot += e2;
-                    else blk += e2;
+                    for (int jj = 0; jj < 4; ++jj) {
+                        const int e = sx[jj] - y[jj];
+                        e2s += jj < nq ? (uint32_t)(e * e) : 0u;
+                    }
+                    if (xc >= xr) rgt += e2s;
+                    else if (i >= uh - dh) bot += e2s;
+                    else blk += e2s;
+                } else {
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) {
+                        if (jj >= nq) break;
+                        const int e = sx[jj] - y[jj];
+                        const uint32_t e2 = (uint32_t)(e * e);
+                        if (xc + jj >= xr) rgt += e2;
+                        else if (i >= uh - dh) bot += e2;
+                        else blk += e2;
+                    }
                 }
             }
         }
@@ -1447,14 +1463,29 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
             const uint2 sv = *reinterpret_cast<const uint2 *>(srct + rr * TL + c0);
             const int sx[4] = {lo(sv.x), hi(sv.x), lo(sv.y), hi(sv.y)};
             const bool bottom = (bottom_rows >> rr) & 1;
+            // the four columns share their sse_region part unless the right
+            // strip starts inside them (a unit width not a multiple of 4)
+            const int xc = tx + c0, xr = uw - dw;
+            if (xc + nq <= xr || xc >= xr) {
+                uint32_t e2s = 0;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                if (j >= nq) break;
-                const int e = sx[j] - y[j];
-                const uint32_t e2 = (uint32_t)(e * e);
-                if (tx + c0 + j >= uw - dw) rgt32 += e2;
-                else if (bottom) bot32 += e2;
-                else blk32 += e2;
+                for (int j = 0; j < 4; ++j) {
+                    const int e = sx[j] - y[j];
+                    e2s += j < nq ? (uint32_t)(e * e) : 0u;
+                }
+                if (xc >= xr) rgt32 += e2s;
+                else if (bottom) bot32 += e2s;
+                else blk32 += e2s;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (j >= nq) break;
+                    const int e = sx[j] - y[j];
+                    const uint32_t e2 = (uint32_t)(e * e);
+                    if (xc + j >= xr) rgt32 += e2;
+                    else if (bottom) bot32 += e2;
+                    else blk32 += e2;
+                }
             }
         }
     };
