@@ -251,17 +251,23 @@ def kernel_bytes(name, w, h, px):
 
 
 # DRAM bytes (read + write) per luma pixel of one launch, from one ncu
-# capture of each kernel on a 3840x2160 8-bit preset-6 frame (the committed
-# summary of the top kernels' captures); the roofline's `traffic` scales
-# them to the launch's frame.
+# capture of each kernel's first launch in the bench's profile run (the
+# 3840x2160 8-bit preset-4 qp-24 frame; the committed summary of the top
+# kernels' captures); the roofline's `traffic` scales them to the launch's
+# frame. The level trials' launches cover one plane kind each, so theirs is
+# DRAM bytes per algorithmic byte of the captured launch (luma slot, four
+# levels), scaled by the library's byte count of the average launch.
 KERNEL_DRAM_BYTES_PER_PX = {
-    "k_cdef_apply": 14.070016e6 / (3840 * 2160),
-    "k_cdef_search": 26.51392e6 / (3840 * 2160),
-    "k_lr_stats5": (25.926912e6 + 256.0) / (3840 * 2160),
+    "k_cdef_apply": 14.181376e6 / (3840 * 2160),
+    "k_cdef_search": 26.4896e6 / (3840 * 2160),
+    "k_lr_stats5": 25.799424e6 / (3840 * 2160),
     "k_cdef_finish": 0.19712e6 / (3840 * 2160),
-    "k_deblock_apply": 14.565888e6 / (3840 * 2160),
-    "k_lr_trial_tiles": (25.97632e6 + 6144.0) / (3840 * 2160),
+    "k_deblock_apply": 14.568448e6 / (3840 * 2160),
+    "k_lr_trial_tiles": (26.008064e6 + 2560.0) / (3840 * 2160),
     "k_lr_apply": 0.049664e6 / (3840 * 2160),
+}
+KERNEL_DRAM_PER_ALGO_BYTE = {
+    "k_deblock_sse": 18.717952e6 / (2 * 3840 * 2160),
 }
 
 
@@ -445,7 +451,8 @@ def run_ours(args):
     ctx.profile_reset()
     step_device()
     ctx.sync()
-    prof = ctx.profile_read()
+    prof_b = ctx.profile_read_bytes()
+    prof = {k: v[:2] for k, v in prof_b.items()}
     ctx.profile(False)
     # the dominant kernel among those that stream planes (the joint strength
     # search reads only the mse rows and is latency bound: it is listed in
@@ -454,7 +461,12 @@ def run_ours(args):
     top = max(streaming.items(), key=lambda kv: kv[1][1]) if streaming else ("none", (1, 0.0))
     name, (nl, tot_ms) = top
     per_launch_ms = tot_ms / max(nl, 1)
-    bytes_per_launch = np.mean([kernel_bytes(name, f.w, f.h, 1) for f in frames])
+    # the library's own count where it records one (the level trials: each
+    # launch reads the slots' planes and source planes once), else the
+    # kernel's whole-frame formula
+    lib_bytes = prof_b.get(name, (0, 0.0, 0))[2]
+    bytes_per_launch = (lib_bytes / max(nl, 1) if lib_bytes
+                        else np.mean([kernel_bytes(name, f.w, f.h, 1) for f in frames]))
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -463,12 +475,18 @@ def run_ours(args):
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9 if per_launch_ms > 0 else 0.0
     bpp = KERNEL_DRAM_BYTES_PER_PX.get(name)
-    traffic = int(bpp * np.mean([f.luma_px for f in frames])) if bpp else None
+    if name in KERNEL_DRAM_PER_ALGO_BYTE:
+        traffic = int(KERNEL_DRAM_PER_ALGO_BYTE[name] * bytes_per_launch)
+        traffic_source = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one luma trial launch of a "
+                          "3840x2160 frame, per algorithmic byte, times the average launch's algorithmic bytes")
+    else:
+        traffic = int(bpp * np.mean([f.luma_px for f in frames])) if bpp else None
+        traffic_source = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one 4K launch, scaled by luma "
+                          "pixels") if traffic else None
     roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": traffic,
                 "algorithmic_bytes": int(bytes_per_launch),
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 4K preset-6 launch, "
-                                  "scaled by luma pixels" if traffic else None,
+                "traffic_source": traffic_source,
                 "peak_source": "of measured" if "hbm_gbs" in peaks else "of fallback",
                 "stage_bytes_per_px": 4.75,
                 "stage_frac": round((4.75 * px_step / (ms / 1e3) / 1e9) / peak, 5)}

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define ZF_ABI_VERSION 1
+#define ZF_ABI_VERSION 2
 
 enum {
     ZF_OK = 0,
@@ -498,6 +498,9 @@ typedef struct zf_kernel_time {
     char name[32];
     uint64_t launches;
     double total_ms;            /* CUDA-event time on the context's stream */
+    uint64_t bytes;             /* algorithmic bytes of the launches (planes read and
+                                   written once), where the library records them
+                                   (the deblock level trials); else 0 */
 } zf_kernel_time;
 
 /* CUDA graphs (no counterpart in the reference). enable != 0: every

@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol(pkg):
     assert len(syms) >= 14
     for s in syms:
         assert hasattr(L, s), s
-    assert L.zf_abi_version() == 1
+    assert L.zf_abi_version() == 2
 
 
 def test_pack_geom_roundtrip_and_rejects_misaligned(pkg):

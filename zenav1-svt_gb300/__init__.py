@@ -255,9 +255,13 @@ class Context:
 
     def profile_read(self):
         """{kernel name: (launches, total_ms)} measured with CUDA events."""
+        return {k: v[:2] for k, v in self.profile_read_bytes().items()}
+
+    def profile_read_bytes(self):
+        """{kernel name: (launches, total_ms, algorithmic bytes or 0)}."""
         buf = (abi.ZfKernelTime * 64)()
         n = lib().zf_profile_read(self.h, buf, 64)
-        return {buf[i].name.decode(): (buf[i].launches, buf[i].total_ms) for i in range(min(n, 64))}
+        return {buf[i].name.decode(): (buf[i].launches, buf[i].total_ms, buf[i].bytes) for i in range(min(n, 64))}
 
     def filter_stage_raw(self, s, dec, st):
         """zf_filter_stage on a prepared zf_frame / Decisions / ZfStats."""

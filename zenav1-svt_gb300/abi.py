@@ -117,7 +117,7 @@ SGR_UNIT = np.dtype([("set", np.int32), ("w0", np.int32), ("w1", np.int32), ("pa
 
 
 class ZfKernelTime(C.Structure):
-    _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double)]
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double), ("bytes", C.c_uint64)]
 
 
 def ptr(a):

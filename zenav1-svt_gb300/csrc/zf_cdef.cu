@@ -228,9 +228,14 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v
 // msb(threshold)) (cdef.rs:113-120); threshold 0 gives 0 for any shift.
 // sign(d) * min(|d|, m) with m = max(0, thr - (|d| >> shift)) >= 0 is d
 // clamped to [-m, m].
+//
+// Computed as sign(d) * max(0, min(|d|, thr - (|d| >> shift))) -- the same
+// value, since |d| >= 0 -- whose clamp is one three-operand min-with-zero
+// (a DPX instruction) instead of three two-operand min/max.
 __device__ __forceinline__ int constrain_s(int d, int thr, int shift) {
-    const int m = max(0, thr - (abs(d) >> shift));
-    return min(max(d, -m), m);
+    const int a = abs(d);
+    const int r = __vimin_s32_relu(a, thr - (a >> shift));
+    return d < 0 ? -r : r;
 }
 __device__ __forceinline__ int damp_shift(int thr, int damping) {
     return thr ? max(0, damping - msb((unsigned)thr)) : 0;
@@ -263,13 +268,29 @@ __device__ __forceinline__ void load_taps(const uint16_t *reg, int pos, const in
     q[0] = pos + o[0]; q[1] = pos - o[0]; q[2] = pos + o[1]; q[3] = pos - o[1];
     q[4] = pos + o[2]; q[5] = pos - o[2]; q[6] = pos + o[4]; q[7] = pos - o[4];
     q[8] = pos + o[3]; q[9] = pos - o[3]; q[10] = pos + o[5]; q[11] = pos - o[5];
+    if constexpr (EDGE) {
 #pragma unroll
-    for (int t = 0; t < 12; ++t) {
-        const uint16_t r = reg[q[t]];
-        const int v = (int16_t)r;
-        if (!EDGE || r != kVeryLarge) mx = max(mx, v);
-        mn = min(mn, v);
-        d[t] = v - x;
+        for (int t = 0; t < 12; ++t) {
+            const uint16_t r = reg[q[t]];
+            const int v = (int16_t)r;
+            if (r != kVeryLarge) mx = max(mx, v);
+            mn = min(mn, v);
+            d[t] = v - x;
+        }
+    } else {
+        // no sentinel: the 13 values' max and min by three-operand DPX
+        // min/max, two taps per instruction
+        int v[12];
+#pragma unroll
+        for (int t = 0; t < 12; ++t) {
+            v[t] = (int16_t)reg[q[t]];
+            d[t] = v[t] - x;
+        }
+#pragma unroll
+        for (int t = 0; t < 12; t += 2) {
+            mx = __vimax3_s32(mx, v[t], v[t + 1]);
+            mn = __vimin3_s32(mn, v[t], v[t + 1]);
+        }
     }
 }
 

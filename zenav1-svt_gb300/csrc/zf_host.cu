@@ -46,6 +46,7 @@ struct zf_ctx {
     struct Pending {
         const char *name;
         cudaEvent_t a, b;
+        uint64_t bytes;
     };
     std::vector<Pending> pending;
     std::vector<zf_kernel_time> totals;
@@ -78,8 +79,9 @@ namespace {
 struct LaunchScope {
     zf_ctx *ctx;
     const char *name;
+    uint64_t bytes;  // algorithmic bytes of the launch, 0 when not recorded
     cudaEvent_t a = nullptr, b = nullptr;
-    LaunchScope(zf_ctx *c, const char *n) : ctx(c), name(n) {
+    LaunchScope(zf_ctx *c, const char *n, uint64_t nbytes = 0) : ctx(c), name(n), bytes(nbytes) {
         ctx->launches++;
         if (ctx->profiling && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess)
             cudaEventRecord(a, ctx->stream);
@@ -87,7 +89,7 @@ struct LaunchScope {
     ~LaunchScope() {
         if (a && b) {
             cudaEventRecord(b, ctx->stream);
-            ctx->pending.push_back({name, a, b});
+            ctx->pending.push_back({name, a, b, bytes});
         }
     }
 };
@@ -110,6 +112,7 @@ void collect_profile(zf_ctx *ctx) {
         }
         t->launches += 1;
         t->total_ms += ms;
+        t->bytes += p.bytes;
     }
     ctx->pending.clear();
 }
@@ -1194,11 +1197,13 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     auto run_trials = [&](std::vector<TrialSlot> &ts) -> int {
         WorkList wl;
         std::vector<int> lv(ts.size() * zf::kDbLevels, -1);
+        uint64_t nbytes = 0;  // each slot's plane and source plane, read once
         for (size_t k = 0; k < ts.size(); ++k) {
             const Plan &p = plans[ts[k].frame];
             for (size_t j = 0; j < ts[k].levels.size(); ++j) lv[k * zf::kDbLevels + j] = ts[k].levels[j];
             const int pw = ts[k].plane ? p.d.w / 2 : p.d.w, ph = ts[k].plane ? p.d.h / 2 : p.d.h;
             wl.add(ts[k].frame, ts[k].plane, (int)k, 0, ((pw + 63) / 64) * ((ph + 63) / 64));
+            nbytes += 2ull * pw * ph * p.px;
         }
         if (ts.size() > db_slots) return fail(ctx, ZF_ERR_UNSUPPORTED, "too many search slots");
         std::vector<uint8_t> wl_img(wl.bytes());
@@ -1206,7 +1211,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         CU(cudaMemcpyAsync(base + o_dbs_items, wl_img.data(), wl_img.size(), cudaMemcpyHostToDevice, st));
         CU(cudaMemcpyAsync(base + o_dbs_lv, lv.data(), lv.size() * 4, cudaMemcpyHostToDevice, st));
         CU(cudaMemsetAsync(base + o_dbs_sse, 0, lv.size() * 8, st));
-        { LaunchScope ls_(ctx, "k_deblock_sse");
+        { LaunchScope ls_(ctx, "k_deblock_sse", nbytes);
         zf::k_deblock_sse<<<wl.ctas, 256, 0, st>>>(d_desc, (const WorkItem *)(base + o_dbs_items),
                                                    (int)wl.items.size(), (const int *)(base + o_dbs_lv),
                                                    zf::kDbLevels, (unsigned long long *)(base + o_dbs_sse)); }
