@@ -4,13 +4,15 @@ Workload (N=1): the plain per-image 4K configuration -- four 3840x2160
 8-bit 4:2:0 stills, presets {4, 6} x qp {24, 40}, seeded synthetic content
 and stage inputs (zenav1-svt_gb300/synth.py). One step = the four frames,
 each through zf_filter_stage (deblock pick + apply, CDEF search + apply,
-Wiener search + apply).
+Wiener search + apply), on two contexts (two streams) driven by two host
+threads, the frames alternating between them.
 
-  value  MPix/s with inputs resident in HBM (device pointers), CUDA-event
-         timed on the library stream, L2 flushed between steps.
+  value  MPix/s with inputs resident in HBM (device pointers), timed by CUDA
+         events that bracket both streams, L2 flushed between steps.
   e2e    the same through the C ABI with pinned HOST buffers (H2D of source,
          recon and geometry, D2H of the filtered recon and decisions inside
          the timed region).
+  single_context  both, on one context, frame after frame.
 
 More keys on the same line (N=1 only):
   highres_10bit  one 4096x3072 10-bit preset-2 frame per step (u16 planes,
@@ -31,8 +33,9 @@ More keys on the same line (N=1 only):
            and served MPix/s per rate.
 
 --impl reference times the reference algorithm on the host cores: the
-Rust reference cannot be built here, so this is the C++ oracle port, one
-thread per frame, on a bounded sample of the same workload.
+Rust reference cannot be built here, so this is the C++ oracle port on the
+same four frames, as many copies of each at once as fill the host's cores,
+one thread per copy.
 """
 import argparse
 import json
@@ -169,6 +172,8 @@ def ours_config(nframes, world=1):
     return {"workload": "plain per-image 3840x2160 8-bit 4:2:0, presets {4,6} x qp {24,40}",
             "frames_per_step": nframes,
             "l2": "GPU arm: flushed between steps (256 MB write); CPU arm: not applicable",
+            "concurrency": "GPU arm: two contexts (two streams) on two host threads, frames alternating; "
+                           "CPU arm: one host thread per frame copy",
             "parallelism": "replicas" if world > 1 else "single"}
 
 
@@ -280,12 +285,12 @@ KERNEL_DRAM_PER_ALGO_BYTE = {
 # times of the same step) against the issue peak, four warp instructions
 # per clock per SM at the SM clock sampled during the timed region.
 KERNEL_WARP_INST_PER_PX = {
-    "k_deblock_sse": 18.1571,
-    "k_deblock_apply": 5.3884,
-    "k_cdef_search": 11.9243,
-    "k_cdef_apply": 5.8323,
-    "k_lr_stats5": 5.8570,
-    "k_lr_trial_tiles": 8.2514,
+    "k_deblock_sse": 18.2232,
+    "k_deblock_apply": 5.3854,
+    "k_cdef_search": 12.0090,
+    "k_cdef_apply": 5.7870,
+    "k_lr_stats5": 5.8569,
+    "k_lr_trial_tiles": 7.9187,
 }
 
 
@@ -309,6 +314,38 @@ def issue_roofline(prof, frames, sm_count, sm_mhz):
             % (sm_count, sm_mhz), "kernels": out}
 
 
+def run_concurrent(ctxs, streams, work):
+    """One step of the plain path on several contexts at once: host thread k
+    runs work[k] (a list of (zf_frame, Decisions, ZfStats)) through
+    zf_filter_stage on ctxs[k]. Device time from an event on streams[0]
+    before any launch (the other streams wait on it) to an event on
+    streams[0] after every stream's last launch (it waits on theirs), in
+    ms."""
+    import threading
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(streams[0])
+    for st in streams[1:]:
+        st.wait_event(e0)
+
+    def worker(k):
+        for s, d, stt in work[k]:
+            ctxs[k].filter_stage_raw(s, d, stt)
+
+    ths = [threading.Thread(target=worker, args=(k,)) for k in range(len(ctxs))]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    for st in streams[1:]:
+        ev = torch.cuda.Event()
+        ev.record(st)
+        streams[0].wait_event(ev)
+    e1.record(streams[0])
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
 def run_ours(args):
     import torch
     rank, world, local = env_rank()
@@ -325,6 +362,12 @@ def run_ours(args):
     ctx = pkg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream_handle(), device=torch.device("cuda", local))
     dev = torch.device("cuda", local)
+    # the step runs on two contexts (two streams) from two host threads, the
+    # frames alternating, so one frame's copies, host round trips and
+    # few-CTA passes overlap the other's streaming kernels
+    ctx2 = pkg.Context(local)
+    stream2 = torch.cuda.ExternalStream(ctx2.stream_handle(), device=dev)
+    ctxs, streams = [ctx, ctx2], [stream, stream2]
 
     # device-resident inputs + a pristine copy of each recon
     d_src, d_rec, d_rec0, d_mi, structs, decs, stats = [], [], [], [], [], [], []
@@ -355,32 +398,44 @@ def run_ours(args):
         for s, d, st in zip(structs, decs, stats):
             ctx.filter_stage_raw(s, d, st)
 
+    def split(items):  # frames alternate between the two contexts
+        return [items[0::2], items[1::2]]
+
+    dev_work = split(list(zip(structs, decs, stats)))
+
     # correctness of the timed configuration: device run == oracle on frame 0
     # is covered by the -m gpu tests; here only the determinism across steps.
     for _ in range(args.warmup):
         restore()
-        step_device()
+        run_concurrent(ctxs, streams, dev_work)
     if world > 1:
         torch.distributed.barrier()
     clocks = ClockSampler(local)
     clocks.start()
-    launches0 = ctx.launch_count()
+    launches0 = ctx.launch_count() + ctx2.launch_count()
     times = []
     torch.cuda.synchronize()
     for _ in range(args.steps):
+        restore()
+        times.append(run_concurrent(ctxs, streams, dev_work))
+    torch.cuda.synchronize()
+    launches = ctx.launch_count() + ctx2.launch_count() - launches0
+    clk = clocks.stop()
+    px_step = sum(f.luma_px for f in frames)
+    ms = float(np.mean(times))
+    t_max = replicas.max_over_ranks(ms, device=dev)  # replicas: the slowest rank's time
+    # the same step on one context, frame after frame
+    single = []
+    for k in range(args.warmup + args.steps):
         restore()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         step_device()
         e1.record(stream)
         e1.synchronize()
-        times.append(e0.elapsed_time(e1))
-    torch.cuda.synchronize()
-    launches = ctx.launch_count() - launches0
-    clk = clocks.stop()
-    px_step = sum(f.luma_px for f in frames)
-    ms = float(np.mean(times))
-    t_max = replicas.max_over_ranks(ms, device=dev)  # replicas: the slowest rank's time
+        if k >= args.warmup:
+            single.append(e0.elapsed_time(e1))
+    single_ms = float(np.mean(single))
 
     # the same step with each call's launches run as a CUDA graph (not the
     # headline: a comparison of the two launch modes)
@@ -397,7 +452,7 @@ def run_ours(args):
             g_times.append(e0.elapsed_time(e1))
     g_stats = ctx.graph_stats()
     ctx.use_graphs(False)
-    graphs = {"ms_per_step": round(float(np.mean(g_times)), 3), "direct_ms_per_step": round(ms, 3),
+    graphs = {"ms_per_step": round(float(np.mean(g_times)), 3), "direct_ms_per_step": round(single_ms, 3),
               "graph_launches": int(g_stats[0]), "updates": int(g_stats[1]), "instantiations": int(g_stats[2])}
     value = replicas.job_rate(px_step, world, t_max / 1e3) / 1e6
 
@@ -428,12 +483,19 @@ def run_ours(args):
         flush.fill_(1)
         torch.cuda.synchronize()
 
+    host_work = split(list(zip(e_structs, decs, stats)))
     for _ in range(args.warmup):
         restore_host()
-        for s, d, st in zip(e_structs, decs, stats):
-            ctx.filter_stage_raw(s, d, st)
+        run_concurrent(ctxs, streams, host_work)
     e_times = []
     for _ in range(args.steps):
+        restore_host()
+        e_times.append(run_concurrent(ctxs, streams, host_work))
+    e_ms = replicas.max_over_ranks(float(np.mean(e_times)), device=dev)
+    e2e = replicas.job_rate(px_step, world, e_ms / 1e3) / 1e6
+    # one context, frame after frame
+    e_single = []
+    for k in range(args.warmup + args.steps):
         restore_host()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -441,9 +503,9 @@ def run_ours(args):
             ctx.filter_stage_raw(s, d, st)
         e1.record(stream)
         e1.synchronize()
-        e_times.append(e0.elapsed_time(e1))
-    e_ms = replicas.max_over_ranks(float(np.mean(e_times)), device=dev)
-    e2e = replicas.job_rate(px_step, world, e_ms / 1e3) / 1e6
+        if k >= args.warmup:
+            e_single.append(e0.elapsed_time(e1))
+    e_single_ms = float(np.mean(e_single))
 
     # per-kernel device times (separate profiled pass, CUDA events per launch)
     restore()
@@ -500,6 +562,10 @@ def run_ours(args):
                 "e2e": {"value": round(e2e, 3), "unit": "MPix/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e_ms, 3)},
                 "gpu_launches": int(launches),
+                "single_context": {"ms_per_step": round(single_ms, 3),
+                                   "value": round(px_step / (single_ms / 1e3) / 1e6, 3),
+                                   "e2e_ms_per_step": round(e_single_ms, 3),
+                                   "e2e_value": round(px_step / (e_single_ms / 1e3) / 1e6, 3)},
                 "roofline": roofline, "kernels": kernels, "clocks": clk, "graphs": graphs}
         sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
         ir = issue_roofline(prof, frames, sm_count, clk.get("sm_mhz"))
@@ -522,6 +588,7 @@ def run_ours(args):
             line["served"] = run_served(args, local, gen_frames(served_jobs(32)))
         print(json.dumps(line))
     ctx.close()
+    ctx2.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
