@@ -1009,6 +1009,12 @@ def run_served(args, device, frames):
         for k in range(len(pool)):
             srv.submit(request(k))
         srv.drain(timeout=600)
+    # pinned recon slots for requests that overlap on one pool image, made
+    # here: a page-locked allocation inside a measured window stalls it
+    for e in pool:
+        while len(e["slots"]) < 4:
+            e["slots"].append({"rec": [torch.from_numpy(p.copy()).pin_memory().numpy() for p in e["rec0"]],
+                               "req": None})
     out = {}
     import gc
     for rate in args.served_rates:

@@ -156,8 +156,9 @@ uint64_t zf_device_bytes(const zf_ctx *ctx);
  * call allocates again. No counterpart in the reference. */
 int32_t zf_trim(zf_ctx *ctx);
 /* Grow the arena to at least device_bytes and each pinned host staging
- * buffer (metadata up, decisions down) to at least host_bytes now, so that
- * later calls up to that size allocate nothing (allocation and release
+ * buffer (metadata up, decisions down) to at least host_bytes now, and the
+ * gathered host-plane copies' job lists to 400 frames' worth, so that later
+ * calls up to that size allocate nothing (allocation and release
  * synchronise the device). No counterpart in the reference. */
 int32_t zf_reserve(zf_ctx *ctx, uint64_t device_bytes, uint64_t host_bytes);
 

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libzf.so")
-SOURCES = ["zf_deblock.cu", "zf_cdef.cu", "zf_lr.cu", "zf_lr_tc.cu", "zf_sgr.cu", "zf_post.cu", "zf_host.cu", "zf_syntax.cpp"]
+SOURCES = ["zf_deblock.cu", "zf_cdef.cu", "zf_lr.cu", "zf_lr_tc.cu", "zf_sgr.cu", "zf_post.cu", "zf_copy.cu", "zf_host.cu", "zf_syntax.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -55,6 +55,9 @@ struct zf_ctx {
     // in one copy
     uint8_t *h_meta = nullptr, *h_out = nullptr;
     size_t h_meta_cap = 0, h_out_cap = 0;
+    // job lists of the gathered host-plane copies (pinned up, device side)
+    uint8_t *h_jobs = nullptr, *d_jobs = nullptr;
+    size_t h_jobs_cap = 0, d_jobs_cap = 0;
     // CUDA graph mode: one executable graph, updated from each call's capture
     bool graphs = false;
     bool capturing = false;
@@ -636,6 +639,28 @@ int ensure_host(zf_ctx *ctx, uint8_t *&buf, size_t &cap, size_t need) {
     return ZF_OK;
 }
 
+// The job buffers of the gathered copies: room for `njobs` jobs (pinned
+// staging and device side), grown when a call needs more.
+int ensure_jobs(zf_ctx *ctx, size_t njobs) {
+    const size_t need = njobs * sizeof(zf::CopyJob);
+    const int rc = ensure_host(ctx, ctx->h_jobs, ctx->h_jobs_cap, need);
+    if (rc != ZF_OK) return rc;
+    if (need <= ctx->d_jobs_cap) return ZF_OK;
+    if (ctx->d_jobs) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(ctx->d_jobs);
+        ctx->d_jobs = nullptr;
+        ctx->d_jobs_cap = 0;
+    }
+    const size_t c = align_up(need + need / 4, 1 << 12);
+    if (cudaMalloc((void **)&ctx->d_jobs, c) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, ZF_ERR_ALLOC, "copy job list allocation failed");
+    }
+    ctx->d_jobs_cap = c;
+    return ZF_OK;
+}
+
 int ensure_arena(zf_ctx *ctx, size_t need) {
     if (ctx->budget && need > ctx->budget)
         return fail(ctx, ZF_ERR_ALLOC, "device footprint " + std::to_string(need) + " exceeds the HBM budget");
@@ -671,6 +696,74 @@ int copy_in(zf_ctx *ctx, void *dst, const void *src, size_t n, bool on_device) {
 }
 int copy_out(zf_ctx *ctx, void *dst, const void *src, size_t n, bool on_device) {
     CU(cudaMemcpyAsync(dst, src, n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx->stream));
+    return ZF_OK;
+}
+
+// Caller host planes that the device addresses directly (page-locked and
+// mapped: cudaPointerGetAttributes gives a device pointer) and that are at
+// most kGatherMaxBytes go through one k_copy_list launch per direction when
+// a call has at least kGatherMinCopies of them (a batch of small images is
+// hundreds of copies, each with its own fixed cost: 6.2 -> 12.1 GPix/s for
+// the 256-image batch through host buffers); fewer, larger planes and
+// pageable memory keep a cudaMemcpyAsync each, which measured as fast or
+// faster for single frames.
+constexpr size_t kGatherMaxBytes = 4u << 20;
+constexpr size_t kGatherMinCopies = 16;
+void *mapped_host(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // an unknown pointer is pageable host memory
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+struct HostCopies {
+    struct Copy {
+        void *dst;
+        const void *src;
+        size_t n;
+        bool to_device;
+        void *mapped;  // the host side's device address
+    };
+    std::vector<Copy> copies;
+    // dst and src as cudaMemcpyAsync would take them; true when queued
+    bool add(void *dst, const void *src, size_t n, bool to_device) {
+        if (n == 0 || n > kGatherMaxBytes) return false;
+        void *h = mapped_host(to_device ? src : dst);
+        if (!h) return false;
+        copies.push_back({dst, src, n, to_device, h});
+        return true;
+    }
+};
+// Issue the queued copies: one gathered launch when there are enough of
+// them (the job list goes to slot `slot` of the context's job buffers,
+// sized for the call beforehand), else a cudaMemcpyAsync each.
+int flush_copies(zf_ctx *ctx, const HostCopies &hc, size_t slot) {
+    if (hc.copies.empty()) return ZF_OK;
+    if (hc.copies.size() < kGatherMinCopies) {
+        for (const auto &c : hc.copies)
+            CU(cudaMemcpyAsync(c.dst, c.src, c.n, c.to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
+                               ctx->stream));
+        return ZF_OK;
+    }
+    std::vector<zf::CopyJob> jobs;
+    jobs.reserve(hc.copies.size());
+    uint64_t chunks = 0;
+    for (const auto &c : hc.copies) {
+        zf::CopyJob j;
+        j.src = c.to_device ? static_cast<const uint8_t *>(c.mapped) : static_cast<const uint8_t *>(c.src);
+        j.dst = c.to_device ? static_cast<uint8_t *>(c.dst) : static_cast<uint8_t *>(c.mapped);
+        j.bytes = c.n;
+        j.first_chunk = chunks;
+        chunks += (c.n + zf::kCopyChunk - 1) / zf::kCopyChunk;
+        jobs.push_back(j);
+    }
+    const size_t bytes = jobs.size() * sizeof(zf::CopyJob), off = slot * sizeof(zf::CopyJob);
+    std::memcpy(ctx->h_jobs + off, jobs.data(), bytes);
+    CU(cudaMemcpyAsync(ctx->d_jobs + off, ctx->h_jobs + off, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    { LaunchScope ls_(ctx, "k_copy_list");
+    CU(zf::launch_copy_list(reinterpret_cast<const zf::CopyJob *>(ctx->d_jobs + off), (int)jobs.size(), chunks,
+                            ctx->stream)); }
     return ZF_OK;
 }
 
@@ -1098,6 +1191,15 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
     CU(cudaMemsetAsync(base + o_out, 0, out_bytes, st));
 
     // ---- inputs
+    // job room for every plane copy of the call: in (rec, src, pre-CDEF per
+    // plane, geometry) then out (the filtered planes)
+    const size_t in_jobs = (size_t)n * 10;
+    TRY(ensure_jobs(ctx, in_jobs + (size_t)n * 3));
+    HostCopies hin, hout;
+    auto plane_in = [&](void *dst, const void *src, size_t nb, bool dev) -> int {
+        if (dev || !hin.add(dst, src, nb, true)) return copy_in(ctx, dst, src, nb, dev);
+        return ZF_OK;
+    };
     for (int i = 0; i < n; ++i) {
         Plan &p = plans[i];
         const zf_frame *f = p.in;
@@ -1117,12 +1219,11 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             p.d.mi = f->mi;
         } else {
             for (int pl = 0; pl < p.nplanes; ++pl) {
-                TRY(copy_in(ctx, base + p.off_set[set][pl], f->rec[pl], p.pbytes[pl], dev));
-                TRY(copy_in(ctx, base + p.off_src[pl], f->src[pl], p.pbytes[pl], dev));
-                if (run.pre_cdef_in)
-                    TRY(copy_in(ctx, base + p.off_set[SET_B][pl], run.pre_cdef[pl], p.pbytes[pl], dev));
+                TRY(plane_in(base + p.off_set[set][pl], f->rec[pl], p.pbytes[pl], dev));
+                TRY(plane_in(base + p.off_src[pl], f->src[pl], p.pbytes[pl], dev));
+                if (run.pre_cdef_in) TRY(plane_in(base + p.off_set[SET_B][pl], run.pre_cdef[pl], p.pbytes[pl], dev));
             }
-            TRY(copy_in(ctx, base + p.off_mi, f->mi, (size_t)p.d.mi_cols * p.d.mi_rows * 4, dev));
+            TRY(plane_in(base + p.off_mi, f->mi, (size_t)p.d.mi_cols * p.d.mi_rows * 4, dev));
         }
         for (int pl = 0; pl < 3; ++pl)
             if (!p.rects[pl].empty())
@@ -1184,6 +1285,7 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
             }
         }
     }
+    TRY(flush_copies(ctx, hin, 0));
 
     // ---- deblock level pick (presets <= 5: device SSE trials + host
     // hill-climb), or the caller's table of trial levels
@@ -1543,9 +1645,13 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
         const zf_frame *f = p.in;
         const bool dev = f->planes_on_device != 0;
         if ((run.stages & (STG_DB_APPLY | STG_CDEF_APPLY | STG_LR_APPLY)) && !p.zero_copy)
-            for (int pl = 0; pl < p.nplanes; ++pl)
-                TRY(copy_out(ctx, f->rec[pl], base + p.off_set[run.rec_out][pl], p.pbytes[pl], dev));
+            for (int pl = 0; pl < p.nplanes; ++pl) {
+                void *dst = f->rec[pl];
+                const void *src = base + p.off_set[run.rec_out][pl];
+                if (dev || !hout.add(dst, src, p.pbytes[pl], false)) TRY(copy_out(ctx, dst, src, p.pbytes[pl], dev));
+            }
     }
+    TRY(flush_copies(ctx, hout, in_jobs));
     CU(cudaStreamSynchronize(st));
     TRY(launch_check(ctx, "stream"));
     if (use_graph) TRY(check_cancel(ctx));
@@ -1729,6 +1835,8 @@ void zf_destroy(zf_ctx *ctx) {
     if (ctx->arena) cudaFree(ctx->arena);
     if (ctx->h_meta) cudaFreeHost(ctx->h_meta);
     if (ctx->h_out) cudaFreeHost(ctx->h_out);
+    if (ctx->h_jobs) cudaFreeHost(ctx->h_jobs);
+    if (ctx->d_jobs) cudaFree(ctx->d_jobs);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->trace_owned) std::fclose(ctx->trace);
@@ -1779,6 +1887,8 @@ int32_t zf_reserve(zf_ctx *ctx, uint64_t device_bytes, uint64_t host_bytes) {
     TRY(ensure_arena(ctx, (size_t)device_bytes));
     TRY(ensure_host(ctx, ctx->h_meta, ctx->h_meta_cap, (size_t)host_bytes));
     TRY(ensure_host(ctx, ctx->h_out, ctx->h_out_cap, (size_t)host_bytes));
+    // job lists for the gathered copies of up to 400 frames a call
+    TRY(ensure_jobs(ctx, 400 * 13));
     return ZF_OK;
 }
 

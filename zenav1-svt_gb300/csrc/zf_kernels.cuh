@@ -60,6 +60,18 @@ constexpr int kLrPairMaxHost = 20100;   // k_lr_finish pair-table entries (units
 __global__ void k_lr_finish(FrameDesc *frames, int nframes);
 __global__ void k_lr_apply(FrameDesc *frames, const WorkItem *items, int nitems, int group);
 
+// One plane copy of a gathered copy launch (zf_copy.cu): bytes from src to
+// dst (device addresses; host memory through its mapped address), taking
+// chunks [first_chunk, first_chunk + ceil(bytes / kCopyChunk)) of the launch.
+struct CopyJob {
+    const uint8_t *src;
+    uint8_t *dst;
+    uint64_t bytes;
+    uint64_t first_chunk;
+};
+constexpr int kCopyChunk = 64 * 1024;
+cudaError_t launch_copy_list(const CopyJob *jobs, int njobs, uint64_t nchunks, cudaStream_t st);
+
 // Fills dims and the CDEF policy of *d from a frame (host; zf_host.cu).
 int describe_cdef_frame(const zf_frame *f, FrameDesc *d);
 
