@@ -910,6 +910,56 @@ def run_batched(args, ctx, stream, dev, frames):
         same = same and a["lf"] == b["lf"] and a["cdef_y"] == b["cdef_y"] and a["cdef_uv"] == b["cdef_uv"] \
             and a["cdef_bits"] == b["cdef_bits"] and bool((a["cdef_fb_idx"] == b["cdef_fb_idx"]).all()) \
             and a["lr"] == b["lr"]
+
+    # the same batch as two halves (images alternating) on two contexts at
+    # once, one zf_submit_batch each from two host threads
+    import threading
+    ctx2 = pkg.Context(dev.index or 0)
+    stream2 = torch.cuda.ExternalStream(ctx2.stream_handle(), device=dev)
+    halves = [list(range(0, n, 2)), list(range(1, n, 2))]
+    decs2 = [abi.Decisions(f.w, f.h, f.true_w, f.true_h) for f in frames]
+    parts = []
+    for hv in halves:
+        ha = (abi.ZfFrame * len(hv))()
+        hd = (abi.ZfDecisions * len(hv))()
+        for k, i in enumerate(hv):
+            ha[k] = arr[i]
+            hd[k] = decs2[i].c
+        parts.append((ha, len(hv), hd, (abi.ZfStats * len(hv))()))  # submit_batch_raw's arguments
+
+    def batch2():
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        stream2.wait_event(e0)
+        ths = [threading.Thread(target=c.submit_batch_raw, args=part) for c, part in zip((ctx, ctx2), parts)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        ev = torch.cuda.Event()
+        ev.record(stream2)
+        stream.wait_event(ev)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    for _ in range(2):
+        restore()
+        batch2()
+    b2 = []
+    for _ in range(args.steps):
+        restore()
+        b2.append(batch2())
+    b2_ms = float(np.mean(b2))
+    for hv, (ha, hn, hd, hs) in zip(halves, parts):
+        for k, i in enumerate(hv):
+            decs2[i].c = hd[k]
+    same2 = all(torch.equal(a, b) for ra, rb in zip(out_batch, d_rec) for a, b in zip(ra, rb))
+    for a, d in zip(dec_batch, decs2):
+        b = d.as_dict()
+        same2 = same2 and a["lf"] == b["lf"] and a["cdef_y"] == b["cdef_y"] and a["cdef_bits"] == b["cdef_bits"] \
+            and bool((a["cdef_fb_idx"] == b["cdef_fb_idx"]).all()) and a["lr"] == b["lr"]
+    ctx2.close()
     del out_batch
 
     # e2e: the batch from pinned host buffers (H2D and D2H inside the call)
@@ -954,6 +1004,8 @@ def run_batched(args, ctx, stream, dev, frames):
             "plain_mpix_per_s": round(px / (p_ms / 1e3) / 1e6, 3), "plain_ms": round(p_ms, 3),
             "batched_over_plain": round(p_ms / b_ms, 3),
             "graphs": {"plain_ms": round(pg_ms, 3), "batched_ms": round(bg_ms, 3)},
+            "two_contexts": {"batched_ms": round(b2_ms, 3), "batched_mpix_per_s": round(px / (b2_ms / 1e3) / 1e6, 3),
+                             "identical": bool(same2)},
             "batched_e2e_mpix_per_s": round(px / (e_ms / 1e3) / 1e6, 3),
             "e2e_h2d_bytes": int(h2d), "e2e_d2h_bytes": int(h2d // 2),
             "identical_to_plain": bool(same), "autotune": tune,

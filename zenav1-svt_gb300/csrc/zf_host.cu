@@ -1383,16 +1383,36 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                           s.hc.result, (long long)s.hc.err[s.hc.result]);
             p_trace[s.frame].push_back(line);
         };
-        bool chroma_phase = false;
-        for (int guard = 0; guard < 256 && !slots.empty(); ++guard) {
+        // A frame's chroma climbs (searched only when its luma level is not
+        // 0) start as soon as the luma climb has left level 0, and share
+        // launches with it from then on: one round trip per step of the
+        // longer climb instead of the two climbs' steps in sequence. A luma
+        // climb that ends at 0 after all discards them.
+        const size_t nluma = slots.size();
+        std::vector<int> chroma_at(n, -1);  // index of a frame's U slot (V follows)
+        auto maybe_spawn = [&](size_t k) {
+            const int fi = slots[k].frame;
+            if (plans[fi].nplanes != 3 || chroma_at[fi] >= 0) return;
+            if (!(slots[k].hc.done ? slots[k].hc.result != 0 : slots[k].hc.at_mid > 0)) return;
+            const int conv = slots[k].hc.conv_th;
+            chroma_at[fi] = (int)slots.size();
+            for (int pl = 1; pl <= 2; ++pl) {
+                Slot c{fi, pl, HillClimb(), 0};
+                c.hc.conv_th = conv;
+                slots.push_back(c);
+            }
+        };
+        bool finished = false;
+        for (int guard = 0; guard < 256 && !finished; ++guard) {
             std::vector<TrialSlot> ts;
             std::vector<int> owner;
-            for (size_t k = 0; k < slots.size(); ++k) {
-                Slot &s = slots[k];
-                if (s.hc.done) continue;
+            for (size_t k = 0; k < slots.size(); ++k) {  // slots may grow: chroma climbs appended
+                if (slots[k].hc.done) continue;
                 int need[2];
-                const int m = s.hc.needs(need);
+                const int m = slots[k].hc.needs(need);
+                if (k < nluma) maybe_spawn(k);
                 if (m == 0) continue;
+                Slot &s = slots[k];
                 // four levels in each of a climb's first two launches (most
                 // climbs end within them), ctx->db_levels in later ones. A
                 // refining climb (conv_th != 1) on a plane of >= 512 tiles
@@ -1415,27 +1435,10 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 owner.push_back((int)k);
             }
             if (owner.empty()) {
-                bool all_done = true;
-                for (auto &s : slots) all_done = all_done && s.hc.done;
-                if (!all_done) return fail(ctx, ZF_ERR_UNSUPPORTED, "deblock search stalled");
-                for (auto &s : slots) trace_climb(s);
-                if (chroma_phase) break;
-                // luma finished: record levels, start chroma where luma > 0
-                std::vector<Slot> next;
-                for (auto &s : slots) {
-                    Plan &p = plans[s.frame];
-                    p.d.lf[0] = p.d.lf[1] = (uint8_t)s.hc.result;
-                    p.d.lf[2] = p.d.lf[3] = 0;
-                    if (s.hc.result != 0 && p.nplanes == 3)
-                        for (int pl = 1; pl <= 2; ++pl) {
-                            Slot c{s.frame, pl, HillClimb(), 0};
-                            c.hc.conv_th = s.hc.conv_th;
-                            next.push_back(c);
-                        }
-                }
-                slots.swap(next);
-                chroma_phase = true;
-                continue;
+                for (auto &s : slots)
+                    if (!s.hc.done) return fail(ctx, ZF_ERR_UNSUPPORTED, "deblock search stalled");
+                finished = true;
+                break;
             }
             TRY(run_trials(ts));
             for (size_t k = 0; k < owner.size(); ++k) {
@@ -1447,8 +1450,20 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                 }
             }
         }
-        if (chroma_phase)
-            for (auto &s : slots) plans[s.frame].d.lf[1 + s.plane] = (uint8_t)s.hc.result;
+        if (!finished) return fail(ctx, ZF_ERR_UNSUPPORTED, "deblock search did not converge");
+        for (size_t k = 0; k < nluma; ++k) {
+            const Slot &s = slots[k];
+            Plan &p = plans[s.frame];
+            p.d.lf[0] = p.d.lf[1] = (uint8_t)s.hc.result;
+            p.d.lf[2] = p.d.lf[3] = 0;
+            trace_climb(s);
+            if (s.hc.result != 0 && chroma_at[s.frame] >= 0)
+                for (int pl = 1; pl <= 2; ++pl) {
+                    const Slot &c = slots[chroma_at[s.frame] + pl - 1];
+                    p.d.lf[1 + pl] = (uint8_t)c.hc.result;
+                    trace_climb(c);
+                }
+        }
     }
 
     // ---- graph mode: everything from here to the decision readback is

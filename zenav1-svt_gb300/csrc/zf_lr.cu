@@ -979,14 +979,24 @@ constexpr int kTrialCluster = 8;
 constexpr int TRIAL_SW = TT_W + 8, TRIAL_SH = TT_H + 7;  // staged window rows 8-byte aligned
 constexpr int TRIAL_WIN = TRIAL_SH * TRIAL_SW, TRIAL_SRC = TT_H * TT_W, TRIAL_TMP = TRIAL_SH * TT_W;
 
+// With at most kTrialCacheTiles tiles per CTA every tile keeps its own
+// horizontal-pass buffer: the trials of the vertical taps (the second
+// refinement pass) leave the horizontal taps alone, so they reuse it and run
+// only the vertical pass. Above that the CTA keeps two buffers, alternating.
+constexpr int kTrialCacheTiles = 5;
 struct TrialTiles {
     const uint16_t *win, *src;  // [n][TRIAL_WIN], [n][TRIAL_SRC]
-    uint16_t *tmp;              // [2][TRIAL_TMP]
+    uint16_t *tmp;              // [n][TRIAL_TMP] when cached, else [2][TRIAL_TMP]
     int n, ntx, rank, CL;
+    bool cached;
 };
 
+// do_h: run the horizontal pass (always when the buffers are not cached;
+// when they are, a trial whose horizontal taps equal those of the buffers'
+// last pass may skip it).
 __device__ int64_t trial_sse(const FrameDesc &f, const UnitRect &r, const Taps &t, const TrialTiles &T,
-                             unsigned long long *red, unsigned long long (*inbox)[kTrialCluster][3], int &buf) {
+                             unsigned long long *red, unsigned long long (*inbox)[kTrialCluster][3], int &buf,
+                             bool do_h = true) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     const int bd = f.bd;
@@ -1008,13 +1018,20 @@ __device__ int64_t trial_sse(const FrameDesc &f, const UnitRect &r, const Taps &
     const int hc3 = 128 + hf[3], hoff = 1 << (bd + 6), hlim = (1 << (bd + 5)) - 1;
     const int vc3 = 128 + vf[3], voff = -(1 << (bd + 10)), vmax = (1 << bd) - 1;
     uint32_t blk = 0, rgt = 0, bot = 0;  // a thread's parts of one trial: <= 9 tiles x 8 pixels of e^2 <= 1023^2
-    for (int k = 0; k <= T.n; ++k) {
-        if (k < T.n) {
+    // cached buffers: every tile's horizontal pass (unless skipped), one
+    // barrier, then every tile's vertical pass; else the horizontal pass of
+    // tile k and the vertical pass of tile k - 1 share a barrier
+    const int hk = T.cached ? T.n : 1;  // tiles per phase
+    const int nphase = T.cached ? (do_h ? 2 : 1) : T.n + 1;
+    for (int ph = 0; ph < nphase; ++ph) {
+        const int kh0 = T.cached ? (do_h && ph == 0 ? 0 : T.n) : ph;        // horizontal tiles [kh0, kh0 + hk)
+        const int kv0 = T.cached ? (do_h && ph == 0 ? T.n : 0) : ph - 1;    // vertical tiles [kv0, kv0 + hk)
+        for (int k = kh0; k < min(kh0 + hk, T.n); ++k) {
             // horizontal pass of tile k: every staged row x 16 runs of four columns
             const int tile = T.rank + k * T.CL;
             const int tw = min(TT_W, uw - (tile % T.ntx) * TT_W);
             const uint16_t *stage = T.win + k * TRIAL_WIN;
-            uint16_t *tmp = T.tmp + (k & 1) * TRIAL_TMP;
+            uint16_t *tmp = T.tmp + (T.cached ? k : (k & 1)) * TRIAL_TMP;
             for (int q = threadIdx.x; q < TRIAL_SH * (TT_W / 4); q += blockDim.x) {
                 const int rr = q >> 4, c0 = (q & 15) * 4;
                 if (c0 >= tw) continue;
@@ -1038,15 +1055,15 @@ __device__ int64_t trial_sse(const FrameDesc &f, const UnitRect &r, const Taps &
                 *reinterpret_cast<uint2 *>(tmp + rr * TT_W + c0) = make_uint2(o[0] | o[1] << 16, o[2] | o[3] << 16);
             }
         }
-        if (k > 0) {
-            // vertical pass of tile k - 1: four columns of one row per
-            // thread, packed pair sums (tmp values are < 2^15), the SSE
-            // parts against the staged source
-            const int tile = T.rank + (k - 1) * T.CL;
+        for (int k = max(kv0, 0); k < min(kv0 + hk, T.n); ++k) {
+            // vertical pass of tile k: four columns of one row per thread,
+            // packed pair sums (tmp values are < 2^15), the SSE parts
+            // against the staged source
+            const int tile = T.rank + k * T.CL;
             const int ty = (tile / T.ntx) * TT_H, tx = (tile % T.ntx) * TT_W;
             const int th = min(TT_H, uh - ty), tw = min(TT_W, uw - tx);
-            const uint16_t *tmp = T.tmp + ((k - 1) & 1) * TRIAL_TMP;
-            const uint16_t *srct = T.src + (k - 1) * TRIAL_SRC;
+            const uint16_t *tmp = T.tmp + (T.cached ? k : (k & 1)) * TRIAL_TMP;
+            const uint16_t *srct = T.src + k * TRIAL_SRC;
             for (int q = threadIdx.x; q < th * (TT_W / 4); q += blockDim.x) {
                 const int rr = q >> 4, c0 = (q & 15) * 4;
                 if (c0 >= tw) continue;
@@ -1127,7 +1144,8 @@ __device__ int64_t trial_sse(const FrameDesc &f, const UnitRect &r, const Taps &
 }
 
 size_t lr_trial_smem(int max_tiles) {
-    return (size_t)max_tiles * (TRIAL_WIN + TRIAL_SRC) * 2 + 2 * TRIAL_TMP * 2;
+    const int tmps = max_tiles <= kTrialCacheTiles ? max_tiles : 2;
+    return ((size_t)max_tiles * (TRIAL_WIN + TRIAL_SRC) + (size_t)tmps * TRIAL_TMP) * 2;
 }
 __host__ __device__ int lr_trial_tiles_per_cta(int uw, int uh) {
     return (((uw + TT_W - 1) / TT_W) * ((uh + TT_H - 1) / TT_H) + kTrialCluster - 1) / kTrialCluster;
@@ -1169,6 +1187,7 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256, 3)
     T.win = trial_dyn;
     T.src = trial_dyn + max_tiles * TRIAL_WIN;
     T.tmp = trial_dyn + max_tiles * (TRIAL_WIN + TRIAL_SRC);
+    T.cached = max_tiles <= kTrialCacheTiles;  // uniform over the launch
     {
         const int bd = f.bd, stride = plane_stride(f, wi.plane);
         const uint8_t *dg = f.A[wi.plane], *sr = f.S[wi.plane];
@@ -1199,6 +1218,10 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256, 3)
         const int tap_min[3] = {-5, -23, -17}, tap_max[3] = {10, 8, 46};
         const int s = 4;
         for (int pass = 0; pass < 2; ++pass) {
+            // the second pass changes vertical taps only: with cached
+            // buffers its first trial runs the horizontal pass with the
+            // horizontal taps the first pass settled on, the rest reuse it
+            bool h_ready = false;
             for (int p = plane_off; p < 3; ++p) {
                 bool skip = false;
                 // minus direction
@@ -1211,7 +1234,8 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256, 3)
                         fp[3] += 2 * s;
                     }
                     __syncthreads();
-                    const int64_t e2 = trial_sse(f, r, t, T, red, inbox, buf);
+                    const int64_t e2 = trial_sse(f, r, t, T, red, inbox, buf, !(T.cached && pass == 1 && h_ready));
+                    h_ready = h_ready || pass == 1;
                     if (e2 > err) {
                         __syncthreads();
                         if (threadIdx.x == 0) {
@@ -1235,7 +1259,8 @@ __global__ void __cluster_dims__(kTrialCluster, 1, 1) __launch_bounds__(256, 3)
                         fp[3] -= 2 * s;
                     }
                     __syncthreads();
-                    const int64_t e2 = trial_sse(f, r, t, T, red, inbox, buf);
+                    const int64_t e2 = trial_sse(f, r, t, T, red, inbox, buf, !(T.cached && pass == 1 && h_ready));
+                    h_ready = h_ready || pass == 1;
                     if (e2 > err) {
                         __syncthreads();
                         if (threadIdx.x == 0) {
