@@ -593,7 +593,7 @@ __global__ void __launch_bounds__(kFinThreads, 1)
     cg::cluster_group cl = cg::this_cluster();
     // dynamic: the double-buffered pair partials, then (when they fit) the
     // compacted rows and their filter-block ids
-    extern __shared__ unsigned long long dyn64[];
+    extern __shared__ __align__(16) unsigned long long dyn64[];
     __shared__ uint8_t wlev[kFinWarps][2][16];
     __shared__ int scan[kFinThreads];
     __shared__ int local_sb, last_flag;
@@ -638,9 +638,15 @@ __global__ void __launch_bounds__(kFinThreads, 1)
     // the stride its slice was sized for
     const size_t pbytes = (size_t)2 * pslots * 8;
     const bool in_smem = pbytes + (size_t)sbr * (n2 + 1) * 4 <= (size_t)smem_bytes;
-    const int sbp = in_smem && !(sbr & 1) && pbytes + ((size_t)(sbr + 1) * n2 + sbr) * 4 <= (size_t)smem_bytes
-                        ? sbr + 1
-                        : sbr;
+    const bool wide = npairs >= kFinWideMinPairs && sbr <= kFinBstMax;
+    // the pair-per-thread step reads four rows of a column per 16-byte load:
+    // columns 16-byte aligned at a stride of an odd multiple of 16 bytes, so
+    // the eight loads of a quarter warp (eight columns) hit distinct banks;
+    // the warp-per-pair step wants an odd word stride
+    const int sbq = (sbr + 3) / 8 * 8 + 4, sbo = sbr | 1;
+    auto fits = [&](int st) { return in_smem && pbytes + ((size_t)st * n2 + sbr) * 4 <= (size_t)smem_bytes; };
+    const int sbp = wide && fits(sbq) ? sbq : !wide && fits(sbo) ? sbo : sbr;
+    const bool quad = wide && sbp == sbq;
     uint32_t *R = in_smem ? dyn : f.cdef_rows32 + ((size_t)level * nfb + fb0) * n2;
     int *ids = in_smem ? reinterpret_cast<int *>(dyn + (size_t)sbp * n2) : f.cdef_ids + (size_t)level * nfb + fb0;
     {
@@ -678,8 +684,7 @@ __global__ void __launch_bounds__(kFinThreads, 1)
     int buf = 0;
     // One search_one_dual step (cdef.rs:824-862) over the whole frame for
     // strength slot nbs; returns the best total and records the pair.
-    __shared__ uint32_t bsts[kFinBstMax];
-    const bool wide = npairs >= kFinWideMinPairs && sbr <= kFinBstMax;
+    __shared__ __align__(16) uint32_t bsts[kFinBstMax];
     auto step = [&](int nbs) -> unsigned long long {
         if (wide) {
             // the best of the fixed strengths per row, then one pair per
@@ -699,6 +704,13 @@ __global__ void __launch_bounds__(kFinThreads, 1)
                 unsigned long long acc = 0;
                 int s = 0;
                 // four rows per u32 partial: each min is below 2^30
+                if (quad)
+                    for (; s + 4 <= sbr; s += 4) {
+                        const uint4 a = *reinterpret_cast<const uint4 *>(rj + s);
+                        const uint4 b = *reinterpret_cast<const uint4 *>(rk + s);
+                        const uint4 c = *reinterpret_cast<const uint4 *>(bsts + s);
+                        acc += min(a.x + b.x, c.x) + min(a.y + b.y, c.y) + min(a.z + b.z, c.z) + min(a.w + b.w, c.w);
+                    }
                 for (; s + 4 <= sbr; s += 4) {
                     uint32_t m = 0;
 #pragma unroll
@@ -1803,12 +1815,12 @@ extern "C" int32_t zf_cdef_search_noalloc(void *stream, const zf_frame *f, zf_de
     if (launch_cdef_search(d.cdef.first_pass_num, d.cdef.ncand / d.cdef.first_pass_num, nfb, st, &sc->desc,
                            &sc->item, 1) != cudaSuccess)
         return ZF_ERR_CUDA;
-    // pair partials (an inbox per rank) + compacted rows (an odd column
-    // stride) and ids: at most 51 + 42 KiB for ncand <= 20 and nfb <= 2048
+    // pair partials (an inbox per rank) + compacted rows (a padded column
+    // stride) and ids: at most 51 + 44 KiB for ncand <= 20 and nfb <= 2048
     const int np = d.cdef.ncand * d.cdef.ncand;
     const int CL = kFinCluster;
     const int rows = (nfb + CL - 1) / CL;
-    const int per_cta = (int)fin_pair_bytes(np, CL) + (rows + 1) * 2 * d.cdef.ncand * 4 + rows * 4;
+    const int per_cta = (int)fin_pair_bytes(np, CL) + (rows + 12) * 2 * d.cdef.ncand * 4 + rows * 4;
     // raise the kernel's dynamic shared memory opt-in when this launch needs
     // more, never lower it: the attribute is per function and device, and a
     // context set it to its own cap at creation

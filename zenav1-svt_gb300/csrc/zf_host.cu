@@ -1557,9 +1557,10 @@ int run_batch(zf_ctx *ctx, const zf_frame *frames, int n, zf_decisions *outs, zf
                     const size_t nc = (size_t)plans[fi].d.cdef.ncand, np = nc * nc;
                     const size_t pb = zf::fin_pair_bytes((int)np, cl);
                     pairs = std::max(pairs, pb);
-                    // rows (+ one padding row per column: the odd stride) and ids
+                    // rows (+ up to 12 padding rows per column: the padded
+                    // strides) and ids
                     const size_t rows = ((size_t)plans[fi].nfb + cl - 1) / cl;
-                    want = std::max(want, pb + (rows + 1) * 2 * nc * 4 + rows * 4);
+                    want = std::max(want, pb + (rows + 12) * 2 * nc * 4 + rows * 4);
                 }
                 return std::max(pairs, std::min<size_t>(want, kFinishSmemCap));
             };
