@@ -450,11 +450,35 @@ __global__ void __launch_bounds__(256, 5) k_deblock_sse(const FrameDesc *frames,
     const int tix = blockIdx.x - wi.cta_begin;
     DbTile t{&f, plane, pw, ph, (tix % tiles_x) * DB_T, (tix / tiles_x) * DB_T};
     const int bd = f.bd;
-    db_load(t, f.IN[plane], pristine);
-    // the tile's source samples (0 outside the plane: such positions are
-    // skipped by the sum below), word-wide where the plane allows
+    // the region and the tile's source samples (0 outside the plane: such
+    // positions are skipped by the sum below), word-wide where the planes
+    // allow
     const int spw = bd == 8 ? 4 : 2, wpr = DB_T / spw, lgw = bd == 8 ? 4 : 5;  // wpr = 1 << lgw
-    if (word_ok(f.S[plane])) {
+    if (bd != 8 && word_ok(f.IN[plane]) && word_ok(f.S[plane])) {
+        // 16-bit samples land in shared memory as they are: every word of
+        // the region and the source tile as a 4-byte asynchronous copy, all
+        // in flight at once (zeros outside the plane), one wait
+        const int rpr = DB_R / 2, tot_r = DB_R * rpr, tot = tot_r + DB_T * wpr;
+        for (int i = threadIdx.x; i < tot; i += blockDim.x) {
+            if (i < tot_r) {
+                const int ry = i / rpr, wx = i - ry * rpr;
+                const int y = t.y0 - DB_H + ry, x = t.x0 - DB_H + wx * 2;
+                const bool in = x >= 0 && x < t.pw && y >= 0 && y < t.ph;
+                cp_async4(pristine + ry * DB_P + wx * 2, in ? (const void *)word_at(f.IN[plane], (int64_t)y * t.pw + x, bd)
+                                                           : (const void *)f.IN[plane],
+                          in ? 4u : 0u);
+            } else {
+                const int k = i - tot_r, ty = k >> lgw, wx = k & (wpr - 1);
+                const int y = t.y0 + ty, x = t.x0 + wx * 2;
+                const bool in = x < pw && y < ph;
+                cp_async4(srct + ty * DB_T + wx * 2, in ? (const void *)word_at(f.S[plane], (int64_t)y * pw + x, bd)
+                                                       : (const void *)f.S[plane],
+                          in ? 4u : 0u);
+            }
+        }
+        cp_async_wait_all();
+    } else if (word_ok(f.S[plane])) {
+        db_load(t, f.IN[plane], pristine);
         for (int i = threadIdx.x; i < DB_T * wpr; i += blockDim.x) {
             const int ty = i >> lgw, wx = i & (wpr - 1);
             const int y = t.y0 + ty, x = t.x0 + wx * spw;
@@ -462,6 +486,7 @@ __global__ void __launch_bounds__(256, 5) k_deblock_sse(const FrameDesc *frames,
             unpack_word(v, bd, srct + ty * DB_T + wx * spw);
         }
     } else {
+        db_load(t, f.IN[plane], pristine);
         for (int i = threadIdx.x; i < DB_T * DB_T; i += blockDim.x) {
             const int ty = i / DB_T, tx = i % DB_T, y = t.y0 + ty, x = t.x0 + tx;
             srct[i] = (uint16_t)((x < pw && y < ph) ? ldpx(f.S[plane], (int64_t)y * pw + x, bd) : 0);

@@ -270,6 +270,18 @@ __device__ __forceinline__ void stage_window(int bd, int pw, int nrows, int xa, 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
+
+// A 4-byte asynchronous global -> shared copy (cp.async.ca): `src_bytes`
+// 4 copies the word, 0 writes zeros (src is then not read, but stays a
+// valid address). Completion: cp_async_wait_all() by the issuing thread,
+// then a barrier for the others.
+__device__ __forceinline__ void cp_async4(void *dst, const void *src, uint32_t src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
 __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
