@@ -220,21 +220,24 @@ def test_random_streams_decode_with_the_spec_reader(pkg, seed):
 
 
 # -- the filter syntax of a tile, coded and read back ---------------------------
-def tile_walk(ec, dec, w, h, sb, rng, skip_prob=0.5):
+def tile_walk(ec, dec, w, h, sb, rng, skip_prob=0.5, monochrome=False, sr_denom=0, coded_w=None):
     """Per superblock in raster order: the restoration units, then 32x32
     coded blocks in Z order, each a skip flag (a stand-in for the rest of the
-    block's syntax) followed by cdef_idx where due. Returns the block list."""
+    block's syntax) followed by cdef_idx where due. Returns the block list.
+    With superres the superblocks walk the coded width; w is the upscaled
+    width the restoration units live on."""
     sb_mi = sb // 4
     blocks = []
+    cw = w if coded_w is None else coded_w
     for sr in range(0, (h + sb - 1) // sb):
-        for sc in range(0, (w + sb - 1) // sb):
-            ec.lr_sb(dec, sr * sb_mi, sc * sb_mi, sb_mi, w, h)
+        for sc in range(0, (cw + sb - 1) // sb):
+            ec.lr_sb(dec, sr * sb_mi, sc * sb_mi, sb_mi, w, h, monochrome, sr_denom)
             st = ec.cdef_sb(dec, sr, sc, sb)
             for q in range((sb // 64) ** 2):
                 qx, qy = sc * sb + (q & 1) * 64, sr * sb + (q >> 1) * 64
                 for b in range(4):
                     bx, by = qx + (b & 1) * 32, qy + (b >> 1) * 32
-                    if bx >= w or by >= h:
+                    if bx >= cw or by >= h:
                         continue
                     skip = int(rng.random() < skip_prob)
                     ec.bool(skip)
@@ -243,7 +246,7 @@ def tile_walk(ec, dec, w, h, sb, rng, skip_prob=0.5):
     return blocks
 
 
-def read_tile(data, dec_planes, nhfb, cdef_bits, w, h, sb, blocks):
+def read_tile(data, dec_planes, nhfb, cdef_bits, w, h, sb, blocks, monochrome=False, sr_denom=0):
     """The decoder's side of tile_walk (spec read_lr per superblock, then per
     block the skip flag and read_cdef)."""
     r = SpecReader(data)
@@ -256,11 +259,11 @@ def read_tile(data, dec_planes, nhfb, cdef_bits, w, h, sb, blocks):
     for sr, sc, bx, by, skip in blocks:
         if (sr, sc) != last_sb:
             last_sb = (sr, sc)
-            for p in range(3):
+            for p in range(1 if monochrome else 3):
                 plane = dec_planes[p]
                 if plane["frame_rtype"] == 0:
                     continue
-                cr = c_reference(plane["unit_size"], p > 0, sr * sb_mi, sc * sb_mi, sb_mi, w, h, 0)
+                cr = c_reference(plane["unit_size"], p > 0, sr * sb_mi, sc * sb_mi, sb_mi, w, h, sr_denom)
                 if cr is None:
                     continue
                 for rrow in range(cr[2], cr[3]):
@@ -310,6 +313,29 @@ def test_restoration_units_read_back(pkg, w, h, sb):
     units, _ = read_tile(ec.done(), plane_info(dec), 0, 0, w, h, sb, blocks)
     check_units(units, dec)
     assert len(units) == sum(dec.lr[p].hunits * dec.lr[p].vunits for p in range(3))
+
+
+def test_monochrome_and_superres_units_read_back(pkg):
+    """Monochrome: luma units only. Superres (denominators 9, 12, 16): the
+    superblocks walk the coded width while the units live on the upscaled
+    one, so a superblock holds the corners that corners_in_sb remaps."""
+    rng = np.random.default_rng(5)
+    dec, keep = make_decisions(rng, 1000, 600)
+    ec = pkg.RangeCoder()
+    blocks = tile_walk(ec, dec, 1000, 600, 64, rng, monochrome=True)
+    units, _ = read_tile(ec.done(), plane_info(dec), 0, 0, 1000, 600, 64, blocks, monochrome=True)
+    check_units(units, dec)
+    assert {p for p, _ in units} == {0} and len(units) == dec.lr[0].hunits * dec.lr[0].vunits
+    for denom in (9, 12, 16):
+        w, h = 1024, 512
+        coded = pkg.lib().zf_superres_scaled_size(w, denom)
+        assert 0 < coded < w
+        dec, keep = make_decisions(rng, w, h)
+        ec = pkg.RangeCoder()
+        blocks = tile_walk(ec, dec, w, h, 64, rng, sr_denom=denom, coded_w=coded)
+        units, _ = read_tile(ec.done(), plane_info(dec), 0, 0, w, h, 64, blocks, sr_denom=denom)
+        check_units(units, dec)
+        assert len(units) == sum(dec.lr[p].hunits * dec.lr[p].vunits for p in range(3)), denom
 
 
 FRAMES = [
