@@ -1033,7 +1033,7 @@ def run_batched(args, ctx, stream, dev, frames):
 def run_served(args, device, frames):
     """Served requests: Poisson arrivals at 50 / 200 / 800 req/s, sizes
     log-uniform 128^2 .. 6000x4000 (80 % 8-bit), preset 6, through the
-    continuous-batching loop (three worker contexts, 120 GB HBM budget).
+    continuous-batching loop (--served-workers contexts, 120 GB HBM budget).
     Requests cycle through a pool of pre-generated images (pinned host
     buffers); latency = completion - scheduled arrival."""
     import copy
@@ -1044,10 +1044,10 @@ def run_served(args, device, frames):
     for f in frames:
         src = [torch.from_numpy(p).pin_memory().numpy() for p in f.src]
         pool.append({"f": f, "src": src, "rec0": f.rec, "mi": pkg.pack_geom(f.geom), "slots": []})
-    executors = [serve.FilterExecutor(device) for _ in range(3)]
+    executors = [serve.FilterExecutor(device) for _ in range(args.served_workers)]
     # every worker's arena sized up front for a full batch (48 MP at 10 bits
     # needs < 1 GB), so no arena grows while requests are timed
-    srv = serve.Server(executors, hbm_budget_bytes=120 << 30, max_batch=64, max_batch_px=48 << 20,
+    srv = serve.Server(executors, hbm_budget_bytes=120 << 30, max_batch=64, max_batch_px=args.served_batch_mpix << 20,
                        reserve_bytes=3 << 29)
     for e in pool:
         r = serve.Request(e["f"], mi=e["mi"])
@@ -1112,7 +1112,8 @@ def run_served(args, device, frames):
         e.close()
     return {"workload": ("Poisson arrivals, sizes log-uniform 128^2..6000x4000, 80% 8-bit / 20% 10-bit, "
                          "qp ~ U[18,45], preset 6; requests cycle a pool of {} images").format(len(pool)),
-            "seconds_per_rate": args.served_seconds, "workers": 3, "hbm_budget_gb": 120,
+            "seconds_per_rate": args.served_seconds, "workers": args.served_workers,
+            "max_batch_mpix": args.served_batch_mpix, "hbm_budget_gb": 120,
             "peak_reserved_gb": round(srv.peak_reserved / 2 ** 30, 3), "arena_grows": srv.arena_grows,
             "rates": out}
 
@@ -1185,6 +1186,8 @@ def main():
     ap.add_argument("--batch-n", type=int, default=256)
     ap.add_argument("--served-seconds", type=float, default=4.0, help="arrival window per rate")
     ap.add_argument("--served-rates", type=int, nargs="+", default=[50, 200, 800], help="arrival rates (req/s)")
+    ap.add_argument("--served-workers", type=int, default=3, help="worker contexts of the served loop")
+    ap.add_argument("--served-batch-mpix", type=int, default=48, help="luma megapixels a served batch holds at most")
     args = ap.parse_args()
     if args.profile_run:
         return run_profile(args)
