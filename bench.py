@@ -1135,7 +1135,7 @@ def run_profile(args):
     if args.workload == "highres10":
         frames = [synth.workload_10bit_4096()]
     elif args.workload == "batch":
-        frames = synth.workload_batch(n=args.batch_n)
+        frames = gen_frames(batch_jobs(args.batch_n))
     else:
         frames = make_workload(args.pw, args.ph)[:args.nframes]  # the timed frames (same seeds)
     ctx = pkg.Context(0)
@@ -1155,12 +1155,19 @@ def run_profile(args):
                                               on_device=True), abi.Decisions(f.w, f.h, f.true_w, f.true_h),
                         abi.ZfStats()))
     torch.cuda.synchronize()
+    n = len(structs)
+    arr, darr, sarr = (abi.ZfFrame * n)(), (abi.ZfDecisions * n)(), (abi.ZfStats * n)()
+    for i, (s, d, st) in enumerate(structs):
+        arr[i], darr[i] = s, d.c
     for _ in range(args.warmup + args.steps):
         for a, b in pairs:  # every pass filters the same pre-deblock recon
             a.copy_(b)
         torch.cuda.synchronize()
-        for s, d, st in structs:
-            ctx.filter_stage_raw(s, d, st)
+        if args.submit_batch:  # the frames as one zf_submit_batch
+            ctx.submit_batch_raw(arr, n, darr, sarr)
+        else:
+            for s, d, st in structs:
+                ctx.filter_stage_raw(s, d, st)
         ctx.sync()
     print("profile run done: %d frames %dx%d, %d passes" % (len(frames), args.pw, args.ph, args.warmup + args.steps))
     ctx.close()
@@ -1181,6 +1188,7 @@ def main():
     ap.add_argument("--stats-tc", action="store_true", help="profile run: tensor-core Wiener statistics")
     ap.add_argument("--workload", default="plain4k", choices=["plain4k", "highres10", "batch"],
                     help="profile run: the frames to run (one zf_filter_stage per frame)")
+    ap.add_argument("--submit-batch", action="store_true", help="profile run: the frames as one zf_submit_batch")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-image batch")
     ap.add_argument("--no-served", action="store_true", help="skip the served request loop")
     ap.add_argument("--batch-n", type=int, default=256)
