@@ -115,6 +115,8 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
     constexpr int SR = WIN == 5 ? G::ROWS : 1;
     __shared__ int Mrow[SR][WIN2];
     __shared__ unsigned Srow[SR][WIN2], Erow[SR][4];
+    constexpr int kSlotSums = 2 * WIN2 + 4;  // Mr entries, shift sums, sse / source sums
+    __shared__ long long slot_part[WIN == 5 ? 4 : 1][kSlotSums];
     static_assert(G::DROWS * G::DSB <= (int)sizeof(D) && G::ROWS * G::XSB <= (int)sizeof(X), "byte layout fits");
     static_assert(WIN != 5 || (kTmaDBoxH == G::DROWS && kTmaXBoxH == G::ROWS &&
                                kTmaDBoxW * 4 * kTmaDBoxH <= (int)sizeof(D) && kTmaXBoxW * 4 * kTmaXBoxH <= (int)sizeof(X) &&
@@ -521,21 +523,6 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
         constexpr int NE = WIN * (WIN + 1) / 2;
         static_assert(G::ROWS * G::NDR * NE * 4 <= G::DROWS * G::DCOLS * 2, "row-sum buffer fits in D");
         int *RS = reinterpret_cast<int *>(D);
-        if constexpr (WIN == 5) {
-            // the row slots of the (row, window row) and sse walks: 25 Mr
-            // entries, 25 shift sums, 4 sse / source sums, over the unit rows
-            // of this CTA (each entry of Ms / Ss / Es is written here only)
-            const int nr = xi1 - xi0, q = (int)blockDim.x - 1 - t;  // the highest threads
-            if (q < 2 * WIN2 + 4) {
-                long long a = 0;
-                for (int r = 0; r < nr; ++r)
-                    a += q < WIN2 ? (long long)Mrow[r][q] : q < 2 * WIN2 ? (long long)Srow[r][q - WIN2]
-                                                                         : (long long)Erow[r][q - 2 * WIN2];
-                if (q < WIN2) Ms[q] = (unsigned long long)a;
-                else if (q < 2 * WIN2) Ss[q - WIN2] = (unsigned long long)a;
-                else Es[q - 2 * WIN2] = (unsigned long long)a;
-            }
-        }
         if (keep) {
             int e = 0;
 #pragma unroll
@@ -543,7 +530,35 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
 #pragma unroll
                 for (int ca = 0; ca + dc < WIN; ++ca) RS[t * NE + e++] = rs[dc][ca];
         }
+        if constexpr (WIN == 5) {
+            // the row slots of the (row, window row) and sse walks: 25 Mr
+            // entries, 25 shift sums, 4 sse / source sums, over the unit rows
+            // of this CTA, in four interleaved parts of the rows (short
+            // chains of loads and adds on many threads), added after the
+            // barrier (each entry of Ms / Ss / Es is written there only)
+            const int nr = xi1 - xi0;
+            if (t < 4 * kSlotSums) {
+                const int part = t / kSlotSums, q = t - part * kSlotSums;
+                long long a = 0;
+                for (int r = part; r < nr; r += 4)
+                    a += q < WIN2 ? (long long)Mrow[r][q] : q < 2 * WIN2 ? (long long)Srow[r][q - WIN2]
+                                                                         : (long long)Erow[r][q - 2 * WIN2];
+                slot_part[part][q] = a;
+            }
+        }
         __syncthreads();
+        if constexpr (WIN == 5) {
+            if (t < kSlotSums) {
+                const unsigned long long a = (unsigned long long)(slot_part[0][t] + slot_part[1][t] + slot_part[2][t] +
+                                                                  slot_part[3][t]);
+                if (t < WIN2) Ms[t] = a;
+                else if (t < 2 * WIN2) Ss[t - WIN2] = a;
+                else Es[t - 2 * WIN2] = a;
+            }
+        }
+        // every (dr, dc, ca) and window row ra below is a distinct H entry
+        // (ia, ib) -- (ca, ra) and (ca + dc, ra + dr) give back all four --
+        // so each entry of Hs has one writer here and takes a plain add
         for (int q = t; q < G::NDR * NE; q += blockDim.x) {
             const int dri = q / NE, dr = dri - (WIN - 1);
             int e = q - dri * NE, dc = 0;
@@ -560,7 +575,7 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                 if (acc == 0) continue;
                 for (int ra = ra0; ra < ra1; ++ra) {
                     const int ia = ca * WIN + ra, ib = (ca + dc) * WIN + ra + dr;
-                    atomicAdd(&Hs[ia * WIN2 + ib], (unsigned long long)acc);
+                    Hs[ia * WIN2 + ib] += (unsigned long long)acc;
                 }
             } else {  // a row adds to the vertical shifts sr = ra - HALF whose window [sr, sr + uh) holds it
                 long long acc[WIN];
@@ -577,7 +592,7 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                 for (int ra = 0; ra < WIN; ++ra) {
                     if (ra < ra0 || ra >= ra1 || acc[ra] == 0) continue;
                     const int ia = ca * WIN + ra, ib = (ca + dc) * WIN + ra + dr;
-                    atomicAdd(&Hs[ia * WIN2 + ib], (unsigned long long)acc[ra]);
+                    Hs[ia * WIN2 + ib] += (unsigned long long)acc[ra];
                 }
             }
         }
