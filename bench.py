@@ -290,7 +290,7 @@ KERNEL_WARP_INST_PER_PX = {
     "k_deblock_apply": 5.3854,
     "k_cdef_search": 12.0090,
     "k_cdef_apply": 5.7870,
-    "k_lr_stats5": 5.8569,
+    "k_lr_stats5": 5.9467,
     "k_lr_trial_tiles": 7.9187,
 }
 
