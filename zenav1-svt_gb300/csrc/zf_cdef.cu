@@ -169,22 +169,25 @@ __device__ void find_dirs(const uint16_t *reg, int rs, int cs, const int *blist,
 __device__ __noinline__ void load_region(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n,
                                          uint16_t *reg, int pitch) {
     const int rs = n + 4;
-    stage_window<1>(
-        bd, pw, rs, x0 - 2, rs, false, kVeryLarge,
-        [&](int ry) {
-            const int y = y0 - 2 + ry;
-            return (y >= 0 && y < ph) ? row_ptr(plane, y, pw, bd) : (const uint8_t *)nullptr;
-        },
-        [&](int ry, int rx, int v) { reg[ry * pitch + rx] = (uint16_t)v; });
+    auto rowf = [&](int ry) {
+        const int y = y0 - 2 + ry;
+        return (y >= 0 && y < ph) ? row_ptr(plane, y, pw, bd) : (const uint8_t *)nullptr;
+    };
+    auto putf = [&](int ry, int rx, int v) { reg[ry * pitch + rx] = (uint16_t)v; };
+    // the staging loop once with the bit depth a constant (8-bit rows: four
+    // samples a word and their extraction resolved at compile time, 8 % off
+    // the CDEF search on 8-bit frames), once for other depths
+    if (bd == 8) stage_window<1>(8, pw, rs, x0 - 2, rs, false, kVeryLarge, rowf, putf);
+    else stage_window<1>(bd, pw, rs, x0 - 2, rs, false, kVeryLarge, rowf, putf);
 }
 
 // Stage the n x n source tile at (x0, y0), 0 outside the canvas.
 __device__ __noinline__ void load_src(const uint8_t *plane, int bd, int pw, int ph, int x0, int y0, int n,
                                       uint16_t *src, int pitch) {
-    stage_window<1>(
-        bd, pw, n, x0, n, false, 0,
-        [&](int ry) { return y0 + ry < ph ? row_ptr(plane, y0 + ry, pw, bd) : (const uint8_t *)nullptr; },
-        [&](int ry, int rx, int v) { src[ry * pitch + rx] = (uint16_t)v; });
+    auto rowf = [&](int ry) { return y0 + ry < ph ? row_ptr(plane, y0 + ry, pw, bd) : (const uint8_t *)nullptr; };
+    auto putf = [&](int ry, int rx, int v) { src[ry * pitch + rx] = (uint16_t)v; };
+    if (bd == 8) stage_window<1>(8, pw, n, x0, n, false, 0, rowf, putf);  // as in load_region
+    else stage_window<1>(bd, pw, n, x0, n, false, 0, rowf, putf);
 }
 
 // Non-skip 8x8 blocks of one filter block (the dlist, cdef.rs:1203-1213):

@@ -235,8 +235,7 @@ __device__ __forceinline__ const uint32_t *word_at(const uint8_t *plane, int64_t
 }
 
 // Load the region of a tile into shared memory as u16.
-__device__ void db_load(const DbTile &t, const uint8_t *plane, uint16_t *reg) {
-    const int bd = t.f->bd;
+__device__ __forceinline__ void db_load_bd(const DbTile &t, const uint8_t *plane, uint16_t *reg, const int bd) {
     if (word_ok(plane)) {
         const int spw = bd == 8 ? 4 : 2, wpr = DB_R / spw;
         // flat over (row, word), four words per thread at a time: their
@@ -267,6 +266,14 @@ __device__ void db_load(const DbTile &t, const uint8_t *plane, uint16_t *reg) {
         if (x >= 0 && x < t.pw && y >= 0 && y < t.ph) v = ldpx(plane, (int64_t)y * t.pw + x, bd);
         reg[ry * DB_P + rx] = (uint16_t)v;
     }
+}
+
+// The loader compiled once with the bit depth a constant for 8-bit planes
+// (samples per word and their unpacking resolved at compile time), once for
+// other depths.
+__device__ void db_load(const DbTile &t, const uint8_t *plane, uint16_t *reg) {
+    if (t.f->bd == 8) db_load_bd(t, plane, reg, 8);
+    else db_load_bd(t, plane, reg, t.f->bd);
 }
 
 // The filtering edges of a tile, bucketed by filter length (4, 6, 8, 14):

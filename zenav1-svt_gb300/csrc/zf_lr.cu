@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
     const LrPlane &pl = f.lr[wi.plane];
     const UnitRect r = pl.rects[wi.a];
     LrUnit &u = pl.units[wi.a];
-    const int bd = f.bd, stride = plane_stride(f, wi.plane);
+    const int bd = BD ? BD : f.bd, stride = plane_stride(f, wi.plane);  // BD: every frame of the launch
     const int uw = r.h_end - r.h_start, uh = r.v_end - r.v_start;
     const bool packed = BD ? (WIN == 5 && BD == 8) : (WIN == 5 && bd == 8);
     uint8_t *Db = reinterpret_cast<uint8_t *>(D), *Xb = reinterpret_cast<uint8_t *>(X);
@@ -280,9 +280,9 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                                       *rb_ = Db + (y + dr - dy0) * dpitch + dlead + HALF;
                         if (x + 4 <= xm1) {
                             uint32_t w0 = ld_word(rb_ + x);
-                            // two steps per iteration: the next step's loads
+                            // four steps per iteration: the next steps' loads
                             // issue before this step's products need theirs
-#pragma unroll 2
+#pragma unroll 4
                             for (; x + 4 <= xm1; x += 4) {
                                 const uint32_t a4 = ld_word(ra_ + x), w1 = ld_word(rb_ + x + 4);
                                 pre[0] = (int)__dp4a(a4, w0, (uint32_t)pre[0]);
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                     constexpr int SH = decltype(shc)::value;
                     const uint8_t *ra = rd - SH;
                     uint32_t w0 = ld_word(ra), w1 = ld_word(ra + 4);
-#pragma unroll 2
+#pragma unroll 4
                     for (; j < uw4; j += 4) {
                         const uint32_t w2 = ld_word(ra + j + 8), xv = ld_word(rx + j);
                         const uint32_t e0 = bytes_at<SH>(w0, w1), e1 = bytes_at<SH + 1>(w0, w1);
@@ -473,12 +473,12 @@ __global__ void __launch_bounds__(256, WIN == 5 ? 5 : 1) k_lr_stats(FrameDesc *f
                 else e_in = __dp4a(e, e, e_in);
             };
             if (((dlead + HALF) & 3) == 0) {
-#pragma unroll 2
+#pragma unroll 4
                 for (; j < uw4; j += 4) ewalk(ld_word(rx + j), ld_word(rd + j));
             } else {
                 const uint8_t *ra = rd - 2;
                 uint32_t w0 = ld_word(ra);
-#pragma unroll 2
+#pragma unroll 4
                 for (; j < uw4; j += 4) {
                     const uint32_t w1 = ld_word(ra + j + 4);
                     ewalk(ld_word(rx + j), bytes_at<2>(w0, w1));
@@ -1371,18 +1371,24 @@ __global__ void __launch_bounds__(256) k_lr_trial_tiles(FrameDesc *frames, const
         }
     }
     const int na = th + 7, rows = na + 4 * ne;  // A rows, then per edge B[b-2], B[b-1], B[b], B[min(b+1, ph-1)]
-    stage_window(
-        bd, pl.pw, rows, x0 - 3, tw + 7, true, 0,
-        [&](int rr) {
-            if (rr < na) return row_ptr(dg, clampi(y0 - 3 + rr, 0, ph - 1), stride, bd);
-            const int e = (rr - na) >> 2, k = (rr - na) & 3;
-            const int b = e == 0 ? eb[0] : e == 1 ? eb[1] : eb[2];
-            return row_ptr(pre, k < 3 ? b - 2 + k : min(b + 1, ph - 1), stride, bd);
-        },
-        [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
-    stage_window(
-        bd, pl.pw, th, x0, tw, true, 0, [&](int rr) { return row_ptr(sr, y0 + rr, stride, bd); },
-        [&](int rr, int cc, int v) { srct[rr * TL + cc] = (uint16_t)v; });
+    // the staging compiled once with the bit depth a constant for 8-bit
+    // planes (samples per word resolved at compile time), once for others
+    auto stage_all = [&](const int bdc) {
+        stage_window(
+            bdc, pl.pw, rows, x0 - 3, tw + 7, true, 0,
+            [&](int rr) {
+                if (rr < na) return row_ptr(dg, clampi(y0 - 3 + rr, 0, ph - 1), stride, bdc);
+                const int e = (rr - na) >> 2, k = (rr - na) & 3;
+                const int b = e == 0 ? eb[0] : e == 1 ? eb[1] : eb[2];
+                return row_ptr(pre, k < 3 ? b - 2 + k : min(b + 1, ph - 1), stride, bdc);
+            },
+            [&](int rr, int cc, int v) { stage[rr * SW + cc] = (uint16_t)v; });
+        stage_window(
+            bdc, pl.pw, th, x0, tw, true, 0, [&](int rr) { return row_ptr(sr, y0 + rr, stride, bdc); },
+            [&](int rr, int cc, int v) { srct[rr * TL + cc] = (uint16_t)v; });
+    };
+    if (bd == 8) stage_all(8);
+    else stage_all(bd);
     __syncthreads();
     const bool t5 = hf[0] == 0 && vf[0] == 0;  // uniform over the CTA
     // The solver's taps are symmetric (f[6 - k] = f[k], f[7] = 0), so each
