@@ -286,12 +286,12 @@ KERNEL_DRAM_PER_ALGO_BYTE = {
 # times of the same step) against the issue peak, four warp instructions
 # per clock per SM at the SM clock sampled during the timed region.
 KERNEL_WARP_INST_PER_PX = {
-    "k_deblock_sse": 18.2232,
-    "k_deblock_apply": 5.3854,
-    "k_cdef_search": 12.0090,
-    "k_cdef_apply": 5.7870,
-    "k_lr_stats5": 5.9467,
-    "k_lr_trial_tiles": 7.9187,
+    "k_deblock_sse": 17.7277,
+    "k_deblock_apply": 4.9196,
+    "k_cdef_search": 11.2519,
+    "k_cdef_apply": 5.2361,
+    "k_lr_stats5": 5.3851,
+    "k_lr_trial_tiles": 7.2574,
 }
 
 
