@@ -58,3 +58,36 @@ def test_random_mixed_batch_matches_oracle(ctx, oracle, seed):
         d1, s1, r1 = ctx.filter_stage(frames[k])
         assert_same_planes(r1, outs[k][2], chroma=frames[k].chroma)
         assert s1 == outs[k][1]
+
+
+def test_random_frames_through_each_call_site(ctx, oracle):
+    """Six frames of the sweep through the per-call-site entry points, chained
+    as the reference pipeline calls them (deblock pick, deblock apply, CDEF
+    search, CDEF apply, Wiener search, Wiener apply), each step against the
+    oracle's same step on the same input."""
+    frames, desc = sweep_frames(4, 6)
+    for k, fr in enumerate(frames):
+        try:
+            ro, rg = fr.copy_rec(), fr.copy_rec()
+            lf = oracle.deblock_pick(fr, ro)
+            assert ctx.pick_filter_levels(fr, rg) == lf
+            oracle.deblock_apply(fr, ro, lf)
+            ctx.apply_deblock_frame(fr, rg, lf)
+            assert_same_planes(rg, ro, chroma=fr.chroma)
+            d_o = oracle.cdef_search(fr, ro)[0]
+            d_g = ctx.cdef_search_still(fr, rg)
+            assert_same_decisions(d_g.as_dict(), d_o.as_dict(), lr=False)
+            pre_o, pre_g = [p.copy() for p in ro], [p.copy() for p in rg]
+            so = oracle.cdef_apply(fr, ro, d_o)
+            sg = ctx.apply_cdef_frame(fr, rg, d_g)
+            assert_same_planes(rg, ro, chroma=fr.chroma)
+            assert sg["cdef_filtered_px"] == so["cdef_filtered_px"]
+            assert sg["cdef_changed_px"] == so["cdef_changed_px"]
+            l_o = oracle.lr_search(fr, ro)
+            l_g = ctx.search_restoration_still(fr, rg)
+            assert_same_decisions(l_g.as_dict(), l_o.as_dict())
+            oracle.lr_apply(fr, ro, pre_o, l_o)
+            ctx.apply_restoration_frame(fr, rg, pre_g, l_g)
+            assert_same_planes(rg, ro, chroma=fr.chroma)
+        except AssertionError as e:
+            raise AssertionError("frame %d (%s): %s" % (k, desc[k], e)) from e
