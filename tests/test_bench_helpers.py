@@ -75,3 +75,22 @@ def test_config_is_shared_by_both_arms():
     assert "3840x2160" in c["workload"] and "presets {4,6}" in c["workload"]
     assert "one context (one stream) per frame" in c["concurrency"]
     assert bench.ours_config(4, world=8)["parallelism"] == "replicas"
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """The reference arm's JSON line on small frames: the oracle on the host
+    cores with the GPU arm's config, its own cpu_baseline and an e2e with no
+    device copies."""
+    import json
+    from zenav1_svt_gb300 import synth
+    small = [synth.make_frame(synth.frame_seed(2, 900 + k), 96, 64, 8, qp, preset, "power")
+             for k, (preset, qp) in enumerate(bench.WORKLOAD)]
+    monkeypatch.setattr(bench, "make_workload", lambda *a, **k: small)
+    monkeypatch.setattr(bench, "env_rank", lambda: (0, 1, 0))
+    args = types.SimpleNamespace(steps=1, warmup=0)
+    assert bench.run_reference(args) == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "MPix/s" and line["value"] > 0
+    assert line["config"] == bench.ours_config(len(small))
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": "MPix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
